@@ -1,0 +1,136 @@
+"""The oracle against the compiled, unmodified reference (oracle/_ref, built
+from the reference sources by oracle/build_ref.py).  Skipped where the
+reference checkout is absent.
+
+* Probe cases: per-bead forces and exchange scalars on identical ring-polymer
+  configurations must be bit-identical (same operation order, same libm).
+* Trajectories: the reference's own main, one process per bead, from the same
+  initial state; Langevin noise from RANMAR streams seeded seed+bead as the
+  reference draws it.  The reference's state dumps carry 13 significant
+  digits, which bounds the comparison.
+* Fixture replays: the reference's regression cases, run for their first
+  1000 steps, reproduce the golden simulation.out rows.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from oracle import refrun as R
+from tests import golden_cases as G
+
+pytestmark = pytest.mark.skipif(not R.available("d3"), reason="compiled reference not built here")
+
+
+def _sections(N, P, bosonic, pbc, inter, ext, size_ang, T="1.0 kelvin", cutoff="-1.0 angstrom"):
+    sec = {"simulation": {"nbeads": P, "bosonic": str(bosonic).lower(), "pbc": str(pbc).lower(),
+                          "thermostat": "langevin", "seed": 7},
+           "system": {"temperature": T, "natoms": N, "size": f"{size_ang} angstrom", "mass": "4.0026 dalton"},
+           "interaction_potential": {"name": inter, "cutoff": cutoff}, "external_potential": {"name": ext},
+           "observables": {"energy": "off"}}
+    if inter == "harmonic":
+        sec["interaction_potential"]["omega"] = "1.0 millielectronvolt"
+    if inter == "dipole":
+        sec["interaction_potential"]["strength"] = "2.4799673e-4"
+    if ext == "harmonic":
+        sec["external_potential"]["omega"] = "3.0 millielectronvolt"
+    if ext == "double_well":
+        sec["external_potential"].update(strength="1.32684e-7 millielectronvolt", location="3 angstrom")
+    if ext == "cosine":
+        sec["external_potential"].update(amplitude="1.0 millielectronvolt", phase="0.3")
+    return sec
+
+
+PROBES = [
+    # N, P, D, bosonic, pbc, interaction, external, box (angstrom), T, cutoff
+    (8, 8, 3, True, False, "free", "harmonic", 10.0, "1.0 kelvin", "-1.0 angstrom"),
+    (16, 32, 3, True, False, "free", "harmonic", 10.0, "1.0 kelvin", "-1.0 angstrom"),
+    (32, 8, 3, True, True, "aziz", "free", 12.0, "1.5 kelvin", "6 angstrom"),
+    (20, 6, 3, False, True, "aziz", "double_well", 12.0, "1.0 kelvin", "-1.0 angstrom"),
+    (24, 5, 2, True, False, "dipole", "harmonic", 30.0, "2.0 kelvin", "-1.0 angstrom"),
+    (12, 4, 3, True, False, "harmonic", "cosine", 10.0, "1.0 kelvin", "-1.0 angstrom"),
+    (48, 16, 3, True, True, "aziz", "double_well", 14.0, "1.0 kelvin", "7 angstrom"),
+    (6, 2, 3, True, False, "free", "harmonic", 10.0, "1.0 kelvin", "-1.0 angstrom"),
+]
+
+
+@pytest.mark.parametrize("case", PROBES)
+def test_probe_bit_identical(case, tmp_path):
+    N, P, D, bos, pbc, inter, ext, box, T, cut = case
+    rng = np.random.default_rng(N * 1000 + P)
+    L = box * R.ANGSTROM
+    x = rng.uniform(-0.5 * L, 0.5 * L, (N, D))[None] + rng.normal(0, 0.3 * R.ANGSTROM, (P, N, D))
+    sec = _sections(N, P, bos, pbc, inter, ext, box, T, cut)
+    R.write_ini(tmp_path / "c.ini", sec)
+    s, _ = O.system_from_ini(tmp_path / "c.ini", ndim=D)
+    ref = R.probe(sec, x, variant="d3" if D == 3 else "d2")
+    got = O.update_forces(s, x)
+    assert np.array_equal(got["f"], ref["f"])
+    assert np.array_equal(got["spring"], ref["spring"])
+    assert np.array_equal(got["phys"], ref["phys"])
+    if s.bosonic:
+        ex = O.exchange(s, x)
+        sc = ref["scalars"][0]
+        assert [ex["VB"], ex["prim"], ex["p_distinct"], ex["p_longest"]] == list(sc[:4])
+        assert ref["scalars"][P - 1][0] == ex["VB"]
+
+
+TRAJ = [
+    # N, P, D, bosonic, propagator, thermostat, nmthermostat, fixcom, interaction, external, pbc
+    (8, 8, 3, True, "cartesian", "none", False, False, "free", "harmonic", False),
+    (8, 8, 3, True, "cartesian", "langevin", True, True, "free", "harmonic", False),
+    (8, 6, 3, False, "normal_modes", "langevin", True, True, "free", "harmonic", False),
+    (7, 5, 3, False, "normal_modes", "none", False, True, "free", "harmonic", False),
+    (10, 4, 3, True, "cartesian", "langevin", False, True, "aziz", "free", True),
+    (9, 4, 2, True, "cartesian", "langevin", False, True, "free", "harmonic", False),
+]
+
+
+@pytest.mark.parametrize("case", TRAJ)
+def test_trajectory_matches_reference(case, tmp_path):
+    N, P, D, bos, prop, thermo, nmth, fixcom, inter, ext, pbc = case
+    steps, seed = 15, 4242
+    rng = np.random.default_rng(steps * N + P)
+    box = 9.0
+    x_ang = rng.uniform(-0.5 * box, 0.5 * box, (N, D))[None] + rng.normal(0, 0.2, (P, N, D))
+    v = rng.normal(0, 2.0, (P, N, D))
+    sec = _sections(N, P, bos, pbc, inter, ext, box, "2.0 kelvin", "5 angstrom")
+    sec["simulation"].update(thermostat=thermo, nmthermostat=str(nmth).lower(), propagator=prop,
+                             fixcom=str(fixcom).lower(), seed=seed, steps=steps, sfreq=1, dt="1.0 femtosecond")
+    ref = R.run_trajectory(sec, x_ang, v, variant="d3" if D == 3 else "d2")
+    R.write_ini(tmp_path / "c.ini", sec)
+    s, _ = O.system_from_ini(tmp_path / "c.ini", ndim=D)
+    tr = O.Trajectory(s, x_ang * R.ANGSTROM, s.mass * (v * R.ANG_PER_PS))
+    streams = [O.RanMars(seed + b) for b in range(P)]
+    for st in range(steps + 1):
+        for got, want in ((tr.x, ref["x"][st]), (tr.p / s.mass, ref["v"][st]), (tr.f, ref["f"][st])):
+            scale = max(np.abs(want).max(), 1e-300)
+            assert np.abs(got - want).max() <= 2e-12 * scale
+        xi = O.ranmars_noise(streams, N, D) if thermo == "langevin" else np.zeros((2, P, N, D))
+        assert tr.step(xi) == 0
+
+
+@pytest.mark.parametrize("case", sorted(G.load()[1]))
+def test_fixture_replay_first_1000_steps(case, tmp_path):
+    """The compiled reference through the MPI shim reproduces the reference's
+    own golden simulation.out rows (9 significant digits)."""
+    import os
+    import subprocess
+    z, index = G.load()
+    ini = index[case]["ini"].replace("steps = 100000", "steps = 1000")
+    (tmp_path / "c.ini").write_text(ini)
+    variant = "d3_fact" if "factorial" in case else "d3"
+    P = int(float([ln.split("=")[1] for ln in ini.splitlines() if ln.strip().startswith("nbeads")][0]))
+    env = dict(os.environ, PIMDB_SHIM_NP=str(P), PIMDB_SHIM_TIMEOUT="120")
+    r = subprocess.run([str(R.REF / f"pimdb_{variant}"), "-in", "c.ini"], cwd=tmp_path, env=env,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "[X]" not in r.stdout, r.stdout + r.stderr
+    lines = (tmp_path / "output" / "simulation.out").read_text().split("\n")
+    cols = lines[0].split()
+    got = np.array([list(map(float, ln.split())) for ln in lines[1:] if ln.strip()])
+    want = z[f"{case}/simulation_out"]
+    gold_cols = index[case]["columns"]
+    n = min(len(got), len(want))
+    assert n >= 2
+    for j, c in enumerate(cols):
+        k = gold_cols.index(c)
+        assert np.allclose(got[:n, j], want[:n, k], rtol=1e-5), c
