@@ -1,0 +1,373 @@
+"""Throughput benchmark of the GB300 PIMD-B++ hot path: bead-steps/s
+(N * P * MD steps per second).
+
+Default workload (the second benchmark system of the project): N = 256
+He-4-mass bosons, P = 64 beads, NDIM = 3, T = 1.5 K, Aziz HFDHE2 pair
+potential with cutoff L/2 and minimum image in a periodic cube at number
+density 0.0218 A^-3 (L = 22.7297 A), no external potential, normal-mode
+propagator with the normal-mode Langevin thermostat, dt = 2 fs, FP64.
+
+One bench "step" is one MD step of the whole ring polymer.  Synthetic inputs:
+uniform random particle centres (random sequential addition keeping pairs
+>= 2.2 A apart, seed 12345) shared by all beads plus a 0.05 A per-bead
+jitter; Maxwell-Boltzmann momenta at the ring-polymer temperature.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload cfg2|cfg1|cfg3|cfg5] [--precision fp64|mixed]
+
+For N > 1 (torchrun) every rank runs its own replica (replicas only: the
+bead ring of one system is never split across GPUs); value = all ranks'
+bead-steps / max time.  --impl reference times the CPU oracle port on the
+host cores (the reference's own binaries cannot be built on the GPU host).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+ANG = 1.8897261
+KELVIN = 3.1668152e-06
+MEV = 0.036749326e-3
+DALTON = 1822.8885
+FS = 4.1341373e16 * 1e-15
+METRIC = "bead-steps/s (N·P·steps/s): plain FP64 vs mixed+batched at stated force error"
+
+WORKLOADS = {
+    "cfg2": dict(desc="N=256 He-4 bosons, P=64, 3D PBC, Aziz cutoff L/2 (min image), rho=0.0218/A^3 "
+                      "(L=22.7297 A), T=1.5 K, normal-mode propagator + normal-mode Langevin, dt=2 fs",
+                 ndim=3, natoms=256, nbeads=64, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=22.7297,
+                 inter="aziz", int_p=(0, 0, 0), cutoff_ang=11.36485, ext="free", ext_p=(0, 0, 0),
+                 propagator="normal_modes", nmthermostat=True, dt_fs=2.0, min_sep_ang=2.2, jitter_ang=0.05),
+    "cfg1": dict(desc="N=16 bosons, P=32, 3D, harmonic trap 3 meV, free pair, VV + Langevin, dt=1 fs",
+                 ndim=3, natoms=16, nbeads=32, T_K=1.0, mass_amu=1.0, pbc=False, box_ang=10.0, inter="free",
+                 int_p=(0, 0, 0), cutoff_ang=-1.0, ext="harmonic", ext_p=(3.0 * MEV, 0, 0), propagator="cartesian",
+                 nmthermostat=False, dt_fs=1.0, min_sep_ang=0.0, jitter_ang=0.0),
+    "cfg3": dict(desc="N=1024 bosons, P=32, 2D, dipole D=1 meV A^3 (no cutoff), harmonic trap 1 meV, "
+                      "VV + Langevin, dt=1 fs", ndim=2, natoms=1024, nbeads=32, T_K=2.0, mass_amu=1.0, pbc=False,
+                 box_ang=60.0, inter="dipole", int_p=(2.4799673e-4, 0, 0), cutoff_ang=-1.0, ext="harmonic",
+                 ext_p=(1.0 * MEV, 0, 0), propagator="cartesian", nmthermostat=False, dt_fs=1.0, min_sep_ang=1.0,
+                 jitter_ang=0.3),
+    "cfg5": dict(desc="N=4096 He-4 bosons, P=128, 3D PBC, Aziz cutoff 7 A + double well, rho=0.0218/A^3 "
+                      "(L=57.2754 A), T=1 K, normal-mode propagator, dt=2 fs", ndim=3, natoms=4096, nbeads=128,
+                 T_K=1.0, mass_amu=4.0026, pbc=True, box_ang=57.2754, inter="aziz", int_p=(0, 0, 0), cutoff_ang=7.0,
+                 ext="double_well", ext_p=(1.32684e-7 * MEV, 3.0 * ANG, 0), propagator="normal_modes",
+                 nmthermostat=False, dt_fs=2.0, min_sep_ang=2.2, jitter_ang=0.05),
+}
+
+
+def workload_config(w, precision):
+    pk = importlib.import_module("pimd-b_gb300")
+    return pk.make_config(
+        ndim=w["ndim"], natoms=w["natoms"], nbeads=w["nbeads"], bosonic=1, pbc=int(w["pbc"]), fixcom=1,
+        propagator=w["propagator"], thermostat="langevin", nmthermostat=int(w["nmthermostat"]), precision=precision,
+        temperature=w["T_K"] * KELVIN, mass=w["mass_amu"] * DALTON, size=w["box_ang"] * ANG, dt=w["dt_fs"] * FS,
+        gamma=-1.0, ext_kind=w["ext"], ext_params=w["ext_p"], int_kind=w["inter"], int_params=w["int_p"],
+        cutoff=w["cutoff_ang"] * ANG, seed=12345, replica=0)
+
+
+def initial_state(w, seed=12345):
+    rng = np.random.default_rng(seed)
+    N, P, D = w["natoms"], w["nbeads"], w["ndim"]
+    L = w["box_ang"] * ANG
+    dmin = w["min_sep_ang"] * ANG
+    pts = []
+    while len(pts) < N:
+        c = rng.uniform(-0.5 * L, 0.5 * L, D)
+        if dmin > 0 and pts:
+            d = np.asarray(pts) - c
+            if w["pbc"]:
+                d -= L * np.floor(d / L + 0.5)
+            if np.min(np.einsum("ij,ij->i", d, d)) < dmin * dmin:
+                continue
+        pts.append(c)
+    x = np.asarray(pts)[None] + rng.normal(0.0, w["jitter_ang"] * ANG, (P, N, D))
+    m = w["mass_amu"] * DALTON
+    thermo_beta = 1.0 / (w["T_K"] * KELVIN) / P
+    p = rng.normal(0.0, math.sqrt(m / thermo_beta), (P, N, D))
+    return x, p
+
+
+def pair_flops(w, x):
+    """Algorithmic FLOPs of one evaluation of the pair kernel: every unique
+    pair costs the separation test (15 FLOPs with the minimum image); pairs
+    inside the cutoff add the gradient.  Aziz: 63 arithmetic + sqrt + 3
+    divisions (10 each) + 2 exp (20 each) = 133; dipole: 8 + sqrt + div = 28;
+    harmonic: 6."""
+    per_in = {"aziz": 133, "dipole": 28, "harmonic": 6, "free": 0}[w["inter"]]
+    if w["inter"] == "free":
+        return 0.0, 0
+    N, P = w["natoms"], w["nbeads"]
+    L = w["box_ang"] * ANG
+    cut = w["cutoff_ang"] * ANG
+    inside = 0
+    for b in range(P):
+        d = x[b][:, None, :] - x[b][None, :, :]
+        if w["pbc"]:
+            d -= L * np.floor(d / L + 0.5)
+        r = np.sqrt(np.einsum("ijk,ijk->ij", d, d))
+        iu = np.triu_indices(N, 1)
+        inside += int(np.sum(r[iu] < cut)) if cut > 0 else len(iu[0])
+    pairs = P * N * (N - 1) // 2
+    return float(pairs * 15 + inside * per_in), inside
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = [ln.split(", ") for ln in self.path.read_text().splitlines() if ln.strip()]
+        self.path.unlink(missing_ok=True)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if len(r) > 5 + k and r[5 + k].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(w, seconds=12.0, nthreads=None):
+    """The oracle port (FP64, reference operation order) on the host cores,
+    over a bounded sample of MD steps of the same workload."""
+    from oracle import oracle as O
+    nthreads = nthreads or os.cpu_count() or 1
+    s = O.make_system(ndim=w["ndim"], natoms=w["natoms"], nbeads=w["nbeads"], temperature=w["T_K"] * KELVIN,
+                      mass=w["mass_amu"] * DALTON, bosonic=True, pbc=w["pbc"], size=w["box_ang"] * ANG, fixcom=True,
+                      propagator=w["propagator"], thermostat="langevin", nmthermostat=w["nmthermostat"],
+                      dt=w["dt_fs"] * FS, ext=w["ext"], ext_p=w["ext_p"], interaction=w["inter"], int_p=w["int_p"],
+                      cutoff=w["cutoff_ang"] * ANG)
+    x, p = initial_state(w)
+    tr = O.Trajectory(s, x, p)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        xi = O.philox_noise_device(12345, 0, steps, s.nbeads, s.natoms, s.ndim)
+        tr.step(xi, nthreads=nthreads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and steps >= 2) or steps >= 100000:
+            break
+    value = w["natoms"] * w["nbeads"] * steps / el
+    return {"value": value, "unit": "bead-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{steps} MD steps of the same workload ({el:.1f} s), FP64 oracle port with the "
+                      f"per-bead force loops on {nthreads} POSIX threads"}
+
+
+def run_reference(args, w, rank, world):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    W = max(args.warmup, 0)
+    K = max(args.steps, 1)
+    nthreads = os.cpu_count() or 1
+    s = O.make_system(ndim=w["ndim"], natoms=w["natoms"], nbeads=w["nbeads"], temperature=w["T_K"] * KELVIN,
+                      mass=w["mass_amu"] * DALTON, bosonic=True, pbc=w["pbc"], size=w["box_ang"] * ANG, fixcom=True,
+                      propagator=w["propagator"], thermostat="langevin", nmthermostat=w["nmthermostat"],
+                      dt=w["dt_fs"] * FS, ext=w["ext"], ext_p=w["ext_p"], interaction=w["inter"], int_p=w["int_p"],
+                      cutoff=w["cutoff_ang"] * ANG)
+    x, p = initial_state(w)
+    tr = O.Trajectory(s, x, p)
+    for st in range(W):
+        tr.step(O.philox_noise_device(12345, 0, st, s.nbeads, s.natoms, s.ndim), nthreads=nthreads)
+    noise = [O.philox_noise_device(12345, 0, W + k, s.nbeads, s.natoms, s.ndim) for k in range(K)]
+    t0 = time.perf_counter()
+    for k in range(K):
+        tr.step(noise[k], nthreads=nthreads)
+    el = time.perf_counter() - t0
+    value = w["natoms"] * w["nbeads"] * K / el
+    line = {"metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * el / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": w["desc"], "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": "bead-steps/s", "cores": nthreads, "kind": "port",
+                             "sample": f"{K} MD steps after {W} warm-up steps, FP64 oracle port of the reference "
+                                       f"(the reference's own build needs its sources, absent on the GPU host)"},
+            "e2e": {"value": value, "unit": "bead-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="short run for an ncu capture")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, w, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pk = importlib.import_module("pimd-b_gb300")
+    stream = torch.cuda.current_stream()
+    cfg = workload_config(w, args.precision)
+    cfg.replica = rank
+    x0, p0 = initial_state(w, seed=12345 + rank)
+    N, P, D = w["natoms"], w["nbeads"], w["ndim"]
+    units = N * P
+    sysm = pk.System(cfg, stream=stream.cuda_stream)
+    sysm.set_state(x0, p0)
+    W = max(args.warmup, 3)
+    K = max(args.steps, 1)
+    sysm.step_async(W)
+    sysm.synchronize()
+    if args.profile_only:
+        sysm.step_async(K)
+        sysm.synchronize()
+        return
+
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    sampler = ClockSampler(local) if rank == 0 else None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(K):
+        flush.zero_()
+        ev[k][0].record(stream)
+        sysm.step_async(1)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    sysm.synchronize()
+    clocks = sampler.stop() if sampler else None
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_s = sum(step_ms) / 1e3
+    if dist:
+        t = torch.tensor([tot_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_s = float(t.item())
+    value = world * units * K / tot_s
+
+    # kernel launches in the timed region: the same K steps, counted
+    prof = sysm.profile(0)
+    sysm.step_async(K)
+    sysm.synchronize()
+    launches = sysm.profile(-1)["launches"]
+    # per-kernel device times (events around each launch on the library stream)
+    sysm.profile(1)
+    sysm.step_async(K)
+    sysm.synchronize()
+    prof = sysm.profile(-1)
+    sysm.profile(0)
+
+    # end to end through the C ABI with pinned host buffers
+    shape = (P, N, D)
+    hx = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    hp = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    hf = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    sysm.get_state_ptr(hx.data_ptr(), hp.data_ptr(), None, device=False)
+    Ke = max(1, K // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        sysm.set_state_ptr(hx.data_ptr(), hp.data_ptr(), device=False)
+        sysm.step(1)
+        sysm.get_state_ptr(hx.data_ptr(), hp.data_ptr(), hf.data_ptr(), device=False)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * units * Ke / e2e_s, "unit": "bead-steps/s", "h2d_bytes_per_step": 2 * P * N * D * 8,
+           "d2h_bytes_per_step": 3 * P * N * D * 8, "steps": Ke}
+    sysm.close()
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel class
+    ms, cnt = prof["ms"], prof["counts"]
+    dom = max(ms, key=lambda k: ms[k])
+    dom_ms = ms[dom] / max(cnt[dom], 1)
+    fp64_peak = pk.measure_fp64_peak()
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    roof = {"kernel": dom, "kernel_share": ms[dom] / max(sum(ms.values()), 1e-30), "launch_ms": dom_ms,
+            "per_class_ms_per_step": {k: v / K for k, v in ms.items() if v > 0}}
+    if dom == "bead_forces" and w["inter"] != "free":
+        fl, inside = pair_flops(w, x0)
+        ach = fl / (dom_ms * 1e-3) / 1e12
+        peak = fp64_peak if args.precision == "fp64" else None
+        roof.update({"bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": ach,
+                     "peak": peak, "unit": "TFLOP/s", "frac": (ach / peak) if peak else None,
+                     "traffic": None, "peak_source": "measured in-run (FP64 FMA probe)",
+                     "algorithmic": f"{fl:.4g} FLOP per launch ({inside} unique pairs inside the cutoff)"})
+    else:
+        bytes_per = 6 * 8 * units * D
+        ach = bytes_per / (dom_ms * 1e-3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roof.update({"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs"})
+    line = {"metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * tot_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["desc"], "natoms": N, "nbeads": P, "ndim": D, "precision": args.precision,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single system",
+                       "l2": "flushed before every timed step (512 MiB write, outside the step's events)"},
+            "e2e": e2e, "roofline": roof, "gpu_launches": launches, "clocks": clocks,
+            "fp64_peak_tflops": fp64_peak}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, seconds=args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * pimdb_gb300 — C ABI of the GB300-native PIMD-B++ per-step hot path.
+ *
+ * One handle holds every bead of one ring-polymer system on one GPU (the
+ * reference spreads the beads over MPI ranks, one bead per rank).  All
+ * arrays crossing this boundary are plain FP64 in the reference's per-bead
+ * dVec order, stacked over beads: [bead][particle][axis]
+ * (include/common.h:79-248 of the reference), in Hartree atomic units.
+ * Every entry point returns a pimdb_status.  No pointer passed in is kept
+ * after the call returns.
+ *
+ * Which reference interface each entry point stands in for is noted beside
+ * it (paths are within the PIMD-B++ source tree).
+ */
+#ifndef PIMDB_GB300_H
+#define PIMDB_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIMDB_ABI_VERSION 1
+
+/* Status codes.  The reference throws std::invalid_argument for configuration
+ * errors (src/params.cpp:11-260) and std::overflow_error for a non-finite
+ * exchange potential (src/bosonic_exchange/quadratic_bosonic_exchange.cpp:92-97,119-124). */
+typedef enum pimdb_status {
+    PIMDB_OK = 0,
+    PIMDB_ERR_CONFIG = 1,        /* invalid configuration (std::invalid_argument) */
+    PIMDB_ERR_NONFINITE_VB = 2,  /* V or V_backwards not finite (std::overflow_error) */
+    PIMDB_ERR_CUDA = 3,          /* CUDA runtime error; see pimdb_last_error */
+    PIMDB_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+    PIMDB_ERR_BOUNDS = 5,        /* a device-side index check failed */
+    PIMDB_ERR_ARG = 6,           /* NULL handle or invalid argument */
+    PIMDB_ERR_NO_DEVICE = 7,     /* no CUDA device visible */
+    PIMDB_ERR_PARSE = 8          /* config.ini could not be read */
+} pimdb_status;
+
+/* Potentials (src/simulation.cpp:612-645; names as in config.ini). */
+enum pimdb_potential {
+    PIMDB_POT_FREE = 0,
+    PIMDB_POT_HARMONIC = 1,    /* params: omega */
+    PIMDB_POT_DOUBLE_WELL = 2, /* params: strength, location (external only) */
+    PIMDB_POT_COSINE = 3,      /* params: amplitude, phase (external only) */
+    PIMDB_POT_AZIZ = 4,        /* HFDHE2 (interaction only) */
+    PIMDB_POT_DIPOLE = 5       /* params: strength in Hartree bohr^3 (interaction only) */
+};
+enum pimdb_propagator { PIMDB_PROP_CARTESIAN = 0, PIMDB_PROP_NORMAL_MODES = 1 };
+enum pimdb_thermostat { PIMDB_THERMO_NONE = 0, PIMDB_THERMO_LANGEVIN = 1 };
+/* Arithmetic of the pair forces: FP64 throughout, or FP32 pair arithmetic
+ * with FP64 per-atom accumulation.  Exchange and integrator are FP64 in both. */
+enum pimdb_precision { PIMDB_FP64 = 0, PIMDB_MIXED = 1 };
+
+/* The hot-path subset of the reference's Params (src/params.cpp:8-260),
+ * already converted to atomic units. */
+typedef struct pimdb_config {
+    int ndim;            /* 1, 2 or 3 (the reference's compile-time NDIM) */
+    int natoms;          /* [system] natoms */
+    int nbeads;          /* [simulation] nbeads */
+    int bosonic;         /* [simulation] bosonic (ignored when nbeads == 1) */
+    int pbc;             /* [simulation] pbc */
+    int fixcom;          /* [simulation] fixcom */
+    int propagator;      /* enum pimdb_propagator */
+    int thermostat;      /* enum pimdb_thermostat */
+    int nmthermostat;    /* [simulation] nmthermostat */
+    int precision;       /* enum pimdb_precision */
+    double temperature;  /* kB T in Hartree */
+    double mass;         /* electron masses */
+    double size;         /* box edge L, bohr */
+    double dt;           /* atomic time units */
+    double gamma;        /* Langevin friction; < 0 selects 1/(100 dt) */
+    int ext_kind;        /* enum pimdb_potential */
+    double ext_params[3];
+    int int_kind;        /* enum pimdb_potential */
+    double int_params[3];
+    double cutoff;       /* interaction cutoff before min(cutoff, L/2) under PBC; < 0 = all pairs */
+    unsigned long long seed;  /* Langevin noise key */
+    unsigned int replica;     /* folded into the noise counter */
+} pimdb_config;
+
+typedef struct pimdb_handle pimdb_handle;
+
+/* Reference defaults (src/params.cpp:15-259) for a 3-dimensional system. */
+int pimdb_config_default(pimdb_config* cfg);
+
+/* Reads a reference config.ini (schema, defaults, units and validation of
+ * src/params.cpp:8-260 and src/units.cpp).  `ndim` stands for the reference's
+ * compile-time NDIM.  On failure returns PIMDB_ERR_PARSE or PIMDB_ERR_CONFIG
+ * and writes the reference's message into err (if err_len > 0). */
+int pimdb_config_from_ini(const char* path, int ndim, pimdb_config* cfg, char* err, int err_len);
+
+/* Simulation::Simulation (src/simulation.cpp:16-101) minus initial
+ * conditions: allocates the device state of all beads.  `cuda_stream` is a
+ * cudaStream_t to run on, or NULL for a stream owned by the handle. */
+int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_handle** out);
+int pimdb_destroy(pimdb_handle* h);
+
+/* Sets coordinates and momenta of every bead (host arrays
+ * [bead][particle][axis]); either may be NULL to keep the current values.
+ * Forces are reset to zero, as after the reference's constructor
+ * (src/simulation.cpp:16-101 never evaluates them). */
+int pimdb_set_state(pimdb_handle* h, const double* x, const double* p);
+/* Same with device pointers in the same layout. */
+int pimdb_set_state_device(pimdb_handle* h, const double* x, const double* p);
+/* Copies coordinates, momenta and forces (Simulation::forces) to host arrays;
+ * any may be NULL. */
+int pimdb_get_state(pimdb_handle* h, double* x, double* p, double* f);
+int pimdb_get_state_device(pimdb_handle* h, double* x, double* p, double* f);
+
+/* MD step index used as the Langevin noise counter. */
+int pimdb_set_step(pimdb_handle* h, long long step);
+int pimdb_get_step(pimdb_handle* h, long long* step);
+
+/* Simulation::updateForces on every bead (src/simulation.cpp:353-374):
+ * exchange springs on beads 1 and P, interior springs, external and pair
+ * forces. */
+int pimdb_compute_forces(pimdb_handle* h);
+
+/* `nsteps` iterations of the body of Simulation::run
+ * (src/simulation.cpp:246-259): thermostat O-step, COM removal, propagator
+ * (VelocityVerletPropagator::step, src/propagators/velocity_verlet.cpp:7-22,
+ * or NormalModesPropagator::step, src/propagators/normal_modes_propagator.cpp:19-71),
+ * thermostat O-step, COM removal.  Synchronous: returns after the GPU is done
+ * and reports a non-finite exchange potential. */
+int pimdb_step(pimdb_handle* h, int nsteps);
+/* Same, only enqueued on the handle's stream; errors surface at the next
+ * pimdb_synchronize or synchronous call. */
+int pimdb_step_async(pimdb_handle* h, int nsteps);
+int pimdb_synchronize(pimdb_handle* h);
+
+/* BosonicExchange on the current coordinates
+ * (src/bosonic_exchange/quadratic_bosonic_exchange.cpp:30-279):
+ *   scalars[0] = effectivePotential()      V_B = V[N]
+ *   scalars[1] = primEstimator()           -d(beta_ex V_B)/d(beta_ex) / P at fixed E
+ *   scalars[2] = getDistinctProbability()
+ *   scalars[3] = getLongestProbability()
+ *   f_first    = exterior spring force on bead 1 (springForceFirstBead), [particle][axis]
+ *   f_last     = exterior spring force on bead P (springForceLastBead)
+ * Any output may be NULL.  Requires a bosonic configuration. */
+int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first, double* f_last);
+/* Intermediate arrays of the last pimdb_exchange / force evaluation:
+ * E (N(N+1)/2, the reference's E_kn order, getEnk(m,k) = E[m(m+1)/2 - k]),
+ * V (N+1), V_backwards (N+1).  Any may be NULL. */
+int pimdb_exchange_arrays(pimdb_handle* h, double* E_kn, double* V, double* V_backwards);
+
+/* Instrumentation (no counterpart in the reference, which only reports the
+ * wall time per step, src/simulation.cpp:517-572).  Kernel classes: */
+enum pimdb_kernel_class {
+    PIMDB_K_BEAD_FORCES = 0,      /* external + pair forces + interior springs */
+    PIMDB_K_EXCH_ENERGIES = 1,    /* cycle energies E */
+    PIMDB_K_EXCH_RECURSIONS = 2,  /* V and V_backwards recursions */
+    PIMDB_K_EXCH_FORCES = 3,      /* connection probabilities -> forces on beads 1 and P */
+    PIMDB_K_EXCH_ESTIMATORS = 4,  /* primEstimator and topology probabilities */
+    PIMDB_K_CART_UPDATE = 5,      /* B / A / Langevin / COM on Cartesian momenta */
+    PIMDB_K_NM_PROPAGATE = 6,     /* normal-mode free ring-polymer propagation */
+    PIMDB_K_NM_THERMO = 7,        /* normal-mode Langevin O-step */
+    PIMDB_NUM_KERNEL_CLASSES = 8
+};
+/* Reads the accumulated per-class device milliseconds and launch counts and
+ * the total number of kernels launched since the last reset (any output may
+ * be NULL).  enable = 1 / 0 resets the counters and turns the per-launch
+ * event timing on / off (timing synchronises after every launch); enable = -1
+ * only reads. */
+int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, long long* launches);
+
+/* Measures the FP64 fused-multiply-add throughput of the current device in
+ * TFLOP/s (the roofline denominator of the FP64 kernels). */
+int pimdb_measure_fp64_peak(double* tflops);
+
+/* Human-readable text of the last error on this handle (or a global one if
+ * h is NULL). */
+int pimdb_last_error(const pimdb_handle* h, char* buf, int len);
+const char* pimdb_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

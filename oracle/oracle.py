@@ -303,3 +303,17 @@ def system_from_ini(path, **overrides):
     extras = dict(steps=int(float(get("simulation", "steps", "1e5"))), sfreq=int(get("simulation", "sfreq", "1000")),
                   seed=int(float(get("simulation", "seed", "1234"))), temperature=T)
     return make_system(**kw), extras
+
+
+def philox_noise_device(seed: int, replica: int, step: int, nbeads: int, natoms: int, ndim: int) -> np.ndarray:
+    """The project's Langevin noise for both O-steps of MD step `step`, as the
+    GPU kernels draw it: the normal number of (bead-or-mode b, axis a,
+    particle i) is element i%2 of the Box-Muller pair number
+    (b*ndim + a)*ceil(natoms/2) + i//2.  Returned as [substep][b][i][a]."""
+    half = (natoms + 1) // 2
+    n = nbeads * ndim * half * 2
+    out = np.empty((2, nbeads, natoms, ndim))
+    for o in range(2):
+        z = philox_normals(seed, replica, step, o, n).reshape(nbeads, ndim, 2 * half)[:, :, :natoms]
+        out[o] = z.transpose(0, 2, 1)
+    return out

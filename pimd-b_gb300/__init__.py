@@ -1,0 +1,269 @@
+"""Python access to ``libpimdb_gb300.so`` — the GB300-native PIMD-B++ hot
+path behind its C ABI (``include/pimdb_gb300.h``).
+
+The package directory name contains a hyphen, so import it with
+``importlib.import_module("pimd-b_gb300")``.  There is no CPU fallback: every
+entry point runs the CUDA kernels, and loading fails loudly when the shared
+library has not been built (``build.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libpimdb_gb300.so"
+
+# status codes (pimdb_status)
+OK, ERR_CONFIG, ERR_NONFINITE_VB, ERR_CUDA, ERR_TIMEOUT, ERR_BOUNDS, ERR_ARG, ERR_NO_DEVICE, ERR_PARSE = range(9)
+POT = {"free": 0, "harmonic": 1, "double_well": 2, "cosine": 3, "aziz": 4, "dipole": 5}
+PROP = {"cartesian": 0, "normal_modes": 1}
+THERMO = {"none": 0, "langevin": 1}
+PRECISION = {"fp64": 0, "mixed": 1}
+
+EXPORTS = [
+    "pimdb_config_default", "pimdb_config_from_ini", "pimdb_create", "pimdb_destroy", "pimdb_set_state",
+    "pimdb_set_state_device", "pimdb_get_state", "pimdb_get_state_device", "pimdb_set_step", "pimdb_get_step",
+    "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
+    "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
+    "pimdb_measure_fp64_peak",
+]
+KERNEL_CLASSES = ["bead_forces", "exch_energies", "exch_recursions", "exch_forces", "exch_estimators",
+                  "cart_update", "nm_propagate", "nm_thermo"]
+
+
+class Config(C.Structure):
+    """Mirror of ``pimdb_config``."""
+    _fields_ = [
+        ("ndim", C.c_int), ("natoms", C.c_int), ("nbeads", C.c_int), ("bosonic", C.c_int), ("pbc", C.c_int),
+        ("fixcom", C.c_int), ("propagator", C.c_int), ("thermostat", C.c_int), ("nmthermostat", C.c_int),
+        ("precision", C.c_int), ("temperature", C.c_double), ("mass", C.c_double), ("size", C.c_double),
+        ("dt", C.c_double), ("gamma", C.c_double), ("ext_kind", C.c_int), ("ext_params", C.c_double * 3),
+        ("int_kind", C.c_int), ("int_params", C.c_double * 3), ("cutoff", C.c_double),
+        ("seed", C.c_ulonglong), ("replica", C.c_uint),
+    ]
+
+
+class PimdbError(RuntimeError):
+    pass
+
+
+class ConfigError(PimdbError, ValueError):
+    """The reference's std::invalid_argument."""
+
+
+class ExchangeOverflowError(PimdbError, OverflowError):
+    """The reference's std::overflow_error (non-finite V_B)."""
+
+
+_lib = None
+
+
+def lib():
+    """Loads the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: run build.build() (nvcc, sm_103a) first")
+        L = C.CDLL(str(LIB_PATH))
+        vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+        cfgp = C.POINTER(Config)
+        sig = {
+            "pimdb_config_default": ([cfgp], C.c_int),
+            "pimdb_config_from_ini": ([C.c_char_p, C.c_int, cfgp, C.c_char_p, C.c_int], C.c_int),
+            "pimdb_create": ([cfgp, vp, C.POINTER(vp)], C.c_int),
+            "pimdb_destroy": ([vp], C.c_int),
+            "pimdb_set_state": ([vp, vp, vp], C.c_int),
+            "pimdb_set_state_device": ([vp, vp, vp], C.c_int),
+            "pimdb_get_state": ([vp, vp, vp, vp], C.c_int),
+            "pimdb_get_state_device": ([vp, vp, vp, vp], C.c_int),
+            "pimdb_set_step": ([vp, C.c_longlong], C.c_int),
+            "pimdb_get_step": ([vp, C.POINTER(C.c_longlong)], C.c_int),
+            "pimdb_compute_forces": ([vp], C.c_int),
+            "pimdb_step": ([vp, C.c_int], C.c_int),
+            "pimdb_step_async": ([vp, C.c_int], C.c_int),
+            "pimdb_synchronize": ([vp], C.c_int),
+            "pimdb_exchange": ([vp, vp, vp, vp], C.c_int),
+            "pimdb_exchange_arrays": ([vp, vp, vp, vp], C.c_int),
+            "pimdb_last_error": ([vp, C.c_char_p, C.c_int], C.c_int),
+            "pimdb_status_string": ([C.c_int], C.c_char_p),
+            "pimdb_profile": ([vp, C.c_int, vp, vp, vp], C.c_int),
+            "pimdb_measure_fp64_peak": ([vp], C.c_int),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _last_error(h=None) -> str:
+    buf = C.create_string_buffer(1024)
+    lib().pimdb_last_error(h, buf, len(buf))
+    return buf.value.decode()
+
+
+def _check(st: int, h=None):
+    if st == OK:
+        return
+    msg = f"{lib().pimdb_status_string(st).decode()}: {_last_error(h)}"
+    if st in (ERR_CONFIG, ERR_PARSE):
+        raise ConfigError(msg)
+    if st == ERR_NONFINITE_VB:
+        raise ExchangeOverflowError(msg)
+    raise PimdbError(msg)
+
+
+def measure_fp64_peak() -> float:
+    """Measured FP64 FMA throughput of the current device, TFLOP/s."""
+    v = C.c_double()
+    _check(lib().pimdb_measure_fp64_peak(C.byref(v)))
+    return v.value
+
+
+def default_config() -> Config:
+    c = Config()
+    _check(lib().pimdb_config_default(C.byref(c)))
+    return c
+
+
+def config_from_ini(path, ndim: int = 3) -> Config:
+    """Reads a reference config.ini through the library's C++ reader."""
+    c = Config()
+    err = C.create_string_buffer(512)
+    st = lib().pimdb_config_from_ini(str(path).encode(), ndim, C.byref(c), err, len(err))
+    if st != OK:
+        raise ConfigError(err.value.decode())
+    return c
+
+
+def make_config(**kw) -> Config:
+    """Builds a config from keyword arguments (atomic units); potential,
+    propagator, thermostat and precision may be given by name."""
+    c = default_config()
+    for k, v in kw.items():
+        if k in ("ext_kind", "int_kind") and isinstance(v, str):
+            v = POT[v]
+        elif k == "propagator" and isinstance(v, str):
+            v = PROP[v]
+        elif k == "thermostat" and isinstance(v, str):
+            v = THERMO[v]
+        elif k == "precision" and isinstance(v, str):
+            v = PRECISION[v]
+        if k in ("ext_params", "int_params"):
+            arr = getattr(c, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(c, k, v)
+    return c
+
+
+class System:
+    """One ring-polymer system on the GPU (all beads), driven through the C ABI.
+
+    Arrays use the reference's per-bead order, stacked: [bead][particle][axis].
+    """
+
+    def __init__(self, cfg: Config, stream: int | None = None):
+        self.cfg = cfg
+        self.shape = (cfg.nbeads, cfg.natoms, cfg.ndim)
+        h = C.c_void_p()
+        _check(lib().pimdb_create(C.byref(cfg), C.c_void_p(stream) if stream else None, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pimdb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _arr(self, a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.size != np.prod(self.shape):
+            raise ValueError(f"expected {self.shape} elements, got {a.shape}")
+        return a
+
+    def set_state(self, x=None, p=None):
+        x, p = self._arr(x), self._arr(p)
+        _check(lib().pimdb_set_state(self._h, _ptr(x), _ptr(p)), self._h)
+
+    def get_state(self):
+        x, p, f = (np.empty(self.shape) for _ in range(3))
+        _check(lib().pimdb_get_state(self._h, _ptr(x), _ptr(p), _ptr(f)), self._h)
+        return x, p, f
+
+    def set_state_ptr(self, x_ptr, p_ptr, device: bool):
+        fn = lib().pimdb_set_state_device if device else lib().pimdb_set_state
+        _check(fn(self._h, C.c_void_p(x_ptr) if x_ptr else None, C.c_void_p(p_ptr) if p_ptr else None), self._h)
+
+    def get_state_ptr(self, x_ptr, p_ptr, f_ptr, device: bool):
+        fn = lib().pimdb_get_state_device if device else lib().pimdb_get_state
+        args = [C.c_void_p(v) if v else None for v in (x_ptr, p_ptr, f_ptr)]
+        _check(fn(self._h, *args), self._h)
+
+    def set_step(self, step: int):
+        _check(lib().pimdb_set_step(self._h, step), self._h)
+
+    def get_step(self) -> int:
+        v = C.c_longlong()
+        _check(lib().pimdb_get_step(self._h, C.byref(v)), self._h)
+        return v.value
+
+    def compute_forces(self):
+        _check(lib().pimdb_compute_forces(self._h), self._h)
+
+    def step(self, nsteps: int = 1):
+        _check(lib().pimdb_step(self._h, nsteps), self._h)
+
+    def step_async(self, nsteps: int = 1):
+        _check(lib().pimdb_step_async(self._h, nsteps), self._h)
+
+    def synchronize(self):
+        _check(lib().pimdb_synchronize(self._h), self._h)
+
+    def exchange(self):
+        N, D = self.cfg.natoms, self.cfg.ndim
+        sc = np.zeros(4)
+        f1 = np.zeros((N, D))
+        fP = np.zeros((N, D))
+        _check(lib().pimdb_exchange(self._h, _ptr(sc), _ptr(f1), _ptr(fP)), self._h)
+        return dict(VB=sc[0], prim=sc[1], p_distinct=sc[2], p_longest=sc[3], f1=f1, fP=fP)
+
+    def profile(self, enable: int = -1):
+        """Per-kernel-class device ms and launch counts, and total launches."""
+        ms = np.zeros(len(KERNEL_CLASSES))
+        n = np.zeros(len(KERNEL_CLASSES), dtype=np.int64)
+        tot = C.c_longlong()
+        _check(lib().pimdb_profile(self._h, enable, _ptr(ms), _ptr(n), C.byref(tot)), self._h)
+        return dict(ms=dict(zip(KERNEL_CLASSES, ms.tolist())), counts=dict(zip(KERNEL_CLASSES, n.tolist())),
+                    launches=tot.value)
+
+    def exchange_arrays(self):
+        N = self.cfg.natoms
+        E = np.zeros(N * (N + 1) // 2)
+        V = np.zeros(N + 1)
+        Vb = np.zeros(N + 1)
+        _check(lib().pimdb_exchange_arrays(self._h, _ptr(E), _ptr(V), _ptr(Vb)), self._h)
+        return dict(E=E, V=V, Vb=Vb)

@@ -1,0 +1,614 @@
+// C ABI (include/pimdb_gb300.h): handle lifetime, state transfer and the
+// per-step schedule of kernels on one CUDA stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/pimdb_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace pimdb;
+
+struct pimdb_handle {
+    pimdb_config cfg;
+    int D = 3;
+    Sys s{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    double* d_C = nullptr;    // cart -> NM rows [P][P]
+    double* d_T = nullptr;    // NM -> cart rows [P][P]
+    double* d_rot = nullptr;  // [P][3]
+    double* d_red[2] = {nullptr, nullptr};
+    double* d_stage = nullptr;
+    int* d_err = nullptr;
+    long long step = 0;
+    int red_last = 0;         // buffer holding the pending COM partials
+    int nred_last = 0;
+    bool com_pending = false;
+    std::string last_error;
+    // instrumentation: kernel launch count and, when enabled, per-class
+    // device time measured with events bracketing each launch
+    long long launches = 0;
+    bool profile = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double prof_ms[PIMDB_NUM_KERNEL_CLASSES] = {};
+    long long prof_n[PIMDB_NUM_KERNEL_CLASSES] = {};
+};
+
+// Enqueues one kernel launch of class `cls` on the handle's stream.
+template <class F>
+static void launch(pimdb_handle* h, int cls, F&& f) {
+    h->launches += 1;
+    if (!h->profile) {
+        f();
+        return;
+    }
+    cudaEventRecord(h->ev0, h->stream);
+    f();
+    cudaEventRecord(h->ev1, h->stream);
+    cudaEventSynchronize(h->ev1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->prof_ms[cls] += ms;
+    h->prof_n[cls] += 1;
+}
+
+static std::string g_last_error;
+
+static int fail(pimdb_handle* h, int code, const std::string& msg) {
+    if (h) h->last_error = msg;
+    g_last_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(h, expr)                                                                       \
+    do {                                                                                        \
+        cudaError_t e_ = (expr);                                                                \
+        if (e_ != cudaSuccess) return fail((h), PIMDB_ERR_CUDA, std::string(#expr ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" const char* pimdb_status_string(int st) {
+    switch (st) {
+    case PIMDB_OK: return "ok";
+    case PIMDB_ERR_CONFIG: return "invalid configuration";
+    case PIMDB_ERR_NONFINITE_VB: return "non-finite bosonic exchange potential";
+    case PIMDB_ERR_CUDA: return "CUDA error";
+    case PIMDB_ERR_TIMEOUT: return "device wait timed out";
+    case PIMDB_ERR_BOUNDS: return "device index out of bounds";
+    case PIMDB_ERR_ARG: return "invalid argument";
+    case PIMDB_ERR_NO_DEVICE: return "no CUDA device";
+    case PIMDB_ERR_PARSE: return "cannot read configuration file";
+    default: return "unknown status";
+    }
+}
+
+extern "C" int pimdb_last_error(const pimdb_handle* h, char* buf, int len) {
+    if (!buf || len <= 0) return PIMDB_ERR_ARG;
+    const std::string& m = h ? h->last_error : g_last_error;
+    std::snprintf(buf, (size_t)len, "%s", m.c_str());
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_config_default(pimdb_config* c) {
+    if (!c) return PIMDB_ERR_ARG;
+    std::memset(c, 0, sizeof(*c));
+    // src/params.cpp:15-259 defaults
+    c->ndim = 3;
+    c->natoms = 1;
+    c->nbeads = 4;
+    c->fixcom = 1;
+    c->dt = 1.0 * 4.1341373e16 * 1e-15;        // 1 femtosecond
+    c->gamma = -1.0;
+    c->temperature = 1.0 * 3.1668152e-06;      // 1 kelvin
+    c->mass = 1.0 * 1822.8885;                 // 1 dalton
+    c->size = 1.0 * 1.8897261e10 * 1e-12;      // 1 picometer
+    c->cutoff = -1.0 * 1.8897261;              // -1 angstrom
+    c->seed = 1234;
+    c->thermostat = PIMDB_THERMO_LANGEVIN;
+    return PIMDB_OK;
+}
+
+static std::string validate(const pimdb_config& c) {
+    if (c.ndim < 1 || c.ndim > 3) return "ndim must be 1, 2 or 3";
+    if (c.nbeads < 1) return "The specified number of beads is less than one!";
+    if (c.natoms < 1) return "The specified number of particles is smaller than one!";
+    if (!(c.temperature > 0.0)) return "The specified temperature is unphysical!";
+    if (!(c.mass > 0.0)) return "The provided mass is unphysical!";
+    if (!(c.size > 0.0)) return "The provided system size is unphysical!";
+    if (!(c.dt > 0.0)) return "dt must be positive";
+    if (c.propagator != PIMDB_PROP_CARTESIAN && c.propagator != PIMDB_PROP_NORMAL_MODES)
+        return "The specified time propagator is not supported!";
+    if (c.thermostat != PIMDB_THERMO_NONE && c.thermostat != PIMDB_THERMO_LANGEVIN)
+        return "The specified thermostat is not supported!";
+    if (c.nmthermostat && c.thermostat == PIMDB_THERMO_NONE) return "nmthermostat cannot be used in nve ensemble!";
+    if (c.ext_kind != PIMDB_POT_FREE && c.ext_kind != PIMDB_POT_HARMONIC && c.ext_kind != PIMDB_POT_DOUBLE_WELL &&
+        c.ext_kind != PIMDB_POT_COSINE)
+        return "The specified external potential is not supported!";
+    if (c.int_kind != PIMDB_POT_FREE && c.int_kind != PIMDB_POT_HARMONIC && c.int_kind != PIMDB_POT_AZIZ &&
+        c.int_kind != PIMDB_POT_DIPOLE)
+        return "The specified interaction potential is not supported!";
+    if (c.precision != PIMDB_FP64 && c.precision != PIMDB_MIXED) return "unknown precision";
+    if ((long long)c.natoms * c.nbeads * c.ndim > (1ll << 31)) return "system too large";
+    if (c.bosonic && c.nbeads > 1 && c.natoms > 16384) return "bosonic exchange supports at most 16384 particles";
+    return "";
+}
+
+// Reference normal-mode rows (src/normal_modes.cpp:48-79), bit for bit.
+static void nm_tables(int P, double omega_p, double mass, double dt, std::vector<double>& C, std::vector<double>& T,
+                      std::vector<double>& rot) {
+    const double pi = 3.14159265358979323846;
+    C.assign((size_t)P * P, 0.0);
+    T.assign((size_t)P * P, 0.0);
+    rot.assign((size_t)P * 3, 0.0);
+    for (int k = 0; k < P; ++k) {
+        double* row = &C[(size_t)k * P];
+        const double fund = 2 * pi / P * k;
+        if (k == 0) {
+            const double pref = 1 / std::sqrt((double)P);
+            for (int i = 0; i < P; ++i) row[i] = pref;
+        } else if (k < 0.5 * P) {
+            const double pref = std::sqrt(2.0 / P);
+            for (int i = 0; i < P; ++i) row[i] = pref * std::cos(fund * i);
+        } else if (k == 0.5 * P) {
+            const double pref = 1 / std::sqrt((double)P);
+            for (int i = 0; i < P; ++i) row[i] = pref * (i % 2 == 0 ? 1.0 : -1.0);
+        } else {
+            const double pref = std::sqrt(2.0 / P);
+            for (int i = 0; i < P; ++i) row[i] = -pref * std::sin(fund * i);
+        }
+        // normal_modes_propagator.cpp:13-16
+        const double freq = 2 * omega_p * std::sin(k * pi / P);
+        rot[3 * k] = std::cos(freq * dt);
+        rot[3 * k + 1] = std::sin(freq * dt);
+        rot[3 * k + 2] = mass * freq;
+    }
+    for (int j = 0; j < P; ++j) {
+        double* row = &T[(size_t)j * P];
+        const double fund = 2 * pi / P * j;
+        const double pref = std::sqrt(2.0 / P);
+        row[0] = 1 / std::sqrt((double)P);
+        for (int i = 1; i < 0.5 * P; ++i) row[i] = pref * std::cos(fund * i);
+        if (P % 2 == 0) row[P / 2] = 1 / std::sqrt((double)P) * (j % 2 == 0 ? 1.0 : -1.0);
+        for (int i = (int)std::ceil(0.5 * (P + 1)); i < P; ++i) row[i] = -pref * std::sin(fund * i);
+    }
+}
+
+static void free_handle(pimdb_handle* h) {
+    double* bufs[] = {h->s.x, h->s.p, h->s.f, h->s.fphys, h->s.fx, h->s.E, h->s.V, h->s.Vb, h->s.scal,
+                      h->d_C, h->d_T, h->d_rot, h->d_red[0], h->d_red[1], h->d_stage};
+    for (double* b : bufs)
+        if (b) cudaFree(b);
+    if (h->d_err) cudaFree(h->d_err);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_handle** out) {
+    if (!cfg || !out) return fail(nullptr, PIMDB_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    const std::string why = validate(*cfg);
+    if (!why.empty()) return fail(nullptr, PIMDB_ERR_CONFIG, why);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(nullptr, PIMDB_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    pimdb_handle* h = new (std::nothrow) pimdb_handle();
+    if (!h) return fail(nullptr, PIMDB_ERR_ARG, "out of host memory");
+    h->cfg = *cfg;
+    const pimdb_config& c = h->cfg;
+    h->D = c.ndim;
+    Sys& s = h->s;
+    s.N = c.natoms;
+    s.P = c.nbeads;
+    s.ld = (c.natoms + 31) / 32 * 32;
+    s.bosonic = (c.bosonic && c.nbeads > 1) ? 1 : 0;  // simulation.cpp:690
+    s.pbc = c.pbc ? 1 : 0;
+    s.L = c.size;
+    s.invL = 1.0 / c.size;
+    s.mass = c.mass;
+    s.dt = c.dt;
+    // simulation.cpp:37-52 (IPI convention, kB = hbar = 1)
+    const double beta = 1.0 / (1.0 * c.temperature);
+    const double thermo_beta = beta / c.nbeads;
+    s.omega_p = c.nbeads / (beta * 1.0);
+    s.kappa = c.mass * s.omega_p * s.omega_p;
+    s.beta_ex = beta / c.nbeads;  // bosonic_exchange_base.cpp:16-18
+    // langevin.cpp:11-12, params.cpp:17-20
+    const double gamma = c.gamma < 0 ? 1 / (100.0 * c.dt) : c.gamma;
+    s.c1 = std::exp(-0.5 * gamma * c.dt);
+    s.c2 = std::sqrt((1 - s.c1 * s.c1) * c.mass / thermo_beta);
+    // simulation.cpp:84-90
+    double cut = (c.int_kind == PIMDB_POT_FREE) ? 0.0 : c.cutoff;
+    if (c.pbc && 0.5 * c.size < cut) cut = 0.5 * c.size;
+    s.cutoff = cut;
+    s.ext_kind = c.ext_kind;
+    if (c.ext_kind == PIMDB_POT_HARMONIC) {
+        s.ext_a = c.mass * c.ext_params[0] * c.ext_params[0];
+    } else if (c.ext_kind == PIMDB_POT_DOUBLE_WELL) {
+        s.ext_a = 4 * c.mass * c.ext_params[0];
+        s.ext_b = c.ext_params[1] * c.ext_params[1];
+        s.ext_c = c.mass * c.ext_params[0];
+    } else if (c.ext_kind == PIMDB_POT_COSINE) {
+        const double k = 2 * 3.14159265358979323846 / c.size;
+        s.ext_a = -c.ext_params[0] * k;
+        s.ext_b = k;
+        s.ext_c = c.ext_params[1];
+    }
+    s.int_kind = c.int_kind;
+    if (c.int_kind == PIMDB_POT_HARMONIC) s.int_a = c.mass * c.int_params[0] * c.int_params[0];
+    else if (c.int_kind == PIMDB_POT_DIPOLE) s.int_a = c.int_params[0];
+    s.seed = c.seed;
+    s.replica = c.replica;
+
+    auto alloc = [&](double** p, size_t n) -> cudaError_t {
+        cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(double));
+        if (e == cudaSuccess) e = cudaMemset(*p, 0, std::max<size_t>(n, 1) * sizeof(double));
+        return e;
+    };
+    const size_t nstate = (size_t)s.P * h->D * s.ld;
+    const int nred = std::max(cart_update_blocks(s, h->D), nm_blocks(s, h->D));
+    cudaError_t e = cudaSuccess;
+    if (cuda_stream) {
+        h->stream = (cudaStream_t)cuda_stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+        h->own_stream = (e == cudaSuccess);
+    }
+    if (e == cudaSuccess) e = alloc(&s.x, nstate);
+    if (e == cudaSuccess) e = alloc(&s.p, nstate);
+    if (e == cudaSuccess) e = alloc(&s.f, nstate);
+    if (e == cudaSuccess) e = alloc(&s.fphys, nstate);
+    if (e == cudaSuccess) e = alloc(&s.fx, (size_t)2 * h->D * s.ld);
+    if (e == cudaSuccess) e = alloc(&s.E, s.bosonic ? (size_t)s.N * (s.N + 1) / 2 : 1);
+    if (e == cudaSuccess) e = alloc(&s.V, (size_t)s.N + 1);
+    if (e == cudaSuccess) e = alloc(&s.Vb, (size_t)s.N + 1);
+    if (e == cudaSuccess) e = alloc(&s.scal, 4);
+    if (e == cudaSuccess) e = alloc(&h->d_red[0], (size_t)3 * nred);
+    if (e == cudaSuccess) e = alloc(&h->d_red[1], (size_t)3 * nred);
+    if (e == cudaSuccess) e = alloc(&h->d_stage, (size_t)s.P * s.N * h->D);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
+    if (e == cudaSuccess && (c.propagator == PIMDB_PROP_NORMAL_MODES || c.nmthermostat)) {
+        std::vector<double> C, T, rot;
+        nm_tables(s.P, s.omega_p, s.mass, s.dt, C, T, rot);
+        e = alloc(&h->d_C, C.size());
+        if (e == cudaSuccess) e = alloc(&h->d_T, T.size());
+        if (e == cudaSuccess) e = alloc(&h->d_rot, rot.size());
+        if (e == cudaSuccess) e = cudaMemcpy(h->d_C, C.data(), C.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(h->d_T, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->d_rot, rot.data(), rot.size() * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    s.err = h->d_err;
+    s.red = h->d_red[0];
+    if (e != cudaSuccess) {
+        std::string msg = std::string("allocation failed: ") + cudaGetErrorString(e);
+        free_handle(h);
+        return fail(nullptr, PIMDB_ERR_CUDA, msg);
+    }
+    *out = h;
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_destroy(pimdb_handle* h) {
+    if (!h) return PIMDB_ERR_ARG;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_handle(h);
+    return PIMDB_OK;
+}
+
+static int check_err_word(pimdb_handle* h) {
+    int err = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (err) {
+        CUDA_TRY(h, cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+        if (err & ERRB_NONFINITE_VB)
+            return fail(h, PIMDB_ERR_NONFINITE_VB, "Invalid sig_denom in bosonic exchange potential");
+        if (err & ERRB_TIMEOUT) return fail(h, PIMDB_ERR_TIMEOUT, "device wait timed out");
+        return fail(h, PIMDB_ERR_BOUNDS, "device index check failed");
+    }
+    return PIMDB_OK;
+}
+
+static int set_state_impl(pimdb_handle* h, const double* x, const double* p, cudaMemcpyKind kind) {
+    if (!h) return PIMDB_ERR_ARG;
+    Sys& s = h->s;
+    const size_t n = (size_t)s.P * s.N * h->D;
+    const double* src[2] = {x, p};
+    double* dst[2] = {s.x, s.p};
+    for (int k = 0; k < 2; ++k) {
+        if (!src[k]) continue;
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, src[k], n * sizeof(double), kind, h->stream));
+        launch_pack(s, h->D, h->d_stage, dst[k], h->stream);
+    }
+    const size_t nstate = (size_t)s.P * h->D * s.ld;
+    CUDA_TRY(h, cudaMemsetAsync(s.f, 0, nstate * sizeof(double), h->stream));
+    CUDA_TRY(h, cudaMemsetAsync(s.fphys, 0, nstate * sizeof(double), h->stream));
+    CUDA_TRY(h, cudaMemsetAsync(s.fx, 0, (size_t)2 * h->D * s.ld * sizeof(double), h->stream));
+    h->com_pending = false;
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_set_state(pimdb_handle* h, const double* x, const double* p) {
+    return set_state_impl(h, x, p, cudaMemcpyHostToDevice);
+}
+extern "C" int pimdb_set_state_device(pimdb_handle* h, const double* x, const double* p) {
+    return set_state_impl(h, x, p, cudaMemcpyDeviceToDevice);
+}
+
+static int get_state_impl(pimdb_handle* h, double* x, double* p, double* f, cudaMemcpyKind kind) {
+    if (!h) return PIMDB_ERR_ARG;
+    Sys& s = h->s;
+    const size_t n = (size_t)s.P * s.N * h->D;
+    double* dst[3] = {x, p, f};
+    const double* src[3] = {s.x, s.p, s.f};
+    for (int k = 0; k < 3; ++k) {
+        if (!dst[k]) continue;
+        launch_unpack(s, h->D, src[k], h->d_stage, h->stream);
+        CUDA_TRY(h, cudaMemcpyAsync(dst[k], h->d_stage, n * sizeof(double), kind, h->stream));
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_get_state(pimdb_handle* h, double* x, double* p, double* f) {
+    return get_state_impl(h, x, p, f, cudaMemcpyDeviceToHost);
+}
+extern "C" int pimdb_get_state_device(pimdb_handle* h, double* x, double* p, double* f) {
+    return get_state_impl(h, x, p, f, cudaMemcpyDeviceToDevice);
+}
+
+extern "C" int pimdb_set_step(pimdb_handle* h, long long step) {
+    if (!h) return PIMDB_ERR_ARG;
+    h->step = step;
+    return PIMDB_OK;
+}
+extern "C" int pimdb_get_step(pimdb_handle* h, long long* step) {
+    if (!h || !step) return PIMDB_ERR_ARG;
+    *step = h->step;
+    return PIMDB_OK;
+}
+
+// Simulation::updateForces for all beads.
+static void enqueue_forces(pimdb_handle* h) {
+    const Sys& s = h->s;
+    const bool nm = h->cfg.propagator == PIMDB_PROP_NORMAL_MODES;
+    if (s.bosonic) {
+        launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
+        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, h->stream); });
+    }
+    launch(h, PIMDB_K_BEAD_FORCES,
+           [&] { launch_bead_forces(s, h->D, h->cfg.precision == PIMDB_MIXED, nm ? 1 : 0, h->stream); });
+    if (s.bosonic) launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 1, h->stream); });
+}
+
+extern "C" int pimdb_compute_forces(pimdb_handle* h) {
+    if (!h) return PIMDB_ERR_ARG;
+    enqueue_forces(h);
+    CUDA_TRY(h, cudaGetLastError());
+    return check_err_word(h);
+}
+
+// Momentum kernels with the COM bookkeeping: a kernel that applies the
+// pending correction reads buffer red_last and writes new partials into the
+// other buffer.
+static void cart(pimdb_handle* h, int flags, int substep, int kick_nm) {
+    const int rin = h->red_last, rout = 1 - h->red_last;
+    if (!h->com_pending) flags &= ~SF_COM_APPLY;
+    launch(h, PIMDB_K_CART_UPDATE, [&] {
+        launch_cart_update(h->s, h->D, flags, h->d_red[rin], h->nred_last, h->d_red[rout], h->step, substep, kick_nm,
+                           h->stream);
+    });
+    if (flags & SF_COM_APPLY) h->com_pending = false;
+    if (flags & SF_COM_PARTIAL) {
+        h->red_last = rout;
+        h->nred_last = cart_update_blocks(h->s, h->D);
+        h->com_pending = true;
+    }
+}
+
+static void nm_thermo(pimdb_handle* h, int flags, int substep) {
+    const int rin = h->red_last, rout = 1 - h->red_last;
+    if (!h->com_pending) flags &= ~SF_COM_APPLY;
+    launch(h, PIMDB_K_NM_THERMO, [&] {
+        launch_nm_thermo(h->s, h->D, h->d_C, h->d_T, flags, h->d_red[rin], h->nred_last, h->d_red[rout], h->step,
+                         substep, h->stream);
+    });
+    if (flags & SF_COM_APPLY) h->com_pending = false;
+    if (flags & SF_COM_PARTIAL) {
+        h->red_last = rout;
+        h->nred_last = nm_blocks(h->s, h->D);
+        h->com_pending = true;
+    }
+}
+
+// Applies the O-step of the configured thermostat (thermostat.cpp:15-19)
+// followed, when fixcom, by the partial sums for the COM removal.
+static void thermostat_step(pimdb_handle* h, int substep) {
+    const pimdb_config& c = h->cfg;
+    const int part = c.fixcom ? SF_COM_PARTIAL : 0;
+    if (c.thermostat == PIMDB_THERMO_LANGEVIN && c.nmthermostat) {
+        nm_thermo(h, SF_COM_APPLY | part, substep);
+    } else if (c.thermostat == PIMDB_THERMO_LANGEVIN) {
+        cart(h, SF_COM_APPLY | SF_LANGEVIN | part, substep, 0);
+    } else if (c.fixcom || h->com_pending) {
+        cart(h, SF_COM_APPLY | part, substep, 0);
+    }
+}
+
+static void enqueue_steps(pimdb_handle* h, int nsteps) {
+    const pimdb_config& c = h->cfg;
+    const bool nm = c.propagator == PIMDB_PROP_NORMAL_MODES;
+    const bool cart_langevin = c.thermostat == PIMDB_THERMO_LANGEVIN && !c.nmthermostat;
+    for (int it = 0; it < nsteps; ++it) {
+        // O, [COM]
+        thermostat_step(h, 0);
+        if (!nm) {
+            // [COM], B, A (velocity_verlet.cpp:9-12)
+            cart(h, SF_COM_APPLY | SF_KICK | SF_DRIFT, 0, 0);
+            enqueue_forces(h);
+            // B, then O (+ partials) when the thermostat is Cartesian Langevin
+            if (cart_langevin) {
+                cart(h, SF_KICK | SF_LANGEVIN | (c.fixcom ? SF_COM_PARTIAL : 0), 1, 0);
+            } else {
+                cart(h, SF_KICK, 1, 0);
+                thermostat_step(h, 1);
+            }
+        } else {
+            // [COM] + half-kick + free ring-polymer propagation
+            const int rin = h->red_last;
+            const int apply = h->com_pending ? 1 : 0;
+            launch(h, PIMDB_K_NM_PROPAGATE, [&] {
+                launch_nm_propagate(h->s, h->D, h->d_C, h->d_T, h->d_rot, apply, h->d_red[rin], h->nred_last,
+                                    h->stream);
+            });
+            h->com_pending = false;
+            enqueue_forces(h);
+            if (cart_langevin) {
+                cart(h, SF_KICK | SF_LANGEVIN | (c.fixcom ? SF_COM_PARTIAL : 0), 1, 1);
+            } else {
+                cart(h, SF_KICK, 1, 1);
+                thermostat_step(h, 1);
+            }
+        }
+        h->step += 1;
+    }
+    // the last COM removal of the last step
+    if (h->com_pending) {
+        const long long keep = h->step;
+        cart(h, SF_COM_APPLY, 0, 0);
+        h->step = keep;
+    }
+}
+
+extern "C" int pimdb_step_async(pimdb_handle* h, int nsteps) {
+    if (!h || nsteps < 0) return PIMDB_ERR_ARG;
+    enqueue_steps(h, nsteps);
+    CUDA_TRY(h, cudaGetLastError());
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_step(pimdb_handle* h, int nsteps) {
+    int st = pimdb_step_async(h, nsteps);
+    if (st != PIMDB_OK) return st;
+    return check_err_word(h);
+}
+
+extern "C" int pimdb_synchronize(pimdb_handle* h) {
+    if (!h) return PIMDB_ERR_ARG;
+    CUDA_TRY(h, cudaGetLastError());
+    return check_err_word(h);
+}
+
+extern "C" int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first, double* f_last) {
+    if (!h) return PIMDB_ERR_ARG;
+    const Sys& s = h->s;
+    if (!s.bosonic) return fail(h, PIMDB_ERR_CONFIG, "pimdb_exchange needs a bosonic configuration with nbeads > 1");
+    launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
+    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, h->stream); });
+    launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 0, h->stream); });
+    launch(h, PIMDB_K_EXCH_ESTIMATORS, [&] { launch_exchange_estimators(s, h->stream); });
+    CUDA_TRY(h, cudaGetLastError());
+    int st = check_err_word(h);
+    if (st != PIMDB_OK) return st;
+    if (scalars) CUDA_TRY(h, cudaMemcpy(scalars, s.scal, 4 * sizeof(double), cudaMemcpyDeviceToHost));
+    const int D = h->D;
+    std::vector<double> fx((size_t)2 * D * s.ld);
+    if (f_first || f_last) {
+        CUDA_TRY(h, cudaMemcpy(fx.data(), s.fx, fx.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int side = 0; side < 2; ++side) {
+            double* out = side == 0 ? f_first : f_last;
+            if (!out) continue;
+            for (int i = 0; i < s.N; ++i)
+                for (int a = 0; a < D; ++a) out[(size_t)i * D + a] = fx[((size_t)side * D + a) * s.ld + i];
+        }
+    }
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_exchange_arrays(pimdb_handle* h, double* E_kn, double* V, double* Vb) {
+    if (!h) return PIMDB_ERR_ARG;
+    const Sys& s = h->s;
+    if (!s.bosonic) return fail(h, PIMDB_ERR_CONFIG, "no exchange arrays for a distinguishable configuration");
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (E_kn) CUDA_TRY(h, cudaMemcpy(E_kn, s.E, (size_t)s.N * (s.N + 1) / 2 * sizeof(double), cudaMemcpyDeviceToHost));
+    if (V) CUDA_TRY(h, cudaMemcpy(V, s.V, (size_t)(s.N + 1) * sizeof(double), cudaMemcpyDeviceToHost));
+    if (Vb) CUDA_TRY(h, cudaMemcpy(Vb, s.Vb, (size_t)(s.N + 1) * sizeof(double), cudaMemcpyDeviceToHost));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, long long* launches) {
+    if (!h) return PIMDB_ERR_ARG;
+    for (int k = 0; k < PIMDB_NUM_KERNEL_CLASSES; ++k) {
+        if (ms) ms[k] = h->prof_ms[k];
+        if (counts) counts[k] = h->prof_n[k];
+    }
+    if (launches) *launches = h->launches;
+    if (enable >= 0) {
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        h->profile = enable > 0;
+        for (int k = 0; k < PIMDB_NUM_KERNEL_CLASSES; ++k) {
+            h->prof_ms[k] = 0.0;
+            h->prof_n[k] = 0;
+        }
+        h->launches = 0;
+    }
+    return PIMDB_OK;
+}
+
+// FP64 pipe throughput probe: independent fused multiply-add chains, no
+// memory traffic.  Used as the measured FP64 peak of the roofline.
+__global__ void k_fp64_fma_probe(double* out, int iters, double a, double b) {
+    double r0 = threadIdx.x * 1e-9, r1 = r0 + 1e-9, r2 = r0 + 2e-9, r3 = r0 + 3e-9;
+    double r4 = r0 + 4e-9, r5 = r0 + 5e-9, r6 = r0 + 6e-9, r7 = r0 + 7e-9;
+    for (int i = 0; i < iters; ++i) {
+        r0 = fma(r0, a, b); r1 = fma(r1, a, b); r2 = fma(r2, a, b); r3 = fma(r3, a, b);
+        r4 = fma(r4, a, b); r5 = fma(r5, a, b); r6 = fma(r6, a, b); r7 = fma(r7, a, b);
+    }
+    const double s = r0 + r1 + r2 + r3 + r4 + r5 + r6 + r7;
+    if (s == 1.2345) out[0] = s;  // keeps the chains alive
+}
+
+extern "C" int pimdb_measure_fp64_peak(double* tflops) {
+    if (!tflops) return PIMDB_ERR_ARG;
+    int dev = 0, sms = 0;
+    CUDA_TRY(nullptr, cudaGetDevice(&dev));
+    CUDA_TRY(nullptr, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double* out = nullptr;
+    CUDA_TRY(nullptr, cudaMalloc((void**)&out, sizeof(double)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    k_fp64_fma_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e0);
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r) k_fp64_fma_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    CUDA_TRY(nullptr, cudaGetLastError());
+    const double flops = 2.0 * 8.0 * iters * (double)threads * blocks * reps;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return PIMDB_OK;
+}

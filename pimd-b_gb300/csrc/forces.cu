@@ -1,0 +1,224 @@
+// Per-bead forces: external potential, all-pairs interaction (shared-memory
+// tiled, minimum image, cutoff) and the distinguishable ring springs.
+//
+// Reference: Simulation::updateForces / updateSpringForces /
+// updatePhysicalForces (src/simulation.cpp:353-455) and the potentials'
+// gradV (src/potentials/{harmonic,aziz,dipole,double_well,cosine}.cpp).
+//
+// One thread owns one particle of one bead and sums the pair gradient over
+// every other particle of the same bead (j ascending), so no atomics are
+// needed and the result is deterministic.  Precision: `R` is the arithmetic
+// type of the pair gradient (double for the plain path, float for the mixed
+// path, which reconstructs separations from hi/lo float pairs and adds each
+// tile's float partial sum into a double accumulator).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pimdb {
+
+// Aziz HFDHE2 (reference aziz.cpp:6-13, aziz.h:25-34).
+struct Aziz {
+    static constexpr double rm = 5.60738, A = 0.5448504e6, eps = 3.42016E-5, alpha = 13.353384, D = 1.241314,
+                            C6 = 1.3732412, C8 = 0.4253785, C10 = 0.1781;
+};
+
+// grad V(r) = s(r) * r for the radial pair potentials.  `r2` is |r|^2.
+template <typename R>
+__device__ __forceinline__ R pair_scale(int kind, R r2, R param);
+
+template <>
+__device__ __forceinline__ double pair_scale<double>(int kind, double r2, double param) {
+    if (kind == POT_HARMONIC) return param;  // harmonic.cpp:21-23, k = m w^2
+    const double norm = sqrt(r2);
+    if (kind == POT_DIPOLE) {                 // dipole.cpp:24-45
+        const double n2 = norm * norm;
+        return -3.0 * param / (n2 * n2 * norm);
+    }
+    // POT_AZIZ, aziz.cpp:56-106
+    const double rs = norm * (1.0 / Aziz::rm);
+    const double T1 = -Aziz::A * Aziz::alpha * exp(-Aziz::alpha * rs);
+    double g;
+    if (rs > 1.0E-7 && rs < 0.01) {
+        g = T1 * (Aziz::eps / Aziz::rm);
+    } else {
+        const double ix = 1.0 / rs;
+        const double ix2 = ix * ix;
+        const double ix6 = ix2 * ix2 * ix2;
+        const double ix7 = ix6 * ix, ix8 = ix6 * ix2, ix9 = ix8 * ix, ix10 = ix8 * ix2, ix11 = ix10 * ix;
+        double F = 1.0, dF = 0.0;
+        if (rs < Aziz::D) {
+            const double t = Aziz::D * ix - 1.0;
+            const double e = exp(-t * t);
+            F = e;
+            dF = 2.0 * Aziz::D * ix2 * t * e;
+        }
+        const double T2 = (6.0 * Aziz::C6 * ix7 + 8.0 * Aziz::C8 * ix9 + 10.0 * Aziz::C10 * ix11) * F;
+        const double T3 = -(Aziz::C6 * ix6 + Aziz::C8 * ix8 + Aziz::C10 * ix10) * dF;
+        g = (Aziz::eps / Aziz::rm) * (T1 + T2 + T3);
+    }
+    return g / norm;
+}
+
+template <>
+__device__ __forceinline__ float pair_scale<float>(int kind, float r2, float param) {
+    if (kind == POT_HARMONIC) return param;
+    const float rinv = rsqrtf(r2);
+    if (kind == POT_DIPOLE) {
+        const float ri2 = rinv * rinv;
+        return -3.0f * param * ri2 * ri2 * rinv;
+    }
+    const float norm = r2 * rinv;
+    const float rs = norm * (float)(1.0 / Aziz::rm);
+    const float T1 = (float)(-Aziz::A * Aziz::alpha) * expf(-(float)Aziz::alpha * rs);
+    float g;
+    if (rs > 1.0E-7f && rs < 0.01f) {
+        g = T1 * (float)(Aziz::eps / Aziz::rm);
+    } else {
+        const float ix = (float)Aziz::rm * rinv;
+        const float ix2 = ix * ix;
+        const float ix6 = ix2 * ix2 * ix2;
+        const float ix7 = ix6 * ix, ix8 = ix6 * ix2, ix9 = ix8 * ix, ix10 = ix8 * ix2, ix11 = ix10 * ix;
+        float F = 1.0f, dF = 0.0f;
+        if (rs < (float)Aziz::D) {
+            const float t = (float)Aziz::D * ix - 1.0f;
+            const float e = expf(-t * t);
+            F = e;
+            dF = 2.0f * (float)Aziz::D * ix2 * t * e;
+        }
+        const float T2 = ((float)(6.0 * Aziz::C6) * ix7 + (float)(8.0 * Aziz::C8) * ix9 +
+                          (float)(10.0 * Aziz::C10) * ix11) * F;
+        const float T3 = -((float)Aziz::C6 * ix6 + (float)Aziz::C8 * ix8 + (float)Aziz::C10 * ix10) * dF;
+        g = (float)(Aziz::eps / Aziz::rm) * (T1 + T2 + T3);
+    }
+    return g * rinv;
+}
+
+// -grad V_ext for one particle (double_well.cpp:22-40, cosine.cpp:23-35,
+// harmonic.cpp:21-23).
+template <int D>
+__device__ __forceinline__ void ext_force(const Sys& s, const double* xi, double* out) {
+    if (s.ext_kind == POT_HARMONIC) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) out[a] = -(xi[a] * s.ext_a);
+    } else if (s.ext_kind == POT_DOUBLE_WELL) {
+        double r2 = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) r2 += xi[a] * xi[a];
+        const double pre = s.ext_a * (r2 - s.ext_b);
+#pragma unroll
+        for (int a = 0; a < D; ++a) out[a] = -(pre * xi[a]);
+    } else if (s.ext_kind == POT_COSINE) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) out[a] = -(s.ext_a * sin(s.ext_b * xi[a] + s.ext_c));
+    } else {
+#pragma unroll
+        for (int a = 0; a < D; ++a) out[a] = 0.0;
+    }
+}
+
+constexpr int kPairThreads = 128;
+
+template <int D, typename R>
+__global__ void __launch_bounds__(kPairThreads) k_bead_forces(Sys s, int write_phys) {
+    __shared__ double xs[D][kPairThreads];
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * kPairThreads + threadIdx.x;
+    const bool active = i < s.N;
+    double xi[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xi[a] = active ? s.x[idx<D>(s, b, a, i)] : 0.0;
+
+    double acc[D];
+    ext_force<D>(s, xi, acc);
+
+    const bool pairs = s.int_kind != POT_FREE && s.cutoff != 0.0;
+    if (pairs) {
+        const double cut = s.cutoff;
+        const R cutR = (R)cut;
+        const R paramR = (R)s.int_a;
+        R hi[D], lo[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            hi[a] = (R)xi[a];
+            lo[a] = (R)(xi[a] - (double)hi[a]);
+        }
+        for (int j0 = 0; j0 < s.N; j0 += kPairThreads) {
+            const int jl = j0 + threadIdx.x;
+            __syncthreads();
+#pragma unroll
+            for (int a = 0; a < D; ++a) xs[a][threadIdx.x] = jl < s.N ? s.x[idx<D>(s, b, a, jl)] : 0.0;
+            __syncthreads();
+            if (!active) continue;
+            const int jn = min(kPairThreads, s.N - j0);
+            R t[D];
+#pragma unroll
+            for (int a = 0; a < D; ++a) t[a] = (R)0;
+            for (int jj = 0; jj < jn; ++jj) {
+                const int j = j0 + jj;
+                if (j == i) continue;
+                R r[D];
+                R r2 = (R)0;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    R d;
+                    if constexpr (sizeof(R) == 8) {
+                        d = xi[a] - xs[a][jj];
+                        if (s.pbc) d = min_image(d, s.L, s.invL);
+                    } else {
+                        const double xj = xs[a][jj];
+                        const float hj = (float)xj;
+                        const float lj = (float)(xj - (double)hj);
+                        d = (hi[a] - hj) + (lo[a] - lj);
+                        if (s.pbc) d = min_image_f(d, (float)s.L, (float)s.invL);
+                    }
+                    r[a] = d;
+                    r2 += d * d;
+                }
+                if (cut < 0.0 || (sizeof(R) == 8 ? sqrt((double)r2) < cut : r2 < cutR * cutR)) {
+                    const R sc = pair_scale<R>(s.int_kind, r2, paramR);
+#pragma unroll
+                    for (int a = 0; a < D; ++a) t[a] -= sc * r[a];
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < D; ++a) acc[a] += (double)t[a];
+        }
+    }
+    if (!active) return;
+
+    const bool bosonic_bead = s.bosonic && (b == 0 || b == s.P - 1);
+    const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        const size_t o = idx<D>(s, b, a, i);
+        if (write_phys) s.fphys[o] = acc[a];
+        if (bosonic_bead) {
+            s.f[o] = acc[a];  // the exchange kernels add the exterior springs
+        } else {
+            double dp = s.x[idx<D>(s, bp, a, i)] - xi[a];
+            double dn = s.x[idx<D>(s, bn, a, i)] - xi[a];
+            if (s.pbc) {
+                dp = min_image(dp, s.L, s.invL);
+                dn = min_image(dn, s.L, s.invL);
+            }
+            s.f[o] = s.kappa * (dp + dn) + acc[a];  // simulation.cpp:405-419, :363-373
+        }
+    }
+}
+
+template <int D>
+void launch_bead_forces(const Sys& s, int mixed, int write_phys, cudaStream_t st) {
+    dim3 grid((s.N + kPairThreads - 1) / kPairThreads, s.P);
+    if (mixed)
+        k_bead_forces<D, float><<<grid, kPairThreads, 0, st>>>(s, write_phys);
+    else
+        k_bead_forces<D, double><<<grid, kPairThreads, 0, st>>>(s, write_phys);
+}
+
+void launch_bead_forces(const Sys& s, int D, int mixed, int write_phys, cudaStream_t st) {
+    if (D == 1) launch_bead_forces<1>(s, mixed, write_phys, st);
+    else if (D == 2) launch_bead_forces<2>(s, mixed, write_phys, st);
+    else launch_bead_forces<3>(s, mixed, write_phys, st);
+}
+
+}  // namespace pimdb

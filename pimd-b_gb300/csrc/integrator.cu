@@ -1,0 +1,312 @@
+// Integrator pieces of the OBABO step (src/simulation.cpp:236-260):
+//   Langevin O-step, Cartesian coupling  langevin.cpp:15-27, thermostat_coupling.cpp:11-25
+//   Langevin O-step, normal-mode coupling thermostat_coupling.cpp:29-47, normal_modes.cpp:99-139
+//   centre-of-mass momentum removal      simulation.cpp:581-603
+//   velocity-Verlet B and A              velocity_verlet.cpp:7-38
+//   normal-mode propagator               normal_modes_propagator.cpp:19-103
+// plus the layout conversions between the reference's per-bead dVec order
+// [bead][particle][axis] and the device order [bead][axis][particle].
+//
+// The centre-of-mass correction needs a sum over every bead and particle.
+// The kernel that last changed the momenta writes per-block partial sums
+// (`red_out`); the next kernel reduces them in a fixed order at start-up
+// (`red_in`), so the result is deterministic.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pimdb {
+
+template <int D>
+__global__ void k_pack(Sys s, const double* __restrict__ src, double* __restrict__ dst) {
+    const size_t n = (size_t)s.P * s.N * D;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(e % D);
+        const size_t bi = e / D;
+        const int i = (int)(bi % s.N);
+        const int b = (int)(bi / s.N);
+        dst[idx<D>(s, b, a, i)] = src[e];
+    }
+}
+
+template <int D>
+__global__ void k_unpack(Sys s, const double* __restrict__ src, double* __restrict__ dst) {
+    const size_t n = (size_t)s.P * s.N * D;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(e % D);
+        const size_t bi = e / D;
+        const int i = (int)(bi % s.N);
+        const int b = (int)(bi / s.N);
+        dst[e] = src[idx<D>(s, b, a, i)];
+    }
+}
+
+template <int D>
+__device__ __forceinline__ void com_from_partials(const Sys& s, const double* red_in, int nred, double* cm,
+                                                  double* shred) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < nred; k += blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) acc[a] += red_in[3 * k + a];
+    }
+    const double inv = 1.0 / ((double)s.N * (double)s.P);
+#pragma unroll
+    for (int a = 0; a < D; ++a) cm[a] = block_sum(acc[a], shred) * inv;
+}
+
+template <int D>
+__device__ __forceinline__ void com_write_partials(double* part, double* red_out, double* shred) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        const double t = block_sum(part[a], shred);
+        if (threadIdx.x == 0) red_out[3 * blockIdx.x + a] = t;
+    }
+}
+
+// Kick source for the normal-mode propagator (normal_modes_propagator.cpp:73-103):
+// physical forces, plus on bosonic beads the exchange spring minus the
+// distinguishable inner springs.
+template <int D>
+__device__ __forceinline__ double nm_kick_force(const Sys& s, int b, int a, int i) {
+    const size_t o = idx<D>(s, b, a, i);
+    double fk = s.fphys[o];
+    if (s.bosonic && (b == 0 || b == s.P - 1)) {
+        const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
+        const double inner = -s.kappa * (2 * s.x[o] - s.x[idx<D>(s, bp, a, i)] - s.x[idx<D>(s, bn, a, i)]);
+        fk = fk + s.fx[((size_t)(b == 0 ? 0 : 1) * D + a) * s.ld + i] - inner;
+    }
+    return fk;
+}
+
+// One thread per (bead, axis, particle pair).
+template <int D>
+__global__ void k_cart_update(Sys s, int flags, const double* __restrict__ red_in, int nred_in,
+                              double* __restrict__ red_out, long long step, int substep, int kick_nm) {
+    __shared__ double shred[32];
+    const int half = (s.N + 1) / 2;
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t total = (size_t)s.P * D * half;
+    double cm[3] = {0.0, 0.0, 0.0};
+    if (flags & SF_COM_APPLY) com_from_partials<D>(s, red_in, nred_in, cm, shred);
+    double part[3] = {0.0, 0.0, 0.0};
+    if (t < total) {
+        const int i2 = (int)(t % half);
+        const int ba = (int)(t / half);
+        const int a = ba % D;
+        const int b = ba / D;
+        double2 z = make_double2(0.0, 0.0);
+        if (flags & SF_LANGEVIN)
+            z = philox_normal_pair(s.seed, s.replica, 2ull * (unsigned long long)step + substep,
+                                   (uint32_t)((size_t)ba * half + i2));
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = 2 * i2 + h;
+            if (i >= s.N) break;
+            const size_t o = idx<D>(s, b, a, i);
+            double p = s.p[o];
+            if (flags & SF_COM_APPLY) p -= cm[a];
+            if (flags & SF_KICK) {
+                const double fk = kick_nm ? nm_kick_force<D>(s, b, a, i) : s.f[o];
+                p += 0.5 * s.dt * fk;
+            }
+            if (flags & SF_LANGEVIN) p = s.c1 * p + s.c2 * (h == 0 ? z.x : z.y);
+            if (flags & SF_DRIFT) s.x[o] += s.dt * p / s.mass;
+            s.p[o] = p;
+            part[a] += p;
+        }
+    }
+    if (flags & SF_COM_PARTIAL) com_write_partials<D>(part, red_out, shred);
+}
+
+constexpr int kNmTile = 32;   // particles per block (one per lane)
+constexpr int kNmThreads = 256;
+
+// Langevin O-step on the normal modes: p_nm = C p, p_nm <- c1 p_nm + c2 xi,
+// p = C^T p_nm.  One block per (particle tile, axis).
+template <int D>
+__global__ void __launch_bounds__(kNmThreads) k_nm_thermo(Sys s, const double* __restrict__ C,
+                                                          const double* __restrict__ T, int flags,
+                                                          const double* __restrict__ red_in, int nred_in,
+                                                          double* __restrict__ red_out, long long step,
+                                                          int substep) {
+    extern __shared__ double sm[];
+    __shared__ double shred[32];
+    const int P = s.P;
+    double* sp = sm;                 // [P][32]
+    double* sq = sm + P * kNmTile;   // [P][32]
+    const int a = blockIdx.y;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int i = blockIdx.x * kNmTile + lane;
+    const bool act = i < s.N;
+    double cm[3] = {0.0, 0.0, 0.0};
+    if (flags & SF_COM_APPLY) com_from_partials<D>(s, red_in, nred_in, cm, shred);
+    for (int b = w; b < P; b += nw) sp[b * kNmTile + lane] = act ? s.p[idx<D>(s, b, a, i)] - cm[a] : 0.0;
+    __syncthreads();
+    const int half = (s.N + 1) / 2;
+    for (int k = w; k < P; k += nw) {
+        double q = 0.0;
+        for (int b = 0; b < P; ++b) q += C[k * P + b] * sp[b * kNmTile + lane];
+        const double2 z = philox_normal_pair(s.seed, s.replica, 2ull * (unsigned long long)step + substep,
+                                             (uint32_t)((size_t)(k * D + a) * half + (i >> 1)));
+        sq[k * kNmTile + lane] = s.c1 * q + s.c2 * ((i & 1) ? z.y : z.x);
+    }
+    __syncthreads();
+    double part[3] = {0.0, 0.0, 0.0};
+    for (int j = w; j < P; j += nw) {
+        double v = 0.0;
+        for (int k = 0; k < P; ++k) v += T[j * P + k] * sq[k * kNmTile + lane];
+        if (act) {
+            s.p[idx<D>(s, j, a, i)] = v;
+            part[a] += v;
+        }
+    }
+    if (flags & SF_COM_PARTIAL) {
+        // partial index: flattened block id
+        double pa[3] = {0.0, 0.0, 0.0};
+        pa[a] = part[a];
+        const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+#pragma unroll
+        for (int ax = 0; ax < D; ++ax) {
+            const double tsum = block_sum(pa[ax], shred);
+            if (threadIdx.x == 0) red_out[3 * bid + ax] = tsum;
+        }
+    }
+}
+
+// Normal-mode propagator step up to the force evaluation
+// (normal_modes_propagator.cpp:19-63): half-kick with the stored physical
+// forces, Cartesian -> normal modes, exact free ring-polymer rotation, back
+// to Cartesian.  rot[k] = {cos(w_k dt), sin(w_k dt), m w_k} (w_0 = 0 is the
+// free-particle drift).
+template <int D>
+__global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double* __restrict__ C,
+                                                             const double* __restrict__ T,
+                                                             const double* __restrict__ rot, int com_apply,
+                                                             const double* __restrict__ red_in, int nred_in) {
+    extern __shared__ double sm[];
+    __shared__ double shred[32];
+    const int P = s.P;
+    double* sx = sm;
+    double* sp = sm + P * kNmTile;
+    double* sq = sm + 2 * P * kNmTile;
+    double* spi = sm + 3 * P * kNmTile;
+    const int a = blockIdx.y;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int i = blockIdx.x * kNmTile + lane;
+    const bool act = i < s.N;
+    double cm[3] = {0.0, 0.0, 0.0};
+    if (com_apply) com_from_partials<D>(s, red_in, nred_in, cm, shred);
+    for (int b = w; b < P; b += nw) {
+        double x = 0.0, p = 0.0;
+        if (act) {
+            const size_t o = idx<D>(s, b, a, i);
+            x = s.x[o];
+            p = s.p[o] - cm[a];
+            p += 0.5 * s.dt * nm_kick_force<D>(s, b, a, i);
+        }
+        sx[b * kNmTile + lane] = x;
+        sp[b * kNmTile + lane] = p;
+    }
+    __syncthreads();
+    for (int k = w; k < P; k += nw) {
+        double q = 0.0, pi = 0.0;
+        for (int b = 0; b < P; ++b) {
+            const double c = C[k * P + b];
+            q += c * sx[b * kNmTile + lane];
+            pi += c * sp[b * kNmTile + lane];
+        }
+        const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+        double qn, pn;
+        if (mw == 0.0) {
+            qn = q + s.dt / s.mass * pi;
+            pn = pi;
+        } else {
+            qn = cs * q + sn / mw * pi;
+            pn = -mw * sn * q + cs * pi;
+        }
+        sq[k * kNmTile + lane] = qn;
+        spi[k * kNmTile + lane] = pn;
+    }
+    __syncthreads();
+    for (int j = w; j < P; j += nw) {
+        double xv = 0.0, pv = 0.0;
+        for (int k = 0; k < P; ++k) {
+            const double t = T[j * P + k];
+            xv += t * sq[k * kNmTile + lane];
+            pv += t * spi[k * kNmTile + lane];
+        }
+        if (act) {
+            const size_t o = idx<D>(s, j, a, i);
+            s.x[o] = xv;
+            s.p[o] = pv;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+static int pack_grid(size_t n) {
+    size_t g = (n + 255) / 256;
+    return (int)(g > 4096 ? 4096 : (g ? g : 1));
+}
+
+void launch_pack(const Sys& s, int D, const double* src, double* dst, cudaStream_t st) {
+    const int g = pack_grid((size_t)s.P * s.N * D);
+    if (D == 1) k_pack<1><<<g, 256, 0, st>>>(s, src, dst);
+    else if (D == 2) k_pack<2><<<g, 256, 0, st>>>(s, src, dst);
+    else k_pack<3><<<g, 256, 0, st>>>(s, src, dst);
+}
+
+void launch_unpack(const Sys& s, int D, const double* src, double* dst, cudaStream_t st) {
+    const int g = pack_grid((size_t)s.P * s.N * D);
+    if (D == 1) k_unpack<1><<<g, 256, 0, st>>>(s, src, dst);
+    else if (D == 2) k_unpack<2><<<g, 256, 0, st>>>(s, src, dst);
+    else k_unpack<3><<<g, 256, 0, st>>>(s, src, dst);
+}
+
+int cart_update_blocks(const Sys& s, int D) {
+    const size_t total = (size_t)s.P * D * ((s.N + 1) / 2);
+    return (int)((total + 255) / 256);
+}
+
+int nm_blocks(const Sys& s, int D) { return ((s.N + kNmTile - 1) / kNmTile) * D; }
+
+void launch_cart_update(const Sys& s, int D, int flags, const double* red_in, int nred_in, double* red_out,
+                        long long step, int substep, int kick_nm, cudaStream_t st) {
+    const int g = cart_update_blocks(s, D);
+    if (D == 1) k_cart_update<1><<<g, 256, 0, st>>>(s, flags, red_in, nred_in, red_out, step, substep, kick_nm);
+    else if (D == 2) k_cart_update<2><<<g, 256, 0, st>>>(s, flags, red_in, nred_in, red_out, step, substep, kick_nm);
+    else k_cart_update<3><<<g, 256, 0, st>>>(s, flags, red_in, nred_in, red_out, step, substep, kick_nm);
+}
+
+template <int D>
+static void nm_thermo_launch(const Sys& s, const double* C, const double* T, int flags, const double* red_in,
+                             int nred_in, double* red_out, long long step, int substep, cudaStream_t st) {
+    const size_t smem = sizeof(double) * 2 * (size_t)s.P * kNmTile;
+    cudaFuncSetAttribute(k_nm_thermo<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((s.N + kNmTile - 1) / kNmTile, D);
+    k_nm_thermo<D><<<grid, kNmThreads, smem, st>>>(s, C, T, flags, red_in, nred_in, red_out, step, substep);
+}
+
+void launch_nm_thermo(const Sys& s, int D, const double* C, const double* T, int flags, const double* red_in,
+                      int nred_in, double* red_out, long long step, int substep, cudaStream_t st) {
+    if (D == 1) nm_thermo_launch<1>(s, C, T, flags, red_in, nred_in, red_out, step, substep, st);
+    else if (D == 2) nm_thermo_launch<2>(s, C, T, flags, red_in, nred_in, red_out, step, substep, st);
+    else nm_thermo_launch<3>(s, C, T, flags, red_in, nred_in, red_out, step, substep, st);
+}
+
+template <int D>
+static void nm_prop_launch(const Sys& s, const double* C, const double* T, const double* rot, int com_apply,
+                           const double* red_in, int nred_in, cudaStream_t st) {
+    const size_t smem = sizeof(double) * 4 * (size_t)s.P * kNmTile;
+    cudaFuncSetAttribute(k_nm_propagate<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((s.N + kNmTile - 1) / kNmTile, D);
+    k_nm_propagate<D><<<grid, kNmThreads, smem, st>>>(s, C, T, rot, com_apply, red_in, nred_in);
+}
+
+void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, const double* rot, int com_apply,
+                         const double* red_in, int nred_in, cudaStream_t st) {
+    if (D == 1) nm_prop_launch<1>(s, C, T, rot, com_apply, red_in, nred_in, st);
+    else if (D == 2) nm_prop_launch<2>(s, C, T, rot, com_apply, red_in, nred_in, st);
+    else nm_prop_launch<3>(s, C, T, rot, com_apply, red_in, nred_in, st);
+}
+
+}  // namespace pimdb

@@ -1,0 +1,43 @@
+// Host-side launch wrappers for the device kernels (one system per call).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace pimdb {
+
+// Flags of the momentum-update kernels.  Within one launch the operations
+// run in this order: COM correction from the pending partial sums, B
+// half-kick, Langevin O-step, A drift, partial sums for the next COM removal.
+enum StepFlags : int {
+    SF_COM_APPLY = 1,
+    SF_LANGEVIN = 2,
+    SF_COM_PARTIAL = 4,
+    SF_KICK = 8,
+    SF_DRIFT = 16,
+};
+
+// forces.cu: external + pair forces and distinguishable springs on every
+// bead; on bosonic beads 0 and P-1 only the physical part is stored in f.
+void launch_bead_forces(const Sys& s, int D, int mixed, int write_phys, cudaStream_t st);
+
+// exchange.cu: Feldman-Hirshberg exchange on beads 1 and P.
+void launch_exchange_energies(const Sys& s, int D, cudaStream_t st);
+void launch_exchange_recursions(const Sys& s, cudaStream_t st);
+void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st);
+void launch_exchange_estimators(const Sys& s, cudaStream_t st);
+
+// integrator.cu
+void launch_pack(const Sys& s, int D, const double* src, double* dst, cudaStream_t st);
+void launch_unpack(const Sys& s, int D, const double* src, double* dst, cudaStream_t st);
+int cart_update_blocks(const Sys& s, int D);
+int nm_blocks(const Sys& s, int D);
+void launch_cart_update(const Sys& s, int D, int flags, const double* red_in, int nred_in, double* red_out,
+                        long long step, int substep, int kick_nm, cudaStream_t st);
+void launch_nm_thermo(const Sys& s, int D, const double* C, const double* T, int flags, const double* red_in,
+                      int nred_in, double* red_out, long long step, int substep, cudaStream_t st);
+void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, const double* rot, int com_apply,
+                         const double* red_in, int nred_in, cudaStream_t st);
+
+}  // namespace pimdb

@@ -1,0 +1,199 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle (which is
+bit-identical to the compiled reference, see test_oracle_vs_reference.py) and
+against the reference's own golden fixtures.
+
+Tolerances: the FP64 path must agree within 1e-10 relative (forces per bead,
+V_B, trajectories); the mixed path within 1e-6 norm-relative force error."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import golden_cases as G
+from tests.gpu_cases import case, momenta, pk, rel_per_bead, ring
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+
+FORCE_CASES = {
+    # name: (case kwargs, ring kwargs)
+    "bosons_trap_N16_P32": (dict(natoms=16, nbeads=32, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+                            dict(spread_ang=0.5)),
+    "bosons_aziz_pbc_N64_P8": (dict(natoms=64, nbeads=8, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=14.0,
+                                    inter="aziz", cutoff_ang=7.0), dict(spread_ang=0.2)),
+    "dist_aziz_allpairs_doublewell": (dict(natoms=40, nbeads=6, bosonic=False, pbc=True, box_ang=12.0,
+                                           mass_amu=4.0026, inter="aziz", cutoff_ang=-1.0, ext="double_well",
+                                           ext_p=(1.32684e-7 * 0.036749326e-3, 3.0 * 1.8897261, 0)),
+                                      dict(spread_ang=0.2)),
+    "bosons_dipole_2d": (dict(ndim=2, natoms=48, nbeads=5, T_K=2.0, inter="dipole", int_p=(2.4799673e-4, 0, 0),
+                              ext="harmonic", ext_p=(1.0 * 0.036749326e-3, 0, 0), box_ang=60.0),
+                         dict(spread_ang=0.3)),
+    "bosons_pairharm_cosine": (dict(natoms=12, nbeads=4, inter="harmonic", int_p=(1.0 * 0.036749326e-3, 0, 0),
+                                    ext="cosine", ext_p=(1.0 * 0.036749326e-3, 0.3, 0)), dict(spread_ang=0.3)),
+    "bosons_1d": (dict(ndim=1, natoms=10, nbeads=3, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+                  dict(spread_ang=0.3)),
+    "bosons_P2": (dict(natoms=6, nbeads=2, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)), dict()),
+    "boson_N1": (dict(natoms=1, nbeads=4, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)), dict()),
+    "dist_P1": (dict(natoms=9, nbeads=1, inter="harmonic", int_p=(1.0 * 0.036749326e-3, 0, 0)), dict()),
+    "bosons_aziz_pbc_N300_P4": (dict(natoms=300, nbeads=4, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=24.0,
+                                     inter="aziz", cutoff_ang=12.0), dict(spread_ang=0.2)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FORCE_CASES))
+def test_forces_match_oracle(name):
+    kw, rk = FORCE_CASES[name]
+    s, cfg = case(**kw)
+    x = ring(s, seed=len(name), **rk)
+    want = O.update_forces(s, x)["f"]
+    with pk.System(cfg) as g:
+        g.set_state(x, np.zeros_like(x))
+        g.compute_forces()
+        _, _, f = g.get_state()
+    assert rel_per_bead(f, want) < FP64_TOL
+
+
+@pytest.mark.parametrize("name", [n for n in sorted(FORCE_CASES) if FORCE_CASES[n][0].get("bosonic", True)
+                                  and FORCE_CASES[n][0].get("nbeads", 4) > 1])
+def test_exchange_matches_oracle(name):
+    kw, rk = FORCE_CASES[name]
+    s, cfg = case(**kw)
+    x = ring(s, seed=len(name) + 7, **rk)
+    ref = O.exchange(s, x)
+    with pk.System(cfg) as g:
+        g.set_state(x, np.zeros_like(x))
+        got = g.exchange()
+        arr = g.exchange_arrays()
+    assert abs(got["VB"] - ref["VB"]) <= FP64_TOL * abs(ref["VB"])
+    for key in ("prim", "p_distinct", "p_longest"):
+        assert abs(got[key] - ref[key]) <= 1e-9 * abs(ref[key]) + 1e-300, key
+    np.testing.assert_allclose(arr["E"], ref["E"], rtol=1e-12, atol=1e-14 * np.abs(ref["E"]).max())
+    np.testing.assert_allclose(arr["V"], ref["V"], rtol=FP64_TOL, atol=1e-14 * np.abs(ref["V"]).max())
+    np.testing.assert_allclose(arr["Vb"][1:], ref["Vb"][1:], rtol=FP64_TOL, atol=1e-14 * np.abs(ref["Vb"]).max())
+    for key in ("f1", "fP"):
+        assert np.abs(got[key] - ref[key]).max() <= FP64_TOL * np.abs(ref[key]).max(), key
+
+
+TRAJ_CASES = {
+    "vv_langevin_bosons_N16_P32": dict(natoms=16, nbeads=32, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    "vv_nve_bosons_aziz": dict(natoms=10, nbeads=6, thermostat="none", fixcom=False, pbc=True, box_ang=9.0,
+                               mass_amu=4.0026, inter="aziz", cutoff_ang=4.5),
+    "vv_nmthermo_bosons": dict(natoms=8, nbeads=8, nmthermostat=True, ext="harmonic",
+                               ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    "nm_langevin_dist": dict(natoms=12, nbeads=8, bosonic=False, propagator="normal_modes",
+                             ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    "nm_nmthermo_bosons_aziz": dict(natoms=16, nbeads=8, propagator="normal_modes", nmthermostat=True,
+                                    T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=11.0, inter="aziz",
+                                    cutoff_ang=5.5, dt_fs=2.0),
+    "nm_none_dist_odd_P": dict(natoms=7, nbeads=5, bosonic=False, propagator="normal_modes", thermostat="none",
+                               ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    "vv_langevin_dipole_2d": dict(ndim=2, natoms=20, nbeads=4, T_K=2.0, inter="dipole", int_p=(2.4799673e-4, 0, 0),
+                                  ext="harmonic", ext_p=(1.0 * 0.036749326e-3, 0, 0), box_ang=40.0),
+}
+
+
+def _run_pair(kw, steps, seed_state=3):
+    s, cfg = case(**kw)
+    x = ring(s, seed=seed_state, spread_ang=0.2)
+    p = momenta(s, seed_state)
+    tr = O.Trajectory(s, x, p)
+    frames = []
+    with pk.System(cfg) as g:
+        g.set_state(x, p)
+        g.set_step(0)
+        for st in range(steps):
+            xi = O.philox_noise_device(cfg.seed, cfg.replica, st, s.nbeads, s.natoms, s.ndim)
+            assert tr.step(xi) == 0
+            g.step(1)
+            frames.append(((tr.x.copy(), tr.p.copy(), tr.f.copy()), g.get_state()))
+    return frames
+
+
+@pytest.mark.parametrize("name", sorted(TRAJ_CASES))
+def test_trajectory_matches_oracle(name):
+    frames = _run_pair(TRAJ_CASES[name], steps=12)
+    for k, (want, got) in enumerate(frames):
+        for w, gq, label in zip(want, got, "xpf"):
+            assert rel_per_bead(gq, w) < 1e-9, (k, label, rel_per_bead(gq, w))
+
+
+def test_multi_step_call_equals_single_steps():
+    kw = TRAJ_CASES["vv_langevin_bosons_N16_P32"]
+    s, cfg = case(**kw)
+    x = ring(s, seed=5, spread_ang=0.2)
+    p = momenta(s, 5)
+    with pk.System(cfg) as a, pk.System(cfg) as b:
+        a.set_state(x, p)
+        b.set_state(x, p)
+        a.step(6)
+        for _ in range(6):
+            b.step(1)
+        sa, sb = a.get_state(), b.get_state()
+    for u, v in zip(sa, sb):
+        assert rel_per_bead(u, v) < 1e-13
+
+
+def test_deterministic():
+    kw = TRAJ_CASES["nm_nmthermo_bosons_aziz"]
+    s, cfg = case(**kw)
+    x = ring(s, seed=9, spread_ang=0.2)
+    p = momenta(s, 9)
+    out = []
+    for _ in range(2):
+        with pk.System(cfg) as g:
+            g.set_state(x, p)
+            g.step(5)
+            out.append(g.get_state())
+    for u, v in zip(*out):
+        assert np.array_equal(u, v)
+
+
+@pytest.mark.parametrize("case_name", G.dynamics_cases())
+def test_gpu_forces_match_golden_frames(case_name, tmp_path):
+    z, _ = G.load()
+    ini = G.write_ini(case_name, tmp_path)
+    # forces do not depend on the thermostat; the Nose-Hoover cases are read as Langevin
+    ini.write_text("\n".join("thermostat = langevin" if ln.strip().startswith("thermostat") else ln
+                             for ln in ini.read_text().splitlines()))
+    cfg = pk.config_from_ini(ini)
+    X = z[f"{case_name}/positions_angstrom"]
+    F = z[f"{case_name}/forces_ev_per_angstrom"]
+    with pk.System(cfg) as g:
+        for fr in range(1, X.shape[0], 4):
+            g.set_state(X[fr] * G.ANGSTROM, np.zeros_like(X[fr]))
+            g.compute_forces()
+            f = g.get_state()[2] / G.EV_PER_ANG
+            assert np.allclose(f, F[fr], rtol=1e-5)
+            assert np.abs(f - F[fr]).max() <= 1e-9 * np.abs(F[fr]).max()
+
+
+MIXED_CASES = ["bosons_aziz_pbc_N64_P8", "bosons_dipole_2d", "bosons_pairharm_cosine", "bosons_aziz_pbc_N300_P4"]
+
+
+@pytest.mark.parametrize("name", MIXED_CASES)
+def test_mixed_precision_force_error(name):
+    kw, rk = FORCE_CASES[name]
+    s, cfg = case(precision="mixed", **kw)
+    x = ring(s, seed=len(name), **rk)
+    want = O.update_forces(s, x)
+    with pk.System(cfg) as g:
+        g.set_state(x, np.zeros_like(x))
+        g.compute_forces()
+        f = g.get_state()[2]
+    err = np.linalg.norm(f - want["f"]) / np.linalg.norm(want["f"])
+    phys_err = np.linalg.norm(f - want["spring"] - want["phys"]) / np.linalg.norm(want["phys"])
+    assert err <= 1e-6 and phys_err <= 1e-6, (err, phys_err)
+
+
+def test_nonfinite_exchange_potential_is_reported():
+    s, cfg = case(natoms=8, nbeads=4, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0))
+    x = ring(s, seed=1)
+    x[0, 3, 1] = np.nan
+    with pk.System(cfg) as g:
+        g.set_state(x, np.zeros_like(x))
+        with pytest.raises(pk.ExchangeOverflowError):
+            g.compute_forces()
+        # the handle stays usable after the error
+        x[0, 3, 1] = 0.0
+        g.set_state(x, np.zeros_like(x))
+        g.compute_forces()
