@@ -250,7 +250,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     pk = importlib.import_module("pimd-b_gb300")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library launches on it and the events below are
+    # recorded on it (the legacy default stream has handle 0, which the C ABI
+    # reads as "create your own stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     cfg = workload_config(w, args.precision)
     cfg.replica = rank
     x0, p0 = initial_state(w, seed=12345 + rank)

@@ -163,6 +163,15 @@ enum pimdb_kernel_class {
  * only reads. */
 int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, long long* launches);
 
+/* Execution options (no counterpart in the reference):
+ *   "exact_exchange" 1: evaluate V and V_backwards level by level with the
+ *                    FP64 log-sum-exp in the reference's own order
+ *                    (evaluateVBn / evaluateVBackwards, :73-128) instead of
+ *                    the estimate + triangular-solve evaluation (default 0);
+ *   "newton3"        0: all-pairs pair kernel (each pair evaluated from both
+ *                    sides) instead of the pair-tile kernel (default 1). */
+int pimdb_set_option(pimdb_handle* h, const char* name, int value);
+
 /* Measures the FP64 fused-multiply-add throughput of the current device in
  * TFLOP/s (the roofline denominator of the FP64 kernels). */
 int pimdb_measure_fp64_peak(double* tflops);

@@ -28,7 +28,7 @@ EXPORTS = [
     "pimdb_set_state_device", "pimdb_get_state", "pimdb_get_state_device", "pimdb_set_step", "pimdb_get_step",
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
     "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
-    "pimdb_measure_fp64_peak",
+    "pimdb_measure_fp64_peak", "pimdb_set_option",
 ]
 KERNEL_CLASSES = ["bead_forces", "exch_energies", "exch_recursions", "exch_forces", "exch_estimators",
                   "cart_update", "nm_propagate", "nm_thermo"]
@@ -91,6 +91,7 @@ def lib():
             "pimdb_status_string": ([C.c_int], C.c_char_p),
             "pimdb_profile": ([vp, C.c_int, vp, vp, vp], C.c_int),
             "pimdb_measure_fp64_peak": ([vp], C.c_int),
+            "pimdb_set_option": ([vp, C.c_char_p, C.c_int], C.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -222,6 +223,9 @@ class System:
         fn = lib().pimdb_get_state_device if device else lib().pimdb_get_state
         args = [C.c_void_p(v) if v else None for v in (x_ptr, p_ptr, f_ptr)]
         _check(fn(self._h, *args), self._h)
+
+    def set_option(self, name: str, value: int):
+        _check(lib().pimdb_set_option(self._h, name.encode(), int(value)), self._h)
 
     def set_step(self, step: int):
         _check(lib().pimdb_set_step(self._h, step), self._h)

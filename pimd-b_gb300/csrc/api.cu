@@ -27,6 +27,7 @@ struct pimdb_handle {
     double* d_rot = nullptr;  // [P][3]
     double* d_red[2] = {nullptr, nullptr};
     double* d_stage = nullptr;
+    double* d_part = nullptr;  // pair-tile partial sums (Newton's third law path)
     int* d_err = nullptr;
     long long step = 0;
     int red_last = 0;         // buffer holding the pending COM partials
@@ -36,6 +37,8 @@ struct pimdb_handle {
     // instrumentation: kernel launch count and, when enabled, per-class
     // device time measured with events bracketing each launch
     long long launches = 0;
+    int opt_exact_exchange = 0;
+    int opt_newton3 = 1;
     bool profile = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double prof_ms[PIMDB_NUM_KERNEL_CLASSES] = {};
@@ -44,8 +47,8 @@ struct pimdb_handle {
 
 // Enqueues one kernel launch of class `cls` on the handle's stream.
 template <class F>
-static void launch(pimdb_handle* h, int cls, F&& f) {
-    h->launches += 1;
+static void launch(pimdb_handle* h, int cls, F&& f, int nkernels = 1) {
+    h->launches += nkernels;
     if (!h->profile) {
         f();
         return;
@@ -181,11 +184,14 @@ static void nm_tables(int P, double omega_p, double mass, double dt, std::vector
 }
 
 static void free_handle(pimdb_handle* h) {
-    double* bufs[] = {h->s.x, h->s.p, h->s.f, h->s.fphys, h->s.fx, h->s.E, h->s.V, h->s.Vb, h->s.scal,
-                      h->d_C, h->d_T, h->d_rot, h->d_red[0], h->d_red[1], h->d_stage};
+    double* bufs[] = {h->s.x,   h->s.p,   h->s.f,   h->s.fphys, h->s.fx,   h->s.E,        h->s.V,
+                      h->s.Vb,  h->s.scal, h->s.Vh, h->s.Vbh,  h->s.yf,   h->s.yb,       h->s.Wf,
+                      h->s.Wb,  h->s.rowR, h->s.rowC, h->d_C,  h->d_T,    h->d_rot,      h->d_red[0],
+                      h->d_red[1], h->d_stage, h->d_part};
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (h->d_err) cudaFree(h->d_err);
+    if (h->s.xflags) cudaFree(h->s.xflags);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -273,6 +279,21 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     if (e == cudaSuccess) e = alloc(&s.V, (size_t)s.N + 1);
     if (e == cudaSuccess) e = alloc(&s.Vb, (size_t)s.N + 1);
     if (e == cudaSuccess) e = alloc(&s.scal, 4);
+    const size_t ntri = s.bosonic ? (size_t)s.N * (s.N + 1) / 2 : 1;
+    if (e == cudaSuccess) e = alloc(&s.Vh, (size_t)s.N + 1);
+    if (e == cudaSuccess) e = alloc(&s.Vbh, (size_t)s.N + 1);
+    if (e == cudaSuccess) e = alloc(&s.yf, (size_t)s.N + 1);
+    if (e == cudaSuccess) e = alloc(&s.yb, (size_t)s.N + 1);
+    if (e == cudaSuccess) e = alloc(&s.Wf, ntri);
+    if (e == cudaSuccess) e = alloc(&s.Wb, ntri);
+    if (e == cudaSuccess) e = alloc(&s.rowR, (size_t)s.N);
+    if (e == cudaSuccess) e = alloc(&s.rowC, (size_t)s.N);
+    // Newton's-third-law pair tiles need P * ceil(N/32) * D * ld partial sums;
+    // beyond 512 MiB the all-pairs kernel (no partials) is used instead.
+    const size_t npart = pair_partial_doubles(s, h->D);
+    if (e == cudaSuccess && npart * sizeof(double) <= (512ull << 20)) e = alloc(&h->d_part, npart);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s.xflags, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(s.xflags, 0, 4 * sizeof(int));
     if (e == cudaSuccess) e = alloc(&h->d_red[0], (size_t)3 * nred);
     if (e == cudaSuccess) e = alloc(&h->d_red[1], (size_t)3 * nred);
     if (e == cudaSuccess) e = alloc(&h->d_stage, (size_t)s.P * s.N * h->D);
@@ -391,10 +412,18 @@ static void enqueue_forces(pimdb_handle* h) {
     const bool nm = h->cfg.propagator == PIMDB_PROP_NORMAL_MODES;
     if (s.bosonic) {
         launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
-        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, h->stream); });
+        const int ex = h->opt_exact_exchange;
+        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 3);
     }
-    launch(h, PIMDB_K_BEAD_FORCES,
-           [&] { launch_bead_forces(s, h->D, h->cfg.precision == PIMDB_MIXED, nm ? 1 : 0, h->stream); });
+    const int mixed = h->cfg.precision == PIMDB_MIXED;
+    if (h->d_part && h->opt_newton3) {
+        const bool pairs = s.int_kind != PIMDB_POT_FREE && s.cutoff != 0.0;
+        launch(
+            h, PIMDB_K_BEAD_FORCES,
+            [&] { launch_pair_tiles_and_finish(s, h->D, mixed, nm ? 1 : 0, h->d_part, h->stream); }, pairs ? 2 : 1);
+    } else {
+        launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_bead_forces(s, h->D, mixed, nm ? 1 : 0, h->stream); });
+    }
     if (s.bosonic) launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 1, h->stream); });
 }
 
@@ -521,7 +550,8 @@ extern "C" int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first,
     const Sys& s = h->s;
     if (!s.bosonic) return fail(h, PIMDB_ERR_CONFIG, "pimdb_exchange needs a bosonic configuration with nbeads > 1");
     launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
-    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, h->stream); });
+    const int ex = h->opt_exact_exchange;
+    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 3);
     launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 0, h->stream); });
     launch(h, PIMDB_K_EXCH_ESTIMATORS, [&] { launch_exchange_estimators(s, h->stream); });
     CUDA_TRY(h, cudaGetLastError());
@@ -610,5 +640,14 @@ extern "C" int pimdb_measure_fp64_peak(double* tflops) {
     CUDA_TRY(nullptr, cudaGetLastError());
     const double flops = 2.0 * 8.0 * iters * (double)threads * blocks * reps;
     *tflops = flops / (ms * 1e-3) / 1e12;
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
+    if (!h || !name) return PIMDB_ERR_ARG;
+    const std::string n(name);
+    if (n == "exact_exchange") h->opt_exact_exchange = value ? 1 : 0;
+    else if (n == "newton3") h->opt_newton3 = value ? 1 : 0;
+    else return fail(h, PIMDB_ERR_ARG, "unknown option " + n);
     return PIMDB_OK;
 }

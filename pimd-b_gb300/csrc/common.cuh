@@ -60,6 +60,16 @@ struct Sys {
     double* scal;   // exchange scalars: V_B, prim, P_distinct, P_longest
     double* red;    // reduction partials
     int* err;       // error word
+    // exchange work arrays
+    double* Vh;     // FP32-accurate estimate of V (stored as double), N+1
+    double* Vbh;    // estimate of V_backwards, N+1
+    double* yf;     // y_m = exp(-beta (V_m - Vh_m)), N+1
+    double* yb;     // y_l = exp(-beta (Vb_l - Vbh_l)), N+1
+    double* Wf;     // forward weights, packed like E
+    double* Wb;     // backward weights, packed like E
+    double* rowR;   // per-row factors exp(-beta (Vh[l+1] + Vb[l+1] - V[N])), N
+    double* rowC;   // cut probabilities exp(-beta (V[l+1] + Vb[l+1] - V[N])), N
+    int* xflags;    // [0] forward used the exact fallback, [1] backward, [2] completion counter
 };
 
 template <int D>

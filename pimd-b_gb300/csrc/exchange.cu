@@ -1,21 +1,39 @@
 // Feldman-Hirshberg bosonic exchange on the first and last beads.
 //
 // Reference: BosonicExchange (src/bosonic_exchange/quadratic_bosonic_exchange.cpp)
-//   evaluateCycleEnergies :34-61   -> k_exch_energies
-//   evaluateVBn :73-99             -> k_exch_recursions (block 0)
-//   evaluateVBackwards :101-128    -> k_exch_recursions (block 1)
-//   evaluateConnectionProbabilities :142-157 and
+//   evaluateCycleEnergies :34-61            -> k_exch_energies
+//   evaluateVBn :73-99, evaluateVBackwards :101-128
+//                                           -> k_exch_estimate + k_exch_weights + k_exch_solve
+//   evaluateConnectionProbabilities :142-157,
 //   springForceLastBead / springForceFirstBead :159-215
-//                                  -> k_exch_forces (probabilities are formed
-//                                     on the fly; the N x N matrix is never stored)
+//                                           -> k_exch_forces (probabilities formed on the fly)
 //   primEstimator :250-279, getDistinctProbability :222-229,
-//   getLongestProbability :238-240 -> k_exch_estimators
-// Everything is FP64.
+//   getLongestProbability :238-240          -> k_exch_estimators
 //
-// Cycle energies are stored packed by row: E(m, k) of the reference (the
-// cycle of particles m-k+1..m, 1-based) lives at row v = m-1, column
-// u = m-k, offset v(v+1)/2 + u.  Row v is contiguous, which is what the
-// forward recursion reads at level m = v+1.
+// Cycle energies are stored packed by row: the reference's E(m, k) (cycle of
+// particles m-k+1..m, 1-based) lives at row v = m-1, column u = m-k, offset
+// v(v+1)/2 + u, which is exactly the reference's E_kn[m(m+1)/2 - k].
+//
+// How the recursions are evaluated.  The reference's forward recursion
+//   V[m] = -1/beta log( 1/m sum_{u<m} exp(-beta (E[m-1][u] + V[u])) )
+// is sequential in m and costs one FP64 exponential per term, which on one
+// streaming multiprocessor is far too slow (GB300 runs FP64 at 1/64 of FP32).
+// It is evaluated in three passes with the same result in FP64:
+//   1. k_exch_estimate: the recursion in FP32 (hardware exp2), one block,
+//      one barrier per level ("wavefront": when V[j] is final every later
+//      level adds its term u = j to a running log-sum-exp).  Gives Vh.
+//   2. k_exch_weights: every FP64 exponential at once, spread over the GPU:
+//      Wf[m-1][u] = exp(-beta (E[m-1][u] + Vh[u] - Vh[m])) / m.
+//   3. k_exch_solve: y_0 = 1, y_m = sum_u Wf[m-1][u] y_u (an FP64 triangular
+//      solve, multiply-adds only) and V[m] = Vh[m] - log(y_m)/beta exactly.
+// Because Vh is within FP32 accuracy of V, every y stays near 1, no term
+// over- or underflows and the FP64 result carries the reference's precision.
+// If the estimate is ever off by more than 200 kT (not expected; e.g. for
+// non-finite input), the solve kernel recomputes the level-by-level FP64
+// log-sum-exp in the reference's own order instead.  The backward recursion
+// is handled the same way by the second block of each kernel.
+#include <math_constants.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -67,60 +85,267 @@ __global__ void k_exch_energies(Sys s) {
     }
 }
 
-// Block 0: forward recursion V[m] (:73-99).  Block 1: backward recursion
-// V_backwards[l] (:101-128).  Each level is a block-wide log-sum-exp with
-// the reference's minimum shift.
-__global__ void k_exch_recursions(Sys s) {
-    extern __shared__ double sh[];
-    double* Vs = sh;              // N+1
-    double* red = sh + s.N + 1;   // 32
-    const int N = s.N;
-    const double beta = s.beta_ex;
-    const int tid = threadIdx.x, bd = blockDim.x;
-    if (blockIdx.x == 0) {
-        if (tid == 0) Vs[0] = 0.0;
-        __syncthreads();
-        for (int m = 1; m <= N; ++m) {
-            const double* row = s.E + tri(m - 1);
-            double lmin = 1.79769313486231570815e308;
-            for (int u = tid; u < m; u += bd) lmin = fmin(lmin, row[u] + Vs[u]);
-            const double shift = block_min(lmin, red);
-            double ls = 0.0;
-            for (int u = tid; u < m; u += bd) ls += exp(-beta * (row[u] + Vs[u] - shift));
-            const double tot = block_sum(ls, red);
-            if (tid == 0) {
-                const double v = shift - (1.0 / beta) * log(tot / (double)m);
-                Vs[m] = v;
-                if (!isfinite(v)) atomicOr(s.err, ERRB_NONFINITE_VB);
-            }
-            __syncthreads();
-        }
-        for (int m = tid; m <= N; m += bd) s.V[m] = Vs[m];
+__device__ __forceinline__ void lse_add(float& mx, float& sm, float t) {
+    if (t > mx) {
+        sm = sm * __expf(mx - t) + 1.0f;
+        mx = t;
     } else {
-        if (tid == 0) Vs[N] = 0.0;
+        sm += __expf(t - mx);
+    }
+}
+
+// Pass 1: FP32 estimates.  Thread tid owns levels tid+1+k*blockDim (k < K).
+template <int K>
+__global__ void __launch_bounds__(1024) k_exch_estimate(Sys s) {
+    extern __shared__ float vs[];  // N+1
+    const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
+    const float beta = (float)s.beta_ex;
+    float mx[K], sm[K], en[K];
+    int lv[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        lv[k] = tid + 1 + k * bd;
+        mx[k] = -CUDART_INF_F;
+        sm[k] = 0.0f;
+        en[k] = 0.0f;
+    }
+    if (blockIdx.x == 0) {
+        // forward: level m has terms u = 0..m-1 with E[m-1][u] + V[u]
+        if (tid == 0) vs[0] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (lv[k] <= N) en[k] = (float)s.E[tri(lv[k] - 1)];
         __syncthreads();
-        for (int l = N - 1; l > 0; --l) {
-            double lmin = 1.79769313486231570815e308;
-            for (int p = l + tid; p < N; p += bd) lmin = fmin(lmin, s.E[tri(p) + l] + Vs[p + 1]);
-            const double shift = block_min(lmin, red);
-            double ls = 0.0;
-            for (int p = l + tid; p < N; p += bd) ls += exp(-beta * (s.E[tri(p) + l] + Vs[p + 1] - shift)) / (p + 1);
-            const double tot = block_sum(ls, red);
-            if (tid == 0) {
-                const double v = shift - log(tot) / beta;
-                Vs[l] = v;
-                if (!isfinite(v)) atomicOr(s.err, ERRB_NONFINITE_VB);
+        for (int j = 0; j < N; ++j) {
+            float ec[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                ec[k] = en[k];
+                if (lv[k] <= N && lv[k] > j + 1) en[k] = (float)s.E[tri(lv[k] - 1) + j + 1];
+            }
+            const float vj = vs[j];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (lv[k] <= N && lv[k] > j) {
+                    lse_add(mx[k], sm[k], -beta * (ec[k] + vj));
+                    if (lv[k] == j + 1) vs[j + 1] = -(mx[k] + __logf(sm[k]) - __logf((float)lv[k])) / beta;
+                }
             }
             __syncthreads();
         }
-        for (int l = tid + 1; l <= N; l += bd) s.Vb[l] = Vs[l];
+        for (int m = tid; m <= N; m += bd) s.Vh[m] = (double)vs[m];
+    } else {
+        // backward: level l (1..N-1) has terms p = l..N-1 with E[p][l] + Vb[p+1] and weight 1/(p+1)
+        if (tid == 0) vs[N] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (lv[k] <= N - 1) en[k] = (float)s.E[tri(N - 1) + lv[k]];
+        __syncthreads();
+        for (int j = N; j >= 2; --j) {
+            const int p = j - 1;
+            float ec[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                ec[k] = en[k];
+                if (lv[k] <= p - 1) en[k] = (float)s.E[tri(p - 1) + lv[k]];
+            }
+            const float vj = vs[j];
+            const float lj = __logf((float)j);
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (lv[k] <= p) {
+                    lse_add(mx[k], sm[k], -beta * (ec[k] + vj) - lj);
+                    if (lv[k] == p) vs[p] = -(mx[k] + __logf(sm[k])) / beta;
+                }
+            }
+            __syncthreads();
+        }
+        for (int l = tid; l <= N; l += bd) s.Vbh[l] = (l >= 1) ? (double)vs[l] : 0.0;
+    }
+}
+
+// Pass 2: every FP64 exponential, one thread per packed entry (row p, column u).
+__global__ void k_exch_weights(Sys s) {
+    const int p = blockIdx.y;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u > p) return;
+    const double beta = s.beta_ex;
+    const size_t e = tri(p) + u;
+    const double E = s.E[e];
+    const double inv = 1.0 / (p + 1);
+    s.Wf[e] = exp(-beta * (E + s.Vh[u] - s.Vh[p + 1])) * inv;
+    s.Wb[e] = u >= 1 ? exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u])) * inv : 0.0;
+}
+
+// Exact level-by-level FP64 log-sum-exp in the reference's order (used only
+// when the estimate is unusable).  `vs` holds N+1 doubles, `red` 32.
+__device__ void exact_forward(const Sys& s, double* vs, double* red) {
+    const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
+    const double beta = s.beta_ex;
+    if (tid == 0) vs[0] = 0.0;
+    __syncthreads();
+    for (int m = 1; m <= N; ++m) {
+        const double* row = s.E + tri(m - 1);
+        double lmin = 1.79769313486231570815e308;
+        for (int u = tid; u < m; u += bd) lmin = fmin(lmin, row[u] + vs[u]);
+        const double shift = block_min(lmin, red);
+        double ls = 0.0;
+        for (int u = tid; u < m; u += bd) ls += exp(-beta * (row[u] + vs[u] - shift));
+        const double tot = block_sum(ls, red);
+        if (tid == 0) vs[m] = shift - (1.0 / beta) * log(tot / (double)m);
+        __syncthreads();
+    }
+}
+
+__device__ void exact_backward(const Sys& s, double* vs, double* red) {
+    const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
+    const double beta = s.beta_ex;
+    if (tid == 0) vs[N] = 0.0;
+    __syncthreads();
+    for (int l = N - 1; l > 0; --l) {
+        double lmin = 1.79769313486231570815e308;
+        for (int p = l + tid; p < N; p += bd) lmin = fmin(lmin, s.E[tri(p) + l] + vs[p + 1]);
+        const double shift = block_min(lmin, red);
+        double ls = 0.0;
+        for (int p = l + tid; p < N; p += bd) ls += exp(-beta * (s.E[tri(p) + l] + vs[p + 1] - shift)) / (p + 1);
+        const double tot = block_sum(ls, red);
+        if (tid == 0) vs[l] = shift - log(tot) / beta;
+        __syncthreads();
+    }
+}
+
+// Pass 3: y solves, exact V / V_backwards, and (by the block that finishes
+// last) the per-row factors of the connection probabilities.
+template <int K>
+__global__ void __launch_bounds__(1024) k_exch_solve(Sys s, int force_exact) {
+    extern __shared__ double ys[];  // N+1, then 32 for reductions
+    double* red = ys + s.N + 1;
+    __shared__ int last_block;
+    const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
+    const double beta = s.beta_ex;
+    double acc[K], wn[K];
+    int lv[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        lv[k] = tid + 1 + k * bd;
+        acc[k] = 0.0;
+        wn[k] = 0.0;
+    }
+    int bad = force_exact;
+    if (blockIdx.x == 0) {
+        if (tid == 0) ys[0] = 1.0;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (lv[k] <= N && !force_exact) wn[k] = s.Wf[tri(lv[k] - 1)];
+        __syncthreads();
+        for (int j = 0; j < (force_exact ? 0 : N); ++j) {
+            double wc[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                wc[k] = wn[k];
+                if (lv[k] <= N && lv[k] > j + 1) wn[k] = s.Wf[tri(lv[k] - 1) + j + 1];
+            }
+            const double yj = ys[j];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (lv[k] <= N && lv[k] > j) {
+                    acc[k] = fma(wc[k], yj, acc[k]);
+                    if (lv[k] == j + 1) ys[j + 1] = acc[k];
+                }
+            }
+            __syncthreads();
+        }
+        for (int m = tid; m <= N && !force_exact; m += bd) {
+            const double y = ys[m];
+            const double ly = log(y);
+            if (!(y > 0.0) || !(fabs(ly) < 200.0)) bad = 1;
+            s.yf[m] = y;
+            s.V[m] = s.Vh[m] - ly / beta;
+        }
+        bad = __syncthreads_or(bad);
+        if (bad) {
+            exact_forward(s, ys, red);
+            for (int m = tid; m <= N; m += bd) s.V[m] = ys[m];
+        }
+        if (tid == 0) s.xflags[0] = bad;
+        __syncthreads();
+        for (int m = tid; m <= N; m += bd)
+            if (!isfinite(s.V[m])) atomicOr(s.err, ERRB_NONFINITE_VB);
+    } else {
+        if (tid == 0) ys[N] = 1.0;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (lv[k] <= N - 1 && !force_exact) wn[k] = s.Wb[tri(N - 1) + lv[k]];
+        __syncthreads();
+        for (int j = N; j >= (force_exact ? N + 1 : 2); --j) {
+            const int p = j - 1;
+            double wc[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                wc[k] = wn[k];
+                if (lv[k] <= p - 1) wn[k] = s.Wb[tri(p - 1) + lv[k]];
+            }
+            const double yj = ys[j];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (lv[k] <= p) {
+                    acc[k] = fma(wc[k], yj, acc[k]);
+                    if (lv[k] == p) ys[p] = acc[k];
+                }
+            }
+            __syncthreads();
+        }
+        for (int l = tid + 1; l <= N; l += bd) {
+            if (l == N) {
+                s.Vb[N] = 0.0;
+                s.yb[N] = 1.0;
+                continue;
+            }
+            if (force_exact) continue;
+            const double y = ys[l];
+            const double ly = log(y);
+            if (!(y > 0.0) || !(fabs(ly) < 200.0)) bad = 1;
+            s.yb[l] = y;
+            s.Vb[l] = s.Vbh[l] - ly / beta;
+        }
+        bad = __syncthreads_or(bad);
+        if (bad) {
+            exact_backward(s, ys, red);
+            for (int l = tid + 1; l <= N; l += bd) s.Vb[l] = ys[l];
+        }
+        if (tid == 0) s.xflags[1] = bad;
+        __syncthreads();
+        for (int l = tid + 1; l <= N; l += bd)
+            if (!isfinite(s.Vb[l])) atomicOr(s.err, ERRB_NONFINITE_VB);
+    }
+    // The block that finishes second computes the per-row factors, which need
+    // both V and V_backwards (threadFenceReduction pattern; no waiting).
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last_block = (atomicAdd(&s.xflags[2], 1) == 1);
+    __syncthreads();
+    if (!last_block) return;
+    __threadfence();
+    const double VN = ((volatile double*)s.V)[N];
+    for (int l = tid; l < N; l += bd) {
+        const double vbl = ((volatile double*)s.Vb)[l + 1];
+        const double vl = ((volatile double*)s.V)[l + 1];
+        s.rowR[l] = exp(-beta * (s.Vh[l + 1] + vbl - VN));
+        s.rowC[l] = exp(-beta * (vl + vbl - VN));
+    }
+    if (tid == 0) {
+        s.xflags[2] = 0;
+        s.Vb[0] = VN;  // V_backwards[0] = V[N] (:127)
+        s.scal[0] = VN;
     }
 }
 
 // Exterior spring forces (:159-215).  Warps [0, N) handle bead P (row l of
 // the connection-probability matrix), warps [N, 2N) bead 1 (column l).
-// f on those beads already holds the physical forces; the spring part is
-// added (simulation.cpp:363-373) and also kept in fx.
+// Probabilities: close-cycle P[l][u] = Wf[l][u] y_u R_l (u <= l), direct
+// link P[l][l+1] = 1 - C_l; with the exact fallback they are evaluated
+// from their defining exponentials.  When `accumulate`, the spring force is
+// added to f (which holds the physical forces; simulation.cpp:363-373).
 template <int D>
 __global__ void k_exch_forces(Sys s, int accumulate) {
     const int lane = threadIdx.x & 31;
@@ -129,6 +354,7 @@ __global__ void k_exch_forces(Sys s, int accumulate) {
     if (w >= 2 * N) return;
     const double beta = s.beta_ex;
     const double VN = s.V[N];
+    const bool exact = s.xflags[0] != 0;
     const int first = 0, last = s.P - 1;
     double sum[D];
 #pragma unroll
@@ -138,16 +364,23 @@ __global__ void k_exch_forces(Sys s, int accumulate) {
         l = w;
         bead = last;
         nb = (s.P - 2 + s.P) % s.P;
-        const double vbl = s.Vb[l + 1];
         const size_t r = tri(l);
+        const double Rl = s.rowR[l];
+        const double vbl = s.Vb[l + 1];
         const int nmax = min(l + 1, N - 1);
+        double xl[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) xl[a] = s.x[idx<D>(s, last, a, l)];
         for (int n = lane; n <= nmax; n += 32) {
             double pr;
-            if (n <= l) pr = exp(-beta * (s.V[n] + s.E[r + n] + vbl - VN)) / (l + 1);
-            else pr = 1.0 - exp(-beta * (s.V[l + 1] + vbl - VN));
+            if (n <= l) {
+                pr = exact ? exp(-beta * (s.V[n] + s.E[r + n] + vbl - VN)) / (l + 1) : s.Wf[r + n] * s.yf[n] * Rl;
+            } else {
+                pr = 1.0 - s.rowC[l];
+            }
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                double d = s.x[idx<D>(s, first, a, n)] - s.x[idx<D>(s, last, a, l)];
+                double d = s.x[idx<D>(s, first, a, n)] - xl[a];
                 if (s.pbc) d = min_image(d, s.L, s.invL);
                 sum[a] += pr * d;
             }
@@ -156,13 +389,22 @@ __global__ void k_exch_forces(Sys s, int accumulate) {
         l = w - N;
         bead = first;
         nb = 1 % s.P;
+        const double yl = s.yf[l];
+        const double vl = s.V[l];
+        double xl[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) xl[a] = s.x[idx<D>(s, first, a, l)];
         for (int q = max(0, l - 1) + lane; q < N; q += 32) {
             double pr;
-            if (q >= l) pr = exp(-beta * (s.V[l] + s.E[tri(q) + l] + s.Vb[q + 1] - VN)) / (q + 1);
-            else pr = 1.0 - exp(-beta * (s.V[q + 1] + s.Vb[q + 1] - VN));
+            if (q >= l) {
+                pr = exact ? exp(-beta * (vl + s.E[tri(q) + l] + s.Vb[q + 1] - VN)) / (q + 1)
+                           : s.Wf[tri(q) + l] * yl * s.rowR[q];
+            } else {
+                pr = 1.0 - s.rowC[q];
+            }
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                double d = s.x[idx<D>(s, last, a, q)] - s.x[idx<D>(s, first, a, l)];
+                double d = s.x[idx<D>(s, last, a, q)] - xl[a];
                 if (s.pbc) d = min_image(d, s.L, s.invL);
                 sum[a] += pr * d;
             }
@@ -184,14 +426,10 @@ __global__ void k_exch_forces(Sys s, int accumulate) {
             }
         }
     }
-    if (w == 0 && lane == 0) {
-        s.Vb[0] = VN;
-        s.scal[0] = VN;
-    }
 }
 
 // primEstimator (:250-279), getDistinctProbability (:222-229) and
-// getLongestProbability (:238-240); one block.
+// getLongestProbability (:238-240); one block, evaluated on request.
 __global__ void k_exch_estimators(Sys s, int nbeads) {
     extern __shared__ double sh[];
     double* G = sh;             // N+1
@@ -223,11 +461,9 @@ __global__ void k_exch_estimators(Sys s, int nbeads) {
     }
 }
 
-static int recursion_threads(int N) {
+static int wave_threads(int N) {
     int t = ((N + 31) / 32) * 32;
-    if (t > 512) t = 512;
-    if (t < 32) t = 32;
-    return t;
+    return t > 1024 ? 1024 : (t < 32 ? 32 : t);
 }
 
 void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
@@ -238,9 +474,30 @@ void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
     else k_exch_energies<3><<<grid, warps * 32, 0, st>>>(s);
 }
 
-void launch_exchange_recursions(const Sys& s, cudaStream_t st) {
+template <int K>
+static int recursions_k(const Sys& s, int threads, int exact, cudaStream_t st) {
+    if (!exact) {
+        const size_t esmem = sizeof(float) * (size_t)(s.N + 1);
+        if (esmem > 48 * 1024)
+            cudaFuncSetAttribute(k_exch_estimate<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
+        k_exch_estimate<K><<<2, threads, esmem, st>>>(s);
+        dim3 wgrid((s.N + 255) / 256, s.N);
+        k_exch_weights<<<wgrid, 256, 0, st>>>(s);
+    }
     const size_t smem = sizeof(double) * (size_t)(s.N + 1 + 32);
-    k_exch_recursions<<<2, recursion_threads(s.N), smem, st>>>(s);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_exch_solve<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_exch_solve<K><<<2, threads, smem, st>>>(s, exact);
+    return exact ? 1 : 3;
+}
+
+int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st) {
+    const int threads = wave_threads(s.N);
+    const int per = (s.N + threads - 1) / threads;
+    if (per <= 1) return recursions_k<1>(s, threads, exact, st);
+    if (per <= 2) return recursions_k<2>(s, threads, exact, st);
+    if (per <= 4) return recursions_k<4>(s, threads, exact, st);
+    if (per <= 8) return recursions_k<8>(s, threads, exact, st);
+    return recursions_k<16>(s, threads, exact, st);
 }
 
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st) {
@@ -253,7 +510,10 @@ void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream
 
 void launch_exchange_estimators(const Sys& s, cudaStream_t st) {
     const size_t smem = sizeof(double) * (size_t)(s.N + 1 + 32);
-    k_exch_estimators<<<1, recursion_threads(s.N), smem, st>>>(s, s.P);
+    int t = ((s.N + 31) / 32) * 32;
+    t = t > 512 ? 512 : (t < 32 ? 32 : t);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_exch_estimators, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_exch_estimators<<<1, t, smem, st>>>(s, s.P);
 }
 
 }  // namespace pimdb

@@ -206,6 +206,202 @@ __global__ void __launch_bounds__(kPairThreads) k_bead_forces(Sys s, int write_p
     }
 }
 
+// ---------------------------------------------------------------------------
+// Newton's-third-law pair forces.  The N x N pair matrix of one bead is cut
+// into 32 x 32 tiles; one warp owns one tile (it, jt) with jt >= it.  Lane t
+// holds particle i = 32 it + t and, rotating one lane per step, every j of
+// tile jt together with j's force accumulator, so each unordered pair is
+// evaluated once and no atomics are needed.  The warp writes its two partial
+// sums into part[b][slot][axis][particle], slot = the other tile's index;
+// every (particle, slot) is written exactly once, and k_bead_finish adds the
+// slots in ascending order (deterministic).
+constexpr int kTile = 32;
+
+template <typename R, int D>
+struct PairPos {
+    R h[D], l[D];  // value = h + l (for R = double, l = 0)
+};
+
+template <typename R, int D>
+__device__ __forceinline__ PairPos<R, D> split_pos(const double* x) {
+    PairPos<R, D> q;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        q.h[a] = (R)x[a];
+        q.l[a] = (R)(x[a] - (double)q.h[a]);
+    }
+    return q;
+}
+
+template <int D, typename R>
+__device__ __forceinline__ bool pair_force(const Sys& s, const PairPos<R, D>& pi, const PairPos<R, D>& pj,
+                                           R* g) {
+    R r[D];
+    R r2 = (R)0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        R d;
+        if constexpr (sizeof(R) == 8) {
+            d = pi.h[a] - pj.h[a];
+            if (s.pbc) d = min_image(d, s.L, s.invL);
+        } else {
+            d = (pi.h[a] - pj.h[a]) + (pi.l[a] - pj.l[a]);
+            if (s.pbc) d = min_image_f(d, (float)s.L, (float)s.invL);
+        }
+        r[a] = d;
+        r2 += d * d;
+    }
+    const double cut = s.cutoff;
+    bool in;
+    if (cut < 0.0) in = true;
+    else if constexpr (sizeof(R) == 8) in = sqrt((double)r2) < cut;
+    else in = r2 < (float)(cut * cut);
+    if (!in) return false;
+    const R sc = pair_scale<R>(s.int_kind, r2, (R)s.int_a);
+#pragma unroll
+    for (int a = 0; a < D; ++a) g[a] = sc * r[a];  // grad V(r_i - r_j)
+    return true;
+}
+
+template <typename R, int D>
+__device__ __forceinline__ void rotate(PairPos<R, D>& q, R* acc, int& jidx, int lane) {
+    const int src = (lane + 1) & 31;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        q.h[a] = __shfl_sync(0xffffffffu, q.h[a], src);
+        if constexpr (sizeof(R) == 4) q.l[a] = __shfl_sync(0xffffffffu, q.l[a], src);
+        acc[a] = __shfl_sync(0xffffffffu, acc[a], src);
+    }
+    jidx = __shfl_sync(0xffffffffu, jidx, src);
+}
+
+template <int D, typename R>
+__global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ part, int T, int npairs) {
+    const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.y;
+    if (w >= npairs) return;
+    // tile pair (it, jt), jt >= it, row-major over the upper triangle
+    int it = (int)((2.0 * T + 1.0 - sqrt((2.0 * T + 1.0) * (2.0 * T + 1.0) - 8.0 * w)) * 0.5);
+    while (it > 0 && it * T - it * (it - 1) / 2 > w) --it;
+    while ((it + 1) * T - (it + 1) * it / 2 <= w) ++it;
+    const int jt = it + (w - (it * T - it * (it - 1) / 2));
+    const bool diag = it == jt;
+
+    const int i = it * kTile + lane;
+    int jidx = jt * kTile + lane;
+    double xi[D], xj[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        xi[a] = i < s.N ? s.x[idx<D>(s, b, a, i)] : 0.0;
+        xj[a] = jidx < s.N ? s.x[idx<D>(s, b, a, jidx)] : 0.0;
+    }
+    const PairPos<R, D> pi = split_pos<R, D>(xi);
+    PairPos<R, D> pj = split_pos<R, D>(xj);
+    R ai[D], aj[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) ai[a] = aj[a] = (R)0;
+    int rot = 0;
+    const int first = diag ? 1 : 0, lastS = diag ? 16 : 31;
+    if (diag) {
+        rotate<R, D>(pj, aj, jidx, lane);
+        ++rot;
+    }
+    for (int st = first; st <= lastS; ++st) {
+        const bool act = i < s.N && jidx < s.N && (!diag || st < 16 || lane < 16);
+        if (act) {
+            R g[D];
+            if (pair_force<D, R>(s, pi, pj, g)) {
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    ai[a] -= g[a];
+                    aj[a] += g[a];
+                }
+            }
+        }
+        rotate<R, D>(pj, aj, jidx, lane);
+        ++rot;
+    }
+    while (rot & 31) {  // bring every j accumulator back to its home lane
+        rotate<R, D>(pj, aj, jidx, lane);
+        ++rot;
+    }
+    const size_t base_b = (size_t)b * T;
+    if (diag) {
+        if (i < s.N) {
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+                part[((base_b + it) * D + a) * s.ld + i] = (double)ai[a] + (double)aj[a];
+        }
+    } else {
+        if (i < s.N) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) part[((base_b + jt) * D + a) * s.ld + i] = (double)ai[a];
+        }
+        if (jidx < s.N) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) part[((base_b + it) * D + a) * s.ld + jidx] = (double)aj[a];
+        }
+    }
+}
+
+// f = springs + (-grad V_ext + sum of the pair slots), one thread per
+// (bead, axis, particle).  T = 0 when there are no pair forces.
+template <int D>
+__global__ void k_bead_finish(Sys s, const double* __restrict__ part, int T, int write_phys) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int i = (int)(e % s.ld);
+    const size_t ba = e / s.ld;
+    if (ba >= (size_t)s.P * D || i >= s.N) return;
+    const int a = (int)(ba % D), b = (int)(ba / D);
+    double xi[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) xi[c] = s.x[idx<D>(s, b, c, i)];
+    double fe[D];
+    ext_force<D>(s, xi, fe);
+    double acc = fe[a];
+    for (int q = 0; q < T; ++q) acc += part[(((size_t)b * T + q) * D + a) * s.ld + i];
+    const size_t o = idx<D>(s, b, a, i);
+    if (write_phys) s.fphys[o] = acc;
+    if (s.bosonic && (b == 0 || b == s.P - 1)) {
+        s.f[o] = acc;
+    } else {
+        const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
+        double dp = s.x[idx<D>(s, bp, a, i)] - xi[a];
+        double dn = s.x[idx<D>(s, bn, a, i)] - xi[a];
+        if (s.pbc) {
+            dp = min_image(dp, s.L, s.invL);
+            dn = min_image(dn, s.L, s.invL);
+        }
+        s.f[o] = s.kappa * (dp + dn) + acc;
+    }
+}
+
+size_t pair_partial_doubles(const Sys& s, int D) {
+    const int T = (s.N + kTile - 1) / kTile;
+    return (size_t)s.P * T * D * s.ld;
+}
+
+template <int D>
+static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, cudaStream_t st) {
+    const bool pairs = s.int_kind != POT_FREE && s.cutoff != 0.0;
+    const int T = pairs ? (s.N + kTile - 1) / kTile : 0;
+    if (pairs) {
+        const int np = T * (T + 1) / 2;
+        dim3 grid((np + 3) / 4, s.P);
+        if (mixed) k_pair_tiles<D, float><<<grid, 128, 0, st>>>(s, part, T, np);
+        else k_pair_tiles<D, double><<<grid, 128, 0, st>>>(s, part, T, np);
+    }
+    const size_t n = (size_t)s.P * D * s.ld;
+    k_bead_finish<D><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, part, T, write_phys);
+}
+
+void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part, cudaStream_t st) {
+    if (D == 1) tiles_launch<1>(s, mixed, write_phys, part, st);
+    else if (D == 2) tiles_launch<2>(s, mixed, write_phys, part, st);
+    else tiles_launch<3>(s, mixed, write_phys, part, st);
+}
+
 template <int D>
 void launch_bead_forces(const Sys& s, int mixed, int write_phys, cudaStream_t st) {
     dim3 grid((s.N + kPairThreads - 1) / kPairThreads, s.P);

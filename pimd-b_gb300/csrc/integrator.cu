@@ -117,11 +117,13 @@ __global__ void k_cart_update(Sys s, int flags, const double* __restrict__ red_i
     if (flags & SF_COM_PARTIAL) com_write_partials<D>(part, red_out, shred);
 }
 
-constexpr int kNmTile = 32;   // particles per block (one per lane)
-constexpr int kNmThreads = 256;
+constexpr int kNmTile = 8;      // particles per block
+constexpr int kNmThreads = 256; // 4 particle pairs x 64 mode groups
 
 // Langevin O-step on the normal modes: p_nm = C p, p_nm <- c1 p_nm + c2 xi,
-// p = C^T p_nm.  One block per (particle tile, axis).
+// p = C^T p_nm.  One block per (8-particle tile, axis); thread (pair pp,
+// group g) handles particles 2pp, 2pp+1 of the tile for modes g, g+64, ...
+// and then for beads g, g+64, ...
 template <int D>
 __global__ void __launch_bounds__(kNmThreads) k_nm_thermo(Sys s, const double* __restrict__ C,
                                                           const double* __restrict__ T, int flags,
@@ -131,43 +133,59 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_thermo(Sys s, const double* _
     extern __shared__ double sm[];
     __shared__ double shred[32];
     const int P = s.P;
-    double* sp = sm;                 // [P][32]
-    double* sq = sm + P * kNmTile;   // [P][32]
+    double* sp = sm;                 // [P][8]
+    double* sq = sm + P * kNmTile;   // [P][8]
     const int a = blockIdx.y;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int i = blockIdx.x * kNmTile + lane;
-    const bool act = i < s.N;
+    const int i0 = blockIdx.x * kNmTile;
+    const int pp = threadIdx.x & 3, g = threadIdx.x >> 2;
     double cm[3] = {0.0, 0.0, 0.0};
     if (flags & SF_COM_APPLY) com_from_partials<D>(s, red_in, nred_in, cm, shred);
-    for (int b = w; b < P; b += nw) sp[b * kNmTile + lane] = act ? s.p[idx<D>(s, b, a, i)] - cm[a] : 0.0;
-    __syncthreads();
-    const int half = (s.N + 1) / 2;
-    for (int k = w; k < P; k += nw) {
-        double q = 0.0;
-        for (int b = 0; b < P; ++b) q += C[k * P + b] * sp[b * kNmTile + lane];
-        const double2 z = philox_normal_pair(s.seed, s.replica, 2ull * (unsigned long long)step + substep,
-                                             (uint32_t)((size_t)(k * D + a) * half + (i >> 1)));
-        sq[k * kNmTile + lane] = s.c1 * q + s.c2 * ((i & 1) ? z.y : z.x);
+    for (int e = threadIdx.x; e < P * kNmTile; e += blockDim.x) {
+        const int b = e / kNmTile, il = e % kNmTile, i = i0 + il;
+        sp[e] = i < s.N ? s.p[idx<D>(s, b, a, i)] - cm[a] : 0.0;
     }
     __syncthreads();
-    double part[3] = {0.0, 0.0, 0.0};
-    for (int j = w; j < P; j += nw) {
-        double v = 0.0;
-        for (int k = 0; k < P; ++k) v += T[j * P + k] * sq[k * kNmTile + lane];
-        if (act) {
-            s.p[idx<D>(s, j, a, i)] = v;
-            part[a] += v;
+    const int half = (s.N + 1) / 2;
+    const uint64_t t = 2ull * (unsigned long long)step + substep;
+    for (int k = g; k < P; k += 64) {
+        double q0 = 0.0, q1 = 0.0;
+        const double* ck = C + (size_t)k * P;
+        for (int b = 0; b < P; ++b) {
+            const double c = ck[b];
+            q0 += c * sp[b * kNmTile + 2 * pp];
+            q1 += c * sp[b * kNmTile + 2 * pp + 1];
+        }
+        const int ie = i0 + 2 * pp;
+        const double2 z = philox_normal_pair(s.seed, s.replica, t, (uint32_t)((size_t)(k * D + a) * half + (ie >> 1)));
+        sq[k * kNmTile + 2 * pp] = s.c1 * q0 + s.c2 * z.x;
+        sq[k * kNmTile + 2 * pp + 1] = s.c1 * q1 + s.c2 * z.y;
+    }
+    __syncthreads();
+    double part = 0.0;
+    for (int j = g; j < P; j += 64) {
+        double v0 = 0.0, v1 = 0.0;
+        const double* tj = T + (size_t)j * P;
+        for (int k = 0; k < P; ++k) {
+            const double c = tj[k];
+            v0 += c * sq[k * kNmTile + 2 * pp];
+            v1 += c * sq[k * kNmTile + 2 * pp + 1];
+        }
+        const int ie = i0 + 2 * pp;
+        if (ie < s.N) {
+            s.p[idx<D>(s, j, a, ie)] = v0;
+            part += v0;
+        }
+        if (ie + 1 < s.N) {
+            s.p[idx<D>(s, j, a, ie + 1)] = v1;
+            part += v1;
         }
     }
     if (flags & SF_COM_PARTIAL) {
-        // partial index: flattened block id
-        double pa[3] = {0.0, 0.0, 0.0};
-        pa[a] = part[a];
         const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+        const double tsum = block_sum(part, shred);
+        if (threadIdx.x == 0) {
 #pragma unroll
-        for (int ax = 0; ax < D; ++ax) {
-            const double tsum = block_sum(pa[ax], shred);
-            if (threadIdx.x == 0) red_out[3 * bid + ax] = tsum;
+            for (int ax = 0; ax < D; ++ax) red_out[3 * bid + ax] = ax == a ? tsum : 0.0;
         }
     }
 }
@@ -190,54 +208,72 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
     double* sq = sm + 2 * P * kNmTile;
     double* spi = sm + 3 * P * kNmTile;
     const int a = blockIdx.y;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int i = blockIdx.x * kNmTile + lane;
-    const bool act = i < s.N;
+    const int i0 = blockIdx.x * kNmTile;
+    const int pp = threadIdx.x & 3, g = threadIdx.x >> 2;
     double cm[3] = {0.0, 0.0, 0.0};
     if (com_apply) com_from_partials<D>(s, red_in, nred_in, cm, shred);
-    for (int b = w; b < P; b += nw) {
+    for (int e = threadIdx.x; e < P * kNmTile; e += blockDim.x) {
+        const int b = e / kNmTile, il = e % kNmTile, i = i0 + il;
         double x = 0.0, p = 0.0;
-        if (act) {
+        if (i < s.N) {
             const size_t o = idx<D>(s, b, a, i);
             x = s.x[o];
             p = s.p[o] - cm[a];
             p += 0.5 * s.dt * nm_kick_force<D>(s, b, a, i);
         }
-        sx[b * kNmTile + lane] = x;
-        sp[b * kNmTile + lane] = p;
+        sx[e] = x;
+        sp[e] = p;
     }
     __syncthreads();
-    for (int k = w; k < P; k += nw) {
-        double q = 0.0, pi = 0.0;
+    for (int k = g; k < P; k += 64) {
+        double q0 = 0.0, q1 = 0.0, p0 = 0.0, p1 = 0.0;
+        const double* ck = C + (size_t)k * P;
         for (int b = 0; b < P; ++b) {
-            const double c = C[k * P + b];
-            q += c * sx[b * kNmTile + lane];
-            pi += c * sp[b * kNmTile + lane];
+            const double c = ck[b];
+            q0 += c * sx[b * kNmTile + 2 * pp];
+            q1 += c * sx[b * kNmTile + 2 * pp + 1];
+            p0 += c * sp[b * kNmTile + 2 * pp];
+            p1 += c * sp[b * kNmTile + 2 * pp + 1];
         }
         const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
-        double qn, pn;
+        double qa, qb, pa, pb;
         if (mw == 0.0) {
-            qn = q + s.dt / s.mass * pi;
-            pn = pi;
+            qa = q0 + s.dt / s.mass * p0;
+            qb = q1 + s.dt / s.mass * p1;
+            pa = p0;
+            pb = p1;
         } else {
-            qn = cs * q + sn / mw * pi;
-            pn = -mw * sn * q + cs * pi;
+            qa = cs * q0 + sn / mw * p0;
+            qb = cs * q1 + sn / mw * p1;
+            pa = -mw * sn * q0 + cs * p0;
+            pb = -mw * sn * q1 + cs * p1;
         }
-        sq[k * kNmTile + lane] = qn;
-        spi[k * kNmTile + lane] = pn;
+        sq[k * kNmTile + 2 * pp] = qa;
+        sq[k * kNmTile + 2 * pp + 1] = qb;
+        spi[k * kNmTile + 2 * pp] = pa;
+        spi[k * kNmTile + 2 * pp + 1] = pb;
     }
     __syncthreads();
-    for (int j = w; j < P; j += nw) {
-        double xv = 0.0, pv = 0.0;
+    for (int j = g; j < P; j += 64) {
+        double x0 = 0.0, x1 = 0.0, v0 = 0.0, v1 = 0.0;
+        const double* tj = T + (size_t)j * P;
         for (int k = 0; k < P; ++k) {
-            const double t = T[j * P + k];
-            xv += t * sq[k * kNmTile + lane];
-            pv += t * spi[k * kNmTile + lane];
+            const double c = tj[k];
+            x0 += c * sq[k * kNmTile + 2 * pp];
+            x1 += c * sq[k * kNmTile + 2 * pp + 1];
+            v0 += c * spi[k * kNmTile + 2 * pp];
+            v1 += c * spi[k * kNmTile + 2 * pp + 1];
         }
-        if (act) {
-            const size_t o = idx<D>(s, j, a, i);
-            s.x[o] = xv;
-            s.p[o] = pv;
+        const int ie = i0 + 2 * pp;
+        if (ie < s.N) {
+            const size_t o = idx<D>(s, j, a, ie);
+            s.x[o] = x0;
+            s.p[o] = v0;
+        }
+        if (ie + 1 < s.N) {
+            const size_t o = idx<D>(s, j, a, ie + 1);
+            s.x[o] = x1;
+            s.p[o] = v1;
         }
     }
 }

@@ -21,10 +21,16 @@ enum StepFlags : int {
 // forces.cu: external + pair forces and distinguishable springs on every
 // bead; on bosonic beads 0 and P-1 only the physical part is stored in f.
 void launch_bead_forces(const Sys& s, int D, int mixed, int write_phys, cudaStream_t st);
+// Same result with Newton's third law: pair tiles write partial sums into
+// `part` (pair_partial_doubles doubles), a second kernel adds them in order.
+size_t pair_partial_doubles(const Sys& s, int D);
+void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part, cudaStream_t st);
 
 // exchange.cu: Feldman-Hirshberg exchange on beads 1 and P.
 void launch_exchange_energies(const Sys& s, int D, cudaStream_t st);
-void launch_exchange_recursions(const Sys& s, cudaStream_t st);
+// Returns the number of kernels launched (3, or 1 with `exact`: the
+// reference-order FP64 log-sum-exp recursion only).
+int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st);
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st);
 void launch_exchange_estimators(const Sys& s, cudaStream_t st);
 

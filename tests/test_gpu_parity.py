@@ -37,30 +37,37 @@ FORCE_CASES = {
     "dist_P1": (dict(natoms=9, nbeads=1, inter="harmonic", int_p=(1.0 * 0.036749326e-3, 0, 0)), dict()),
     "bosons_aziz_pbc_N300_P4": (dict(natoms=300, nbeads=4, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=24.0,
                                      inter="aziz", cutoff_ang=12.0), dict(spread_ang=0.2)),
+    "bosons_trap_N1100_P3_far_from_equilibrium": (dict(natoms=1100, nbeads=3, ext="harmonic",
+                                                       ext_p=(3.0 * 0.036749326e-3, 0, 0), box_ang=40.0),
+                                                  dict(spread_ang=3.0)),
 }
 
 
+@pytest.mark.parametrize("newton3", [1, 0])
 @pytest.mark.parametrize("name", sorted(FORCE_CASES))
-def test_forces_match_oracle(name):
+def test_forces_match_oracle(name, newton3):
     kw, rk = FORCE_CASES[name]
     s, cfg = case(**kw)
     x = ring(s, seed=len(name), **rk)
     want = O.update_forces(s, x)["f"]
     with pk.System(cfg) as g:
+        g.set_option("newton3", newton3)
         g.set_state(x, np.zeros_like(x))
         g.compute_forces()
         _, _, f = g.get_state()
     assert rel_per_bead(f, want) < FP64_TOL
 
 
+@pytest.mark.parametrize("exact", [0, 1])
 @pytest.mark.parametrize("name", [n for n in sorted(FORCE_CASES) if FORCE_CASES[n][0].get("bosonic", True)
                                   and FORCE_CASES[n][0].get("nbeads", 4) > 1])
-def test_exchange_matches_oracle(name):
+def test_exchange_matches_oracle(name, exact):
     kw, rk = FORCE_CASES[name]
     s, cfg = case(**kw)
     x = ring(s, seed=len(name) + 7, **rk)
     ref = O.exchange(s, x)
     with pk.System(cfg) as g:
+        g.set_option("exact_exchange", exact)
         g.set_state(x, np.zeros_like(x))
         got = g.exchange()
         arr = g.exchange_arrays()
