@@ -152,7 +152,8 @@ enum pimdb_kernel_class {
     PIMDB_K_EXCH_FORCES = 3,      /* connection probabilities -> forces on beads 1 and P */
     PIMDB_K_EXCH_ESTIMATORS = 4,  /* primEstimator and topology probabilities */
     PIMDB_K_CART_UPDATE = 5,      /* B / A / Langevin / COM on Cartesian momenta */
-    PIMDB_K_NM_PROPAGATE = 6,     /* normal-mode free ring-polymer propagation */
+    PIMDB_K_NM_PROPAGATE = 6,     /* normal-mode free ring-polymer propagation (fused with the
+                                     normal-mode thermostat when both are selected) */
     PIMDB_K_NM_THERMO = 7,        /* normal-mode Langevin O-step */
     PIMDB_NUM_KERNEL_CLASSES = 8
 };
@@ -169,7 +170,12 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
  *                    (evaluateVBn / evaluateVBackwards, :73-128) instead of
  *                    the estimate + triangular-solve evaluation (default 0);
  *   "newton3"        0: all-pairs pair kernel (each pair evaluated from both
- *                    sides) instead of the pair-tile kernel (default 1). */
+ *                    sides) instead of the pair-tile kernel (default 1);
+ *   "fused_normal_modes" 0: with the normal-mode propagator and thermostat,
+ *                    run the thermostat and the propagator as separate
+ *                    kernels in the reference's order instead of the fused
+ *                    normal-mode-frame kernel (default 1 when all its blocks
+ *                    fit on the GPU at once). */
 int pimdb_set_option(pimdb_handle* h, const char* name, int value);
 
 /* Measures the FP64 fused-multiply-add throughput of the current device in

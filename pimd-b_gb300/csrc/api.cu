@@ -22,6 +22,10 @@ struct pimdb_handle {
     Sys s{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // second stream: the exchange chain (latency-bound, two blocks) runs
+    // beside the pair forces (throughput-bound, every SM)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     double* d_C = nullptr;    // cart -> NM rows [P][P]
     double* d_T = nullptr;    // NM -> cart rows [P][P]
     double* d_rot = nullptr;  // [P][3]
@@ -38,6 +42,12 @@ struct pimdb_handle {
     // device time measured with events bracketing each launch
     long long launches = 0;
     int opt_exact_exchange = 0;
+    // fused normal-mode step (normal-mode propagator + normal-mode thermostat)
+    bool fused_nm = false;
+    bool nm_tail_pending = false;
+    double* d_cmpart = nullptr;
+    unsigned* d_bar = nullptr;
+    cudaError_t async_err = cudaSuccess;
     int opt_newton3 = 1;
     bool profile = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -192,6 +202,11 @@ static void free_handle(pimdb_handle* h) {
         if (b) cudaFree(b);
     if (h->d_err) cudaFree(h->d_err);
     if (h->s.xflags) cudaFree(h->s.xflags);
+    if (h->d_cmpart) cudaFree(h->d_cmpart);
+    if (h->d_bar) cudaFree(h->d_bar);
+    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+    if (h->join_ev) cudaEventDestroy(h->join_ev);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -292,13 +307,21 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     // beyond 512 MiB the all-pairs kernel (no partials) is used instead.
     const size_t npart = pair_partial_doubles(s, h->D);
     if (e == cudaSuccess && npart * sizeof(double) <= (512ull << 20)) e = alloc(&h->d_part, npart);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s.xflags, 4 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(s.xflags, 0, 4 * sizeof(int));
+    // xflags: [0],[1] exact fallback used (forward, backward); [2] completion
+    // counter; [3] next evaluation needs a fresh FP32 estimate; [4],[5] the
+    // forward / backward solve asked for one.
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s.xflags, 8 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(s.xflags, 0, 8 * sizeof(int));
+    const int one = 1;
+    if (e == cudaSuccess) e = cudaMemcpy(s.xflags + 3, &one, sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = alloc(&h->d_red[0], (size_t)3 * nred);
     if (e == cudaSuccess) e = alloc(&h->d_red[1], (size_t)3 * nred);
     if (e == cudaSuccess) e = alloc(&h->d_stage, (size_t)s.P * s.N * h->D);
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
     if (e == cudaSuccess && (c.propagator == PIMDB_PROP_NORMAL_MODES || c.nmthermostat)) {
@@ -312,6 +335,14 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
         if (e == cudaSuccess)
             e = cudaMemcpy(h->d_rot, rot.data(), rot.size() * sizeof(double), cudaMemcpyHostToDevice);
     }
+    if (e == cudaSuccess && c.propagator == PIMDB_PROP_NORMAL_MODES && c.nmthermostat &&
+        c.thermostat == PIMDB_THERMO_LANGEVIN && nm_fused_fits(s, h->D)) {
+        e = alloc(&h->d_cmpart, (size_t)2 * nm_blocks(s, h->D));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_bar, 2 * sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMemset(h->d_bar, 0, 2 * sizeof(unsigned));
+        h->fused_nm = (e == cudaSuccess);
+    }
+    cudaGetLastError();
     s.err = h->d_err;
     s.red = h->d_red[0];
     if (e != cudaSuccess) {
@@ -359,6 +390,9 @@ static int set_state_impl(pimdb_handle* h, const double* x, const double* p, cud
     CUDA_TRY(h, cudaMemsetAsync(s.f, 0, nstate * sizeof(double), h->stream));
     CUDA_TRY(h, cudaMemsetAsync(s.fphys, 0, nstate * sizeof(double), h->stream));
     CUDA_TRY(h, cudaMemsetAsync(s.fx, 0, (size_t)2 * h->D * s.ld * sizeof(double), h->stream));
+    // new coordinates: the exchange recomputes its FP32 estimate first
+    static const int one = 1;
+    CUDA_TRY(h, cudaMemcpyAsync(s.xflags + 3, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
     h->com_pending = false;
     CUDA_TRY(h, cudaGetLastError());
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -410,11 +444,20 @@ extern "C" int pimdb_get_step(pimdb_handle* h, long long* step) {
 static void enqueue_forces(pimdb_handle* h) {
     const Sys& s = h->s;
     const bool nm = h->cfg.propagator == PIMDB_PROP_NORMAL_MODES;
-    if (s.bosonic) {
-        launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
-        const int ex = h->opt_exact_exchange;
-        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 3);
+    // exchange chain on the side stream when not profiling (profiling times
+    // every launch on the main stream)
+    const bool fork = s.bosonic && !h->profile;
+    cudaStream_t xs = fork ? h->side : h->stream;
+    if (fork) {
+        cudaEventRecord(h->fork_ev, h->stream);
+        cudaStreamWaitEvent(h->side, h->fork_ev, 0);
     }
+    if (s.bosonic) {
+        launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, xs); });
+        const int ex = h->opt_exact_exchange;
+        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, xs); }, ex ? 1 : 3);
+    }
+    if (fork) cudaEventRecord(h->join_ev, h->side);
     const int mixed = h->cfg.precision == PIMDB_MIXED;
     if (h->d_part && h->opt_newton3) {
         const bool pairs = s.int_kind != PIMDB_POT_FREE && s.cutoff != 0.0;
@@ -424,6 +467,7 @@ static void enqueue_forces(pimdb_handle* h) {
     } else {
         launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_bead_forces(s, h->D, mixed, nm ? 1 : 0, h->stream); });
     }
+    if (fork) cudaStreamWaitEvent(h->stream, h->join_ev, 0);
     if (s.bosonic) launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 1, h->stream); });
 }
 
@@ -486,8 +530,8 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
     const bool nm = c.propagator == PIMDB_PROP_NORMAL_MODES;
     const bool cart_langevin = c.thermostat == PIMDB_THERMO_LANGEVIN && !c.nmthermostat;
     for (int it = 0; it < nsteps; ++it) {
-        // O, [COM]
-        thermostat_step(h, 0);
+        // O, [COM] (inside the fused normal-mode kernel when that is used)
+        if (!(nm && h->fused_nm)) thermostat_step(h, 0);
         if (!nm) {
             // [COM], B, A (velocity_verlet.cpp:9-12)
             cart(h, SF_COM_APPLY | SF_KICK | SF_DRIFT, 0, 0);
@@ -499,6 +543,17 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
                 cart(h, SF_KICK, 1, 0);
                 thermostat_step(h, 1);
             }
+        } else if (h->fused_nm) {
+            // tail of the previous step (if pending) and head of this one
+            const int mode = (h->nm_tail_pending ? 1 : 0) | 2;
+            const long long st = h->step;
+            launch(h, PIMDB_K_NM_PROPAGATE, [&] {
+                cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, mode, st,
+                                                c.fixcom, h->stream);
+                if (e != cudaSuccess) h->async_err = e;
+            });
+            enqueue_forces(h);
+            h->nm_tail_pending = true;
         } else {
             // [COM] + half-kick + free ring-polymer propagation
             const int rin = h->red_last;
@@ -518,6 +573,15 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
         }
         h->step += 1;
     }
+    if (h->nm_tail_pending) {
+        const long long st = h->step;
+        launch(h, PIMDB_K_NM_PROPAGATE, [&] {
+            cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, 1, st,
+                                            h->cfg.fixcom, h->stream);
+            if (e != cudaSuccess) h->async_err = e;
+        });
+        h->nm_tail_pending = false;
+    }
     // the last COM removal of the last step
     if (h->com_pending) {
         const long long keep = h->step;
@@ -529,6 +593,11 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
 extern "C" int pimdb_step_async(pimdb_handle* h, int nsteps) {
     if (!h || nsteps < 0) return PIMDB_ERR_ARG;
     enqueue_steps(h, nsteps);
+    if (h->async_err != cudaSuccess) {
+        const cudaError_t e = h->async_err;
+        h->async_err = cudaSuccess;
+        return fail(h, PIMDB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    }
     CUDA_TRY(h, cudaGetLastError());
     return PIMDB_OK;
 }
@@ -647,6 +716,7 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
     if (!h || !name) return PIMDB_ERR_ARG;
     const std::string n(name);
     if (n == "exact_exchange") h->opt_exact_exchange = value ? 1 : 0;
+    else if (n == "fused_normal_modes") h->fused_nm = value && h->d_cmpart != nullptr;
     else if (n == "newton3") h->opt_newton3 = value ? 1 : 0;
     else return fail(h, PIMDB_ERR_ARG, "unknown option " + n);
     return PIMDB_OK;

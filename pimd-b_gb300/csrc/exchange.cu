@@ -56,7 +56,9 @@ __device__ __forceinline__ double sepsq(const Sys& s, int ba, int ia, int bb, in
 
 // One warp per row v: E[v][v] = k/2 |xP_v - x1_v|^2, then
 // E[v][u] = E[v][u+1] + k/2 (|x1_{u+1} - xP_u|^2 - |xP_v - x1_{u+1}|^2 + |xP_v - x1_u|^2)
-// for u = v-1 .. 0, evaluated as a warp-wide suffix scan over u.
+// for u = v-1 .. 0, evaluated as a warp-wide suffix scan over u.  The middle
+// distance of entry u is the last distance of entry u+1, so each entry costs
+// two distance evaluations (passed between lanes by a shuffle).
 template <int D>
 __global__ void k_exch_energies(Sys s) {
     const int lane = threadIdx.x & 31;
@@ -65,15 +67,30 @@ __global__ void k_exch_energies(Sys s) {
     const int first = 0, last = s.P - 1;
     const double hk = 0.5 * s.kappa;
     double* row = s.E + tri(v);
-    double carry = hk * sepsq<D>(s, first, v, last, v);
+    double xv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xv[a] = s.x[idx<D>(s, last, a, v)];
+    auto dist_to_v = [&](int u) {  // |xP_v - x1_u|^2
+        double d2 = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double d = xv[a] - s.x[idx<D>(s, first, a, u)];
+            if (s.pbc) d = min_image(d, s.L, s.invL);
+            d2 += d * d;
+        }
+        return d2;
+    };
+    double cnext = dist_to_v(v);  // |xP_v - x1_{u+1}|^2 for the lane holding u = base
+    double carry = hk * cnext;
     if (lane == 0) row[v] = carry;
     for (int base = v - 1; base >= 0; base -= 32) {
         const int u = base - lane;
+        const double c = u >= 0 ? dist_to_v(u) : 0.0;
+        double cu1 = __shfl_up_sync(0xffffffffu, c, 1);
+        if (lane == 0) cu1 = cnext;
         double term = 0.0;
-        if (u >= 0) {
-            term = hk * (sepsq<D>(s, last, u, first, u + 1) - sepsq<D>(s, first, u + 1, last, v) +
-                         sepsq<D>(s, first, u, last, v));
-        }
+        if (u >= 0) term = hk * (sepsq<D>(s, last, u, first, u + 1) - cu1 + c);
+        cnext = __shfl_sync(0xffffffffu, c, 31);
         // inclusive scan over lanes (lane 0 holds the largest u)
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -94,71 +111,90 @@ __device__ __forceinline__ void lse_add(float& mx, float& sm, float t) {
     }
 }
 
-// Pass 1: FP32 estimates.  Thread tid owns levels tid+1+k*blockDim (k < K).
+// Depth of the register prefetch ring of the wavefront kernels: the operand
+// of round j + ring is loaded during round j, hiding the L2 latency.  Fewer
+// slots when each thread owns many levels, to stay within 64 registers.
+template <int K>
+struct Ring {
+    static constexpr int n = K <= 2 ? 8 : (K <= 4 ? 4 : 2);
+};
+
+// Pass 1: FP32 estimates, one block per direction.  Thread tid owns levels
+// tid+1+k*blockDim (k < K).  Skipped (early exit) when the previous
+// evaluation's exact V is still a good estimate (xflags[3] == 0).
 template <int K>
 __global__ void __launch_bounds__(1024) k_exch_estimate(Sys s) {
+    constexpr int RING = Ring<K>::n;
+    if (((volatile int*)s.xflags)[3] == 0) return;
     extern __shared__ float vs[];  // N+1
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
     const float beta = (float)s.beta_ex;
-    float mx[K], sm[K], en[K];
+    float mx[K], sm[K], rg[RING][K];
     int lv[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         lv[k] = tid + 1 + k * bd;
         mx[k] = -CUDART_INF_F;
         sm[k] = 0.0f;
-        en[k] = 0.0f;
     }
     if (blockIdx.x == 0) {
         // forward: level m has terms u = 0..m-1 with E[m-1][u] + V[u]
         if (tid == 0) vs[0] = 0.0f;
 #pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (lv[k] <= N) en[k] = (float)s.E[tri(lv[k] - 1)];
+        for (int r = 0; r < RING; ++r)
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                rg[r][k] = (lv[k] <= N && lv[k] > r) ? (float)s.E[tri(lv[k] - 1) + r] : 0.0f;
         __syncthreads();
-        for (int j = 0; j < N; ++j) {
-            float ec[K];
+        for (int j0 = 0; j0 < N; j0 += RING) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                ec[k] = en[k];
-                if (lv[k] <= N && lv[k] > j + 1) en[k] = (float)s.E[tri(lv[k] - 1) + j + 1];
-            }
-            const float vj = vs[j];
+            for (int r = 0; r < RING; ++r) {
+                const int j = j0 + r;
+                if (j < N) {
+                    const float vj = vs[j];
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                if (lv[k] <= N && lv[k] > j) {
-                    lse_add(mx[k], sm[k], -beta * (ec[k] + vj));
-                    if (lv[k] == j + 1) vs[j + 1] = -(mx[k] + __logf(sm[k]) - __logf((float)lv[k])) / beta;
+                    for (int k = 0; k < K; ++k) {
+                        if (lv[k] <= N && lv[k] > j) {
+                            lse_add(mx[k], sm[k], -beta * (rg[r][k] + vj));
+                            if (lv[k] == j + 1) vs[j + 1] = -(mx[k] + __logf(sm[k]) - __logf((float)lv[k])) / beta;
+                            if (lv[k] > j + RING) rg[r][k] = (float)s.E[tri(lv[k] - 1) + j + RING];
+                        }
+                    }
                 }
+                __syncthreads();
             }
-            __syncthreads();
         }
         for (int m = tid; m <= N; m += bd) s.Vh[m] = (double)vs[m];
     } else {
-        // backward: level l (1..N-1) has terms p = l..N-1 with E[p][l] + Vb[p+1] and weight 1/(p+1)
+        // backward: level l (1..N-1) has terms p = l..N-1 with E[p][l] + Vb[p+1]
+        // and weight 1/(p+1); round q handles p = N-1-q
         if (tid == 0) vs[N] = 0.0f;
 #pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (lv[k] <= N - 1) en[k] = (float)s.E[tri(N - 1) + lv[k]];
+        for (int r = 0; r < RING; ++r)
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int p = N - 1 - r;
+                rg[r][k] = (p >= 1 && lv[k] <= p) ? (float)s.E[tri(p) + lv[k]] : 0.0f;
+            }
         __syncthreads();
-        for (int j = N; j >= 2; --j) {
-            const int p = j - 1;
-            float ec[K];
+        for (int q0 = 0; q0 < N - 1; q0 += RING) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                ec[k] = en[k];
-                if (lv[k] <= p - 1) en[k] = (float)s.E[tri(p - 1) + lv[k]];
-            }
-            const float vj = vs[j];
-            const float lj = __logf((float)j);
+            for (int r = 0; r < RING; ++r) {
+                const int p = N - 1 - (q0 + r);
+                if (p >= 1) {
+                    const float vj = vs[p + 1];
+                    const float lj = __logf((float)(p + 1));
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                if (lv[k] <= p) {
-                    lse_add(mx[k], sm[k], -beta * (ec[k] + vj) - lj);
-                    if (lv[k] == p) vs[p] = -(mx[k] + __logf(sm[k])) / beta;
+                    for (int k = 0; k < K; ++k) {
+                        if (lv[k] <= p) {
+                            lse_add(mx[k], sm[k], -beta * (rg[r][k] + vj) - lj);
+                            if (lv[k] == p) vs[p] = -(mx[k] + __logf(sm[k])) / beta;
+                            if (lv[k] <= p - RING) rg[r][k] = (float)s.E[tri(p - RING) + lv[k]];
+                        }
+                    }
                 }
+                __syncthreads();
             }
-            __syncthreads();
         }
         for (int l = tid; l <= N; l += bd) s.Vbh[l] = (l >= 1) ? (double)vs[l] : 0.0;
     }
@@ -178,7 +214,8 @@ __global__ void k_exch_weights(Sys s) {
 }
 
 // Exact level-by-level FP64 log-sum-exp in the reference's order (used only
-// when the estimate is unusable).  `vs` holds N+1 doubles, `red` 32.
+// when the estimate is unusable, or on request).  `vs` holds N+1 doubles,
+// `red` 32.
 __device__ void exact_forward(const Sys& s, double* vs, double* red) {
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
     const double beta = s.beta_ex;
@@ -214,51 +251,62 @@ __device__ void exact_backward(const Sys& s, double* vs, double* red) {
     }
 }
 
+// |log y| above which the next evaluation computes a fresh FP32 estimate
+// instead of reusing the current potentials, and above which the present
+// evaluation switches to the exact level-by-level recursion.
+constexpr double kRefreshLogY = 30.0;
+constexpr double kExactLogY = 200.0;
+
 // Pass 3: y solves, exact V / V_backwards, and (by the block that finishes
 // last) the per-row factors of the connection probabilities.
 template <int K>
 __global__ void __launch_bounds__(1024) k_exch_solve(Sys s, int force_exact) {
+    constexpr int RING = Ring<K>::n;
     extern __shared__ double ys[];  // N+1, then 32 for reductions
     double* red = ys + s.N + 1;
     __shared__ int last_block;
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
     const double beta = s.beta_ex;
-    double acc[K], wn[K];
+    double acc[K], rg[RING][K];
     int lv[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         lv[k] = tid + 1 + k * bd;
         acc[k] = 0.0;
-        wn[k] = 0.0;
     }
-    int bad = force_exact;
+    int bad = force_exact, stale = 0;
     if (blockIdx.x == 0) {
         if (tid == 0) ys[0] = 1.0;
+        if (!force_exact) {
 #pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (lv[k] <= N && !force_exact) wn[k] = s.Wf[tri(lv[k] - 1)];
+            for (int r = 0; r < RING; ++r)
+#pragma unroll
+                for (int k = 0; k < K; ++k) rg[r][k] = (lv[k] <= N && lv[k] > r) ? s.Wf[tri(lv[k] - 1) + r] : 0.0;
+        }
         __syncthreads();
-        for (int j = 0; j < (force_exact ? 0 : N); ++j) {
-            double wc[K];
+        for (int j0 = 0; j0 < (force_exact ? 0 : N); j0 += RING) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                wc[k] = wn[k];
-                if (lv[k] <= N && lv[k] > j + 1) wn[k] = s.Wf[tri(lv[k] - 1) + j + 1];
-            }
-            const double yj = ys[j];
+            for (int r = 0; r < RING; ++r) {
+                const int j = j0 + r;
+                if (j < N) {
+                    const double yj = ys[j];
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                if (lv[k] <= N && lv[k] > j) {
-                    acc[k] = fma(wc[k], yj, acc[k]);
-                    if (lv[k] == j + 1) ys[j + 1] = acc[k];
+                    for (int k = 0; k < K; ++k) {
+                        if (lv[k] <= N && lv[k] > j) {
+                            acc[k] = fma(rg[r][k], yj, acc[k]);
+                            if (lv[k] == j + 1) ys[j + 1] = acc[k];
+                            if (lv[k] > j + RING) rg[r][k] = s.Wf[tri(lv[k] - 1) + j + RING];
+                        }
+                    }
                 }
+                __syncthreads();
             }
-            __syncthreads();
         }
         for (int m = tid; m <= N && !force_exact; m += bd) {
             const double y = ys[m];
             const double ly = log(y);
-            if (!(y > 0.0) || !(fabs(ly) < 200.0)) bad = 1;
+            if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
+            if (!(fabs(ly) < kRefreshLogY)) stale = 1;
             s.yf[m] = y;
             s.V[m] = s.Vh[m] - ly / beta;
         }
@@ -267,33 +315,46 @@ __global__ void __launch_bounds__(1024) k_exch_solve(Sys s, int force_exact) {
             exact_forward(s, ys, red);
             for (int m = tid; m <= N; m += bd) s.V[m] = ys[m];
         }
-        if (tid == 0) s.xflags[0] = bad;
+        int nonfinite = 0;
         __syncthreads();
         for (int m = tid; m <= N; m += bd)
-            if (!isfinite(s.V[m])) atomicOr(s.err, ERRB_NONFINITE_VB);
+            if (!isfinite(s.V[m])) nonfinite = 1;
+        nonfinite = __syncthreads_or(nonfinite);
+        stale = __syncthreads_or(stale);
+        if (tid == 0) {
+            s.xflags[0] = bad;
+            s.xflags[4] = stale | nonfinite;
+            if (nonfinite) atomicOr(s.err, ERRB_NONFINITE_VB);
+        }
     } else {
         if (tid == 0) ys[N] = 1.0;
+        if (!force_exact) {
 #pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (lv[k] <= N - 1 && !force_exact) wn[k] = s.Wb[tri(N - 1) + lv[k]];
-        __syncthreads();
-        for (int j = N; j >= (force_exact ? N + 1 : 2); --j) {
-            const int p = j - 1;
-            double wc[K];
+            for (int r = 0; r < RING; ++r)
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                wc[k] = wn[k];
-                if (lv[k] <= p - 1) wn[k] = s.Wb[tri(p - 1) + lv[k]];
-            }
-            const double yj = ys[j];
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                if (lv[k] <= p) {
-                    acc[k] = fma(wc[k], yj, acc[k]);
-                    if (lv[k] == p) ys[p] = acc[k];
+                for (int k = 0; k < K; ++k) {
+                    const int p = N - 1 - r;
+                    rg[r][k] = (p >= 1 && lv[k] <= p) ? s.Wb[tri(p) + lv[k]] : 0.0;
                 }
+        }
+        __syncthreads();
+        for (int q0 = 0; q0 < (force_exact ? 0 : N - 1); q0 += RING) {
+#pragma unroll
+            for (int r = 0; r < RING; ++r) {
+                const int p = N - 1 - (q0 + r);
+                if (p >= 1) {
+                    const double yj = ys[p + 1];
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        if (lv[k] <= p) {
+                            acc[k] = fma(rg[r][k], yj, acc[k]);
+                            if (lv[k] == p) ys[p] = acc[k];
+                            if (lv[k] <= p - RING) rg[r][k] = s.Wb[tri(p - RING) + lv[k]];
+                        }
+                    }
+                }
+                __syncthreads();
             }
-            __syncthreads();
         }
         for (int l = tid + 1; l <= N; l += bd) {
             if (l == N) {
@@ -304,7 +365,8 @@ __global__ void __launch_bounds__(1024) k_exch_solve(Sys s, int force_exact) {
             if (force_exact) continue;
             const double y = ys[l];
             const double ly = log(y);
-            if (!(y > 0.0) || !(fabs(ly) < 200.0)) bad = 1;
+            if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
+            if (!(fabs(ly) < kRefreshLogY)) stale = 1;
             s.yb[l] = y;
             s.Vb[l] = s.Vbh[l] - ly / beta;
         }
@@ -313,28 +375,44 @@ __global__ void __launch_bounds__(1024) k_exch_solve(Sys s, int force_exact) {
             exact_backward(s, ys, red);
             for (int l = tid + 1; l <= N; l += bd) s.Vb[l] = ys[l];
         }
-        if (tid == 0) s.xflags[1] = bad;
+        int nonfinite = 0;
         __syncthreads();
         for (int l = tid + 1; l <= N; l += bd)
-            if (!isfinite(s.Vb[l])) atomicOr(s.err, ERRB_NONFINITE_VB);
+            if (!isfinite(s.Vb[l])) nonfinite = 1;
+        nonfinite = __syncthreads_or(nonfinite);
+        stale = __syncthreads_or(stale);
+        if (tid == 0) {
+            s.xflags[1] = bad;
+            s.xflags[5] = stale | nonfinite;
+            if (nonfinite) atomicOr(s.err, ERRB_NONFINITE_VB);
+        }
     }
     // The block that finishes second computes the per-row factors, which need
-    // both V and V_backwards (threadFenceReduction pattern; no waiting).
+    // both V and V_backwards (threadFenceReduction pattern; no waiting), and
+    // keeps V, V_backwards as the estimates of the next evaluation.
     __threadfence();
     __syncthreads();
     if (tid == 0) last_block = (atomicAdd(&s.xflags[2], 1) == 1);
     __syncthreads();
     if (!last_block) return;
     __threadfence();
-    const double VN = ((volatile double*)s.V)[N];
+    volatile double* V = s.V;
+    volatile double* Vb = s.Vb;
+    const double VN = V[N];
     for (int l = tid; l < N; l += bd) {
-        const double vbl = ((volatile double*)s.Vb)[l + 1];
-        const double vl = ((volatile double*)s.V)[l + 1];
+        const double vbl = Vb[l + 1];
         s.rowR[l] = exp(-beta * (s.Vh[l + 1] + vbl - VN));
-        s.rowC[l] = exp(-beta * (vl + vbl - VN));
+        s.rowC[l] = exp(-beta * (V[l + 1] + vbl - VN));
+    }
+    __syncthreads();
+    const int need = ((volatile int*)s.xflags)[4] | ((volatile int*)s.xflags)[5];
+    for (int m = tid; m <= N; m += bd) {
+        s.Vh[m] = V[m];
+        s.Vbh[m] = m >= 1 ? Vb[m] : 0.0;
     }
     if (tid == 0) {
         s.xflags[2] = 0;
+        s.xflags[3] = need;
         s.Vb[0] = VN;  // V_backwards[0] = V[N] (:127)
         s.scal[0] = VN;
     }
@@ -467,7 +545,7 @@ static int wave_threads(int N) {
 }
 
 void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
-    const int warps = 8;
+    const int warps = 2;
     dim3 grid((s.N + warps - 1) / warps);
     if (D == 1) k_exch_energies<1><<<grid, warps * 32, 0, st>>>(s);
     else if (D == 2) k_exch_energies<2><<<grid, warps * 32, 0, st>>>(s);

@@ -29,34 +29,39 @@ __device__ __forceinline__ R pair_scale(int kind, R r2, R param);
 template <>
 __device__ __forceinline__ double pair_scale<double>(int kind, double r2, double param) {
     if (kind == POT_HARMONIC) return param;  // harmonic.cpp:21-23, k = m w^2
-    const double norm = sqrt(r2);
-    if (kind == POT_DIPOLE) {                 // dipole.cpp:24-45
-        const double n2 = norm * norm;
-        return -3.0 * param / (n2 * n2 * norm);
+    // one reciprocal square root serves |r|, 1/r_scaled and the final 1/|r|
+    const double rinv = rsqrt(r2);
+    if (kind == POT_DIPOLE) {  // dipole.cpp:24-45: -3 D / |r|^5
+        const double ri2 = rinv * rinv;
+        return -3.0 * param * (ri2 * ri2 * rinv);
     }
-    // POT_AZIZ, aziz.cpp:56-106
+    // POT_AZIZ, aziz.cpp:56-106 (same terms, factored)
+    const double norm = r2 * rinv;
     const double rs = norm * (1.0 / Aziz::rm);
     const double T1 = -Aziz::A * Aziz::alpha * exp(-Aziz::alpha * rs);
     double g;
     if (rs > 1.0E-7 && rs < 0.01) {
         g = T1 * (Aziz::eps / Aziz::rm);
     } else {
-        const double ix = 1.0 / rs;
+        const double ix = Aziz::rm * rinv;  // 1 / r_scaled
         const double ix2 = ix * ix;
         const double ix6 = ix2 * ix2 * ix2;
-        const double ix7 = ix6 * ix, ix8 = ix6 * ix2, ix9 = ix8 * ix, ix10 = ix8 * ix2, ix11 = ix10 * ix;
-        double F = 1.0, dF = 0.0;
+        double tail = 0.0;
         if (rs < Aziz::D) {
+            // T2 + T3 = F(rs) [ix^7 (6 C6 + 8 C8 ix^2 + 10 C10 ix^4)
+            //                  - 2 D ix^2 (D ix - 1) ix^6 (C6 + C8 ix^2 + C10 ix^4)]
             const double t = Aziz::D * ix - 1.0;
             const double e = exp(-t * t);
-            F = e;
-            dF = 2.0 * Aziz::D * ix2 * t * e;
+            const double pa = fma(fma(10.0 * Aziz::C10, ix2, 8.0 * Aziz::C8), ix2, 6.0 * Aziz::C6);
+            const double pb = fma(fma(Aziz::C10, ix2, Aziz::C8), ix2, Aziz::C6);
+            tail = e * ix6 * (ix * pa - 2.0 * Aziz::D * ix2 * t * pb);
+        } else {
+            const double pa = fma(fma(10.0 * Aziz::C10, ix2, 8.0 * Aziz::C8), ix2, 6.0 * Aziz::C6);
+            tail = ix6 * ix * pa;  // F = 1, dF = 0
         }
-        const double T2 = (6.0 * Aziz::C6 * ix7 + 8.0 * Aziz::C8 * ix9 + 10.0 * Aziz::C10 * ix11) * F;
-        const double T3 = -(Aziz::C6 * ix6 + Aziz::C8 * ix8 + Aziz::C10 * ix10) * dF;
-        g = (Aziz::eps / Aziz::rm) * (T1 + T2 + T3);
+        g = (Aziz::eps / Aziz::rm) * (T1 + tail);
     }
-    return g / norm;
+    return g * rinv;
 }
 
 template <>
@@ -236,6 +241,20 @@ __device__ __forceinline__ PairPos<R, D> split_pos(const double* x) {
 template <int D, typename R>
 __device__ __forceinline__ bool pair_force(const Sys& s, const PairPos<R, D>& pi, const PairPos<R, D>& pj,
                                            R* g) {
+    const double cut = s.cutoff;
+    if constexpr (sizeof(R) == 8) {
+        // cheap FP32 screen: pairs clearly beyond the cutoff skip the FP64 work
+        if (cut > 0.0) {
+            float r2f = 0.0f;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                float d = (float)pi.h[a] - (float)pj.h[a];
+                if (s.pbc) d = min_image_f(d, (float)s.L, (float)s.invL);
+                r2f += d * d;
+            }
+            if (r2f > (float)(cut * cut) * 1.0001f) return false;
+        }
+    }
     R r[D];
     R r2 = (R)0;
 #pragma unroll
@@ -251,10 +270,9 @@ __device__ __forceinline__ bool pair_force(const Sys& s, const PairPos<R, D>& pi
         r[a] = d;
         r2 += d * d;
     }
-    const double cut = s.cutoff;
     bool in;
     if (cut < 0.0) in = true;
-    else if constexpr (sizeof(R) == 8) in = sqrt((double)r2) < cut;
+    else if constexpr (sizeof(R) == 8) in = r2 < cut * cut;  // |r| < cutoff (simulation.cpp:444)
     else in = r2 < (float)(cut * cut);
     if (!in) return false;
     const R sc = pair_scale<R>(s.int_kind, r2, (R)s.int_a);

@@ -278,6 +278,233 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fused normal-mode step for the normal-mode propagator with the
+// normal-mode Langevin thermostat.  Between two force evaluations the
+// reference applies (normal_modes_propagator.cpp:19-103,
+// thermostat_coupling.cpp:29-47, simulation.cpp:246-259):
+//   tail of step s-1:  kick(F), O (normal modes), COM removal
+//   head of step s:    O (normal modes), COM removal, kick(F), free ring rotation
+// Every piece is linear in the normal-mode frame, so one kernel transforms
+// p, the kick force F and x once, applies all of it in that frame and
+// transforms x and p back: 5 bead transforms instead of 8.  The COM removal
+// becomes a shift of the centroid mode (C's first row is 1/sqrt(P), every
+// other row sums to zero), which needs the sum over all particles: blocks
+// meet at a grid barrier (cooperative launch, so all blocks are resident; the
+// barrier gives up after a bounded number of polls and raises ERRB_TIMEOUT).
+// mode bit 0: tail of step-1, bit 1: head of step.
+
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* err) {
+    __syncthreads();
+    __shared__ int timed_out;
+    if (threadIdx.x == 0) {
+        timed_out = 0;
+        volatile unsigned* gen = bar + 1;
+        const unsigned my = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == nblocks - 1) {
+            bar[0] = 0;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned it = 0;
+            while (*gen == my) {
+                if (++it > (1u << 24)) {
+                    atomicOr(err, ERRB_TIMEOUT);
+                    timed_out = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return !timed_out;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __restrict__ C,
+                                                         const double* __restrict__ T,
+                                                         const double* __restrict__ rot, double* cmpart,
+                                                         unsigned* bar, int mode, long long step, int fixcom) {
+    extern __shared__ double sm[];
+    __shared__ double shred[32];
+    const int P = s.P;
+    double* sp = sm;                    // p, later C p
+    double* sf = sm + P * kNmTile;      // kick force, later C F
+    double* sx = sm + 2 * P * kNmTile;  // x, later C x
+    double* sq = sm + 3 * P * kNmTile;  // normal-mode p
+    double* sg = sm + 4 * P * kNmTile;  // normal-mode F
+    double* sy = sm + 5 * P * kNmTile;  // normal-mode x
+    const int a = blockIdx.y;
+    const int i0 = blockIdx.x * kNmTile;
+    const int pp = threadIdx.x & 3, g = threadIdx.x >> 2;
+    const int nblocks = gridDim.x * gridDim.y;
+    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+    const bool head = mode & 2, tail = mode & 1;
+    for (int e = threadIdx.x; e < P * kNmTile; e += blockDim.x) {
+        const int b = e / kNmTile, il = e % kNmTile, i = i0 + il;
+        double x = 0.0, p = 0.0, f = 0.0;
+        if (i < s.N) {
+            const size_t o = idx<D>(s, b, a, i);
+            x = s.x[o];
+            p = s.p[o];
+            f = nm_kick_force<D>(s, b, a, i);
+        }
+        sx[e] = x;
+        sp[e] = p;
+        sf[e] = f;
+    }
+    __syncthreads();
+    for (int k = g; k < P; k += 64) {
+        double q0 = 0.0, q1 = 0.0, f0 = 0.0, f1 = 0.0, x0 = 0.0, x1 = 0.0;
+        const double* ck = C + (size_t)k * P;
+        for (int b = 0; b < P; ++b) {
+            const double c = ck[b];
+            const int o = b * kNmTile + 2 * pp;
+            q0 += c * sp[o];
+            q1 += c * sp[o + 1];
+            f0 += c * sf[o];
+            f1 += c * sf[o + 1];
+            if (head) {
+                x0 += c * sx[o];
+                x1 += c * sx[o + 1];
+            }
+        }
+        const int o = k * kNmTile + 2 * pp;
+        sq[o] = q0;
+        sq[o + 1] = q1;
+        sg[o] = f0;
+        sg[o + 1] = f1;
+        sy[o] = x0;
+        sy[o + 1] = x1;
+    }
+    __syncthreads();
+    const int half = (s.N + 1) / 2;
+    const double hdt = 0.5 * s.dt;
+    const double sqrtP = sqrt((double)P);
+    const double cm_scale = sqrtP * sqrtP / ((double)s.N * (double)P);  // q0 -> sqrt(P) cm
+    auto thermostat = [&](uint64_t t) {
+        for (int k = g; k < P; k += 64) {
+            const int o = k * kNmTile + 2 * pp;
+            const int ie = i0 + 2 * pp;
+            const double2 z =
+                philox_normal_pair(s.seed, s.replica, t, (uint32_t)((size_t)(k * D + a) * half + (ie >> 1)));
+            sq[o] = s.c1 * sq[o] + s.c2 * z.x;
+            sq[o + 1] = s.c1 * sq[o + 1] + s.c2 * z.y;
+        }
+        __syncthreads();
+    };
+    auto remove_com = [&](int buf) -> bool {
+        // centroid sum of this tile (real particles only), grid barrier,
+        // then every block subtracts sqrt(P) cm from its centroid mode.  The
+        // two removals of one launch use separate halves of cmpart.
+        double* cp = cmpart + (size_t)buf * nblocks;
+        double part = 0.0;
+        if (threadIdx.x < kNmTile && i0 + (int)threadIdx.x < s.N) part = sq[threadIdx.x];
+        const double tsum = block_sum(part, shred);
+        if (threadIdx.x == 0) cp[bid] = tsum;
+        if (!grid_barrier(bar, nblocks, s.err)) return false;
+        double acc = 0.0;
+        for (int k = threadIdx.x; k < gridDim.x; k += blockDim.x) acc += ((volatile double*)cp)[a * gridDim.x + k];
+        const double shift = block_sum(acc, shred) * cm_scale;  // sqrt(P) * cm
+        if (threadIdx.x < kNmTile) sq[threadIdx.x] -= shift;
+        __syncthreads();
+        return true;
+    };
+    if (tail) {
+        for (int e = threadIdx.x; e < P * kNmTile; e += blockDim.x) sq[e] += hdt * sg[e];
+        __syncthreads();
+        thermostat(2ull * (unsigned long long)(step - 1) + 1);
+        if (fixcom && !remove_com(0)) return;
+    }
+    if (head) {
+        thermostat(2ull * (unsigned long long)step);
+        if (fixcom && !remove_com(1)) return;
+        for (int k = g; k < P; k += 64) {
+            const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+            for (int h2 = 0; h2 < 2; ++h2) {
+                const int o = k * kNmTile + 2 * pp + h2;
+                const double q = sy[o];
+                const double pk = sq[o] + hdt * sg[o];
+                if (mw == 0.0) {
+                    sy[o] = q + s.dt / s.mass * pk;
+                    sq[o] = pk;
+                } else {
+                    sy[o] = cs * q + sn / mw * pk;
+                    sq[o] = -mw * sn * q + cs * pk;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int j = g; j < P; j += 64) {
+        double x0 = 0.0, x1 = 0.0, v0 = 0.0, v1 = 0.0;
+        const double* tj = T + (size_t)j * P;
+        for (int k = 0; k < P; ++k) {
+            const double c = tj[k];
+            const int o = k * kNmTile + 2 * pp;
+            v0 += c * sq[o];
+            v1 += c * sq[o + 1];
+            if (head) {
+                x0 += c * sy[o];
+                x1 += c * sy[o + 1];
+            }
+        }
+        const int ie = i0 + 2 * pp;
+        if (ie < s.N) {
+            const size_t o = idx<D>(s, j, a, ie);
+            s.p[o] = v0;
+            if (head) s.x[o] = x0;
+        }
+        if (ie + 1 < s.N) {
+            const size_t o = idx<D>(s, j, a, ie + 1);
+            s.p[o] = v1;
+            if (head) s.x[o] = x1;
+        }
+    }
+}
+
+size_t nm_fused_smem(const Sys& s) { return sizeof(double) * 6 * (size_t)s.P * kNmTile; }
+
+template <int D>
+static bool nm_fused_fits_t(const Sys& s) {
+    const size_t smem = nm_fused_smem(s);
+    if (smem > 200 * 1024) return false;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_nm_fused<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return false;
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nm_fused<D>, kNmThreads, smem) != cudaSuccess) return false;
+    const long long need = (long long)((s.N + kNmTile - 1) / kNmTile) * D;
+    return need <= (long long)per * sms;
+}
+
+bool nm_fused_fits(const Sys& s, int D) {
+    if (D == 1) return nm_fused_fits_t<1>(s);
+    if (D == 2) return nm_fused_fits_t<2>(s);
+    return nm_fused_fits_t<3>(s);
+}
+
+template <int D>
+static cudaError_t nm_fused_t(const Sys& s, const double* C, const double* T, const double* rot, double* cmpart,
+                              unsigned* bar, int mode, long long step, int fixcom, cudaStream_t st) {
+    dim3 grid((s.N + kNmTile - 1) / kNmTile, D);
+    Sys sc = s;
+    void* args[] = {&sc, &C, &T, &rot, &cmpart, &bar, &mode, &step, &fixcom};
+    return cudaLaunchCooperativeKernel((void*)k_nm_fused<D>, grid, dim3(kNmThreads), args, nm_fused_smem(s), st);
+}
+
+cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
+                            unsigned* bar, int mode, long long step, int fixcom, cudaStream_t st) {
+    if (D == 1) return nm_fused_t<1>(s, C, T, rot, cmpart, bar, mode, step, fixcom, st);
+    if (D == 2) return nm_fused_t<2>(s, C, T, rot, cmpart, bar, mode, step, fixcom, st);
+    return nm_fused_t<3>(s, C, T, rot, cmpart, bar, mode, step, fixcom, st);
+}
+
 // ------------------------------------------------------------------ launchers
 static int pack_grid(size_t n) {
     size_t g = (n + 255) / 256;

@@ -46,4 +46,12 @@ void launch_nm_thermo(const Sys& s, int D, const double* C, const double* T, int
 void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, const double* rot, int com_apply,
                          const double* red_in, int nred_in, cudaStream_t st);
 
+// Fused normal-mode step (normal-mode propagator + normal-mode Langevin):
+// mode bit 0 = tail of step-1 (kick, O, COM), bit 1 = head of step (O, COM,
+// kick, rotation).  Cooperative launch; nm_fused_fits tells whether every
+// block can be resident.
+bool nm_fused_fits(const Sys& s, int D);
+cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
+                            unsigned* bar, int mode, long long step, int fixcom, cudaStream_t st);
+
 }  // namespace pimdb

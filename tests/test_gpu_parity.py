@@ -96,16 +96,26 @@ TRAJ_CASES = {
                                ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
     "vv_langevin_dipole_2d": dict(ndim=2, natoms=20, nbeads=4, T_K=2.0, inter="dipole", int_p=(2.4799673e-4, 0, 0),
                                   ext="harmonic", ext_p=(1.0 * 0.036749326e-3, 0, 0), box_ang=40.0),
+    "nm_nmthermo_dist_nofixcom_odd_N": dict(natoms=13, nbeads=6, bosonic=False, propagator="normal_modes",
+                                            nmthermostat=True, fixcom=False, ext="harmonic",
+                                            ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    "nm_nmthermo_bosons_P16_2d": dict(ndim=2, natoms=24, nbeads=16, propagator="normal_modes", nmthermostat=True,
+                                      inter="dipole", int_p=(2.4799673e-4, 0, 0), ext="harmonic",
+                                      ext_p=(1.0 * 0.036749326e-3, 0, 0), box_ang=40.0),
 }
+# options applied to the GPU side only
+TRAJ_OPTIONS = {"nm_nmthermo_bosons_aziz": [{}, {"fused_normal_modes": 0}]}
 
 
-def _run_pair(kw, steps, seed_state=3):
+def _run_pair(kw, steps, seed_state=3, options=None):
     s, cfg = case(**kw)
     x = ring(s, seed=seed_state, spread_ang=0.2)
     p = momenta(s, seed_state)
     tr = O.Trajectory(s, x, p)
     frames = []
     with pk.System(cfg) as g:
+        for k, v in (options or {}).items():
+            g.set_option(k, v)
         g.set_state(x, p)
         g.set_step(0)
         for st in range(steps):
@@ -116,16 +126,17 @@ def _run_pair(kw, steps, seed_state=3):
     return frames
 
 
-@pytest.mark.parametrize("name", sorted(TRAJ_CASES))
-def test_trajectory_matches_oracle(name):
-    frames = _run_pair(TRAJ_CASES[name], steps=12)
+@pytest.mark.parametrize("name,options", [(n, o) for n in sorted(TRAJ_CASES) for o in TRAJ_OPTIONS.get(n, [{}])])
+def test_trajectory_matches_oracle(name, options):
+    frames = _run_pair(TRAJ_CASES[name], steps=12, options=options)
     for k, (want, got) in enumerate(frames):
         for w, gq, label in zip(want, got, "xpf"):
             assert rel_per_bead(gq, w) < 1e-9, (k, label, rel_per_bead(gq, w))
 
 
-def test_multi_step_call_equals_single_steps():
-    kw = TRAJ_CASES["vv_langevin_bosons_N16_P32"]
+@pytest.mark.parametrize("name", ["vv_langevin_bosons_N16_P32", "nm_nmthermo_bosons_aziz"])
+def test_multi_step_call_equals_single_steps(name):
+    kw = TRAJ_CASES[name]
     s, cfg = case(**kw)
     x = ring(s, seed=5, spread_ang=0.2)
     p = momenta(s, 5)
@@ -137,7 +148,7 @@ def test_multi_step_call_equals_single_steps():
             b.step(1)
         sa, sb = a.get_state(), b.get_state()
     for u, v in zip(sa, sb):
-        assert rel_per_bead(u, v) < 1e-13
+        assert rel_per_bead(u, v) < 1e-12
 
 
 def test_deterministic():
