@@ -196,7 +196,7 @@ static void nm_tables(int P, double omega_p, double mass, double dt, std::vector
 static void free_handle(pimdb_handle* h) {
     double* bufs[] = {h->s.x,   h->s.p,   h->s.f,   h->s.fphys, h->s.fx,   h->s.E,        h->s.V,
                       h->s.Vb,  h->s.scal, h->s.Vh, h->s.Vbh,  h->s.yf,   h->s.yb,       h->s.Wf,
-                      h->s.Wb,  h->s.rowR, h->s.rowC, h->d_C,  h->d_T,    h->d_rot,      h->d_red[0],
+                      h->s.Wb,  h->s.Et, h->s.rowR, h->s.rowC, h->d_C,  h->d_T,    h->d_rot,      h->d_red[0],
                       h->d_red[1], h->d_stage, h->d_part};
     for (double* b : bufs)
         if (b) cudaFree(b);
@@ -301,6 +301,7 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     if (e == cudaSuccess) e = alloc(&s.yb, (size_t)s.N + 1);
     if (e == cudaSuccess) e = alloc(&s.Wf, ntri);
     if (e == cudaSuccess) e = alloc(&s.Wb, ntri);
+    if (e == cudaSuccess) e = alloc(&s.Et, ntri);
     if (e == cudaSuccess) e = alloc(&s.rowR, (size_t)s.N);
     if (e == cudaSuccess) e = alloc(&s.rowC, (size_t)s.N);
     // Newton's-third-law pair tiles need P * ceil(N/32) * D * ld partial sums;

@@ -66,7 +66,8 @@ struct Sys {
     double* yf;     // y_m = exp(-beta (V_m - Vh_m)), N+1
     double* yb;     // y_l = exp(-beta (Vb_l - Vbh_l)), N+1
     double* Wf;     // forward weights, packed like E
-    double* Wb;     // backward weights, packed like E
+    double* Wb;     // backward weights, packed by backward node (see exchange.cu)
+    double* Et;     // E re-packed by backward node
     double* rowR;   // per-row factors exp(-beta (Vh[l+1] + Vb[l+1] - V[N])), N
     double* rowC;   // cut probabilities exp(-beta (V[l+1] + Vb[l+1] - V[N])), N
     int* xflags;    // [0] forward used the exact fallback, [1] backward, [2] completion counter

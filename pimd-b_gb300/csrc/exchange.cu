@@ -97,9 +97,15 @@ __global__ void k_exch_energies(Sys s) {
             const double y = __shfl_up_sync(0xffffffffu, term, o);
             if (lane >= o) term += y;
         }
-        if (u >= 0) row[u] = carry + term;
+        if (u >= 0) {
+            const double e = carry + term;
+            row[u] = e;
+            // backward node r = N - u depends on node r' = N - 1 - v
+            if (u >= 1) s.Et[tri(s.N - u - 1) + (s.N - 1 - v)] = e;
+        }
         carry += __shfl_sync(0xffffffffu, term, 31);
     }
+    if (lane == 0 && v >= 1) s.Et[tri(s.N - v - 1) + (s.N - 1 - v)] = row[v];
 }
 
 __device__ __forceinline__ void lse_add(float& mx, float& sm, float t) {
@@ -111,92 +117,127 @@ __device__ __forceinline__ void lse_add(float& mx, float& sm, float t) {
     }
 }
 
-// Depth of the register prefetch ring of the wavefront kernels: the operand
-// of round j + ring is loaded during round j, hiding the L2 latency.  Fewer
-// slots when each thread owns many levels, to stay within 64 registers.
-template <int K>
-struct Ring {
-    static constexpr int n = K <= 2 ? 8 : (K <= 4 ? 4 : 2);
-};
+// The recursions as "node" recursions.  Forward: node n = level m = n,
+// node 0 known (V = 0), node n depends on nodes u < n through the packed row
+// E[n-1][u].  Backward: node r = N - l, node 0 (l = N) known, node r depends
+// on nodes r' < r through Et[r-1][r'] = E[p][l] with p = N - 1 - r' (so
+// p + 1 = N - r').  Both are evaluated by the same blocked scheme: nodes are
+// taken 32 at a time; warp 0 resolves the 32 nodes of a block one after the
+// other with shuffles (no barrier), then every thread folds the finished
+// block into the accumulators of all later nodes (one barrier pair per 32
+// nodes instead of one barrier per node).
+constexpr int kWaveThreads = 256;
 
-// Pass 1: FP32 estimates, one block per direction.  Thread tid owns levels
-// tid+1+k*blockDim (k < K).  Skipped (early exit) when the previous
-// evaluation's exact V is still a good estimate (xflags[3] == 0).
-template <int K>
-__global__ void __launch_bounds__(1024) k_exch_estimate(Sys s) {
-    constexpr int RING = Ring<K>::n;
-    if (((volatile int*)s.xflags)[3] == 0) return;
-    extern __shared__ float vs[];  // N+1
-    const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
-    const float beta = (float)s.beta_ex;
-    float mx[K], sm[K], rg[RING][K];
-    int lv[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        lv[k] = tid + 1 + k * bd;
-        mx[k] = -CUDART_INF_F;
-        sm[k] = 0.0f;
+// FP32 log-sum-exp node recursion.  fwd: value(n) = -(LSE - log n)/beta;
+// bwd: terms carry -log(N - r') and value(r) = -LSE/beta.
+__device__ void blocked_estimate(const double* __restrict__ Eg, int nn, int N, float beta, bool fwd, float* val,
+                                 float* amx, float* asm_) {
+    const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    for (int n = tid; n < nn; n += bd) {
+        amx[n] = -CUDART_INF_F;
+        asm_[n] = 0.0f;
     }
+    __syncthreads();
+    const int nb = (nn + 31) / 32;
+    for (int b = 0; b < nb; ++b) {
+        const int base = 32 * b;
+        if (warp == 0) {
+            const int n = base + lane;
+            float mx = n < nn ? amx[n] : -CUDART_INF_F, sm = n < nn ? asm_[n] : 0.0f;
+            float e[32];
+#pragma unroll
+            for (int t = 0; t < 32; ++t) e[t] = (n < nn && n >= 1 && t < lane) ? (float)Eg[tri(n - 1) + base + t] : 0.0f;
+            float v = 0.0f;
+#pragma unroll
+            for (int t = 0; t < 32; ++t) {
+                if (lane == t && n < nn && n >= 1)
+                    v = -(mx + __logf(sm) - (fwd ? __logf((float)n) : 0.0f)) / beta;
+                const float vt = __shfl_sync(0xffffffffu, v, t);
+                if (lane > t && n < nn) {
+                    const int u = base + t;
+                    lse_add(mx, sm, -beta * (e[t] + vt) - (fwd ? 0.0f : __logf((float)(N - u))));
+                }
+            }
+            if (n < nn) val[n] = v;
+        }
+        __syncthreads();
+        for (int m = base + 32 + tid; m < nn; m += bd) {
+            float t[32];
+            float lmx = -CUDART_INF_F;
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                const int u = base + q;
+                t[q] = -beta * ((float)Eg[tri(m - 1) + u] + val[u]) - (fwd ? 0.0f : __logf((float)(N - u)));
+                lmx = fmaxf(lmx, t[q]);
+            }
+            float ls = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 32; ++q) ls += __expf(t[q] - lmx);
+            float mx = amx[m], sm = asm_[m];
+            if (lmx > mx) {
+                sm = sm * __expf(mx - lmx) + ls;
+                mx = lmx;
+            } else {
+                sm += ls * __expf(lmx - mx);
+            }
+            amx[m] = mx;
+            asm_[m] = sm;
+        }
+        __syncthreads();
+    }
+}
+
+// FP64 triangular node solve: y(0) = 1, y(n) = sum_{u<n} W[n-1][u] y(u).
+__device__ void blocked_solve(const double* __restrict__ W, int nn, double* y, double* acc) {
+    const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    for (int n = tid; n < nn; n += bd) acc[n] = 0.0;
+    __syncthreads();
+    const int nb = (nn + 31) / 32;
+    for (int b = 0; b < nb; ++b) {
+        const int base = 32 * b;
+        if (warp == 0) {
+            const int n = base + lane;
+            double a = n == 0 ? 1.0 : (n < nn ? acc[n] : 0.0);
+            double w[32];
+#pragma unroll
+            for (int t = 0; t < 32; ++t) w[t] = (n < nn && n >= 1 && t < lane) ? W[tri(n - 1) + base + t] : 0.0;
+#pragma unroll
+            for (int t = 0; t < 32; ++t) {
+                const double yt = __shfl_sync(0xffffffffu, a, t);
+                if (lane > t) a = fma(w[t], yt, a);
+            }
+            if (n < nn) y[n] = a;
+        }
+        __syncthreads();
+        for (int m = base + 32 + tid; m < nn; m += bd) {
+            const double* row = W + tri(m - 1) + base;
+            double sacc = acc[m];
+#pragma unroll 8
+            for (int q = 0; q < 32; ++q) sacc = fma(row[q], y[base + q], sacc);
+            acc[m] = sacc;
+        }
+        __syncthreads();
+    }
+}
+
+// Pass 1: FP32 estimates (block 0 forward, block 1 backward).  Skipped
+// (early exit) when the previous evaluation's exact potentials are still a
+// good estimate (xflags[3] == 0).
+__global__ void __launch_bounds__(kWaveThreads) k_exch_estimate(Sys s) {
+    if (((volatile int*)s.xflags)[3] == 0) return;
+    extern __shared__ float fsm[];  // 3 (N+1)
+    const int N = s.N;
+    float* val = fsm;
+    float* amx = fsm + (N + 1);
+    float* asm_ = fsm + 2 * (N + 1);
+    const float beta = (float)s.beta_ex;
     if (blockIdx.x == 0) {
-        // forward: level m has terms u = 0..m-1 with E[m-1][u] + V[u]
-        if (tid == 0) vs[0] = 0.0f;
-#pragma unroll
-        for (int r = 0; r < RING; ++r)
-#pragma unroll
-            for (int k = 0; k < K; ++k)
-                rg[r][k] = (lv[k] <= N && lv[k] > r) ? (float)s.E[tri(lv[k] - 1) + r] : 0.0f;
-        __syncthreads();
-        for (int j0 = 0; j0 < N; j0 += RING) {
-#pragma unroll
-            for (int r = 0; r < RING; ++r) {
-                const int j = j0 + r;
-                if (j < N) {
-                    const float vj = vs[j];
-#pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        if (lv[k] <= N && lv[k] > j) {
-                            lse_add(mx[k], sm[k], -beta * (rg[r][k] + vj));
-                            if (lv[k] == j + 1) vs[j + 1] = -(mx[k] + __logf(sm[k]) - __logf((float)lv[k])) / beta;
-                            if (lv[k] > j + RING) rg[r][k] = (float)s.E[tri(lv[k] - 1) + j + RING];
-                        }
-                    }
-                }
-                __syncthreads();
-            }
-        }
-        for (int m = tid; m <= N; m += bd) s.Vh[m] = (double)vs[m];
+        blocked_estimate(s.E, N + 1, N, beta, true, val, amx, asm_);
+        for (int m = threadIdx.x; m <= N; m += blockDim.x) s.Vh[m] = (double)val[m];
     } else {
-        // backward: level l (1..N-1) has terms p = l..N-1 with E[p][l] + Vb[p+1]
-        // and weight 1/(p+1); round q handles p = N-1-q
-        if (tid == 0) vs[N] = 0.0f;
-#pragma unroll
-        for (int r = 0; r < RING; ++r)
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const int p = N - 1 - r;
-                rg[r][k] = (p >= 1 && lv[k] <= p) ? (float)s.E[tri(p) + lv[k]] : 0.0f;
-            }
-        __syncthreads();
-        for (int q0 = 0; q0 < N - 1; q0 += RING) {
-#pragma unroll
-            for (int r = 0; r < RING; ++r) {
-                const int p = N - 1 - (q0 + r);
-                if (p >= 1) {
-                    const float vj = vs[p + 1];
-                    const float lj = __logf((float)(p + 1));
-#pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        if (lv[k] <= p) {
-                            lse_add(mx[k], sm[k], -beta * (rg[r][k] + vj) - lj);
-                            if (lv[k] == p) vs[p] = -(mx[k] + __logf(sm[k])) / beta;
-                            if (lv[k] <= p - RING) rg[r][k] = (float)s.E[tri(p - RING) + lv[k]];
-                        }
-                    }
-                }
-                __syncthreads();
-            }
-        }
-        for (int l = tid; l <= N; l += bd) s.Vbh[l] = (l >= 1) ? (double)vs[l] : 0.0;
+        // nodes r = 0..N-1 <-> l = N..1
+        blocked_estimate(s.Et, N, N, beta, false, val, amx, asm_);
+        for (int l = threadIdx.x; l <= N; l += blockDim.x) s.Vbh[l] = (l >= 1) ? (double)val[N - l] : 0.0;
     }
 }
 
@@ -210,7 +251,8 @@ __global__ void k_exch_weights(Sys s) {
     const double E = s.E[e];
     const double inv = 1.0 / (p + 1);
     s.Wf[e] = exp(-beta * (E + s.Vh[u] - s.Vh[p + 1])) * inv;
-    s.Wb[e] = u >= 1 ? exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u])) * inv : 0.0;
+    // backward node r = N - u from node r' = N - 1 - p (u >= 1)
+    if (u >= 1) s.Wb[tri(s.N - u - 1) + (s.N - 1 - p)] = exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u])) * inv;
 }
 
 // Exact level-by-level FP64 log-sum-exp in the reference's order (used only
@@ -259,56 +301,25 @@ constexpr double kExactLogY = 200.0;
 
 // Pass 3: y solves, exact V / V_backwards, and (by the block that finishes
 // last) the per-row factors of the connection probabilities.
-template <int K>
-__global__ void __launch_bounds__(1024) k_exch_solve(Sys s, int force_exact) {
-    constexpr int RING = Ring<K>::n;
-    extern __shared__ double ys[];  // N+1, then 32 for reductions
-    double* red = ys + s.N + 1;
+__global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_exact) {
+    extern __shared__ double ys[];  // y: N+1, acc: N+1, then 32 for reductions
+    double* acc = ys + s.N + 1;
+    double* red = ys + 2 * (s.N + 1);
     __shared__ int last_block;
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
     const double beta = s.beta_ex;
-    double acc[K], rg[RING][K];
-    int lv[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        lv[k] = tid + 1 + k * bd;
-        acc[k] = 0.0;
-    }
     int bad = force_exact, stale = 0;
     if (blockIdx.x == 0) {
-        if (tid == 0) ys[0] = 1.0;
         if (!force_exact) {
-#pragma unroll
-            for (int r = 0; r < RING; ++r)
-#pragma unroll
-                for (int k = 0; k < K; ++k) rg[r][k] = (lv[k] <= N && lv[k] > r) ? s.Wf[tri(lv[k] - 1) + r] : 0.0;
-        }
-        __syncthreads();
-        for (int j0 = 0; j0 < (force_exact ? 0 : N); j0 += RING) {
-#pragma unroll
-            for (int r = 0; r < RING; ++r) {
-                const int j = j0 + r;
-                if (j < N) {
-                    const double yj = ys[j];
-#pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        if (lv[k] <= N && lv[k] > j) {
-                            acc[k] = fma(rg[r][k], yj, acc[k]);
-                            if (lv[k] == j + 1) ys[j + 1] = acc[k];
-                            if (lv[k] > j + RING) rg[r][k] = s.Wf[tri(lv[k] - 1) + j + RING];
-                        }
-                    }
-                }
-                __syncthreads();
+            blocked_solve(s.Wf, N + 1, ys, acc);
+            for (int m = tid; m <= N; m += bd) {
+                const double y = ys[m];
+                const double ly = log(y);
+                if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
+                if (!(fabs(ly) < kRefreshLogY)) stale = 1;
+                s.yf[m] = y;
+                s.V[m] = s.Vh[m] - ly / beta;
             }
-        }
-        for (int m = tid; m <= N && !force_exact; m += bd) {
-            const double y = ys[m];
-            const double ly = log(y);
-            if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
-            if (!(fabs(ly) < kRefreshLogY)) stale = 1;
-            s.yf[m] = y;
-            s.V[m] = s.Vh[m] - ly / beta;
         }
         bad = __syncthreads_or(bad);
         if (bad) {
@@ -327,48 +338,21 @@ __global__ void __launch_bounds__(1024) k_exch_solve(Sys s, int force_exact) {
             if (nonfinite) atomicOr(s.err, ERRB_NONFINITE_VB);
         }
     } else {
-        if (tid == 0) ys[N] = 1.0;
         if (!force_exact) {
-#pragma unroll
-            for (int r = 0; r < RING; ++r)
-#pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    const int p = N - 1 - r;
-                    rg[r][k] = (p >= 1 && lv[k] <= p) ? s.Wb[tri(p) + lv[k]] : 0.0;
-                }
-        }
-        __syncthreads();
-        for (int q0 = 0; q0 < (force_exact ? 0 : N - 1); q0 += RING) {
-#pragma unroll
-            for (int r = 0; r < RING; ++r) {
-                const int p = N - 1 - (q0 + r);
-                if (p >= 1) {
-                    const double yj = ys[p + 1];
-#pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        if (lv[k] <= p) {
-                            acc[k] = fma(rg[r][k], yj, acc[k]);
-                            if (lv[k] == p) ys[p] = acc[k];
-                            if (lv[k] <= p - RING) rg[r][k] = s.Wb[tri(p - RING) + lv[k]];
-                        }
-                    }
-                }
-                __syncthreads();
+            // nodes r = 0..N-1 <-> levels l = N..1
+            blocked_solve(s.Wb, N, ys, acc);
+            for (int l = tid + 1; l < N; l += bd) {
+                const double y = ys[N - l];
+                const double ly = log(y);
+                if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
+                if (!(fabs(ly) < kRefreshLogY)) stale = 1;
+                s.yb[l] = y;
+                s.Vb[l] = s.Vbh[l] - ly / beta;
             }
         }
-        for (int l = tid + 1; l <= N; l += bd) {
-            if (l == N) {
-                s.Vb[N] = 0.0;
-                s.yb[N] = 1.0;
-                continue;
-            }
-            if (force_exact) continue;
-            const double y = ys[l];
-            const double ly = log(y);
-            if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
-            if (!(fabs(ly) < kRefreshLogY)) stale = 1;
-            s.yb[l] = y;
-            s.Vb[l] = s.Vbh[l] - ly / beta;
+        if (tid == 0) {
+            s.Vb[N] = 0.0;
+            s.yb[N] = 1.0;
         }
         bad = __syncthreads_or(bad);
         if (bad) {
@@ -539,11 +523,6 @@ __global__ void k_exch_estimators(Sys s, int nbeads) {
     }
 }
 
-static int wave_threads(int N) {
-    int t = ((N + 31) / 32) * 32;
-    return t > 1024 ? 1024 : (t < 32 ? 32 : t);
-}
-
 void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
     const int warps = 2;
     dim3 grid((s.N + warps - 1) / warps);
@@ -552,30 +531,19 @@ void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
     else k_exch_energies<3><<<grid, warps * 32, 0, st>>>(s);
 }
 
-template <int K>
-static int recursions_k(const Sys& s, int threads, int exact, cudaStream_t st) {
+int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st) {
     if (!exact) {
-        const size_t esmem = sizeof(float) * (size_t)(s.N + 1);
+        const size_t esmem = sizeof(float) * 3 * (size_t)(s.N + 1);
         if (esmem > 48 * 1024)
-            cudaFuncSetAttribute(k_exch_estimate<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
-        k_exch_estimate<K><<<2, threads, esmem, st>>>(s);
+            cudaFuncSetAttribute(k_exch_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
+        k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s);
         dim3 wgrid((s.N + 255) / 256, s.N);
         k_exch_weights<<<wgrid, 256, 0, st>>>(s);
     }
-    const size_t smem = sizeof(double) * (size_t)(s.N + 1 + 32);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_exch_solve<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_exch_solve<K><<<2, threads, smem, st>>>(s, exact);
+    const size_t smem = sizeof(double) * (2 * (size_t)(s.N + 1) + 32);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_exch_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, exact);
     return exact ? 1 : 3;
-}
-
-int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st) {
-    const int threads = wave_threads(s.N);
-    const int per = (s.N + threads - 1) / threads;
-    if (per <= 1) return recursions_k<1>(s, threads, exact, st);
-    if (per <= 2) return recursions_k<2>(s, threads, exact, st);
-    if (per <= 4) return recursions_k<4>(s, threads, exact, st);
-    if (per <= 8) return recursions_k<8>(s, threads, exact, st);
-    return recursions_k<16>(s, threads, exact, st);
 }
 
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st) {
