@@ -363,6 +363,148 @@ __global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ 
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP64 pair tiles with lane compaction (plain path with a finite cutoff).
+// A warp-instruction on the FP64 pipe costs the same whether or not its lanes
+// are active, so evaluating the Aziz gradient only in the lanes whose pair is
+// inside the cutoff wastes the pipe on the others.  Each warp therefore
+//   1. screens its tile's pairs with FP32 distances and records, per i lane,
+//      the j's inside the cutoff (plus a small margin), and per j lane the
+//      (i, position) of those entries;
+//   2. lays the entries out i-major and evaluates them 32 at a time in FP64,
+//      every lane busy, storing each gradient in shared memory;
+//   3. sums the gradients per i and per j in list order (deterministic).
+// Same result as k_pair_tiles; the exact FP64 cutoff test is applied in step 2.
+constexpr int kCompactWarps = 2;
+
+template <int D>
+struct CompactSmem {
+    double xi[kTile][D], xj[kTile][D];
+    double g[kTile * kTile][D];
+    unsigned char ilist[kTile][kTile];     // j's of lane i
+    unsigned short jlist[kTile][kTile];    // (i << 8 | k) entries of lane j
+    int icnt[kTile], jcnt[kTile], off[kTile];
+    unsigned char fi[kTile * kTile], fj[kTile * kTile];
+};
+
+template <int D>
+__global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s, double* __restrict__ part, int T,
+                                                                          int npairs) {
+    extern __shared__ __align__(16) unsigned char csm_raw[];
+    CompactSmem<D>& sm = reinterpret_cast<CompactSmem<D>*>(csm_raw)[threadIdx.x >> 5];
+    const int w = blockIdx.x * kCompactWarps + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.y;
+    if (w >= npairs) return;
+    int it = (int)((2.0 * T + 1.0 - sqrt((2.0 * T + 1.0) * (2.0 * T + 1.0) - 8.0 * w)) * 0.5);
+    while (it > 0 && it * T - it * (it - 1) / 2 > w) --it;
+    while ((it + 1) * T - (it + 1) * it / 2 <= w) ++it;
+    const int jt = it + (w - (it * T - it * (it - 1) / 2));
+    const bool diag = it == jt;
+    const int i = it * kTile + lane, j = jt * kTile + lane;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        sm.xi[lane][a] = i < s.N ? s.x[idx<D>(s, b, a, i)] : 0.0;
+        sm.xj[lane][a] = j < s.N ? s.x[idx<D>(s, b, a, j)] : 0.0;
+    }
+    sm.icnt[lane] = 0;
+    sm.jcnt[lane] = 0;
+    __syncwarp();
+    // 1. FP32 screen, one rotation step at a time (lane i meets j = i + st)
+    const double cut = s.cutoff;
+    const float cut2f = (float)(cut * cut) * 1.0001f;
+    const float Lf = (float)s.L, invLf = (float)s.invL;
+    float xif[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xif[a] = (float)sm.xi[lane][a];
+    int icnt = 0;
+    const int first = diag ? 1 : 0, lastS = diag ? 16 : 31;
+    for (int st = first; st <= lastS; ++st) {
+        const int jl = (lane + st) & 31;
+        bool in = i < s.N && jt * kTile + jl < s.N && (!diag || st < 16 || lane < 16);
+        if (in) {
+            float r2 = 0.0f;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                float d = xif[a] - (float)sm.xj[jl][a];
+                if (s.pbc) d = min_image_f(d, Lf, invLf);
+                r2 += d * d;
+            }
+            in = r2 <= cut2f;
+        }
+        if (in) {
+            const int jc = sm.jcnt[jl];  // lanes of one step hit distinct j's
+            sm.jlist[jl][jc] = (unsigned short)((lane << 8) | icnt);
+            sm.jcnt[jl] = jc + 1;
+            sm.ilist[lane][icnt++] = (unsigned char)jl;
+        }
+        __syncwarp();
+    }
+    sm.icnt[lane] = icnt;
+    // 2. i-major layout: offsets by a warp scan of the counts
+    int off = icnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, off, o);
+        if (lane >= o) off += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, off, 31);
+    off -= icnt;
+    sm.off[lane] = off;
+    for (int k = 0; k < icnt; ++k) {
+        sm.fi[off + k] = (unsigned char)lane;
+        sm.fj[off + k] = sm.ilist[lane][k];
+    }
+    __syncwarp();
+    for (int f = lane; f < total; f += 32) {
+        const int il = sm.fi[f], jl = sm.fj[f];
+        double r[D];
+        double r2 = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double d = sm.xi[il][a] - sm.xj[jl][a];
+            if (s.pbc) d = min_image(d, s.L, s.invL);
+            r[a] = d;
+            r2 += d * d;
+        }
+        const double sc = r2 < cut * cut ? pair_scale<double>(s.int_kind, r2, s.int_a) : 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) sm.g[f][a] = sc * r[a];  // grad V(r_i - r_j)
+    }
+    __syncwarp();
+    // 3. deterministic sums: i side over its own (contiguous) entries, j side
+    //    over its list in recording order
+    double ai[D], aj[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) ai[a] = aj[a] = 0.0;
+    for (int k = 0; k < icnt; ++k)
+#pragma unroll
+        for (int a = 0; a < D; ++a) ai[a] -= sm.g[off + k][a];
+    const int jc = sm.jcnt[lane];
+    for (int k = 0; k < jc; ++k) {
+        const int e = sm.jlist[lane][k];
+        const int f = sm.off[e >> 8] + (e & 255);
+#pragma unroll
+        for (int a = 0; a < D; ++a) aj[a] += sm.g[f][a];
+    }
+    const size_t base_b = (size_t)b * T;
+    if (diag) {
+        if (i < s.N) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) part[((base_b + it) * D + a) * s.ld + i] = ai[a] + aj[a];
+        }
+    } else {
+        if (i < s.N) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) part[((base_b + jt) * D + a) * s.ld + i] = ai[a];
+        }
+        if (j < s.N) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) part[((base_b + it) * D + a) * s.ld + j] = aj[a];
+        }
+    }
+}
+
 // f = springs + (-grad V_ext + sum of the pair slots), one thread per
 // (bead, axis, particle).  T = 0 when there are no pair forces.
 template <int D>
@@ -406,9 +548,20 @@ static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, 
     const int T = pairs ? (s.N + kTile - 1) / kTile : 0;
     if (pairs) {
         const int np = T * (T + 1) / 2;
-        dim3 grid((np + 3) / 4, s.P);
-        if (mixed) k_pair_tiles<D, float><<<grid, 128, 0, st>>>(s, part, T, np);
-        else k_pair_tiles<D, double><<<grid, 128, 0, st>>>(s, part, T, np);
+        if (!mixed && s.cutoff > 0.0) {
+            const size_t smem = sizeof(CompactSmem<D>) * kCompactWarps;
+            static bool attr = false;
+            if (!attr) {
+                cudaFuncSetAttribute(k_pair_tiles_compact<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                attr = true;
+            }
+            dim3 grid((np + kCompactWarps - 1) / kCompactWarps, s.P);
+            k_pair_tiles_compact<D><<<grid, 32 * kCompactWarps, smem, st>>>(s, part, T, np);
+        } else {
+            dim3 grid((np + 3) / 4, s.P);
+            if (mixed) k_pair_tiles<D, float><<<grid, 128, 0, st>>>(s, part, T, np);
+            else k_pair_tiles<D, double><<<grid, 128, 0, st>>>(s, part, T, np);
+        }
     }
     const size_t n = (size_t)s.P * D * s.ld;
     k_bead_finish<D><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, part, T, write_phys);
