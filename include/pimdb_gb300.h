@@ -175,7 +175,10 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
  *                    run the thermostat and the propagator as separate
  *                    kernels in the reference's order instead of the fused
  *                    normal-mode-frame kernel (default 1 when all its blocks
- *                    fit on the GPU at once). */
+ *                    fit on the GPU at once);
+ *   "fft_normal_modes" 0: in the fused kernel, transform with the P x P
+ *                    matrices instead of FFTs (FFTs are used when P is a
+ *                    power of two; default 1). */
 int pimdb_set_option(pimdb_handle* h, const char* name, int value);
 
 /* Measures the FP64 fused-multiply-add throughput of the current device in

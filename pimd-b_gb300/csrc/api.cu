@@ -47,6 +47,9 @@ struct pimdb_handle {
     bool nm_tail_pending = false;
     double* d_cmpart = nullptr;
     unsigned* d_bar = nullptr;
+    double* d_tw = nullptr;   // FFT twiddles (P/2 complex) when P is a power of two
+    int logP = 0;
+    int opt_fft = 1;
     cudaError_t async_err = cudaSuccess;
     int opt_newton3 = 1;
     bool profile = false;
@@ -204,6 +207,7 @@ static void free_handle(pimdb_handle* h) {
     if (h->s.xflags) cudaFree(h->s.xflags);
     if (h->d_cmpart) cudaFree(h->d_cmpart);
     if (h->d_bar) cudaFree(h->d_bar);
+    if (h->d_tw) cudaFree(h->d_tw);
     if (h->fork_ev) cudaEventDestroy(h->fork_ev);
     if (h->join_ev) cudaEventDestroy(h->join_ev);
     if (h->side) cudaStreamDestroy(h->side);
@@ -342,6 +346,18 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
         if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_bar, 2 * sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMemset(h->d_bar, 0, 2 * sizeof(unsigned));
         h->fused_nm = (e == cudaSuccess);
+        const int P = s.P;
+        if (e == cudaSuccess && P >= 2 && (P & (P - 1)) == 0) {
+            std::vector<double> tw((size_t)P);
+            const double pi = 3.14159265358979323846;
+            for (int t = 0; t < P / 2; ++t) {
+                tw[2 * t] = std::cos(2 * pi * t / P);
+                tw[2 * t + 1] = -std::sin(2 * pi * t / P);
+            }
+            e = alloc(&h->d_tw, (size_t)P);
+            if (e == cudaSuccess) e = cudaMemcpy(h->d_tw, tw.data(), (size_t)P * sizeof(double), cudaMemcpyHostToDevice);
+            while ((1 << h->logP) < P) ++h->logP;
+        }
     }
     cudaGetLastError();
     s.err = h->d_err;
@@ -550,7 +566,8 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
             const long long st = h->step;
             launch(h, PIMDB_K_NM_PROPAGATE, [&] {
                 cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, mode, st,
-                                                c.fixcom, h->stream);
+                                                c.fixcom, h->opt_fft ? (const double2*)h->d_tw : nullptr, h->logP,
+                                                h->stream);
                 if (e != cudaSuccess) h->async_err = e;
             });
             enqueue_forces(h);
@@ -578,7 +595,8 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
         const long long st = h->step;
         launch(h, PIMDB_K_NM_PROPAGATE, [&] {
             cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, 1, st,
-                                            h->cfg.fixcom, h->stream);
+                                            h->cfg.fixcom, h->opt_fft ? (const double2*)h->d_tw : nullptr, h->logP,
+                                            h->stream);
             if (e != cudaSuccess) h->async_err = e;
         });
         h->nm_tail_pending = false;
@@ -718,6 +736,7 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
     const std::string n(name);
     if (n == "exact_exchange") h->opt_exact_exchange = value ? 1 : 0;
     else if (n == "fused_normal_modes") h->fused_nm = value && h->d_cmpart != nullptr;
+    else if (n == "fft_normal_modes") h->opt_fft = value ? 1 : 0;
     else if (n == "newton3") h->opt_newton3 = value ? 1 : 0;
     else return fail(h, PIMDB_ERR_ARG, "unknown option " + n);
     return PIMDB_OK;

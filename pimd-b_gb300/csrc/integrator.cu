@@ -279,6 +279,120 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
 }
 
 // ---------------------------------------------------------------------------
+// Normal-mode transforms by FFT (P a power of two).  C's rows are the scaled
+// real DFT: for X_k = sum_b x_b exp(-2 pi i k b / P),
+//   q_0 = X_0 / sqrt(P), q_{P/2} = X_{P/2} / sqrt(P),
+//   q_k = sqrt(2/P) Re X_k (0 < k < P/2), q_k = sqrt(2/P) Im X_k (k > P/2)
+// (with Im X_{P-k} = -Im X_k for real input)
+// (normal_modes.cpp:52-79).  Two particles share one complex FFT (real and
+// imaginary parts); radix-2 Stockham stages in shared memory with twiddles
+// tw[t] = exp(-2 pi i t / P), t < P/2.  The inverse builds the Hermitian
+// spectra of C^T and runs the conjugate transform.
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// One Stockham radix-2 pass structure for `nf` transforms; stage 0 gets its
+// operands from `load(f, b)`.  Returns the buffer holding out[f * P + k].
+template <class Load>
+__device__ double2* fft_stages(Load load, int nf, int P, int logP, const double2* __restrict__ tw, bool inv,
+                               double2* w0, double2* w1) {
+    const int half = P >> 1;
+    const double2* src = nullptr;
+    double2* dst = w0;
+    for (int st = 0, Ns = 1; st < logP; ++st, Ns <<= 1) {
+        for (int e = threadIdx.x; e < nf * half; e += blockDim.x) {
+            const int f = e / half, j = e - f * half;
+            double2 v0, v1;
+            if (st == 0) {
+                v0 = load(f, j);
+                v1 = load(f, j + half);
+            } else {
+                v0 = src[f * P + j];
+                v1 = src[f * P + j + half];
+            }
+            const int k = j & (Ns - 1);
+            double2 t = tw[k * (half / Ns)];
+            if (inv) t.y = -t.y;
+            const double2 bb = cmul(v1, t);
+            const int o = f * P + (j - k) * 2 + k;
+            dst[o] = make_double2(v0.x + bb.x, v0.y + bb.y);
+            dst[o + Ns] = make_double2(v0.x - bb.x, v0.y - bb.y);
+        }
+        __syncthreads();
+        src = dst;
+        dst = (dst == w0) ? w1 : w0;
+    }
+    return const_cast<double2*>(src);
+}
+
+// in[n] -> out[n] for n < narr: arrays of [P][kNmTile] doubles (bead or mode major).
+struct NmArrays {
+    const double* in[3];
+    double* out[3];
+};
+
+__device__ void nm_forward_fft(const NmArrays& ar, int narr, int P, int logP, const double2* __restrict__ tw,
+                               double2* w0, double2* w1) {
+    const int nf = narr * (kNmTile / 2);
+    auto load = [&](int f, int b) {
+        const double* a = ar.in[f / (kNmTile / 2)] + 2 * (f % (kNmTile / 2));
+        return make_double2(a[b * kNmTile], a[b * kNmTile + 1]);
+    };
+    const double2* R = fft_stages(load, nf, P, logP, tw, false, w0, w1);
+    const int half = P >> 1;
+    const double c = sqrt(2.0 / P), c0 = 1.0 / sqrt((double)P);
+    for (int e = threadIdx.x; e < nf * (half + 1); e += blockDim.x) {
+        const int f = e / (half + 1), k = e - f * (half + 1);
+        const double2 Zk = R[f * P + k], Zm = R[f * P + ((P - k) & (P - 1))];
+        const double xar = 0.5 * (Zk.x + Zm.x), xai = 0.5 * (Zk.y - Zm.y);
+        const double xbr = 0.5 * (Zk.y + Zm.y), xbi = 0.5 * (Zm.x - Zk.x);
+        double* o = ar.out[f / (kNmTile / 2)] + 2 * (f % (kNmTile / 2));
+        if (k == 0 || k == half) {
+            o[k * kNmTile] = c0 * xar;
+            o[k * kNmTile + 1] = c0 * xbr;
+        } else {
+            o[k * kNmTile] = c * xar;
+            o[k * kNmTile + 1] = c * xbr;
+            // q_{P-k} = sqrt(2/P) Im X_{P-k} = -sqrt(2/P) Im X_k (real input)
+            o[(P - k) * kNmTile] = -c * xai;
+            o[(P - k) * kNmTile + 1] = -c * xbi;
+        }
+    }
+    __syncthreads();
+}
+
+// Normal modes -> Cartesian for ar.in[0..narr); result[f * P + j] = x_a + i x_b
+// for particles 2 (f % 4), 2 (f % 4) + 1 of array f / 4.
+__device__ const double2* nm_inverse_fft(const NmArrays& ar, int narr, int P, int logP,
+                                         const double2* __restrict__ tw, double2* w0, double2* w1) {
+    const int nf = narr * (kNmTile / 2);
+    const int half = P >> 1;
+    const double c = 0.5 * sqrt(2.0 / P), c0 = 1.0 / sqrt((double)P);
+    auto load = [&](int f, int k) {
+        const double* a = ar.in[f / (kNmTile / 2)] + 2 * (f % (kNmTile / 2));
+        double zar, zai, zbr, zbi;
+        if (k == 0 || k == half) {
+            zar = c0 * a[k * kNmTile];
+            zbr = c0 * a[k * kNmTile + 1];
+            zai = zbi = 0.0;
+        } else if (k < half) {
+            zar = c * a[k * kNmTile];
+            zai = -c * a[(P - k) * kNmTile];
+            zbr = c * a[k * kNmTile + 1];
+            zbi = -c * a[(P - k) * kNmTile + 1];
+        } else {
+            zar = c * a[(P - k) * kNmTile];
+            zai = c * a[k * kNmTile];
+            zbr = c * a[(P - k) * kNmTile + 1];
+            zbi = c * a[k * kNmTile + 1];
+        }
+        return make_double2(zar - zbi, zai + zbr);
+    };
+    return fft_stages(load, nf, P, logP, tw, true, w0, w1);
+}
+
+// ---------------------------------------------------------------------------
 // Fused normal-mode step for the normal-mode propagator with the
 // normal-mode Langevin thermostat.  Between two force evaluations the
 // reference applies (normal_modes_propagator.cpp:19-103,
@@ -327,7 +441,8 @@ template <int D>
 __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __restrict__ C,
                                                          const double* __restrict__ T,
                                                          const double* __restrict__ rot, double* cmpart,
-                                                         unsigned* bar, int mode, long long step, int fixcom) {
+                                                         unsigned* bar, int mode, long long step, int fixcom,
+                                                         const double2* __restrict__ tw, int logP) {
     extern __shared__ double sm[];
     __shared__ double shred[32];
     const int P = s.P;
@@ -357,6 +472,12 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
         sf[e] = f;
     }
     __syncthreads();
+    double2* w0 = reinterpret_cast<double2*>(sm + 6 * P * kNmTile);
+    double2* w1 = w0 + 3 * (kNmTile / 2) * P;
+    if (tw) {
+        NmArrays ar = {{sp, sf, sx}, {sq, sg, sy}};
+        nm_forward_fft(ar, head ? 3 : 2, P, logP, tw, w0, w1);
+    } else {
     for (int k = g; k < P; k += 64) {
         double q0 = 0.0, q1 = 0.0, f0 = 0.0, f1 = 0.0, x0 = 0.0, x1 = 0.0;
         const double* ck = C + (size_t)k * P;
@@ -381,6 +502,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
         sy[o + 1] = x1;
     }
     __syncthreads();
+    }
     const int half = (s.N + 1) / 2;
     const double hdt = 0.5 * s.dt;
     const double sqrtP = sqrt((double)P);
@@ -439,6 +561,28 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
         }
         __syncthreads();
     }
+    if (tw) {
+        NmArrays ar = {{sq, sy, nullptr}, {nullptr, nullptr, nullptr}};
+        const double2* R = nm_inverse_fft(ar, head ? 2 : 1, P, logP, tw, w0, w1);
+        for (int e = threadIdx.x; e < P * (kNmTile / 2); e += blockDim.x) {
+            const int j = e / (kNmTile / 2), q = e % (kNmTile / 2);
+            const int ie = i0 + 2 * q;
+            const double2 pv = R[q * P + j];
+            double2 xv = make_double2(0.0, 0.0);
+            if (head) xv = R[((kNmTile / 2) + q) * P + j];
+            if (ie < s.N) {
+                const size_t o = idx<D>(s, j, a, ie);
+                s.p[o] = pv.x;
+                if (head) s.x[o] = xv.x;
+            }
+            if (ie + 1 < s.N) {
+                const size_t o = idx<D>(s, j, a, ie + 1);
+                s.p[o] = pv.y;
+                if (head) s.x[o] = xv.y;
+            }
+        }
+        return;
+    }
     for (int j = g; j < P; j += 64) {
         double x0 = 0.0, x1 = 0.0, v0 = 0.0, v1 = 0.0;
         const double* tj = T + (size_t)j * P;
@@ -466,7 +610,10 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
     }
 }
 
-size_t nm_fused_smem(const Sys& s) { return sizeof(double) * 6 * (size_t)s.P * kNmTile; }
+// [6][P][8] arrays plus two FFT work buffers of 12 complex transforms
+size_t nm_fused_smem(const Sys& s) {
+    return sizeof(double) * (6 * (size_t)s.P * kNmTile + 2 * 2 * 3 * (kNmTile / 2) * (size_t)s.P);
+}
 
 template <int D>
 static bool nm_fused_fits_t(const Sys& s) {
@@ -491,18 +638,20 @@ bool nm_fused_fits(const Sys& s, int D) {
 
 template <int D>
 static cudaError_t nm_fused_t(const Sys& s, const double* C, const double* T, const double* rot, double* cmpart,
-                              unsigned* bar, int mode, long long step, int fixcom, cudaStream_t st) {
+                              unsigned* bar, int mode, long long step, int fixcom, const double2* tw, int logP,
+                              cudaStream_t st) {
     dim3 grid((s.N + kNmTile - 1) / kNmTile, D);
     Sys sc = s;
-    void* args[] = {&sc, &C, &T, &rot, &cmpart, &bar, &mode, &step, &fixcom};
+    void* args[] = {&sc, &C, &T, &rot, &cmpart, &bar, &mode, &step, &fixcom, &tw, &logP};
     return cudaLaunchCooperativeKernel((void*)k_nm_fused<D>, grid, dim3(kNmThreads), args, nm_fused_smem(s), st);
 }
 
 cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
-                            unsigned* bar, int mode, long long step, int fixcom, cudaStream_t st) {
-    if (D == 1) return nm_fused_t<1>(s, C, T, rot, cmpart, bar, mode, step, fixcom, st);
-    if (D == 2) return nm_fused_t<2>(s, C, T, rot, cmpart, bar, mode, step, fixcom, st);
-    return nm_fused_t<3>(s, C, T, rot, cmpart, bar, mode, step, fixcom, st);
+                            unsigned* bar, int mode, long long step, int fixcom, const double2* tw, int logP,
+                            cudaStream_t st) {
+    if (D == 1) return nm_fused_t<1>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
+    if (D == 2) return nm_fused_t<2>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
+    return nm_fused_t<3>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
 }
 
 // ------------------------------------------------------------------ launchers

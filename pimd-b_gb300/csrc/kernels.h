@@ -51,7 +51,10 @@ void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, 
 // kick, rotation).  Cooperative launch; nm_fused_fits tells whether every
 // block can be resident.
 bool nm_fused_fits(const Sys& s, int D);
+// `tw` (P/2 twiddles exp(-2 pi i t/P)) selects the FFT transforms (P a power
+// of two, logP = log2 P); NULL selects the P x P matrix products.
 cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
-                            unsigned* bar, int mode, long long step, int fixcom, cudaStream_t st);
+                            unsigned* bar, int mode, long long step, int fixcom, const double2* tw, int logP,
+                            cudaStream_t st);
 
 }  // namespace pimdb

@@ -104,7 +104,7 @@ TRAJ_CASES = {
                                       ext_p=(1.0 * 0.036749326e-3, 0, 0), box_ang=40.0),
 }
 # options applied to the GPU side only
-TRAJ_OPTIONS = {"nm_nmthermo_bosons_aziz": [{}, {"fused_normal_modes": 0}]}
+TRAJ_OPTIONS = {"nm_nmthermo_bosons_aziz": [{}, {"fused_normal_modes": 0}, {"fft_normal_modes": 0}]}
 
 
 def _run_pair(kw, steps, seed_state=3, options=None):
