@@ -534,14 +534,14 @@ void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
 int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st) {
     if (!exact) {
         const size_t esmem = sizeof(float) * 3 * (size_t)(s.N + 1);
-        if (esmem > 48 * 1024)
+        if (esmem + 1024 > 48 * 1024)
             cudaFuncSetAttribute(k_exch_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
         k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s);
         dim3 wgrid((s.N + 255) / 256, s.N);
         k_exch_weights<<<wgrid, 256, 0, st>>>(s);
     }
     const size_t smem = sizeof(double) * (2 * (size_t)(s.N + 1) + 32);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_exch_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem + 1024 > 48 * 1024) cudaFuncSetAttribute(k_exch_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, exact);
     return exact ? 1 : 3;
 }
@@ -558,7 +558,7 @@ void launch_exchange_estimators(const Sys& s, cudaStream_t st) {
     const size_t smem = sizeof(double) * (size_t)(s.N + 1 + 32);
     int t = ((s.N + 31) / 32) * 32;
     t = t > 512 ? 512 : (t < 32 ? 32 : t);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_exch_estimators, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem + 1024 > 48 * 1024) cudaFuncSetAttribute(k_exch_estimators, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_exch_estimators<<<1, t, smem, st>>>(s, s.P);
 }
 

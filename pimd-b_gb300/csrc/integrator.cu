@@ -619,8 +619,9 @@ template <int D>
 static bool nm_fused_fits_t(const Sys& s) {
     const size_t smem = nm_fused_smem(s);
     if (smem > 200 * 1024) return false;
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_nm_fused<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    // the kernel also has static shared memory, so opt in whenever the dynamic
+    // part alone reaches the 48 KiB default
+    if (cudaFuncSetAttribute(k_nm_fused<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return false;
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
