@@ -181,6 +181,31 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
  *                    power of two; default 1). */
 int pimdb_set_option(pimdb_handle* h, const char* name, int value);
 
+/* Bosonic exchange without any allocation (no counterpart in the reference).
+ * For callers that may not call cudaMalloc while they need the exchange: an
+ * engine holding a CUDA stream capture open across its step, a program whose
+ * device memory belongs to another allocator or a fixed budget, or a loop
+ * that cannot afford cudaMalloc's implicit device synchronisation.
+ * Inputs and outputs are device memory supplied by the caller:
+ *   ring       x[bead][particle][axis] of all `nbeads` beads (only beads 1, 2,
+ *              P-1 and P are read), atomic units;
+ *   scalars    4 doubles: V_B, primEstimator, P_distinct, P_longest (as
+ *              pimdb_exchange);
+ *   f_first, f_last  exterior spring forces on beads 1 and P, [particle][axis]
+ *              (either may be NULL).
+ * spring_constant = m omega_P^2 and beta_ex = beta/P as in the reference.
+ * All intermediate arrays live in one fixed __device__ array of about 1.1 MB
+ * that every GPU loading the library keeps until the process exits; hence at
+ * most 256 particles (larger natoms returns PIMDB_ERR_ARG and a message in
+ * err).  The first call on a device looks up that array's device address, so
+ * make it before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU (different streams or host threads) race.  The call runs
+ * on `cuda_stream` (NULL = legacy default stream) and returns after it is
+ * done, reporting a non-finite V_B as PIMDB_ERR_NONFINITE_VB. */
+int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms, int ndim, double spring_constant,
+                           double beta_ex, int pbc, double box, double* scalars, double* f_first, double* f_last,
+                           void* cuda_stream, char* err, int err_len);
+
 /* Measures the FP64 fused-multiply-add throughput of the current device in
  * TFLOP/s (the roofline denominator of the FP64 kernels). */
 int pimdb_measure_fp64_peak(double* tflops);

@@ -20,7 +20,7 @@ BUILD = HERE / "_build"
 LIB = HERE / "libpimdb_gb300.so"
 CLI = HERE / "pimdb_gb300"
 
-CU_SOURCES = ["csrc/forces.cu", "csrc/exchange.cu", "csrc/integrator.cu", "csrc/api.cu"]
+CU_SOURCES = ["csrc/forces.cu", "csrc/exchange.cu", "csrc/integrator.cu", "csrc/api.cu", "csrc/noalloc.cu"]
 CPP_SOURCES = ["host/params.cpp"]
 CLI_SOURCES = ["host/pimdb_main.cpp"]
 HEADERS = ["csrc/common.cuh", "csrc/kernels.h", "host/units.hpp", "host/pimdb_host.hpp"]
