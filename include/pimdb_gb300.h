@@ -128,6 +128,22 @@ int pimdb_step(pimdb_handle* h, int nsteps);
 int pimdb_step_async(pimdb_handle* h, int nsteps);
 int pimdb_synchronize(pimdb_handle* h);
 
+/* The step's pieces one by one, for hosts that mirror the reference's
+ * plugin calls (Simulation::run, src/simulation.cpp:246-259).  Together,
+ *   thermostat_step(0); zero_momentum(); propagate(); thermostat_step(1);
+ *   zero_momentum(); set_step(step + 1)
+ * give the same state as pimdb_step(h, 1) (the fused normal-mode kernel
+ * aside, which reorders the same linear operations).
+ *   pimdb_thermostat_step  Thermostat::step (src/thermostats/thermostat.cpp:15-19);
+ *                          `substep` 0 / 1 selects the first / second O-step's
+ *                          noise of the current MD step;
+ *   pimdb_zero_momentum    Simulation::zeroMomentum (src/simulation.cpp:581-603);
+ *   pimdb_propagate        Propagator::step (velocity_verlet.cpp:7-22 or
+ *                          normal_modes_propagator.cpp:19-71); synchronous. */
+int pimdb_thermostat_step(pimdb_handle* h, int substep);
+int pimdb_zero_momentum(pimdb_handle* h);
+int pimdb_propagate(pimdb_handle* h);
+
 /* BosonicExchange on the current coordinates
  * (src/bosonic_exchange/quadratic_bosonic_exchange.cpp:30-279):
  *   scalars[0] = effectivePotential()      V_B = V[N]

@@ -28,7 +28,8 @@ EXPORTS = [
     "pimdb_set_state_device", "pimdb_get_state", "pimdb_get_state_device", "pimdb_set_step", "pimdb_get_step",
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
     "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
-    "pimdb_measure_fp64_peak", "pimdb_set_option",
+    "pimdb_measure_fp64_peak", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
+    "pimdb_propagate",
 ]
 KERNEL_CLASSES = ["bead_forces", "exch_energies", "exch_recursions", "exch_forces", "exch_estimators",
                   "cart_update", "nm_propagate", "nm_thermo"]
@@ -92,6 +93,9 @@ def lib():
             "pimdb_profile": ([vp, C.c_int, vp, vp, vp], C.c_int),
             "pimdb_measure_fp64_peak": ([vp], C.c_int),
             "pimdb_set_option": ([vp, C.c_char_p, C.c_int], C.c_int),
+            "pimdb_thermostat_step": ([vp, C.c_int], C.c_int),
+            "pimdb_zero_momentum": ([vp], C.c_int),
+            "pimdb_propagate": ([vp], C.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -243,6 +247,15 @@ class System:
 
     def step_async(self, nsteps: int = 1):
         _check(lib().pimdb_step_async(self._h, nsteps), self._h)
+
+    def thermostat_step(self, substep: int):
+        _check(lib().pimdb_thermostat_step(self._h, substep), self._h)
+
+    def zero_momentum(self):
+        _check(lib().pimdb_zero_momentum(self._h), self._h)
+
+    def propagate(self):
+        _check(lib().pimdb_propagate(self._h), self._h)
 
     def synchronize(self):
         _check(lib().pimdb_synchronize(self._h), self._h)

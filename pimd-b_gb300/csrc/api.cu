@@ -741,3 +741,45 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
     else return fail(h, PIMDB_ERR_ARG, "unknown option " + n);
     return PIMDB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Fine-grained steps mirroring the reference's plugin calls one by one
+// (Simulation::run, src/simulation.cpp:246-259).  They use the separate
+// (unfused) kernels; pimdb_step composes the same operations.
+
+extern "C" int pimdb_thermostat_step(pimdb_handle* h, int substep) {
+    if (!h || substep < 0 || substep > 1) return PIMDB_ERR_ARG;
+    const pimdb_config& c = h->cfg;
+    if (h->com_pending) cart(h, SF_COM_APPLY, 0, 0);  // finish an earlier COM removal first
+    if (c.thermostat == PIMDB_THERMO_LANGEVIN && c.nmthermostat) nm_thermo(h, 0, substep);
+    else if (c.thermostat == PIMDB_THERMO_LANGEVIN) cart(h, SF_LANGEVIN, substep, 0);
+    CUDA_TRY(h, cudaGetLastError());
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_zero_momentum(pimdb_handle* h) {
+    if (!h) return PIMDB_ERR_ARG;
+    if (h->com_pending) cart(h, SF_COM_APPLY, 0, 0);
+    cart(h, SF_COM_PARTIAL, 0, 0);
+    cart(h, SF_COM_APPLY, 0, 0);
+    CUDA_TRY(h, cudaGetLastError());
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_propagate(pimdb_handle* h) {
+    if (!h) return PIMDB_ERR_ARG;
+    if (h->com_pending) cart(h, SF_COM_APPLY, 0, 0);
+    if (h->cfg.propagator == PIMDB_PROP_NORMAL_MODES) {
+        launch(h, PIMDB_K_NM_PROPAGATE, [&] {
+            launch_nm_propagate(h->s, h->D, h->d_C, h->d_T, h->d_rot, 0, h->d_red[0], 0, h->stream);
+        });
+        enqueue_forces(h);
+        cart(h, SF_KICK, 0, 1);
+    } else {
+        cart(h, SF_KICK | SF_DRIFT, 0, 0);
+        enqueue_forces(h);
+        cart(h, SF_KICK, 0, 0);
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    return check_err_word(h);
+}

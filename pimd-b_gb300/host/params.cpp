@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/pimdb_gb300.h"
+#include "pimdb_host.hpp"
 #include "units.hpp"
 
 namespace pimdb_host {
@@ -147,21 +148,22 @@ static std::string fmt3(double v) {
     return b;
 }
 
-static void read_config(const IniFile& r, int ndim, pimdb_config& c) {
+static void read_config(const IniFile& r, int ndim, pimdb_config& c, RunParams& run) {
     using std::invalid_argument;
     pimdb_config_default(&c);
     c.ndim = ndim;
     const std::string SIM = "simulation", SYS = "system", INT = "interaction_potential", EXT = "external_potential";
 
     c.dt = get_quantity("time", r.Get(SIM, "dt", "1.0 femtosecond"));
-    r.GetReal(SIM, "threshold", 0.1);
+    run.threshold = r.GetReal(SIM, "threshold", 0.1);
     c.gamma = r.GetReal(SIM, "gamma", -1.0);
     if (c.gamma < 0) c.gamma = 1 / (100.0 * c.dt);
     const int nchains = r.GetInteger(SIM, "nchains", 4);
     if (nchains < 1)
         throw invalid_argument("The specified number of Nose-Hoover chains (" + std::to_string(nchains) +
                                ") is less than one!");
-    (void)std::stod(r.Get(SIM, "steps", "1e5"));
+    run.steps = (long)std::stod(r.Get(SIM, "steps", "1e5"));
+    run.sfreq = r.GetLong(SIM, "sfreq", 1000);
     c.nbeads = r.GetInteger(SIM, "nbeads", 4);
     if (c.nbeads < 1)
         throw invalid_argument("The specified number of beads (" + std::to_string(c.nbeads) + ") is less than one!");
@@ -179,10 +181,17 @@ static void read_config(const IniFile& r, int ndim, pimdb_config& c) {
         throw invalid_argument("The coordinate initialization method format is invalid!");
     if (tok != "random" && tok != "xyz" && tok != "grid")
         throw invalid_argument("The specified coordinate initialization method (" + tok + ") is not supported!");
+    run.init_pos_type = tok;
+    run.init_pos_spec = spec;
     if (!parse_token_parentheses(r.Get(SIM, "initial_velocity", "random"), tok, spec))
         throw invalid_argument("The velocity initialization method format is invalid!");
     if (tok != "random" && tok != "manual")
         throw invalid_argument("The specified velocity initialization method (" + tok + ") is not supported!");
+    run.init_vel_type = tok;
+    run.init_vel_spec = spec;
+    run.output_positions = r.Get("output", "positions", "off");
+    run.output_velocities = r.Get("output", "velocities", "off");
+    run.output_forces = r.Get("output", "forces", "off");
 
     const std::string propagator = r.GetString(SIM, "propagator", "cartesian");
     if (bosonic && propagator == "normal_modes")
@@ -250,6 +259,13 @@ static void read_config(const IniFile& r, int ndim, pimdb_config& c) {
     }
 }
 
+void read_params(const std::string& path, int ndim, pimdb_config& cfg, RunParams& run) {
+    if (ndim < 1 || ndim > 3) throw std::invalid_argument("ndim must be 1, 2 or 3");
+    IniFile r(path);
+    if (r.ParseError() < 0) throw std::invalid_argument("Unable to read the configuration file " + path);
+    read_config(r, ndim, cfg, run);
+}
+
 }  // namespace pimdb_host
 
 extern "C" int pimdb_config_from_ini(const char* path, int ndim, pimdb_config* cfg, char* err, int err_len) {
@@ -267,7 +283,8 @@ extern "C" int pimdb_config_from_ini(const char* path, int ndim, pimdb_config* c
         return PIMDB_ERR_PARSE;
     }
     try {
-        pimdb_host::read_config(r, ndim, *cfg);
+        pimdb_host::RunParams run;
+        pimdb_host::read_config(r, ndim, *cfg, run);
     } catch (const std::exception& ex) {
         report(ex.what());
         return PIMDB_ERR_CONFIG;

@@ -1,0 +1,337 @@
+// C++20 host layer over the C ABI: the reference's plugin classes
+// (Potential, Propagator, Thermostat, BosonicExchangeBase, Simulation, Params)
+// with the reference's names and call structure, each holding every bead of
+// the ring polymer on the GPU instead of one MPI rank's bead.
+//
+//   Params              include/params.h:19-53, src/params.cpp:8-260
+//   Potential family    include/potentials/*.h (constructor signatures kept)
+//   BosonicExchange     include/bosonic_exchange/bosonic_exchange_base.h:16-54
+//   Propagator          include/propagators/propagator.h:7-18
+//   Thermostat          include/thermostats/thermostat.h:9-19
+//   Simulation          include/simulation.h:20-131, src/simulation.cpp
+//
+// Errors surface as the reference's exception types: std::invalid_argument
+// (configuration), std::overflow_error (non-finite exchange potential),
+// std::runtime_error (CUDA).
+#pragma once
+
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <memory>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "pimdb_gb300.h"
+
+namespace pimdb_host {
+
+// Run-control keys of config.ini that the hot path does not use.
+struct RunParams {
+    long steps = 100000;
+    long sfreq = 1000;
+    double threshold = 0.1;
+    std::string init_pos_type = "random", init_pos_spec;
+    std::string init_vel_type = "random", init_vel_spec;
+    std::string output_positions = "off", output_velocities = "off", output_forces = "off";
+};
+
+// Reads config.ini (schema and messages of src/params.cpp:8-260); throws
+// std::invalid_argument.
+void read_params(const std::string& path, int ndim, pimdb_config& cfg, RunParams& run);
+
+// "grid" initial positions (src/simulation.cpp:133-193) of one bead.
+inline void grid_positions(const pimdb_config& cfg, double* pos) {
+    const int N = cfg.natoms, D = cfg.ndim;
+    const double L = cfg.size;
+    const double volume = std::pow(L, D);
+    const double side = std::pow((1.0 * N / volume), -1.0 / (1.0 * D));
+    int total = 1;
+    int num[3];
+    double sz[3];
+    for (int i = 0; i < D; i++) {
+        num[i] = (int)std::ceil((L / side) - 1.0E-7);
+        num[i] = std::max(num[i], 1);
+        sz[i] = L / (1.0 * num[i]);
+        total *= num[i];
+    }
+    if (total < N) throw std::runtime_error("Number of grid boxes is less than the number of particles");
+    for (int n = 0; n < N; n++) {
+        for (int i = 0; i < D; i++) {
+            int scale = 1;
+            for (int j = i + 1; j < D; j++) scale *= num[j];
+            const int gi = (n / scale) % num[i];
+            double v = (gi + 0.5) * sz[i] - 0.5 * L;
+            if (cfg.pbc) v -= L * std::floor(v / L + 0.5);
+            pos[(size_t)n * D + i] = v;
+        }
+    }
+}
+
+// Initial conditions as the reference draws them: bead b uses
+// std::mt19937(seed + b) (src/simulation.cpp:58); random positions uniform in
+// [-L/2, L/2] (:118-126) or the grid (:133-193); Maxwell-Boltzmann momenta
+// from a fresh std::normal_distribution per draw (:200-217).  With
+// zero_com, the centre-of-mass momentum is removed here the way
+// Simulation::zeroMomentum does it (:581-603, :750-751).
+inline void initial_state(const pimdb_config& cfg, const RunParams& run, std::vector<double>& x0,
+                          std::vector<double>& p0, bool zero_com = false) {
+    const int P = cfg.nbeads, N = cfg.natoms, D = cfg.ndim;
+    x0.assign((size_t)P * N * D, 0.0);
+    p0.assign((size_t)P * N * D, 0.0);
+    const double beta = 1.0 / (1.0 * cfg.temperature);
+    const double thermo_beta = beta / P;
+    if (run.init_vel_type != "random")
+        throw std::invalid_argument("initial_velocity " + run.init_vel_type +
+                                    " needs the reference's file loaders (not part of the hot path)");
+    for (int b = 0; b < P; ++b) {
+        std::mt19937 gen((unsigned)(cfg.seed + b));
+        double* x = &x0[(size_t)b * N * D];
+        double* p = &p0[(size_t)b * N * D];
+        if (run.init_pos_type == "grid") {
+            grid_positions(cfg, x);
+        } else if (run.init_pos_type == "random") {
+            std::uniform_real_distribution<double> u(-0.5 * cfg.size, 0.5 * cfg.size);
+            for (int i = 0; i < N * D; ++i) x[i] = u(gen);
+        } else {
+            throw std::invalid_argument("initial_position " + run.init_pos_type +
+                                        " needs the reference's file loaders (not part of the hot path)");
+        }
+        for (int i = 0; i < N * D; ++i) {
+            std::normal_distribution<double> nd(0.0, 1 / std::sqrt(thermo_beta * cfg.mass));
+            p[i] = cfg.mass * nd(gen);
+        }
+    }
+    if (zero_com) {
+        double cm[3] = {0.0, 0.0, 0.0};
+        for (int b = 0; b < P; ++b) {
+            double per[3] = {0.0, 0.0, 0.0};
+            for (int i = 0; i < N; ++i)
+                for (int a = 0; a < D; ++a) per[a] += p0[((size_t)b * N + i) * D + a];
+            for (int a = 0; a < D; ++a) cm[a] += per[a] / (N * P);
+        }
+        for (size_t i = 0; i < (size_t)P * N; ++i)
+            for (int a = 0; a < D; ++a) p0[i * D + a] -= cm[a];
+    }
+}
+
+inline void check(int st, pimdb_handle* h = nullptr) {
+    if (st == PIMDB_OK) return;
+    char buf[512];
+    pimdb_last_error(h, buf, sizeof buf);
+    const std::string msg = std::string(pimdb_status_string(st)) + ": " + buf;
+    if (st == PIMDB_ERR_CONFIG || st == PIMDB_ERR_PARSE || st == PIMDB_ERR_ARG) throw std::invalid_argument(msg);
+    if (st == PIMDB_ERR_NONFINITE_VB) throw std::overflow_error(msg);
+    throw std::runtime_error(msg);
+}
+
+}  // namespace pimdb_host
+
+namespace pimdb_gb300 {
+
+using pimdb_host::check;
+
+class Params {
+public:
+    explicit Params(const std::string& filename, int ndim = 3) { pimdb_host::read_params(filename, ndim, config, run); }
+    pimdb_config config{};
+    pimdb_host::RunParams run;
+};
+
+// ----------------------------------------------------------------- potentials
+// The GPU evaluates the potentials; these objects carry their parameters
+// (constructor signatures as in the reference).
+class Potential {
+public:
+    virtual ~Potential() = default;
+    virtual int kind() const { return PIMDB_POT_FREE; }
+    virtual std::array<double, 3> params() const { return {0.0, 0.0, 0.0}; }
+};
+class HarmonicPotential : public Potential {  // harmonic.cpp:3-5
+public:
+    HarmonicPotential(double mass, double omega) : mass(mass), omega(omega) {}
+    int kind() const override { return PIMDB_POT_HARMONIC; }
+    std::array<double, 3> params() const override { return {omega, 0.0, 0.0}; }
+    double mass, omega;
+};
+class DoubleWellPotential : public Potential {  // double_well.cpp:3-4
+public:
+    DoubleWellPotential(double mass, double strength, double loc) : mass(mass), strength(strength), loc(loc) {}
+    int kind() const override { return PIMDB_POT_DOUBLE_WELL; }
+    std::array<double, 3> params() const override { return {strength, loc, 0.0}; }
+    double mass, strength, loc;
+};
+class CosinePotential : public Potential {  // cosine.cpp:4-7
+public:
+    CosinePotential(double amplitude, double wavelength, double phase)
+        : amplitude(amplitude), wavelength(wavelength), phase(phase) {}
+    int kind() const override { return PIMDB_POT_COSINE; }
+    std::array<double, 3> params() const override { return {amplitude, phase, 0.0}; }
+    double amplitude, wavelength, phase;
+};
+class DipolePotential : public Potential {  // dipole.cpp:3
+public:
+    explicit DipolePotential(double strength) : strength(strength) {}
+    int kind() const override { return PIMDB_POT_DIPOLE; }
+    std::array<double, 3> params() const override { return {strength, 0.0, 0.0}; }
+    double strength;
+};
+class AzizPotential : public Potential {  // aziz.cpp:3-16
+public:
+    int kind() const override { return PIMDB_POT_AZIZ; }
+};
+
+// The device state shared by the plugins of one simulation.
+class Engine {
+public:
+    explicit Engine(const pimdb_config& cfg, void* stream = nullptr) : cfg_(cfg) { check(pimdb_create(&cfg_, stream, &h_)); }
+    ~Engine() {
+        if (h_) pimdb_destroy(h_);
+    }
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+    pimdb_handle* handle() const { return h_; }
+    const pimdb_config& config() const { return cfg_; }
+
+private:
+    pimdb_config cfg_;
+    pimdb_handle* h_ = nullptr;
+};
+
+// ------------------------------------------------------------ bosonic exchange
+class BosonicExchangeBase {
+public:
+    explicit BosonicExchangeBase(Engine& e) : e_(e) {}
+    virtual ~BosonicExchangeBase() = default;
+    BosonicExchangeBase(const BosonicExchangeBase&) = delete;
+    BosonicExchangeBase& operator=(const BosonicExchangeBase&) = delete;
+
+    // exterior spring force of bead 1 (first = true) or bead P, [particle][axis]
+    void exteriorSpringForce(std::vector<double>& f, bool first) const { f = first ? f_first_ : f_last_; }
+    virtual void prepare() = 0;
+    virtual double effectivePotential() = 0;
+    virtual double primEstimator() = 0;
+    virtual double getDistinctProbability() = 0;
+    virtual double getLongestProbability() = 0;
+
+protected:
+    Engine& e_;
+    std::vector<double> f_first_, f_last_;
+};
+
+class BosonicExchange final : public BosonicExchangeBase {  // Feldman-Hirshberg, on the GPU
+public:
+    explicit BosonicExchange(Engine& e) : BosonicExchangeBase(e) {}
+    void prepare() override {
+        const auto& c = e_.config();
+        f_first_.assign((size_t)c.natoms * c.ndim, 0.0);
+        f_last_.assign((size_t)c.natoms * c.ndim, 0.0);
+        check(pimdb_exchange(e_.handle(), scal_.data(), f_first_.data(), f_last_.data()), e_.handle());
+    }
+    double effectivePotential() override { return scal_[0]; }
+    double primEstimator() override { return scal_[1]; }
+    double getDistinctProbability() override { return scal_[2]; }
+    double getLongestProbability() override { return scal_[3]; }
+
+private:
+    std::array<double, 4> scal_{};
+};
+
+// ------------------------------------------------------ propagator, thermostat
+class Propagator {
+public:
+    explicit Propagator(Engine& e) : e_(e) {}
+    virtual ~Propagator() = default;
+    virtual void step() { check(pimdb_propagate(e_.handle()), e_.handle()); }
+
+protected:
+    Engine& e_;
+};
+class VelocityVerletPropagator final : public Propagator {
+public:
+    using Propagator::Propagator;
+};
+class NormalModesPropagator final : public Propagator {
+public:
+    using Propagator::Propagator;
+};
+
+class Thermostat {
+public:
+    Thermostat(Engine& e, bool normal_modes) : e_(e), normal_modes_(normal_modes) {}
+    virtual ~Thermostat() = default;
+    // substep 0 / 1: first / second O-step of the current MD step
+    void step(int substep) { check(pimdb_thermostat_step(e_.handle(), substep), e_.handle()); }
+    virtual double getAdditionToH() { return 0.0; }
+
+protected:
+    Engine& e_;
+    bool normal_modes_;
+};
+class LangevinThermostat final : public Thermostat {
+public:
+    using Thermostat::Thermostat;
+};
+
+// ----------------------------------------------------------------- simulation
+// Simulation::Simulation / run (src/simulation.cpp:16-101, :236-260) for all
+// beads at once; the initial state is pimdb_host::initial_state's.
+class Simulation {
+public:
+    explicit Simulation(Params& params, void* stream = nullptr) : cfg(params.config), run_params(params.run) {
+        engine = std::make_unique<Engine>(cfg, stream);
+        if (cfg.bosonic && cfg.nbeads > 1) bosonic_exchange = std::make_unique<BosonicExchange>(*engine);
+        if (cfg.propagator == PIMDB_PROP_NORMAL_MODES) propagator = std::make_unique<NormalModesPropagator>(*engine);
+        else propagator = std::make_unique<VelocityVerletPropagator>(*engine);
+        if (cfg.thermostat == PIMDB_THERMO_LANGEVIN) thermostat = std::make_unique<LangevinThermostat>(*engine, cfg.nmthermostat);
+        else thermostat = std::make_unique<Thermostat>(*engine, cfg.nmthermostat);
+        initialize_state();
+    }
+
+    // One MD step through the plugins (src/simulation.cpp:246-259).
+    void plugin_step() {
+        thermostat->step(0);
+        if (cfg.fixcom) zeroMomentum();
+        propagator->step();
+        thermostat->step(1);
+        if (cfg.fixcom) zeroMomentum();
+        check(pimdb_set_step(engine->handle(), ++md_step), engine->handle());
+    }
+    // The same step with the fused device schedule.
+    void fast_step(int n = 1) {
+        check(pimdb_step(engine->handle(), n), engine->handle());
+        md_step += n;
+    }
+    void zeroMomentum() { check(pimdb_zero_momentum(engine->handle()), engine->handle()); }
+    void updateForces() { check(pimdb_compute_forces(engine->handle()), engine->handle()); }
+    void get_state(std::vector<double>& x, std::vector<double>& p, std::vector<double>& f) const {
+        const size_t n = (size_t)cfg.nbeads * cfg.natoms * cfg.ndim;
+        x.resize(n);
+        p.resize(n);
+        f.resize(n);
+        check(pimdb_get_state(engine->handle(), x.data(), p.data(), f.data()), engine->handle());
+    }
+    long getStep() const { return md_step; }
+
+    pimdb_config cfg;
+    pimdb_host::RunParams run_params;
+    std::unique_ptr<Engine> engine;
+    std::unique_ptr<BosonicExchangeBase> bosonic_exchange;
+    std::unique_ptr<Propagator> propagator;
+    std::unique_ptr<Thermostat> thermostat;
+    std::vector<double> x0, p0;  // initial state [bead][particle][axis]
+
+private:
+    void initialize_state() {
+        pimdb_host::initial_state(cfg, run_params, x0, p0);
+        check(pimdb_set_state(engine->handle(), x0.data(), p0.data()), engine->handle());
+        zeroMomentum();
+    }
+
+    long md_step = 0;
+};
+
+}  // namespace pimdb_gb300
