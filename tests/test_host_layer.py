@@ -34,10 +34,10 @@ def _need_cli():
 
 
 def _sections(P=8, N=8, fixcom="true", steps=0, propagator="cartesian", thermostat="langevin",
-              nmthermostat="false", init_pos="random", T="5.802 kelvin"):
+              nmthermostat="false", init_pos="random", T="5.802 kelvin", bosonic="true"):
     return {
         "simulation": {"dt": "1.0 femtosecond", "steps": steps, "sfreq": 1, "nbeads": P, "fixcom": fixcom,
-                       "bosonic": "true", "seed": 90846, "pbc": "false", "initial_position": init_pos,
+                       "bosonic": bosonic, "seed": 90846, "pbc": "false", "initial_position": init_pos,
                        "initial_velocity": "random", "thermostat": thermostat, "propagator": propagator,
                        "nmthermostat": nmthermostat},
         "system": {"temperature": T, "natoms": N, "size": "300.0 atomic_unit", "mass": "1.0 atomic_unit"},
@@ -69,14 +69,16 @@ def test_cli_check_reports_configuration(tmp_path):
     assert "natoms=6 nbeads=4 ndim=3 bosonic=1 propagator=0 thermostat=1 steps=17" in r.stdout
 
 
-def test_cli_configuration_error_is_reported_like_the_reference(tmp_path):
+@pytest.mark.parametrize("key,value,message", [("thermostat", "nose_hoover", "not part of the GPU hot path"),
+                                               ("propagator", "normal_modes", "not available for bosons")])
+def test_cli_configuration_error_is_reported_like_the_reference(key, value, message, tmp_path):
     _need_cli()
     sec = _sections()
-    sec["simulation"]["thermostat"] = "nose_hoover"
+    sec["simulation"][key] = value
     R.write_ini(tmp_path / "c.ini", sec)
     r = _cli(["-in", "c.ini", "--check"], tmp_path)
     assert r.returncode == 0          # src/pimdb.cpp catches and returns 0
-    assert "[X] Invalid argument error:" in r.stdout
+    assert "[X] Invalid argument error:" in r.stdout and message in r.stdout
 
 
 def test_cli_initial_state_grid_positions(tmp_path):
@@ -148,12 +150,16 @@ def test_plugin_calls_equal_fused_step(name):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("plugin", [False, True])
-@pytest.mark.parametrize("propagator,nmthermostat", [("cartesian", "false"), ("normal_modes", "true")])
-def test_cli_run_matches_oracle(plugin, propagator, nmthermostat, tmp_path):
+# the reference's reader rejects bosons with the normal-mode propagator
+# (src/params.cpp:146-148), so that case runs distinguishable particles
+@pytest.mark.parametrize("propagator,nmthermostat,bosonic", [("cartesian", "false", "true"),
+                                                             ("cartesian", "true", "true"),
+                                                             ("normal_modes", "true", "false")])
+def test_cli_run_matches_oracle(plugin, propagator, nmthermostat, bosonic, tmp_path):
     _need_cli()
     steps = 6
     P, N = 8, 8
-    sec = _sections(P=P, N=N, steps=steps, propagator=propagator, nmthermostat=nmthermostat)
+    sec = _sections(P=P, N=N, steps=steps, propagator=propagator, nmthermostat=nmthermostat, bosonic=bosonic)
     x0, p0 = _initial(tmp_path, sec, P, N)
     args = ["-in", "c.ini", "--positions", "final.xyz"] + (["--plugin-steps"] if plugin else [])
     r = _cli(args, tmp_path)
