@@ -222,6 +222,51 @@ int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms, int ndim,
                            double beta_ex, int pbc, double box, double* scalars, double* f_first, double* f_last,
                            void* cuda_stream, char* err, int err_len);
 
+/* ------------------------------------------------------------------------
+ * Batched replicas (no counterpart in the reference, which runs one system
+ * per MPI job: src/pimdb.cpp:31-68).  A batch is many independent systems,
+ * each with its own pimdb_config (natoms, nbeads, temperature, potentials,
+ * seed, replica), advanced together: one launch per MD step, and a run of
+ * steps is replayed as one CUDA graph.  Each step is the body of
+ * Simulation::run (src/simulation.cpp:246-259) with the cartesian
+ * propagator (VelocityVerletPropagator::step,
+ * src/propagators/velocity_verlet.cpp:7-22) and the cartesian Langevin
+ * thermostat or none, for every replica.  Every replica must share ndim and
+ * precision; natoms <= 2048; at most 65535 replicas.  With PIMDB_MIXED the
+ * pair forces are FP32 with FP64 accumulation and the Langevin normals are
+ * drawn in FP32 (same Philox stream); exchange and integrator stay FP64.
+ * Host arrays of the batch are the replicas' [bead][particle][axis] arrays
+ * concatenated in replica order (pimdb_batch_size gives the total length).
+ */
+typedef struct pimdb_batch pimdb_batch;
+int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void* cuda_stream, pimdb_batch** out);
+int pimdb_batch_destroy(pimdb_batch* b);
+int pimdb_batch_size(const pimdb_batch* b, int* nreplicas, long long* host_doubles);
+/* As pimdb_set_state / pimdb_get_state for every replica at once. */
+int pimdb_batch_set_states(pimdb_batch* b, const double* x, const double* p);
+int pimdb_batch_get_states(pimdb_batch* b, double* x, double* p, double* f);
+/* MD step index shared by the replicas (the Langevin noise counter). */
+int pimdb_batch_set_step(pimdb_batch* b, long long step);
+int pimdb_batch_get_step(pimdb_batch* b, long long* step);
+/* Simulation::updateForces (src/simulation.cpp:353-374) on every replica. */
+int pimdb_batch_compute_forces(pimdb_batch* b);
+/* `nsteps` MD steps of every replica; synchronous, reports a non-finite V_B
+ * of any replica (the message names it).  _async only enqueues. */
+int pimdb_batch_step(pimdb_batch* b, int nsteps);
+int pimdb_batch_step_async(pimdb_batch* b, int nsteps);
+int pimdb_batch_synchronize(pimdb_batch* b);
+/* pimdb_exchange's four scalars for every replica, scalars[nreplicas][4]
+ * (zeros for distinguishable replicas); evaluates the forces first. */
+int pimdb_batch_exchange(pimdb_batch* b, double* scalars);
+/* "threads" (32..512 per CTA), "ctas_per_sm" (resident CTAs per SM the grid
+ * is sized for), "graph" (0: plain launches instead of a CUDA graph). */
+int pimdb_batch_set_option(pimdb_batch* b, const char* name, int value);
+int pimdb_batch_get_launch(pimdb_batch* b, int* threads, int* ctas_per_sm, int* grid, long long* launches);
+/* Chooses threads per CTA and CTAs per SM by timing `steps` steps of each
+ * candidate from a copy of the current state; the state is restored. */
+int pimdb_batch_autotune(pimdb_batch* b, int steps, int* threads, int* ctas_per_sm);
+int pimdb_batch_last_error(const pimdb_batch* b, char* buf, int len);
+
 /* Measures the FP64 fused-multiply-add throughput of the current device in
  * TFLOP/s (the roofline denominator of the FP64 kernels). */
 int pimdb_measure_fp64_peak(double* tflops);

@@ -29,7 +29,10 @@ EXPORTS = [
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
     "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
     "pimdb_measure_fp64_peak", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
-    "pimdb_propagate",
+    "pimdb_propagate", "pimdb_batch_create", "pimdb_batch_destroy", "pimdb_batch_size", "pimdb_batch_set_states",
+    "pimdb_batch_get_states", "pimdb_batch_set_step", "pimdb_batch_get_step", "pimdb_batch_compute_forces",
+    "pimdb_batch_step", "pimdb_batch_step_async", "pimdb_batch_synchronize", "pimdb_batch_exchange",
+    "pimdb_batch_set_option", "pimdb_batch_get_launch", "pimdb_batch_autotune", "pimdb_batch_last_error",
 ]
 KERNEL_CLASSES = ["bead_forces", "exch_energies", "exch_recursions", "exch_forces", "exch_estimators",
                   "cart_update", "nm_propagate", "nm_thermo"]
@@ -96,6 +99,22 @@ def lib():
             "pimdb_thermostat_step": ([vp, C.c_int], C.c_int),
             "pimdb_zero_momentum": ([vp], C.c_int),
             "pimdb_propagate": ([vp], C.c_int),
+            "pimdb_batch_create": ([cfgp, C.c_int, vp, C.POINTER(vp)], C.c_int),
+            "pimdb_batch_destroy": ([vp], C.c_int),
+            "pimdb_batch_size": ([vp, ip, C.POINTER(C.c_longlong)], C.c_int),
+            "pimdb_batch_set_states": ([vp, vp, vp], C.c_int),
+            "pimdb_batch_get_states": ([vp, vp, vp, vp], C.c_int),
+            "pimdb_batch_set_step": ([vp, C.c_longlong], C.c_int),
+            "pimdb_batch_get_step": ([vp, C.POINTER(C.c_longlong)], C.c_int),
+            "pimdb_batch_compute_forces": ([vp], C.c_int),
+            "pimdb_batch_step": ([vp, C.c_int], C.c_int),
+            "pimdb_batch_step_async": ([vp, C.c_int], C.c_int),
+            "pimdb_batch_synchronize": ([vp], C.c_int),
+            "pimdb_batch_exchange": ([vp, vp], C.c_int),
+            "pimdb_batch_set_option": ([vp, C.c_char_p, C.c_int], C.c_int),
+            "pimdb_batch_get_launch": ([vp, ip, ip, ip, C.POINTER(C.c_longlong)], C.c_int),
+            "pimdb_batch_autotune": ([vp, C.c_int, ip, ip], C.c_int),
+            "pimdb_batch_last_error": ([vp, C.c_char_p, C.c_int], C.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -115,10 +134,17 @@ def _last_error(h=None) -> str:
     return buf.value.decode()
 
 
-def _check(st: int, h=None):
+def _batch_last_error(b=None) -> str:
+    buf = C.create_string_buffer(1024)
+    lib().pimdb_batch_last_error(b, buf, len(buf))
+    return buf.value.decode()
+
+
+def _check(st: int, h=None, batch=False):
     if st == OK:
         return
-    msg = f"{lib().pimdb_status_string(st).decode()}: {_last_error(h)}"
+    detail = _batch_last_error(h) if batch else _last_error(h)
+    msg = f"{lib().pimdb_status_string(st).decode()}: {detail}"
     if st in (ERR_CONFIG, ERR_PARSE):
         raise ConfigError(msg)
     if st == ERR_NONFINITE_VB:
@@ -284,3 +310,97 @@ class System:
         Vb = np.zeros(N + 1)
         _check(lib().pimdb_exchange_arrays(self._h, _ptr(E), _ptr(V), _ptr(Vb)), self._h)
         return dict(E=E, V=V, Vb=Vb)
+
+
+class Batch:
+    """Independent replicas (each its own Config) advanced together by the
+    batched engine: one launch per MD step, runs of steps replayed as one
+    CUDA graph.  Per-replica arrays are [bead][particle][axis]; the batch's
+    host layout is their concatenation in replica order."""
+
+    def __init__(self, cfgs, stream: int | None = None):
+        cfgs = list(cfgs)
+        arr = (Config * len(cfgs))(*cfgs)
+        self.cfgs = cfgs
+        self.shapes = [(c.nbeads, c.natoms, c.ndim) for c in cfgs]
+        self.offsets = np.cumsum([0] + [int(np.prod(s)) for s in self.shapes])
+        b = C.c_void_p()
+        _check(lib().pimdb_batch_create(arr, len(cfgs), C.c_void_p(stream) if stream else None, C.byref(b)),
+               None, batch=True)
+        self._b = b
+
+    def close(self):
+        if getattr(self, "_b", None):
+            lib().pimdb_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _c(self, st):
+        _check(st, self._b, batch=True)
+
+    def flatten(self, arrays):
+        """Concatenates per-replica arrays into the batch's host layout."""
+        return np.ascontiguousarray(np.concatenate([np.asarray(a, dtype=np.float64).ravel() for a in arrays]))
+
+    def split(self, flat):
+        return [flat[self.offsets[r]:self.offsets[r + 1]].reshape(self.shapes[r]) for r in range(len(self.shapes))]
+
+    def set_states(self, xs=None, ps=None):
+        x = None if xs is None else (xs if isinstance(xs, np.ndarray) and xs.ndim == 1 else self.flatten(xs))
+        p = None if ps is None else (ps if isinstance(ps, np.ndarray) and ps.ndim == 1 else self.flatten(ps))
+        self._c(lib().pimdb_batch_set_states(self._b, _ptr(x), _ptr(p)))
+
+    def get_states(self, flat=False):
+        n = int(self.offsets[-1])
+        x, p, f = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._c(lib().pimdb_batch_get_states(self._b, _ptr(x), _ptr(p), _ptr(f)))
+        if flat:
+            return x, p, f
+        return self.split(x), self.split(p), self.split(f)
+
+    def set_step(self, step: int):
+        self._c(lib().pimdb_batch_set_step(self._b, step))
+
+    def get_step(self) -> int:
+        v = C.c_longlong()
+        self._c(lib().pimdb_batch_get_step(self._b, C.byref(v)))
+        return v.value
+
+    def compute_forces(self):
+        self._c(lib().pimdb_batch_compute_forces(self._b))
+
+    def step(self, nsteps: int = 1):
+        self._c(lib().pimdb_batch_step(self._b, nsteps))
+
+    def step_async(self, nsteps: int = 1):
+        self._c(lib().pimdb_batch_step_async(self._b, nsteps))
+
+    def synchronize(self):
+        self._c(lib().pimdb_batch_synchronize(self._b))
+
+    def exchange(self) -> np.ndarray:
+        sc = np.zeros((len(self.cfgs), 4))
+        self._c(lib().pimdb_batch_exchange(self._b, _ptr(sc)))
+        return sc
+
+    def set_option(self, name: str, value: int):
+        self._c(lib().pimdb_batch_set_option(self._b, name.encode(), int(value)))
+
+    def launch(self):
+        t, c, g = C.c_int(), C.c_int(), C.c_int()
+        n = C.c_longlong()
+        self._c(lib().pimdb_batch_get_launch(self._b, C.byref(t), C.byref(c), C.byref(g), C.byref(n)))
+        return dict(threads=t.value, ctas_per_sm=c.value, grid=g.value, launches=n.value)
+
+    def autotune(self, steps: int = 3):
+        t, c = C.c_int(), C.c_int()
+        self._c(lib().pimdb_batch_autotune(self._b, steps, C.byref(t), C.byref(c)))
+        return t.value, c.value

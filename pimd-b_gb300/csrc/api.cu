@@ -12,6 +12,7 @@
 
 #include "../../include/pimdb_gb300.h"
 #include "common.cuh"
+#include "config.h"
 #include "kernels.h"
 
 using namespace pimdb;
@@ -131,7 +132,7 @@ extern "C" int pimdb_config_default(pimdb_config* c) {
     return PIMDB_OK;
 }
 
-static std::string validate(const pimdb_config& c) {
+std::string validate_config(const pimdb_config& c) {
     if (c.ndim < 1 || c.ndim > 3) return "ndim must be 1, 2 or 3";
     if (c.nbeads < 1) return "The specified number of beads is less than one!";
     if (c.natoms < 1) return "The specified number of particles is smaller than one!";
@@ -154,6 +155,50 @@ static std::string validate(const pimdb_config& c) {
     if ((long long)c.natoms * c.nbeads * c.ndim > (1ll << 31)) return "system too large";
     if (c.bosonic && c.nbeads > 1 && c.natoms > 16384) return "bosonic exchange supports at most 16384 particles";
     return "";
+}
+
+void sys_params_from_config(const pimdb_config& c, Sys& s) {
+    s.N = c.natoms;
+    s.P = c.nbeads;
+    s.ld = (c.natoms + 31) / 32 * 32;
+    s.bosonic = (c.bosonic && c.nbeads > 1) ? 1 : 0;  // simulation.cpp:690
+    s.pbc = c.pbc ? 1 : 0;
+    s.L = c.size;
+    s.invL = 1.0 / c.size;
+    s.mass = c.mass;
+    s.dt = c.dt;
+    // simulation.cpp:37-52 (IPI convention, kB = hbar = 1)
+    const double beta = 1.0 / (1.0 * c.temperature);
+    const double thermo_beta = beta / c.nbeads;
+    s.omega_p = c.nbeads / (beta * 1.0);
+    s.kappa = c.mass * s.omega_p * s.omega_p;
+    s.beta_ex = beta / c.nbeads;  // bosonic_exchange_base.cpp:16-18
+    // langevin.cpp:11-12, params.cpp:17-20
+    const double gamma = c.gamma < 0 ? 1 / (100.0 * c.dt) : c.gamma;
+    s.c1 = std::exp(-0.5 * gamma * c.dt);
+    s.c2 = std::sqrt((1 - s.c1 * s.c1) * c.mass / thermo_beta);
+    // simulation.cpp:84-90
+    double cut = (c.int_kind == PIMDB_POT_FREE) ? 0.0 : c.cutoff;
+    if (c.pbc && 0.5 * c.size < cut) cut = 0.5 * c.size;
+    s.cutoff = cut;
+    s.ext_kind = c.ext_kind;
+    if (c.ext_kind == PIMDB_POT_HARMONIC) {
+        s.ext_a = c.mass * c.ext_params[0] * c.ext_params[0];
+    } else if (c.ext_kind == PIMDB_POT_DOUBLE_WELL) {
+        s.ext_a = 4 * c.mass * c.ext_params[0];
+        s.ext_b = c.ext_params[1] * c.ext_params[1];
+        s.ext_c = c.mass * c.ext_params[0];
+    } else if (c.ext_kind == PIMDB_POT_COSINE) {
+        const double k = 2 * 3.14159265358979323846 / c.size;
+        s.ext_a = -c.ext_params[0] * k;
+        s.ext_b = k;
+        s.ext_c = c.ext_params[1];
+    }
+    s.int_kind = c.int_kind;
+    if (c.int_kind == PIMDB_POT_HARMONIC) s.int_a = c.mass * c.int_params[0] * c.int_params[0];
+    else if (c.int_kind == PIMDB_POT_DIPOLE) s.int_a = c.int_params[0];
+    s.seed = c.seed;
+    s.replica = c.replica;
 }
 
 // Reference normal-mode rows (src/normal_modes.cpp:48-79), bit for bit.
@@ -220,7 +265,7 @@ static void free_handle(pimdb_handle* h) {
 extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_handle** out) {
     if (!cfg || !out) return fail(nullptr, PIMDB_ERR_ARG, "NULL argument");
     *out = nullptr;
-    const std::string why = validate(*cfg);
+    const std::string why = validate_config(*cfg);
     if (!why.empty()) return fail(nullptr, PIMDB_ERR_CONFIG, why);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -233,47 +278,7 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     const pimdb_config& c = h->cfg;
     h->D = c.ndim;
     Sys& s = h->s;
-    s.N = c.natoms;
-    s.P = c.nbeads;
-    s.ld = (c.natoms + 31) / 32 * 32;
-    s.bosonic = (c.bosonic && c.nbeads > 1) ? 1 : 0;  // simulation.cpp:690
-    s.pbc = c.pbc ? 1 : 0;
-    s.L = c.size;
-    s.invL = 1.0 / c.size;
-    s.mass = c.mass;
-    s.dt = c.dt;
-    // simulation.cpp:37-52 (IPI convention, kB = hbar = 1)
-    const double beta = 1.0 / (1.0 * c.temperature);
-    const double thermo_beta = beta / c.nbeads;
-    s.omega_p = c.nbeads / (beta * 1.0);
-    s.kappa = c.mass * s.omega_p * s.omega_p;
-    s.beta_ex = beta / c.nbeads;  // bosonic_exchange_base.cpp:16-18
-    // langevin.cpp:11-12, params.cpp:17-20
-    const double gamma = c.gamma < 0 ? 1 / (100.0 * c.dt) : c.gamma;
-    s.c1 = std::exp(-0.5 * gamma * c.dt);
-    s.c2 = std::sqrt((1 - s.c1 * s.c1) * c.mass / thermo_beta);
-    // simulation.cpp:84-90
-    double cut = (c.int_kind == PIMDB_POT_FREE) ? 0.0 : c.cutoff;
-    if (c.pbc && 0.5 * c.size < cut) cut = 0.5 * c.size;
-    s.cutoff = cut;
-    s.ext_kind = c.ext_kind;
-    if (c.ext_kind == PIMDB_POT_HARMONIC) {
-        s.ext_a = c.mass * c.ext_params[0] * c.ext_params[0];
-    } else if (c.ext_kind == PIMDB_POT_DOUBLE_WELL) {
-        s.ext_a = 4 * c.mass * c.ext_params[0];
-        s.ext_b = c.ext_params[1] * c.ext_params[1];
-        s.ext_c = c.mass * c.ext_params[0];
-    } else if (c.ext_kind == PIMDB_POT_COSINE) {
-        const double k = 2 * 3.14159265358979323846 / c.size;
-        s.ext_a = -c.ext_params[0] * k;
-        s.ext_b = k;
-        s.ext_c = c.ext_params[1];
-    }
-    s.int_kind = c.int_kind;
-    if (c.int_kind == PIMDB_POT_HARMONIC) s.int_a = c.mass * c.int_params[0] * c.int_params[0];
-    else if (c.int_kind == PIMDB_POT_DIPOLE) s.int_a = c.int_params[0];
-    s.seed = c.seed;
-    s.replica = c.replica;
+    sys_params_from_config(c, s);
 
     auto alloc = [&](double** p, size_t n) -> cudaError_t {
         cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(double));

@@ -1,0 +1,881 @@
+// Batched replicas: many independent ring polymers, each with its own N, P,
+// temperature, potentials and noise key, advanced together by one launch
+// per MD step.
+//
+// The reference runs one system per MPI job (src/pimdb.cpp:31-68,
+// src/simulation.cpp:236-260); an ensemble of small systems is many jobs.
+// Here a persistent grid takes whole replicas from a work counter, largest
+// first, and one CTA runs the complete step of one replica:
+//   head    O-step (substep 0), COM removal, B half-kick, A drift
+//   forces  external + pair forces per bead (one warp per bead, positions
+//           staged in shared memory), interior springs, and on bosonic
+//           replicas the Feldman-Hirshberg exchange on beads 1 and P
+//           (the block-level pieces shared with the one-system kernels)
+//   tail    B half-kick, O-step (substep 1), COM removal
+// in the order of src/simulation.cpp:246-259 with the cartesian propagator
+// (src/propagators/velocity_verlet.cpp:7-38) and the Langevin thermostat
+// (src/thermostats/langevin.cpp:10-27).  Nothing waits on another CTA: the
+// only cross-CTA state is the work counter, reset by the CTA that finishes
+// last, which also advances the device-side step counter, so a sequence of
+// step launches can be captured once in a CUDA graph and replayed.
+//
+// Precision: `R` is the pair-force arithmetic.  R = double is the FP64 path
+// (same noise, formulas and exchange as the one-system path).  R = float
+// computes pair separations from hi/lo float pairs and pair gradients in
+// FP32, sums each 32-particle tile in FP32 and accumulates tiles in FP64,
+// and draws the Langevin normals with FP32 Box-Muller from the same Philox
+// bits; the exchange recursions and the integrator stay FP64.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "config.h"
+#include "exchange_dev.cuh"
+#include "forces_dev.cuh"
+#include "kernels.h"
+
+namespace pimdb {
+
+enum BatchFlags : int { BF_LANGEVIN = 1, BF_FIXCOM = 2 };
+enum BatchMode : int { BM_HEAD = 1, BM_FORCES = 2, BM_TAIL = 4, BM_ADVANCE = 8, BM_ESTIMATORS = 16 };
+
+struct BatchRep {
+    Sys s;
+    int flags;  // BatchFlags
+    int pad;
+};
+
+constexpr int kBatchMaxThreads = 512;
+
+// FP32 Box-Muller on the top 24 bits of the same Philox outputs the FP64
+// path uses (philox_normal_pair takes the top 53).
+__device__ __forceinline__ float2 philox_normal_pair_f(uint64_t seed, uint32_t replica, uint64_t t, uint32_t pair) {
+    uint32_t c[4] = {pair, replica, (uint32_t)t, (uint32_t)(t >> 32)};
+    philox4x32_10(c, seed);
+    const float u1 = ((float)(c[1] >> 8) + 0.5f) * 0x1p-24f;
+    const float u2 = ((float)(c[3] >> 8) + 0.5f) * 0x1p-24f;
+    const float r = sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    return make_float2(r * cs, r * sn);
+}
+
+template <typename R>
+__device__ __forceinline__ void normal_pair(const Sys& s, long long step, int substep, uint32_t pair, double& z0,
+                                            double& z1) {
+    const uint64_t t = 2ull * (unsigned long long)step + substep;
+    if constexpr (sizeof(R) == 8) {
+        const double2 z = philox_normal_pair(s.seed, s.replica, t, pair);
+        z0 = z.x;
+        z1 = z.y;
+    } else {
+        const float2 z = philox_normal_pair_f(s.seed, s.replica, t, pair);
+        z0 = (double)z.x;
+        z1 = (double)z.y;
+    }
+}
+
+// Sums v[0..D) over the block; every thread receives the totals.  `sh`
+// holds 3 * 32 doubles.
+template <int D>
+__device__ __forceinline__ void block_sum_axes(double* v, double* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        const double t = warp_sum(v[a]);
+        if (lane == 0) sh[a * 32 + w] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double t = 0.0;
+        for (int k = 0; k < nw; ++k) t += sh[a * 32 + k];
+        v[a] = t;
+    }
+    __syncthreads();
+}
+
+// One pass over the momenta of a replica, element pairs (i, i+1) per thread
+// so that one Philox call serves both normals (pair index as in the
+// one-system kernels: (b D + a) ceil(N/2) + i/2).
+//   com_in:  subtract cm (a COM correction computed before this pass)
+//   kick:    p += dt/2 f
+//   o:       p = c1 p + c2 xi (substep)
+//   drift:   x += dt p / m
+// Returns the per-axis sums of the new p in `sum` (this thread's share).
+template <int D, typename R>
+__device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int substep, const double* cm, bool com_in,
+                                             bool kick, bool o, bool drift, double* sum) {
+    const int H = (s.N + 1) / 2;
+    const int total = s.P * H;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        sum[a] = 0.0;
+        for (int q = threadIdx.x; q < total; q += blockDim.x) {
+            const int b = q / H, i2 = q - b * H;
+            double z0 = 0.0, z1 = 0.0;
+            if (o) normal_pair<R>(s, step, substep, (uint32_t)((b * D + a) * H + i2), z0, z1);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int i = 2 * i2 + h;
+                if (i >= s.N) break;
+                const size_t e = idx<D>(s, b, a, i);
+                double p = s.p[e];
+                if (com_in) p -= cm[a];
+                if (kick) p += 0.5 * s.dt * s.f[e];
+                if (o) p = s.c1 * p + s.c2 * (h == 0 ? z0 : z1);
+                if (drift) s.x[e] += s.dt * p / s.mass;
+                s.p[e] = p;
+                sum[a] += p;
+            }
+        }
+    }
+}
+
+// Physical forces of bead b plus its interior springs, by one warp.  The
+// bead's positions are staged in `stage` (D N doubles for R = double; hi
+// and lo floats, D N each, for R = float).  Bosonic end beads keep the
+// physical part only: the exchange adds their springs.
+template <int D, typename R>
+__device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
+    const int N = s.N;
+    const bool pairs = s.int_kind != POT_FREE && s.cutoff != 0.0;
+    R* sh = stage;
+    R* sl = stage + D * N;
+    if (pairs) {
+        for (int a = 0; a < D; ++a)
+            for (int j = lane; j < N; j += 32) {
+                const double x = s.x[idx<D>(s, b, a, j)];
+                if constexpr (sizeof(R) == 8) {
+                    sh[a * N + j] = x;
+                } else {
+                    const float h = (float)x;
+                    sh[a * N + j] = h;
+                    sl[a * N + j] = (float)(x - (double)h);
+                }
+            }
+        __syncwarp();
+    }
+    const double cut = s.cutoff;
+    const R cut2 = (R)(cut * cut);
+    const R param = (R)s.int_a;
+    const bool bosonic_bead = s.bosonic && (b == 0 || b == s.P - 1);
+    const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
+    for (int i = lane; i < N; i += 32) {
+        double xi[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) xi[a] = s.x[idx<D>(s, b, a, i)];
+        double acc[D];
+        ext_force<D>(s, xi, acc);
+        if (pairs) {
+            R hi[D], lo[D];
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                hi[a] = sh[a * N + i];
+                lo[a] = (sizeof(R) == 8) ? (R)0 : sl[a * N + i];
+            }
+            for (int j0 = 0; j0 < N; j0 += 32) {
+                const int jn = min(32, N - j0);
+                R t[D];
+#pragma unroll
+                for (int a = 0; a < D; ++a) t[a] = (R)0;
+                for (int jj = 0; jj < jn; ++jj) {
+                    const int j = j0 + jj;
+                    if (j == i) continue;
+                    R r[D];
+                    R r2 = (R)0;
+#pragma unroll
+                    for (int a = 0; a < D; ++a) {
+                        R d;
+                        if constexpr (sizeof(R) == 8) {
+                            d = hi[a] - sh[a * N + j];
+                            if (s.pbc) d = min_image(d, s.L, s.invL);
+                        } else {
+                            d = (hi[a] - sh[a * N + j]) + (lo[a] - sl[a * N + j]);
+                            if (s.pbc) d = min_image_f(d, (float)s.L, (float)s.invL);
+                        }
+                        r[a] = d;
+                        r2 += d * d;
+                    }
+                    if (cut < 0.0 || r2 < cut2) {
+                        const R sc = pair_scale<R>(s.int_kind, r2, param);
+#pragma unroll
+                        for (int a = 0; a < D; ++a) t[a] -= sc * r[a];
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < D; ++a) acc[a] += (double)t[a];
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            const size_t o = idx<D>(s, b, a, i);
+            if (bosonic_bead) {
+                s.f[o] = acc[a];
+            } else {
+                double dp = s.x[idx<D>(s, bp, a, i)] - xi[a];
+                double dn = s.x[idx<D>(s, bn, a, i)] - xi[a];
+                if (s.pbc) {
+                    dp = min_image(dp, s.L, s.invL);
+                    dn = min_image(dn, s.L, s.invL);
+                }
+                s.f[o] = s.kappa * (dp + dn) + acc[a];  // simulation.cpp:405-419, :363-373
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// The Feldman-Hirshberg exchange of one replica by the whole block; adds the
+// exterior springs to f on beads 1 and P (which hold the physical forces).
+template <int D>
+__device__ void batch_exchange(const Sys& s, unsigned char* work) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int N = s.N;
+    for (int v = warp; v < N; v += nw) energy_row<D>(s, v, lane);
+    __syncthreads();
+    const int fresh = ((volatile int*)s.xflags)[3];
+    __syncthreads();
+    if (fresh) {
+        estimate_direction(s, 0, reinterpret_cast<float*>(work));
+        __syncthreads();
+        estimate_direction(s, 1, reinterpret_cast<float*>(work));
+        __syncthreads();
+    }
+    for (int p = warp; p < N; p += nw)
+        for (int u = lane; u <= p; u += 32) exch_weight(s, p, u);
+    __syncthreads();
+    solve_direction(s, 0, 0, reinterpret_cast<double*>(work));
+    __syncthreads();
+    solve_direction(s, 1, 0, reinterpret_cast<double*>(work));
+    __syncthreads();
+    solve_finish(s);
+    __syncthreads();
+    for (int w = warp; w < 2 * N; w += nw) exch_force_row<D>(s, w, lane, 1);
+}
+
+template <int D, typename R>
+__device__ void batch_replica(const Sys& s, int flags, long long step, int mode, double* red, unsigned char* work) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const bool langevin = flags & BF_LANGEVIN, fixcom = flags & BF_FIXCOM;
+    const double inv_np = 1.0 / ((double)s.N * s.P);
+    double cm[D], sum[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) cm[a] = 0.0;
+    if (mode & BM_HEAD) {
+        if (langevin || fixcom) {
+            momenta_pass<D, R>(s, step, 0, cm, false, false, langevin, false, sum);
+            if (fixcom) {
+                block_sum_axes<D>(sum, red);
+#pragma unroll
+                for (int a = 0; a < D; ++a) cm[a] = sum[a] * inv_np;
+            } else {
+                __syncthreads();
+            }
+        }
+        momenta_pass<D, R>(s, step, 0, cm, fixcom, true, false, true, sum);
+        __syncthreads();
+    }
+    if (mode & BM_FORCES) {
+        R* stage = reinterpret_cast<R*>(work) + (size_t)warp * ((sizeof(R) == 8 ? 1 : 2) * D * s.N);
+        for (int b = warp; b < s.P; b += nw) bead_forces_warp<D, R>(s, b, lane, stage);
+        __syncthreads();
+        if (s.bosonic) {
+            batch_exchange<D>(s, work);
+            __syncthreads();
+        }
+    }
+    if (mode & BM_TAIL) {
+        momenta_pass<D, R>(s, step, 1, cm, false, true, langevin, false, sum);
+        if (fixcom) {
+            block_sum_axes<D>(sum, red);
+#pragma unroll
+            for (int a = 0; a < D; ++a) cm[a] = sum[a] * inv_np;
+            momenta_pass<D, R>(s, step, 1, cm, true, false, false, false, sum);
+        }
+        __syncthreads();
+    }
+    if (mode & BM_ESTIMATORS) {
+        if (s.bosonic) estimators_block(s, s.P, reinterpret_cast<double*>(work));
+        __syncthreads();
+    }
+}
+
+// One launch: every replica through `mode`.  ctl[0] is the work counter,
+// ctl[1] counts finished CTAs; the last CTA resets both and, with
+// BM_ADVANCE, advances the step counter.
+template <int D, typename R>
+__global__ void __launch_bounds__(kBatchMaxThreads)
+    k_batch(const BatchRep* __restrict__ reps, const int* __restrict__ order, int nrep, int* ctl,
+            long long* step_ctr, int mode) {
+    extern __shared__ __align__(16) unsigned char bsm[];
+    double* red = reinterpret_cast<double*>(bsm);
+    unsigned char* work = bsm + 3 * 32 * sizeof(double);
+    __shared__ Sys ss;
+    __shared__ int item, sflags;
+    const long long step = *(volatile long long*)step_ctr;
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(&ctl[0], 1);
+        __syncthreads();
+        const int k = item;
+        if (k < nrep && threadIdx.x == 0) {
+            ss = reps[order[k]].s;
+            sflags = reps[order[k]].flags;
+        }
+        __syncthreads();
+        if (k >= nrep) break;
+        batch_replica<D, R>(ss, sflags, step, mode, red, work);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctl[1], 1) == (int)gridDim.x - 1) {
+            ctl[0] = 0;
+            ctl[1] = 0;
+            if (mode & BM_ADVANCE) *step_ctr = step + 1;
+            __threadfence();
+        }
+    }
+}
+
+// Host-layout <-> device-layout copies for every replica (blockIdx.y =
+// replica): which = 0 x, 1 p, 2 f.
+template <int D>
+__global__ void k_batch_pack(const BatchRep* __restrict__ reps, const size_t* __restrict__ hoff,
+                             const double* __restrict__ src, int which) {
+    const Sys& s = reps[blockIdx.y].s;
+    double* dst = which == 0 ? s.x : (which == 1 ? s.p : s.f);
+    const size_t n = (size_t)s.P * s.N * D;
+    const double* in = src + hoff[blockIdx.y];
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(e % D);
+        const size_t bi = e / D;
+        const int i = (int)(bi % s.N), b = (int)(bi / s.N);
+        dst[idx<D>(s, b, a, i)] = in[e];
+    }
+}
+
+template <int D>
+__global__ void k_batch_unpack(const BatchRep* __restrict__ reps, const size_t* __restrict__ hoff,
+                               double* __restrict__ out_all, int which) {
+    const Sys& s = reps[blockIdx.y].s;
+    const double* src = which == 0 ? s.x : (which == 1 ? s.p : s.f);
+    const size_t n = (size_t)s.P * s.N * D;
+    double* out = out_all + hoff[blockIdx.y];
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(e % D);
+        const size_t bi = e / D;
+        const int i = (int)(bi % s.N), b = (int)(bi / s.N);
+        out[e] = src[idx<D>(s, b, a, i)];
+    }
+}
+
+// After new coordinates: forces to zero (the reference's constructor never
+// evaluates them), a fresh FP32 exchange estimate, cleared error word.
+__global__ void k_batch_reset(const BatchRep* __restrict__ reps, int D) {
+    const Sys& s = reps[blockIdx.x].s;
+    const size_t n = (size_t)s.P * D * s.ld;
+    for (size_t e = threadIdx.x; e < n; e += blockDim.x) s.f[e] = 0.0;
+    for (size_t e = threadIdx.x; e < (size_t)2 * D * s.ld; e += blockDim.x) s.fx[e] = 0.0;
+    if (threadIdx.x < 8) s.xflags[threadIdx.x] = threadIdx.x == 3 ? 1 : 0;
+    if (threadIdx.x == 0) *s.err = 0;
+}
+
+}  // namespace pimdb
+
+using namespace pimdb;
+
+// --------------------------------------------------------------------- host
+struct pimdb_batch {
+    int nrep = 0, D = 3, mixed = 0;
+    std::vector<pimdb_config> cfgs;
+    std::vector<BatchRep> reps;
+    std::vector<size_t> hoff;  // replica offsets in the host layout (doubles)
+    size_t htotal = 0;
+    std::vector<int> order;
+    BatchRep* d_reps = nullptr;
+    int* d_order = nullptr;
+    size_t* d_hoff = nullptr;
+    int* d_ctl = nullptr;
+    long long* d_step = nullptr;
+    int* d_err = nullptr;       // one word per replica
+    int* d_iflags = nullptr;    // 8 exchange flags per replica
+    double* d_scal = nullptr;   // [nrep][4]
+    double* pool = nullptr;
+    size_t pool_doubles = 0;
+    double* d_stage = nullptr;  // host-layout staging (htotal doubles)
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int threads = 256, ctas_per_sm = 2, grid = 1, maxN = 1, sms = 1;
+    size_t smem = 0;
+    bool use_graph = true;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0, graph_threads = 0, graph_grid = 0;
+    long long step = 0;
+    long long launches = 0;
+    std::string err;
+};
+
+static thread_local std::string g_batch_error;
+
+static int bfail(pimdb_batch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    g_batch_error = msg;
+    return code;
+}
+
+#define BATCH_CUDA(b, expr)                                                               \
+    do {                                                                                  \
+        cudaError_t e_ = (expr);                                                          \
+        if (e_ != cudaSuccess) return bfail(b, PIMDB_ERR_CUDA, cudaGetErrorString(e_));   \
+    } while (0)
+
+static size_t batch_smem(int D, int maxN, int threads) {
+    const size_t nw = threads / 32;
+    const size_t stage = nw * (size_t)D * maxN * sizeof(double);
+    const size_t est = sizeof(float) * 3 * (size_t)(maxN + 1);
+    const size_t solve = sizeof(double) * (2 * (size_t)(maxN + 1) + 32);
+    const size_t estim = sizeof(double) * ((size_t)maxN + 1 + 32);
+    return 3 * 32 * sizeof(double) + std::max(std::max(stage, est), std::max(solve, estim));
+}
+
+template <typename F>
+static void with_kernel(int D, int mixed, F&& f) {
+    if (mixed) {
+        if (D == 1) f(k_batch<1, float>);
+        else if (D == 2) f(k_batch<2, float>);
+        else f(k_batch<3, float>);
+    } else {
+        if (D == 1) f(k_batch<1, double>);
+        else if (D == 2) f(k_batch<2, double>);
+        else f(k_batch<3, double>);
+    }
+}
+
+static int configure_launch(pimdb_batch* b, int threads, int ctas_per_sm) {
+    if (threads < 32 || threads > kBatchMaxThreads || threads % 32) return bfail(b, PIMDB_ERR_ARG, "threads must be a multiple of 32 in [32, 512]");
+    if (ctas_per_sm < 1) return bfail(b, PIMDB_ERR_ARG, "ctas_per_sm must be >= 1");
+    const size_t smem = batch_smem(b->D, b->maxN, threads);
+    int resident = 0;
+    cudaError_t e = cudaSuccess;
+    with_kernel(b->D, b->mixed, [&](auto k) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k, threads, smem);
+    });
+    if (e != cudaSuccess) return bfail(b, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    if (resident < 1) return bfail(b, PIMDB_ERR_CONFIG, "batched kernel does not fit on an SM with this block size");
+    b->threads = threads;
+    b->ctas_per_sm = std::min(ctas_per_sm, resident);
+    b->smem = smem;
+    b->grid = std::max(1, std::min(b->nrep, b->sms * b->ctas_per_sm));
+    return PIMDB_OK;
+}
+
+static void launch_batch(pimdb_batch* b, int mode) {
+    with_kernel(b->D, b->mixed, [&](auto k) {
+        k<<<b->grid, b->threads, b->smem, b->stream>>>(b->d_reps, b->d_order, b->nrep, b->d_ctl, b->d_step, mode);
+    });
+    ++b->launches;
+}
+
+static void free_batch(pimdb_batch* b) {
+    if (!b) return;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    cudaFree(b->d_reps);
+    cudaFree(b->d_order);
+    cudaFree(b->d_hoff);
+    cudaFree(b->d_ctl);
+    cudaFree(b->d_step);
+    cudaFree(b->d_err);
+    cudaFree(b->d_iflags);
+    cudaFree(b->d_scal);
+    cudaFree(b->pool);
+    cudaFree(b->d_stage);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void* cuda_stream, pimdb_batch** out) {
+    if (!cfgs || !out || nreplicas < 1) return bfail(nullptr, PIMDB_ERR_ARG, "NULL argument or no replicas");
+    *out = nullptr;
+    const int D = cfgs[0].ndim, precision = cfgs[0].precision;
+    for (int r = 0; r < nreplicas; ++r) {
+        const pimdb_config& c = cfgs[r];
+        const std::string why = validate_config(c);
+        if (!why.empty()) return bfail(nullptr, PIMDB_ERR_CONFIG, "replica " + std::to_string(r) + ": " + why);
+        if (c.ndim != D) return bfail(nullptr, PIMDB_ERR_CONFIG, "every replica of a batch must have the same ndim");
+        if (c.precision != precision)
+            return bfail(nullptr, PIMDB_ERR_CONFIG, "every replica of a batch must have the same precision");
+        if (c.propagator != PIMDB_PROP_CARTESIAN || c.nmthermostat)
+            return bfail(nullptr, PIMDB_ERR_CONFIG,
+                         "replica " + std::to_string(r) +
+                             ": the batched engine runs the cartesian propagator with the cartesian Langevin thermostat");
+        if (c.natoms > 2048) return bfail(nullptr, PIMDB_ERR_CONFIG, "the batched engine supports at most 2048 particles per replica");
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return bfail(nullptr, PIMDB_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    pimdb_batch* b = new (std::nothrow) pimdb_batch();
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "out of host memory");
+    b->nrep = nreplicas;
+    b->D = D;
+    b->mixed = precision == PIMDB_MIXED;
+    b->cfgs.assign(cfgs, cfgs + nreplicas);
+    b->reps.resize(nreplicas);
+    b->hoff.resize(nreplicas);
+    // pool layout: every array rounded up to 32 doubles (256 bytes)
+    auto up = [](size_t n) { return (n + 31) / 32 * 32; };
+    std::vector<std::vector<size_t>> offs(nreplicas);
+    size_t off = 0, hoff = 0;
+    for (int r = 0; r < nreplicas; ++r) {
+        Sys s{};
+        sys_params_from_config(cfgs[r], s);
+        b->maxN = std::max(b->maxN, s.N);
+        const size_t nstate = (size_t)s.P * D * s.ld;
+        const size_t ntri = s.bosonic ? (size_t)s.N * (s.N + 1) / 2 : 1;
+        const size_t sizes[] = {nstate, nstate, nstate, (size_t)2 * D * s.ld, ntri, ntri, ntri, ntri,
+                                (size_t)s.N + 1, (size_t)s.N + 1, (size_t)s.N + 1, (size_t)s.N + 1,
+                                (size_t)s.N + 1, (size_t)s.N + 1, (size_t)s.N, (size_t)s.N};
+        for (size_t n : sizes) {
+            offs[r].push_back(off);
+            off += up(n);
+        }
+        b->reps[r].s = s;
+        b->reps[r].flags = (cfgs[r].thermostat == PIMDB_THERMO_LANGEVIN ? BF_LANGEVIN : 0) | (cfgs[r].fixcom ? BF_FIXCOM : 0);
+        b->hoff[r] = hoff;
+        hoff += (size_t)s.P * s.N * D;
+    }
+    b->pool_doubles = off;
+    b->htotal = hoff;
+    cudaError_t e = cudaSuccess;
+    if (cuda_stream) {
+        b->stream = (cudaStream_t)cuda_stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        b->own_stream = (e == cudaSuccess);
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->pool, std::max<size_t>(off, 1) * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(b->pool, 0, std::max<size_t>(off, 1) * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_err, sizeof(int) * nreplicas);
+    if (e == cudaSuccess) e = cudaMemset(b->d_err, 0, sizeof(int) * nreplicas);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_iflags, sizeof(int) * 8 * nreplicas);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_scal, sizeof(double) * 4 * nreplicas);
+    if (e == cudaSuccess) e = cudaMemset(b->d_scal, 0, sizeof(double) * 4 * nreplicas);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_ctl, sizeof(int) * 2);
+    if (e == cudaSuccess) e = cudaMemset(b->d_ctl, 0, sizeof(int) * 2);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_step, sizeof(long long));
+    if (e == cudaSuccess) e = cudaMemset(b->d_step, 0, sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_stage, std::max<size_t>(hoff, 1) * sizeof(double));
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return bfail(nullptr, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    }
+    std::vector<int> iflags(8 * (size_t)nreplicas, 0);
+    for (int r = 0; r < nreplicas; ++r) {
+        Sys& s = b->reps[r].s;
+        const size_t* o = offs[r].data();
+        double* P = b->pool;
+        s.x = P + o[0];
+        s.p = P + o[1];
+        s.f = P + o[2];
+        s.fphys = nullptr;
+        s.fx = P + o[3];
+        s.E = P + o[4];
+        s.Et = P + o[5];
+        s.Wf = P + o[6];
+        s.Wb = P + o[7];
+        s.V = P + o[8];
+        s.Vb = P + o[9];
+        s.Vh = P + o[10];
+        s.Vbh = P + o[11];
+        s.yf = P + o[12];
+        s.yb = P + o[13];
+        s.rowR = P + o[14];
+        s.rowC = P + o[15];
+        s.scal = b->d_scal + 4 * (size_t)r;
+        s.red = nullptr;
+        s.err = b->d_err + r;
+        s.xflags = b->d_iflags + 8 * (size_t)r;
+        iflags[8 * (size_t)r + 3] = 1;
+    }
+    // largest replicas first: pair work P N^2, exchange N^2 FP64 exponentials
+    b->order.resize(nreplicas);
+    std::iota(b->order.begin(), b->order.end(), 0);
+    auto cost = [&](int r) {
+        const Sys& s = b->reps[r].s;
+        const double n = s.N, p = s.P;
+        return p * n * (n + 32.0) + (s.bosonic ? 64.0 * n * n : 0.0);
+    };
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int a, int c) { return cost(a) > cost(c); });
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_reps, sizeof(BatchRep) * nreplicas);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_reps, b->reps.data(), sizeof(BatchRep) * nreplicas, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_order, sizeof(int) * nreplicas);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_order, b->order.data(), sizeof(int) * nreplicas, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_hoff, sizeof(size_t) * nreplicas);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_hoff, b->hoff.data(), sizeof(size_t) * nreplicas, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_iflags, iflags.data(), sizeof(int) * iflags.size(), cudaMemcpyHostToDevice);
+    int dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return bfail(nullptr, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const int st = configure_launch(b, 256, 2);
+    if (st != PIMDB_OK) {
+        const std::string msg = b->err;
+        free_batch(b);
+        return bfail(nullptr, st, msg);
+    }
+    *out = b;
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_batch_destroy(pimdb_batch* b) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    cudaStreamSynchronize(b->stream);
+    free_batch(b);
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_batch_size(const pimdb_batch* b, int* nreplicas, long long* host_doubles) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    if (nreplicas) *nreplicas = b->nrep;
+    if (host_doubles) *host_doubles = (long long)b->htotal;
+    return PIMDB_OK;
+}
+
+static int check_errors(pimdb_batch* b) {
+    std::vector<int> errs(b->nrep);
+    BATCH_CUDA(b, cudaMemcpyAsync(errs.data(), b->d_err, sizeof(int) * b->nrep, cudaMemcpyDeviceToHost, b->stream));
+    BATCH_CUDA(b, cudaStreamSynchronize(b->stream));
+    for (int r = 0; r < b->nrep; ++r)
+        if (errs[r] & ERRB_NONFINITE_VB)
+            return bfail(b, PIMDB_ERR_NONFINITE_VB,
+                         "replica " + std::to_string(r) + ": Invalid sig_denom in bosonic exchange potential");
+    return PIMDB_OK;
+}
+
+// All replicas from host arrays concatenated in replica order, each
+// [bead][particle][axis]; x or p may be NULL to keep the current values.
+extern "C" int pimdb_batch_set_states(pimdb_batch* b, const double* x, const double* p) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    const double* src[2] = {x, p};
+    for (int k = 0; k < 2; ++k) {
+        if (!src[k]) continue;
+        BATCH_CUDA(b, cudaMemcpyAsync(b->d_stage, src[k], b->htotal * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+        dim3 grid(8, b->nrep);
+        if (b->D == 1) k_batch_pack<1><<<grid, 256, 0, b->stream>>>(b->d_reps, b->d_hoff, b->d_stage, k);
+        else if (b->D == 2) k_batch_pack<2><<<grid, 256, 0, b->stream>>>(b->d_reps, b->d_hoff, b->d_stage, k);
+        else k_batch_pack<3><<<grid, 256, 0, b->stream>>>(b->d_reps, b->d_hoff, b->d_stage, k);
+        ++b->launches;
+    }
+    k_batch_reset<<<b->nrep, 256, 0, b->stream>>>(b->d_reps, b->D);
+    ++b->launches;
+    BATCH_CUDA(b, cudaGetLastError());
+    BATCH_CUDA(b, cudaStreamSynchronize(b->stream));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_batch_get_states(pimdb_batch* b, double* x, double* p, double* f) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    double* dst[3] = {x, p, f};
+    for (int k = 0; k < 3; ++k) {
+        if (!dst[k]) continue;
+        dim3 grid(8, b->nrep);
+        if (b->D == 1) k_batch_unpack<1><<<grid, 256, 0, b->stream>>>(b->d_reps, b->d_hoff, b->d_stage, k);
+        else if (b->D == 2) k_batch_unpack<2><<<grid, 256, 0, b->stream>>>(b->d_reps, b->d_hoff, b->d_stage, k);
+        else k_batch_unpack<3><<<grid, 256, 0, b->stream>>>(b->d_reps, b->d_hoff, b->d_stage, k);
+        ++b->launches;
+        BATCH_CUDA(b, cudaMemcpyAsync(dst[k], b->d_stage, b->htotal * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    }
+    BATCH_CUDA(b, cudaGetLastError());
+    BATCH_CUDA(b, cudaStreamSynchronize(b->stream));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_batch_set_step(pimdb_batch* b, long long step) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    BATCH_CUDA(b, cudaMemcpyAsync(b->d_step, &step, sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+    BATCH_CUDA(b, cudaStreamSynchronize(b->stream));
+    b->step = step;
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_batch_get_step(pimdb_batch* b, long long* step) {
+    if (!b || !step) return bfail(b, PIMDB_ERR_ARG, "NULL argument");
+    BATCH_CUDA(b, cudaMemcpyAsync(step, b->d_step, sizeof(long long), cudaMemcpyDeviceToHost, b->stream));
+    BATCH_CUDA(b, cudaStreamSynchronize(b->stream));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_batch_compute_forces(pimdb_batch* b) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    launch_batch(b, BM_FORCES);
+    BATCH_CUDA(b, cudaGetLastError());
+    return check_errors(b);
+}
+
+static int enqueue_batch_steps(pimdb_batch* b, int nsteps) {
+    const int mode = BM_HEAD | BM_FORCES | BM_TAIL | BM_ADVANCE;
+    if (!b->use_graph || nsteps == 1) {
+        for (int k = 0; k < nsteps; ++k) launch_batch(b, mode);
+        BATCH_CUDA(b, cudaGetLastError());
+        return PIMDB_OK;
+    }
+    if (!b->graph || b->graph_steps != nsteps || b->graph_threads != b->threads || b->graph_grid != b->grid) {
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        BATCH_CUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const long long before = b->launches;
+        for (int k = 0; k < nsteps; ++k) launch_batch(b, mode);
+        b->launches = before;
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->graph = nullptr;
+            return bfail(b, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+        }
+        b->graph_steps = nsteps;
+        b->graph_threads = b->threads;
+        b->graph_grid = b->grid;
+    }
+    BATCH_CUDA(b, cudaGraphLaunch(b->graph, b->stream));
+    b->launches += nsteps;
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_batch_step_async(pimdb_batch* b, int nsteps) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    if (nsteps < 0) return bfail(b, PIMDB_ERR_ARG, "nsteps < 0");
+    if (nsteps == 0) return PIMDB_OK;
+    const int st = enqueue_batch_steps(b, nsteps);
+    if (st == PIMDB_OK) b->step += nsteps;
+    return st;
+}
+
+extern "C" int pimdb_batch_step(pimdb_batch* b, int nsteps) {
+    const int st = pimdb_batch_step_async(b, nsteps);
+    if (st != PIMDB_OK) return st;
+    return check_errors(b);
+}
+
+extern "C" int pimdb_batch_synchronize(pimdb_batch* b) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    return check_errors(b);
+}
+
+// V_B, primEstimator, P_distinct and P_longest of every replica at the
+// current coordinates (forces are evaluated first); scalars [nrep][4]
+// (zeros for distinguishable replicas).
+extern "C" int pimdb_batch_exchange(pimdb_batch* b, double* scalars) {
+    if (!b || !scalars) return bfail(b, PIMDB_ERR_ARG, "NULL argument");
+    launch_batch(b, BM_FORCES | BM_ESTIMATORS);
+    BATCH_CUDA(b, cudaGetLastError());
+    const int st = check_errors(b);
+    if (st != PIMDB_OK) return st;
+    BATCH_CUDA(b, cudaMemcpyAsync(scalars, b->d_scal, sizeof(double) * 4 * b->nrep, cudaMemcpyDeviceToHost, b->stream));
+    BATCH_CUDA(b, cudaStreamSynchronize(b->stream));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_batch_set_option(pimdb_batch* b, const char* name, int value) {
+    if (!b || !name) return bfail(b, PIMDB_ERR_ARG, "NULL argument");
+    if (!strcmp(name, "threads")) return configure_launch(b, value, b->ctas_per_sm);
+    if (!strcmp(name, "ctas_per_sm")) return configure_launch(b, b->threads, value);
+    if (!strcmp(name, "graph")) {
+        b->use_graph = value != 0;
+        return PIMDB_OK;
+    }
+    return bfail(b, PIMDB_ERR_ARG, std::string("unknown option ") + name);
+}
+
+extern "C" int pimdb_batch_get_launch(pimdb_batch* b, int* threads, int* ctas_per_sm, int* grid, long long* launches) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    if (threads) *threads = b->threads;
+    if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+    if (grid) *grid = b->grid;
+    if (launches) *launches = b->launches;
+    return PIMDB_OK;
+}
+
+// Block shape of the step kernel chosen by measurement: every candidate
+// (threads per CTA x CTAs per SM that fit) runs `steps` steps from a copy of
+// the current device state, timed with events; the fastest is kept and the
+// state, the exchange estimates and the step counter are restored.
+extern "C" int pimdb_batch_autotune(pimdb_batch* b, int steps, int* threads, int* ctas_per_sm) {
+    if (!b) return bfail(nullptr, PIMDB_ERR_ARG, "NULL batch");
+    if (steps < 1) steps = 2;
+    double* snap = nullptr;
+    int* fsnap = nullptr;
+    long long step0 = 0;
+    BATCH_CUDA(b, cudaStreamSynchronize(b->stream));
+    BATCH_CUDA(b, cudaMalloc((void**)&snap, b->pool_doubles * sizeof(double)));
+    cudaError_t e = cudaMalloc((void**)&fsnap, sizeof(int) * 8 * b->nrep);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(snap, b->pool, b->pool_doubles * sizeof(double), cudaMemcpyDeviceToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fsnap, b->d_iflags, sizeof(int) * 8 * b->nrep, cudaMemcpyDeviceToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&step0, b->d_step, sizeof(long long), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&t1);
+    const int old_threads = b->threads, old_ctas = b->ctas_per_sm;
+    const bool old_graph = b->use_graph;
+    b->use_graph = false;
+    int best_t = old_threads, best_c = old_ctas;
+    float best_ms = 1e30f;
+    const int cand_t[] = {128, 256, 512};
+    const int cand_c[] = {1, 2, 3, 4};
+    for (int ti = 0; ti < 3 && e == cudaSuccess; ++ti) {
+        for (int ci = 0; ci < 4 && e == cudaSuccess; ++ci) {
+            if (configure_launch(b, cand_t[ti], cand_c[ci]) != PIMDB_OK) continue;
+            if (b->ctas_per_sm != cand_c[ci]) continue;  // does not fit
+            enqueue_batch_steps(b, 1);  // warm-up
+            e = cudaEventRecord(t0, b->stream);
+            if (e == cudaSuccess) enqueue_batch_steps(b, steps);
+            if (e == cudaSuccess) e = cudaEventRecord(t1, b->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(t1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t0, t1);
+            if (e == cudaSuccess && ms < best_ms) {
+                best_ms = ms;
+                best_t = cand_t[ti];
+                best_c = cand_c[ci];
+            }
+            if (e == cudaSuccess) e = cudaMemcpyAsync(b->pool, snap, b->pool_doubles * sizeof(double), cudaMemcpyDeviceToDevice, b->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_iflags, fsnap, sizeof(int) * 8 * b->nrep, cudaMemcpyDeviceToDevice, b->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_step, &step0, sizeof(long long), cudaMemcpyHostToDevice, b->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        }
+    }
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    cudaFree(snap);
+    cudaFree(fsnap);
+    b->use_graph = old_graph;
+    if (e != cudaSuccess) return bfail(b, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    const int st = configure_launch(b, best_t, best_c);
+    if (st != PIMDB_OK) return st;
+    if (threads) *threads = b->threads;
+    if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+    return check_errors(b);
+}
+
+extern "C" int pimdb_batch_last_error(const pimdb_batch* b, char* buf, int len) {
+    const std::string& m = b ? b->err : g_batch_error;
+    if (buf && len > 0) {
+        std::snprintf(buf, (size_t)len, "%s", m.c_str());
+    }
+    return PIMDB_OK;
+}

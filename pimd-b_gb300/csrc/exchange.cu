@@ -32,495 +32,65 @@
 // non-finite input), the solve kernel recomputes the level-by-level FP64
 // log-sum-exp in the reference's own order instead.  The backward recursion
 // is handled the same way by the second block of each kernel.
-#include <math_constants.h>
-
-#include "common.cuh"
+#include "exchange_dev.cuh"
 #include "kernels.h"
 
 namespace pimdb {
 
-__device__ __forceinline__ size_t tri(int v) { return (size_t)v * (size_t)(v + 1) / 2; }
-
-template <int D>
-__device__ __forceinline__ double sepsq(const Sys& s, int ba, int ia, int bb, int ib) {
-    // |x_bb[ib] - x_ba[ia]|^2 with the minimum image (bosonic_exchange_base.cpp:30-64)
-    double d2 = 0.0;
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-        double d = s.x[idx<D>(s, bb, a, ib)] - s.x[idx<D>(s, ba, a, ia)];
-        if (s.pbc) d = min_image(d, s.L, s.invL);
-        d2 += d * d;
-    }
-    return d2;
-}
-
-// One warp per row v: E[v][v] = k/2 |xP_v - x1_v|^2, then
-// E[v][u] = E[v][u+1] + k/2 (|x1_{u+1} - xP_u|^2 - |xP_v - x1_{u+1}|^2 + |xP_v - x1_u|^2)
-// for u = v-1 .. 0, evaluated as a warp-wide suffix scan over u.  The middle
-// distance of entry u is the last distance of entry u+1, so each entry costs
-// two distance evaluations (passed between lanes by a shuffle).
+// Cycle energies: one warp per row.
 template <int D>
 __global__ void k_exch_energies(Sys s) {
     const int lane = threadIdx.x & 31;
     const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (v >= s.N) return;
-    const int first = 0, last = s.P - 1;
-    const double hk = 0.5 * s.kappa;
-    double* row = s.E + tri(v);
-    double xv[D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) xv[a] = s.x[idx<D>(s, last, a, v)];
-    auto dist_to_v = [&](int u) {  // |xP_v - x1_u|^2
-        double d2 = 0.0;
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-            double d = xv[a] - s.x[idx<D>(s, first, a, u)];
-            if (s.pbc) d = min_image(d, s.L, s.invL);
-            d2 += d * d;
-        }
-        return d2;
-    };
-    double cnext = dist_to_v(v);  // |xP_v - x1_{u+1}|^2 for the lane holding u = base
-    double carry = hk * cnext;
-    if (lane == 0) row[v] = carry;
-    for (int base = v - 1; base >= 0; base -= 32) {
-        const int u = base - lane;
-        const double c = u >= 0 ? dist_to_v(u) : 0.0;
-        double cu1 = __shfl_up_sync(0xffffffffu, c, 1);
-        if (lane == 0) cu1 = cnext;
-        double term = 0.0;
-        if (u >= 0) term = hk * (sepsq<D>(s, last, u, first, u + 1) - cu1 + c);
-        cnext = __shfl_sync(0xffffffffu, c, 31);
-        // inclusive scan over lanes (lane 0 holds the largest u)
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double y = __shfl_up_sync(0xffffffffu, term, o);
-            if (lane >= o) term += y;
-        }
-        if (u >= 0) {
-            const double e = carry + term;
-            row[u] = e;
-            // backward node r = N - u depends on node r' = N - 1 - v
-            if (u >= 1) s.Et[tri(s.N - u - 1) + (s.N - 1 - v)] = e;
-        }
-        carry += __shfl_sync(0xffffffffu, term, 31);
-    }
-    if (lane == 0 && v >= 1) s.Et[tri(s.N - v - 1) + (s.N - 1 - v)] = row[v];
+    energy_row<D>(s, v, lane);
 }
 
-__device__ __forceinline__ void lse_add(float& mx, float& sm, float t) {
-    if (t > mx) {
-        sm = sm * __expf(mx - t) + 1.0f;
-        mx = t;
-    } else {
-        sm += __expf(t - mx);
-    }
-}
-
-// The recursions as "node" recursions.  Forward: node n = level m = n,
-// node 0 known (V = 0), node n depends on nodes u < n through the packed row
-// E[n-1][u].  Backward: node r = N - l, node 0 (l = N) known, node r depends
-// on nodes r' < r through Et[r-1][r'] = E[p][l] with p = N - 1 - r' (so
-// p + 1 = N - r').  Both are evaluated by the same blocked scheme: nodes are
-// taken 32 at a time; warp 0 resolves the 32 nodes of a block one after the
-// other with shuffles (no barrier), then every thread folds the finished
-// block into the accumulators of all later nodes (one barrier pair per 32
-// nodes instead of one barrier per node).
-constexpr int kWaveThreads = 256;
-
-// FP32 log-sum-exp node recursion.  fwd: value(n) = -(LSE - log n)/beta;
-// bwd: terms carry -log(N - r') and value(r) = -LSE/beta.
-__device__ void blocked_estimate(const double* __restrict__ Eg, int nn, int N, float beta, bool fwd, float* val,
-                                 float* amx, float* asm_) {
-    const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, warp = tid >> 5;
-    for (int n = tid; n < nn; n += bd) {
-        amx[n] = -CUDART_INF_F;
-        asm_[n] = 0.0f;
-    }
-    __syncthreads();
-    const int nb = (nn + 31) / 32;
-    for (int b = 0; b < nb; ++b) {
-        const int base = 32 * b;
-        if (warp == 0) {
-            const int n = base + lane;
-            float mx = n < nn ? amx[n] : -CUDART_INF_F, sm = n < nn ? asm_[n] : 0.0f;
-            float e[32];
-#pragma unroll
-            for (int t = 0; t < 32; ++t) e[t] = (n < nn && n >= 1 && t < lane) ? (float)Eg[tri(n - 1) + base + t] : 0.0f;
-            float v = 0.0f;
-#pragma unroll
-            for (int t = 0; t < 32; ++t) {
-                if (lane == t && n < nn && n >= 1)
-                    v = -(mx + __logf(sm) - (fwd ? __logf((float)n) : 0.0f)) / beta;
-                const float vt = __shfl_sync(0xffffffffu, v, t);
-                if (lane > t && n < nn) {
-                    const int u = base + t;
-                    lse_add(mx, sm, -beta * (e[t] + vt) - (fwd ? 0.0f : __logf((float)(N - u))));
-                }
-            }
-            if (n < nn) val[n] = v;
-        }
-        __syncthreads();
-        for (int m = base + 32 + tid; m < nn; m += bd) {
-            float t[32];
-            float lmx = -CUDART_INF_F;
-#pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                const int u = base + q;
-                t[q] = -beta * ((float)Eg[tri(m - 1) + u] + val[u]) - (fwd ? 0.0f : __logf((float)(N - u)));
-                lmx = fmaxf(lmx, t[q]);
-            }
-            float ls = 0.0f;
-#pragma unroll
-            for (int q = 0; q < 32; ++q) ls += __expf(t[q] - lmx);
-            float mx = amx[m], sm = asm_[m];
-            if (lmx > mx) {
-                sm = sm * __expf(mx - lmx) + ls;
-                mx = lmx;
-            } else {
-                sm += ls * __expf(lmx - mx);
-            }
-            amx[m] = mx;
-            asm_[m] = sm;
-        }
-        __syncthreads();
-    }
-}
-
-// FP64 triangular node solve: y(0) = 1, y(n) = sum_{u<n} W[n-1][u] y(u).
-__device__ void blocked_solve(const double* __restrict__ W, int nn, double* y, double* acc) {
-    const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, warp = tid >> 5;
-    for (int n = tid; n < nn; n += bd) acc[n] = 0.0;
-    __syncthreads();
-    const int nb = (nn + 31) / 32;
-    for (int b = 0; b < nb; ++b) {
-        const int base = 32 * b;
-        if (warp == 0) {
-            const int n = base + lane;
-            double a = n == 0 ? 1.0 : (n < nn ? acc[n] : 0.0);
-            double w[32];
-#pragma unroll
-            for (int t = 0; t < 32; ++t) w[t] = (n < nn && n >= 1 && t < lane) ? W[tri(n - 1) + base + t] : 0.0;
-#pragma unroll
-            for (int t = 0; t < 32; ++t) {
-                const double yt = __shfl_sync(0xffffffffu, a, t);
-                if (lane > t) a = fma(w[t], yt, a);
-            }
-            if (n < nn) y[n] = a;
-        }
-        __syncthreads();
-        for (int m = base + 32 + tid; m < nn; m += bd) {
-            const double* row = W + tri(m - 1) + base;
-            double sacc = acc[m];
-#pragma unroll 8
-            for (int q = 0; q < 32; ++q) sacc = fma(row[q], y[base + q], sacc);
-            acc[m] = sacc;
-        }
-        __syncthreads();
-    }
-}
-
-// Pass 1: FP32 estimates (block 0 forward, block 1 backward).  Skipped
-// (early exit) when the previous evaluation's exact potentials are still a
-// good estimate (xflags[3] == 0).
+// Pass 1: block 0 forward, block 1 backward.  Skipped (early exit) when the
+// previous evaluation's exact potentials are still a good estimate
+// (xflags[3] == 0).
 __global__ void __launch_bounds__(kWaveThreads) k_exch_estimate(Sys s) {
     if (((volatile int*)s.xflags)[3] == 0) return;
     extern __shared__ float fsm[];  // 3 (N+1)
-    const int N = s.N;
-    float* val = fsm;
-    float* amx = fsm + (N + 1);
-    float* asm_ = fsm + 2 * (N + 1);
-    const float beta = (float)s.beta_ex;
-    if (blockIdx.x == 0) {
-        blocked_estimate(s.E, N + 1, N, beta, true, val, amx, asm_);
-        for (int m = threadIdx.x; m <= N; m += blockDim.x) s.Vh[m] = (double)val[m];
-    } else {
-        // nodes r = 0..N-1 <-> l = N..1
-        blocked_estimate(s.Et, N, N, beta, false, val, amx, asm_);
-        for (int l = threadIdx.x; l <= N; l += blockDim.x) s.Vbh[l] = (l >= 1) ? (double)val[N - l] : 0.0;
-    }
+    estimate_direction(s, blockIdx.x, fsm);
 }
 
-// Pass 2: every FP64 exponential, one thread per packed entry (row p, column u).
+// Pass 2: every FP64 exponential at once, one thread per packed entry.
 __global__ void k_exch_weights(Sys s) {
     const int p = blockIdx.y;
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u > p) return;
-    const double beta = s.beta_ex;
-    const size_t e = tri(p) + u;
-    const double E = s.E[e];
-    const double inv = 1.0 / (p + 1);
-    s.Wf[e] = exp(-beta * (E + s.Vh[u] - s.Vh[p + 1])) * inv;
-    // backward node r = N - u from node r' = N - 1 - p (u >= 1)
-    if (u >= 1) s.Wb[tri(s.N - u - 1) + (s.N - 1 - p)] = exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u])) * inv;
+    exch_weight(s, p, u);
 }
 
-// Exact level-by-level FP64 log-sum-exp in the reference's order (used only
-// when the estimate is unusable, or on request).  `vs` holds N+1 doubles,
-// `red` 32.
-__device__ void exact_forward(const Sys& s, double* vs, double* red) {
-    const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
-    const double beta = s.beta_ex;
-    if (tid == 0) vs[0] = 0.0;
-    __syncthreads();
-    for (int m = 1; m <= N; ++m) {
-        const double* row = s.E + tri(m - 1);
-        double lmin = 1.79769313486231570815e308;
-        for (int u = tid; u < m; u += bd) lmin = fmin(lmin, row[u] + vs[u]);
-        const double shift = block_min(lmin, red);
-        double ls = 0.0;
-        for (int u = tid; u < m; u += bd) ls += exp(-beta * (row[u] + vs[u] - shift));
-        const double tot = block_sum(ls, red);
-        if (tid == 0) vs[m] = shift - (1.0 / beta) * log(tot / (double)m);
-        __syncthreads();
-    }
-}
-
-__device__ void exact_backward(const Sys& s, double* vs, double* red) {
-    const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
-    const double beta = s.beta_ex;
-    if (tid == 0) vs[N] = 0.0;
-    __syncthreads();
-    for (int l = N - 1; l > 0; --l) {
-        double lmin = 1.79769313486231570815e308;
-        for (int p = l + tid; p < N; p += bd) lmin = fmin(lmin, s.E[tri(p) + l] + vs[p + 1]);
-        const double shift = block_min(lmin, red);
-        double ls = 0.0;
-        for (int p = l + tid; p < N; p += bd) ls += exp(-beta * (s.E[tri(p) + l] + vs[p + 1] - shift)) / (p + 1);
-        const double tot = block_sum(ls, red);
-        if (tid == 0) vs[l] = shift - log(tot) / beta;
-        __syncthreads();
-    }
-}
-
-// |log y| above which the next evaluation computes a fresh FP32 estimate
-// instead of reusing the current potentials, and above which the present
-// evaluation switches to the exact level-by-level recursion.
-constexpr double kRefreshLogY = 30.0;
-constexpr double kExactLogY = 200.0;
-
-// Pass 3: y solves, exact V / V_backwards, and (by the block that finishes
-// last) the per-row factors of the connection probabilities.
+// Pass 3: block 0 forward, block 1 backward.
 __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_exact) {
     extern __shared__ double ys[];  // y: N+1, acc: N+1, then 32 for reductions
-    double* acc = ys + s.N + 1;
-    double* red = ys + 2 * (s.N + 1);
     __shared__ int last_block;
-    const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
-    const double beta = s.beta_ex;
-    int bad = force_exact, stale = 0;
-    if (blockIdx.x == 0) {
-        if (!force_exact) {
-            blocked_solve(s.Wf, N + 1, ys, acc);
-            for (int m = tid; m <= N; m += bd) {
-                const double y = ys[m];
-                const double ly = log(y);
-                if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
-                if (!(fabs(ly) < kRefreshLogY)) stale = 1;
-                s.yf[m] = y;
-                s.V[m] = s.Vh[m] - ly / beta;
-            }
-        }
-        bad = __syncthreads_or(bad);
-        if (bad) {
-            exact_forward(s, ys, red);
-            for (int m = tid; m <= N; m += bd) s.V[m] = ys[m];
-        }
-        int nonfinite = 0;
-        __syncthreads();
-        for (int m = tid; m <= N; m += bd)
-            if (!isfinite(s.V[m])) nonfinite = 1;
-        nonfinite = __syncthreads_or(nonfinite);
-        stale = __syncthreads_or(stale);
-        if (tid == 0) {
-            s.xflags[0] = bad;
-            s.xflags[4] = stale | nonfinite;
-            if (nonfinite) atomicOr(s.err, ERRB_NONFINITE_VB);
-        }
-    } else {
-        if (!force_exact) {
-            // nodes r = 0..N-1 <-> levels l = N..1
-            blocked_solve(s.Wb, N, ys, acc);
-            for (int l = tid + 1; l < N; l += bd) {
-                const double y = ys[N - l];
-                const double ly = log(y);
-                if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
-                if (!(fabs(ly) < kRefreshLogY)) stale = 1;
-                s.yb[l] = y;
-                s.Vb[l] = s.Vbh[l] - ly / beta;
-            }
-        }
-        if (tid == 0) {
-            s.Vb[N] = 0.0;
-            s.yb[N] = 1.0;
-        }
-        bad = __syncthreads_or(bad);
-        if (bad) {
-            exact_backward(s, ys, red);
-            for (int l = tid + 1; l <= N; l += bd) s.Vb[l] = ys[l];
-        }
-        int nonfinite = 0;
-        __syncthreads();
-        for (int l = tid + 1; l <= N; l += bd)
-            if (!isfinite(s.Vb[l])) nonfinite = 1;
-        nonfinite = __syncthreads_or(nonfinite);
-        stale = __syncthreads_or(stale);
-        if (tid == 0) {
-            s.xflags[1] = bad;
-            s.xflags[5] = stale | nonfinite;
-            if (nonfinite) atomicOr(s.err, ERRB_NONFINITE_VB);
-        }
-    }
-    // The block that finishes second computes the per-row factors, which need
-    // both V and V_backwards (threadFenceReduction pattern; no waiting), and
-    // keeps V, V_backwards as the estimates of the next evaluation.
+    solve_direction(s, blockIdx.x, force_exact, ys);
+    // The block that finishes second runs solve_finish (threadFenceReduction
+    // pattern; no waiting).
     __threadfence();
     __syncthreads();
-    if (tid == 0) last_block = (atomicAdd(&s.xflags[2], 1) == 1);
+    if (threadIdx.x == 0) last_block = (atomicAdd(&s.xflags[2], 1) == 1);
     __syncthreads();
     if (!last_block) return;
     __threadfence();
-    volatile double* V = s.V;
-    volatile double* Vb = s.Vb;
-    const double VN = V[N];
-    for (int l = tid; l < N; l += bd) {
-        const double vbl = Vb[l + 1];
-        s.rowR[l] = exp(-beta * (s.Vh[l + 1] + vbl - VN));
-        s.rowC[l] = exp(-beta * (V[l + 1] + vbl - VN));
-    }
-    __syncthreads();
-    const int need = ((volatile int*)s.xflags)[4] | ((volatile int*)s.xflags)[5];
-    for (int m = tid; m <= N; m += bd) {
-        s.Vh[m] = V[m];
-        s.Vbh[m] = m >= 1 ? Vb[m] : 0.0;
-    }
-    if (tid == 0) {
-        s.xflags[2] = 0;
-        s.xflags[3] = need;
-        s.Vb[0] = VN;  // V_backwards[0] = V[N] (:127)
-        s.scal[0] = VN;
-    }
+    solve_finish(s);
 }
 
-// Exterior spring forces (:159-215).  Warps [0, N) handle bead P (row l of
-// the connection-probability matrix), warps [N, 2N) bead 1 (column l).
-// Probabilities: close-cycle P[l][u] = Wf[l][u] y_u R_l (u <= l), direct
-// link P[l][l+1] = 1 - C_l; with the exact fallback they are evaluated
-// from their defining exponentials.  When `accumulate`, the spring force is
-// added to f (which holds the physical forces; simulation.cpp:363-373).
+// Exterior spring forces: one warp per row (bead P) or column (bead 1).
 template <int D>
 __global__ void k_exch_forces(Sys s, int accumulate) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int N = s.N;
-    if (w >= 2 * N) return;
-    const double beta = s.beta_ex;
-    const double VN = s.V[N];
-    const bool exact = s.xflags[0] != 0;
-    const int first = 0, last = s.P - 1;
-    double sum[D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) sum[a] = 0.0;
-    int bead, nb, l;
-    if (w < N) {  // last bead, particle l: sum over n <= l+1
-        l = w;
-        bead = last;
-        nb = (s.P - 2 + s.P) % s.P;
-        const size_t r = tri(l);
-        const double Rl = s.rowR[l];
-        const double vbl = s.Vb[l + 1];
-        const int nmax = min(l + 1, N - 1);
-        double xl[D];
-#pragma unroll
-        for (int a = 0; a < D; ++a) xl[a] = s.x[idx<D>(s, last, a, l)];
-        for (int n = lane; n <= nmax; n += 32) {
-            double pr;
-            if (n <= l) {
-                pr = exact ? exp(-beta * (s.V[n] + s.E[r + n] + vbl - VN)) / (l + 1) : s.Wf[r + n] * s.yf[n] * Rl;
-            } else {
-                pr = 1.0 - s.rowC[l];
-            }
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-                double d = s.x[idx<D>(s, first, a, n)] - xl[a];
-                if (s.pbc) d = min_image(d, s.L, s.invL);
-                sum[a] += pr * d;
-            }
-        }
-    } else {  // first bead, particle l: sum over q >= l-1
-        l = w - N;
-        bead = first;
-        nb = 1 % s.P;
-        const double yl = s.yf[l];
-        const double vl = s.V[l];
-        double xl[D];
-#pragma unroll
-        for (int a = 0; a < D; ++a) xl[a] = s.x[idx<D>(s, first, a, l)];
-        for (int q = max(0, l - 1) + lane; q < N; q += 32) {
-            double pr;
-            if (q >= l) {
-                pr = exact ? exp(-beta * (vl + s.E[tri(q) + l] + s.Vb[q + 1] - VN)) / (q + 1)
-                           : s.Wf[tri(q) + l] * yl * s.rowR[q];
-            } else {
-                pr = 1.0 - s.rowC[q];
-            }
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-                double d = s.x[idx<D>(s, last, a, q)] - xl[a];
-                if (s.pbc) d = min_image(d, s.L, s.invL);
-                sum[a] += pr * d;
-            }
-        }
-    }
-#pragma unroll
-    for (int a = 0; a < D; ++a) sum[a] = warp_sum(sum[a]);
-    if (lane == 0) {
-        const int side = (bead == first) ? 0 : 1;
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-            double d = s.x[idx<D>(s, nb, a, l)] - s.x[idx<D>(s, bead, a, l)];
-            if (s.pbc) d = min_image(d, s.L, s.invL);
-            const double fs = (sum[a] + d) * s.kappa;
-            s.fx[((size_t)side * D + a) * s.ld + l] = fs;
-            if (accumulate) {
-                const size_t o = idx<D>(s, bead, a, l);
-                s.f[o] = fs + s.f[o];
-            }
-        }
-    }
+    if (w >= 2 * s.N) return;
+    exch_force_row<D>(s, w, lane, accumulate);
 }
 
-// primEstimator (:250-279), getDistinctProbability (:222-229) and
-// getLongestProbability (:238-240); one block, evaluated on request.
 __global__ void k_exch_estimators(Sys s, int nbeads) {
     extern __shared__ double sh[];
-    double* G = sh;             // N+1
-    double* red = sh + s.N + 1; // 32
-    const int N = s.N;
-    const double beta = s.beta_ex;
-    const int tid = threadIdx.x, bd = blockDim.x;
-    if (tid == 0) G[0] = 0.0;
-    __syncthreads();
-    for (int m = 1; m <= N; ++m) {
-        const double* row = s.E + tri(m - 1);
-        double lmin = 1.79769313486231570815e308;
-        for (int u = tid; u < m; u += bd) lmin = fmin(lmin, row[u] + s.V[u]);
-        const double shift = block_min(lmin, red);
-        double ls = 0.0;
-        for (int u = tid; u < m; u += bd) ls += (G[u] - row[u]) * exp(-beta * (row[u] + s.V[u] - shift));
-        const double tot = block_sum(ls, red);
-        if (tid == 0) G[m] = tot / (m * exp(-beta * (s.V[m] - shift)));
-        __syncthreads();
-    }
-    double diag = 0.0;
-    for (int m = tid; m < N; m += bd) diag += s.E[tri(m) + m];
-    diag = block_sum(diag, red);
-    if (tid == 0) {
-        const double VN = s.V[N];
-        s.scal[1] = G[N] / nbeads;
-        s.scal[2] = exp(-beta * (diag - VN) - lgamma((double)(N + 1)));
-        s.scal[3] = exp(-beta * (s.E[tri(N - 1)] - VN));
-    }
+    estimators_block(s, nbeads, sh);
 }
 
 void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {

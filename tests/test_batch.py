@@ -1,0 +1,228 @@
+"""Batched replicas (pimdb_batch_*): many independent systems with their own
+N, P, temperature and potentials advanced by one launch per step.
+
+GPU parity: every replica of an FP64 batch matches the oracle run on that
+replica alone (forces and exchange scalars within 1e-10, trajectories within
+1e-9 relative per bead), and the one-system path within 1e-12.  Mixed
+batches: FP32 pair forces with FP64 accumulation within 1e-6 norm-relative
+force error of the FP64 oracle.  CPU: configuration checks that need no GPU.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.gpu_cases import MEV, case, momenta, pk, rel_per_bead, ring
+
+REPLICAS_3D = [
+    # case kwargs: uneven N, P, temperature and potentials
+    dict(natoms=16, nbeads=32, ext="harmonic", ext_p=(3.0 * MEV, 0, 0)),
+    dict(natoms=7, nbeads=5, T_K=2.5, ext="harmonic", ext_p=(3.0 * MEV, 0, 0), inter="harmonic",
+         int_p=(1.0 * MEV, 0, 0)),
+    dict(natoms=40, nbeads=8, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=12.0, inter="aziz", cutoff_ang=6.0),
+    dict(natoms=33, nbeads=3, bosonic=False, ext="double_well", ext_p=(1.32684e-7 * MEV, 3.0 * 1.8897261, 0),
+         inter="harmonic", int_p=(1.0 * MEV, 0, 0)),
+    dict(natoms=1, nbeads=4, ext="harmonic", ext_p=(3.0 * MEV, 0, 0)),
+    dict(natoms=9, nbeads=1, T_K=0.7, inter="harmonic", int_p=(1.0 * MEV, 0, 0), ext="cosine",
+         ext_p=(1.0 * MEV, 0.3, 0)),
+    dict(natoms=70, nbeads=16, T_K=3.0, ext="harmonic", ext_p=(3.0 * MEV, 0, 0), inter="harmonic",
+         int_p=(1.0 * MEV, 0, 0), thermostat="none", fixcom=False),
+    dict(natoms=6, nbeads=2, fixcom=False, ext="harmonic", ext_p=(3.0 * MEV, 0, 0)),
+]
+
+REPLICAS_2D = [
+    dict(ndim=2, natoms=24, nbeads=5, T_K=2.0, inter="dipole", int_p=(2.4799673e-4, 0, 0), ext="harmonic",
+         ext_p=(1.0 * MEV, 0, 0), box_ang=40.0),
+    dict(ndim=2, natoms=11, nbeads=8, T_K=1.0, ext="harmonic", ext_p=(1.0 * MEV, 0, 0)),
+]
+
+
+def build(replicas, precision="fp64"):
+    systems, cfgs, xs, ps = [], [], [], []
+    for r, kw in enumerate(replicas):
+        s, cfg = case(precision=precision, **kw)
+        cfg.seed = 1000 + 17 * r
+        cfg.replica = r
+        systems.append(s)
+        cfgs.append(cfg)
+        xs.append(ring(s, seed=50 + r, spread_ang=0.2))
+        ps.append(momenta(s, 50 + r))
+    return systems, cfgs, xs, ps
+
+
+def norm_rel(got, want):
+    return float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
+
+
+# ------------------------------------------------------------------------ CPU
+def test_batch_rejects_mixed_dimensions():
+    _, c3 = case(natoms=4, nbeads=2)
+    _, c2 = case(ndim=2, natoms=4, nbeads=2)
+    with pytest.raises(pk.ConfigError, match="same ndim"):
+        pk.Batch([c3, c2])
+
+
+def test_batch_rejects_normal_mode_propagator():
+    _, c = case(natoms=4, nbeads=4, bosonic=False, propagator="normal_modes")
+    with pytest.raises(pk.ConfigError, match="cartesian propagator"):
+        pk.Batch([c])
+
+
+def test_batch_rejects_mixed_precisions():
+    _, a = case(natoms=4, nbeads=2)
+    _, b = case(natoms=4, nbeads=2, precision="mixed")
+    with pytest.raises(pk.ConfigError, match="same precision"):
+        pk.Batch([a, b])
+
+
+# ------------------------------------------------------------------------ GPU
+@pytest.mark.gpu
+@pytest.mark.parametrize("replicas", [REPLICAS_3D, REPLICAS_2D], ids=["3d", "2d"])
+def test_batch_forces_match_oracle(replicas):
+    systems, cfgs, xs, ps = build(replicas)
+    with pk.Batch(cfgs) as b:
+        b.set_states(xs, ps)
+        b.compute_forces()
+        _, _, fs = b.get_states()
+    for r, s in enumerate(systems):
+        want = O.update_forces(s, xs[r])["f"]
+        assert rel_per_bead(fs[r], want) < 1e-10, r
+
+
+@pytest.mark.gpu
+def test_batch_exchange_scalars_match_oracle():
+    systems, cfgs, xs, ps = build(REPLICAS_3D)
+    with pk.Batch(cfgs) as b:
+        b.set_states(xs, ps)
+        sc = b.exchange()
+    for r, s in enumerate(systems):
+        if not (s.bosonic and s.nbeads > 1):
+            assert not sc[r].any()
+            continue
+        ex = O.exchange(s, xs[r])
+        want = np.array([ex["VB"], ex["prim"], ex["p_distinct"], ex["p_longest"]])
+        assert np.allclose(sc[r], want, rtol=1e-10, atol=0), (r, sc[r], want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("replicas", [REPLICAS_3D, REPLICAS_2D], ids=["3d", "2d"])
+def test_batch_trajectories_match_oracle(replicas):
+    systems, cfgs, xs, ps = build(replicas)
+    trs = [O.Trajectory(s, xs[r], ps[r]) for r, s in enumerate(systems)]
+    with pk.Batch(cfgs) as b:
+        b.set_states(xs, ps)
+        b.set_step(0)
+        for st in range(8):
+            for r, (s, c) in enumerate(zip(systems, cfgs)):
+                xi = O.philox_noise_device(c.seed, c.replica, st, s.nbeads, s.natoms, s.ndim)
+                assert trs[r].step(xi) == 0
+            b.step(1)
+            gx, gp, gf = b.get_states()
+            for r, tr in enumerate(trs):
+                for got, want, label in ((gx[r], tr.x, "x"), (gp[r], tr.p, "p"), (gf[r], tr.f, "f")):
+                    assert rel_per_bead(got, want) < 1e-9, (st, r, label, rel_per_bead(got, want))
+
+
+@pytest.mark.gpu
+def test_batch_replica_equals_one_system_path():
+    systems, cfgs, xs, ps = build(REPLICAS_3D[:3])
+    with pk.Batch(cfgs) as b:
+        b.set_states(xs, ps)
+        b.set_step(0)
+        b.step(6)
+        bx, bp, bf = b.get_states()
+    for r, c in enumerate(cfgs):
+        with pk.System(c) as g:
+            g.set_state(xs[r], ps[r])
+            g.set_step(0)
+            g.step(6)
+            x, p, f = g.get_state()
+        for u, v in ((bx[r], x), (bp[r], p), (bf[r], f)):
+            assert rel_per_bead(u, v) < 1e-12, r
+
+
+@pytest.mark.gpu
+def test_batch_graph_replay_equals_plain_launches():
+    _, cfgs, xs, ps = build(REPLICAS_3D)
+    out = []
+    for graph in (1, 0):
+        with pk.Batch(cfgs) as b:
+            b.set_option("graph", graph)
+            b.set_states(xs, ps)
+            b.step(5)
+            b.step(5)  # the second call replays the cached graph
+            assert b.get_step() == 10
+            out.append(b.get_states(flat=True))
+    for u, v in zip(*out):
+        assert np.array_equal(u, v)
+
+
+@pytest.mark.gpu
+def test_batch_deterministic_and_block_shape_independent():
+    _, cfgs, xs, ps = build(REPLICAS_3D)
+    out = []
+    for threads, ctas in ((256, 2), (256, 2), (128, 4), (512, 1)):
+        with pk.Batch(cfgs) as b:
+            b.set_option("threads", threads)
+            b.set_option("ctas_per_sm", ctas)
+            b.set_states(xs, ps)
+            b.step(4)
+            out.append(b.get_states(flat=True))
+    for u, v in zip(out[0], out[1]):
+        assert np.array_equal(u, v)
+    for other in out[2:]:
+        for u, v in zip(out[0], other):
+            assert np.abs(u - v).max() <= 1e-12 * np.abs(v).max()
+
+
+@pytest.mark.gpu
+def test_batch_autotune_keeps_the_state():
+    _, cfgs, xs, ps = build(REPLICAS_3D)
+    with pk.Batch(cfgs) as a, pk.Batch(cfgs) as b:
+        for g in (a, b):
+            g.set_states(xs, ps)
+            g.set_step(3)
+        threads, ctas = a.autotune(steps=2)
+        assert threads in (128, 256, 512) and ctas >= 1
+        assert a.get_step() == 3
+        a.step(3)
+        b.step(3)
+        for u, v in zip(a.get_states(flat=True), b.get_states(flat=True)):
+            assert np.abs(u - v).max() <= 1e-12 * np.abs(v).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("replicas", [REPLICAS_3D, REPLICAS_2D], ids=["3d", "2d"])
+def test_batch_mixed_force_error(replicas):
+    systems, cfgs, xs, ps = build(replicas, precision="mixed")
+    with pk.Batch(cfgs) as b:
+        b.set_states(xs, ps)
+        b.compute_forces()
+        _, _, fs = b.get_states()
+    for r, s in enumerate(systems):
+        want = O.update_forces(s, xs[r])["f"]
+        assert norm_rel(fs[r], want) <= 1e-6, (r, norm_rel(fs[r], want))
+
+
+@pytest.mark.gpu
+def test_batch_mixed_trajectory_tracks_fp64():
+    _, c64, xs, ps = build(REPLICAS_3D)
+    _, c32, _, _ = build(REPLICAS_3D, precision="mixed")
+    out = []
+    for cfgs in (c64, c32):
+        with pk.Batch(cfgs) as b:
+            b.set_states(xs, ps)
+            b.step(5)
+            out.append(b.get_states()[0])
+    for r in range(len(c64)):
+        assert norm_rel(out[1][r], out[0][r]) < 1e-6, r
+
+
+@pytest.mark.gpu
+def test_batch_nonfinite_exchange_names_the_replica():
+    systems, cfgs, xs, ps = build(REPLICAS_3D[:3])
+    xs[2] = xs[2].copy()
+    xs[2][0, 0, 0] = np.nan
+    with pk.Batch(cfgs) as b:
+        b.set_states(xs, ps)
+        with pytest.raises(pk.ExchangeOverflowError, match="replica 2"):
+            b.compute_forces()
