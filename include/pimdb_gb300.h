@@ -159,6 +159,28 @@ int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first, double* f_
  * V (N+1), V_backwards (N+1).  Any may be NULL. */
 int pimdb_exchange_arrays(pimdb_handle* h, double* E_kn, double* V, double* V_backwards);
 
+/* The forward function of pimdb_compute_forces: the potential energy U of
+ * the ring polymer at the current coordinates, whose negative gradient the
+ * force kernels return (the adjoint).  Terms, from the potentials' V()
+ * (src/potentials/{harmonic,aziz,dipole,double_well,cosine}.cpp) and
+ * classicalSpringEnergy (src/simulation.cpp:464-486):
+ *   terms[0]  external V summed over beads and particles
+ *   terms[1]  pair V summed over beads, each pair once (same cutoff and
+ *             minimum image as the forces)
+ *   terms[2]  ring springs outside the exchange: all P links when
+ *             distinguishable, links b -> b+1 (b < P-1) when bosonic
+ *   terms[3]  V_B = effectivePotential() when bosonic, else 0
+ * U = terms[0] + terms[1] + terms[2] + terms[3].  (The reference's double
+ * well gradV uses |x|^2 of all axes while its V sums per axis, so for ndim > 1
+ * its force is not -dU/dx; everything else is.) */
+int pimdb_potential_energy(pimdb_handle* h, double* terms);
+/* Energy of every term of U that involves particle i of bead b, for n items
+ * items[2k] = b, items[2k+1] = i: external V, pair V with every other
+ * particle of bead b, and the adjacent springs outside the exchange.  Its
+ * derivative with respect to x_bi, plus that of V_B on bosonic beads 1 and
+ * P, is -f_bi; finite differences of it stay accurate at any N. */
+int pimdb_local_energy(pimdb_handle* h, int n, const int* items, double* out);
+
 /* Instrumentation (no counterpart in the reference, which only reports the
  * wall time per step, src/simulation.cpp:517-572).  Kernel classes: */
 enum pimdb_kernel_class {

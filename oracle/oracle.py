@@ -73,6 +73,8 @@ def lib():
         L.orc_system_init.argtypes = [S, C.c_double, C.c_double]
         L.orc_exchange.argtypes = [S, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_exchange.restype = C.c_int
+        L.orc_potential_energy.argtypes = [S, dp, dp]
+        L.orc_potential_energy.restype = C.c_int
         L.orc_update_forces.argtypes = [S, dp, dp, dp, dp, C.c_int]
         L.orc_update_forces.restype = C.c_int
         L.orc_md_step.argtypes = [S, C.POINTER(State), dp, C.c_int]
@@ -134,6 +136,14 @@ def exchange(s: System, x: np.ndarray):
     st = lib().orc_exchange(C.byref(s), _dp(x), _dp(f1), _dp(fP), _dp(sc), _dp(E), _dp(V), _dp(Vb), _dp(prob))
     return dict(status=st, f1=f1, fP=fP, VB=sc[0], prim=sc[1], p_distinct=sc[2], p_longest=sc[3], E=E, V=V, Vb=Vb,
                 prob=prob)
+
+
+def potential_energy(s: System, x: np.ndarray) -> np.ndarray:
+    """[external, pair, non-exchange springs, V_B] (orc_potential_energy)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    t = np.zeros(4)
+    lib().orc_potential_energy(C.byref(s), _dp(x), _dp(t))
+    return t
 
 
 def update_forces(s: System, x: np.ndarray, nthreads: int = 1):

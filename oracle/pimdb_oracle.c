@@ -446,6 +446,54 @@ void orc_physical_forces(const orc_system* s, const double* x, double* f) {
     }
 }
 
+/* Potential energy of the ring polymer, the function whose negative gradient
+ * orc_update_forces returns: terms[0] external V over beads (the potentials'
+ * V(), src/potentials/[*].cpp), terms[1] pair V over beads (each pair once,
+ * cutoff and minimum image as simulation.cpp:428-455), terms[2] the springs
+ * outside the exchange (classicalSpringEnergy, simulation.cpp:464-486: every
+ * link when distinguishable, the interior links when bosonic), terms[3]
+ * V_B (effectivePotential, quadratic_bosonic_exchange.cpp:130-132). */
+int orc_potential_energy(const orc_system* s, const double* x_all, double* terms) {
+    const int N = s->natoms, D = s->ndim, P = s->nbeads;
+    const long bead = (long)N * D;
+    const int bosonic = s->bosonic && P > 1;
+    terms[0] = terms[1] = terms[2] = terms[3] = 0.0;
+    for (int b = 0; b < P; ++b) {
+        const double* x = x_all + (long)b * bead;
+        terms[0] += orc_ext_value(s, x, N);
+        if (s->cutoff != 0.0) {
+            double r[3];
+            for (int i = 0; i < N; ++i)
+                for (int j = i + 1; j < N; ++j) {
+                    for (int a = 0; a < D; ++a) {
+                        double d = x[(long)i * D + a] - x[(long)j * D + a];
+                        if (s->pbc) d = orc_min_image(d, s->size);
+                        r[a] = d;
+                    }
+                    const double dist = vnorm(r, D);
+                    if (dist < s->cutoff || s->cutoff < 0.0) terms[1] += orc_pair_value(s, r);
+                }
+        }
+        if (P > 1 && (!bosonic || b > 0)) {
+            const double* xp = x_all + (long)((b - 1 + P) % P) * bead;
+            double e = 0.0;
+            for (long k = 0; k < bead; ++k) {
+                double diff = xp[k] - x[k];
+                if (s->pbc) diff = orc_min_image(diff, s->size);
+                e += diff * diff;
+            }
+            terms[2] += e * (0.5 * s->spring_constant);
+        }
+    }
+    if (bosonic) {
+        double sc[4];
+        const int st = orc_exchange(s, x_all, NULL, NULL, sc, NULL, NULL, NULL, NULL);
+        terms[3] = sc[0];
+        return st;
+    }
+    return 0;
+}
+
 /* ---- a tiny parallel-for over POSIX threads ---- */
 typedef void (*orc_body)(void* ctx, int i);
 typedef struct {

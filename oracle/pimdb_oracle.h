@@ -94,6 +94,8 @@ void orc_spring_forces_interior(const orc_system* s, const double* x_prev, const
                                 double* f);
 void orc_physical_forces(const orc_system* s, const double* x, double* f);
 /* spring_out / phys_out may be NULL.  Returns the exchange status. */
+/* External, pair, non-exchange spring energies and V_B (terms[4]). */
+int orc_potential_energy(const orc_system* s, const double* x_all, double* terms);
 int orc_update_forces(const orc_system* s, const double* x_all, double* f_all, double* spring_out, double* phys_out,
                       int nthreads);
 

@@ -29,7 +29,7 @@ EXPORTS = [
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
     "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
     "pimdb_measure_fp64_peak", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
-    "pimdb_propagate", "pimdb_batch_create", "pimdb_batch_destroy", "pimdb_batch_size", "pimdb_batch_set_states",
+    "pimdb_propagate", "pimdb_potential_energy", "pimdb_local_energy", "pimdb_batch_create", "pimdb_batch_destroy", "pimdb_batch_size", "pimdb_batch_set_states",
     "pimdb_batch_get_states", "pimdb_batch_set_step", "pimdb_batch_get_step", "pimdb_batch_compute_forces",
     "pimdb_batch_step", "pimdb_batch_step_async", "pimdb_batch_synchronize", "pimdb_batch_exchange",
     "pimdb_batch_set_option", "pimdb_batch_get_launch", "pimdb_batch_autotune", "pimdb_batch_last_error",
@@ -99,6 +99,8 @@ def lib():
             "pimdb_thermostat_step": ([vp, C.c_int], C.c_int),
             "pimdb_zero_momentum": ([vp], C.c_int),
             "pimdb_propagate": ([vp], C.c_int),
+            "pimdb_potential_energy": ([vp, vp], C.c_int),
+            "pimdb_local_energy": ([vp, C.c_int, vp, vp], C.c_int),
             "pimdb_batch_create": ([cfgp, C.c_int, vp, C.POINTER(vp)], C.c_int),
             "pimdb_batch_destroy": ([vp], C.c_int),
             "pimdb_batch_size": ([vp, ip, C.POINTER(C.c_longlong)], C.c_int),
@@ -302,6 +304,19 @@ class System:
         _check(lib().pimdb_profile(self._h, enable, _ptr(ms), _ptr(n), C.byref(tot)), self._h)
         return dict(ms=dict(zip(KERNEL_CLASSES, ms.tolist())), counts=dict(zip(KERNEL_CLASSES, n.tolist())),
                     launches=tot.value)
+
+    def potential_energy(self):
+        """Terms of U: external, pair, non-exchange springs, V_B."""
+        t = np.zeros(4)
+        _check(lib().pimdb_potential_energy(self._h, _ptr(t)), self._h)
+        return t
+
+    def local_energy(self, items):
+        """Energy of every term involving (bead, particle) for each item."""
+        it = np.ascontiguousarray(np.asarray(items, dtype=np.int32).reshape(-1, 2))
+        out = np.zeros(len(it))
+        _check(lib().pimdb_local_energy(self._h, len(it), _ptr(it), _ptr(out)), self._h)
+        return out
 
     def exchange_arrays(self):
         N = self.cfg.natoms

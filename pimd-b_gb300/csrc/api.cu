@@ -665,6 +665,58 @@ extern "C" int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first,
     return PIMDB_OK;
 }
 
+extern "C" int pimdb_potential_energy(pimdb_handle* h, double* terms) {
+    if (!h || !terms) return fail(h, PIMDB_ERR_ARG, "NULL argument");
+    const Sys& s = h->s;
+    const int nb = energy_blocks(s);
+    const size_t n = (size_t)s.P * nb * 3;
+    double* part = nullptr;
+    CUDA_TRY(h, cudaMalloc((void**)&part, n * sizeof(double)));
+    launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_energy_terms(s, h->D, part, h->stream); });
+    if (s.bosonic) {
+        launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
+        const int ex = h->opt_exact_exchange;
+        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 3);
+    }
+    std::vector<double> hp(n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), part, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(part);
+    if (e != cudaSuccess) return fail(h, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    const int st = check_err_word(h);
+    if (st != PIMDB_OK) return st;
+    for (int k = 0; k < 3; ++k) {
+        double t = 0.0;
+        for (size_t q = 0; q < (size_t)s.P * nb; ++q) t += hp[q * 3 + k];
+        terms[k] = t;
+    }
+    terms[3] = 0.0;
+    if (s.bosonic) CUDA_TRY(h, cudaMemcpy(&terms[3], s.scal, sizeof(double), cudaMemcpyDeviceToHost));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_local_energy(pimdb_handle* h, int n, const int* items, double* out) {
+    if (!h || (n > 0 && (!items || !out)) || n < 0) return fail(h, PIMDB_ERR_ARG, "NULL argument or n < 0");
+    if (n == 0) return PIMDB_OK;
+    int* d_items = nullptr;
+    double* d_out = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d_items, sizeof(int) * 2 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_out, sizeof(double) * (size_t)n);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_items, items, sizeof(int) * 2 * (size_t)n, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_local_energy(h->s, h->D, n, d_items, d_out, h->stream); });
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d_items);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return fail(h, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    return check_err_word(h);
+}
+
 extern "C" int pimdb_exchange_arrays(pimdb_handle* h, double* E_kn, double* V, double* Vb) {
     if (!h) return PIMDB_ERR_ARG;
     const Sys& s = h->s;

@@ -483,4 +483,148 @@ void launch_bead_forces(const Sys& s, int D, int mixed, int write_phys, cudaStre
     else launch_bead_forces<3>(s, mixed, write_phys, st);
 }
 
+// ---------------------------------------------------------------------------
+// Potential energy, the function whose negative gradient the force kernels
+// evaluate: external + pair energies of every bead (each pair once, same
+// cutoff and minimum image as the forces) and the ring springs that do not
+// take part in the exchange (all P links when distinguishable; links
+// b -> b+1, b < P-1, when bosonic, whose exterior links live in V_B).
+// Spring energy as classicalSpringEnergy (simulation.cpp:464-486).
+constexpr int kEnergyThreads = 128;
+
+template <int D>
+__device__ __forceinline__ double link_energy(const Sys& s, int b, int bn, int i) {
+    double e = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double d = s.x[idx<D>(s, bn, a, i)] - s.x[idx<D>(s, b, a, i)];
+        if (s.pbc) d = min_image(d, s.L, s.invL);
+        e += d * d;
+    }
+    return 0.5 * s.kappa * e;
+}
+
+template <int D>
+__device__ __forceinline__ double pair_energy_ij(const Sys& s, const double* xi, const double* xj) {
+    double r2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double d = xi[a] - xj[a];
+        if (s.pbc) d = min_image(d, s.L, s.invL);
+        r2 += d * d;
+    }
+    if (s.cutoff > 0.0 && !(sqrt(r2) < s.cutoff)) return 0.0;
+    return pair_value(s.int_kind, r2, s.int_a);
+}
+
+// part[(b * gridDim.x + block) * 3 + {0 external, 1 pair, 2 spring}]
+template <int D>
+__global__ void __launch_bounds__(kEnergyThreads) k_energy_terms(Sys s, double* __restrict__ part) {
+    __shared__ double xs[D][kEnergyThreads];
+    __shared__ double red[3 * 32];
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * kEnergyThreads + threadIdx.x;
+    const bool active = i < s.N;
+    double xi[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xi[a] = active ? s.x[idx<D>(s, b, a, i)] : 0.0;
+    double e[3] = {0.0, 0.0, 0.0};
+    if (active) {
+        e[0] = ext_value<D>(s, xi);
+        if (s.P > 1 && (!s.bosonic || b < s.P - 1)) e[2] = link_energy<D>(s, b, (b + 1) % s.P, i);
+    }
+    const bool pairs = s.int_kind != POT_FREE && s.cutoff != 0.0;
+    if (pairs) {
+        for (int j0 = blockIdx.x * kEnergyThreads; j0 < s.N; j0 += kEnergyThreads) {
+            __syncthreads();
+            const int jl = j0 + threadIdx.x;
+#pragma unroll
+            for (int a = 0; a < D; ++a) xs[a][threadIdx.x] = jl < s.N ? s.x[idx<D>(s, b, a, jl)] : 0.0;
+            __syncthreads();
+            if (!active) continue;
+            const int jn = min(kEnergyThreads, s.N - j0);
+            for (int jj = 0; jj < jn; ++jj) {
+                const int j = j0 + jj;
+                if (j <= i) continue;
+                double xj[D];
+#pragma unroll
+                for (int a = 0; a < D; ++a) xj[a] = xs[a][jj];
+                e[1] += pair_energy_ij<D>(s, xi, xj);
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double t = warp_sum(e[k]);
+        if (lane == 0) red[k * 32 + w] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int q = 0; q < nw; ++q) t += red[threadIdx.x * 32 + q];
+        part[((size_t)b * gridDim.x + blockIdx.x) * 3 + threadIdx.x] = t;
+    }
+}
+
+// Energy of every term that involves particle i of bead b (one warp per
+// item): its external energy, its pair energies with every other particle
+// of the bead, and its non-exchange springs.  The derivative of this sum
+// (plus V_B on bosonic beads 1 and P) with respect to x_bi is -f_bi.
+template <int D>
+__global__ void k_local_energy(Sys s, int n, const int* __restrict__ items, double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (w >= n) return;
+    const int b = items[2 * w], i = items[2 * w + 1];
+    if (b < 0 || b >= s.P || i < 0 || i >= s.N) {
+        if (lane == 0) {
+            atomicOr(s.err, ERRB_BOUNDS);
+            out[w] = 0.0;
+        }
+        return;
+    }
+    double xi[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xi[a] = s.x[idx<D>(s, b, a, i)];
+    double e = 0.0;
+    if (s.int_kind != POT_FREE && s.cutoff != 0.0) {
+        for (int j = lane; j < s.N; j += 32) {
+            if (j == i) continue;
+            double xj[D];
+#pragma unroll
+            for (int a = 0; a < D; ++a) xj[a] = s.x[idx<D>(s, b, a, j)];
+            e += pair_energy_ij<D>(s, xi, xj);
+        }
+    }
+    e = warp_sum(e);
+    if (lane == 0) {
+        e += ext_value<D>(s, xi);
+        if (s.P > 1) {
+            const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
+            if (!s.bosonic || b > 0) e += link_energy<D>(s, bp, b, i);
+            if (!s.bosonic || b < s.P - 1) e += link_energy<D>(s, b, bn, i);
+        }
+        out[w] = e;
+    }
+}
+
+int energy_blocks(const Sys& s) { return (s.N + kEnergyThreads - 1) / kEnergyThreads; }
+
+void launch_energy_terms(const Sys& s, int D, double* part, cudaStream_t st) {
+    dim3 grid(energy_blocks(s), s.P);
+    if (D == 1) k_energy_terms<1><<<grid, kEnergyThreads, 0, st>>>(s, part);
+    else if (D == 2) k_energy_terms<2><<<grid, kEnergyThreads, 0, st>>>(s, part);
+    else k_energy_terms<3><<<grid, kEnergyThreads, 0, st>>>(s, part);
+}
+
+void launch_local_energy(const Sys& s, int D, int n, const int* items, double* out, cudaStream_t st) {
+    const int warps = 4;
+    const int grid = (n + warps - 1) / warps;
+    if (grid == 0) return;
+    if (D == 1) k_local_energy<1><<<grid, 32 * warps, 0, st>>>(s, n, items, out);
+    else if (D == 2) k_local_energy<2><<<grid, 32 * warps, 0, st>>>(s, n, items, out);
+    else k_local_energy<3><<<grid, 32 * warps, 0, st>>>(s, n, items, out);
+}
+
 }  // namespace pimdb

@@ -113,4 +113,50 @@ __device__ __forceinline__ void ext_force(const Sys& s, const double* xi, double
     }
 }
 
+// Pair potential V(r) of one separation (`r2` = |r|^2), the reference's
+// V() for one distance vector: harmonic.cpp:7-19 (1/2 k r^2), dipole.cpp:5-20
+// (D / r^3), aziz.cpp:18-54 with F of aziz.h:25-27.
+__device__ inline double pair_value(int kind, double r2, double param) {
+    if (kind == POT_HARMONIC) return 0.5 * param * r2;
+    const double r = sqrt(r2);
+    if (kind == POT_DIPOLE) return param / (r * r * r);
+    if (kind != POT_AZIZ) return 0.0;
+    const double rs = r / Aziz::rm;
+    const double urep = Aziz::A * exp(-Aziz::alpha * rs);
+    if (rs > 1.0E-7 && rs < 0.01) return Aziz::eps * urep;
+    const double ix2 = 1.0 / (rs * rs);
+    const double ix6 = ix2 * ix2 * ix2;
+    const double ix8 = ix6 * ix2;
+    const double ix10 = ix8 * ix2;
+    const double t = Aziz::D / rs - 1.0;
+    const double F = rs < Aziz::D ? exp(-t * t) : 1.0;
+    const double uatt = -(Aziz::C6 * ix6 + Aziz::C8 * ix8 + Aziz::C10 * ix10) * F;
+    return Aziz::eps * (urep + uatt);
+}
+
+// External potential of one particle: harmonic.cpp:7-19 (1/2 k |x|^2),
+// double_well.cpp:6-20 (m s sum_a (x_a^2 - loc^2)^2), cosine.cpp:9-21
+// (A sum_a cos(k x_a + phase)).  Sys holds ext_a = m w^2 | 4 m s | -A k,
+// ext_b = - | loc^2 | k, ext_c = - | m s | phase.
+template <int D>
+__device__ __forceinline__ double ext_value(const Sys& s, const double* xi) {
+    double v = 0.0;
+    if (s.ext_kind == POT_HARMONIC) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) v += xi[a] * xi[a];
+        return 0.5 * s.ext_a * v;
+    }
+    if (s.ext_kind == POT_DOUBLE_WELL) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) v += (xi[a] * xi[a] - s.ext_b) * (xi[a] * xi[a] - s.ext_b);
+        return s.ext_c * v;
+    }
+    if (s.ext_kind == POT_COSINE) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) v += cos(s.ext_b * xi[a] + s.ext_c);
+        return (-s.ext_a / s.ext_b) * v;
+    }
+    return 0.0;
+}
+
 }  // namespace pimdb

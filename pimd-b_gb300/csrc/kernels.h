@@ -26,6 +26,13 @@ void launch_bead_forces(const Sys& s, int D, int mixed, int write_phys, cudaStre
 size_t pair_partial_doubles(const Sys& s, int D);
 void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part, cudaStream_t st);
 
+// Potential energy: per-bead partial sums of the external, pair and
+// non-exchange spring energies, part[(b * energy_blocks + blk) * 3 + term];
+// and the local energy of listed (bead, particle) items ([n][2] ints).
+int energy_blocks(const Sys& s);
+void launch_energy_terms(const Sys& s, int D, double* part, cudaStream_t st);
+void launch_local_energy(const Sys& s, int D, int n, const int* items, double* out, cudaStream_t st);
+
 // exchange.cu: Feldman-Hirshberg exchange on beads 1 and P.
 void launch_exchange_energies(const Sys& s, int D, cudaStream_t st);
 // Returns the number of kernels launched (3, or 1 with `exact`: the
