@@ -216,7 +216,10 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
  *                    fit on the GPU at once);
  *   "fft_normal_modes" 0: in the fused kernel, transform with the P x P
  *                    matrices instead of FFTs (FFTs are used when P is a
- *                    power of two; default 1). */
+ *                    power of two; default 1);
+ *   "cell_lists"     1 / 0 / -1: pair forces from cell lists (periodic box
+ *                    with at least 4 cutoff-wide cells per edge) on / off /
+ *                    automatic (default: on from 512 particles). */
 int pimdb_set_option(pimdb_handle* h, const char* name, int value);
 
 /* Bosonic exchange without any allocation (no counterpart in the reference).

@@ -53,6 +53,11 @@ struct pimdb_handle {
     int opt_fft = 1;
     cudaError_t async_err = cudaSuccess;
     int opt_newton3 = 1;
+    // cell lists (periodic box with a short cutoff): cells per edge, work
+    // buffer, and the option (-1 automatic: on when nc >= 4 and N >= 512)
+    int cell_nc = 0;
+    void* d_cells = nullptr;
+    int opt_cells = -1;
     bool profile = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double prof_ms[PIMDB_NUM_KERNEL_CLASSES] = {};
@@ -253,6 +258,7 @@ static void free_handle(pimdb_handle* h) {
     if (h->d_cmpart) cudaFree(h->d_cmpart);
     if (h->d_bar) cudaFree(h->d_bar);
     if (h->d_tw) cudaFree(h->d_tw);
+    if (h->d_cells) cudaFree(h->d_cells);
     if (h->fork_ev) cudaEventDestroy(h->fork_ev);
     if (h->join_ev) cudaEventDestroy(h->join_ev);
     if (h->side) cudaStreamDestroy(h->side);
@@ -317,6 +323,8 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     // beyond 512 MiB the all-pairs kernel (no partials) is used instead.
     const size_t npart = pair_partial_doubles(s, h->D);
     if (e == cudaSuccess && npart * sizeof(double) <= (512ull << 20)) e = alloc(&h->d_part, npart);
+    h->cell_nc = cell_grid(s, h->D);
+    if (e == cudaSuccess && h->cell_nc > 0) e = cudaMalloc(&h->d_cells, cell_buffer_bytes(s, h->D, h->cell_nc));
     // xflags: [0],[1] exact fallback used (forward, backward); [2] completion
     // counter; [3] next evaluation needs a fresh FP32 estimate; [4],[5] the
     // forward / backward solve asked for one.
@@ -477,11 +485,15 @@ static void enqueue_forces(pimdb_handle* h) {
     if (s.bosonic) {
         launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, xs); });
         const int ex = h->opt_exact_exchange;
-        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, xs); }, ex ? 1 : 3);
+        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, xs); }, ex ? 1 : 6);
     }
     if (fork) cudaEventRecord(h->join_ev, h->side);
     const int mixed = h->cfg.precision == PIMDB_MIXED;
-    if (h->d_part && h->opt_newton3) {
+    const bool cells = h->d_cells && (h->opt_cells == 1 || (h->opt_cells < 0 && s.N >= 512));
+    if (cells) {
+        launch(h, PIMDB_K_BEAD_FORCES,
+               [&] { launch_pair_cells_and_finish(s, h->D, h->cell_nc, mixed, nm ? 1 : 0, h->d_cells, h->stream); }, 3);
+    } else if (h->d_part && h->opt_newton3) {
         const bool pairs = s.int_kind != PIMDB_POT_FREE && s.cutoff != 0.0;
         launch(
             h, PIMDB_K_BEAD_FORCES,
@@ -644,7 +656,7 @@ extern "C" int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first,
     if (!s.bosonic) return fail(h, PIMDB_ERR_CONFIG, "pimdb_exchange needs a bosonic configuration with nbeads > 1");
     launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
     const int ex = h->opt_exact_exchange;
-    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 3);
+    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 6);
     launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 0, h->stream); });
     launch(h, PIMDB_K_EXCH_ESTIMATORS, [&] { launch_exchange_estimators(s, h->stream); });
     CUDA_TRY(h, cudaGetLastError());
@@ -676,7 +688,7 @@ extern "C" int pimdb_potential_energy(pimdb_handle* h, double* terms) {
     if (s.bosonic) {
         launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
         const int ex = h->opt_exact_exchange;
-        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 3);
+        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 6);
     }
     std::vector<double> hp(n);
     cudaError_t e = cudaGetLastError();
@@ -795,7 +807,11 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
     else if (n == "fused_normal_modes") h->fused_nm = value && h->d_cmpart != nullptr;
     else if (n == "fft_normal_modes") h->opt_fft = value ? 1 : 0;
     else if (n == "newton3") h->opt_newton3 = value ? 1 : 0;
-    else return fail(h, PIMDB_ERR_ARG, "unknown option " + n);
+    else if (n == "cell_lists") {
+        if (value > 0 && !h->d_cells)
+            return fail(h, PIMDB_ERR_CONFIG, "cell lists need a periodic box with at least 4 cutoff-wide cells per edge");
+        h->opt_cells = value < 0 ? -1 : (value ? 1 : 0);
+    } else return fail(h, PIMDB_ERR_ARG, "unknown option " + n);
     return PIMDB_OK;
 }
 

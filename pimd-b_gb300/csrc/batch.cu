@@ -239,21 +239,31 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work) {
     const int N = s.N;
     for (int v = warp; v < N; v += nw) energy_row<D>(s, v, lane);
     __syncthreads();
-    const int fresh = ((volatile int*)s.xflags)[3];
+    int fresh = ((volatile int*)s.xflags)[3];
     __syncthreads();
-    if (fresh) {
-        estimate_direction(s, 0, reinterpret_cast<float*>(work));
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (fresh) {
+            estimate_direction(s, 0, reinterpret_cast<float*>(work));
+            __syncthreads();
+            estimate_direction(s, 1, reinterpret_cast<float*>(work));
+            __syncthreads();
+        }
+        for (int p = warp; p < N; p += nw)
+            for (int u = lane; u <= p; u += 32) exch_weight(s, p, u);
         __syncthreads();
-        estimate_direction(s, 1, reinterpret_cast<float*>(work));
+        // a reused estimate that fails is replaced by a fresh one (second
+        // attempt) rather than by the exact recursion
+        solve_direction(s, 0, 0, reinterpret_cast<double*>(work), fresh);
+        __syncthreads();
+        solve_direction(s, 1, 0, reinterpret_cast<double*>(work), fresh);
+        __syncthreads();
+        const int retry = ((volatile int*)s.xflags)[6];
+        __syncthreads();
+        if (!retry) break;
+        if (threadIdx.x == 0) s.xflags[6] = 0;
+        fresh = 1;
         __syncthreads();
     }
-    for (int p = warp; p < N; p += nw)
-        for (int u = lane; u <= p; u += 32) exch_weight(s, p, u);
-    __syncthreads();
-    solve_direction(s, 0, 0, reinterpret_cast<double*>(work));
-    __syncthreads();
-    solve_direction(s, 1, 0, reinterpret_cast<double*>(work));
-    __syncthreads();
     solve_finish(s);
     __syncthreads();
     for (int w = warp; w < 2 * N; w += nw) exch_force_row<D>(s, w, lane, 1);

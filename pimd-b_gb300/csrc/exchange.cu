@@ -46,28 +46,40 @@ __global__ void k_exch_energies(Sys s) {
     energy_row<D>(s, v, lane);
 }
 
-// Pass 1: block 0 forward, block 1 backward.  Skipped (early exit) when the
-// previous evaluation's exact potentials are still a good estimate
-// (xflags[3] == 0).
-__global__ void __launch_bounds__(kWaveThreads) k_exch_estimate(Sys s) {
-    if (((volatile int*)s.xflags)[3] == 0) return;
+// Pass 1: block 0 forward, block 1 backward.  Phase 0 skips (early exit)
+// when the previous evaluation's exact potentials are still a good estimate
+// (xflags[3] == 0) and records in xflags[7] that they were reused; phase 1
+// (the retry) runs only when the solve asked for it (xflags[6]).
+__global__ void __launch_bounds__(kWaveThreads) k_exch_estimate(Sys s, int phase) {
+    if (phase == 0) {
+        const int fresh = ((volatile int*)s.xflags)[3];
+        if (blockIdx.x == 0 && threadIdx.x == 0) s.xflags[7] = !fresh;
+        if (!fresh) return;
+    } else if (((volatile int*)s.xflags)[6] == 0) {
+        return;
+    }
     extern __shared__ float fsm[];  // 3 (N+1)
     estimate_direction(s, blockIdx.x, fsm);
 }
 
-// Pass 2: every FP64 exponential at once, one thread per packed entry.
-__global__ void k_exch_weights(Sys s) {
-    const int p = blockIdx.y;
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u > p) return;
-    exch_weight(s, p, u);
+// Pass 2: every FP64 exponential at once, one thread per packed entry
+// (grid-stride over rows; phase 1 runs only on a retry).
+__global__ void k_exch_weights(Sys s, int phase) {
+    if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    for (int p = blockIdx.y; p < s.N; p += gridDim.y)
+        for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= p; u += gridDim.x * blockDim.x) exch_weight(s, p, u);
 }
 
-// Pass 3: block 0 forward, block 1 backward.
-__global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_exact) {
+// Pass 3: block 0 forward, block 1 backward.  Phase 0 may not fall back to
+// the exact recursion when it reused the previous potentials (xflags[7]); a
+// failed solve then leaves xflags[6] set and the phase-1 kernels redo the
+// evaluation from a fresh estimate.
+__global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_exact, int phase) {
     extern __shared__ double ys[];  // y: N+1, acc: N+1, then 32 for reductions
     __shared__ int last_block;
-    solve_direction(s, blockIdx.x, force_exact, ys);
+    if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    const int allow_exact = force_exact || phase == 1 || !((volatile int*)s.xflags)[7];
+    solve_direction(s, blockIdx.x, force_exact, ys, allow_exact);
     // The block that finishes second runs solve_finish (threadFenceReduction
     // pattern; no waiting).
     __threadfence();
@@ -76,7 +88,12 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
     __syncthreads();
     if (!last_block) return;
     __threadfence();
+    if (phase == 0 && ((volatile int*)s.xflags)[6]) {
+        if (threadIdx.x == 0) s.xflags[2] = 0;  // retry pending: phase 1 finishes
+        return;
+    }
     solve_finish(s);
+    if (threadIdx.x == 0) s.xflags[6] = 0;
 }
 
 // Exterior spring forces: one warp per row (bead P) or column (bead 1).
@@ -102,18 +119,23 @@ void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
 }
 
 int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st) {
-    if (!exact) {
-        const size_t esmem = sizeof(float) * 3 * (size_t)(s.N + 1);
-        if (esmem + 1024 > 48 * 1024)
-            cudaFuncSetAttribute(k_exch_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
-        k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s);
-        dim3 wgrid((s.N + 255) / 256, s.N);
-        k_exch_weights<<<wgrid, 256, 0, st>>>(s);
-    }
+    const size_t esmem = sizeof(float) * 3 * (size_t)(s.N + 1);
     const size_t smem = sizeof(double) * (2 * (size_t)(s.N + 1) + 32);
+    if (esmem + 1024 > 48 * 1024)
+        cudaFuncSetAttribute(k_exch_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
     if (smem + 1024 > 48 * 1024) cudaFuncSetAttribute(k_exch_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, exact);
-    return exact ? 1 : 3;
+    if (exact) {
+        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 1, 0);
+        return 1;
+    }
+    const dim3 wgrid((s.N + 255) / 256, s.N < 65535 ? s.N : 65535);
+    const dim3 rgrid(1, s.N < 256 ? s.N : 256);  // the retry's weights: a small grid-stride launch
+    for (int phase = 0; phase < 2; ++phase) {
+        k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s, phase);
+        k_exch_weights<<<phase ? rgrid : wgrid, 256, 0, st>>>(s, phase);
+        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase);
+    }
+    return 6;
 }
 
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st) {

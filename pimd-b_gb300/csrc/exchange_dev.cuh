@@ -251,7 +251,11 @@ constexpr double kRefreshLogY = 30.0;
 constexpr double kExactLogY = 200.0;
 // Pass 3, one direction (0 forward, 1 backward) by the whole block: the y
 // solve and the exact V / V_backwards.  `ys` holds 2 (N+1) + 32 doubles.
-__device__ inline void solve_direction(const Sys& s, int dir, int force_exact, double* ys) {
+// When the solve is unusable (|log y| >= 200) and `allow_exact` is 0 (the
+// estimate was the previous evaluation's potentials, not a fresh FP32
+// recursion), no exact recursion is run: xflags[6] asks the caller to
+// retry with a fresh estimate instead.
+__device__ inline void solve_direction(const Sys& s, int dir, int force_exact, double* ys, int allow_exact = 1) {
     double* acc = ys + s.N + 1;
     double* red = ys + 2 * (s.N + 1);
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
@@ -270,6 +274,10 @@ __device__ inline void solve_direction(const Sys& s, int dir, int force_exact, d
             }
         }
         bad = __syncthreads_or(bad);
+        if (bad && !allow_exact) {
+            if (tid == 0) s.xflags[6] = 1;
+            return;
+        }
         if (bad) {
             exact_forward(s, ys, red);
             for (int m = tid; m <= N; m += bd) s.V[m] = ys[m];
@@ -303,6 +311,10 @@ __device__ inline void solve_direction(const Sys& s, int dir, int force_exact, d
             s.yb[N] = 1.0;
         }
         bad = __syncthreads_or(bad);
+        if (bad && !allow_exact) {
+            if (tid == 0) s.xflags[6] = 1;
+            return;
+        }
         if (bad) {
             exact_backward(s, ys, red);
             for (int l = tid + 1; l <= N; l += bd) s.Vb[l] = ys[l];

@@ -11,6 +11,9 @@
 // type of the pair gradient (double for the plain path, float for the mixed
 // path, which reconstructs separations from hi/lo float pairs and adds each
 // tile's float partial sum into a double accumulator).
+#include <algorithm>
+#include <cmath>
+
 #include "forces_dev.cuh"
 #include "kernels.h"
 
@@ -263,34 +266,46 @@ __global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ 
 // A warp-instruction on the FP64 pipe costs the same whether or not its lanes
 // are active, so evaluating the Aziz gradient only in the lanes whose pair is
 // inside the cutoff wastes the pipe on the others.  Each warp therefore
-//   1. screens its tile's pairs with FP32 distances and records, per i lane,
-//      the j's inside the cutoff (plus a small margin), and per j lane the
-//      (i, position) of those entries;
-//   2. lays the entries out i-major and evaluates them 32 at a time in FP64,
-//      every lane busy, storing each gradient in shared memory;
-//   3. sums the gradients per i and per j in list order (deterministic).
-// Same result as k_pair_tiles; the exact FP64 cutoff test is applied in step 2.
+//   1. screens its tile's pairs with FP32 distances (an FP32 copy of the j
+//      positions, converted once) and records, per i lane, the j's inside
+//      the cutoff plus a small margin, and per j lane the (i, position) of
+//      those entries; entries inside the Aziz damping radius D r_m are marked;
+//   2. lays the entries out i-major, orders them short-range first (so that
+//      the rarely taken damping branch stays within a few 32-entry chunks
+//      instead of splitting most of them) and evaluates them 32 at a time in
+//      FP64, every lane busy, storing each gradient in shared memory;
+//   3. sums the gradients per i and per j in list order (deterministic: the
+//      evaluation order does not enter any sum).
+// Under PBC the tile's positions are wrapped into the box once, so a
+// separation lies in (-L, L) and its minimum image is one conditional shift
+// (a compare of the bit patterns and one FP64 add) instead of
+// dx - L floor(dx/L + 1/2).  The exponentials use exp_tang.  Same result as
+// k_pair_tiles up to rounding; the exact FP64 cutoff test is applied in step 2.
 constexpr int kCompactWarps = 2;
 
 template <int D>
 struct CompactSmem {
-    double xi[kTile][D], xj[kTile][D];
+    double xi[kTile][D], xj[kTile][D];  // wrapped into the box under PBC
+    float xjf[kTile][D];                // FP32 copy of xj for the screen
     double g[kTile * kTile][D];
-    unsigned char ilist[kTile][kTile];     // j's of lane i
-    unsigned short jlist[kTile][kTile];    // (i << 8 | k) entries of lane j
+    unsigned char ilist[kTile][kTile];  // j's of lane i, bit 7 = short-range
+    unsigned short jlist[kTile][kTile]; // (i << 8 | k) entries of lane j
     int icnt[kTile], jcnt[kTile], off[kTile];
-    unsigned char fi[kTile * kTile], fj[kTile * kTile];
+    unsigned char fi[kTile * kTile], fj[kTile * kTile];  // fi bit 7 = short-range
+    unsigned short perm[kTile * kTile]; // evaluation order
 };
 
+// d in (-L, L) -> its minimum image; `half_bits` = bit pattern of L/2.
+__device__ __forceinline__ double min_image_wrapped(double d, double L, long long half_bits) {
+    const long long bits = __double_as_longlong(d);
+    const double sh = ((bits & 0x7fffffffffffffffLL) > half_bits) ? copysign(L, d) : 0.0;
+    return d - sh;
+}
+
+// One tile task: bead b, tile pair w (it <= jt) of the bead's T(T+1)/2.
 template <int D>
-__global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s, double* __restrict__ part, int T,
-                                                                          int npairs) {
-    extern __shared__ __align__(16) unsigned char csm_raw[];
-    CompactSmem<D>& sm = reinterpret_cast<CompactSmem<D>*>(csm_raw)[threadIdx.x >> 5];
-    const int w = blockIdx.x * kCompactWarps + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    const int b = blockIdx.y;
-    if (w >= npairs) return;
+__device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ part, int T, int b, int w,
+                                             CompactSmem<D>& sm, const double* tbl, int lane) {
     int it = (int)((2.0 * T + 1.0 - sqrt((2.0 * T + 1.0) * (2.0 * T + 1.0) - 8.0 * w)) * 0.5);
     while (it > 0 && it * T - it * (it - 1) / 2 > w) --it;
     while ((it + 1) * T - (it + 1) * it / 2 <= w) ++it;
@@ -299,8 +314,15 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
     const int i = it * kTile + lane, j = jt * kTile + lane;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-        sm.xi[lane][a] = i < s.N ? s.x[idx<D>(s, b, a, i)] : 0.0;
-        sm.xj[lane][a] = j < s.N ? s.x[idx<D>(s, b, a, j)] : 0.0;
+        double xv = i < s.N ? s.x[idx<D>(s, b, a, i)] : 0.0;
+        double yv = j < s.N ? s.x[idx<D>(s, b, a, j)] : 0.0;
+        if (s.pbc) {
+            xv -= s.L * rint(xv * s.invL);
+            yv -= s.L * rint(yv * s.invL);
+        }
+        sm.xi[lane][a] = xv;
+        sm.xj[lane][a] = yv;
+        sm.xjf[lane][a] = (float)yv;
     }
     sm.icnt[lane] = 0;
     sm.jcnt[lane] = 0;
@@ -308,7 +330,8 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
     // 1. FP32 screen, one rotation step at a time (lane i meets j = i + st)
     const double cut = s.cutoff;
     const float cut2f = (float)(cut * cut) * 1.0001f;
-    const float Lf = (float)s.L, invLf = (float)s.invL;
+    const float near2f = s.int_kind == POT_AZIZ ? (float)(Aziz::D * Aziz::rm * Aziz::D * Aziz::rm) * 1.0001f : -1.0f;
+    const float Lf = (float)s.L, halfLf = 0.5f * (float)s.L;
     float xif[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) xif[a] = (float)sm.xi[lane][a];
@@ -317,12 +340,12 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
     for (int st = first; st <= lastS; ++st) {
         const int jl = (lane + st) & 31;
         bool in = i < s.N && jt * kTile + jl < s.N && (!diag || st < 16 || lane < 16);
+        float r2 = 0.0f;
         if (in) {
-            float r2 = 0.0f;
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                float d = xif[a] - (float)sm.xj[jl][a];
-                if (s.pbc) d = min_image_f(d, Lf, invLf);
+                float d = xif[a] - sm.xjf[jl][a];
+                if (s.pbc && fabsf(d) > halfLf) d -= copysignf(Lf, d);
                 r2 += d * d;
             }
             in = r2 <= cut2f;
@@ -331,7 +354,7 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
             const int jc = sm.jcnt[jl];  // lanes of one step hit distinct j's
             sm.jlist[jl][jc] = (unsigned short)((lane << 8) | icnt);
             sm.jcnt[jl] = jc + 1;
-            sm.ilist[lane][icnt++] = (unsigned char)jl;
+            sm.ilist[lane][icnt++] = (unsigned char)(jl | (r2 < near2f ? 0x80 : 0));
         }
         __syncwarp();
     }
@@ -347,24 +370,65 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
     off -= icnt;
     sm.off[lane] = off;
     for (int k = 0; k < icnt; ++k) {
-        sm.fi[off + k] = (unsigned char)lane;
-        sm.fj[off + k] = sm.ilist[lane][k];
+        const int e = sm.ilist[lane][k];
+        sm.fi[off + k] = (unsigned char)(lane | (e & 0x80));
+        sm.fj[off + k] = (unsigned char)(e & 31);
     }
     __syncwarp();
-    for (int f = lane; f < total; f += 32) {
-        const int il = sm.fi[f], jl = sm.fj[f];
-        double r[D];
+    // evaluation order: short-range entries, then the rest
+    const unsigned lt = (1u << lane) - 1u;
+    int pos = 0, nnear = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int f0 = 0; f0 < total; f0 += 32) {
+            const int f = f0 + lane;
+            const bool take = f < total && ((sm.fi[f] >> 7) == (pass == 0 ? 1 : 0));
+            const unsigned bal = __ballot_sync(0xffffffffu, take);
+            if (take) sm.perm[pos + __popc(bal & lt)] = (unsigned short)f;
+            pos += __popc(bal);
+        }
+        if (pass == 0) nnear = pos;
+    }
+    __syncwarp();
+    const long long half_bits = __double_as_longlong(0.5 * s.L);
+    const double cut2 = cut * cut;
+    auto separation = [&](int f, double* r) {
+        const int il = sm.fi[f] & 31, jl = sm.fj[f];
         double r2 = 0.0;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
             double d = sm.xi[il][a] - sm.xj[jl][a];
-            if (s.pbc) d = min_image(d, s.L, s.invL);
+            if (s.pbc) d = min_image_wrapped(d, s.L, half_bits);
             r[a] = d;
             r2 += d * d;
         }
-        const double sc = r2 < cut * cut ? pair_scale<double>(s.int_kind, r2, s.int_a) : 0.0;
+        return r2;
+    };
+    auto store = [&](int f, double sc, const double* r) {
 #pragma unroll
         for (int a = 0; a < D; ++a) sm.g[f][a] = sc * r[a];  // grad V(r_i - r_j)
+    };
+    // short-range entries (and every entry of the other potentials)
+    const int ngen = s.int_kind == POT_AZIZ ? nnear : total;
+    for (int k = lane; k < ngen; k += 32) {
+        const int f = sm.perm[k];
+        double r[D];
+        const double r2 = separation(f, r);
+        store(f, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
+    }
+    // Aziz beyond the damping radius: two independent entries per lane and
+    // iteration on the branch-free path; an entry the FP32 screen placed
+    // here although it lies inside D r_m takes the general path
+    for (int k = ngen + lane; k < total; k += 64) {
+        const int f0 = sm.perm[k];
+        const bool two = k + 32 < total;
+        const int f1 = two ? sm.perm[k + 32] : f0;
+        double r0[D], r1[D];
+        const double q0 = separation(f0, r0), q1 = separation(f1, r1);
+        double sc0 = aziz_far_scale(q0, tbl), sc1 = aziz_far_scale(q1, tbl);
+        if (!aziz_is_far(q0)) sc0 = pair_scale_d<true>(s.int_kind, q0, s.int_a, tbl);
+        if (!aziz_is_far(q1)) sc1 = pair_scale_d<true>(s.int_kind, q1, s.int_a, tbl);
+        store(f0, q0 < cut2 ? sc0 : 0.0, r0);
+        if (two) store(f1, q1 < cut2 ? sc1 : 0.0, r1);
     }
     __syncwarp();
     // 3. deterministic sums: i side over its own (contiguous) entries, j side
@@ -396,6 +460,38 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
         if (j < s.N) {
 #pragma unroll
             for (int a = 0; a < D; ++a) part[((base_b + it) * D + a) * s.ld + j] = aj[a];
+        }
+    }
+}
+
+// Persistent warps take tile tasks (bead-major) from ctr[0] until none are
+// left; the warp that finishes last resets both counters for the next
+// launch (no waiting).
+template <int D>
+__global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s, double* __restrict__ part, int T,
+                                                                          int npairs, int* ctr) {
+    extern __shared__ __align__(16) unsigned char csm_raw[];
+    __shared__ double tbl[32];
+    if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
+    __syncthreads();
+    CompactSmem<D>& sm = reinterpret_cast<CompactSmem<D>*>(csm_raw)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int ntask = s.P * npairs;
+    for (;;) {
+        int task = 0;
+        if (lane == 0) task = atomicAdd(&ctr[0], 1);
+        task = __shfl_sync(0xffffffffu, task, 0);
+        if (task >= ntask) break;
+        const int b = task / npairs;
+        compact_tile<D>(s, part, T, b, task - b * npairs, sm, tbl, lane);
+        __syncwarp();
+    }
+    if (lane == 0) {
+        __threadfence();
+        if (atomicAdd(&ctr[1], 1) == (int)(gridDim.x * kCompactWarps) - 1) {
+            ctr[0] = 0;
+            ctr[1] = 0;
+            __threadfence();
         }
     }
 }
@@ -432,9 +528,286 @@ __global__ void k_bead_finish(Sys s, const double* __restrict__ part, int T, int
     }
 }
 
+// ---------------------------------------------------------------------------
+// Cell lists for a periodic box whose cutoff is small against the box
+// (nc = floor(L / rc) >= 4 cells per edge, each at least rc wide): every
+// pair inside the cutoff lies in one of the 3^D cells around a particle's
+// own, so each particle tests ~27 cells' worth of candidates instead of N.
+//
+// k_cell_bin (one block per bead) wraps the bead's positions into the box,
+// bins them by cell and writes them cell-sorted, stably (particles of a
+// cell in ascending index: the order of every later sum is fixed), with
+// FP64 and FP32 hi/lo copies.  k_pair_cells (one thread per particle in
+// sorted order) screens the candidates in FP32 into a per-thread list, then
+// the warp evaluates the lists in lockstep (FP64, or FP32 in the mixed
+// path) and sums the pair gradient on its own particle only; the result is
+// one partial-sum slot for k_bead_finish.
+constexpr int kCellBinThreads = 1024;
+constexpr int kCellThreads = 128;
+constexpr int kCellList = 64;
+
+template <int D>
+__device__ __forceinline__ int cell_of(const double* u, int nc, double L) {
+    int c = 0;
+#pragma unroll
+    for (int a = D - 1; a >= 0; --a) {
+        int k = (int)floor((u[a] + 0.5 * L) * (nc / L));
+        k = min(max(k, 0), nc - 1);
+        c = c * nc + k;
+    }
+    return c;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kCellBinThreads) k_cell_bin(Sys s, int nc, int* __restrict__ cstart,
+                                                              int* __restrict__ clist, double* __restrict__ xw,
+                                                              float* __restrict__ xh, float* __restrict__ xl) {
+    extern __shared__ int cur[];  // ncell (+1)
+    int ncell = 1;
+    for (int a = 0; a < D; ++a) ncell *= nc;
+    const int b = blockIdx.x, N = s.N;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    for (int c = tid; c <= ncell; c += blockDim.x) cur[c] = 0;
+    __syncthreads();
+    auto wrapped = [&](int i, double* u) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            const double x = s.x[idx<D>(s, b, a, i)];
+            u[a] = x - s.L * rint(x * s.invL);
+        }
+    };
+    for (int i = tid; i < N; i += blockDim.x) {
+        double u[D];
+        wrapped(i, u);
+        atomicAdd(&cur[cell_of<D>(u, nc, s.L)], 1);
+    }
+    __syncthreads();
+    // exclusive scan of the counts by warp 0 (each lane a contiguous range)
+    int* cs = cstart + (size_t)b * (ncell + 1);
+    if (warp == 0) {
+        const int per = (ncell + 31) / 32, c0 = lane * per, c1 = min(ncell, c0 + per);
+        int sum = 0;
+        for (int c = c0; c < c1; ++c) sum += cur[c];
+        int pre = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, pre, o);
+            if (lane >= o) pre += y;
+        }
+        int run = pre - sum;
+        for (int c = c0; c < c1; ++c) {
+            const int n = cur[c];
+            cs[c] = run;
+            cur[c] = run;
+            run += n;
+        }
+        if (lane == 31) cs[ncell] = pre;
+    }
+    __syncthreads();
+    // stable scatter: chunks of blockDim particles in index order; inside a
+    // chunk the warps take their turns and a group of lanes with the same
+    // cell is placed by its lowest lane
+    const unsigned lt = (1u << lane) - 1u;
+    for (int i0 = 0; i0 < N; i0 += blockDim.x) {
+        const int i = i0 + tid;
+        const bool valid = i < N;
+        double u[D];
+        int c = -1;
+        if (valid) {
+            wrapped(i, u);
+            c = cell_of<D>(u, nc, s.L);
+        }
+        const unsigned grp = __match_any_sync(0xffffffffu, c);
+        const int leader = __ffs(grp) - 1;
+        int base = 0;
+        for (int w = 0; w < nw; ++w) {
+            if (w == warp && valid && lane == leader) {
+                base = cur[c];
+                cur[c] = base + __popc(grp);
+            }
+            __syncthreads();
+        }
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (valid) {
+            const int pos = base + __popc(grp & lt);
+            clist[(size_t)b * N + pos] = i;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                const size_t o = ((size_t)b * D + a) * N + pos;
+                xw[o] = u[a];
+                const float h = (float)u[a];
+                xh[o] = h;
+                xl[o] = (float)(u[a] - (double)h);
+            }
+        }
+    }
+}
+
+template <int D, typename R>
+__global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, const int* __restrict__ cstart,
+                                                             const int* __restrict__ clist,
+                                                             const double* __restrict__ xw,
+                                                             const float* __restrict__ xh,
+                                                             const float* __restrict__ xl, double* __restrict__ fpair) {
+    __shared__ double tbl[32];
+    extern __shared__ int lists[];  // kCellList x kCellThreads
+    if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
+    __syncthreads();
+    int ncell = 1;
+    for (int a = 0; a < D; ++a) ncell *= nc;
+    const int b = blockIdx.y, N = s.N;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = k < N;
+    const int kk = active ? k : 0;
+    const int* cs = cstart + (size_t)b * (ncell + 1);
+    const double* Xw = xw + (size_t)b * D * N;
+    const float* Xh = xh + (size_t)b * D * N;
+    const float* Xl = xl + (size_t)b * D * N;
+    int* my = lists + threadIdx.x;
+    const double cut = s.cutoff, cut2 = cut * cut;
+    const float cut2f = (float)cut2 * 1.0001f;
+    const float Lf = (float)s.L, halfLf = 0.5f * (float)s.L;
+    const long long half_bits = __double_as_longlong(0.5 * s.L);
+    double xi[D];
+    float hi[D], lo[D];
+    int cc[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        xi[a] = Xw[(size_t)a * N + kk];
+        hi[a] = Xh[(size_t)a * N + kk];
+        lo[a] = Xl[(size_t)a * N + kk];
+        cc[a] = min(max((int)floor((xi[a] + 0.5 * s.L) * (nc / s.L)), 0), nc - 1);
+    }
+    double acc[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) acc[a] = 0.0;
+    // gradient of one candidate q (sorted index), subtracted from acc
+    auto eval = [&](int q) {
+        R r[D];
+        R r2 = (R)0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            R d;
+            if constexpr (sizeof(R) == 8) {
+                d = min_image_wrapped(xi[a] - Xw[(size_t)a * N + q], s.L, half_bits);
+            } else {
+                d = (hi[a] - Xh[(size_t)a * N + q]) + (lo[a] - Xl[(size_t)a * N + q]);
+                if (fabsf(d) > halfLf) d -= copysignf(Lf, d);
+            }
+            r[a] = d;
+            r2 += d * d;
+        }
+        if (!(r2 < (R)cut2)) return;
+        R sc;
+        if constexpr (sizeof(R) == 8) {
+            sc = (s.int_kind == POT_AZIZ && aziz_is_far(r2)) ? aziz_far_scale(r2, tbl)
+                                                              : pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl);
+        } else {
+            sc = pair_scale<float>(s.int_kind, r2, (float)s.int_a);
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) acc[a] -= (double)(sc * r[a]);
+    };
+    // 1. FP32 screen of the 3^D neighbour cells into the per-thread list
+    int cnt = 0;
+    if (active) {
+        int ncand = 1;
+        for (int a = 0; a < D; ++a) ncand *= 3;
+        for (int t = 0; t < ncand; ++t) {
+            int c = 0, tt = t;
+            int code[D];
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                code[a] = tt % 3 - 1;
+                tt /= 3;
+            }
+#pragma unroll
+            for (int a = D - 1; a >= 0; --a) c = c * nc + (cc[a] + code[a] + nc) % nc;
+            for (int q = cs[c]; q < cs[c + 1]; ++q) {
+                if (q == k) continue;
+                float r2 = 0.0f;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    float d = hi[a] - Xh[(size_t)a * N + q];
+                    if (fabsf(d) > halfLf) d -= copysignf(Lf, d);
+                    r2 += d * d;
+                }
+                if (r2 <= cut2f) {
+                    if (cnt < kCellList) my[cnt * kCellThreads] = q;
+                    else eval(q);  // rare overflow: evaluated on the spot
+                    ++cnt;
+                }
+            }
+        }
+    }
+    // 2. lockstep evaluation of the lists
+    const int mine = min(cnt, kCellList);
+    const int most = __reduce_max_sync(0xffffffffu, mine);
+    for (int e = 0; e < most; ++e)
+        if (e < mine) eval(my[e * kCellThreads]);
+    if (active) {
+        const int i = clist[(size_t)b * N + k];
+#pragma unroll
+        for (int a = 0; a < D; ++a) fpair[idx<D>(s, b, a, i)] = acc[a];
+    }
+}
+
+// Cell-list geometry: cells per edge (0 when cell lists do not apply).
+int cell_grid(const Sys& s, int D) {
+    if (!s.pbc || !(s.cutoff > 0.0) || s.int_kind == POT_FREE) return 0;
+    int nc = (int)std::floor(s.L / (s.cutoff * 1.000001));
+    if (nc < 4) return 0;
+    const int cap = D == 3 ? 16 : (D == 2 ? 64 : 4096);
+    return std::min(nc, cap);
+}
+
+size_t cell_buffer_bytes(const Sys& s, int D, int nc) {
+    size_t ncell = 1;
+    for (int a = 0; a < D; ++a) ncell *= nc;
+    const size_t n = (size_t)s.P * s.N;
+    return s.P * (ncell + 1) * sizeof(int) + n * sizeof(int) + n * D * (sizeof(double) + 2 * sizeof(float)) +
+           (size_t)s.P * D * s.ld * sizeof(double) + 256 * 6;
+}
+
+template <int D>
+static void cells_launch(const Sys& s, int nc, int mixed, int write_phys, unsigned char* buf, cudaStream_t st) {
+    size_t ncell = 1;
+    for (int a = 0; a < D; ++a) ncell *= nc;
+    const size_t n = (size_t)s.P * s.N;
+    auto carve = [&](size_t bytes) {
+        unsigned char* p = buf;
+        buf += (bytes + 255) / 256 * 256;
+        return p;
+    };
+    int* cstart = reinterpret_cast<int*>(carve(s.P * (ncell + 1) * sizeof(int)));
+    int* clist = reinterpret_cast<int*>(carve(n * sizeof(int)));
+    double* xw = reinterpret_cast<double*>(carve(n * D * sizeof(double)));
+    float* xh = reinterpret_cast<float*>(carve(n * D * sizeof(float)));
+    float* xl = reinterpret_cast<float*>(carve(n * D * sizeof(float)));
+    double* fpair = reinterpret_cast<double*>(carve((size_t)s.P * D * s.ld * sizeof(double)));
+    const size_t bin_smem = (ncell + 1) * sizeof(int);
+    if (bin_smem > 48 * 1024) cudaFuncSetAttribute(k_cell_bin<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bin_smem);
+    k_cell_bin<D><<<s.P, kCellBinThreads, bin_smem, st>>>(s, nc, cstart, clist, xw, xh, xl);
+    const size_t list_smem = sizeof(int) * kCellList * kCellThreads;
+    dim3 grid((s.N + kCellThreads - 1) / kCellThreads, s.P);
+    if (mixed) k_pair_cells<D, float><<<grid, kCellThreads, list_smem, st>>>(s, nc, cstart, clist, xw, xh, xl, fpair);
+    else k_pair_cells<D, double><<<grid, kCellThreads, list_smem, st>>>(s, nc, cstart, clist, xw, xh, xl, fpair);
+    const size_t ne = (size_t)s.P * D * s.ld;
+    k_bead_finish<D><<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(s, fpair, 1, write_phys);
+}
+
+void launch_pair_cells_and_finish(const Sys& s, int D, int nc, int mixed, int write_phys, void* buf, cudaStream_t st) {
+    unsigned char* b = reinterpret_cast<unsigned char*>(buf);
+    if (D == 1) cells_launch<1>(s, nc, mixed, write_phys, b, st);
+    else if (D == 2) cells_launch<2>(s, nc, mixed, write_phys, b, st);
+    else cells_launch<3>(s, nc, mixed, write_phys, b, st);
+}
+
+// The partial sums plus one trailing double that holds the compact kernel's
+// two task counters (zero between launches).
 size_t pair_partial_doubles(const Sys& s, int D) {
     const int T = (s.N + kTile - 1) / kTile;
-    return (size_t)s.P * T * D * s.ld;
+    return (size_t)s.P * T * D * s.ld + 1;
 }
 
 template <int D>
@@ -445,13 +818,20 @@ static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, 
         const int np = T * (T + 1) / 2;
         if (!mixed && s.cutoff > 0.0) {
             const size_t smem = sizeof(CompactSmem<D>) * kCompactWarps;
-            static bool attr = false;
-            if (!attr) {
+            static int resident = 0, sms = 0;
+            if (!resident) {
                 cudaFuncSetAttribute(k_pair_tiles_compact<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                attr = true;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_pair_tiles_compact<D>, 32 * kCompactWarps,
+                                                              smem);
+                int dev = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                if (resident < 1) resident = 1;
             }
-            dim3 grid((np + kCompactWarps - 1) / kCompactWarps, s.P);
-            k_pair_tiles_compact<D><<<grid, 32 * kCompactWarps, smem, st>>>(s, part, T, np);
+            const int ntask = s.P * np;
+            const int blocks = std::min((ntask + kCompactWarps - 1) / kCompactWarps, resident * sms);
+            int* ctr = reinterpret_cast<int*>(part + (pair_partial_doubles(s, D) - 1));
+            k_pair_tiles_compact<D><<<blocks, 32 * kCompactWarps, smem, st>>>(s, part, T, np, ctr);
         } else {
             dim3 grid((np + 3) / 4, s.P);
             if (mixed) k_pair_tiles<D, float><<<grid, 128, 0, st>>>(s, part, T, np);

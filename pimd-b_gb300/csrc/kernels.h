@@ -25,6 +25,12 @@ void launch_bead_forces(const Sys& s, int D, int mixed, int write_phys, cudaStre
 // `part` (pair_partial_doubles doubles), a second kernel adds them in order.
 size_t pair_partial_doubles(const Sys& s, int D);
 void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part, cudaStream_t st);
+// Cell lists for a periodic box with a short cutoff: cells per edge (0 when
+// they do not apply), the work buffer they need, and the force evaluation
+// (binning, pair forces, finish) into that buffer.
+int cell_grid(const Sys& s, int D);
+size_t cell_buffer_bytes(const Sys& s, int D, int nc);
+void launch_pair_cells_and_finish(const Sys& s, int D, int nc, int mixed, int write_phys, void* buf, cudaStream_t st);
 
 // Potential energy: per-bead partial sums of the external, pair and
 // non-exchange spring energies, part[(b * energy_blocks + blk) * 3 + term];
@@ -35,8 +41,9 @@ void launch_local_energy(const Sys& s, int D, int n, const int* items, double* o
 
 // exchange.cu: Feldman-Hirshberg exchange on beads 1 and P.
 void launch_exchange_energies(const Sys& s, int D, cudaStream_t st);
-// Returns the number of kernels launched (3, or 1 with `exact`: the
-// reference-order FP64 log-sum-exp recursion only).
+// Returns the number of kernels launched (6: estimate, weights, solve and
+// their retry, which exits at once unless a reused estimate failed; or 1
+// with `exact`: the reference-order FP64 log-sum-exp recursion only).
 int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st);
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st);
 void launch_exchange_estimators(const Sys& s, cudaStream_t st);

@@ -42,6 +42,25 @@ def ring(s, seed, spread_ang=0.3, box_ang=None):
     return centres[None] + rng.normal(0.0, spread_ang * ANG, (s.nbeads, s.natoms, s.ndim))
 
 
+def ring_separated(s, seed, dmin_ang=2.2, spread_ang=0.05):
+    """Centres placed by random sequential addition at least dmin apart
+    (minimum image under PBC), each bead displaced by a Gaussian jitter: a
+    liquid-like configuration without overlapping cores."""
+    rng = np.random.default_rng(seed)
+    L, dmin = s.size, dmin_ang * ANG
+    pts = []
+    while len(pts) < s.natoms:
+        c = rng.uniform(-0.5 * L, 0.5 * L, s.ndim)
+        if pts:
+            d = np.asarray(pts) - c
+            if s.pbc:
+                d -= L * np.floor(d / L + 0.5)
+            if np.min(np.einsum("ij,ij->i", d, d)) < dmin * dmin:
+                continue
+        pts.append(c)
+    return np.asarray(pts)[None] + rng.normal(0.0, spread_ang * ANG, (s.nbeads, s.natoms, s.ndim))
+
+
 def momenta(s, seed):
     rng = np.random.default_rng(seed + 1)
     return rng.normal(0.0, np.sqrt(s.mass / s.thermo_beta), (s.nbeads, s.natoms, s.ndim))

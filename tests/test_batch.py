@@ -226,3 +226,26 @@ def test_batch_nonfinite_exchange_names_the_replica():
         b.set_states(xs, ps)
         with pytest.raises(pk.ExchangeOverflowError, match="replica 2"):
             b.compute_forces()
+
+
+@pytest.mark.gpu
+def test_batch_exchange_retry_after_large_jump():
+    from tests.test_gpu_parity import _violent
+    s, cfg, x, p = _violent()
+    systems, cfgs, xs, ps = build(REPLICAS_3D[:2])
+    systems.append(s)
+    cfgs.append(cfg)
+    xs.append(x)
+    ps.append(p)
+    trs = [O.Trajectory(q, xs[r], ps[r]) for r, q in enumerate(systems)]
+    with pk.Batch(cfgs) as b:
+        b.set_states(xs, ps)
+        b.set_step(0)
+        for st in range(4):
+            for r, (q, c) in enumerate(zip(systems, cfgs)):
+                xi = O.philox_noise_device(c.seed, c.replica, st, q.nbeads, q.natoms, q.ndim)
+                assert trs[r].step(xi) == 0
+            b.step(1)
+            gx = b.get_states()[0]
+            for r, tr in enumerate(trs):
+                assert rel_per_bead(gx[r], tr.x) < 1e-9, (st, r)

@@ -9,7 +9,7 @@ import pytest
 
 from oracle import oracle as O
 from tests import golden_cases as G
-from tests.gpu_cases import case, momenta, pk, rel_per_bead, ring
+from tests.gpu_cases import case, momenta, pk, rel_per_bead, ring, ring_separated
 
 pytestmark = pytest.mark.gpu
 
@@ -215,3 +215,92 @@ def test_nonfinite_exchange_potential_is_reported():
         x[0, 3, 1] = 0.0
         g.set_state(x, np.zeros_like(x))
         g.compute_forces()
+
+
+def _violent(seed=11):
+    """Beads 1 and P thrown apart by 30 bohr per step: V moves by thousands
+    of kT between steps, so the previous step's potentials fail as the
+    estimate and the exchange takes its fresh-estimate retry every step."""
+    s, cfg = case(natoms=24, nbeads=8, T_K=0.5, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0),
+                  thermostat="none", fixcom=False)
+    x = ring(s, seed=seed, spread_ang=0.2)
+    p = momenta(s, seed)
+    p[0, :, 0] += s.mass * 30.0 / s.dt
+    p[-1, :, 0] -= s.mass * 30.0 / s.dt
+    return s, cfg, x, p
+
+
+def test_exchange_retry_after_large_jump():
+    s, cfg, x, p = _violent()
+    tr = O.Trajectory(s, x, p)
+    with pk.System(cfg) as g:
+        g.set_state(x, p)
+        g.set_step(0)
+        for st in range(4):
+            assert tr.step(np.zeros((2,) + x.shape)) == 0
+            g.step(1)
+            gx, gp, gf = g.get_state()
+            for got, want, label in ((gx, tr.x, "x"), (gp, tr.p, "p"), (gf, tr.f, "f")):
+                assert rel_per_bead(got, want) < 1e-9, (st, label, rel_per_bead(got, want))
+
+
+CELL_CASES = {
+    # periodic boxes with at least 4 cutoff-wide cells per edge; centres at
+    # least 2.2 A (Aziz) or 1 A (dipole) apart, beads jittered by 0.05 A
+    "aziz_3d_N600_P4": (dict(natoms=600, nbeads=4, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=24.0, inter="aziz",
+                             cutoff_ang=5.5), 2.2),
+    "dipole_2d_N700_P3": (dict(ndim=2, natoms=700, nbeads=3, T_K=2.0, pbc=True, box_ang=60.0, inter="dipole",
+                               int_p=(2.4799673e-4, 0, 0), cutoff_ang=9.0, ext="harmonic",
+                               ext_p=(1.0 * 0.036749326e-3, 0, 0)), 1.0),
+    "aziz_3d_dist_N300_P2": (dict(natoms=300, nbeads=2, bosonic=False, T_K=1.0, mass_amu=4.0026, pbc=True,
+                                  box_ang=20.0, inter="aziz", cutoff_ang=4.8), 2.2),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CELL_CASES))
+def test_cell_list_forces_match_oracle_and_tiles(name):
+    kw, dmin = CELL_CASES[name]
+    s, cfg = case(**kw)
+    x = ring_separated(s, seed=21, dmin_ang=dmin)
+    want = O.update_forces(s, x)["f"]
+    out = {}
+    for opt in (1, 0):
+        with pk.System(cfg) as g:
+            g.set_option("cell_lists", opt)
+            g.set_state(x, np.zeros_like(x))
+            g.compute_forces()
+            out[opt] = g.get_state()[2]
+    assert rel_per_bead(out[1], want) < FP64_TOL
+    assert rel_per_bead(out[1], out[0]) < 1e-12
+    s2, cfg2 = case(precision="mixed", **kw)
+    with pk.System(cfg2) as g:
+        g.set_option("cell_lists", 1)
+        g.set_state(x, np.zeros_like(x))
+        g.compute_forces()
+        f32 = g.get_state()[2]
+    assert np.linalg.norm(f32 - want) / np.linalg.norm(want) <= 1e-6
+
+
+def test_cell_list_trajectory_matches_oracle():
+    kw, dmin = CELL_CASES["aziz_3d_N600_P4"]
+    s, cfg = case(**kw)
+    x = ring_separated(s, seed=22, dmin_ang=dmin)
+    p = momenta(s, 22)
+    tr = O.Trajectory(s, x, p)
+    with pk.System(cfg) as g:
+        g.set_option("cell_lists", 1)
+        g.set_state(x, p)
+        g.set_step(0)
+        for st in range(4):
+            tr.step(O.philox_noise_device(cfg.seed, cfg.replica, st, s.nbeads, s.natoms, s.ndim))
+            g.step(1)
+            gx, gp, gf = g.get_state()
+            for got, want, label in ((gx, tr.x, "x"), (gp, tr.p, "p"), (gf, tr.f, "f")):
+                assert rel_per_bead(got, want) < 1e-9, (st, label)
+
+
+def test_cell_list_option_needs_cells():
+    s, cfg = case(natoms=8, nbeads=2, pbc=True, box_ang=10.0, inter="aziz", cutoff_ang=4.0)
+    with pk.System(cfg) as g:
+        with pytest.raises(pk.ConfigError, match="cell lists"):
+            g.set_option("cell_lists", 1)
