@@ -78,6 +78,25 @@ WORKLOADS = {
 }
 
 
+def max_over_ranks(x, dist, device="cuda"):
+    """The largest of each rank's `x` (the slowest rank's time); `x` itself
+    without a process group."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_workload(w, precision, rank):
+    """Rank r runs its own replica: replica id r in the noise counter and
+    initial state seed 12345 + r (no data is shared between ranks)."""
+    cfg = workload_config(w, precision)
+    cfg.replica = rank
+    return cfg, initial_state(w, seed=12345 + rank)
+
+
 def batched_workload(precision, n=512, seed=12345):
     """The ensemble workload: configs and initial states of `n` replicas."""
     pk = importlib.import_module("pimd-b_gb300")
@@ -133,12 +152,8 @@ def run_batched(pk, torch, stream, K, W, rank, world, dist):
         ev1.record(stream)
         torch.cuda.synchronize()
         b.synchronize()
-        t = ev0.elapsed_time(ev1) / 1e3
+        t = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, dist)
         launches = b.launch()["launches"] - launches0
-        if dist:
-            tt = torch.tensor([t], device="cuda", dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t = float(tt.item())
         # end to end: pinned host state in, one step, state and forces out
         n = int(b.offsets[-1])
         hx = torch.empty(n, dtype=torch.float64, pin_memory=True)
@@ -155,11 +170,7 @@ def run_batched(pk, torch, stream, K, W, rank, world, dist):
             b._c(lib.pimdb_batch_set_states(b._b, ptr(hx), ptr(hp)))
             b.step(1)
             b._c(lib.pimdb_batch_get_states(b._b, ptr(hx), ptr(hp), ptr(hf)))
-        te = time.perf_counter() - t0
-        if dist:
-            tt = torch.tensor([te], device="cuda", dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            te = float(tt.item())
+        te = max_over_ranks(time.perf_counter() - t0, dist)
     return {"value": world * units * K / t, "unit": "bead-steps/s", "ms_per_step": 1e3 * t / K, "steps": K,
             "replicas": len(cfgs), "bead_particles": units, "precision": "mixed (FP32 pair forces and Langevin "
             "normals, FP64 accumulation, exchange and integrator)",
@@ -372,9 +383,7 @@ def main():
             b.set_states(xs, ps)
             b.step(max(args.warmup, 1) + max(args.steps, 1))
         return
-    cfg = workload_config(w, args.precision)
-    cfg.replica = rank
-    x0, p0 = initial_state(w, seed=12345 + rank)
+    cfg, (x0, p0) = rank_workload(w, args.precision, rank)
     N, P, D = w["natoms"], w["nbeads"], w["ndim"]
     units = N * P
     sysm = pk.System(cfg, stream=stream.cuda_stream)
@@ -403,11 +412,7 @@ def main():
     sysm.synchronize()
     clocks = sampler.stop() if sampler else None
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    tot_s = sum(step_ms) / 1e3
-    if dist:
-        t = torch.tensor([tot_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_s = float(t.item())
+    tot_s = max_over_ranks(sum(step_ms) / 1e3, dist)
     value = world * units * K / tot_s
 
     # kernel launches in the timed region: the same K steps, counted
@@ -435,11 +440,7 @@ def main():
         sysm.set_state_ptr(hx.data_ptr(), hp.data_ptr(), device=False)
         sysm.step(1)
         sysm.get_state_ptr(hx.data_ptr(), hp.data_ptr(), hf.data_ptr(), device=False)
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     e2e = {"value": world * units * Ke / e2e_s, "unit": "bead-steps/s", "h2d_bytes_per_step": 2 * P * N * D * 8,
            "d2h_bytes_per_step": 3 * P * N * D * 8, "steps": Ke}
     sysm.close()
