@@ -121,7 +121,13 @@ int pimdb_compute_forces(pimdb_handle* h);
  * (VelocityVerletPropagator::step, src/propagators/velocity_verlet.cpp:7-22,
  * or NormalModesPropagator::step, src/propagators/normal_modes_propagator.cpp:19-71),
  * thermostat O-step, COM removal.  Synchronous: returns after the GPU is done
- * and reports a non-finite exchange potential. */
+ * and reports a non-finite exchange potential.  The last operations of the
+ * last step (with the fused normal-mode kernel: its kick, O-step and COM
+ * removal; otherwise a COM correction) are deferred and folded into the next
+ * step; every call that reads or changes the state (get/set_state, forces,
+ * exchange, energies, the plugin calls) completes them first, so the state
+ * seen by the caller is always that at the end of the step.  Runs of steps
+ * are captured once per step count and replayed as CUDA graphs. */
 int pimdb_step(pimdb_handle* h, int nsteps);
 /* Same, only enqueued on the handle's stream; errors surface at the next
  * pimdb_synchronize or synchronous call. */
@@ -219,7 +225,9 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
  *                    power of two; default 1);
  *   "cell_lists"     1 / 0 / -1: pair forces from cell lists (periodic box
  *                    with at least 4 cutoff-wide cells per edge) on / off /
- *                    automatic (default: on from 512 particles). */
+ *                    automatic (default: on from 512 particles);
+ *   "cuda_graphs"    0: enqueue every step's kernels instead of replaying a
+ *                    captured graph (default 1). */
 int pimdb_set_option(pimdb_handle* h, const char* name, int value);
 
 /* Bosonic exchange without any allocation (no counterpart in the reference).

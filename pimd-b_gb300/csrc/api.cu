@@ -6,7 +6,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -58,6 +60,30 @@ struct pimdb_handle {
     int cell_nc = 0;
     void* d_cells = nullptr;
     int opt_cells = -1;
+    // CUDA graphs of pimdb_step_async: keyed by the step count and the
+    // host-side step state at entry; the step index comes from d_step, which
+    // every graph advances by its step count
+    struct StepState {
+        int red_last, nred_last;
+        bool com_pending, nm_tail_pending;
+        bool operator<(const StepState& o) const {
+            return std::tie(red_last, nred_last, com_pending, nm_tail_pending) <
+                   std::tie(o.red_last, o.nred_last, o.com_pending, o.nm_tail_pending);
+        }
+    };
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        StepState after{};
+        long long kernels = 0;
+    };
+    std::map<std::pair<int, StepState>, StepGraph> graphs;
+    long long* d_step = nullptr;
+    bool dstep_valid = false;
+    bool capturing = false;
+    long long graph_base = 0;
+    int opt_graph = 1;
+    bool graph_broken = false;
+    bool warm = false;  // one uncaptured step first: lazy attribute and occupancy set-up stays out of captures
     bool profile = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double prof_ms[PIMDB_NUM_KERNEL_CLASSES] = {};
@@ -81,6 +107,25 @@ static void launch(pimdb_handle* h, int cls, F&& f, int nkernels = 1) {
     h->prof_ms[cls] += ms;
     h->prof_n[cls] += 1;
 }
+
+// Step index argument of a launch: absolute, or relative to the graph's
+// start while a graph is being captured.
+static StepRef step_ref(const pimdb_handle* h, long long step) {
+    if (h->capturing) return StepRef{h->d_step, step - h->graph_base};
+    return StepRef{nullptr, step};
+}
+
+// The last node of a step graph: the device step counter moves on.
+__global__ void k_step_advance(long long* step, int n) { *step += n; }
+static void launch_step_advance(long long* step, int n, cudaStream_t st) { k_step_advance<<<1, 1, 0, st>>>(step, n); }
+
+static void drop_graphs(pimdb_handle* h) {
+    for (auto& kv : h->graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    h->graphs.clear();
+}
+
+static void complete_pending(pimdb_handle* h);
 
 static std::string g_last_error;
 
@@ -259,6 +304,8 @@ static void free_handle(pimdb_handle* h) {
     if (h->d_bar) cudaFree(h->d_bar);
     if (h->d_tw) cudaFree(h->d_tw);
     if (h->d_cells) cudaFree(h->d_cells);
+    if (h->d_step) cudaFree(h->d_step);
+    drop_graphs(h);
     if (h->fork_ev) cudaEventDestroy(h->fork_ev);
     if (h->join_ev) cudaEventDestroy(h->join_ev);
     if (h->side) cudaStreamDestroy(h->side);
@@ -323,6 +370,7 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     // beyond 512 MiB the all-pairs kernel (no partials) is used instead.
     const size_t npart = pair_partial_doubles(s, h->D);
     if (e == cudaSuccess && npart * sizeof(double) <= (512ull << 20)) e = alloc(&h->d_part, npart);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_step, sizeof(long long));
     h->cell_nc = cell_grid(s, h->D);
     if (e == cudaSuccess && h->cell_nc > 0) e = cudaMalloc(&h->d_cells, cell_buffer_bytes(s, h->D, h->cell_nc));
     // xflags: [0],[1] exact fallback used (forward, backward); [2] completion
@@ -407,6 +455,7 @@ static int check_err_word(pimdb_handle* h) {
 
 static int set_state_impl(pimdb_handle* h, const double* x, const double* p, cudaMemcpyKind kind) {
     if (!h) return PIMDB_ERR_ARG;
+    complete_pending(h);
     Sys& s = h->s;
     const size_t n = (size_t)s.P * s.N * h->D;
     const double* src[2] = {x, p};
@@ -438,6 +487,7 @@ extern "C" int pimdb_set_state_device(pimdb_handle* h, const double* x, const do
 
 static int get_state_impl(pimdb_handle* h, double* x, double* p, double* f, cudaMemcpyKind kind) {
     if (!h) return PIMDB_ERR_ARG;
+    complete_pending(h);
     Sys& s = h->s;
     const size_t n = (size_t)s.P * s.N * h->D;
     double* dst[3] = {x, p, f};
@@ -462,6 +512,7 @@ extern "C" int pimdb_get_state_device(pimdb_handle* h, double* x, double* p, dou
 extern "C" int pimdb_set_step(pimdb_handle* h, long long step) {
     if (!h) return PIMDB_ERR_ARG;
     h->step = step;
+    h->dstep_valid = false;
     return PIMDB_OK;
 }
 extern "C" int pimdb_get_step(pimdb_handle* h, long long* step) {
@@ -482,31 +533,45 @@ static void enqueue_forces(pimdb_handle* h) {
         cudaEventRecord(h->fork_ev, h->stream);
         cudaStreamWaitEvent(h->side, h->fork_ev, 0);
     }
+    const int mixed = h->cfg.precision == PIMDB_MIXED;
+    const bool cells = h->d_cells && (h->opt_cells == 1 || (h->opt_cells < 0 && s.N >= 512));
+    const bool tiles = !cells && h->d_part && h->opt_newton3;
+    // with the tile or cell paths the exchange forces go to fx on the side
+    // stream and the finishing kernel adds them: off the critical path
+    const bool fx_in_finish = s.bosonic && (cells || tiles);
     if (s.bosonic) {
         launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, xs); });
         const int ex = h->opt_exact_exchange;
         launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, xs); }, ex ? 1 : 6);
+        if (fx_in_finish) launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 0, xs); });
     }
     if (fork) cudaEventRecord(h->join_ev, h->side);
-    const int mixed = h->cfg.precision == PIMDB_MIXED;
-    const bool cells = h->d_cells && (h->opt_cells == 1 || (h->opt_cells < 0 && s.N >= 512));
+    cudaEvent_t before_finish = fork && fx_in_finish ? h->join_ev : nullptr;
     if (cells) {
-        launch(h, PIMDB_K_BEAD_FORCES,
-               [&] { launch_pair_cells_and_finish(s, h->D, h->cell_nc, mixed, nm ? 1 : 0, h->d_cells, h->stream); }, 3);
-    } else if (h->d_part && h->opt_newton3) {
+        launch(h, PIMDB_K_BEAD_FORCES, [&] {
+            launch_pair_cells_and_finish(s, h->D, h->cell_nc, mixed, nm ? 1 : 0, h->d_cells, before_finish,
+                                         fx_in_finish, h->stream);
+        }, 3);
+    } else if (tiles) {
         const bool pairs = s.int_kind != PIMDB_POT_FREE && s.cutoff != 0.0;
         launch(
             h, PIMDB_K_BEAD_FORCES,
-            [&] { launch_pair_tiles_and_finish(s, h->D, mixed, nm ? 1 : 0, h->d_part, h->stream); }, pairs ? 2 : 1);
+            [&] {
+                launch_pair_tiles_and_finish(s, h->D, mixed, nm ? 1 : 0, h->d_part, before_finish, fx_in_finish,
+                                             h->stream);
+            },
+            pairs ? 2 : 1);
     } else {
         launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_bead_forces(s, h->D, mixed, nm ? 1 : 0, h->stream); });
     }
-    if (fork) cudaStreamWaitEvent(h->stream, h->join_ev, 0);
-    if (s.bosonic) launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 1, h->stream); });
+    if (fork && !fx_in_finish) cudaStreamWaitEvent(h->stream, h->join_ev, 0);
+    if (s.bosonic && !fx_in_finish)
+        launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 1, h->stream); });
 }
 
 extern "C" int pimdb_compute_forces(pimdb_handle* h) {
     if (!h) return PIMDB_ERR_ARG;
+    complete_pending(h);
     enqueue_forces(h);
     CUDA_TRY(h, cudaGetLastError());
     return check_err_word(h);
@@ -519,8 +584,8 @@ static void cart(pimdb_handle* h, int flags, int substep, int kick_nm) {
     const int rin = h->red_last, rout = 1 - h->red_last;
     if (!h->com_pending) flags &= ~SF_COM_APPLY;
     launch(h, PIMDB_K_CART_UPDATE, [&] {
-        launch_cart_update(h->s, h->D, flags, h->d_red[rin], h->nred_last, h->d_red[rout], h->step, substep, kick_nm,
-                           h->stream);
+        launch_cart_update(h->s, h->D, flags, h->d_red[rin], h->nred_last, h->d_red[rout], step_ref(h, h->step), substep,
+                           kick_nm, h->stream);
     });
     if (flags & SF_COM_APPLY) h->com_pending = false;
     if (flags & SF_COM_PARTIAL) {
@@ -534,8 +599,8 @@ static void nm_thermo(pimdb_handle* h, int flags, int substep) {
     const int rin = h->red_last, rout = 1 - h->red_last;
     if (!h->com_pending) flags &= ~SF_COM_APPLY;
     launch(h, PIMDB_K_NM_THERMO, [&] {
-        launch_nm_thermo(h->s, h->D, h->d_C, h->d_T, flags, h->d_red[rin], h->nred_last, h->d_red[rout], h->step,
-                         substep, h->stream);
+        launch_nm_thermo(h->s, h->D, h->d_C, h->d_T, flags, h->d_red[rin], h->nred_last, h->d_red[rout],
+                         step_ref(h, h->step), substep, h->stream);
     });
     if (flags & SF_COM_APPLY) h->com_pending = false;
     if (flags & SF_COM_PARTIAL) {
@@ -582,9 +647,9 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
             const int mode = (h->nm_tail_pending ? 1 : 0) | 2;
             const long long st = h->step;
             launch(h, PIMDB_K_NM_PROPAGATE, [&] {
-                cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, mode, st,
-                                                c.fixcom, h->opt_fft ? (const double2*)h->d_tw : nullptr, h->logP,
-                                                h->stream);
+                cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, mode,
+                                                step_ref(h, st), c.fixcom,
+                                                h->opt_fft ? (const double2*)h->d_tw : nullptr, h->logP, h->stream);
                 if (e != cudaSuccess) h->async_err = e;
             });
             enqueue_forces(h);
@@ -608,27 +673,96 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
         }
         h->step += 1;
     }
+}
+
+// Work of the last step deferred until the host needs the state: the tail
+// of the fused normal-mode kernel (kick, O-step, COM removal) and a pending
+// COM correction.  The next step absorbs both when it comes first, so a
+// run of pimdb_step calls pays for one fused launch per step.
+static void complete_pending(pimdb_handle* h) {
     if (h->nm_tail_pending) {
         const long long st = h->step;
         launch(h, PIMDB_K_NM_PROPAGATE, [&] {
-            cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, 1, st,
-                                            h->cfg.fixcom, h->opt_fft ? (const double2*)h->d_tw : nullptr, h->logP,
-                                            h->stream);
+            cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, 1,
+                                            step_ref(h, st), h->cfg.fixcom,
+                                            h->opt_fft ? (const double2*)h->d_tw : nullptr, h->logP, h->stream);
             if (e != cudaSuccess) h->async_err = e;
         });
         h->nm_tail_pending = false;
     }
-    // the last COM removal of the last step
-    if (h->com_pending) {
-        const long long keep = h->step;
-        cart(h, SF_COM_APPLY, 0, 0);
-        h->step = keep;
+    if (h->com_pending) cart(h, SF_COM_APPLY, 0, 0);
+}
+
+// `nsteps` steps as one CUDA graph (captured on first use for this step
+// state, then replayed).  Returns false when graphs cannot be used here;
+// the caller then enqueues the steps directly.
+static bool graph_steps(pimdb_handle* h, int nsteps) {
+    if (!h->opt_graph || h->graph_broken || h->profile || !h->warm || nsteps < 1) return false;
+    const pimdb_handle::StepState before{h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
+    const auto key = std::make_pair(nsteps, before);
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+        pimdb_handle::StepGraph g;
+        const long long step0 = h->step, launches0 = h->launches;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            h->graph_broken = true;
+            return false;
+        }
+        h->capturing = true;
+        h->graph_base = step0;
+        enqueue_steps(h, nsteps);
+        launch_step_advance(h->d_step, nsteps, h->stream);
+        h->capturing = false;
+        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        if (e == cudaSuccess && h->async_err == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        g.after = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
+        g.kernels = h->launches - launches0 + 1;
+        // the capture only recorded the work: restore the host state
+        h->step = step0;
+        h->launches = launches0;
+        h->red_last = before.red_last;
+        h->nred_last = before.nred_last;
+        h->com_pending = before.com_pending;
+        h->nm_tail_pending = before.nm_tail_pending;
+        if (e != cudaSuccess || h->async_err != cudaSuccess) {
+            cudaGetLastError();
+            h->async_err = cudaSuccess;
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            h->graph_broken = true;
+            return false;
+        }
+        it = h->graphs.emplace(key, g).first;
     }
+    if (!h->dstep_valid) {
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess ||
+            cudaMemcpy(h->d_step, &h->step, sizeof(long long), cudaMemcpyHostToDevice) != cudaSuccess) {
+            h->async_err = cudaGetLastError();
+            return true;
+        }
+        h->dstep_valid = true;
+    }
+    const cudaError_t e = cudaGraphLaunch(it->second.exec, h->stream);
+    if (e != cudaSuccess) h->async_err = e;
+    h->step += nsteps;
+    h->launches += it->second.kernels;
+    const pimdb_handle::StepState& a = it->second.after;
+    h->red_last = a.red_last;
+    h->nred_last = a.nred_last;
+    h->com_pending = a.com_pending;
+    h->nm_tail_pending = a.nm_tail_pending;
+    return true;
 }
 
 extern "C" int pimdb_step_async(pimdb_handle* h, int nsteps) {
     if (!h || nsteps < 0) return PIMDB_ERR_ARG;
-    enqueue_steps(h, nsteps);
+    if (!graph_steps(h, nsteps)) {
+        enqueue_steps(h, nsteps);
+        h->dstep_valid = false;
+        h->warm = nsteps > 0;
+    }
     if (h->async_err != cudaSuccess) {
         const cudaError_t e = h->async_err;
         h->async_err = cudaSuccess;
@@ -652,6 +786,7 @@ extern "C" int pimdb_synchronize(pimdb_handle* h) {
 
 extern "C" int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first, double* f_last) {
     if (!h) return PIMDB_ERR_ARG;
+    complete_pending(h);
     const Sys& s = h->s;
     if (!s.bosonic) return fail(h, PIMDB_ERR_CONFIG, "pimdb_exchange needs a bosonic configuration with nbeads > 1");
     launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
@@ -679,6 +814,7 @@ extern "C" int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first,
 
 extern "C" int pimdb_potential_energy(pimdb_handle* h, double* terms) {
     if (!h || !terms) return fail(h, PIMDB_ERR_ARG, "NULL argument");
+    complete_pending(h);
     const Sys& s = h->s;
     const int nb = energy_blocks(s);
     const size_t n = (size_t)s.P * nb * 3;
@@ -711,6 +847,7 @@ extern "C" int pimdb_potential_energy(pimdb_handle* h, double* terms) {
 extern "C" int pimdb_local_energy(pimdb_handle* h, int n, const int* items, double* out) {
     if (!h || (n > 0 && (!items || !out)) || n < 0) return fail(h, PIMDB_ERR_ARG, "NULL argument or n < 0");
     if (n == 0) return PIMDB_OK;
+    complete_pending(h);
     int* d_items = nullptr;
     double* d_out = nullptr;
     cudaError_t e = cudaMalloc((void**)&d_items, sizeof(int) * 2 * (size_t)n);
@@ -803,6 +940,7 @@ extern "C" int pimdb_measure_fp64_peak(double* tflops) {
 extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
     if (!h || !name) return PIMDB_ERR_ARG;
     const std::string n(name);
+    drop_graphs(h);
     if (n == "exact_exchange") h->opt_exact_exchange = value ? 1 : 0;
     else if (n == "fused_normal_modes") h->fused_nm = value && h->d_cmpart != nullptr;
     else if (n == "fft_normal_modes") h->opt_fft = value ? 1 : 0;
@@ -811,6 +949,8 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
         if (value > 0 && !h->d_cells)
             return fail(h, PIMDB_ERR_CONFIG, "cell lists need a periodic box with at least 4 cutoff-wide cells per edge");
         h->opt_cells = value < 0 ? -1 : (value ? 1 : 0);
+    } else if (n == "cuda_graphs") {
+        h->opt_graph = value ? 1 : 0;
     } else return fail(h, PIMDB_ERR_ARG, "unknown option " + n);
     return PIMDB_OK;
 }
@@ -823,7 +963,7 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
 extern "C" int pimdb_thermostat_step(pimdb_handle* h, int substep) {
     if (!h || substep < 0 || substep > 1) return PIMDB_ERR_ARG;
     const pimdb_config& c = h->cfg;
-    if (h->com_pending) cart(h, SF_COM_APPLY, 0, 0);  // finish an earlier COM removal first
+    complete_pending(h);  // finish the previous step's deferred work first
     if (c.thermostat == PIMDB_THERMO_LANGEVIN && c.nmthermostat) nm_thermo(h, 0, substep);
     else if (c.thermostat == PIMDB_THERMO_LANGEVIN) cart(h, SF_LANGEVIN, substep, 0);
     CUDA_TRY(h, cudaGetLastError());
@@ -832,7 +972,7 @@ extern "C" int pimdb_thermostat_step(pimdb_handle* h, int substep) {
 
 extern "C" int pimdb_zero_momentum(pimdb_handle* h) {
     if (!h) return PIMDB_ERR_ARG;
-    if (h->com_pending) cart(h, SF_COM_APPLY, 0, 0);
+    complete_pending(h);
     cart(h, SF_COM_PARTIAL, 0, 0);
     cart(h, SF_COM_APPLY, 0, 0);
     CUDA_TRY(h, cudaGetLastError());
@@ -841,7 +981,7 @@ extern "C" int pimdb_zero_momentum(pimdb_handle* h) {
 
 extern "C" int pimdb_propagate(pimdb_handle* h) {
     if (!h) return PIMDB_ERR_ARG;
-    if (h->com_pending) cart(h, SF_COM_APPLY, 0, 0);
+    complete_pending(h);
     if (h->cfg.propagator == PIMDB_PROP_NORMAL_MODES) {
         launch(h, PIMDB_K_NM_PROPAGATE, [&] {
             launch_nm_propagate(h->s, h->D, h->d_C, h->d_T, h->d_rot, 0, h->d_red[0], 0, h->stream);

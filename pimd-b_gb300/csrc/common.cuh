@@ -73,6 +73,15 @@ struct Sys {
     int* xflags;    // [0] forward used the exact fallback, [1] backward, [2] completion counter
 };
 
+// MD step index of a launch: `off`, plus the value at `base` when the launch
+// belongs to a replayed CUDA graph (base = the handle's device-side step
+// counter, which the graph itself advances).
+struct StepRef {
+    const long long* base;
+    long long off;
+    __device__ __forceinline__ long long get() const { return off + (base ? *base : 0); }
+};
+
 template <int D>
 __host__ __device__ inline size_t idx(const Sys& s, int b, int a, int i) {
     return ((size_t)b * D + a) * s.ld + i;

@@ -286,7 +286,8 @@ constexpr int kCompactWarps = 2;
 template <int D>
 struct CompactSmem {
     double xi[kTile][D], xj[kTile][D];  // wrapped into the box under PBC
-    float xjf[kTile][D];                // FP32 copy of xj for the screen
+    float xjf[kTile][D];                // FP32 copy of xj for the screen (hi part)
+    float xjl[kTile][D];                // lo part, xj - xjf (mixed far path)
     double g[kTile * kTile][D];
     unsigned char ilist[kTile][kTile];  // j's of lane i, bit 7 = short-range
     unsigned short jlist[kTile][kTile]; // (i << 8 | k) entries of lane j
@@ -303,7 +304,11 @@ __device__ __forceinline__ double min_image_wrapped(double d, double L, long lon
 }
 
 // One tile task: bead b, tile pair w (it <= jt) of the bead's T(T+1)/2.
-template <int D>
+// kMixed: entries beyond the Aziz damping radius (and every entry of the
+// other potentials) are evaluated in FP32 from hi/lo separations; entries
+// inside it stay FP64, where the repulsive and attractive terms nearly
+// cancel and FP32 would lose the difference.  Sums are FP64 either way.
+template <int D, bool kMixed>
 __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ part, int T, int b, int w,
                                              CompactSmem<D>& sm, const double* tbl, int lane) {
     int it = (int)((2.0 * T + 1.0 - sqrt((2.0 * T + 1.0) * (2.0 * T + 1.0) - 8.0 * w)) * 0.5);
@@ -322,7 +327,9 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         }
         sm.xi[lane][a] = xv;
         sm.xj[lane][a] = yv;
-        sm.xjf[lane][a] = (float)yv;
+        const float yh = (float)yv;
+        sm.xjf[lane][a] = yh;
+        if (kMixed) sm.xjl[lane][a] = (float)(yv - (double)yh);
     }
     sm.icnt[lane] = 0;
     sm.jcnt[lane] = 0;
@@ -407,6 +414,38 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
 #pragma unroll
         for (int a = 0; a < D; ++a) sm.g[f][a] = sc * r[a];  // grad V(r_i - r_j)
     };
+    if (kMixed) {
+        // FP64 for the short-range Aziz entries, FP32 for the rest
+        const float cut2f32 = (float)cut2;
+        const float paramf = (float)s.int_a;
+        const float Lf = (float)s.L, halfLf = 0.5f * (float)s.L;
+        const int nfp64 = s.int_kind == POT_AZIZ ? nnear : 0;
+        for (int k = lane; k < total; k += 32) {
+            const int f = sm.perm[k];
+            if (k < nfp64) {
+                double r[D];
+                const double r2 = separation(f, r);
+                store(f, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
+            } else {
+                const int il = sm.fi[f] & 31, jl = sm.fj[f];
+                float r[D];
+                float r2 = 0.0f;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    const double xi = sm.xi[il][a];
+                    const float ih = (float)xi, il_ = (float)(xi - (double)ih);
+                    float d = (ih - sm.xjf[jl][a]) + (il_ - sm.xjl[jl][a]);
+                    if (s.pbc && fabsf(d) > halfLf) d -= copysignf(Lf, d);
+                    r[a] = d;
+                    r2 += d * d;
+                }
+                const float sc = r2 < cut2f32 ? pair_scale<float>(s.int_kind, r2, paramf) : 0.0f;
+#pragma unroll
+                for (int a = 0; a < D; ++a) sm.g[f][a] = (double)(sc * r[a]);
+            }
+        }
+        __syncwarp();
+    } else {
     // short-range entries (and every entry of the other potentials)
     const int ngen = s.int_kind == POT_AZIZ ? nnear : total;
     for (int k = lane; k < ngen; k += 32) {
@@ -431,6 +470,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         if (two) store(f1, q1 < cut2 ? sc1 : 0.0, r1);
     }
     __syncwarp();
+    }
     // 3. deterministic sums: i side over its own (contiguous) entries, j side
     //    over its list in recording order
     double ai[D], aj[D];
@@ -467,7 +507,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
 // Persistent warps take tile tasks (bead-major) from ctr[0] until none are
 // left; the warp that finishes last resets both counters for the next
 // launch (no waiting).
-template <int D>
+template <int D, bool kMixed>
 __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s, double* __restrict__ part, int T,
                                                                           int npairs, int* ctr) {
     extern __shared__ __align__(16) unsigned char csm_raw[];
@@ -483,7 +523,7 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= ntask) break;
         const int b = task / npairs;
-        compact_tile<D>(s, part, T, b, task - b * npairs, sm, tbl, lane);
+        compact_tile<D, kMixed>(s, part, T, b, task - b * npairs, sm, tbl, lane);
         __syncwarp();
     }
     if (lane == 0) {
@@ -499,7 +539,7 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
 // f = springs + (-grad V_ext + sum of the pair slots), one thread per
 // (bead, axis, particle).  T = 0 when there are no pair forces.
 template <int D>
-__global__ void k_bead_finish(Sys s, const double* __restrict__ part, int T, int write_phys) {
+__global__ void k_bead_finish(Sys s, const double* __restrict__ part, int T, int write_phys, int add_fx) {
     const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const int i = (int)(e % s.ld);
     const size_t ba = e / s.ld;
@@ -515,7 +555,9 @@ __global__ void k_bead_finish(Sys s, const double* __restrict__ part, int T, int
     const size_t o = idx<D>(s, b, a, i);
     if (write_phys) s.fphys[o] = acc;
     if (s.bosonic && (b == 0 || b == s.P - 1)) {
-        s.f[o] = acc;
+        // exterior springs from the exchange (fx, written beside the pair
+        // forces) or, without add_fx, added by the exchange force kernel
+        s.f[o] = add_fx ? acc + s.fx[((size_t)(b == 0 ? 0 : 1) * D + a) * s.ld + i] : acc;
     } else {
         const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
         double dp = s.x[idx<D>(s, bp, a, i)] - xi[a];
@@ -666,6 +708,8 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
     int* my = lists + threadIdx.x;
     const double cut = s.cutoff, cut2 = cut * cut;
     const float cut2f = (float)cut2 * 1.0001f;
+    // FP32 r^2 below which a mixed-precision Aziz pair is evaluated in FP64
+    const float near2f = (float)((Aziz::D * Aziz::rm) * (Aziz::D * Aziz::rm)) * 1.0001f;
     const float Lf = (float)s.L, halfLf = 0.5f * (float)s.L;
     const long long half_bits = __double_as_longlong(0.5 * s.L);
     double xi[D];
@@ -703,6 +747,22 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
             sc = (s.int_kind == POT_AZIZ && aziz_is_far(r2)) ? aziz_far_scale(r2, tbl)
                                                               : pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl);
         } else {
+            if (s.int_kind == POT_AZIZ && r2 < near2f) {
+                // inside the damping radius the repulsive and attractive
+                // terms nearly cancel: FP64 from the FP64 positions
+                double rd[D];
+                double q2 = 0.0;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    rd[a] = min_image_wrapped(xi[a] - Xw[(size_t)a * N + q], s.L, half_bits);
+                    q2 += rd[a] * rd[a];
+                }
+                if (!(q2 < cut2)) return;
+                const double scd = pair_scale_d<true>(s.int_kind, q2, s.int_a, tbl);
+#pragma unroll
+                for (int a = 0; a < D; ++a) acc[a] -= scd * rd[a];
+                return;
+            }
             sc = pair_scale<float>(s.int_kind, r2, (float)s.int_a);
         }
 #pragma unroll
@@ -770,7 +830,8 @@ size_t cell_buffer_bytes(const Sys& s, int D, int nc) {
 }
 
 template <int D>
-static void cells_launch(const Sys& s, int nc, int mixed, int write_phys, unsigned char* buf, cudaStream_t st) {
+static void cells_launch(const Sys& s, int nc, int mixed, int write_phys, unsigned char* buf, cudaEvent_t before_finish,
+                         int add_fx, cudaStream_t st) {
     size_t ncell = 1;
     for (int a = 0; a < D; ++a) ncell *= nc;
     const size_t n = (size_t)s.P * s.N;
@@ -793,14 +854,16 @@ static void cells_launch(const Sys& s, int nc, int mixed, int write_phys, unsign
     if (mixed) k_pair_cells<D, float><<<grid, kCellThreads, list_smem, st>>>(s, nc, cstart, clist, xw, xh, xl, fpair);
     else k_pair_cells<D, double><<<grid, kCellThreads, list_smem, st>>>(s, nc, cstart, clist, xw, xh, xl, fpair);
     const size_t ne = (size_t)s.P * D * s.ld;
-    k_bead_finish<D><<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(s, fpair, 1, write_phys);
+    if (before_finish) cudaStreamWaitEvent(st, before_finish, 0);
+    k_bead_finish<D><<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(s, fpair, 1, write_phys, add_fx);
 }
 
-void launch_pair_cells_and_finish(const Sys& s, int D, int nc, int mixed, int write_phys, void* buf, cudaStream_t st) {
+void launch_pair_cells_and_finish(const Sys& s, int D, int nc, int mixed, int write_phys, void* buf,
+                                  cudaEvent_t before_finish, int add_fx, cudaStream_t st) {
     unsigned char* b = reinterpret_cast<unsigned char*>(buf);
-    if (D == 1) cells_launch<1>(s, nc, mixed, write_phys, b, st);
-    else if (D == 2) cells_launch<2>(s, nc, mixed, write_phys, b, st);
-    else cells_launch<3>(s, nc, mixed, write_phys, b, st);
+    if (D == 1) cells_launch<1>(s, nc, mixed, write_phys, b, before_finish, add_fx, st);
+    else if (D == 2) cells_launch<2>(s, nc, mixed, write_phys, b, before_finish, add_fx, st);
+    else cells_launch<3>(s, nc, mixed, write_phys, b, before_finish, add_fx, st);
 }
 
 // The partial sums plus one trailing double that holds the compact kernel's
@@ -811,27 +874,28 @@ size_t pair_partial_doubles(const Sys& s, int D) {
 }
 
 template <int D>
-static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, cudaStream_t st) {
+static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, cudaEvent_t before_finish, int add_fx,
+                         cudaStream_t st) {
     const bool pairs = s.int_kind != POT_FREE && s.cutoff != 0.0;
     const int T = pairs ? (s.N + kTile - 1) / kTile : 0;
     if (pairs) {
         const int np = T * (T + 1) / 2;
-        if (!mixed && s.cutoff > 0.0) {
+        if (s.cutoff > 0.0) {
             const size_t smem = sizeof(CompactSmem<D>) * kCompactWarps;
-            static int resident = 0, sms = 0;
-            if (!resident) {
-                cudaFuncSetAttribute(k_pair_tiles_compact<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_pair_tiles_compact<D>, 32 * kCompactWarps,
-                                                              smem);
+            static int resident[2] = {0, 0}, sms = 0;
+            auto kern = mixed ? k_pair_tiles_compact<D, true> : k_pair_tiles_compact<D, false>;
+            if (!resident[mixed]) {
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[mixed], kern, 32 * kCompactWarps, smem);
                 int dev = 0;
                 cudaGetDevice(&dev);
                 cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                if (resident < 1) resident = 1;
+                if (resident[mixed] < 1) resident[mixed] = 1;
             }
             const int ntask = s.P * np;
-            const int blocks = std::min((ntask + kCompactWarps - 1) / kCompactWarps, resident * sms);
+            const int blocks = std::min((ntask + kCompactWarps - 1) / kCompactWarps, resident[mixed] * sms);
             int* ctr = reinterpret_cast<int*>(part + (pair_partial_doubles(s, D) - 1));
-            k_pair_tiles_compact<D><<<blocks, 32 * kCompactWarps, smem, st>>>(s, part, T, np, ctr);
+            kern<<<blocks, 32 * kCompactWarps, smem, st>>>(s, part, T, np, ctr);
         } else {
             dim3 grid((np + 3) / 4, s.P);
             if (mixed) k_pair_tiles<D, float><<<grid, 128, 0, st>>>(s, part, T, np);
@@ -839,13 +903,15 @@ static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, 
         }
     }
     const size_t n = (size_t)s.P * D * s.ld;
-    k_bead_finish<D><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, part, T, write_phys);
+    if (before_finish) cudaStreamWaitEvent(st, before_finish, 0);
+    k_bead_finish<D><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, part, T, write_phys, add_fx);
 }
 
-void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part, cudaStream_t st) {
-    if (D == 1) tiles_launch<1>(s, mixed, write_phys, part, st);
-    else if (D == 2) tiles_launch<2>(s, mixed, write_phys, part, st);
-    else tiles_launch<3>(s, mixed, write_phys, part, st);
+void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part,
+                                  cudaEvent_t before_finish, int add_fx, cudaStream_t st) {
+    if (D == 1) tiles_launch<1>(s, mixed, write_phys, part, before_finish, add_fx, st);
+    else if (D == 2) tiles_launch<2>(s, mixed, write_phys, part, before_finish, add_fx, st);
+    else tiles_launch<3>(s, mixed, write_phys, part, before_finish, add_fx, st);
 }
 
 template <int D>

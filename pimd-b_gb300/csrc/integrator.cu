@@ -80,7 +80,8 @@ __device__ __forceinline__ double nm_kick_force(const Sys& s, int b, int a, int 
 // One thread per (bead, axis, particle pair).
 template <int D>
 __global__ void k_cart_update(Sys s, int flags, const double* __restrict__ red_in, int nred_in,
-                              double* __restrict__ red_out, long long step, int substep, int kick_nm) {
+                              double* __restrict__ red_out, StepRef sref, int substep, int kick_nm) {
+    const long long step = sref.get();
     __shared__ double shred[32];
     const int half = (s.N + 1) / 2;
     const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -117,27 +118,30 @@ __global__ void k_cart_update(Sys s, int flags, const double* __restrict__ red_i
     if (flags & SF_COM_PARTIAL) com_write_partials<D>(part, red_out, shred);
 }
 
-constexpr int kNmTile = 8;      // particles per block
-constexpr int kNmThreads = 256; // 4 particle pairs x 64 mode groups
+constexpr int kNmTile = 4;                           // particles per block
+constexpr int kNmPairs = kNmTile / 2;                // particle pairs per block
+constexpr int kNmGroups = 64;                        // mode groups
+constexpr int kNmThreads = kNmPairs * kNmGroups;
 
 // Langevin O-step on the normal modes: p_nm = C p, p_nm <- c1 p_nm + c2 xi,
-// p = C^T p_nm.  One block per (8-particle tile, axis); thread (pair pp,
+// p = C^T p_nm.  One block per (kNmTile-particle tile, axis); thread (pair pp,
 // group g) handles particles 2pp, 2pp+1 of the tile for modes g, g+64, ...
 // and then for beads g, g+64, ...
 template <int D>
 __global__ void __launch_bounds__(kNmThreads) k_nm_thermo(Sys s, const double* __restrict__ C,
                                                           const double* __restrict__ T, int flags,
                                                           const double* __restrict__ red_in, int nred_in,
-                                                          double* __restrict__ red_out, long long step,
+                                                          double* __restrict__ red_out, StepRef sref,
                                                           int substep) {
+    const long long step = sref.get();
     extern __shared__ double sm[];
     __shared__ double shred[32];
     const int P = s.P;
-    double* sp = sm;                 // [P][8]
-    double* sq = sm + P * kNmTile;   // [P][8]
+    double* sp = sm;                 // [P][kNmTile]
+    double* sq = sm + P * kNmTile;   // [P][kNmTile]
     const int a = blockIdx.y;
     const int i0 = blockIdx.x * kNmTile;
-    const int pp = threadIdx.x & 3, g = threadIdx.x >> 2;
+    const int pp = threadIdx.x % kNmPairs, g = threadIdx.x / kNmPairs;
     double cm[3] = {0.0, 0.0, 0.0};
     if (flags & SF_COM_APPLY) com_from_partials<D>(s, red_in, nred_in, cm, shred);
     for (int e = threadIdx.x; e < P * kNmTile; e += blockDim.x) {
@@ -147,7 +151,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_thermo(Sys s, const double* _
     __syncthreads();
     const int half = (s.N + 1) / 2;
     const uint64_t t = 2ull * (unsigned long long)step + substep;
-    for (int k = g; k < P; k += 64) {
+    for (int k = g; k < P; k += kNmGroups) {
         double q0 = 0.0, q1 = 0.0;
         const double* ck = C + (size_t)k * P;
         for (int b = 0; b < P; ++b) {
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_thermo(Sys s, const double* _
     }
     __syncthreads();
     double part = 0.0;
-    for (int j = g; j < P; j += 64) {
+    for (int j = g; j < P; j += kNmGroups) {
         double v0 = 0.0, v1 = 0.0;
         const double* tj = T + (size_t)j * P;
         for (int k = 0; k < P; ++k) {
@@ -209,7 +213,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
     double* spi = sm + 3 * P * kNmTile;
     const int a = blockIdx.y;
     const int i0 = blockIdx.x * kNmTile;
-    const int pp = threadIdx.x & 3, g = threadIdx.x >> 2;
+    const int pp = threadIdx.x % kNmPairs, g = threadIdx.x / kNmPairs;
     double cm[3] = {0.0, 0.0, 0.0};
     if (com_apply) com_from_partials<D>(s, red_in, nred_in, cm, shred);
     for (int e = threadIdx.x; e < P * kNmTile; e += blockDim.x) {
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
         sp[e] = p;
     }
     __syncthreads();
-    for (int k = g; k < P; k += 64) {
+    for (int k = g; k < P; k += kNmGroups) {
         double q0 = 0.0, q1 = 0.0, p0 = 0.0, p1 = 0.0;
         const double* ck = C + (size_t)k * P;
         for (int b = 0; b < P; ++b) {
@@ -254,7 +258,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
         spi[k * kNmTile + 2 * pp + 1] = pb;
     }
     __syncthreads();
-    for (int j = g; j < P; j += 64) {
+    for (int j = g; j < P; j += kNmGroups) {
         double x0 = 0.0, x1 = 0.0, v0 = 0.0, v1 = 0.0;
         const double* tj = T + (size_t)j * P;
         for (int k = 0; k < P; ++k) {
@@ -441,8 +445,9 @@ template <int D>
 __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __restrict__ C,
                                                          const double* __restrict__ T,
                                                          const double* __restrict__ rot, double* cmpart,
-                                                         unsigned* bar, int mode, long long step, int fixcom,
+                                                         unsigned* bar, int mode, StepRef sref, int fixcom,
                                                          const double2* __restrict__ tw, int logP) {
+    const long long step = sref.get();
     extern __shared__ double sm[];
     __shared__ double shred[32];
     const int P = s.P;
@@ -454,7 +459,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
     double* sy = sm + 5 * P * kNmTile;  // normal-mode x
     const int a = blockIdx.y;
     const int i0 = blockIdx.x * kNmTile;
-    const int pp = threadIdx.x & 3, g = threadIdx.x >> 2;
+    const int pp = threadIdx.x % kNmPairs, g = threadIdx.x / kNmPairs;
     const int nblocks = gridDim.x * gridDim.y;
     const int bid = blockIdx.y * gridDim.x + blockIdx.x;
     const bool head = mode & 2, tail = mode & 1;
@@ -478,7 +483,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
         NmArrays ar = {{sp, sf, sx}, {sq, sg, sy}};
         nm_forward_fft(ar, head ? 3 : 2, P, logP, tw, w0, w1);
     } else {
-    for (int k = g; k < P; k += 64) {
+    for (int k = g; k < P; k += kNmGroups) {
         double q0 = 0.0, q1 = 0.0, f0 = 0.0, f1 = 0.0, x0 = 0.0, x1 = 0.0;
         const double* ck = C + (size_t)k * P;
         for (int b = 0; b < P; ++b) {
@@ -508,7 +513,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
     const double sqrtP = sqrt((double)P);
     const double cm_scale = sqrtP * sqrtP / ((double)s.N * (double)P);  // q0 -> sqrt(P) cm
     auto thermostat = [&](uint64_t t) {
-        for (int k = g; k < P; k += 64) {
+        for (int k = g; k < P; k += kNmGroups) {
             const int o = k * kNmTile + 2 * pp;
             const int ie = i0 + 2 * pp;
             const double2 z =
@@ -544,7 +549,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
     if (head) {
         thermostat(2ull * (unsigned long long)step);
         if (fixcom && !remove_com(1)) return;
-        for (int k = g; k < P; k += 64) {
+        for (int k = g; k < P; k += kNmGroups) {
             const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
             for (int h2 = 0; h2 < 2; ++h2) {
                 const int o = k * kNmTile + 2 * pp + h2;
@@ -583,7 +588,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
         }
         return;
     }
-    for (int j = g; j < P; j += 64) {
+    for (int j = g; j < P; j += kNmGroups) {
         double x0 = 0.0, x1 = 0.0, v0 = 0.0, v1 = 0.0;
         const double* tj = T + (size_t)j * P;
         for (int k = 0; k < P; ++k) {
@@ -610,7 +615,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
     }
 }
 
-// [6][P][8] arrays plus two FFT work buffers of 12 complex transforms
+// [6][P][kNmTile] arrays plus two FFT work buffers of 3 kNmPairs complex transforms
 size_t nm_fused_smem(const Sys& s) {
     return sizeof(double) * (6 * (size_t)s.P * kNmTile + 2 * 2 * 3 * (kNmTile / 2) * (size_t)s.P);
 }
@@ -639,7 +644,7 @@ bool nm_fused_fits(const Sys& s, int D) {
 
 template <int D>
 static cudaError_t nm_fused_t(const Sys& s, const double* C, const double* T, const double* rot, double* cmpart,
-                              unsigned* bar, int mode, long long step, int fixcom, const double2* tw, int logP,
+                              unsigned* bar, int mode, StepRef step, int fixcom, const double2* tw, int logP,
                               cudaStream_t st) {
     dim3 grid((s.N + kNmTile - 1) / kNmTile, D);
     Sys sc = s;
@@ -648,7 +653,7 @@ static cudaError_t nm_fused_t(const Sys& s, const double* C, const double* T, co
 }
 
 cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
-                            unsigned* bar, int mode, long long step, int fixcom, const double2* tw, int logP,
+                            unsigned* bar, int mode, StepRef step, int fixcom, const double2* tw, int logP,
                             cudaStream_t st) {
     if (D == 1) return nm_fused_t<1>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
     if (D == 2) return nm_fused_t<2>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
@@ -683,7 +688,7 @@ int cart_update_blocks(const Sys& s, int D) {
 int nm_blocks(const Sys& s, int D) { return ((s.N + kNmTile - 1) / kNmTile) * D; }
 
 void launch_cart_update(const Sys& s, int D, int flags, const double* red_in, int nred_in, double* red_out,
-                        long long step, int substep, int kick_nm, cudaStream_t st) {
+                        StepRef step, int substep, int kick_nm, cudaStream_t st) {
     const int g = cart_update_blocks(s, D);
     if (D == 1) k_cart_update<1><<<g, 256, 0, st>>>(s, flags, red_in, nred_in, red_out, step, substep, kick_nm);
     else if (D == 2) k_cart_update<2><<<g, 256, 0, st>>>(s, flags, red_in, nred_in, red_out, step, substep, kick_nm);
@@ -692,7 +697,7 @@ void launch_cart_update(const Sys& s, int D, int flags, const double* red_in, in
 
 template <int D>
 static void nm_thermo_launch(const Sys& s, const double* C, const double* T, int flags, const double* red_in,
-                             int nred_in, double* red_out, long long step, int substep, cudaStream_t st) {
+                             int nred_in, double* red_out, StepRef step, int substep, cudaStream_t st) {
     const size_t smem = sizeof(double) * 2 * (size_t)s.P * kNmTile;
     cudaFuncSetAttribute(k_nm_thermo<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid((s.N + kNmTile - 1) / kNmTile, D);
@@ -700,7 +705,7 @@ static void nm_thermo_launch(const Sys& s, const double* C, const double* T, int
 }
 
 void launch_nm_thermo(const Sys& s, int D, const double* C, const double* T, int flags, const double* red_in,
-                      int nred_in, double* red_out, long long step, int substep, cudaStream_t st) {
+                      int nred_in, double* red_out, StepRef step, int substep, cudaStream_t st) {
     if (D == 1) nm_thermo_launch<1>(s, C, T, flags, red_in, nred_in, red_out, step, substep, st);
     else if (D == 2) nm_thermo_launch<2>(s, C, T, flags, red_in, nred_in, red_out, step, substep, st);
     else nm_thermo_launch<3>(s, C, T, flags, red_in, nred_in, red_out, step, substep, st);

@@ -23,14 +23,19 @@ enum StepFlags : int {
 void launch_bead_forces(const Sys& s, int D, int mixed, int write_phys, cudaStream_t st);
 // Same result with Newton's third law: pair tiles write partial sums into
 // `part` (pair_partial_doubles doubles), a second kernel adds them in order.
+// With add_fx the finishing kernel also adds the exchange's exterior spring
+// forces (fx) on beads 1 and P, after waiting for `before_finish` (may be
+// null) that marks them done.
 size_t pair_partial_doubles(const Sys& s, int D);
-void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part, cudaStream_t st);
+void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part,
+                                  cudaEvent_t before_finish, int add_fx, cudaStream_t st);
 // Cell lists for a periodic box with a short cutoff: cells per edge (0 when
 // they do not apply), the work buffer they need, and the force evaluation
 // (binning, pair forces, finish) into that buffer.
 int cell_grid(const Sys& s, int D);
 size_t cell_buffer_bytes(const Sys& s, int D, int nc);
-void launch_pair_cells_and_finish(const Sys& s, int D, int nc, int mixed, int write_phys, void* buf, cudaStream_t st);
+void launch_pair_cells_and_finish(const Sys& s, int D, int nc, int mixed, int write_phys, void* buf,
+                                  cudaEvent_t before_finish, int add_fx, cudaStream_t st);
 
 // Potential energy: per-bead partial sums of the external, pair and
 // non-exchange spring energies, part[(b * energy_blocks + blk) * 3 + term];
@@ -54,9 +59,9 @@ void launch_unpack(const Sys& s, int D, const double* src, double* dst, cudaStre
 int cart_update_blocks(const Sys& s, int D);
 int nm_blocks(const Sys& s, int D);
 void launch_cart_update(const Sys& s, int D, int flags, const double* red_in, int nred_in, double* red_out,
-                        long long step, int substep, int kick_nm, cudaStream_t st);
+                        StepRef step, int substep, int kick_nm, cudaStream_t st);
 void launch_nm_thermo(const Sys& s, int D, const double* C, const double* T, int flags, const double* red_in,
-                      int nred_in, double* red_out, long long step, int substep, cudaStream_t st);
+                      int nred_in, double* red_out, StepRef step, int substep, cudaStream_t st);
 void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, const double* rot, int com_apply,
                          const double* red_in, int nred_in, cudaStream_t st);
 
@@ -68,7 +73,7 @@ bool nm_fused_fits(const Sys& s, int D);
 // `tw` (P/2 twiddles exp(-2 pi i t/P)) selects the FFT transforms (P a power
 // of two, logP = log2 P); NULL selects the P x P matrix products.
 cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
-                            unsigned* bar, int mode, long long step, int fixcom, const double2* tw, int logP,
+                            unsigned* bar, int mode, StepRef step, int fixcom, const double2* tw, int logP,
                             cudaStream_t st);
 
 }  // namespace pimdb

@@ -304,3 +304,50 @@ def test_cell_list_option_needs_cells():
     with pk.System(cfg) as g:
         with pytest.raises(pk.ConfigError, match="cell lists"):
             g.set_option("cell_lists", 1)
+
+
+@pytest.mark.parametrize("cells", [0, 1])
+def test_mixed_precision_liquid_aziz(cells):
+    """Mixed precision on a liquid-like Aziz configuration (centres >= 2.2 A
+    apart at the benchmark density): FP32 beyond the damping radius, FP64
+    inside it, force error <= 1e-6 norm-relative."""
+    kw = dict(natoms=512, nbeads=4, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=28.6434, inter="aziz",
+              cutoff_ang=5.5 if cells else 14.3217)
+    s, cfg = case(precision="mixed", **kw)
+    x = ring_separated(s, seed=31, dmin_ang=2.2)
+    want = O.update_forces(s, x)
+    with pk.System(cfg) as g:
+        g.set_option("cell_lists", cells)
+        g.set_state(x, np.zeros_like(x))
+        g.compute_forces()
+        f = g.get_state()[2]
+    err = np.linalg.norm(f - want["f"]) / np.linalg.norm(want["f"])
+    phys_err = np.linalg.norm(f - want["spring"] - want["phys"]) / np.linalg.norm(want["phys"])
+    assert err <= 1e-6 and phys_err <= 1e-6, (err, phys_err)
+
+
+@pytest.mark.parametrize("name", ["vv_langevin_bosons_N16_P32", "nm_nmthermo_bosons_aziz", "nm_langevin_dist",
+                                  "vv_nve_bosons_aziz"])
+def test_cuda_graph_steps_equal_plain_launches(name):
+    """Replayed step graphs (with the device-side step counter) against plain
+    launches, including a jump of the step index between calls."""
+    kw = TRAJ_CASES[name]
+    s, cfg = case(**kw)
+    x = ring(s, seed=8, spread_ang=0.2)
+    p = momenta(s, 8)
+    out = []
+    for graphs in (1, 0):
+        with pk.System(cfg) as g:
+            g.set_option("cuda_graphs", graphs)
+            g.set_state(x, p)
+            g.set_step(0)
+            for _ in range(4):
+                g.step(1)
+            g.step(2)
+            g.set_step(100)
+            for _ in range(3):
+                g.step(1)
+            assert g.get_step() == 103
+            out.append(g.get_state())
+    for u, v in zip(*out):
+        assert np.array_equal(u, v)
