@@ -187,6 +187,22 @@ int pimdb_potential_energy(pimdb_handle* h, double* terms);
  * P, is -f_bi; finite differences of it stay accurate at any N. */
 int pimdb_local_energy(pimdb_handle* h, int n, const int* items, double* out);
 
+/* The reference's observables of the current state (src/observables/
+ * energy.cpp, classical.cpp, bosonic.cpp, gsf_action.cpp), each bead's
+ * value as the reference computes it on that bead's rank, summed over beads
+ * as ObservablesLogger::log does (src/observables/observable.cpp:82-116).
+ * Atomic units, except temperature in kelvin (classical.cpp:60).  The GSF
+ * force term uses the total gradient on each particle (the reference's
+ * gsf_action.cpp:34 adds arrays of different lengths when an interaction is
+ * present). */
+typedef struct pimdb_observables {
+    double kinetic, potential, ext_pot, int_pot, virial;  /* energy */
+    double temperature, cl_kinetic, cl_spring;            /* classical */
+    double prob_dist, prob_all;                           /* bosonic */
+    double w_gsf, pot_gsf;                                /* gsf */
+} pimdb_observables;
+int pimdb_compute_observables(pimdb_handle* h, pimdb_observables* out);
+
 /* Instrumentation (no counterpart in the reference, which only reports the
  * wall time per step, src/simulation.cpp:517-572).  Kernel classes: */
 enum pimdb_kernel_class {

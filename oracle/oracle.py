@@ -73,6 +73,8 @@ def lib():
         L.orc_system_init.argtypes = [S, C.c_double, C.c_double]
         L.orc_exchange.argtypes = [S, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_exchange.restype = C.c_int
+        L.orc_observables.argtypes = [S, dp, dp, dp]
+        L.orc_observables.restype = C.c_int
         L.orc_potential_energy.argtypes = [S, dp, dp]
         L.orc_potential_energy.restype = C.c_int
         L.orc_update_forces.argtypes = [S, dp, dp, dp, dp, C.c_int]
@@ -136,6 +138,20 @@ def exchange(s: System, x: np.ndarray):
     st = lib().orc_exchange(C.byref(s), _dp(x), _dp(f1), _dp(fP), _dp(sc), _dp(E), _dp(V), _dp(Vb), _dp(prob))
     return dict(status=st, f1=f1, fP=fP, VB=sc[0], prim=sc[1], p_distinct=sc[2], p_longest=sc[3], E=E, V=V, Vb=Vb,
                 prob=prob)
+
+
+OBSERVABLES = ["kinetic", "potential", "ext_pot", "int_pot", "virial", "temperature", "cl_kinetic", "cl_spring",
+               "prob_dist", "prob_all", "w_gsf", "pot_gsf"]
+
+
+def observables(s: System, x: np.ndarray, p: np.ndarray) -> dict:
+    """The reference's observables of one state, summed over beads (atomic
+    units; temperature in kelvin): orc_observables."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    out = np.zeros(12)
+    lib().orc_observables(C.byref(s), _dp(x), _dp(p), _dp(out))
+    return dict(zip(OBSERVABLES, out))
 
 
 def potential_energy(s: System, x: np.ndarray) -> np.ndarray:

@@ -494,6 +494,108 @@ int orc_potential_energy(const orc_system* s, const double* x_all, double* terms
     return 0;
 }
 
+/* Observables of one state (src/observables/{energy,classical,bosonic,
+ * gsf_action}.cpp), each bead's value as the reference computes it on that
+ * bead's rank, summed over beads as ObservablesLogger::log does
+ * (observable.cpp:82-116).  Atomic units, except temperature in kelvin as
+ * classical.cpp:60 always reports it:
+ *   out[0] kinetic (primitive)  out[1] potential  out[2] ext_pot
+ *   out[3] int_pot              out[4] virial     out[5] temperature
+ *   out[6] cl_kinetic           out[7] cl_spring  out[8] prob_dist
+ *   out[9] prob_all             out[10] w_gsf     out[11] pot_gsf
+ * The GSF force term uses the total gradient on each particle; the
+ * reference's gsf_action.cpp:34 adds a one-vector array to an N-vector one,
+ * which reads past the end of the smaller array when N > 1 and an
+ * interaction is present. */
+int orc_observables(const orc_system* s, const double* x_all, const double* p_all, double* out) {
+    const int N = s->natoms, D = s->ndim, P = s->nbeads;
+    const long bead = (long)N * D;
+    const int bosonic = s->bosonic && P > 1;
+    double sc[4] = {0.0, 0.0, 0.0, 0.0};
+    int st = 0;
+    if (bosonic) st = orc_exchange(s, x_all, NULL, NULL, sc, NULL, NULL, NULL, NULL);
+    for (int k = 0; k < 12; ++k) out[k] = 0.0;
+    double* g = (double*)malloc(sizeof(double) * (size_t)bead);
+    double* fe = (double*)malloc(sizeof(double) * (size_t)bead);
+    for (int b = 0; b < P; ++b) {
+        const double* x = x_all + (long)b * bead;
+        const double* p = p_all + (long)b * bead;
+        const double* xp = x_all + (long)((b - 1 + P) % P) * bead;
+        /* classicalSpringEnergy (simulation.cpp:464-486) */
+        double spring = 0.0;
+        for (long k = 0; k < bead; ++k) {
+            double diff = xp[k] - x[k];
+            if (s->pbc) diff = orc_min_image(diff, s->size);
+            spring += diff * diff;
+        }
+        spring *= 0.5 * s->spring_constant;
+        /* energy.cpp:30-51 */
+        double kinetic = 0.5 * D * N / s->beta;
+        if (b == 0 && bosonic) kinetic += sc[1];
+        else kinetic -= spring / P;
+        /* energy.cpp:59-110 */
+        double ext = 0.0, inter = 0.0, virial = 0.0;
+        ext = orc_ext_value(s, x, N);
+        orc_ext_grad(s, x, N, fe);
+        for (long k = 0; k < bead; ++k) {
+            g[k] = fe[k];
+            virial -= x[k] * (-fe[k]);
+        }
+        if (s->cutoff != 0.0) {
+            double r[3], gr[3];
+            for (int i = 0; i < N; ++i)
+                for (int j = i + 1; j < N; ++j) {
+                    for (int a = 0; a < D; ++a) {
+                        double d = x[(long)i * D + a] - x[(long)j * D + a];
+                        if (s->pbc) d = orc_min_image(d, s->size);
+                        r[a] = d;
+                    }
+                    const double dist = vnorm(r, D);
+                    if (dist < s->cutoff || s->cutoff < 0.0) {
+                        orc_pair_grad(s, r, gr);
+                        const double v = orc_pair_value(s, r);
+                        inter += v;
+                        for (int a = 0; a < D; ++a) {
+                            virial -= x[(long)i * D + a] * (-gr[a]);
+                            g[(long)i * D + a] += gr[a];
+                            g[(long)j * D + a] -= gr[a];
+                        }
+                    }
+                }
+        }
+        out[1] += (ext + inter) / P;
+        out[2] += ext / P;
+        out[3] += inter / P;
+        out[4] += virial * (0.5 / P);
+        out[0] += kinetic;
+        /* classical.cpp:32-78 */
+        double ke = 0.0;
+        for (long k = 0; k < bead; ++k) ke += p[k] * p[k];
+        ke *= 0.5 / s->mass;
+        const double dof = (double)D * N * P;
+        out[5] += 2.0 * ke / (dof * 1.0) / P / 3.1668152e-06; /* units.h: kelvin */
+        out[6] += ke;
+        out[7] += (b == 0 && bosonic) ? sc[0] : spring;
+        /* bosonic.cpp:17-22 */
+        if (b == 0 && bosonic) {
+            out[8] += sc[2];
+            out[9] += sc[3];
+        }
+        /* gsf_action.cpp:21-73 (alpha = 0) */
+        double f2 = 0.0;
+        for (long k = 0; k < bead; ++k) f2 += g[k] * g[k];
+        const double sp = s->spring_constant / P;
+        const double pot_term = (ext + inter) / (3 * P);
+        const double f2_term = f2 / (9 * sp * P * P);
+        double w = (b % 2 != 0) ? -pot_term : pot_term + f2_term;
+        out[10] += w * (-s->beta);
+        if (b % 2 != 0) out[11] += (ext + inter) / (0.5 * P);
+    }
+    free(g);
+    free(fe);
+    return st;
+}
+
 /* ---- a tiny parallel-for over POSIX threads ---- */
 typedef void (*orc_body)(void* ctx, int i);
 typedef struct {

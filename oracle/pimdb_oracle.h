@@ -96,6 +96,8 @@ void orc_physical_forces(const orc_system* s, const double* x, double* f);
 /* spring_out / phys_out may be NULL.  Returns the exchange status. */
 /* External, pair, non-exchange spring energies and V_B (terms[4]). */
 int orc_potential_energy(const orc_system* s, const double* x_all, double* terms);
+/* Observables (energy, classical, bosonic, gsf), summed over beads, out[12]. */
+int orc_observables(const orc_system* s, const double* x_all, const double* p_all, double* out);
 int orc_update_forces(const orc_system* s, const double* x_all, double* f_all, double* spring_out, double* phys_out,
                       int nthreads);
 

@@ -29,11 +29,13 @@ EXPORTS = [
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
     "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
     "pimdb_measure_fp64_peak", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
-    "pimdb_propagate", "pimdb_potential_energy", "pimdb_local_energy", "pimdb_batch_create", "pimdb_batch_destroy", "pimdb_batch_size", "pimdb_batch_set_states",
+    "pimdb_propagate", "pimdb_compute_observables", "pimdb_potential_energy", "pimdb_local_energy", "pimdb_batch_create", "pimdb_batch_destroy", "pimdb_batch_size", "pimdb_batch_set_states",
     "pimdb_batch_get_states", "pimdb_batch_set_step", "pimdb_batch_get_step", "pimdb_batch_compute_forces",
     "pimdb_batch_step", "pimdb_batch_step_async", "pimdb_batch_synchronize", "pimdb_batch_exchange",
     "pimdb_batch_set_option", "pimdb_batch_get_launch", "pimdb_batch_autotune", "pimdb_batch_last_error",
 ]
+OBSERVABLES = ["kinetic", "potential", "ext_pot", "int_pot", "virial", "temperature", "cl_kinetic", "cl_spring",
+               "prob_dist", "prob_all", "w_gsf", "pot_gsf"]
 KERNEL_CLASSES = ["bead_forces", "exch_energies", "exch_recursions", "exch_forces", "exch_estimators",
                   "cart_update", "nm_propagate", "nm_thermo"]
 
@@ -99,6 +101,7 @@ def lib():
             "pimdb_thermostat_step": ([vp, C.c_int], C.c_int),
             "pimdb_zero_momentum": ([vp], C.c_int),
             "pimdb_propagate": ([vp], C.c_int),
+            "pimdb_compute_observables": ([vp, vp], C.c_int),
             "pimdb_potential_energy": ([vp, vp], C.c_int),
             "pimdb_local_energy": ([vp, C.c_int, vp, vp], C.c_int),
             "pimdb_batch_create": ([cfgp, C.c_int, vp, C.POINTER(vp)], C.c_int),
@@ -304,6 +307,13 @@ class System:
         _check(lib().pimdb_profile(self._h, enable, _ptr(ms), _ptr(n), C.byref(tot)), self._h)
         return dict(ms=dict(zip(KERNEL_CLASSES, ms.tolist())), counts=dict(zip(KERNEL_CLASSES, n.tolist())),
                     launches=tot.value)
+
+    def observables(self) -> dict:
+        """The reference's observables of the current state, summed over
+        beads (atomic units; temperature in kelvin)."""
+        out = (C.c_double * len(OBSERVABLES))()
+        _check(lib().pimdb_compute_observables(self._h, C.byref(out)), self._h)
+        return dict(zip(OBSERVABLES, list(out)))
 
     def potential_energy(self):
         """Terms of U: external, pair, non-exchange springs, V_B."""

@@ -844,6 +844,68 @@ extern "C" int pimdb_potential_energy(pimdb_handle* h, double* terms) {
     return PIMDB_OK;
 }
 
+extern "C" int pimdb_compute_observables(pimdb_handle* h, pimdb_observables* out) {
+    if (!h || !out) return fail(h, PIMDB_ERR_ARG, "NULL argument");
+    complete_pending(h);
+    const Sys& s = h->s;
+    const int D = h->D, P = s.P, N = s.N;
+    const int nb = energy_blocks(s);
+    const size_t n = (size_t)P * nb * 7;
+    double* part = nullptr;
+    CUDA_TRY(h, cudaMalloc((void**)&part, n * sizeof(double)));
+    launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_observable_terms(s, D, part, h->stream); });
+    if (s.bosonic) {
+        launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, D, h->stream); });
+        const int ex = h->opt_exact_exchange;
+        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 6);
+        launch(h, PIMDB_K_EXCH_ESTIMATORS, [&] { launch_exchange_estimators(s, h->stream); });
+    }
+    std::vector<double> hp(n);
+    double sc[4] = {0.0, 0.0, 0.0, 0.0};
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), part, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && s.bosonic) e = cudaMemcpyAsync(sc, s.scal, sizeof sc, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(part);
+    if (e != cudaSuccess) return fail(h, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    const int st = check_err_word(h);
+    if (st != PIMDB_OK) return st;
+    // assembled per bead as src/observables/{energy,classical,bosonic,
+    // gsf_action}.cpp do on each bead's rank, then summed over beads
+    // (observable.cpp:82-116)
+    pimdb_observables o{};
+    const double beta = 1.0 / (1.0 * h->cfg.temperature);
+    for (int b = 0; b < P; ++b) {
+        double t[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int q = 0; q < nb; ++q)
+            for (int k = 0; k < 7; ++k) t[k] += hp[((size_t)b * nb + q) * 7 + k];
+        const double spring = t[1] * (0.5 * s.kappa);
+        double kinetic = 0.5 * D * N / beta;
+        if (b == 0 && s.bosonic) kinetic += sc[1];
+        else kinetic -= spring / P;
+        o.kinetic += kinetic;
+        o.potential += (t[2] + t[4]) / P;
+        o.ext_pot += t[2] / P;
+        o.int_pot += t[4] / P;
+        o.virial += (t[3] + t[5]) * (0.5 / P);
+        const double ke = t[0] * (0.5 / s.mass);
+        o.temperature += 2.0 * ke / ((double)D * N * P * 1.0) / P / 3.1668152e-06;
+        o.cl_kinetic += ke;
+        o.cl_spring += (b == 0 && s.bosonic) ? sc[0] : spring;
+        if (b == 0 && s.bosonic) {
+            o.prob_dist += sc[2];
+            o.prob_all += sc[3];
+        }
+        const double sp = s.kappa / P;
+        const double pot_term = (t[2] + t[4]) / (3 * P);
+        const double f2_term = t[6] / (9 * sp * P * P);
+        o.w_gsf += ((b % 2 != 0) ? -pot_term : pot_term + f2_term) * (-beta);
+        if (b % 2 != 0) o.pot_gsf += (t[2] + t[4]) / (0.5 * P);
+    }
+    *out = o;
+    return PIMDB_OK;
+}
+
 extern "C" int pimdb_local_energy(pimdb_handle* h, int n, const int* items, double* out) {
     if (!h || (n > 0 && (!items || !out)) || n < 0) return fail(h, PIMDB_ERR_ARG, "NULL argument or n < 0");
     if (n == 0) return PIMDB_OK;

@@ -1055,6 +1055,103 @@ __global__ void k_local_energy(Sys s, int n, const int* __restrict__ items, doub
     }
 }
 
+// Per-bead terms of the reference's observables (src/observables/*.cpp),
+// thread per particle i of bead b:
+//   [0] sum p^2            [1] |x_{b-1} - x_b|^2 (minimum image)
+//   [2] V_ext(x_i)         [3] x_i . grad V_ext(x_i)
+//   [4] V(r_ij), j > i     [5] x_i . grad V(r_ij), j > i   (energy.cpp:82-96:
+//                              only the first particle's coordinate enters)
+//   [6] |grad_i (V_ext + sum_j V(r_ij))|^2 (the GSF force term)
+// part[((b * gridDim.x + block) * kObsTerms + k]
+constexpr int kObsTerms = 7;
+
+template <int D>
+__global__ void __launch_bounds__(kEnergyThreads) k_observable_terms(Sys s, double* __restrict__ part) {
+    __shared__ double xs[D][kEnergyThreads];
+    __shared__ double red[kObsTerms * 32];
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * kEnergyThreads + threadIdx.x;
+    const bool active = i < s.N;
+    double xi[D], t[kObsTerms] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, g[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xi[a] = active ? s.x[idx<D>(s, b, a, i)] : 0.0;
+    if (active) {
+        const int bp = (b - 1 + s.P) % s.P;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            const double pv = s.p[idx<D>(s, b, a, i)];
+            t[0] += pv * pv;
+            double d = s.x[idx<D>(s, bp, a, i)] - xi[a];
+            if (s.pbc) d = min_image(d, s.L, s.invL);
+            t[1] += d * d;
+        }
+        t[2] = ext_value<D>(s, xi);
+        double fe[D];
+        ext_force<D>(s, xi, fe);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            g[a] = -fe[a];
+            t[3] += xi[a] * g[a];
+        }
+    }
+    const bool pairs = s.int_kind != POT_FREE && s.cutoff != 0.0;
+    if (pairs) {
+        for (int j0 = 0; j0 < s.N; j0 += kEnergyThreads) {
+            __syncthreads();
+            const int jl = j0 + threadIdx.x;
+#pragma unroll
+            for (int a = 0; a < D; ++a) xs[a][threadIdx.x] = jl < s.N ? s.x[idx<D>(s, b, a, jl)] : 0.0;
+            __syncthreads();
+            if (!active) continue;
+            const int jn = min(kEnergyThreads, s.N - j0);
+            for (int jj = 0; jj < jn; ++jj) {
+                const int j = j0 + jj;
+                if (j == i) continue;
+                double r[D], r2 = 0.0;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    double d = xi[a] - xs[a][jj];
+                    if (s.pbc) d = min_image(d, s.L, s.invL);
+                    r[a] = d;
+                    r2 += d * d;
+                }
+                if (s.cutoff > 0.0 && !(sqrt(r2) < s.cutoff)) continue;
+                const double sc = pair_scale<double>(s.int_kind, r2, s.int_a);
+#pragma unroll
+                for (int a = 0; a < D; ++a) g[a] += sc * r[a];
+                if (j > i) {
+                    t[4] += pair_value(s.int_kind, r2, s.int_a);
+#pragma unroll
+                    for (int a = 0; a < D; ++a) t[5] += xi[a] * (sc * r[a]);
+                }
+            }
+        }
+    }
+    if (active) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) t[6] += g[a] * g[a];
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kObsTerms; ++k) {
+        const double v = warp_sum(t[k]);
+        if (lane == 0) red[k * 32 + w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kObsTerms) {
+        double v = 0.0;
+        for (int q = 0; q < nw; ++q) v += red[threadIdx.x * 32 + q];
+        part[((size_t)b * gridDim.x + blockIdx.x) * kObsTerms + threadIdx.x] = v;
+    }
+}
+
+void launch_observable_terms(const Sys& s, int D, double* part, cudaStream_t st) {
+    dim3 grid((s.N + kEnergyThreads - 1) / kEnergyThreads, s.P);
+    if (D == 1) k_observable_terms<1><<<grid, kEnergyThreads, 0, st>>>(s, part);
+    else if (D == 2) k_observable_terms<2><<<grid, kEnergyThreads, 0, st>>>(s, part);
+    else k_observable_terms<3><<<grid, kEnergyThreads, 0, st>>>(s, part);
+}
+
 int energy_blocks(const Sys& s) { return (s.N + kEnergyThreads - 1) / kEnergyThreads; }
 
 void launch_energy_terms(const Sys& s, int D, double* part, cudaStream_t st) {

@@ -41,6 +41,9 @@ void launch_pair_cells_and_finish(const Sys& s, int D, int nc, int mixed, int wr
 // non-exchange spring energies, part[(b * energy_blocks + blk) * 3 + term];
 // and the local energy of listed (bead, particle) items ([n][2] ints).
 int energy_blocks(const Sys& s);
+// Per-bead observable terms, part[(b * energy_blocks + blk) * 7 + term]
+// (see k_observable_terms).
+void launch_observable_terms(const Sys& s, int D, double* part, cudaStream_t st);
 void launch_energy_terms(const Sys& s, int D, double* part, cudaStream_t st);
 void launch_local_energy(const Sys& s, int D, int n, const int* items, double* out, cudaStream_t st);
 

@@ -192,6 +192,11 @@ static void read_config(const IniFile& r, int ndim, pimdb_config& c, RunParams& 
     run.output_positions = r.Get("output", "positions", "off");
     run.output_velocities = r.Get("output", "velocities", "off");
     run.output_forces = r.Get("output", "forces", "off");
+    // params.cpp:256-259
+    run.obs_energy = r.Get("observables", "energy", "kelvin");
+    run.obs_classical = r.Get("observables", "classical", "off");
+    run.obs_bosonic = r.Get("observables", "bosonic", "off");
+    run.obs_gsf = r.Get("observables", "gsf", "off");
 
     const std::string propagator = r.GetString(SIM, "propagator", "cartesian");
     if (bosonic && propagator == "normal_modes")

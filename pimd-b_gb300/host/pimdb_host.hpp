@@ -18,7 +18,9 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <format>
 #include <fstream>
+#include <functional>
 #include <memory>
 #include <random>
 #include <stdexcept>
@@ -26,6 +28,7 @@
 #include <vector>
 
 #include "pimdb_gb300.h"
+#include "units.hpp"
 
 namespace pimdb_host {
 
@@ -37,6 +40,8 @@ struct RunParams {
     std::string init_pos_type = "random", init_pos_spec;
     std::string init_vel_type = "random", init_vel_spec;
     std::string output_positions = "off", output_velocities = "off", output_forces = "off";
+    // [observables]: output unit of each observable group, or "off"
+    std::string obs_energy = "kelvin", obs_classical = "off", obs_bosonic = "off", obs_gsf = "off";
 };
 
 // Reads config.ini (schema and messages of src/params.cpp:8-260); throws
@@ -127,6 +132,72 @@ inline void check(int st, pimdb_handle* h = nullptr) {
     if (st == PIMDB_ERR_NONFINITE_VB) throw std::overflow_error(msg);
     throw std::runtime_error(msg);
 }
+
+// ObservablesLogger (src/observables/observable.cpp:61-116): the header and
+// the rows of simulation.out, with the columns the reference's observables
+// declare (energy.cpp:11-19, classical.cpp:11-19, bosonic.cpp:9-12,
+// gsf_action.cpp:10-13) in their output units; the file is appended to.
+class ObservablesLogger {
+public:
+    ObservablesLogger(const pimdb_config& c, const RunParams& run, const std::string& path) {
+        using O = pimdb_observables;
+        auto energy = [](const std::string& u) {
+            return [u](double v) { return u == "none" ? v : Units::convertToUser("energy", u, v); };
+        };
+        auto plain = [](double v) { return v; };
+        auto add = [&](const char* key, double O::*m, std::function<double(double)> conv) {
+            cols_.push_back({key, m, conv});
+        };
+        if (run.obs_energy != "off") {
+            const auto e = energy(run.obs_energy);
+            const bool ext_free = c.ext_kind == PIMDB_POT_FREE, int_free = c.int_kind == PIMDB_POT_FREE;
+            add("kinetic", &O::kinetic, e);
+            if (!(ext_free && int_free)) {
+                add("potential", &O::potential, e);
+                if (!ext_free && !int_free) {
+                    add("ext_pot", &O::ext_pot, e);
+                    add("int_pot", &O::int_pot, e);
+                }
+                add("virial", &O::virial, e);
+            }
+        }
+        if (run.obs_classical != "off") {
+            const auto e = energy(run.obs_classical);
+            add("temperature", &O::temperature, plain);
+            add("cl_kinetic", &O::cl_kinetic, e);
+            add("cl_spring", &O::cl_spring, e);
+        }
+        if (c.bosonic && run.obs_bosonic != "off") {
+            add("prob_dist", &O::prob_dist, plain);
+            add("prob_all", &O::prob_all, plain);
+        }
+        if (run.obs_gsf != "off") {
+            add("w_gsf", &O::w_gsf, plain);
+            add("pot_gsf", &O::pot_gsf, energy(run.obs_gsf));
+        }
+        if (cols_.empty()) return;
+        file_.open(path, std::ios::out | std::ios::app);
+        if (!file_.is_open()) throw std::runtime_error("Failed to open " + path + ".");
+        file_ << std::format("{:^16s}", "step");
+        for (const auto& col : cols_) file_ << std::format(" {:^16s}", col.key);
+        file_ << '\n';
+    }
+    bool enabled() const { return !cols_.empty(); }
+    void log(long step, const pimdb_observables& o) {
+        file_ << std::format("{:^16.8e}", static_cast<double>(step));
+        for (const auto& col : cols_) file_ << std::format(" {:^16.8e}", col.conv(o.*(col.member)));
+        file_ << '\n';
+    }
+
+private:
+    struct Column {
+        const char* key;
+        double pimdb_observables::*member;
+        std::function<double(double)> conv;
+    };
+    std::vector<Column> cols_;
+    std::ofstream file_;
+};
 
 }  // namespace pimdb_host
 
@@ -315,6 +386,41 @@ public:
         check(pimdb_get_state(engine->handle(), x.data(), p.data(), f.data()), engine->handle());
     }
     long getStep() const { return md_step; }
+    void observables(pimdb_observables& o) { check(pimdb_compute_observables(engine->handle(), &o), engine->handle()); }
+
+    // Simulation::run (src/simulation.cpp:236-280): steps+1 MD steps; from
+    // the thermalization threshold on, the observables of every sfreq-th
+    // step go to the logger.  The fused schedule runs the steps between two
+    // logged ones as one call.
+    void run(bool plugin, pimdb_host::ObservablesLogger* logger) {
+        const long steps = run_params.steps, sfreq = std::max(1L, run_params.sfreq);
+        const double threshold = run_params.threshold * steps;
+        long s = 0;
+        while (s <= steps) {
+            long next = -1;
+            if (logger && logger->enabled()) {
+                long t0 = std::max(s, (long)std::ceil(threshold));
+                long t = (t0 + sfreq - 1) / sfreq * sfreq;
+                if (t <= steps) next = t;
+            }
+            const long until = next >= 0 ? next : steps;
+            for (long left = until - s + 1; left > 0;) {
+                const int n = (int)std::min<long>(left, 1L << 30);
+                if (plugin) {
+                    for (int k = 0; k < n; ++k) plugin_step();
+                } else {
+                    fast_step(n);
+                }
+                left -= n;
+            }
+            if (next >= 0) {
+                pimdb_observables o{};
+                observables(o);
+                logger->log(next, o);
+            }
+            s = until + 1;
+        }
+    }
 
     pimdb_config cfg;
     pimdb_host::RunParams run_params;

@@ -1,6 +1,7 @@
 // pimdb_gb300: command-line driver in the shape of the reference's main
 // (src/pimdb.cpp:31-68): reads config.ini, builds the simulation with every
-// bead on one GPU and runs steps+1 MD steps (src/simulation.cpp:236).
+// bead on one GPU, runs steps+1 MD steps (src/simulation.cpp:236) and writes
+// the observables to output/simulation.out in the reference's format.
 //
 //   pimdb_gb300 [-in config.ini] [--dim N] [--check] [--plugin-steps]
 //               [--steps K] [--positions out.xyz]
@@ -18,6 +19,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <iostream>
 #include <fstream>
 #include <string>
@@ -57,12 +59,11 @@ int main(int argc, char** argv) {
             return 0;
         }
         pimdb_gb300::Simulation sim(params);
+        std::filesystem::create_directories("output");
+        pimdb_host::ObservablesLogger logger(params.config, params.run, "output/simulation.out");
         std::cout << "[*] Running the simulation\n";
         const auto t0 = std::chrono::steady_clock::now();
-        for (long s = 0; s <= params.run.steps; ++s) {
-            if (plugin) sim.plugin_step();
-            else sim.fast_step(1);
-        }
+        sim.run(plugin, &logger);
         const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         const double bs = (double)params.config.natoms * params.config.nbeads * (params.run.steps + 1) / wall;
         std::printf("[*] Simulation finished running successfully (Runtime = %.3g sec, %.4g bead-steps/s)\n", wall, bs);

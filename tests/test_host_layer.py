@@ -172,3 +172,28 @@ def test_cli_run_matches_oracle(plugin, propagator, nmthermostat, bosonic, tmp_p
         xi = O.philox_noise_device(cfg.seed, cfg.replica, st, P, N, 3)
         assert tr.step(xi) == 0
     assert rel_per_bead(got, tr.x) < 1e-9
+
+
+GOLDEN_CLI = Path(__file__).resolve().parent / "golden" / "cli"
+
+
+def _read_out(path):
+    lines = [ln for ln in Path(path).read_text().split("\n") if ln.strip()]
+    return lines[0].split(), np.array([list(map(float, ln.split())) for ln in lines[1:]])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(p.name for p in GOLDEN_CLI.iterdir()) if GOLDEN_CLI.exists() else [])
+def test_cli_simulation_out_matches_reference(name, tmp_path):
+    """The driver on a reference config.ini (NVE, random initial state as the
+    reference draws it) writes the reference's simulation.out: same columns,
+    same rows (tests/golden/make_cli_golden.py ran the compiled reference)."""
+    _need_cli()
+    shutil.copy(GOLDEN_CLI / name / "config.ini", tmp_path / "config.ini")
+    r = _cli(["-in", "config.ini"], tmp_path)
+    assert r.returncode == 0 and "[X]" not in r.stdout, r.stdout + r.stderr
+    cols, got = _read_out(tmp_path / "output" / "simulation.out")
+    want_cols, want = _read_out(GOLDEN_CLI / name / "simulation.out")
+    assert cols == want_cols
+    assert got.shape == want.shape
+    np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-300)

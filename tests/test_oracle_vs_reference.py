@@ -134,3 +134,42 @@ def test_fixture_replay_first_1000_steps(case, tmp_path):
     for j, c in enumerate(cols):
         k = gold_cols.index(c)
         assert np.allclose(got[:n, j], want[:n, k], rtol=1e-5), c
+
+
+OBS_CASES = [
+    # N, P, bosonic, pbc, interaction, external, box, T, cutoff, gsf
+    (8, 6, True, False, "harmonic", "harmonic", 10.0, "3.0 kelvin", "-1.0 angstrom", "off"),
+    (6, 4, True, False, "free", "harmonic", 10.0, "2.0 kelvin", "-1.0 angstrom", "atomic_unit"),
+    (7, 5, False, False, "free", "double_well", 10.0, "1.0 kelvin", "-1.0 angstrom", "atomic_unit"),
+    (20, 4, True, True, "aziz", "free", 9.0, "1.5 kelvin", "4 angstrom", "off"),
+]
+
+
+@pytest.mark.parametrize("case", OBS_CASES)
+def test_observables_match_reference_simulation_out(case, tmp_path):
+    """orc_observables on the state at the end of each step (the reference's
+    state dump at the start of the next step) against the reference's own
+    simulation.out row of that step (9 significant digits)."""
+    N, P, bos, pbc, inter, ext, box, T, cut, gsf = case
+    sec = _sections(N, P, bos, pbc, inter, ext, box, T, cut)
+    sec["simulation"].update(steps=5, sfreq=1, threshold=0.0)
+    sec["observables"] = {"energy": "atomic_unit", "classical": "atomic_unit", "bosonic": "atomic_unit", "gsf": gsf}
+    rng = np.random.default_rng(N + P)
+    if pbc:
+        side = np.linspace(-box / 2, box / 2, 4, endpoint=False) + box / 8
+        grid = np.array(np.meshgrid(side, side, side)).reshape(3, -1).T[:N]
+        x = grid[None] + rng.normal(0, 0.05, (P, N, 3))
+    else:
+        x = rng.uniform(-3, 3, (N, 3))[None] + rng.normal(0, 0.3, (P, N, 3))
+    v = rng.normal(0, 3.0, (P, N, 3))
+    res = R.run_trajectory(sec, x, v)
+    R.write_ini(tmp_path / "c.ini", sec)
+    s, _ = O.system_from_ini(tmp_path / "c.ini")
+    lines = res["simulation_out"].strip().split("\n")
+    cols = lines[0].split()
+    rows = np.array([list(map(float, ln.split())) for ln in lines[1:]])
+    assert len(rows) >= 5
+    for k in range(len(rows) - 1):
+        ob = O.observables(s, res["x"][k + 1], res["v"][k + 1] * s.mass)
+        for j, c in enumerate(cols[1:], start=1):
+            assert abs(ob[c] - rows[k, j]) <= 1e-7 * abs(rows[k, j]) + 1e-300, (k, c, ob[c], rows[k, j])
