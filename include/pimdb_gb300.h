@@ -46,7 +46,16 @@ enum pimdb_potential {
     PIMDB_POT_DIPOLE = 5       /* params: strength in Hartree bohr^3 (interaction only) */
 };
 enum pimdb_propagator { PIMDB_PROP_CARTESIAN = 0, PIMDB_PROP_NORMAL_MODES = 1 };
-enum pimdb_thermostat { PIMDB_THERMO_NONE = 0, PIMDB_THERMO_LANGEVIN = 1 };
+/* none, langevin, and the Nose-Hoover chains nose_hoover (one chain per
+ * bead), nose_hoover_np (per bead and particle), nose_hoover_np_dim (per
+ * degree of freedom) of src/thermostats/nose_hoover.cpp. */
+enum pimdb_thermostat {
+    PIMDB_THERMO_NONE = 0,
+    PIMDB_THERMO_LANGEVIN = 1,
+    PIMDB_THERMO_NOSE_HOOVER = 2,
+    PIMDB_THERMO_NOSE_HOOVER_NP = 3,
+    PIMDB_THERMO_NOSE_HOOVER_NP_DIM = 4
+};
 /* Arithmetic of the pair forces: FP64 throughout, or FP32 pair arithmetic
  * with FP64 per-atom accumulation.  Exchange and integrator are FP64 in both. */
 enum pimdb_precision { PIMDB_FP64 = 0, PIMDB_MIXED = 1 };
@@ -76,6 +85,7 @@ typedef struct pimdb_config {
     double cutoff;       /* interaction cutoff before min(cutoff, L/2) under PBC; < 0 = all pairs */
     unsigned long long seed;  /* Langevin noise key */
     unsigned int replica;     /* folded into the noise counter */
+    int nchains;              /* [simulation] nchains: Nose-Hoover chain length */
 } pimdb_config;
 
 typedef struct pimdb_handle pimdb_handle;
@@ -200,6 +210,7 @@ typedef struct pimdb_observables {
     double temperature, cl_kinetic, cl_spring;            /* classical */
     double prob_dist, prob_all;                           /* bosonic */
     double w_gsf, pot_gsf;                                /* gsf */
+    double nh_energy;  /* classical, Nose-Hoover: getAdditionToH summed over beads */
 } pimdb_observables;
 int pimdb_compute_observables(pimdb_handle* h, pimdb_observables* out);
 

@@ -51,13 +51,13 @@ class System(C.Structure):
         ("beta", C.c_double), ("thermo_beta", C.c_double), ("omega_p", C.c_double),
         ("spring_constant", C.c_double), ("beta_ex", C.c_double),
         ("ext_kind", C.c_int), ("ext_p", C.c_double * 3),
-        ("int_kind", C.c_int), ("int_p", C.c_double * 3), ("cutoff", C.c_double),
+        ("int_kind", C.c_int), ("int_p", C.c_double * 3), ("cutoff", C.c_double), ("nchains", C.c_int),
     ]
 
 
 class State(C.Structure):
     _fields_ = [("x", C.c_void_p), ("p", C.c_void_p), ("f", C.c_void_p), ("ext_f", C.c_void_p),
-                ("spring_f", C.c_void_p)]
+                ("spring_f", C.c_void_p), ("nh", C.c_void_p)]
 
 
 _lib = None
@@ -73,6 +73,10 @@ def lib():
         L.orc_system_init.argtypes = [S, C.c_double, C.c_double]
         L.orc_exchange.argtypes = [S, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_exchange.restype = C.c_int
+        L.orc_nh_chains.argtypes = [S]
+        L.orc_nh_chains.restype = C.c_long
+        L.orc_nh_energy.argtypes = [S, dp]
+        L.orc_nh_energy.restype = C.c_double
         L.orc_observables.argtypes = [S, dp, dp, dp]
         L.orc_observables.restype = C.c_int
         L.orc_potential_energy.argtypes = [S, dp, dp]
@@ -102,15 +106,20 @@ def _dp(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+THERMOSTATS = {"none": 0, "langevin": 1, "nose_hoover": 2, "nose_hoover_np": 3, "nose_hoover_np_dim": 4}
+
+
 def make_system(*, ndim, natoms, nbeads, temperature, mass, bosonic=False, pbc=False, size=1.0, fixcom=True,
                 propagator="cartesian", thermostat="langevin", nmthermostat=False, dt=1.0, gamma=-1.0,
-                ext="free", ext_p=(0.0, 0.0, 0.0), interaction="free", int_p=(0.0, 0.0, 0.0), cutoff=-1.0):
+                ext="free", ext_p=(0.0, 0.0, 0.0), interaction="free", int_p=(0.0, 0.0, 0.0), cutoff=-1.0,
+                nchains=4):
     """Builds the oracle's system record; all quantities in atomic units."""
     s = System()
     s.ndim, s.natoms, s.nbeads = ndim, natoms, nbeads
     s.bosonic, s.pbc, s.fixcom = int(bosonic), int(pbc), int(fixcom)
     s.propagator = 1 if propagator == "normal_modes" else 0
-    s.thermostat = 1 if thermostat == "langevin" else 0
+    s.thermostat = THERMOSTATS[thermostat]
+    s.nchains = nchains
     s.nmthermostat = int(nmthermostat)
     s.size, s.mass, s.dt = size, mass, dt
     s.gamma = gamma if gamma >= 0 else 1 / (100.0 * dt)  # params.cpp:17-20
@@ -185,8 +194,13 @@ class Trajectory:
         self.f = np.zeros(shp)
         self.ext_f = np.zeros(shp)
         self.spring_f = np.zeros(shp)
+        self.nh = np.zeros(max(1, 3 * lib().orc_nh_chains(C.byref(s)) * s.nchains))
         self._st = State(self.x.ctypes.data, self.p.ctypes.data, self.f.ctypes.data, self.ext_f.ctypes.data,
-                         self.spring_f.ctypes.data)
+                         self.spring_f.ctypes.data, self.nh.ctypes.data)
+
+    def nh_energy(self) -> float:
+        """Sum over beads of the Nose-Hoover chains' getAdditionToH."""
+        return lib().orc_nh_energy(C.byref(self.s), _dp(self.nh))
 
     def step(self, xi: np.ndarray, nthreads: int = 1) -> int:
         xi = np.ascontiguousarray(xi, dtype=np.float64)
@@ -324,6 +338,7 @@ def system_from_ini(path, **overrides):
               fixcom=getb("simulation", "fixcom", True), propagator=get("simulation", "propagator", "cartesian"),
               thermostat=get("simulation", "thermostat", "none"),
               nmthermostat=getb("simulation", "nmthermostat", False), dt=dt, gamma=gamma, ext=ename, ext_p=ext_p,
+              nchains=int(float(get("simulation", "nchains", "4"))),
               interaction=iname, int_p=int_p, cutoff=cutoff)
     kw.update(overrides)
     extras = dict(steps=int(float(get("simulation", "steps", "1e5"))), sfreq=int(get("simulation", "sfreq", "1000")),

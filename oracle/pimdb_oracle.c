@@ -762,9 +762,157 @@ static void orc_bead_transform(const orc_system* s, const double* M, const doubl
         }
 }
 
+/* ---- Nose-Hoover chains (src/thermostats/nose_hoover.cpp) ---- */
+long orc_nh_chains(const orc_system* s) {
+    const long P = s->nbeads, N = s->natoms, D = s->ndim;
+    switch (s->thermostat) {
+    case ORC_THERMO_NOSE_HOOVER: return P;
+    case ORC_THERMO_NOSE_HOOVER_NP: return P * N;
+    case ORC_THERMO_NOSE_HOOVER_NP_DIM: return P * N * D;
+    default: return 0;
+    }
+}
+
+typedef struct {
+    double Q1, Qi, required, dt2, dt4, dt8;
+    int nchains;
+} orc_nh_par;
+
+static orc_nh_par nh_par(const orc_system* s) {
+    /* constructors, nose_hoover.cpp:9-33, :149-158, :196-206 */
+    orc_nh_par q;
+    const int N = s->natoms, D = s->ndim;
+    q.nchains = s->nchains;
+    q.Qi = 1.0 * 1.0 * s->beta / s->nbeads;
+    if (s->thermostat == ORC_THERMO_NOSE_HOOVER) {
+        q.Q1 = D * N * q.Qi;
+        q.required = D * N / s->thermo_beta;
+    } else if (s->thermostat == ORC_THERMO_NOSE_HOOVER_NP) {
+        q.Q1 = D * q.Qi;
+        q.required = D / s->thermo_beta;
+    } else {
+        q.Q1 = q.Qi;
+        q.required = 1 / s->thermo_beta;
+    }
+    q.dt2 = 0.5 * s->dt;
+    q.dt4 = 0.25 * s->dt;
+    q.dt8 = 0.125 * s->dt;
+    return q;
+}
+
+/* singleChainStep (nose_hoover.cpp:98-144) on one chain; returns the scale */
+static double nh_chain_step(const orc_system* s, const orc_nh_par* q, double current_energy, double* eta,
+                            double* eta_dot, double* eta_dd) {
+    const int M = q->nchains;
+    double exp_factor = 0.0;
+    eta_dd[0] = (current_energy - q->required) / q->Q1;
+    eta_dot[M - 1] += eta_dd[M - 1] * q->dt4;
+    for (int i = M - 2; i >= 0; i--) {
+        exp_factor = exp(-q->dt8 * eta_dot[i + 1]);
+        eta_dot[i] *= exp_factor;
+        eta_dot[i] += eta_dd[i] * q->dt4;
+        eta_dot[i] *= exp_factor;
+    }
+    double scale = exp(-q->dt2 * eta_dot[0]);
+    for (int i = 0; i < M; i++) eta[i] += q->dt2 * eta_dot[i];
+    eta_dd[0] = (current_energy * scale * scale - q->required) / q->Q1;
+    eta_dot[0] *= exp_factor;
+    eta_dot[0] += eta_dd[0] * q->dt4;
+    eta_dot[0] *= exp_factor;
+    double Q_former = q->Q1;
+    for (int i = 1; i < M - 1; i++) {
+        exp_factor = exp(-q->dt8 * eta_dot[i + 1]);
+        eta_dot[i] *= exp_factor;
+        eta_dd[i] = (Q_former * eta_dot[i - 1] * eta_dot[i - 1] - 1 / s->thermo_beta) / q->Qi;
+        eta_dot[i] += eta_dd[i] * q->dt4;
+        eta_dot[i] *= exp_factor;
+        Q_former = q->Qi;
+    }
+    eta_dd[M - 1] = (q->Qi * eta_dot[M - 2] * eta_dot[M - 2] - 1 / s->thermo_beta) / q->Qi;
+    eta_dot[M - 1] += eta_dd[M - 1] * q->dt4;
+    return scale;
+}
+
+/* momentaUpdate of the three variants (nose_hoover.cpp:68-96, :160-184,
+ * :208-221) on every bead (or normal mode) of `p`. */
+static void orc_nose_hoover(const orc_system* s, double* p, double* nh) {
+    const int N = s->natoms, D = s->ndim, P = s->nbeads, M = s->nchains;
+    const orc_nh_par q = nh_par(s);
+    const long nch = orc_nh_chains(s);
+    double* eta = nh;
+    double* eta_dot = nh + nch * M;
+    double* eta_dd = nh + 2 * nch * M;
+    for (int b = 0; b < P; ++b) {
+        double* pb = p + (long)b * N * D;
+        if (s->thermostat == ORC_THERMO_NOSE_HOOVER) {
+            double e = 0.0;
+            for (int i = 0; i < N; ++i)
+                for (int a = 0; a < D; ++a) e += pb[i * D + a] * pb[i * D + a];
+            e /= s->mass;
+            const long c = (long)b * M;
+            const double scale = nh_chain_step(s, &q, e, eta + c, eta_dot + c, eta_dd + c);
+            for (int i = 0; i < N; ++i)
+                for (int a = 0; a < D; ++a) pb[i * D + a] = pb[i * D + a] * scale;
+        } else if (s->thermostat == ORC_THERMO_NOSE_HOOVER_NP) {
+            for (int i = 0; i < N; ++i) {
+                double e = 0.0;
+                for (int a = 0; a < D; ++a) e += pb[i * D + a] * pb[i * D + a];
+                e /= s->mass;
+                const long c = ((long)b * N + i) * M;
+                const double scale = nh_chain_step(s, &q, e, eta + c, eta_dot + c, eta_dd + c);
+                for (int a = 0; a < D; ++a) pb[i * D + a] = pb[i * D + a] * scale;
+            }
+        } else {
+            for (int i = 0; i < N; ++i)
+                for (int a = 0; a < D; ++a) {
+                    const double e = pb[i * D + a] * pb[i * D + a] / s->mass;
+                    const long c = (((long)b * N + i) * D + a) * M;
+                    const double scale = nh_chain_step(s, &q, e, eta + c, eta_dot + c, eta_dd + c);
+                    pb[i * D + a] = pb[i * D + a] * scale;
+                }
+        }
+    }
+}
+
+double orc_nh_energy(const orc_system* s, const double* nh) {
+    const long nch = orc_nh_chains(s);
+    if (!nch || !nh) return 0.0;
+    const int M = s->nchains;
+    const orc_nh_par q = nh_par(s);
+    const double* eta = nh;
+    const double* eta_dot = nh + nch * M;
+    const int ndof = s->thermostat == ORC_THERMO_NOSE_HOOVER ? s->ndim * s->natoms
+                     : s->thermostat == ORC_THERMO_NOSE_HOOVER_NP ? s->ndim : 1;
+    double total = 0.0;
+    for (long c = 0; c < nch; ++c) {
+        const double* e = eta + c * M;
+        const double* ed = eta_dot + c * M;
+        /* singleChainGetAdditionToH (nose_hoover.cpp:51-66) */
+        double h = 0.5 * q.Q1 * ed[0] * ed[0];
+        h += ndof * e[0] / s->thermo_beta;
+        for (int i = 1; i < M; i++) {
+            h += 0.5 * q.Qi * ed[i] * ed[i];
+            h += e[i] / s->thermo_beta;
+        }
+        total += h;
+    }
+    return total;
+}
+
 static void orc_thermostat_step(const orc_system* s, double* p, const double* xi, const double* c2nm,
-                                const double* nm2c, double* work) {
+                                const double* nm2c, double* work, double* nh) {
     /* thermostat.cpp:15-19 */
+    if (orc_nh_chains(s)) {
+        if (!s->nmthermostat) {
+            orc_nose_hoover(s, p, nh);
+            return;
+        }
+        /* NMCoupling (thermostat_coupling.cpp:29-47): chains per normal mode */
+        orc_bead_transform(s, c2nm, p, work);
+        orc_nose_hoover(s, work, nh);
+        orc_bead_transform(s, nm2c, work, p);
+        return;
+    }
     if (s->thermostat != ORC_THERMO_LANGEVIN) return;
     if (!s->nmthermostat) {
         orc_langevin(s, p, xi);
@@ -857,7 +1005,7 @@ int orc_md_step(const orc_system* s, orc_state* st, const double* xi, int nthrea
         orc_nm_matrices(s, c2nm, nm2c);
     }
     int rc = 0;
-    orc_thermostat_step(s, st->p, xi, c2nm, nm2c, w1);
+    orc_thermostat_step(s, st->p, xi, c2nm, nm2c, w1, st->nh);
     if (s->fixcom) orc_zero_momentum(s, st->p);
     if (s->propagator == ORC_PROP_NORMAL_MODES) {
         rc = orc_nm_propagate(s, st, c2nm, nm2c, w1, w2, nthreads);
@@ -867,7 +1015,7 @@ int orc_md_step(const orc_system* s, orc_state* st, const double* xi, int nthrea
         rc = orc_update_forces(s, st->x, st->f, NULL, NULL, nthreads);
         orc_momentum_step(s, st->p, st->f);
     }
-    orc_thermostat_step(s, st->p, xi + n, c2nm, nm2c, w1);
+    orc_thermostat_step(s, st->p, xi + n, c2nm, nm2c, w1, st->nh);
     if (s->fixcom) orc_zero_momentum(s, st->p);
     free(w1);
     free(w2);

@@ -25,7 +25,8 @@ extern "C" {
 enum { ORC_EXT_FREE = 0, ORC_EXT_HARMONIC = 1, ORC_EXT_DOUBLE_WELL = 2, ORC_EXT_COSINE = 3 };
 enum { ORC_INT_FREE = 0, ORC_INT_HARMONIC = 1, ORC_INT_AZIZ = 2, ORC_INT_DIPOLE = 3 };
 enum { ORC_PROP_CARTESIAN = 0, ORC_PROP_NORMAL_MODES = 1 };
-enum { ORC_THERMO_NONE = 0, ORC_THERMO_LANGEVIN = 1 };
+enum { ORC_THERMO_NONE = 0, ORC_THERMO_LANGEVIN = 1, ORC_THERMO_NOSE_HOOVER = 2, ORC_THERMO_NOSE_HOOVER_NP = 3,
+       ORC_THERMO_NOSE_HOOVER_NP_DIM = 4 };
 
 typedef struct {
     int ndim;
@@ -51,6 +52,7 @@ typedef struct {
     int int_kind;
     double int_p[3];        /* harmonic: omega | dipole: strength */
     double cutoff;          /* effective cutoff (simulation.cpp:84-90): 0 = no pairs, <0 = all pairs */
+    int nchains;            /* Nose-Hoover chain length (params.cpp nchains) */
 } orc_system;
 
 /* Fills the derived constants of `s` from T (atomic units), P, mass, ... and
@@ -108,7 +110,16 @@ typedef struct {
     double* f;          /* [P][N][D] forces as stored by Simulation::forces */
     double* ext_f;      /* NM propagator: physical forces member (normal_modes_propagator.h:16) */
     double* spring_f;   /* NM propagator: spring forces member */
+    double* nh;         /* Nose-Hoover chains: eta, eta_dot, eta_dot_dot, each [nh_chains(s)][nchains] */
 } orc_state;
+
+/* Number of Nose-Hoover chains of the whole ring polymer: one per bead
+ * (nose_hoover), per bead and particle (_np) or per degree of freedom
+ * (_np_dim); 0 for the other thermostats. */
+long orc_nh_chains(const orc_system* s);
+/* Sum over beads of NoseHooverThermostat::getAdditionToH
+ * (nose_hoover.cpp:41-66, :186-192, :223-231). */
+double orc_nh_energy(const orc_system* s, const double* nh);
 
 /* Applies one full MD step of Simulation::run (simulation.cpp:236-260):
  * O, [COM], propagator, O, [COM].  xi holds the Gaussian noise of both

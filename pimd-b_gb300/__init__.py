@@ -20,7 +20,7 @@ LIB_PATH = HERE / "libpimdb_gb300.so"
 OK, ERR_CONFIG, ERR_NONFINITE_VB, ERR_CUDA, ERR_TIMEOUT, ERR_BOUNDS, ERR_ARG, ERR_NO_DEVICE, ERR_PARSE = range(9)
 POT = {"free": 0, "harmonic": 1, "double_well": 2, "cosine": 3, "aziz": 4, "dipole": 5}
 PROP = {"cartesian": 0, "normal_modes": 1}
-THERMO = {"none": 0, "langevin": 1}
+THERMO = {"none": 0, "langevin": 1, "nose_hoover": 2, "nose_hoover_np": 3, "nose_hoover_np_dim": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 
 EXPORTS = [
@@ -35,7 +35,7 @@ EXPORTS = [
     "pimdb_batch_set_option", "pimdb_batch_get_launch", "pimdb_batch_autotune", "pimdb_batch_last_error",
 ]
 OBSERVABLES = ["kinetic", "potential", "ext_pot", "int_pot", "virial", "temperature", "cl_kinetic", "cl_spring",
-               "prob_dist", "prob_all", "w_gsf", "pot_gsf"]
+               "prob_dist", "prob_all", "w_gsf", "pot_gsf", "nh_energy"]
 KERNEL_CLASSES = ["bead_forces", "exch_energies", "exch_recursions", "exch_forces", "exch_estimators",
                   "cart_update", "nm_propagate", "nm_thermo"]
 
@@ -48,7 +48,7 @@ class Config(C.Structure):
         ("precision", C.c_int), ("temperature", C.c_double), ("mass", C.c_double), ("size", C.c_double),
         ("dt", C.c_double), ("gamma", C.c_double), ("ext_kind", C.c_int), ("ext_params", C.c_double * 3),
         ("int_kind", C.c_int), ("int_params", C.c_double * 3), ("cutoff", C.c_double),
-        ("seed", C.c_ulonglong), ("replica", C.c_uint),
+        ("seed", C.c_ulonglong), ("replica", C.c_uint), ("nchains", C.c_int),
     ]
 
 

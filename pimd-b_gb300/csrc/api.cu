@@ -59,6 +59,12 @@ struct pimdb_handle {
     // buffer, and the option (-1 automatic: on when nc >= 4 and N >= 512)
     int cell_nc = 0;
     void* d_cells = nullptr;
+    // Nose-Hoover chains: parameters and state (eta, eta_dot, eta_dot_dot),
+    // and the normal-mode momenta buffer of the normal-mode coupling
+    NHPar nh{};
+    long long nh_chains = 0;
+    double* d_nh = nullptr;
+    double* d_pnm = nullptr;
     int opt_cells = -1;
     // CUDA graphs of pimdb_step_async: keyed by the step count and the
     // host-side step state at entry; the step index comes from d_step, which
@@ -179,6 +185,7 @@ extern "C" int pimdb_config_default(pimdb_config* c) {
     c->cutoff = -1.0 * 1.8897261;              // -1 angstrom
     c->seed = 1234;
     c->thermostat = PIMDB_THERMO_LANGEVIN;
+    c->nchains = 4;
     return PIMDB_OK;
 }
 
@@ -192,8 +199,10 @@ std::string validate_config(const pimdb_config& c) {
     if (!(c.dt > 0.0)) return "dt must be positive";
     if (c.propagator != PIMDB_PROP_CARTESIAN && c.propagator != PIMDB_PROP_NORMAL_MODES)
         return "The specified time propagator is not supported!";
-    if (c.thermostat != PIMDB_THERMO_NONE && c.thermostat != PIMDB_THERMO_LANGEVIN)
+    if (c.thermostat < PIMDB_THERMO_NONE || c.thermostat > PIMDB_THERMO_NOSE_HOOVER_NP_DIM)
         return "The specified thermostat is not supported!";
+    if (c.thermostat >= PIMDB_THERMO_NOSE_HOOVER && c.nchains < 1)
+        return "The specified number of Nose-Hoover chains (" + std::to_string(c.nchains) + ") is less than one!";
     if (c.nmthermostat && c.thermostat == PIMDB_THERMO_NONE) return "nmthermostat cannot be used in nve ensemble!";
     if (c.ext_kind != PIMDB_POT_FREE && c.ext_kind != PIMDB_POT_HARMONIC && c.ext_kind != PIMDB_POT_DOUBLE_WELL &&
         c.ext_kind != PIMDB_POT_COSINE)
@@ -304,6 +313,8 @@ static void free_handle(pimdb_handle* h) {
     if (h->d_bar) cudaFree(h->d_bar);
     if (h->d_tw) cudaFree(h->d_tw);
     if (h->d_cells) cudaFree(h->d_cells);
+    if (h->d_nh) cudaFree(h->d_nh);
+    if (h->d_pnm) cudaFree(h->d_pnm);
     if (h->d_step) cudaFree(h->d_step);
     drop_graphs(h);
     if (h->fork_ev) cudaEventDestroy(h->fork_ev);
@@ -400,6 +411,28 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
         if (e == cudaSuccess) e = cudaMemcpy(h->d_T, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
             e = cudaMemcpy(h->d_rot, rot.data(), rot.size() * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess && c.thermostat >= PIMDB_THERMO_NOSE_HOOVER) {
+        // constructors of nose_hoover.cpp:9-33, :149-158, :196-206
+        const int D = h->D, N = s.N, P = s.P;
+        NHPar& q = h->nh;
+        q.variant = c.thermostat - PIMDB_THERMO_NOSE_HOOVER;
+        q.nchains = c.nchains;
+        const double beta = 1.0 / (1.0 * c.temperature);
+        q.thermo_beta = beta / P;
+        q.Qi = 1.0 * 1.0 * beta / P;
+        q.Q1 = q.variant == 0 ? D * N * q.Qi : (q.variant == 1 ? D * q.Qi : q.Qi);
+        q.required = q.variant == 0 ? D * N / q.thermo_beta : (q.variant == 1 ? D / q.thermo_beta : 1 / q.thermo_beta);
+        q.dt2 = 0.5 * c.dt;
+        q.dt4 = 0.25 * c.dt;
+        q.dt8 = 0.125 * c.dt;
+        h->nh_chains = q.variant == 0 ? P : (q.variant == 1 ? (long long)P * N : (long long)P * N * D);
+        const size_t m = (size_t)h->nh_chains * q.nchains;
+        e = alloc(&h->d_nh, 3 * m);
+        q.eta = h->d_nh;
+        q.eta_dot = h->d_nh + m;
+        q.eta_dd = h->d_nh + 2 * m;
+        if (e == cudaSuccess && c.nmthermostat) e = alloc(&h->d_pnm, (size_t)P * D * s.ld);
     }
     if (e == cudaSuccess && c.propagator == PIMDB_PROP_NORMAL_MODES && c.nmthermostat &&
         c.thermostat == PIMDB_THERMO_LANGEVIN && nm_fused_fits(s, h->D)) {
@@ -612,10 +645,23 @@ static void nm_thermo(pimdb_handle* h, int flags, int substep) {
 
 // Applies the O-step of the configured thermostat (thermostat.cpp:15-19)
 // followed, when fixcom, by the partial sums for the COM removal.
+static void nose_hoover(pimdb_handle* h) {
+    const bool nmc = h->cfg.nmthermostat != 0;
+    launch(h, PIMDB_K_NM_THERMO, [&] {
+        launch_nose_hoover(h->s, h->D, h->nh, nmc ? h->d_C : nullptr, nmc ? h->d_T : nullptr, h->d_pnm, h->stream);
+    }, nmc ? 3 : 1);
+}
+
 static void thermostat_step(pimdb_handle* h, int substep) {
     const pimdb_config& c = h->cfg;
     const int part = c.fixcom ? SF_COM_PARTIAL : 0;
-    if (c.thermostat == PIMDB_THERMO_LANGEVIN && c.nmthermostat) {
+    if (c.thermostat >= PIMDB_THERMO_NOSE_HOOVER) {
+        // the pending COM correction first, then the chains; partial sums
+        // for the COM removal that follows (simulation.cpp:246-258)
+        if (h->com_pending) cart(h, SF_COM_APPLY, substep, 0);
+        nose_hoover(h);
+        if (c.fixcom) cart(h, SF_COM_PARTIAL, substep, 0);
+    } else if (c.thermostat == PIMDB_THERMO_LANGEVIN && c.nmthermostat) {
         nm_thermo(h, SF_COM_APPLY | part, substep);
     } else if (c.thermostat == PIMDB_THERMO_LANGEVIN) {
         cart(h, SF_COM_APPLY | SF_LANGEVIN | part, substep, 0);
@@ -902,6 +948,25 @@ extern "C" int pimdb_compute_observables(pimdb_handle* h, pimdb_observables* out
         o.w_gsf += ((b % 2 != 0) ? -pot_term : pot_term + f2_term) * (-beta);
         if (b % 2 != 0) o.pot_gsf += (t[2] + t[4]) / (0.5 * P);
     }
+    if (h->d_nh) {
+        // singleChainGetAdditionToH (nose_hoover.cpp:51-66) of every chain
+        const NHPar& q = h->nh;
+        const size_t m = (size_t)h->nh_chains * q.nchains;
+        std::vector<double> eta(2 * m);
+        CUDA_TRY(h, cudaMemcpy(eta.data(), h->d_nh, 2 * m * sizeof(double), cudaMemcpyDeviceToHost));
+        const int ndof = q.variant == 0 ? D * N : (q.variant == 1 ? D : 1);
+        for (long long ch = 0; ch < h->nh_chains; ++ch) {
+            const double* et = &eta[(size_t)ch * q.nchains];
+            const double* ed = &eta[m + (size_t)ch * q.nchains];
+            double add = 0.5 * q.Q1 * ed[0] * ed[0];
+            add += ndof * et[0] / q.thermo_beta;
+            for (int i = 1; i < q.nchains; i++) {
+                add += 0.5 * q.Qi * ed[i] * ed[i];
+                add += et[i] / q.thermo_beta;
+            }
+            o.nh_energy += add;
+        }
+    }
     *out = o;
     return PIMDB_OK;
 }
@@ -1026,7 +1091,8 @@ extern "C" int pimdb_thermostat_step(pimdb_handle* h, int substep) {
     if (!h || substep < 0 || substep > 1) return PIMDB_ERR_ARG;
     const pimdb_config& c = h->cfg;
     complete_pending(h);  // finish the previous step's deferred work first
-    if (c.thermostat == PIMDB_THERMO_LANGEVIN && c.nmthermostat) nm_thermo(h, 0, substep);
+    if (c.thermostat >= PIMDB_THERMO_NOSE_HOOVER) nose_hoover(h);
+    else if (c.thermostat == PIMDB_THERMO_LANGEVIN && c.nmthermostat) nm_thermo(h, 0, substep);
     else if (c.thermostat == PIMDB_THERMO_LANGEVIN) cart(h, SF_LANGEVIN, substep, 0);
     CUDA_TRY(h, cudaGetLastError());
     return PIMDB_OK;

@@ -521,7 +521,7 @@ extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void*
         if (c.ndim != D) return bfail(nullptr, PIMDB_ERR_CONFIG, "every replica of a batch must have the same ndim");
         if (c.precision != precision)
             return bfail(nullptr, PIMDB_ERR_CONFIG, "every replica of a batch must have the same precision");
-        if (c.propagator != PIMDB_PROP_CARTESIAN || c.nmthermostat)
+        if (c.propagator != PIMDB_PROP_CARTESIAN || c.nmthermostat || c.thermostat >= PIMDB_THERMO_NOSE_HOOVER)
             return bfail(nullptr, PIMDB_ERR_CONFIG,
                          "replica " + std::to_string(r) +
                              ": the batched engine runs the cartesian propagator with the cartesian Langevin thermostat");

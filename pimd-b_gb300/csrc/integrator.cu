@@ -660,6 +660,144 @@ cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* 
     return nm_fused_t<3>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
 }
 
+// ---------------------------------------------------------------------------
+// Nose-Hoover chains (src/thermostats/nose_hoover.cpp): one chain per bead
+// over all its degrees of freedom (variant 0), per bead and particle (1), or
+// per degree of freedom (2); with the normal-mode coupling the "beads" are
+// the normal modes of momenta transformed by k_bead_transform.  Every chain
+// integrates singleChainStep (:98-144, Tuckerman et al. 2006) in the
+// reference's operation order and rescales its momenta.
+
+// singleChainStep on one chain; returns the momentum scale
+__device__ __forceinline__ double nh_chain_step(const NHPar& q, double current_energy, double* eta, double* eta_dot,
+                                                double* eta_dd) {
+    const int M = q.nchains;
+    double exp_factor = 0.0;
+    eta_dd[0] = (current_energy - q.required) / q.Q1;
+    eta_dot[M - 1] += eta_dd[M - 1] * q.dt4;
+    for (int i = M - 2; i >= 0; i--) {
+        exp_factor = exp(-q.dt8 * eta_dot[i + 1]);
+        eta_dot[i] *= exp_factor;
+        eta_dot[i] += eta_dd[i] * q.dt4;
+        eta_dot[i] *= exp_factor;
+    }
+    const double scale = exp(-q.dt2 * eta_dot[0]);
+    for (int i = 0; i < M; i++) eta[i] += q.dt2 * eta_dot[i];
+    eta_dd[0] = (current_energy * scale * scale - q.required) / q.Q1;
+    eta_dot[0] *= exp_factor;
+    eta_dot[0] += eta_dd[0] * q.dt4;
+    eta_dot[0] *= exp_factor;
+    double Q_former = q.Q1;
+    for (int i = 1; i < M - 1; i++) {
+        exp_factor = exp(-q.dt8 * eta_dot[i + 1]);
+        eta_dot[i] *= exp_factor;
+        eta_dd[i] = (Q_former * eta_dot[i - 1] * eta_dot[i - 1] - 1 / q.thermo_beta) / q.Qi;
+        eta_dot[i] += eta_dd[i] * q.dt4;
+        eta_dot[i] *= exp_factor;
+        Q_former = q.Qi;
+    }
+    eta_dd[M - 1] = (q.Qi * eta_dot[M - 2] * eta_dot[M - 2] - 1 / q.thermo_beta) / q.Qi;
+    eta_dot[M - 1] += eta_dd[M - 1] * q.dt4;
+    return scale;
+}
+
+template <int D>
+__global__ void k_nose_hoover(Sys s, NHPar q, double* __restrict__ pa) {
+    const int M = q.nchains;
+    if (q.variant == 0) {  // one chain per bead: block b
+        __shared__ double red[32];
+        __shared__ double sscale;
+        const int b = blockIdx.x;
+        double e = 0.0;
+        for (int t = threadIdx.x; t < D * s.N; t += blockDim.x) {
+            const int a = t / s.N, i = t - a * s.N;
+            const double pv = pa[idx<D>(s, b, a, i)];
+            e += pv * pv;
+        }
+        e = block_sum(e, red);
+        if (threadIdx.x == 0) {
+            const size_t c = (size_t)b * M;
+            sscale = nh_chain_step(q, e / s.mass, q.eta + c, q.eta_dot + c, q.eta_dd + c);
+        }
+        __syncthreads();
+        const double scale = sscale;
+        for (int t = threadIdx.x; t < D * s.N; t += blockDim.x) {
+            const int a = t / s.N, i = t - a * s.N;
+            const size_t o = idx<D>(s, b, a, i);
+            pa[o] = pa[o] * scale;
+        }
+        return;
+    }
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q.variant == 1) {  // one chain per bead and particle
+        if (t >= (size_t)s.P * s.N) return;
+        const int b = (int)(t / s.N), i = (int)(t % s.N);
+        double e = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            const double pv = pa[idx<D>(s, b, a, i)];
+            e += pv * pv;
+        }
+        const size_t c = t * M;
+        const double scale = nh_chain_step(q, e / s.mass, q.eta + c, q.eta_dot + c, q.eta_dd + c);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            const size_t o = idx<D>(s, b, a, i);
+            pa[o] = pa[o] * scale;
+        }
+        return;
+    }
+    // one chain per degree of freedom, chain ((b N + i) D + a)
+    if (t >= (size_t)s.P * s.N * D) return;
+    const int a = (int)(t % D);
+    const size_t bi = t / D;
+    const int b = (int)(bi / s.N), i = (int)(bi % s.N);
+    const size_t o = idx<D>(s, b, a, i);
+    const double pv = pa[o];
+    const size_t c = t * M;
+    const double scale = nh_chain_step(q, pv * pv / s.mass, q.eta + c, q.eta_dot + c, q.eta_dd + c);
+    pa[o] = pv * scale;
+}
+
+// out[k][a][i] = sum_j M[k][j] in[j][a][i] (bead <-> normal-mode rows, j
+// ascending as in normal_modes.cpp:86-139)
+template <int D>
+__global__ void k_bead_transform(Sys s, const double* __restrict__ Mx, const double* __restrict__ in,
+                                 double* __restrict__ out) {
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)s.P * D * s.N) return;
+    const int i = (int)(t % s.N);
+    const size_t ka = t / s.N;
+    const int a = (int)(ka % D), k = (int)(ka / D);
+    double acc = 0.0;
+    for (int j = 0; j < s.P; ++j) acc += Mx[(size_t)k * s.P + j] * in[idx<D>(s, j, a, i)];
+    out[idx<D>(s, k, a, i)] = acc;
+}
+
+template <int D>
+static void nose_hoover_t(const Sys& s, const NHPar& q, const double* C, const double* T, double* pnm,
+                          cudaStream_t st) {
+    const size_t ne = (size_t)s.P * D * s.N;
+    const unsigned gt = (unsigned)((ne + 255) / 256);
+    double* target = s.p;
+    if (C) {
+        k_bead_transform<D><<<gt, 256, 0, st>>>(s, C, s.p, pnm);
+        target = pnm;
+    }
+    if (q.variant == 0) k_nose_hoover<D><<<s.P, 256, 0, st>>>(s, q, target);
+    else if (q.variant == 1) k_nose_hoover<D><<<(unsigned)(((size_t)s.P * s.N + 255) / 256), 256, 0, st>>>(s, q, target);
+    else k_nose_hoover<D><<<gt, 256, 0, st>>>(s, q, target);
+    if (C) k_bead_transform<D><<<gt, 256, 0, st>>>(s, T, pnm, s.p);
+}
+
+int launch_nose_hoover(const Sys& s, int D, const NHPar& q, const double* C, const double* T, double* pnm,
+                       cudaStream_t st) {
+    if (D == 1) nose_hoover_t<1>(s, q, C, T, pnm, st);
+    else if (D == 2) nose_hoover_t<2>(s, q, C, T, pnm, st);
+    else nose_hoover_t<3>(s, q, C, T, pnm, st);
+    return C ? 3 : 1;
+}
+
 // ------------------------------------------------------------------ launchers
 static int pack_grid(size_t n) {
     size_t g = (n + 255) / 256;

@@ -56,6 +56,23 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st);
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st);
 void launch_exchange_estimators(const Sys& s, cudaStream_t st);
 
+// Nose-Hoover chains: parameters of one thermostat (constructors of
+// src/thermostats/nose_hoover.cpp) and its chain state, [chains][nchains]
+// each.  variant 0: a chain per bead, 1: per bead and particle, 2: per
+// degree of freedom.
+struct NHPar {
+    int variant, nchains;
+    double Q1, Qi, required, thermo_beta, dt2, dt4, dt8;
+    double* eta;
+    double* eta_dot;
+    double* eta_dd;
+};
+// One thermostat step on s.p; with C (cart -> NM rows) and T (NM -> cart)
+// the chains act on the normal-mode momenta, staged in pnm ([P][D][ld]).
+// Returns the number of kernels launched.
+int launch_nose_hoover(const Sys& s, int D, const NHPar& q, const double* C, const double* T, double* pnm,
+                       cudaStream_t st);
+
 // integrator.cu
 void launch_pack(const Sys& s, int D, const double* src, double* dst, cudaStream_t st);
 void launch_unpack(const Sys& s, int D, const double* src, double* dst, cudaStream_t st);

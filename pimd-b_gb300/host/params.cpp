@@ -213,9 +213,12 @@ static void read_config(const IniFile& r, int ndim, pimdb_config& c, RunParams& 
     if (thermostat != "langevin" && thermostat != "nose_hoover" && thermostat != "nose_hoover_np" &&
         thermostat != "nose_hoover_np_dim" && thermostat != "none")
         throw invalid_argument("The specified thermostat (" + propagator + ") is not supported!");
-    if (thermostat != "langevin" && thermostat != "none")
-        throw invalid_argument("The thermostat (" + thermostat + ") is not part of the GPU hot path");
-    c.thermostat = thermostat == "langevin" ? PIMDB_THERMO_LANGEVIN : PIMDB_THERMO_NONE;
+    c.thermostat = thermostat == "langevin"             ? PIMDB_THERMO_LANGEVIN
+                   : thermostat == "nose_hoover"        ? PIMDB_THERMO_NOSE_HOOVER
+                   : thermostat == "nose_hoover_np"     ? PIMDB_THERMO_NOSE_HOOVER_NP
+                   : thermostat == "nose_hoover_np_dim" ? PIMDB_THERMO_NOSE_HOOVER_NP_DIM
+                                                        : PIMDB_THERMO_NONE;
+    c.nchains = nchains;
 
     c.temperature = get_quantity("temperature", r.Get(SYS, "temperature", "1.0 kelvin"));
     if (c.temperature <= 0.0)

@@ -166,6 +166,7 @@ public:
             add("temperature", &O::temperature, plain);
             add("cl_kinetic", &O::cl_kinetic, e);
             add("cl_spring", &O::cl_spring, e);
+            if (c.thermostat >= PIMDB_THERMO_NOSE_HOOVER) add("nh_energy", &O::nh_energy, e);
         }
         if (c.bosonic && run.obs_bosonic != "off") {
             add("prob_dist", &O::prob_dist, plain);
@@ -346,6 +347,25 @@ class LangevinThermostat final : public Thermostat {
 public:
     using Thermostat::Thermostat;
 };
+// Nose-Hoover chains (nose_hoover.cpp): the chain state lives on the GPU;
+// getAdditionToH is the nh_energy the observables report.
+class NoseHooverThermostat : public Thermostat {
+public:
+    using Thermostat::Thermostat;
+    double getAdditionToH() override {
+        pimdb_observables o{};
+        check(pimdb_compute_observables(e_.handle(), &o), e_.handle());
+        return o.nh_energy;
+    }
+};
+class NoseHooverNpThermostat final : public NoseHooverThermostat {
+public:
+    using NoseHooverThermostat::NoseHooverThermostat;
+};
+class NoseHooverNpDimThermostat final : public NoseHooverThermostat {
+public:
+    using NoseHooverThermostat::NoseHooverThermostat;
+};
 
 // ----------------------------------------------------------------- simulation
 // Simulation::Simulation / run (src/simulation.cpp:16-101, :236-260) for all
@@ -357,7 +377,15 @@ public:
         if (cfg.bosonic && cfg.nbeads > 1) bosonic_exchange = std::make_unique<BosonicExchange>(*engine);
         if (cfg.propagator == PIMDB_PROP_NORMAL_MODES) propagator = std::make_unique<NormalModesPropagator>(*engine);
         else propagator = std::make_unique<VelocityVerletPropagator>(*engine);
-        if (cfg.thermostat == PIMDB_THERMO_LANGEVIN) thermostat = std::make_unique<LangevinThermostat>(*engine, cfg.nmthermostat);
+        // Simulation::initializeThermostat (src/simulation.cpp:667-684)
+        if (cfg.thermostat == PIMDB_THERMO_LANGEVIN)
+            thermostat = std::make_unique<LangevinThermostat>(*engine, cfg.nmthermostat);
+        else if (cfg.thermostat == PIMDB_THERMO_NOSE_HOOVER)
+            thermostat = std::make_unique<NoseHooverThermostat>(*engine, cfg.nmthermostat);
+        else if (cfg.thermostat == PIMDB_THERMO_NOSE_HOOVER_NP)
+            thermostat = std::make_unique<NoseHooverNpThermostat>(*engine, cfg.nmthermostat);
+        else if (cfg.thermostat == PIMDB_THERMO_NOSE_HOOVER_NP_DIM)
+            thermostat = std::make_unique<NoseHooverNpDimThermostat>(*engine, cfg.nmthermostat);
         else thermostat = std::make_unique<Thermostat>(*engine, cfg.nmthermostat);
         initialize_state();
     }

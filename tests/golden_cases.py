@@ -8,6 +8,7 @@ import numpy as np
 GOLDEN = Path(__file__).resolve().parent / "golden" / "cases.npz"
 ANGSTROM = 1.8897261        # include/units.h:95
 EV_PER_ANG = 0.019446904    # include/units.h:146
+KELVIN = 3.1668152e-06      # include/units.h:64 (energy and temperature)
 
 
 def load():

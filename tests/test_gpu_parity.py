@@ -351,3 +351,39 @@ def test_cuda_graph_steps_equal_plain_launches(name):
             out.append(g.get_state())
     for u, v in zip(*out):
         assert np.array_equal(u, v)
+
+
+NH_TRAJ = {
+    "nh_bosons_trap": dict(natoms=8, nbeads=4, thermostat="nose_hoover", fixcom=False, ext="harmonic",
+                           ext_p=(3.0 * 0.036749326e-3, 0, 0), dt_fs=0.5),
+    "nh_np_bosons_pairharm_fixcom": dict(natoms=10, nbeads=6, thermostat="nose_hoover_np", ext="harmonic",
+                                         ext_p=(3.0 * 0.036749326e-3, 0, 0), inter="harmonic",
+                                         int_p=(1.0 * 0.036749326e-3, 0, 0), dt_fs=0.5),
+    "nh_np_dim_dist_2d": dict(ndim=2, natoms=12, nbeads=5, bosonic=False, thermostat="nose_hoover_np_dim",
+                              ext="harmonic", ext_p=(1.0 * 0.036749326e-3, 0, 0), dt_fs=0.5),
+    "nh_nmcoupling_bosons": dict(natoms=8, nbeads=8, thermostat="nose_hoover", nmthermostat=True, fixcom=False,
+                                 ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0), dt_fs=0.5),
+    "nh_np_nm_propagator_dist": dict(natoms=9, nbeads=4, bosonic=False, propagator="normal_modes",
+                                     thermostat="nose_hoover_np", nmthermostat=True, ext="harmonic",
+                                     ext_p=(3.0 * 0.036749326e-3, 0, 0), dt_fs=0.5),
+}
+
+
+@pytest.mark.parametrize("name", sorted(NH_TRAJ))
+def test_nose_hoover_trajectory_matches_oracle(name):
+    kw = NH_TRAJ[name]
+    s, cfg = case(**kw)
+    x = ring(s, seed=13, spread_ang=0.2)
+    p = momenta(s, 13)
+    tr = O.Trajectory(s, x, p)
+    noise = np.zeros((2,) + x.shape)
+    with pk.System(cfg) as g:
+        g.set_state(x, p)
+        for st in range(12):
+            assert tr.step(noise) == 0
+            g.step(1)
+            gx, gp, gf = g.get_state()
+            for got, want, label in ((gx, tr.x, "x"), (gp, tr.p, "p"), (gf, tr.f, "f")):
+                assert rel_per_bead(got, want) < 1e-9, (st, label, rel_per_bead(got, want))
+        ob = g.observables()
+    assert abs(ob["nh_energy"] - tr.nh_energy()) <= 1e-9 * abs(tr.nh_energy())

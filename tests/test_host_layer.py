@@ -69,7 +69,7 @@ def test_cli_check_reports_configuration(tmp_path):
     assert "natoms=6 nbeads=4 ndim=3 bosonic=1 propagator=0 thermostat=1 steps=17" in r.stdout
 
 
-@pytest.mark.parametrize("key,value,message", [("thermostat", "nose_hoover", "not part of the GPU hot path"),
+@pytest.mark.parametrize("key,value,message", [("thermostat", "berendsen", "is not supported"),
                                                ("propagator", "normal_modes", "not available for bosons")])
 def test_cli_configuration_error_is_reported_like_the_reference(key, value, message, tmp_path):
     _need_cli()
@@ -197,3 +197,24 @@ def test_cli_simulation_out_matches_reference(name, tmp_path):
     assert cols == want_cols
     assert got.shape == want.shape
     np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-300)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["bosonic_quadratic_harmonic_nh_dynamics", "bosonic_quadratic_harmonic_nh_np_dynamics",
+                                  "bosonic_quadratic_harmonic_nh_np_dim_dynamics"])
+def test_cli_replays_nose_hoover_regression_cases(case, tmp_path):
+    """The reference's own Nose-Hoover regression cases (deterministic), run
+    from their config.ini for 5000 steps: the driver's simulation.out rows
+    against the reference's golden rows (energy, classical with nh_energy)."""
+    from tests import golden_cases as G
+    _need_cli()
+    z, index = G.load()
+    ini = index[case]["ini"].replace("steps = 100000", "steps = 5000")
+    (tmp_path / "config.ini").write_text(ini)
+    r = _cli(["-in", "config.ini"], tmp_path)
+    assert r.returncode == 0 and "[X]" not in r.stdout, r.stdout + r.stderr
+    cols, got = _read_out(tmp_path / "output" / "simulation.out")
+    assert cols == index[case]["columns"]
+    want = z[f"{case}/simulation_out"][:len(got)]
+    assert len(got) == 6
+    np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-9)

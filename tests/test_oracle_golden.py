@@ -70,3 +70,61 @@ def test_ranmars_rejects_reference_invalid_seeds():
         O.RanMars(900000001)
     g = O.RanMars(1234).gaussians(100000)
     assert abs(g.mean()) < 0.02 and abs(g.std() - 1) < 0.02
+
+
+NH_CASES = ["bosonic_quadratic_harmonic_nh_dynamics", "bosonic_quadratic_harmonic_nh_np_dynamics",
+            "bosonic_quadratic_harmonic_nh_np_dim_dynamics"]
+
+
+def nh_initial_state(case, tmp_path):
+    """The exact initial state of a regression case (initial_position and
+    initial_velocity = random): the driver's draw, which is the reference's
+    (tests/test_host_layer.py), or golden frame 0 when the driver is absent."""
+    import importlib
+    import subprocess
+    z, index = G.load()
+    s, _ = O.system_from_ini(G.write_ini(case, tmp_path))
+    cli = importlib.import_module("pimd-b_gb300.build").CLI
+    if cli.exists():
+        ini = G.write_ini(case, tmp_path)
+        r = subprocess.run([str(cli), "-in", str(ini), "--check", "--initial", str(tmp_path / "init.bin")],
+                           capture_output=True, text=True, timeout=60)
+        if r.returncode == 0 and (tmp_path / "init.bin").exists():
+            a = np.fromfile(tmp_path / "init.bin")
+            n = a.size // 2
+            shp = (s.nbeads, s.natoms, s.ndim)
+            return s, a[:n].reshape(shp), a[n:].reshape(shp)
+    x = z[f"{case}/positions_angstrom"][0] * G.ANGSTROM
+    v = z[f"{case}/velocities_angstrom_per_ps"][0] * 4.5710289e-5
+    return s, x, v * s.mass
+
+
+@pytest.mark.parametrize("case", NH_CASES)
+def test_nose_hoover_replays_golden_trajectory(case, tmp_path):
+    """Nose-Hoover chains are deterministic: the oracle replays the reference's
+    regression run from its initial state for 5000 steps and meets its
+    golden positions and simulation.out rows (energy, classical with nh_energy)."""
+    z, index = G.load()
+    s, x, p = nh_initial_state(case, tmp_path)
+    assert O.lib().orc_nh_chains(O.C.byref(s)) > 0
+    tr = O.Trajectory(s, x, p)
+    rows = z[f"{case}/simulation_out"]
+    cols = index[case]["columns"]
+    noise = np.zeros((2,) + x.shape)
+    X = z[f"{case}/positions_angstrom"]
+    frames = list(z[f"{case}/frames"])
+    checked = 0
+    for step in range(5001):
+        if step in (1000 * f for f in frames):
+            k = frames.index(step // 1000)
+            np.testing.assert_allclose(tr.x / G.ANGSTROM, X[k], rtol=1e-6, atol=1e-9 * np.abs(X[k]).max())
+            checked += 1
+        assert tr.step(noise) == 0
+        if step % 1000 == 0:
+            ob = O.observables(s, tr.x, tr.p)
+            ob["nh_energy"] = tr.nh_energy()
+            row = rows[list(rows[:, 0]).index(step)]
+            for j, c in enumerate(cols[1:], start=1):
+                val = ob[c] / G.KELVIN if c not in ("temperature",) else ob[c]
+                assert abs(val - row[j]) <= 1e-6 * abs(row[j]) + 1e-9, (step, c, val, row[j])
+    assert checked == 2
