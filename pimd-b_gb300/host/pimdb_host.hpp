@@ -15,12 +15,15 @@
 // std::runtime_error (CUDA).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <filesystem>
 #include <format>
 #include <fstream>
 #include <functional>
+#include <limits>
 #include <memory>
 #include <random>
 #include <stdexcept>
@@ -76,12 +79,69 @@ inline void grid_positions(const pimdb_config& cfg, double* pos) {
     }
 }
 
+// loadTrajectories / loadMomenta (src/common.cpp:49-136): an xyz file
+// (count, comment, "symbol x y z" in angstrom) or a LAMMPS-style velocity
+// file (count, comment, "id type vx vy vz" in angstrom/ps, times the mass).
+inline void load_xyz(const std::string& name, int N, int D, double* out) {
+    std::ifstream in(name);
+    if (!in.is_open()) throw std::runtime_error(std::format("Cannot open the xyz file named {}.", name));
+    int n = 0;
+    in >> n;
+    if (n != N)
+        throw std::runtime_error(
+            std::format("The number of atoms in the xyz file ({}) does not match the requested number of atoms.", name));
+    in.ignore(std::numeric_limits<std::streamsize>::max(), '\n');
+    std::string line;
+    std::getline(in, line, '\n');
+    for (int i = 0; i < N; ++i) {
+        std::string symbol;
+        in >> symbol;
+        for (int a = 0; a < D; ++a) {
+            in >> out[(size_t)i * D + a];
+            out[(size_t)i * D + a] = Units::convertToInternal("length", "angstrom", out[(size_t)i * D + a]);
+        }
+    }
+}
+
+inline void load_momenta(const std::string& name, double mass, int N, int D, double* out) {
+    std::ifstream in(name);
+    if (!in.is_open()) throw std::runtime_error(std::format("Cannot open the velocity file named {}.", name));
+    int n = 0;
+    in >> n;
+    if (n != N)
+        throw std::runtime_error(std::format(
+            "The number of atoms in the velocity file ({}) does not match the requested number of atoms.", name));
+    in.ignore(std::numeric_limits<std::streamsize>::max(), '\n');
+    std::string line;
+    std::getline(in, line, '\n');
+    for (int i = 0; i < N; ++i) {
+        std::string id, type;
+        in >> id >> type;
+        for (int a = 0; a < D; ++a) {
+            in >> out[(size_t)i * D + a];
+            out[(size_t)i * D + a] = mass * Units::convertToInternal("velocity", "angstrom/ps", out[(size_t)i * D + a]);
+        }
+    }
+}
+
+// A file-name specification with "{}" names one file per bead: the bead
+// index starts at 1 when the file for index 0 does not exist
+// (src/params.cpp:62-91, simulation.cpp:709-721).
+inline std::string formatted_bead_file(const std::string& spec, int bead) {
+    const int dummy = 0;
+    const std::string first = std::vformat(spec, std::make_format_args(dummy));
+    if (first == spec) return spec;  // not a format: the same file for every bead
+    const int arg = bead + (std::filesystem::exists(first) ? 0 : 1);
+    return std::vformat(spec, std::make_format_args(arg));
+}
+
 // Initial conditions as the reference draws them: bead b uses
 // std::mt19937(seed + b) (src/simulation.cpp:58); random positions uniform in
-// [-L/2, L/2] (:118-126) or the grid (:133-193); Maxwell-Boltzmann momenta
-// from a fresh std::normal_distribution per draw (:200-217).  With
-// zero_com, the centre-of-mass momentum is removed here the way
-// Simulation::zeroMomentum does it (:581-603, :750-751).
+// [-L/2, L/2] (:118-126), the grid (:133-193) or xyz files (:709-721);
+// Maxwell-Boltzmann momenta from a fresh std::normal_distribution per draw
+// (:200-217) or velocity files (:737-748).  With zero_com, random momenta
+// lose their centre-of-mass momentum the way Simulation::zeroMomentum does
+// it (:581-603, :750-751); loaded momenta are kept as they are.
 inline void initial_state(const pimdb_config& cfg, const RunParams& run, std::vector<double>& x0,
                           std::vector<double>& p0, bool zero_com = false) {
     const int P = cfg.nbeads, N = cfg.natoms, D = cfg.ndim;
@@ -89,9 +149,6 @@ inline void initial_state(const pimdb_config& cfg, const RunParams& run, std::ve
     p0.assign((size_t)P * N * D, 0.0);
     const double beta = 1.0 / (1.0 * cfg.temperature);
     const double thermo_beta = beta / P;
-    if (run.init_vel_type != "random")
-        throw std::invalid_argument("initial_velocity " + run.init_vel_type +
-                                    " needs the reference's file loaders (not part of the hot path)");
     for (int b = 0; b < P; ++b) {
         std::mt19937 gen((unsigned)(cfg.seed + b));
         double* x = &x0[(size_t)b * N * D];
@@ -102,15 +159,20 @@ inline void initial_state(const pimdb_config& cfg, const RunParams& run, std::ve
             std::uniform_real_distribution<double> u(-0.5 * cfg.size, 0.5 * cfg.size);
             for (int i = 0; i < N * D; ++i) x[i] = u(gen);
         } else {
-            throw std::invalid_argument("initial_position " + run.init_pos_type +
-                                        " needs the reference's file loaders (not part of the hot path)");
+            load_xyz(formatted_bead_file(run.init_pos_spec, b), N, D, x);
         }
-        for (int i = 0; i < N * D; ++i) {
-            std::normal_distribution<double> nd(0.0, 1 / std::sqrt(thermo_beta * cfg.mass));
-            p[i] = cfg.mass * nd(gen);
+        if (run.init_vel_type == "random") {
+            for (int i = 0; i < N * D; ++i) {
+                std::normal_distribution<double> nd(0.0, 1 / std::sqrt(thermo_beta * cfg.mass));
+                p[i] = cfg.mass * nd(gen);
+            }
+        } else {
+            const std::string name = run.init_vel_spec.empty() ? std::format("init/vel_{:02}.dat", b + 1)
+                                                                : formatted_bead_file(run.init_vel_spec, b);
+            load_momenta(name, cfg.mass, N, D, p);
         }
     }
-    if (zero_com) {
+    if (zero_com && run.init_vel_type == "random") {
         double cm[3] = {0.0, 0.0, 0.0};
         for (int b = 0; b < P; ++b) {
             double per[3] = {0.0, 0.0, 0.0};
@@ -122,6 +184,63 @@ inline void initial_state(const pimdb_config& cfg, const RunParams& run, std::ve
             for (int a = 0; a < D; ++a) p0[i * D + a] -= cm[a];
     }
 }
+
+// The per-bead state dumps (src/states/{position,velocity,force}.cpp):
+// output/position_<b>.xyz, velocity_<b>.dat, force_<b>.dat, appended at the
+// start of every sfreq-th step, in the configured units ("on", "true" and
+// "none" mean atomic units).
+class StateWriter {
+public:
+    StateWriter(const pimdb_config& c, const RunParams& run, const std::string& dir) : c_(c) {
+        auto unit = [](const std::string& u) { return (u == "on" || u == "true" || u == "none") ? std::string("atomic_unit") : u; };
+        auto on = [](const std::string& u) { return u != "off" && u != "false"; };
+        if (on(run.output_positions)) open(files_[0], dir, "position_{}.xyz", unit(run.output_positions), units_[0]);
+        if (on(run.output_velocities)) open(files_[1], dir, "velocity_{}.dat", unit(run.output_velocities), units_[1]);
+        if (on(run.output_forces)) open(files_[2], dir, "force_{}.dat", unit(run.output_forces), units_[2]);
+    }
+    bool enabled() const { return !files_[0].empty() || !files_[1].empty() || !files_[2].empty(); }
+    bool wants(int k) const { return !files_[k].empty(); }
+    // x, p, f: [bead][particle][axis]; any may be empty when not written
+    void output(long step, const std::vector<double>& x, const std::vector<double>& p, const std::vector<double>& f) {
+        const int N = c_.natoms, D = c_.ndim;
+        static const char* family[3] = {"length", "velocity", "force"};
+        const std::vector<double>* src[3] = {&x, &p, &f};
+        for (int k = 0; k < 3; ++k) {
+            if (files_[k].empty()) continue;
+            for (int b = 0; b < c_.nbeads; ++b) {
+                std::ofstream& o = *files_[k][b];
+                o << std::format("{}\\n", N) << std::format("Step {}\\n", step);
+                for (int i = 0; i < N; ++i) {
+                    if (k == 0) o << "1";
+                    else o << (i + 1) << " 1";
+                    for (int a = 0; a < D; ++a) {
+                        double v = (*src[k])[((size_t)b * N + i) * D + a];
+                        if (k == 1) v /= c_.mass;
+                        o << std::format(" {:^20.12e}", Units::convertToUser(family[k], units_[k], v));
+                    }
+                    if (D == 1) o << " 0.0 0.0";
+                    else if (D == 2) o << " 0.0";
+                    o << "\\n";
+                }
+            }
+        }
+    }
+
+private:
+    void open(std::vector<std::unique_ptr<std::ofstream>>& v, const std::string& dir, const char* pattern,
+              const std::string& unit, std::string& unit_out) {
+        Units::convertToUser(pattern[0] == 'p' ? "length" : (pattern[0] == 'v' ? "velocity" : "force"), unit, 1.0);
+        unit_out = unit;
+        for (int b = 0; b < c_.nbeads; ++b) {
+            const int bead = b;
+            v.push_back(std::make_unique<std::ofstream>(dir + "/" + std::vformat(pattern, std::make_format_args(bead)),
+                                                        std::ios::out | std::ios::app));
+        }
+    }
+    pimdb_config c_;
+    std::vector<std::unique_ptr<std::ofstream>> files_[3];
+    std::string units_[3];
+};
 
 inline void check(int st, pimdb_handle* h = nullptr) {
     if (st == PIMDB_OK) return;
@@ -416,37 +535,46 @@ public:
     long getStep() const { return md_step; }
     void observables(pimdb_observables& o) { check(pimdb_compute_observables(engine->handle(), &o), engine->handle()); }
 
-    // Simulation::run (src/simulation.cpp:236-280): steps+1 MD steps; from
-    // the thermalization threshold on, the observables of every sfreq-th
-    // step go to the logger.  The fused schedule runs the steps between two
-    // logged ones as one call.
-    void run(bool plugin, pimdb_host::ObservablesLogger* logger) {
+    // Simulation::run (src/simulation.cpp:236-280): steps+1 MD steps.  At
+    // the start of every sfreq-th step the states are dumped; from the
+    // thermalization threshold on, the observables of every sfreq-th step
+    // (at its end) go to the logger.  The fused schedule runs the steps in
+    // between as one call.
+    void run(bool plugin, pimdb_host::ObservablesLogger* logger, pimdb_host::StateWriter* states = nullptr) {
         const long steps = run_params.steps, sfreq = std::max(1L, run_params.sfreq);
         const double threshold = run_params.threshold * steps;
+        auto advance = [&](long n) {
+            while (n > 0) {
+                const int k = (int)std::min<long>(n, 1L << 30);
+                if (plugin) {
+                    for (int q = 0; q < k; ++q) plugin_step();
+                } else {
+                    fast_step(k);
+                }
+                n -= k;
+            }
+        };
         long s = 0;
         while (s <= steps) {
-            long next = -1;
-            if (logger && logger->enabled()) {
-                long t0 = std::max(s, (long)std::ceil(threshold));
-                long t = (t0 + sfreq - 1) / sfreq * sfreq;
-                if (t <= steps) next = t;
-            }
-            const long until = next >= 0 ? next : steps;
-            for (long left = until - s + 1; left > 0;) {
-                const int n = (int)std::min<long>(left, 1L << 30);
-                if (plugin) {
-                    for (int k = 0; k < n; ++k) plugin_step();
-                } else {
-                    fast_step(n);
+            if (s % sfreq == 0) {
+                if (states && states->enabled()) {
+                    std::vector<double> x, p, f;
+                    get_state(x, p, f);
+                    states->output(s, x, p, f);
                 }
-                left -= n;
+                advance(1);
+                if (logger && logger->enabled() && s >= threshold) {
+                    pimdb_observables o{};
+                    observables(o);
+                    logger->log(s, o);
+                }
+                s += 1;
+            } else {
+                const long next = (s / sfreq + 1) * sfreq;
+                const long n = std::min(next, steps + 1) - s;
+                advance(n);
+                s += n;
             }
-            if (next >= 0) {
-                pimdb_observables o{};
-                observables(o);
-                logger->log(next, o);
-            }
-            s = until + 1;
         }
     }
 
@@ -462,7 +590,7 @@ private:
     void initialize_state() {
         pimdb_host::initial_state(cfg, run_params, x0, p0);
         check(pimdb_set_state(engine->handle(), x0.data(), p0.data()), engine->handle());
-        zeroMomentum();
+        if (run_params.init_vel_type == "random") zeroMomentum();
     }
 
     long md_step = 0;

@@ -61,9 +61,10 @@ int main(int argc, char** argv) {
         pimdb_gb300::Simulation sim(params);
         std::filesystem::create_directories("output");
         pimdb_host::ObservablesLogger logger(params.config, params.run, "output/simulation.out");
+        pimdb_host::StateWriter states(params.config, params.run, "output");
         std::cout << "[*] Running the simulation\n";
         const auto t0 = std::chrono::steady_clock::now();
-        sim.run(plugin, &logger);
+        sim.run(plugin, &logger, &states);
         const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         const double bs = (double)params.config.natoms * params.config.nbeads * (params.run.steps + 1) / wall;
         std::printf("[*] Simulation finished running successfully (Runtime = %.3g sec, %.4g bead-steps/s)\n", wall, bs);

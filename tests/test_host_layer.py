@@ -218,3 +218,48 @@ def test_cli_replays_nose_hoover_regression_cases(case, tmp_path):
     want = z[f"{case}/simulation_out"][:len(got)]
     assert len(got) == 6
     np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-9)
+    # the state dumps (src/states/*.cpp) at the golden frames (steps 0 and 5000)
+    P, N = index[case]["nbeads"], z[f"{case}/positions_angstrom"].shape[2]
+    for stem, key in (("position_{}.xyz", "positions_angstrom"), ("velocity_{}.dat", "velocities_angstrom_per_ps"),
+                      ("force_{}.dat", "forces_ev_per_angstrom")):
+        frames = np.stack([R.read_frames(tmp_path / "output" / stem.format(b), N, 3) for b in range(P)], axis=1)
+        assert frames.shape[0] == 6
+        gold = z[f"{case}/{key}"]
+        for mine, k in ((frames[0], 0), (frames[5], 1)):
+            scale = np.abs(gold[k]).max()
+            assert np.abs(mine - gold[k]).max() <= 1e-6 * scale + (1e-300 if scale else 0.0), (stem, k)
+
+
+@pytest.mark.skipif(not R.available("d3"), reason="compiled reference not built here")
+@pytest.mark.parametrize("pos_spec,vel_spec", [("xyz(pos_{}.xyz)", "manual(vel_{}.dat)"),
+                                               ("xyz(one.xyz)", "random"),
+                                               ("random", "manual")])
+def test_cli_initial_state_from_files_matches_reference(pos_spec, vel_spec, tmp_path):
+    """xyz / velocity-file initialisation (src/common.cpp:49-136): the driver's
+    initial state against frame 0 of the compiled reference's own dumps."""
+    _need_cli()
+    P, N = 4, 6
+    rng = np.random.default_rng(9)
+    xa = rng.uniform(-4, 4, (P, N, 3))
+    va = rng.normal(0, 3.0, (P, N, 3))
+    for d in (tmp_path, tmp_path / "ref"):
+        d.mkdir(exist_ok=True)
+        (d / "init").mkdir(exist_ok=True)
+        for b in range(P):
+            R._write_xyz(d / f"pos_{b}.xyz", xa[b])
+            R._write_vel(d / f"vel_{b}.dat", va[b])
+            R._write_vel(d / "init" / f"vel_{b + 1:02}.dat", va[b])
+        R._write_xyz(d / "one.xyz", xa[0])
+    sec = _sections(P=P, N=N, init_pos="random")
+    sec["simulation"]["initial_position"] = pos_spec
+    sec["simulation"]["initial_velocity"] = vel_spec
+    x, p = _initial(tmp_path, sec, P, N)
+    R.write_ini(tmp_path / "ref" / "c.ini", sec)
+    env = dict(os.environ, PIMDB_SHIM_NP=str(P), PIMDB_SHIM_TIMEOUT="120")
+    r = subprocess.run([str(R.REF / "pimdb_d3"), "-in", "c.ini"], cwd=tmp_path / "ref", capture_output=True, text=True,
+                       env=env, timeout=300)
+    assert r.returncode == 0 and "[X]" not in r.stdout, r.stdout
+    X = np.stack([R.read_frames(tmp_path / "ref" / "output" / f"position_{b}.xyz", N, 3)[0] for b in range(P)])
+    V = np.stack([R.read_frames(tmp_path / "ref" / "output" / f"velocity_{b}.dat", N, 3)[0] for b in range(P)])
+    assert np.abs(x - X).max() <= 1e-12 * np.abs(X).max()
+    assert np.abs(p / 1.0 - V).max() <= 1e-12 * np.abs(V).max()
