@@ -209,7 +209,7 @@ public:
             if (files_[k].empty()) continue;
             for (int b = 0; b < c_.nbeads; ++b) {
                 std::ofstream& o = *files_[k][b];
-                o << std::format("{}\\n", N) << std::format("Step {}\\n", step);
+                o << std::format("{}\n", N) << std::format("Step {}\n", step);
                 for (int i = 0; i < N; ++i) {
                     if (k == 0) o << "1";
                     else o << (i + 1) << " 1";
@@ -220,7 +220,7 @@ public:
                     }
                     if (D == 1) o << " 0.0 0.0";
                     else if (D == 2) o << " 0.0";
-                    o << "\\n";
+                    o << "\n";
                 }
             }
         }
