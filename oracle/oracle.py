@@ -52,6 +52,7 @@ class System(C.Structure):
         ("spring_constant", C.c_double), ("beta_ex", C.c_double),
         ("ext_kind", C.c_int), ("ext_p", C.c_double * 3),
         ("int_kind", C.c_int), ("int_p", C.c_double * 3), ("cutoff", C.c_double), ("nchains", C.c_int),
+        ("factorial", C.c_int),
     ]
 
 
@@ -112,14 +113,18 @@ THERMOSTATS = {"none": 0, "langevin": 1, "nose_hoover": 2, "nose_hoover_np": 3, 
 def make_system(*, ndim, natoms, nbeads, temperature, mass, bosonic=False, pbc=False, size=1.0, fixcom=True,
                 propagator="cartesian", thermostat="langevin", nmthermostat=False, dt=1.0, gamma=-1.0,
                 ext="free", ext_p=(0.0, 0.0, 0.0), interaction="free", int_p=(0.0, 0.0, 0.0), cutoff=-1.0,
-                nchains=4):
-    """Builds the oracle's system record; all quantities in atomic units."""
+                nchains=4, factorial=False):
+    """Builds the oracle's system record; all quantities in atomic units.
+    factorial=True selects the permutation-sum exchange of
+    factorial_bosonic_exchange.cpp (the reference's compile-time
+    FACTORIAL_BOSONIC_ALGORITHM)."""
     s = System()
     s.ndim, s.natoms, s.nbeads = ndim, natoms, nbeads
     s.bosonic, s.pbc, s.fixcom = int(bosonic), int(pbc), int(fixcom)
     s.propagator = 1 if propagator == "normal_modes" else 0
     s.thermostat = THERMOSTATS[thermostat]
     s.nchains = nchains
+    s.factorial = int(factorial)
     s.nmthermostat = int(nmthermostat)
     s.size, s.mass, s.dt = size, mass, dt
     s.gamma = gamma if gamma >= 0 else 1 / (100.0 * dt)  # params.cpp:17-20

@@ -367,12 +367,170 @@ double orc_longest_probability(const orc_system* s, const double* E, const doubl
     return exp(-s->beta_ex * (E[enk_index(N, N)] - V[N]));
 }
 
+/* ------------------------------------------------------------------------ */
+/* factorial exchange (src/bosonic_exchange/factorial_bosonic_exchange.cpp)   */
+
+/* std::ranges::next_permutation: the next arrangement in lexicographic order;
+ * returns 0 (and restores ascending order) after the last one. */
+static int orc_next_permutation(int* a, int n) {
+    int i = n - 2;
+    while (i >= 0 && !(a[i] < a[i + 1])) --i;
+    if (i < 0) {
+        for (int l = 0, r = n - 1; l < r; ++l, --r) {
+            int t = a[l];
+            a[l] = a[r];
+            a[r] = t;
+        }
+        return 0;
+    }
+    int j = n - 1;
+    while (!(a[i] < a[j])) --j;
+    int t = a[i];
+    a[i] = a[j];
+    a[j] = t;
+    for (int l = i + 1, r = n - 1; l < r; ++l, --r) {
+        t = a[l];
+        a[l] = a[r];
+        a[r] = t;
+    }
+    return 1;
+}
+
+/* labels[] holds the bottom line of the permutation's two-line notation
+ * (:9-12): the last bead of particle l links to the first bead of
+ * labels[l] (lastBeadNeighbor, :47-49); the first bead of particle l links to
+ * the last bead of the particle at l's position (firstBeadNeighbor, :33-35). */
+static void orc_inverse(const int* labels, int n, int* inv) {
+    for (int l = 0; l < n; ++l) inv[labels[l]] = l;
+}
+
+/* getMinExteriorSpringEnergy (:58-82) */
+double orc_factorial_min_energy(const orc_system* s, const double* x_first, const double* x_last) {
+    const int N = s->natoms, D = s->ndim;
+    int* labels = (int*)malloc(sizeof(int) * (size_t)N);
+    for (int l = 0; l < N; ++l) labels[l] = l;
+    double min_delta = DBL_MAX;
+    do {
+        double diff2 = 0.0;
+        for (int l = 0; l < N; ++l) diff2 += sepsq(s, x_first + (long)l * D, x_last + (long)labels[l] * D);
+        const double e = 0.5 * s->spring_constant * diff2;
+        if (e < min_delta) min_delta = e; /* std::min(min_delta, e) */
+    } while (orc_next_permutation(labels, N));
+    free(labels);
+    return min_delta;
+}
+
+/* effectivePotential (:91-114) */
+static double orc_factorial_potential(const orc_system* s, const double* x_first, const double* x_last) {
+    const int N = s->natoms, D = s->ndim;
+    const double beta_half_k = s->thermo_beta * 0.5 * s->spring_constant; /* simulation.cpp:52 */
+    int* labels = (int*)malloc(sizeof(int) * (size_t)N);
+    for (int l = 0; l < N; ++l) labels[l] = l;
+    long counter = 0;
+    double weights_sum = 0.0;
+    do {
+        counter++;
+        double diff2 = 0.0;
+        for (int l = 0; l < N; ++l) diff2 += sepsq(s, x_first + (long)l * D, x_last + (long)labels[l] * D);
+        weights_sum += exp(-beta_half_k * diff2);
+    } while (orc_next_permutation(labels, N));
+    free(labels);
+    return (-1.0 / s->beta_ex) * log(weights_sum / (double)counter);
+}
+
+/* springForceLastBead (:121-172, first == 0) and springForceFirstBead
+ * (:179-230, first == 1).  x is the exchange bead, x_prev / x_next its
+ * neighbours in the reference's bead order; f is overwritten. */
+static void orc_factorial_force(const orc_system* s, int first, const double* x, const double* x_prev,
+                                const double* x_next, double e_shift, double* f) {
+    const int N = s->natoms, D = s->ndim;
+    const double k = s->spring_constant, beta = s->beta_ex;
+    const double* x_first_bead = first ? x : x_next;
+    const double* x_last_bead = first ? x_prev : x;
+    int* labels = (int*)malloc(sizeof(int) * (size_t)N * 2);
+    int* inv = labels + N;
+    double* temp = (double*)malloc(sizeof(double) * (size_t)N * D);
+    for (int l = 0; l < N; ++l) labels[l] = l;
+    for (long i = 0; i < (long)N * D; ++i) f[i] = 0.0;
+    double denom_weight = 0.0;
+    do {
+        orc_inverse(labels, N, inv);
+        double weight = 0.0;
+        for (int l = 0; l < N; ++l) {
+            double sums[3] = {0.0, 0.0, 0.0};
+            double d_ext[3], d_int[3];
+            const double* xl = (first ? x_first_bead : x_last_bead) + (long)l * D;
+            for (int a = 0; a < D; ++a) {
+                if (first) /* last bead of the particle at l's position minus first bead of l */
+                    d_ext[a] = sep(s, xl, x_last_bead + (long)inv[l] * D, a);
+                else /* first bead of labels[l] minus last bead of l */
+                    d_ext[a] = sep(s, xl, x_first_bead + (long)labels[l] * D, a);
+                weight += d_ext[a] * d_ext[a];
+            }
+            for (int a = 0; a < D; ++a) d_int[a] = sep(s, xl, (first ? x_next : x_prev) + (long)l * D, a);
+            for (int a = 0; a < D; ++a) {
+                /* sums += diff_prev + diff_next, each in the reference's roles */
+                sums[a] += first ? d_ext[a] + d_int[a] : d_int[a] + d_ext[a];
+                temp[(long)l * D + a] = sums[a] * k;
+            }
+        }
+        weight = exp(-beta * (0.5 * k * weight - e_shift));
+        for (long i = 0; i < (long)N * D; ++i) f[i] += weight * temp[i];
+        denom_weight += weight;
+    } while (orc_next_permutation(labels, N));
+    for (long i = 0; i < (long)N * D; ++i) f[i] = f[i] / denom_weight;
+    free(labels);
+    free(temp);
+}
+
+/* primEstimator (:259-293) */
+static double orc_factorial_prim(const orc_system* s, const double* x_first, const double* x_last, double e_shift) {
+    const int N = s->natoms, D = s->ndim;
+    const double k = s->spring_constant, beta = s->beta_ex;
+    int* labels = (int*)malloc(sizeof(int) * (size_t)N * 2);
+    int* inv = labels + N;
+    for (int l = 0; l < N; ++l) labels[l] = l;
+    double numerator = 0.0, denom_weight = 0.0;
+    do {
+        orc_inverse(labels, N, inv);
+        double weight = 0.0;
+        for (int l = 0; l < N; ++l) weight += sepsq(s, x_first + (long)l * D, x_last + (long)inv[l] * D);
+        const double delta = 0.5 * k * weight;
+        weight = exp(-beta * (delta - e_shift));
+        numerator += delta * weight;
+        denom_weight += weight;
+    } while (orc_next_permutation(labels, N));
+    free(labels);
+    double e = numerator / denom_weight;
+    e /= s->nbeads; /* IPI_CONVENTION */
+    return (-1.0) * e;
+}
+
+int orc_factorial_exchange(const orc_system* s, const double* x_all, double* f1, double* fP, double* scalars) {
+    const int N = s->natoms, D = s->ndim, P = s->nbeads;
+    const long bead = (long)N * D;
+    const double* x1 = x_all;
+    const double* xP = x_all + (long)(P - 1) * bead;
+    /* prepare() (:19-21): the shift of the weights, from beads 1 and P */
+    const double e_shift = orc_factorial_min_energy(s, x1, xP);
+    if (fP) orc_factorial_force(s, 0, xP, x_all + (long)(P - 2) * bead, x1, e_shift, fP);
+    if (f1) orc_factorial_force(s, 1, x1, xP, x_all + (long)(P > 1 ? 1 : 0) * bead, e_shift, f1);
+    if (scalars) {
+        scalars[0] = orc_factorial_potential(s, x1, xP);
+        scalars[1] = orc_factorial_prim(s, x1, xP, e_shift);
+        scalars[2] = 0.0; /* getDistinctProbability (:237-240): not implemented there */
+        scalars[3] = 0.0; /* getLongestProbability (:249-252) */
+    }
+    return isfinite(e_shift) ? 0 : 2;
+}
+
 int orc_exchange(const orc_system* s, const double* x_all, double* f1, double* fP, double* scalars, double* E_out,
                  double* V_out, double* Vb_out, double* prob_out) {
     const int N = s->natoms, D = s->ndim, P = s->nbeads;
     const long bead = (long)N * D;
     const double* x1 = x_all;
     const double* xP = x_all + (long)(P - 1) * bead;
+    if (s->factorial) return orc_factorial_exchange(s, x_all, f1, fP, scalars);
     double* E = (double*)malloc(sizeof(double) * (size_t)((long)N * (N + 1) / 2 + 1));
     double* V = (double*)malloc(sizeof(double) * (size_t)(N + 1));
     double* Vb = (double*)malloc(sizeof(double) * (size_t)(N + 1));

@@ -53,6 +53,9 @@ typedef struct {
     double int_p[3];        /* harmonic: omega | dipole: strength */
     double cutoff;          /* effective cutoff (simulation.cpp:84-90): 0 = no pairs, <0 = all pairs */
     int nchains;            /* Nose-Hoover chain length (params.cpp nchains) */
+    int factorial;          /* exchange by the sum over all N! permutations
+                               (factorial_bosonic_exchange.cpp, the reference's
+                               compile-time FACTORIAL_BOSONIC_ALGORITHM) */
 } orc_system;
 
 /* Fills the derived constants of `s` from T (atomic units), P, mass, ... and
@@ -85,11 +88,21 @@ double orc_distinct_probability(const orc_system* s, const double* E, const doub
 double orc_longest_probability(const orc_system* s, const double* E, const double* V);
 
 /* Convenience: the whole exchange for one ring.  Any output pointer may be
- * NULL.  f1/fP are the exterior spring forces on beads 1 and P including the
+ * NULL.  With s->factorial set it is orc_factorial_exchange (E_out, V_out,
+ * Vb_out and prob_out are then left untouched).  f1/fP are the exterior spring forces on beads 1 and P including the
  * interior neighbour spring (quadratic_bosonic_exchange.cpp:159-215).
  * scalars = {V_B, primEstimator, P_distinct, P_longest}. */
 int orc_exchange(const orc_system* s, const double* x_all, double* f1, double* fP, double* scalars, double* E_out,
                  double* V_out, double* Vb_out, double* prob_out);
+
+/* ---- factorial exchange (factorial_bosonic_exchange.cpp) on one ring ----
+ * The permutation sum the Feldman-Hirshberg recursion replaces.  For a given
+ * configuration the two are different potentials: the recursion keeps one
+ * representative cycle per particle set, which equals the full sum only after
+ * the interior beads are integrated out.  Same outputs as orc_exchange;
+ * P_distinct and P_longest are 0 as in the reference (:237-252). */
+double orc_factorial_min_energy(const orc_system* s, const double* x_first, const double* x_last);
+int orc_factorial_exchange(const orc_system* s, const double* x_all, double* f1, double* fP, double* scalars);
 
 /* ---- forces on all beads (simulation.cpp:353-455) ---- */
 void orc_spring_forces_interior(const orc_system* s, const double* x_prev, const double* x, const double* x_next,

@@ -38,9 +38,26 @@ def test_forces_are_zero_in_the_first_frame(case):
     assert np.all(z[f"{case}/forces_ev_per_angstrom"][0] == 0.0)
 
 
+def test_factorial_exchange_matches_golden_frames(tmp_path):
+    # The permutation sum over all N! exchanges (factorial_bosonic_exchange.cpp)
+    # recomputed from the golden positions of the factorial build's fixture.
+    z, _ = G.load()
+    case = "bosonic_factorial_harmonic_dynamics"
+    s, _ = O.system_from_ini(G.write_ini(case, tmp_path), factorial=True)
+    X = z[f"{case}/positions_angstrom"]
+    F = z[f"{case}/forces_ev_per_angstrom"]
+    worst = 0.0
+    for fr in range(1, X.shape[0]):
+        f = O.update_forces(s, X[fr] * G.ANGSTROM)["f"] / G.EV_PER_ANG
+        assert np.allclose(f, F[fr], rtol=1e-5)
+        worst = max(worst, float(np.max(np.abs(f - F[fr])) / np.max(np.abs(F[fr]))))
+    assert worst < 1e-9, worst
+
+
 def test_factorial_and_quadratic_potentials_differ_configurationwise(tmp_path):
-    # The factorial fixture cannot pin the FH forces: the FH recursion equals
-    # the permutation sum only after integrating over the interior beads.
+    # The factorial fixture cannot pin the FH forces: the FH recursion keeps
+    # one representative cycle per set of exchanged particles and equals the
+    # permutation sum only after integrating over the interior beads.
     z, _ = G.load()
     case = "bosonic_factorial_harmonic_dynamics"
     s, _ = O.system_from_ini(G.write_ini(case, tmp_path))

@@ -173,3 +173,66 @@ def test_observables_match_reference_simulation_out(case, tmp_path):
         ob = O.observables(s, res["x"][k + 1], res["v"][k + 1] * s.mass)
         for j, c in enumerate(cols[1:], start=1):
             assert abs(ob[c] - rows[k, j]) <= 1e-7 * abs(rows[k, j]) + 1e-300, (k, c, ob[c], rows[k, j])
+
+
+# The factorial build of the reference (FACTORIAL_BOSONIC_ALGORITHM): the
+# permutation sum over all N! exchanges.
+FACT_PROBES = [
+    # N, P, bosonic, pbc, interaction, external, box (angstrom)
+    (1, 3, True, False, "free", "harmonic", 5.0),
+    (3, 2, True, False, "harmonic", "cosine", 6.0),
+    (4, 6, True, False, "free", "harmonic", 10.0),
+    (5, 4, True, True, "aziz", "free", 8.0),
+    (6, 8, True, True, "free", "double_well", 9.0),
+    (7, 5, True, False, "dipole", "harmonic", 12.0),
+]
+needs_fact = pytest.mark.skipif(not R.available("d3_fact"), reason="factorial reference build absent")
+
+
+@needs_fact
+@pytest.mark.parametrize("case", FACT_PROBES)
+def test_factorial_probe_bit_identical(case, tmp_path):
+    N, P, bos, pbc, inter, ext, box = case
+    rng = np.random.default_rng(N * 7 + P)
+    L = box * R.ANGSTROM
+    x = rng.uniform(-0.5 * L, 0.5 * L, (N, 3))[None] + rng.normal(0, 0.3 * R.ANGSTROM, (P, N, 3))
+    sec = _sections(N, P, bos, pbc, inter, ext, box)
+    R.write_ini(tmp_path / "c.ini", sec)
+    s, _ = O.system_from_ini(tmp_path / "c.ini", factorial=True)
+    ref = R.probe(sec, x, variant="d3_fact")
+    got = O.update_forces(s, x)
+    for k in ("f", "spring", "phys"):
+        assert np.array_equal(got[k], ref[k]), k
+    ex = O.exchange(s, x)
+    assert [ex["VB"], ex["prim"], ex["p_distinct"], ex["p_longest"]] == list(ref["scalars"][0][:4])
+    assert list(ref["scalars"][P - 1][:2]) == [ex["VB"], ex["prim"]]
+
+
+@needs_fact
+@pytest.mark.parametrize("thermo", ["langevin", "none"])
+def test_factorial_trajectory_and_observables_match_reference(thermo, tmp_path):
+    N, P, steps, seed = 4, 6, 12, 99
+    rng = np.random.default_rng(41)
+    x_ang = rng.uniform(-2.0, 2.0, (N, 3))[None] + rng.normal(0, 0.2, (P, N, 3))
+    v = rng.normal(0, 2.0, (P, N, 3))
+    sec = _sections(N, P, True, False, "harmonic", "harmonic", 9.0, "2.0 kelvin")
+    sec["simulation"].update(thermostat=thermo, seed=seed, steps=steps, sfreq=1, dt="1.0 femtosecond",
+                             threshold=0.0)
+    sec["observables"] = {"energy": "atomic_unit", "classical": "atomic_unit", "bosonic": "atomic_unit"}
+    ref = R.run_trajectory(sec, x_ang, v, variant="d3_fact")
+    R.write_ini(tmp_path / "c.ini", sec)
+    s, _ = O.system_from_ini(tmp_path / "c.ini", factorial=True)
+    tr = O.Trajectory(s, x_ang * R.ANGSTROM, s.mass * (v * R.ANG_PER_PS))
+    streams = [O.RanMars(seed + b) for b in range(P)]
+    for st in range(steps + 1):
+        for got, want in ((tr.x, ref["x"][st]), (tr.p / s.mass, ref["v"][st]), (tr.f, ref["f"][st])):
+            assert np.abs(got - want).max() <= 2e-12 * max(np.abs(want).max(), 1e-300)
+        xi = O.ranmars_noise(streams, N, 3) if thermo == "langevin" else np.zeros((2, P, N, 3))
+        assert tr.step(xi) == 0
+    lines = ref["simulation_out"].strip().split("\n")
+    cols = lines[0].split()
+    rows = np.array([list(map(float, ln.split())) for ln in lines[1:]])
+    for k in range(len(rows) - 1):
+        ob = O.observables(s, ref["x"][k + 1], ref["v"][k + 1] * s.mass)
+        for j, c in enumerate(cols[1:], start=1):
+            assert abs(ob[c] - rows[k, j]) <= 1e-7 * abs(rows[k, j]) + 1e-300, (k, c, ob[c], rows[k, j])
