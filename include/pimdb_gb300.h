@@ -56,6 +56,15 @@ enum pimdb_thermostat {
     PIMDB_THERMO_NOSE_HOOVER_NP = 3,
     PIMDB_THERMO_NOSE_HOOVER_NP_DIM = 4
 };
+/* Bosonic exchange algorithm (the reference chooses at compile time with
+ * FACTORIAL_BOSONIC_ALGORITHM, CMakeLists.txt:49-54, include/common.h:26-28):
+ * the Feldman-Hirshberg recursion (src/bosonic_exchange/quadratic_bosonic_exchange.cpp),
+ * or the sum over all N! permutations
+ * (src/bosonic_exchange/factorial_bosonic_exchange.cpp; natoms <= 12).  The
+ * two are different potentials for a given configuration with the same
+ * partition function.  The factorial sum is FP64 in both precisions and
+ * reports P_distinct = P_longest = 0 as the reference does. */
+enum pimdb_exchange_algorithm { PIMDB_EXCHANGE_FELDMAN_HIRSHBERG = 0, PIMDB_EXCHANGE_FACTORIAL = 1 };
 /* Arithmetic of the pair forces: FP64 throughout, or FP32 pair arithmetic
  * with FP64 per-atom accumulation.  Exchange and integrator are FP64 in both. */
 enum pimdb_precision { PIMDB_FP64 = 0, PIMDB_MIXED = 1 };
@@ -86,6 +95,7 @@ typedef struct pimdb_config {
     unsigned long long seed;  /* Langevin noise key */
     unsigned int replica;     /* folded into the noise counter */
     int nchains;              /* [simulation] nchains: Nose-Hoover chain length */
+    int exchange;             /* enum pimdb_exchange_algorithm */
 } pimdb_config;
 
 typedef struct pimdb_handle pimdb_handle;
@@ -161,7 +171,10 @@ int pimdb_zero_momentum(pimdb_handle* h);
 int pimdb_propagate(pimdb_handle* h);
 
 /* BosonicExchange on the current coordinates
- * (src/bosonic_exchange/quadratic_bosonic_exchange.cpp:30-279):
+ * (src/bosonic_exchange/quadratic_bosonic_exchange.cpp:30-279; with
+ * PIMDB_EXCHANGE_FACTORIAL FactorialBosonicExchange,
+ * src/bosonic_exchange/factorial_bosonic_exchange.cpp:19-293, whose
+ * scalars[2] and [3] are 0):
  *   scalars[0] = effectivePotential()      V_B = V[N]
  *   scalars[1] = primEstimator()           -d(beta_ex V_B)/d(beta_ex) / P at fixed E
  *   scalars[2] = getDistinctProbability()
@@ -172,7 +185,8 @@ int pimdb_propagate(pimdb_handle* h);
 int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first, double* f_last);
 /* Intermediate arrays of the last pimdb_exchange / force evaluation:
  * E (N(N+1)/2, the reference's E_kn order, getEnk(m,k) = E[m(m+1)/2 - k]),
- * V (N+1), V_backwards (N+1).  Any may be NULL. */
+ * V (N+1), V_backwards (N+1).  Any may be NULL.  PIMDB_ERR_CONFIG with the
+ * factorial exchange, which has none of them. */
 int pimdb_exchange_arrays(pimdb_handle* h, double* E_kn, double* V, double* V_backwards);
 
 /* The forward function of pimdb_compute_forces: the potential energy U of

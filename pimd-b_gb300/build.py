@@ -20,8 +20,8 @@ BUILD = HERE / "_build"
 LIB = HERE / "libpimdb_gb300.so"
 CLI = HERE / "pimdb_gb300"
 
-CU_SOURCES = ["csrc/forces.cu", "csrc/exchange.cu", "csrc/integrator.cu", "csrc/api.cu", "csrc/noalloc.cu",
-              "csrc/batch.cu"]
+CU_SOURCES = ["csrc/forces.cu", "csrc/exchange.cu", "csrc/factorial.cu", "csrc/integrator.cu", "csrc/api.cu",
+              "csrc/noalloc.cu", "csrc/batch.cu"]
 CPP_SOURCES = ["host/params.cpp"]
 CLI_SOURCES = ["host/pimdb_main.cpp"]
 HEADERS = ["csrc/common.cuh", "csrc/kernels.h", "csrc/config.h", "csrc/exchange_dev.cuh", "csrc/forces_dev.cuh",

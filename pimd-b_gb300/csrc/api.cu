@@ -66,6 +66,9 @@ struct pimdb_handle {
     double* d_nh = nullptr;
     double* d_pnm = nullptr;
     int opt_cells = -1;
+    // factorial exchange (sum over all N! permutations): its work buffer
+    bool factorial = false;
+    double* d_fact = nullptr;
     // CUDA graphs of pimdb_step_async: keyed by the step count and the
     // host-side step state at entry; the step index comes from d_step, which
     // every graph advances by its step count
@@ -213,6 +216,10 @@ std::string validate_config(const pimdb_config& c) {
     if (c.precision != PIMDB_FP64 && c.precision != PIMDB_MIXED) return "unknown precision";
     if ((long long)c.natoms * c.nbeads * c.ndim > (1ll << 31)) return "system too large";
     if (c.bosonic && c.nbeads > 1 && c.natoms > 16384) return "bosonic exchange supports at most 16384 particles";
+    if (c.exchange != PIMDB_EXCHANGE_FELDMAN_HIRSHBERG && c.exchange != PIMDB_EXCHANGE_FACTORIAL)
+        return "unknown bosonic exchange algorithm";
+    if (c.exchange == PIMDB_EXCHANGE_FACTORIAL && c.bosonic && c.nbeads > 1 && c.natoms > kFactMaxN)
+        return "the factorial bosonic exchange supports at most " + std::to_string(kFactMaxN) + " particles";
     return "";
 }
 
@@ -314,6 +321,7 @@ static void free_handle(pimdb_handle* h) {
     if (h->d_tw) cudaFree(h->d_tw);
     if (h->d_cells) cudaFree(h->d_cells);
     if (h->d_nh) cudaFree(h->d_nh);
+    if (h->d_fact) cudaFree(h->d_fact);
     if (h->d_pnm) cudaFree(h->d_pnm);
     if (h->d_step) cudaFree(h->d_step);
     drop_graphs(h);
@@ -384,6 +392,9 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_step, sizeof(long long));
     h->cell_nc = cell_grid(s, h->D);
     if (e == cudaSuccess && h->cell_nc > 0) e = cudaMalloc(&h->d_cells, cell_buffer_bytes(s, h->D, h->cell_nc));
+    h->factorial = s.bosonic && c.exchange == PIMDB_EXCHANGE_FACTORIAL;
+    if (e == cudaSuccess && h->factorial)
+        e = cudaMalloc((void**)&h->d_fact, factorial_work_doubles(s.N) * sizeof(double));
     // xflags: [0],[1] exact fallback used (forward, backward); [2] completion
     // counter; [3] next evaluation needs a fresh FP32 estimate; [4],[5] the
     // forward / backward solve asked for one.
@@ -554,6 +565,38 @@ extern "C" int pimdb_get_step(pimdb_handle* h, long long* step) {
     return PIMDB_OK;
 }
 
+// The exchange on beads 1 and P in two parts.  exchange_front: everything
+// up to the forces (Feldman-Hirshberg: cycle energies and the V / V_backwards
+// recursions, which give V_B; factorial: the permutation sums).
+// exchange_forces: the exterior spring forces into fx, also added into f
+// with `accumulate` (factorial: also every scalar).
+static void exchange_front(pimdb_handle* h, cudaStream_t st) {
+    const Sys& s = h->s;
+    if (h->factorial) {
+        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_factorial_sums(s, h->D, h->d_fact, st); }, 2);
+        return;
+    }
+    launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, st); });
+    const int ex = h->opt_exact_exchange;
+    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, st); }, ex ? 1 : 6);
+}
+static void exchange_forces(pimdb_handle* h, int accumulate, cudaStream_t st) {
+    const Sys& s = h->s;
+    if (h->factorial)
+        launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_factorial_finish(s, h->D, h->d_fact, accumulate, st); });
+    else
+        launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, accumulate, st); });
+}
+// All four scalars after exchange_front (and, for the factorial sum, with or
+// without exchange_forces before).
+static void exchange_scalars(pimdb_handle* h, bool forces_done, cudaStream_t st) {
+    if (h->factorial) {
+        if (!forces_done) exchange_forces(h, 0, st);
+        return;
+    }
+    launch(h, PIMDB_K_EXCH_ESTIMATORS, [&] { launch_exchange_estimators(h->s, st); });
+}
+
 // Simulation::updateForces for all beads.
 static void enqueue_forces(pimdb_handle* h) {
     const Sys& s = h->s;
@@ -573,10 +616,8 @@ static void enqueue_forces(pimdb_handle* h) {
     // stream and the finishing kernel adds them: off the critical path
     const bool fx_in_finish = s.bosonic && (cells || tiles);
     if (s.bosonic) {
-        launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, xs); });
-        const int ex = h->opt_exact_exchange;
-        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, xs); }, ex ? 1 : 6);
-        if (fx_in_finish) launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 0, xs); });
+        exchange_front(h, xs);
+        if (fx_in_finish) exchange_forces(h, 0, xs);
     }
     if (fork) cudaEventRecord(h->join_ev, h->side);
     cudaEvent_t before_finish = fork && fx_in_finish ? h->join_ev : nullptr;
@@ -598,8 +639,7 @@ static void enqueue_forces(pimdb_handle* h) {
         launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_bead_forces(s, h->D, mixed, nm ? 1 : 0, h->stream); });
     }
     if (fork && !fx_in_finish) cudaStreamWaitEvent(h->stream, h->join_ev, 0);
-    if (s.bosonic && !fx_in_finish)
-        launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 1, h->stream); });
+    if (s.bosonic && !fx_in_finish) exchange_forces(h, 1, h->stream);
 }
 
 extern "C" int pimdb_compute_forces(pimdb_handle* h) {
@@ -835,11 +875,9 @@ extern "C" int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first,
     complete_pending(h);
     const Sys& s = h->s;
     if (!s.bosonic) return fail(h, PIMDB_ERR_CONFIG, "pimdb_exchange needs a bosonic configuration with nbeads > 1");
-    launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
-    const int ex = h->opt_exact_exchange;
-    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 6);
-    launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_forces_mode(s, h->D, 0, h->stream); });
-    launch(h, PIMDB_K_EXCH_ESTIMATORS, [&] { launch_exchange_estimators(s, h->stream); });
+    exchange_front(h, h->stream);
+    exchange_forces(h, 0, h->stream);
+    exchange_scalars(h, true, h->stream);
     CUDA_TRY(h, cudaGetLastError());
     int st = check_err_word(h);
     if (st != PIMDB_OK) return st;
@@ -868,9 +906,8 @@ extern "C" int pimdb_potential_energy(pimdb_handle* h, double* terms) {
     CUDA_TRY(h, cudaMalloc((void**)&part, n * sizeof(double)));
     launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_energy_terms(s, h->D, part, h->stream); });
     if (s.bosonic) {
-        launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, h->stream); });
-        const int ex = h->opt_exact_exchange;
-        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 6);
+        exchange_front(h, h->stream);
+        if (h->factorial) exchange_scalars(h, false, h->stream);
     }
     std::vector<double> hp(n);
     cudaError_t e = cudaGetLastError();
@@ -901,10 +938,8 @@ extern "C" int pimdb_compute_observables(pimdb_handle* h, pimdb_observables* out
     CUDA_TRY(h, cudaMalloc((void**)&part, n * sizeof(double)));
     launch(h, PIMDB_K_BEAD_FORCES, [&] { launch_observable_terms(s, D, part, h->stream); });
     if (s.bosonic) {
-        launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, D, h->stream); });
-        const int ex = h->opt_exact_exchange;
-        launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, h->stream); }, ex ? 1 : 6);
-        launch(h, PIMDB_K_EXCH_ESTIMATORS, [&] { launch_exchange_estimators(s, h->stream); });
+        exchange_front(h, h->stream);
+        exchange_scalars(h, false, h->stream);
     }
     std::vector<double> hp(n);
     double sc[4] = {0.0, 0.0, 0.0, 0.0};
@@ -997,6 +1032,7 @@ extern "C" int pimdb_exchange_arrays(pimdb_handle* h, double* E_kn, double* V, d
     if (!h) return PIMDB_ERR_ARG;
     const Sys& s = h->s;
     if (!s.bosonic) return fail(h, PIMDB_ERR_CONFIG, "no exchange arrays for a distinguishable configuration");
+    if (h->factorial) return fail(h, PIMDB_ERR_CONFIG, "the factorial exchange has no cycle energies or recursions");
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     if (E_kn) CUDA_TRY(h, cudaMemcpy(E_kn, s.E, (size_t)s.N * (s.N + 1) / 2 * sizeof(double), cudaMemcpyDeviceToHost));
     if (V) CUDA_TRY(h, cudaMemcpy(V, s.V, (size_t)(s.N + 1) * sizeof(double), cudaMemcpyDeviceToHost));

@@ -56,6 +56,17 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st);
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st);
 void launch_exchange_estimators(const Sys& s, cudaStream_t st);
 
+// factorial.cu: the factorial exchange (sum over all N! permutations) on
+// beads 1 and P, for at most kFactMaxN particles.  launch_factorial_sums
+// (2 kernels) fills `work` (factorial_work_doubles(N) doubles);
+// launch_factorial_finish then writes the scalars (V_B, primEstimator, 0, 0)
+// and the exterior spring forces into fx (and adds them into f with
+// `accumulate`).
+constexpr int kFactMaxN = 12;
+size_t factorial_work_doubles(int N);
+int launch_factorial_sums(const Sys& s, int D, double* work, cudaStream_t st);
+void launch_factorial_finish(const Sys& s, int D, double* work, int accumulate, cudaStream_t st);
+
 // Nose-Hoover chains: parameters of one thermostat (constructors of
 // src/thermostats/nose_hoover.cpp) and its chain state, [chains][nchains]
 // each.  variant 0: a chain per bead, 1: per bead and particle, 2: per

@@ -413,9 +413,11 @@ protected:
     std::vector<double> f_first_, f_last_;
 };
 
-class BosonicExchange final : public BosonicExchangeBase {  // Feldman-Hirshberg, on the GPU
+// Both algorithms run on the GPU behind pimdb_exchange; the engine's
+// configuration (pimdb_config::exchange) selects which.
+class DeviceBosonicExchange : public BosonicExchangeBase {
 public:
-    explicit BosonicExchange(Engine& e) : BosonicExchangeBase(e) {}
+    explicit DeviceBosonicExchange(Engine& e) : BosonicExchangeBase(e) {}
     void prepare() override {
         const auto& c = e_.config();
         f_first_.assign((size_t)c.natoms * c.ndim, 0.0);
@@ -429,6 +431,17 @@ public:
 
 private:
     std::array<double, 4> scal_{};
+};
+// Feldman-Hirshberg (quadratic_bosonic_exchange.cpp)
+class BosonicExchange final : public DeviceBosonicExchange {
+public:
+    using DeviceBosonicExchange::DeviceBosonicExchange;
+};
+// Sum over all N! permutations (factorial_bosonic_exchange.cpp); its
+// getDistinctProbability and getLongestProbability are 0 as there.
+class FactorialBosonicExchange final : public DeviceBosonicExchange {
+public:
+    using DeviceBosonicExchange::DeviceBosonicExchange;
 };
 
 // ------------------------------------------------------ propagator, thermostat
@@ -493,7 +506,13 @@ class Simulation {
 public:
     explicit Simulation(Params& params, void* stream = nullptr) : cfg(params.config), run_params(params.run) {
         engine = std::make_unique<Engine>(cfg, stream);
-        if (cfg.bosonic && cfg.nbeads > 1) bosonic_exchange = std::make_unique<BosonicExchange>(*engine);
+        // Simulation::initializeExchangeAlgorithm (src/simulation.cpp:687-698)
+        if (cfg.bosonic && cfg.nbeads > 1) {
+            if (cfg.exchange == PIMDB_EXCHANGE_FACTORIAL)
+                bosonic_exchange = std::make_unique<FactorialBosonicExchange>(*engine);
+            else
+                bosonic_exchange = std::make_unique<BosonicExchange>(*engine);
+        }
         if (cfg.propagator == PIMDB_PROP_NORMAL_MODES) propagator = std::make_unique<NormalModesPropagator>(*engine);
         else propagator = std::make_unique<VelocityVerletPropagator>(*engine);
         // Simulation::initializeThermostat (src/simulation.cpp:667-684)

@@ -4,7 +4,7 @@
 // the observables to output/simulation.out in the reference's format.
 //
 //   pimdb_gb300 [-in config.ini] [--dim N] [--check] [--plugin-steps]
-//               [--steps K] [--positions out.xyz]
+//               [--steps K] [--positions out.xyz] [--factorial] [--bosonic_alg]
 //
 //   --check          parse and validate the configuration only (no GPU)
 //   --plugin-steps   drive the step through the plugin objects one call at a
@@ -13,6 +13,11 @@
 //   --positions F    write the final positions of every bead (xyz, angstrom)
 //   --initial F      with --check: write the initial positions and momenta
 //                    (raw doubles, [bead][particle][axis], atomic units)
+//   --factorial      bosonic exchange by the sum over all N! permutations
+//                    (the reference's FACTORIAL_BOSONIC_ALGORITHM build)
+//                    instead of the Feldman-Hirshberg recursion
+//   --bosonic_alg    print which bosonic algorithm is selected and exit
+//                    (src/pimdb.cpp:12-17)
 //
 // Configuration errors are printed as "[X] Invalid argument error: ..." and,
 // as in the reference, the process still exits 0; CUDA errors exit 1.
@@ -30,7 +35,7 @@
 int main(int argc, char** argv) {
     std::string config = "config.ini", positions, initial;
     int ndim = 3;
-    bool check_only = false, plugin = false;
+    bool check_only = false, plugin = false, factorial = false, show_alg = false;
     long steps_override = -1;
     for (int i = 1; i < argc; ++i) {
         if (!std::strcmp(argv[i], "-in") && i + 1 < argc) config = argv[++i];
@@ -40,15 +45,23 @@ int main(int argc, char** argv) {
         else if (!std::strcmp(argv[i], "--steps") && i + 1 < argc) steps_override = std::atol(argv[++i]);
         else if (!std::strcmp(argv[i], "--positions") && i + 1 < argc) positions = argv[++i];
         else if (!std::strcmp(argv[i], "--initial") && i + 1 < argc) initial = argv[++i];
+        else if (!std::strcmp(argv[i], "--factorial")) factorial = true;
+        else if (!std::strcmp(argv[i], "--bosonic_alg")) show_alg = true;
+    }
+    if (show_alg) {
+        std::cout << (factorial ? "Running with naive bosonic algorithm.\n" : "Running with quadratic bosonic algorithm.\n");
+        return 0;
     }
     try {
         std::cout << "[*] Initializing the simulation parameters\n";
         pimdb_gb300::Params params(config, ndim);
         if (steps_override >= 0) params.run.steps = steps_override;
+        if (factorial) params.config.exchange = PIMDB_EXCHANGE_FACTORIAL;
         if (check_only) {
             const auto& c = params.config;
-            std::printf("[*] natoms=%d nbeads=%d ndim=%d bosonic=%d propagator=%d thermostat=%d steps=%ld\n", c.natoms,
-                        c.nbeads, c.ndim, c.bosonic, c.propagator, c.thermostat, params.run.steps);
+            std::printf("[*] natoms=%d nbeads=%d ndim=%d bosonic=%d propagator=%d thermostat=%d steps=%ld exchange=%s\n",
+                        c.natoms, c.nbeads, c.ndim, c.bosonic, c.propagator, c.thermostat, params.run.steps,
+                        c.exchange == PIMDB_EXCHANGE_FACTORIAL ? "factorial" : "feldman_hirshberg");
             if (!initial.empty()) {
                 std::vector<double> x, p;
                 pimdb_host::initial_state(params.config, params.run, x, p, true);

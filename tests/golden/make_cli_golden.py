@@ -34,19 +34,32 @@ CASES = {
         "external_potential": {"name": "harmonic", "omega": "2.0 millielectronvolt"},
         "observables": {"energy": "millielectronvolt", "classical": "kelvin", "gsf": "kelvin"},
     },
+    "nve_bosons_factorial_trap": {
+        "simulation": {"dt": "1.0 femtosecond", "steps": 40, "sfreq": 5, "threshold": 0.0, "nbeads": 4,
+                       "bosonic": "true", "fixcom": "true", "pbc": "false", "seed": 515, "thermostat": "none",
+                       "initial_position": "random", "initial_velocity": "random", "propagator": "cartesian"},
+        "system": {"temperature": "2.0 kelvin", "natoms": 5, "size": "8 angstrom", "mass": "1.0 dalton"},
+        "interaction_potential": {"name": "harmonic", "omega": "1.0 millielectronvolt"},
+        "external_potential": {"name": "harmonic", "omega": "3.0 millielectronvolt"},
+        "observables": {"energy": "kelvin", "classical": "kelvin", "bosonic": "on"},
+    },
 }
+# Cases run by another build of the reference, with the driver flags that
+# select the same algorithm (written to <case>/args).
+VARIANTS = {"nve_bosons_factorial_trap": ("d3_fact", ["--factorial"])}
 
 
 def main():
-    if not R.available("d3"):
+    if not (R.available("d3") and R.available("d3_fact")):
         raise SystemExit("compiled reference not built (python oracle/build_ref.py)")
     for name, sec in CASES.items():
+        variant, args = VARIANTS.get(name, ("d3", []))
         td = Path(tempfile.mkdtemp(prefix="pimdb_cli_golden_"))
         try:
             R.write_ini(td / "config.ini", sec)
             P = int(sec["simulation"]["nbeads"])
             env = dict(os.environ, PIMDB_SHIM_NP=str(P), PIMDB_SHIM_TIMEOUT="120")
-            r = subprocess.run([str(R.REF / "pimdb_d3"), "-in", "config.ini"], cwd=td, env=env,
+            r = subprocess.run([str(R.REF / f"pimdb_{variant}"), "-in", "config.ini"], cwd=td, env=env,
                                capture_output=True, text=True, timeout=300)
             if r.returncode != 0 or "[X]" in r.stdout:
                 raise SystemExit(f"{name}: reference run failed\n{r.stdout}\n{r.stderr}")
@@ -54,6 +67,8 @@ def main():
             out.mkdir(parents=True, exist_ok=True)
             shutil.copy(td / "config.ini", out / "config.ini")
             shutil.copy(td / "output" / "simulation.out", out / "simulation.out")
+            if args:
+                (out / "args").write_text(" ".join(args) + "\n")
             print(name, (out / "simulation.out").read_text().count("\n"), "lines")
         finally:
             shutil.rmtree(td, ignore_errors=True)

@@ -19,17 +19,18 @@ FS = 4.1341373e16 * 1e-15  # include/units.h:76 with the femto prefix
 def case(ndim=3, natoms=8, nbeads=4, T_K=1.0, mass_amu=1.0, bosonic=True, pbc=False, box_ang=10.0,
          ext="free", ext_p=(0.0, 0.0, 0.0), inter="free", int_p=(0.0, 0.0, 0.0), cutoff_ang=-1.0,
          propagator="cartesian", thermostat="langevin", nmthermostat=False, fixcom=True, dt_fs=1.0, gamma=-1.0,
-         precision="fp64", seed=12345):
+         precision="fp64", seed=12345, exchange="feldman_hirshberg"):
     p = dict(ndim=ndim, natoms=natoms, nbeads=nbeads, temperature=T_K * KELVIN, mass=mass_amu * DALTON,
              bosonic=bosonic, pbc=pbc, size=box_ang * ANG, ext=ext, ext_p=tuple(ext_p), interaction=inter,
              int_p=tuple(int_p), cutoff=cutoff_ang * ANG, propagator=propagator, thermostat=thermostat,
              nmthermostat=nmthermostat, fixcom=fixcom, dt=dt_fs * FS, gamma=gamma)
-    s = O.make_system(**p)
+    s = O.make_system(**p, factorial=exchange == "factorial")
     cfg = pk.make_config(ndim=ndim, natoms=natoms, nbeads=nbeads, bosonic=int(bosonic), pbc=int(pbc),
                          fixcom=int(fixcom), propagator=propagator, thermostat=thermostat,
                          nmthermostat=int(nmthermostat), precision=precision, temperature=p["temperature"],
                          mass=p["mass"], size=p["size"], dt=p["dt"], gamma=gamma, ext_kind=ext, ext_params=ext_p,
-                         int_kind=inter, int_params=int_p, cutoff=p["cutoff"], seed=seed, replica=0)
+                         int_kind=inter, int_params=int_p, cutoff=p["cutoff"], seed=seed, replica=0,
+                         exchange=exchange)
     return s, cfg
 
 

@@ -67,9 +67,22 @@ def test_cli_check_reports_configuration(tmp_path):
     r = _cli(["-in", "c.ini", "--check"], tmp_path)
     assert r.returncode == 0
     assert "natoms=6 nbeads=4 ndim=3 bosonic=1 propagator=0 thermostat=1 steps=17" in r.stdout
+    assert "exchange=feldman_hirshberg" in r.stdout
+    r = _cli(["-in", "c.ini", "--check", "--factorial"], tmp_path)
+    assert r.returncode == 0 and "exchange=factorial" in r.stdout
 
 
-@pytest.mark.parametrize("key,value,message", [("thermostat", "berendsen", "is not supported"),
+def test_cli_bosonic_alg_reports_the_selected_algorithm(tmp_path):
+    # src/pimdb.cpp:12-17: print the algorithm and run nothing
+    _need_cli()
+    r = _cli(["--bosonic_alg"], tmp_path)
+    assert r.returncode == 0 and r.stdout.strip() == "Running with quadratic bosonic algorithm."
+    r = _cli(["--factorial", "--bosonic_alg"], tmp_path)
+    assert r.returncode == 0 and r.stdout.strip() == "Running with naive bosonic algorithm."
+    assert not (tmp_path / "output").exists()
+
+
+@pytest.mark.parametrize("key,value,message",[("thermostat", "berendsen", "is not supported"),
                                                ("propagator", "normal_modes", "not available for bosons")])
 def test_cli_configuration_error_is_reported_like_the_reference(key, value, message, tmp_path):
     _need_cli()
@@ -190,7 +203,8 @@ def test_cli_simulation_out_matches_reference(name, tmp_path):
     same rows (tests/golden/make_cli_golden.py ran the compiled reference)."""
     _need_cli()
     shutil.copy(GOLDEN_CLI / name / "config.ini", tmp_path / "config.ini")
-    r = _cli(["-in", "config.ini"], tmp_path)
+    extra = GOLDEN_CLI / name / "args"  # flags selecting the reference build's algorithm
+    r = _cli(["-in", "config.ini", *(extra.read_text().split() if extra.exists() else [])], tmp_path)
     assert r.returncode == 0 and "[X]" not in r.stdout, r.stdout + r.stderr
     cols, got = _read_out(tmp_path / "output" / "simulation.out")
     want_cols, want = _read_out(GOLDEN_CLI / name / "simulation.out")
