@@ -65,6 +65,18 @@ enum pimdb_thermostat {
  * partition function.  The factorial sum is FP64 in both precisions and
  * reports P_distinct = P_longest = 0 as the reference does. */
 enum pimdb_exchange_algorithm { PIMDB_EXCHANGE_FELDMAN_HIRSHBERG = 0, PIMDB_EXCHANGE_FACTORIAL = 1 };
+/* Langevin noise.  PIMDB_RNG_PHILOX: counter-based Philox4x32-10 normals,
+ * a pure function of (seed, replica, step, degree of freedom), so any step
+ * can be replayed (pimdb_set_step) and graphs need no state.
+ * PIMDB_RNG_RANMAR: the reference's own streams, one RanMars per bead seeded
+ * seed + bead (src/simulation.cpp:54-59, libs/random_mars.cpp), drawn in the
+ * reference's order (src/thermostats/langevin.cpp:15-27), so trajectories
+ * follow the reference's from the same initial state.  The streams advance
+ * with every MD step and are not rewound by pimdb_set_step or
+ * pimdb_set_state; each bead's seed must lie in 1..900000000 as the
+ * reference requires.  Drawing is sequential per bead: a parity mode, not a
+ * fast path. */
+enum pimdb_rng { PIMDB_RNG_PHILOX = 0, PIMDB_RNG_RANMAR = 1 };
 /* Arithmetic of the pair forces: FP64 throughout, or FP32 pair arithmetic
  * with FP64 per-atom accumulation.  Exchange and integrator are FP64 in both. */
 enum pimdb_precision { PIMDB_FP64 = 0, PIMDB_MIXED = 1 };
@@ -96,6 +108,7 @@ typedef struct pimdb_config {
     unsigned int replica;     /* folded into the noise counter */
     int nchains;              /* [simulation] nchains: Nose-Hoover chain length */
     int exchange;             /* enum pimdb_exchange_algorithm */
+    int rng;                  /* enum pimdb_rng */
 } pimdb_config;
 
 typedef struct pimdb_handle pimdb_handle;

@@ -23,6 +23,7 @@ PROP = {"cartesian": 0, "normal_modes": 1}
 THERMO = {"none": 0, "langevin": 1, "nose_hoover": 2, "nose_hoover_np": 3, "nose_hoover_np_dim": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 EXCHANGE = {"feldman_hirshberg": 0, "factorial": 1}
+RNG = {"philox": 0, "ranmars": 1}
 
 EXPORTS = [
     "pimdb_config_default", "pimdb_config_from_ini", "pimdb_create", "pimdb_destroy", "pimdb_set_state",
@@ -50,6 +51,7 @@ class Config(C.Structure):
         ("dt", C.c_double), ("gamma", C.c_double), ("ext_kind", C.c_int), ("ext_params", C.c_double * 3),
         ("int_kind", C.c_int), ("int_params", C.c_double * 3), ("cutoff", C.c_double),
         ("seed", C.c_ulonglong), ("replica", C.c_uint), ("nchains", C.c_int), ("exchange", C.c_int),
+        ("rng", C.c_int),
     ]
 
 
@@ -183,8 +185,8 @@ def config_from_ini(path, ndim: int = 3) -> Config:
 
 def make_config(**kw) -> Config:
     """Builds a config from keyword arguments (atomic units); potential,
-    propagator, thermostat, precision and exchange algorithm may be given by
-    name."""
+    propagator, thermostat, precision, exchange algorithm and noise generator
+    may be given by name."""
     c = default_config()
     for k, v in kw.items():
         if k in ("ext_kind", "int_kind") and isinstance(v, str):
@@ -197,6 +199,8 @@ def make_config(**kw) -> Config:
             v = PRECISION[v]
         elif k == "exchange" and isinstance(v, str):
             v = EXCHANGE[v]
+        elif k == "rng" and isinstance(v, str):
+            v = RNG[v]
         if k in ("ext_params", "int_params"):
             arr = getattr(c, k)
             for i, x in enumerate(v):

@@ -69,6 +69,9 @@ struct pimdb_handle {
     // factorial exchange (sum over all N! permutations): its work buffer
     bool factorial = false;
     double* d_fact = nullptr;
+    // RanMars parity noise: the streams and the staged normals (Sys::noise)
+    RanMarsState* d_rng = nullptr;
+    double* d_noise = nullptr;
     // CUDA graphs of pimdb_step_async: keyed by the step count and the
     // host-side step state at entry; the step index comes from d_step, which
     // every graph advances by its step count
@@ -220,6 +223,10 @@ std::string validate_config(const pimdb_config& c) {
         return "unknown bosonic exchange algorithm";
     if (c.exchange == PIMDB_EXCHANGE_FACTORIAL && c.bosonic && c.nbeads > 1 && c.natoms > kFactMaxN)
         return "the factorial bosonic exchange supports at most " + std::to_string(kFactMaxN) + " particles";
+    if (c.rng != PIMDB_RNG_PHILOX && c.rng != PIMDB_RNG_RANMAR) return "unknown noise generator";
+    // RanMars(params_seed + rank) for every bead (simulation.cpp:59, random_mars.cpp:16-17)
+    if (c.rng == PIMDB_RNG_RANMAR && (c.seed < 1 || c.seed + (unsigned long long)c.nbeads - 1 > 900000000ull))
+        return "Invalid seed for Marsaglia random # generator";
     return "";
 }
 
@@ -322,6 +329,8 @@ static void free_handle(pimdb_handle* h) {
     if (h->d_cells) cudaFree(h->d_cells);
     if (h->d_nh) cudaFree(h->d_nh);
     if (h->d_fact) cudaFree(h->d_fact);
+    if (h->d_rng) cudaFree(h->d_rng);
+    if (h->d_noise) cudaFree(h->d_noise);
     if (h->d_pnm) cudaFree(h->d_pnm);
     if (h->d_step) cudaFree(h->d_step);
     drop_graphs(h);
@@ -395,6 +404,16 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     h->factorial = s.bosonic && c.exchange == PIMDB_EXCHANGE_FACTORIAL;
     if (e == cudaSuccess && h->factorial)
         e = cudaMalloc((void**)&h->d_fact, factorial_work_doubles(s.N) * sizeof(double));
+    if (e == cudaSuccess && c.rng == PIMDB_RNG_RANMAR && c.thermostat == PIMDB_THERMO_LANGEVIN) {
+        std::vector<RanMarsState> st((size_t)s.P);
+        for (int b = 0; b < s.P; ++b) ranmars_seed((int)(c.seed + (unsigned long long)b), st[b]);
+        e = cudaMalloc((void**)&h->d_rng, st.size() * sizeof(RanMarsState));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->d_rng, st.data(), st.size() * sizeof(RanMarsState), cudaMemcpyHostToDevice);
+        // [step parity][substep][bead][axis][ld], plus one row of padding
+        if (e == cudaSuccess) e = alloc(&h->d_noise, ((size_t)4 * s.P * h->D + 1) * s.ld);
+        s.noise = h->d_noise;
+    }
     // xflags: [0],[1] exact fallback used (forward, backward); [2] completion
     // counter; [3] next evaluation needs a fresh FP32 estimate; [4],[5] the
     // forward / backward solve asked for one.
@@ -692,6 +711,15 @@ static void nose_hoover(pimdb_handle* h) {
     }, nmc ? 3 : 1);
 }
 
+// RanMars parity noise: both O-steps' normals of MD step h->step, from the
+// streams' current positions (the previous step's stay in the other half).
+static void draw_noise(pimdb_handle* h) {
+    if (!h->d_noise) return;
+    launch(h, PIMDB_K_CART_UPDATE, [&] {
+        launch_ranmars_draw(h->s, h->D, h->d_rng, h->d_noise, step_ref(h, h->step), h->stream);
+    });
+}
+
 static void thermostat_step(pimdb_handle* h, int substep) {
     const pimdb_config& c = h->cfg;
     const int part = c.fixcom ? SF_COM_PARTIAL : 0;
@@ -715,6 +743,7 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
     const bool nm = c.propagator == PIMDB_PROP_NORMAL_MODES;
     const bool cart_langevin = c.thermostat == PIMDB_THERMO_LANGEVIN && !c.nmthermostat;
     for (int it = 0; it < nsteps; ++it) {
+        draw_noise(h);
         // O, [COM] (inside the fused normal-mode kernel when that is used)
         if (!(nm && h->fused_nm)) thermostat_step(h, 0);
         if (!nm) {
@@ -1127,6 +1156,7 @@ extern "C" int pimdb_thermostat_step(pimdb_handle* h, int substep) {
     if (!h || substep < 0 || substep > 1) return PIMDB_ERR_ARG;
     const pimdb_config& c = h->cfg;
     complete_pending(h);  // finish the previous step's deferred work first
+    if (substep == 0) draw_noise(h);  // the step's normals, as the reference draws them
     if (c.thermostat >= PIMDB_THERMO_NOSE_HOOVER) nose_hoover(h);
     else if (c.thermostat == PIMDB_THERMO_LANGEVIN && c.nmthermostat) nm_thermo(h, 0, substep);
     else if (c.thermostat == PIMDB_THERMO_LANGEVIN) cart(h, SF_LANGEVIN, substep, 0);

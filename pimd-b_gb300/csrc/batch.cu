@@ -526,6 +526,9 @@ extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void*
                          "replica " + std::to_string(r) +
                              ": the batched engine runs the cartesian propagator with the cartesian Langevin thermostat");
         if (c.natoms > 2048) return bfail(nullptr, PIMDB_ERR_CONFIG, "the batched engine supports at most 2048 particles per replica");
+        if (c.rng != PIMDB_RNG_PHILOX)
+            return bfail(nullptr, PIMDB_ERR_CONFIG,
+                         "replica " + std::to_string(r) + ": the batched engine draws counter-based (Philox) noise");
         if (c.exchange != PIMDB_EXCHANGE_FELDMAN_HIRSHBERG && c.bosonic && c.nbeads > 1)
             return bfail(nullptr, PIMDB_ERR_CONFIG,
                          "replica " + std::to_string(r) + ": the batched engine runs the Feldman-Hirshberg exchange");

@@ -71,6 +71,11 @@ struct Sys {
     double* rowR;   // per-row factors exp(-beta (Vh[l+1] + Vb[l+1] - V[N])), N
     double* rowC;   // cut probabilities exp(-beta (V[l+1] + Vb[l+1] - V[N])), N
     int* xflags;    // [0] forward used the exact fallback, [1] backward, [2] completion counter
+    // Langevin normals drawn by the reference's RanMars streams (one per
+    // bead, seeded seed + bead) for the current and the previous MD step:
+    // [t & 3][bead-or-mode][axis][ld] with t = 2 step + substep.  Null when
+    // the noise is the counter-based Philox stream.
+    const double* noise;
 };
 
 // MD step index of a launch: `off`, plus the value at `base` when the launch
@@ -165,6 +170,18 @@ __device__ __forceinline__ double2 philox_normal_pair(uint64_t seed, uint32_t re
     double sn, cs;
     sincos(6.283185307179586 * u2, &sn, &cs);
     return make_double2(r * cs, r * sn);
+}
+
+// The two Langevin normals of (bead-or-mode k, axis a, particles 2 i2 and
+// 2 i2 + 1) at noise counter t = 2 step + substep (half = ceil(N / 2)): the
+// Philox pair, or the RanMars streams' normals staged in s.noise.
+template <int D>
+__device__ __forceinline__ double2 langevin_pair(const Sys& s, uint64_t t, int k, int a, int i2, int half) {
+    if (s.noise) {
+        const double* z = s.noise + (((size_t)(t & 3) * s.P + k) * D + a) * s.ld + 2 * i2;
+        return make_double2(z[0], z[1]);
+    }
+    return philox_normal_pair(s.seed, s.replica, t, (uint32_t)((size_t)(k * D + a) * half + i2));
 }
 
 }  // namespace pimdb

@@ -96,8 +96,7 @@ __global__ void k_cart_update(Sys s, int flags, const double* __restrict__ red_i
         const int b = ba / D;
         double2 z = make_double2(0.0, 0.0);
         if (flags & SF_LANGEVIN)
-            z = philox_normal_pair(s.seed, s.replica, 2ull * (unsigned long long)step + substep,
-                                   (uint32_t)((size_t)ba * half + i2));
+            z = langevin_pair<D>(s, 2ull * (unsigned long long)step + substep, b, a, i2, half);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int i = 2 * i2 + h;
@@ -160,7 +159,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_thermo(Sys s, const double* _
             q1 += c * sp[b * kNmTile + 2 * pp + 1];
         }
         const int ie = i0 + 2 * pp;
-        const double2 z = philox_normal_pair(s.seed, s.replica, t, (uint32_t)((size_t)(k * D + a) * half + (ie >> 1)));
+        const double2 z = langevin_pair<D>(s, t, k, a, ie >> 1, half);
         sq[k * kNmTile + 2 * pp] = s.c1 * q0 + s.c2 * z.x;
         sq[k * kNmTile + 2 * pp + 1] = s.c1 * q1 + s.c2 * z.y;
     }
@@ -516,8 +515,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
         for (int k = g; k < P; k += kNmGroups) {
             const int o = k * kNmTile + 2 * pp;
             const int ie = i0 + 2 * pp;
-            const double2 z =
-                philox_normal_pair(s.seed, s.replica, t, (uint32_t)((size_t)(k * D + a) * half + (ie >> 1)));
+            const double2 z = langevin_pair<D>(s, t, k, a, ie >> 1, half);
             sq[o] = s.c1 * sq[o] + s.c2 * z.x;
             sq[o + 1] = s.c1 * sq[o + 1] + s.c2 * z.y;
         }
@@ -863,6 +861,125 @@ void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, 
     if (D == 1) nm_prop_launch<1>(s, C, T, rot, com_apply, red_in, nred_in, st);
     else if (D == 2) nm_prop_launch<2>(s, C, T, rot, com_apply, red_in, nred_in, st);
     else nm_prop_launch<3>(s, C, T, rot, com_apply, red_in, nred_in, st);
+}
+
+}  // namespace pimdb
+
+// ---------------------------------------------------------------------------
+// RanMars parity noise: the reference's Langevin noise (langevin.cpp:15-27
+// draws sim.mars_gen->gaussian() per particle and axis; one RanMars stream
+// per bead rank, seeded seed + rank, simulation.cpp:54-59).  RANMAR is a
+// lagged-Fibonacci generator (Marsaglia, Zaman & Tsang; F. James, Comp. Phys.
+// Comm. 60, 329 (1990), as in libs/random_mars.cpp) with Marsaglia's polar
+// Gaussian; each stream is sequential, so one thread per stream draws the
+// step's 2 N D normals into s.noise.  Not a fast path: it exists to replay
+// the reference's Langevin trajectories.
+namespace pimdb {
+
+void ranmars_seed(int seed, RanMarsState& r) {
+    // libs/random_mars.cpp:11-47 (seed checked by the caller)
+    r = RanMarsState{};
+    int ij = (seed - 1) / 30082;
+    int kl = (seed - 1) - 30082 * ij;
+    int i = (ij / 177) % 177 + 2, j = ij % 177 + 2, k = (kl / 169) % 178 + 1, l = kl % 169;
+    for (int n = 1; n <= 97; ++n) {
+        double acc = 0.0, bit = 0.5;
+        for (int b = 0; b < 24; ++b) {
+            const int m = ((i * j) % 179) * k % 179;
+            i = j;
+            j = k;
+            k = m;
+            l = (53 * l + 1) % 169;
+            if ((l * m) % 64 >= 32) acc = acc + bit;
+            bit = 0.5 * bit;
+        }
+        r.u[n] = acc;
+    }
+    r.c = 362436.0 / 16777216.0;
+    r.cd = 7654321.0 / 16777216.0;
+    r.cm = 16777213.0 / 16777216.0;
+    r.i97 = 97;
+    r.j97 = 33;
+    // the constructor draws one uniform (random_mars.cpp:46)
+    double uni = r.u[r.i97] - r.u[r.j97];
+    if (uni < 0.0) uni += 1.0;
+    r.u[r.i97] = uni;
+    if (--r.i97 == 0) r.i97 = 97;
+    if (--r.j97 == 0) r.j97 = 97;
+    r.c -= r.cd;
+    if (r.c < 0.0) r.c += r.cm;
+}
+
+namespace {
+
+// RanMars::uniform (random_mars.cpp:59-78) on a stream held in shared memory.
+__device__ double ranmars_uniform(RanMarsState& r) {
+    double uni = __dsub_rn(r.u[r.i97], r.u[r.j97]);
+    if (uni < 0.0) uni = __dadd_rn(uni, 1.0);
+    r.u[r.i97] = uni;
+    if (--r.i97 == 0) r.i97 = 97;
+    if (--r.j97 == 0) r.j97 = 97;
+    r.c = __dsub_rn(r.c, r.cd);
+    if (r.c < 0.0) r.c = __dadd_rn(r.c, r.cm);
+    uni = __dsub_rn(uni, r.c);
+    if (uni < 0.0) uni = __dadd_rn(uni, 1.0);
+    return uni;
+}
+
+// RanMars::gaussian (random_mars.cpp:84-103): the polar method, the second
+// variate of each accepted pair kept for the next call.  Products and sums
+// are rounded separately (no contraction), so the acceptance test sees the
+// same rsq as the reference's.
+__device__ double ranmars_gaussian(RanMarsState& r) {
+    if (r.save) {
+        r.save = 0;
+        return r.second;
+    }
+    double v1, v2, rsq;
+    int tries = 0;
+    do {
+        v1 = __dsub_rn(__dmul_rn(2.0, ranmars_uniform(r)), 1.0);
+        v2 = __dsub_rn(__dmul_rn(2.0, ranmars_uniform(r)), 1.0);
+        rsq = __dadd_rn(__dmul_rn(v1, v1), __dmul_rn(v2, v2));
+    } while ((rsq >= 1.0 || rsq == 0.0) && ++tries < (1 << 20));
+    const double fac = sqrt(__ddiv_rn(__dmul_rn(-2.0, log(rsq)), rsq));
+    r.second = __dmul_rn(v1, fac);
+    r.save = 1;
+    return __dmul_rn(v2, fac);
+}
+
+// One block per stream (bead): lane 0 draws both O-steps' normals of the
+// current MD step into the step-parity half of `noise`, in the reference's
+// order (particle-major, then axis).
+template <int D>
+__global__ void k_ranmars_draw(Sys s, RanMarsState* __restrict__ states, double* __restrict__ noise, StepRef sref) {
+    __shared__ RanMarsState r;
+    const int b = blockIdx.x;
+    const int words = (int)(sizeof(RanMarsState) / sizeof(double));
+    double* sh = reinterpret_cast<double*>(&r);
+    const double* g = reinterpret_cast<const double*>(states + b);
+    for (int w = threadIdx.x; w < words; w += blockDim.x) sh[w] = g[w];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const long long step = sref.get();
+        for (int o = 0; o < 2; ++o) {
+            double* out = noise + ((size_t)((step & 1) * 2 + o) * s.P + b) * D * s.ld;
+            for (int i = 0; i < s.N; ++i)
+#pragma unroll
+                for (int a = 0; a < D; ++a) out[(size_t)a * s.ld + i] = ranmars_gaussian(r);
+        }
+    }
+    __syncthreads();
+    double* gw = reinterpret_cast<double*>(states + b);
+    for (int w = threadIdx.x; w < words; w += blockDim.x) gw[w] = sh[w];
+}
+
+}  // namespace
+
+void launch_ranmars_draw(const Sys& s, int D, RanMarsState* states, double* noise, StepRef step, cudaStream_t st) {
+    if (D == 1) k_ranmars_draw<1><<<s.P, 32, 0, st>>>(s, states, noise, step);
+    else if (D == 2) k_ranmars_draw<2><<<s.P, 32, 0, st>>>(s, states, noise, step);
+    else k_ranmars_draw<3><<<s.P, 32, 0, st>>>(s, states, noise, step);
 }
 
 }  // namespace pimdb

@@ -67,6 +67,18 @@ size_t factorial_work_doubles(int N);
 int launch_factorial_sums(const Sys& s, int D, double* work, cudaStream_t st);
 void launch_factorial_finish(const Sys& s, int D, double* work, int accumulate, cudaStream_t st);
 
+// RanMars parity noise (integrator.cu): one RanMars stream per bead,
+// seeded on the host (ranmars_seed: seed in 1..900000000), drawn on the
+// device into Sys::noise at the start of each MD step.
+struct RanMarsState {
+    double u[98];
+    double c, cd, cm, second;
+    int i97, j97, save, pad;
+};
+static_assert(sizeof(RanMarsState) % sizeof(double) == 0, "RanMarsState is copied as doubles");
+void ranmars_seed(int seed, RanMarsState& r);
+void launch_ranmars_draw(const Sys& s, int D, RanMarsState* states, double* noise, StepRef step, cudaStream_t st);
+
 // Nose-Hoover chains: parameters of one thermostat (constructors of
 // src/thermostats/nose_hoover.cpp) and its chain state, [chains][nchains]
 // each.  variant 0: a chain per bead, 1: per bead and particle, 2: per

@@ -5,6 +5,7 @@
 //
 //   pimdb_gb300 [-in config.ini] [--dim N] [--check] [--plugin-steps]
 //               [--steps K] [--positions out.xyz] [--factorial] [--bosonic_alg]
+//               [--ranmars]
 //
 //   --check          parse and validate the configuration only (no GPU)
 //   --plugin-steps   drive the step through the plugin objects one call at a
@@ -18,6 +19,10 @@
 //                    instead of the Feldman-Hirshberg recursion
 //   --bosonic_alg    print which bosonic algorithm is selected and exit
 //                    (src/pimdb.cpp:12-17)
+//   --ranmars        Langevin noise from the reference's RanMars streams
+//                    (seed + bead, drawn per particle and axis) instead of the
+//                    counter-based Philox stream: with the reference's initial
+//                    state this follows the reference's own trajectory
 //
 // Configuration errors are printed as "[X] Invalid argument error: ..." and,
 // as in the reference, the process still exits 0; CUDA errors exit 1.
@@ -35,7 +40,7 @@
 int main(int argc, char** argv) {
     std::string config = "config.ini", positions, initial;
     int ndim = 3;
-    bool check_only = false, plugin = false, factorial = false, show_alg = false;
+    bool check_only = false, plugin = false, factorial = false, show_alg = false, ranmars = false;
     long steps_override = -1;
     for (int i = 1; i < argc; ++i) {
         if (!std::strcmp(argv[i], "-in") && i + 1 < argc) config = argv[++i];
@@ -47,6 +52,7 @@ int main(int argc, char** argv) {
         else if (!std::strcmp(argv[i], "--initial") && i + 1 < argc) initial = argv[++i];
         else if (!std::strcmp(argv[i], "--factorial")) factorial = true;
         else if (!std::strcmp(argv[i], "--bosonic_alg")) show_alg = true;
+        else if (!std::strcmp(argv[i], "--ranmars")) ranmars = true;
     }
     if (show_alg) {
         std::cout << (factorial ? "Running with naive bosonic algorithm.\n" : "Running with quadratic bosonic algorithm.\n");
@@ -57,6 +63,7 @@ int main(int argc, char** argv) {
         pimdb_gb300::Params params(config, ndim);
         if (steps_override >= 0) params.run.steps = steps_override;
         if (factorial) params.config.exchange = PIMDB_EXCHANGE_FACTORIAL;
+        if (ranmars) params.config.rng = PIMDB_RNG_RANMAR;
         if (check_only) {
             const auto& c = params.config;
             std::printf("[*] natoms=%d nbeads=%d ndim=%d bosonic=%d propagator=%d thermostat=%d steps=%ld exchange=%s\n",

@@ -244,6 +244,49 @@ def test_cli_replays_nose_hoover_regression_cases(case, tmp_path):
             assert np.abs(mine - gold[k]).max() <= 1e-6 * scale + (1e-300 if scale else 0.0), (stem, k)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["bosonic_factorial_harmonic", "bosonic_factorial_harmonic_dynamics",
+                                  "bosonic_quadratic_harmonic", "bosonic_quadratic_harmonic_dynamics",
+                                  "bosonic_quadratic_harmonic_gsf", "bosonic_quadratic_harmonic_nmthermostat_dynamics",
+                                  "dist_harmonic", "dist_harmonic_dynamics", "dist_harmonic_nm_propagation_dynamics"])
+def test_cli_replays_langevin_regression_cases_with_ranmars(case, tmp_path):
+    """The reference's Langevin regression cases run from their config.ini
+    for 5000 steps with the reference's own noise streams (--ranmars; the
+    factorial build's cases with --factorial): simulation.out rows and the
+    state dumps at the golden frames against the reference's golden files."""
+    from tests import golden_cases as G
+    _need_cli()
+    z, index = G.load()
+    ini = index[case]["ini"].replace("steps = 100000", "steps = 5000")
+    (tmp_path / "config.ini").write_text(ini)
+    args = ["-in", "config.ini", "--ranmars"] + (["--factorial"] if "factorial" in case else [])
+    r = _cli(args, tmp_path)
+    assert r.returncode == 0 and "[X]" not in r.stdout, r.stdout + r.stderr
+    cols, got = _read_out(tmp_path / "output" / "simulation.out")
+    # the fixtures come from a revision of the reference that also printed
+    # ext_pot and int_pot with one potential free (energy.cpp:12-18 now
+    # omits them): compare the columns by name
+    gold_cols = index[case]["columns"]
+    assert set(cols) <= set(gold_cols)
+    want = z[f"{case}/simulation_out"][:, [gold_cols.index(c) for c in cols]]  # the run's first rows
+    n = min(len(got), len(want))
+    assert n >= 6 and np.array_equal(got[:n, 0], want[:n, 0])
+    np.testing.assert_allclose(got[:n], want[:n], rtol=1e-6, atol=1e-9)
+    if not index[case]["dynamics"]:
+        return
+    P, N = index[case]["nbeads"], z[f"{case}/positions_angstrom"].shape[2]
+    gap = 100000 // (z[f"{case}/positions_angstrom"].shape[0] - 1)  # golden dumps keep every gap-th step
+    for stem, key in (("position_{}.xyz", "positions_angstrom"), ("velocity_{}.dat", "velocities_angstrom_per_ps"),
+                      ("force_{}.dat", "forces_ev_per_angstrom")):
+        frames = np.stack([R.read_frames(tmp_path / "output" / stem.format(b), N, 3) for b in range(P)], axis=1)
+        step_of = [k * (5000 // (frames.shape[0] - 1)) for k in range(frames.shape[0])]
+        for k in (0, 1):
+            mine = frames[step_of.index(k * gap)]
+            gold = z[f"{case}/{key}"][k]
+            scale = np.abs(gold).max()
+            assert np.abs(mine - gold).max() <= 1e-8 * scale + (1e-300 if scale else 0.0), (stem, k)
+
+
 @pytest.mark.skipif(not R.available("d3"), reason="compiled reference not built here")
 @pytest.mark.parametrize("pos_spec,vel_spec", [("xyz(pos_{}.xyz)", "manual(vel_{}.dat)"),
                                                ("xyz(one.xyz)", "random"),
