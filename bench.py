@@ -430,7 +430,7 @@ def main():
     prof = sysm.profile(-1)
     sysm.profile(0)
 
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI (pimdb_step_io) with pinned host buffers
     shape = (P, N, D)
     hx = torch.empty(shape, dtype=torch.float64, pin_memory=True)
     hp = torch.empty(shape, dtype=torch.float64, pin_memory=True)
@@ -440,9 +440,8 @@ def main():
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(Ke):
-        sysm.set_state_ptr(hx.data_ptr(), hp.data_ptr(), device=False)
-        sysm.step(1)
-        sysm.get_state_ptr(hx.data_ptr(), hp.data_ptr(), hf.data_ptr(), device=False)
+        # pimdb_step_io: x, p in; one step; x, p, f out; one synchronisation
+        sysm.step_io_ptr(hx.data_ptr(), hp.data_ptr(), 1, hx.data_ptr(), hp.data_ptr(), hf.data_ptr())
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     e2e = {"value": world * units * Ke / e2e_s, "unit": "bead-steps/s", "h2d_bytes_per_step": 2 * P * N * D * 8,
            "d2h_bytes_per_step": 3 * P * N * D * 8, "steps": Ke}

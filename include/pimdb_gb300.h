@@ -166,6 +166,13 @@ int pimdb_step(pimdb_handle* h, int nsteps);
  * pimdb_synchronize or synchronous call. */
 int pimdb_step_async(pimdb_handle* h, int nsteps);
 int pimdb_synchronize(pimdb_handle* h);
+/* For callers that keep the state on the host: pimdb_set_state (x_in, p_in;
+ * both NULL keeps the device state), pimdb_step(nsteps) and pimdb_get_state
+ * (x_out, p_out, f_out; any may be NULL) in one call with one
+ * synchronisation.  The host arrays may be pinned or pageable and may
+ * alias (x_in == x_out). */
+int pimdb_step_io(pimdb_handle* h, const double* x_in, const double* p_in, int nsteps, double* x_out, double* p_out,
+                  double* f_out);
 
 /* The step's pieces one by one, for hosts that mirror the reference's
  * plugin calls (Simulation::run, src/simulation.cpp:246-259).  Together,

@@ -28,6 +28,7 @@ RNG = {"philox": 0, "ranmars": 1}
 EXPORTS = [
     "pimdb_config_default", "pimdb_config_from_ini", "pimdb_create", "pimdb_destroy", "pimdb_set_state",
     "pimdb_set_state_device", "pimdb_get_state", "pimdb_get_state_device", "pimdb_set_step", "pimdb_get_step",
+    "pimdb_step_io",
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
     "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
     "pimdb_measure_fp64_peak", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
@@ -92,6 +93,7 @@ def lib():
             "pimdb_get_step": ([vp, C.POINTER(C.c_longlong)], C.c_int),
             "pimdb_compute_forces": ([vp], C.c_int),
             "pimdb_step": ([vp, C.c_int], C.c_int),
+            "pimdb_step_io": ([vp, vp, vp, C.c_int, vp, vp, vp], C.c_int),
             "pimdb_step_async": ([vp, C.c_int], C.c_int),
             "pimdb_synchronize": ([vp], C.c_int),
             "pimdb_exchange": ([vp, vp, vp, vp], C.c_int),
@@ -266,6 +268,19 @@ class System:
         fn = lib().pimdb_get_state_device if device else lib().pimdb_get_state
         args = [C.c_void_p(v) if v else None for v in (x_ptr, p_ptr, f_ptr)]
         _check(fn(self._h, *args), self._h)
+
+    def step_io_ptr(self, x_in, p_in, nsteps, x_out, p_out, f_out):
+        """pimdb_step_io on host pointers (0 / None for an absent array)."""
+        a = [C.c_void_p(v) if v else None for v in (x_in, p_in)]
+        b = [C.c_void_p(v) if v else None for v in (x_out, p_out, f_out)]
+        _check(lib().pimdb_step_io(self._h, *a, int(nsteps), *b), self._h)
+
+    def step_io(self, x=None, p=None, nsteps: int = 1):
+        """Sets x and p (None keeps them), runs nsteps and returns (x, p, f)."""
+        x, p = self._arr(x), self._arr(p)
+        out = [np.empty(self.shape) for _ in range(3)]
+        _check(lib().pimdb_step_io(self._h, _ptr(x), _ptr(p), int(nsteps), *(_ptr(o) for o in out)), self._h)
+        return tuple(out)
 
     def set_option(self, name: str, value: int):
         _check(lib().pimdb_set_option(self._h, name.encode(), int(value)), self._h)

@@ -72,6 +72,7 @@ struct pimdb_handle {
     // RanMars parity noise: the streams and the staged normals (Sys::noise)
     RanMarsState* d_rng = nullptr;
     double* d_noise = nullptr;
+    int* h_err = nullptr;  // pinned copy of the error word
     // CUDA graphs of pimdb_step_async: keyed by the step count and the
     // host-side step state at entry; the step index comes from d_step, which
     // every graph advances by its step count
@@ -330,6 +331,7 @@ static void free_handle(pimdb_handle* h) {
     if (h->d_nh) cudaFree(h->d_nh);
     if (h->d_fact) cudaFree(h->d_fact);
     if (h->d_rng) cudaFree(h->d_rng);
+    if (h->h_err) cudaFreeHost(h->h_err);
     if (h->d_noise) cudaFree(h->d_noise);
     if (h->d_pnm) cudaFree(h->d_pnm);
     if (h->d_step) cudaFree(h->d_step);
@@ -423,7 +425,9 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     if (e == cudaSuccess) e = cudaMemcpy(s.xflags + 3, &one, sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = alloc(&h->d_red[0], (size_t)3 * nred);
     if (e == cudaSuccess) e = alloc(&h->d_red[1], (size_t)3 * nred);
-    if (e == cudaSuccess) e = alloc(&h->d_stage, (size_t)s.P * s.N * h->D);
+    // host-order staging for the state crossing the boundary: [3][P*N*D]
+    if (e == cudaSuccess) e = alloc(&h->d_stage, (size_t)3 * s.P * s.N * h->D);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
@@ -516,27 +520,41 @@ static int check_err_word(pimdb_handle* h) {
     return PIMDB_OK;
 }
 
-static int set_state_impl(pimdb_handle* h, const double* x, const double* p, cudaMemcpyKind kind) {
-    if (!h) return PIMDB_ERR_ARG;
+// The state in, enqueued: copies into the staging buffer, then one kernel
+// (pack, zero the forces, fresh exchange estimate).
+static int enqueue_state_in(pimdb_handle* h, const double* x, const double* p, cudaMemcpyKind kind) {
     complete_pending(h);
-    Sys& s = h->s;
+    const Sys& s = h->s;
     const size_t n = (size_t)s.P * s.N * h->D;
-    const double* src[2] = {x, p};
-    double* dst[2] = {s.x, s.p};
-    for (int k = 0; k < 2; ++k) {
-        if (!src[k]) continue;
-        CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, src[k], n * sizeof(double), kind, h->stream));
-        launch_pack(s, h->D, h->d_stage, dst[k], h->stream);
-    }
-    const size_t nstate = (size_t)s.P * h->D * s.ld;
-    CUDA_TRY(h, cudaMemsetAsync(s.f, 0, nstate * sizeof(double), h->stream));
-    CUDA_TRY(h, cudaMemsetAsync(s.fphys, 0, nstate * sizeof(double), h->stream));
-    CUDA_TRY(h, cudaMemsetAsync(s.fx, 0, (size_t)2 * h->D * s.ld * sizeof(double), h->stream));
-    // new coordinates: the exchange recomputes its FP32 estimate first
-    static const int one = 1;
-    CUDA_TRY(h, cudaMemcpyAsync(s.xflags + 3, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    if (x) CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, x, n * sizeof(double), kind, h->stream));
+    if (p) CUDA_TRY(h, cudaMemcpyAsync(h->d_stage + n, p, n * sizeof(double), kind, h->stream));
+    launch(h, PIMDB_K_CART_UPDATE, [&] {
+        launch_state_in(s, h->D, x ? h->d_stage : nullptr, p ? h->d_stage + n : nullptr, h->stream);
+    });
     h->com_pending = false;
     CUDA_TRY(h, cudaGetLastError());
+    return PIMDB_OK;
+}
+
+// The state out, enqueued: the deferred tail of the last step, one unpack
+// kernel, then a copy per requested array.
+static int enqueue_state_out(pimdb_handle* h, double* x, double* p, double* f, cudaMemcpyKind kind) {
+    complete_pending(h);
+    const Sys& s = h->s;
+    const size_t n = (size_t)s.P * s.N * h->D;
+    const int mask = (x ? 1 : 0) | (p ? 2 : 0) | (f ? 4 : 0);
+    if (mask) launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_out(s, h->D, h->d_stage, mask, h->stream); });
+    double* dst[3] = {x, p, f};
+    for (int k = 0; k < 3; ++k)
+        if (dst[k]) CUDA_TRY(h, cudaMemcpyAsync(dst[k], h->d_stage + k * n, n * sizeof(double), kind, h->stream));
+    CUDA_TRY(h, cudaGetLastError());
+    return PIMDB_OK;
+}
+
+static int set_state_impl(pimdb_handle* h, const double* x, const double* p, cudaMemcpyKind kind) {
+    if (!h) return PIMDB_ERR_ARG;
+    const int st = enqueue_state_in(h, x, p, kind);
+    if (st != PIMDB_OK) return st;
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return PIMDB_OK;
 }
@@ -550,17 +568,8 @@ extern "C" int pimdb_set_state_device(pimdb_handle* h, const double* x, const do
 
 static int get_state_impl(pimdb_handle* h, double* x, double* p, double* f, cudaMemcpyKind kind) {
     if (!h) return PIMDB_ERR_ARG;
-    complete_pending(h);
-    Sys& s = h->s;
-    const size_t n = (size_t)s.P * s.N * h->D;
-    double* dst[3] = {x, p, f};
-    const double* src[3] = {s.x, s.p, s.f};
-    for (int k = 0; k < 3; ++k) {
-        if (!dst[k]) continue;
-        launch_unpack(s, h->D, src[k], h->d_stage, h->stream);
-        CUDA_TRY(h, cudaMemcpyAsync(dst[k], h->d_stage, n * sizeof(double), kind, h->stream));
-    }
-    CUDA_TRY(h, cudaGetLastError());
+    const int st = enqueue_state_out(h, x, p, f, kind);
+    if (st != PIMDB_OK) return st;
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return PIMDB_OK;
 }
@@ -891,6 +900,23 @@ extern "C" int pimdb_step(pimdb_handle* h, int nsteps) {
     int st = pimdb_step_async(h, nsteps);
     if (st != PIMDB_OK) return st;
     return check_err_word(h);
+}
+
+extern "C" int pimdb_step_io(pimdb_handle* h, const double* x_in, const double* p_in, int nsteps, double* x_out,
+                             double* p_out, double* f_out) {
+    if (!h || nsteps < 0) return PIMDB_ERR_ARG;
+    int st = PIMDB_OK;
+    if (x_in || p_in) st = enqueue_state_in(h, x_in, p_in, cudaMemcpyHostToDevice);
+    if (st == PIMDB_OK && nsteps > 0) st = pimdb_step_async(h, nsteps);
+    if (st == PIMDB_OK) st = enqueue_state_out(h, x_out, p_out, f_out, cudaMemcpyDeviceToHost);
+    if (st != PIMDB_OK) {
+        cudaStreamSynchronize(h->stream);
+        return st;
+    }
+    // the error word travels with the outputs: one synchronisation in all
+    CUDA_TRY(h, cudaMemcpyAsync(h->h_err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return *h->h_err ? check_err_word(h) : PIMDB_OK;
 }
 
 extern "C" int pimdb_synchronize(pimdb_handle* h) {

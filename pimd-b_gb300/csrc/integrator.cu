@@ -11,6 +11,8 @@
 // The kernel that last changed the momenta writes per-block partial sums
 // (`red_out`); the next kernel reduces them in a fixed order at start-up
 // (`red_in`), so the result is deterministic.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -37,6 +39,46 @@ __global__ void k_unpack(Sys s, const double* __restrict__ src, double* __restri
         const int i = (int)(bi % s.N);
         const int b = (int)(bi / s.N);
         dst[e] = src[idx<D>(s, b, a, i)];
+    }
+}
+
+// State in, one launch: x and p from host-order staging (either may be
+// absent), every force array zeroed (as after the reference's constructor,
+// src/simulation.cpp:16-101), and xflags[3] set so the exchange draws a
+// fresh FP32 estimate for the new coordinates.
+template <int D>
+__global__ void k_state_in(Sys s, const double* __restrict__ sx, const double* __restrict__ sp) {
+    const size_t n = (size_t)s.P * s.N * D;
+    const size_t nsoa = (size_t)s.P * D * s.ld;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (size_t e = t0; e < n; e += stride) {
+        const int a = (int)(e % D);
+        const size_t bi = e / D;
+        const size_t o = idx<D>(s, (int)(bi / s.N), a, (int)(bi % s.N));
+        if (sx) s.x[o] = sx[e];
+        if (sp) s.p[o] = sp[e];
+    }
+    for (size_t q = t0; q < nsoa; q += stride) {
+        s.f[q] = 0.0;
+        s.fphys[q] = 0.0;
+        if (q < (size_t)2 * D * s.ld) s.fx[q] = 0.0;
+    }
+    if (t0 == 0) s.xflags[3] = 1;
+}
+
+// State out, one launch: x, p and f (bits 1, 2, 4 of `mask`) into
+// host-order staging out[k * n + e].
+template <int D>
+__global__ void k_state_out(Sys s, double* __restrict__ out, int mask) {
+    const size_t n = (size_t)s.P * s.N * D;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(e % D);
+        const size_t bi = e / D;
+        const size_t o = idx<D>(s, (int)(bi / s.N), a, (int)(bi % s.N));
+        if (mask & 1) out[e] = s.x[o];
+        if (mask & 2) out[n + e] = s.p[o];
+        if (mask & 4) out[2 * n + e] = s.f[o];
     }
 }
 
@@ -814,6 +856,21 @@ void launch_unpack(const Sys& s, int D, const double* src, double* dst, cudaStre
     if (D == 1) k_unpack<1><<<g, 256, 0, st>>>(s, src, dst);
     else if (D == 2) k_unpack<2><<<g, 256, 0, st>>>(s, src, dst);
     else k_unpack<3><<<g, 256, 0, st>>>(s, src, dst);
+}
+
+void launch_state_in(const Sys& s, int D, const double* sx, const double* sp, cudaStream_t st) {
+    const size_t n = std::max((size_t)s.P * s.N * D, (size_t)s.P * D * s.ld);
+    const int g = pack_grid(n);
+    if (D == 1) k_state_in<1><<<g, 256, 0, st>>>(s, sx, sp);
+    else if (D == 2) k_state_in<2><<<g, 256, 0, st>>>(s, sx, sp);
+    else k_state_in<3><<<g, 256, 0, st>>>(s, sx, sp);
+}
+
+void launch_state_out(const Sys& s, int D, double* out, int mask, cudaStream_t st) {
+    const int g = pack_grid((size_t)s.P * s.N * D);
+    if (D == 1) k_state_out<1><<<g, 256, 0, st>>>(s, out, mask);
+    else if (D == 2) k_state_out<2><<<g, 256, 0, st>>>(s, out, mask);
+    else k_state_out<3><<<g, 256, 0, st>>>(s, out, mask);
 }
 
 int cart_update_blocks(const Sys& s, int D) {

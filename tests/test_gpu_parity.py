@@ -387,3 +387,42 @@ def test_nose_hoover_trajectory_matches_oracle(name):
                 assert rel_per_bead(got, want) < 1e-9, (st, label, rel_per_bead(got, want))
         ob = g.observables()
     assert abs(ob["nh_energy"] - tr.nh_energy()) <= 1e-9 * abs(tr.nh_energy())
+
+
+@pytest.mark.parametrize("name", ["nm_nmthermo_bosons_aziz", "vv_langevin_bosons_N16_P32"])
+def test_step_io_equals_separate_calls(name):
+    """pimdb_step_io (state in, steps, state out, one synchronisation) gives
+    bitwise the state of pimdb_set_state + pimdb_step + pimdb_get_state."""
+    s, cfg = case(**TRAJ_CASES[name])
+    x = ring(s, seed=8, spread_ang=0.2)
+    p = momenta(s, 8)
+    with pk.System(cfg) as a, pk.System(cfg) as b:
+        for g in (a, b):
+            g.set_step(0)
+        xa, pa = x.copy(), p.copy()
+        xb, pb = x.copy(), p.copy()
+        for n in (1, 2, 1):
+            a.set_state(xa, pa)
+            a.step(n)
+            xa, pa, fa = a.get_state()
+            xb, pb, fb = b.step_io(xb, pb, n)
+            for u, v in ((xa, xb), (pa, pb), (fa, fb)):
+                assert np.array_equal(u, v)
+        # absent inputs keep the device state; nsteps = 0 only reads it
+        xc, pc, fc = b.step_io(None, None, 0)
+        assert np.array_equal(xc, xb) and np.array_equal(pc, pb) and np.array_equal(fc, fb)
+        a.step(1)
+        xa, pa, fa = a.get_state()
+        xc, pc, fc = b.step_io(None, None, 1)
+        for u, v in ((xa, xc), (pa, pc), (fa, fc)):
+            assert np.array_equal(u, v)
+
+
+def test_step_io_reports_a_nonfinite_exchange():
+    kw, rk = FORCE_CASES["bosons_trap_N16_P32"]
+    s, cfg = case(**kw)
+    x = ring(s, seed=2, **rk)
+    x[0, 0, 0] = np.nan
+    with pk.System(cfg) as g:
+        with pytest.raises(pk.ExchangeOverflowError):
+            g.step_io(x, np.zeros_like(x), 1)
