@@ -172,8 +172,8 @@ def run_batched(pk, torch, stream, K, W, rank, world, dist):
             b._c(lib.pimdb_batch_get_states(b._b, ptr(hx), ptr(hp), ptr(hf)))
         te = max_over_ranks(time.perf_counter() - t0, dist)
     return {"value": world * units * K / t, "unit": "bead-steps/s", "ms_per_step": 1e3 * t / K, "steps": K,
-            "replicas": len(cfgs), "bead_particles": units, "precision": "mixed (FP32 pair forces and Langevin "
-            "normals, FP64 accumulation, exchange and integrator)",
+            "replicas": len(cfgs), "bead_particles": units, "precision": "mixed (FP32 pair forces, FP64 accumulation, "
+            "exchange and integrator)",
             "force_error": {"max_norm_rel": max(errs), "median_norm_rel": float(np.median(errs)),
                             "against": "the engine's FP64 path on the same coordinates (which matches the FP64 "
                                        "oracle within 1e-10)"},

@@ -327,8 +327,8 @@ int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms, int ndim,
  * src/propagators/velocity_verlet.cpp:7-22) and the cartesian Langevin
  * thermostat or none, for every replica.  Every replica must share ndim and
  * precision; natoms <= 2048; at most 65535 replicas.  With PIMDB_MIXED the
- * pair forces are FP32 with FP64 accumulation and the Langevin normals are
- * drawn in FP32 (same Philox stream); exchange and integrator stay FP64.
+ * pair forces are FP32 with FP64 accumulation; exchange and integrator stay
+ * FP64.  The Langevin normals are the one-system path's in both precisions.
  * Host arrays of the batch are the replicas' [bead][particle][axis] arrays
  * concatenated in replica order (pimdb_batch_size gives the total length).
  */

@@ -1209,19 +1209,66 @@ static void philox4x32_10(uint32_t* c, uint64_t seed) {
     }
 }
 
+/* Box-Muller on FP32 with its own log, sin and cos from their series,
+ * correctly rounded operations only (fmaf, no contraction): the GPU's
+ * bm_log / bm_sincos_2pi / philox_normal_pair_f32 in the same order, so both
+ * draw bit-identical numbers.  log u = e ln2 + 2 atanh((m-1)/(m+1)) to s^9;
+ * sin to phi^13 and cos to phi^14 on a quadrant. */
+static float bm_log(float u) {
+    uint32_t bits;
+    memcpy(&bits, &u, sizeof bits);
+    int e = (int)((bits >> 23) & 0xffu) - 127;
+    const uint32_t mb = (bits & 0x7fffffu) | 0x3f800000u;
+    float m;
+    memcpy(&m, &mb, sizeof m);
+    if (m > 1.41421354f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float sv = (m - 1.0f) / (m + 1.0f);
+    const float s2 = sv * sv;
+    float q = fmaf(0.111111112f, s2, 0.142857149f);
+    q = fmaf(q, s2, 0.2f);
+    q = fmaf(q, s2, 0.333333343f);
+    q = fmaf(q, s2, 1.0f);
+    const float lm = (2.0f * sv) * q;
+    const float ef = (float)e;
+    return fmaf(ef, 0.693145752f, fmaf(ef, 1.42860677e-06f, lm));
+}
+
+static void bm_sincos_2pi(uint32_t w, float* sn, float* cs) {
+    const uint32_t quad = w >> 30;
+    const float ph = ((float)((w >> 6) & 0xffffffu) * 5.96046448e-08f) * 1.57079637f;
+    const float p2 = ph * ph;
+    float sp = fmaf(1.60590444e-10f, p2, -2.50521079e-08f);
+    sp = fmaf(sp, p2, 2.75573188e-06f);
+    sp = fmaf(sp, p2, -1.98412701e-04f);
+    sp = fmaf(sp, p2, 8.33333377e-03f);
+    sp = fmaf(sp, p2, -0.166666672f);
+    sp = fmaf(sp * p2, ph, ph);
+    float cp = fmaf(-1.14707454e-11f, p2, 2.08767559e-09f);
+    cp = fmaf(cp, p2, -2.75573188e-07f);
+    cp = fmaf(cp, p2, 2.48015876e-05f);
+    cp = fmaf(cp, p2, -1.38888892e-03f);
+    cp = fmaf(cp, p2, 4.16666679e-02f);
+    cp = fmaf(cp, p2, -0.5f);
+    cp = fmaf(cp, p2, 1.0f);
+    const float a = (quad & 1u) ? cp : sp, b = (quad & 1u) ? sp : cp;
+    *sn = (quad & 2u) ? -a : a;
+    *cs = ((quad + 1u) & 2u) ? -b : b;
+}
+
 void orc_philox_normals(uint64_t seed, uint32_t replica, uint64_t step, int substep, int64_t ndof, double* out) {
     const uint64_t t = 2 * step + (uint64_t)substep;
     for (int64_t pair = 0; 2 * pair < ndof; ++pair) {
         uint32_t c[4] = {(uint32_t)pair, replica, (uint32_t)t, (uint32_t)(t >> 32)};
         philox4x32_10(c, seed);
-        const uint64_t a = (((uint64_t)c[1] << 32) | c[0]) >> 11;
-        const uint64_t b = (((uint64_t)c[3] << 32) | c[2]) >> 11;
-        const double u1 = ((double)a + 0.5) * 0x1p-53;
-        const double u2 = ((double)b + 0.5) * 0x1p-53;
-        const double r = sqrt(-2.0 * log(u1));
-        const double th = 6.283185307179586 * u2;
-        out[2 * pair] = r * cos(th);
-        if (2 * pair + 1 < ndof) out[2 * pair + 1] = r * sin(th);
+        const float u1 = (float)((c[0] >> 8) + 1u) * 5.96046448e-08f; /* exact */
+        const float r = sqrtf(-2.0f * bm_log(u1));
+        float sn, cs;
+        bm_sincos_2pi(c[2], &sn, &cs);
+        out[2 * pair] = (double)(r * cs);
+        if (2 * pair + 1 < ndof) out[2 * pair + 1] = (double)(r * sn);
     }
 }
 

@@ -147,9 +147,11 @@ void orc_langevin(const orc_system* s, double* p, const double* xi);          /*
 void orc_nm_matrices(const orc_system* s, double* cart_to_nm, double* nm_to_cart); /* normal_modes.cpp:48-79 */
 
 /* ---- noise sources ---- */
-/* Counter-based Philox4x32-10 (Salmon et al., SC'11) + Box-Muller.  This is
- * the project's noise definition shared with the GPU kernels: normal number of
- * degree of freedom `dof` at (replica, step, substep). */
+/* Counter-based Philox4x32-10 (Salmon et al., SC'11) + Box-Muller on FP32
+ * with series log, sin and cos (correctly rounded operations only, so the GPU
+ * draws bit-identical numbers).  This is the project's noise definition
+ * shared with the GPU kernels: normal number of degree of freedom `dof` at
+ * (replica, step, substep). */
 void orc_philox_normals(uint64_t seed, uint32_t replica, uint64_t step, int substep, int64_t ndof, double* out);
 /* RANMAR (Marsaglia, Zaman & Tsang 1990; F. James, Comp. Phys. Comm. 60, 329)
  * with the polar Gaussian, one stream per bead seeded seed+bead, as the

@@ -52,32 +52,14 @@ struct BatchRep {
 
 constexpr int kBatchMaxThreads = 512;
 
-// FP32 Box-Muller on the top 24 bits of the same Philox outputs the FP64
-// path uses (philox_normal_pair takes the top 53).
-__device__ __forceinline__ float2 philox_normal_pair_f(uint64_t seed, uint32_t replica, uint64_t t, uint32_t pair) {
-    uint32_t c[4] = {pair, replica, (uint32_t)t, (uint32_t)(t >> 32)};
-    philox4x32_10(c, seed);
-    const float u1 = ((float)(c[1] >> 8) + 0.5f) * 0x1p-24f;
-    const float u2 = ((float)(c[3] >> 8) + 0.5f) * 0x1p-24f;
-    const float r = sqrtf(-2.0f * logf(u1));
-    float sn, cs;
-    sincospif(2.0f * u2, &sn, &cs);
-    return make_float2(r * cs, r * sn);
-}
-
 template <typename R>
 __device__ __forceinline__ void normal_pair(const Sys& s, long long step, int substep, uint32_t pair, double& z0,
                                             double& z1) {
     const uint64_t t = 2ull * (unsigned long long)step + substep;
-    if constexpr (sizeof(R) == 8) {
-        const double2 z = philox_normal_pair(s.seed, s.replica, t, pair);
-        z0 = z.x;
-        z1 = z.y;
-    } else {
-        const float2 z = philox_normal_pair_f(s.seed, s.replica, t, pair);
-        z0 = (double)z.x;
-        z1 = (double)z.y;
-    }
+    // the one-system path's normals (drawn on the FP32 pipe in either precision)
+    const float2 z = philox_normal_pair_f32(s.seed, s.replica, t, pair);
+    z0 = (double)z.x;
+    z1 = (double)z.y;
 }
 
 // Sums v[0..D) over the block; every thread receives the totals.  `sh`

@@ -159,17 +159,71 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint64_t seed) {
     }
 }
 
-__device__ __forceinline__ double2 philox_normal_pair(uint64_t seed, uint32_t replica, uint64_t t, uint32_t pair) {
+// Box-Muller on the FP32 pipe (FP64 runs at 1/64 of the FP32 rate, so FP64
+// transcendentals would cost as much as a pair interaction).  Its log, sin and
+// cos are evaluated here from their series with correctly rounded IEEE
+// operations only (explicit round-to-nearest intrinsics, nothing contracted),
+// so a C restatement with fmaf draws bit-identical numbers.
+//   u1 = (k + 1) 2^-24 from the top 24 bits k of word 0, exact (|z| <= 5.8);
+//   log u1 = e ln2 + 2 atanh((m - 1)/(m + 1)), m in [sqrt(1/2), sqrt(2)),
+//            the atanh series to s^9 (next term below 3e-9 relative);
+//   theta = 2 pi u2, u2 from 26 bits of word 2: the top 2 bits select the
+//            quadrant, the next 24 give phi in [0, pi/2), where the Taylor
+//            series of sin to phi^13 and cos to phi^14 are within 7e-10.
+__device__ __forceinline__ float bm_log(float u) {
+    const unsigned bits = __float_as_uint(u);
+    int e = (int)((bits >> 23) & 0xffu) - 127;
+    float m = __uint_as_float((bits & 0x7fffffu) | 0x3f800000u);
+    if (m > 1.41421354f) {
+        m = __fmul_rn(m, 0.5f);
+        e += 1;
+    }
+    const float sv = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+    const float s2 = __fmul_rn(sv, sv);
+    float q = __fmaf_rn(0.111111112f, s2, 0.142857149f);
+    q = __fmaf_rn(q, s2, 0.2f);
+    q = __fmaf_rn(q, s2, 0.333333343f);
+    q = __fmaf_rn(q, s2, 1.0f);
+    const float lm = __fmul_rn(__fmul_rn(2.0f, sv), q);
+    const float ef = (float)e;
+    return __fmaf_rn(ef, 0.693145752f, __fmaf_rn(ef, 1.42860677e-06f, lm));
+}
+
+__device__ __forceinline__ void bm_sincos_2pi(unsigned w, float* sn, float* cs) {
+    const unsigned quad = w >> 30;
+    const float ph = __fmul_rn(__fmul_rn((float)((w >> 6) & 0xffffffu), 5.96046448e-08f), 1.57079637f);
+    const float p2 = __fmul_rn(ph, ph);
+    float sp = __fmaf_rn(1.60590444e-10f, p2, -2.50521079e-08f);
+    sp = __fmaf_rn(sp, p2, 2.75573188e-06f);
+    sp = __fmaf_rn(sp, p2, -1.98412701e-04f);
+    sp = __fmaf_rn(sp, p2, 8.33333377e-03f);
+    sp = __fmaf_rn(sp, p2, -0.166666672f);
+    sp = __fmaf_rn(__fmul_rn(sp, p2), ph, ph);
+    float cp = __fmaf_rn(-1.14707454e-11f, p2, 2.08767559e-09f);
+    cp = __fmaf_rn(cp, p2, -2.75573188e-07f);
+    cp = __fmaf_rn(cp, p2, 2.48015876e-05f);
+    cp = __fmaf_rn(cp, p2, -1.38888892e-03f);
+    cp = __fmaf_rn(cp, p2, 4.16666679e-02f);
+    cp = __fmaf_rn(cp, p2, -0.5f);
+    cp = __fmaf_rn(cp, p2, 1.0f);
+    const float a = (quad & 1u) ? cp : sp, b = (quad & 1u) ? sp : cp;
+    *sn = (quad & 2u) ? -a : a;
+    *cs = ((quad + 1u) & 2u) ? -b : b;
+}
+
+__device__ __forceinline__ float2 philox_normal_pair_f32(uint64_t seed, uint32_t replica, uint64_t t, uint32_t pair) {
     uint32_t c[4] = {pair, replica, (uint32_t)t, (uint32_t)(t >> 32)};
     philox4x32_10(c, seed);
-    const uint64_t a = ((((uint64_t)c[1]) << 32) | c[0]) >> 11;
-    const uint64_t b = ((((uint64_t)c[3]) << 32) | c[2]) >> 11;
-    const double u1 = ((double)a + 0.5) * 0x1p-53;
-    const double u2 = ((double)b + 0.5) * 0x1p-53;
-    const double r = sqrt(-2.0 * log(u1));
-    double sn, cs;
-    sincos(6.283185307179586 * u2, &sn, &cs);
-    return make_double2(r * cs, r * sn);
+    const float u1 = __fmul_rn((float)((c[0] >> 8) + 1u), 5.96046448e-08f);  // exact
+    const float r = __fsqrt_rn(__fmul_rn(-2.0f, bm_log(u1)));
+    float sn, cs;
+    bm_sincos_2pi(c[2], &sn, &cs);
+    return make_float2(__fmul_rn(r, cs), __fmul_rn(r, sn));
+}
+
+__device__ __forceinline__ double2 philox_normal_pair(uint64_t seed, uint32_t replica, uint64_t t, uint32_t pair) {
+    const float2 z = philox_normal_pair_f32(seed, replica, t, pair);
+    return make_double2((double)z.x, (double)z.y);
 }
 
 // The two Langevin normals of (bead-or-mode k, axis a, particles 2 i2 and

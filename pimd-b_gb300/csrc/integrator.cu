@@ -584,7 +584,10 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
         for (int e = threadIdx.x; e < P * kNmTile; e += blockDim.x) sq[e] += hdt * sg[e];
         __syncthreads();
         thermostat(2ull * (unsigned long long)(step - 1) + 1);
-        if (fixcom && !remove_com(0)) return;
+        // With the head in the same launch one removal, after the head's
+        // O-step, stands for both: the removal is a linear projection and the
+        // O-step affine, so COM(O2(COM(O1 p))) = COM(O2(O1 p)).
+        if (fixcom && !head && !remove_com(0)) return;
     }
     if (head) {
         thermostat(2ull * (unsigned long long)step);
