@@ -470,7 +470,7 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     }
     if (e == cudaSuccess && c.propagator == PIMDB_PROP_NORMAL_MODES && c.nmthermostat &&
         c.thermostat == PIMDB_THERMO_LANGEVIN && nm_fused_fits(s, h->D)) {
-        e = alloc(&h->d_cmpart, (size_t)2 * nm_blocks(s, h->D));
+        e = alloc(&h->d_cmpart, nm_fused_partials(s, h->D));
         if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_bar, 2 * sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMemset(h->d_bar, 0, 2 * sizeof(unsigned));
         h->fused_nm = (e == cudaSuccess);
@@ -1161,7 +1161,11 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
     drop_graphs(h);
     if (n == "exact_exchange") h->opt_exact_exchange = value ? 1 : 0;
     else if (n == "fused_normal_modes") h->fused_nm = value && h->d_cmpart != nullptr;
-    else if (n == "fft_normal_modes") h->opt_fft = value ? 1 : 0;
+    else if (n == "fft_normal_modes") {
+        h->opt_fft = value ? 1 : 0;
+        // the matrix transforms run in the block kernel only
+        if (!value && h->fused_nm && !nm_block_fits(h->s, h->D)) h->fused_nm = false;
+    }
     else if (n == "newton3") h->opt_newton3 = value ? 1 : 0;
     else if (n == "cell_lists") {
         if (value > 0 && !h->d_cells)

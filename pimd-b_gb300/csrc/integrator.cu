@@ -658,6 +658,477 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same fused step with the transforms in registers, for P = 32 E
+// (E = 1, 2, 4).  One warp per (particle pair, axis): the pair's two real
+// sequences are the real and imaginary parts of one complex sequence, and
+// lane l holds beads l + 32 e.  Forward: with n = 32 e + l and k = k1 + E k2,
+//   Z_k = sum_l W_32^(l k2) [W_P^(l k1) sum_e z_(32e+l) W_E^(e k1)]:
+// an E-point DFT in the lane, the twiddles, then a 32-point radix-2
+// decimation in frequency across lanes (shuffles, no block barriers); mode k
+// ends in element k1 of lane bitrev5(k2).  Every normal-mode operation (kick,
+// O-step, COM shift, free rotation) is per mode, in registers.  The inverse
+// runs the same steps backwards (decimation in time across lanes from the
+// bit-reversed order), which leaves bead n = 32 e + l in element e of lane l.
+// Only the COM removal still meets at a grid barrier.
+
+__device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+__device__ __forceinline__ double2 shfl_d2(double2 v, int src) {
+    return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+// W_P^t = exp(-2 pi i t / P), 0 <= t < P, from tw[t] (t < P/2)
+__device__ __forceinline__ double2 twid(const double2* tw, int t, int half) {
+    const double2 w = tw[t & (half - 1)];
+    return t < half ? w : make_double2(-w.x, -w.y);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+
+template <int E>
+__device__ __forceinline__ void warp_fft_fwd(double2 (&z)[E], const double2* tw, int P, int lane) {
+    const int half = P >> 1;
+    if constexpr (E == 2) {
+        const double2 a = z[0], b = z[1];
+        z[0] = cadd(a, b);
+        z[1] = csub(a, b);
+    } else if constexpr (E == 4) {
+        const double2 a = cadd(z[0], z[2]), b = csub(z[0], z[2]), c = cadd(z[1], z[3]), d = csub(z[1], z[3]);
+        z[0] = cadd(a, c);
+        z[2] = csub(a, c);
+        z[1] = make_double2(b.x + d.y, b.y - d.x);  // b - i d
+        z[3] = make_double2(b.x - d.y, b.y + d.x);  // b + i d
+    }
+#pragma unroll
+    for (int k1 = 1; k1 < E; ++k1) z[k1] = cmul(z[k1], twid(tw, lane * k1, half));
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+        const bool upper = (lane & d) != 0;
+        const double2 w = upper ? twid(tw, (lane & (d - 1)) * (P / (2 * d)), half) : make_double2(1.0, 0.0);
+#pragma unroll
+        for (int k1 = 0; k1 < E; ++k1) {
+            const double2 o = shfl_xor_d2(z[k1], d);
+            const double2 own = upper ? make_double2(-z[k1].x, -z[k1].y) : z[k1];
+            z[k1] = cmul(cadd(o, own), w);  // lower: own + other; upper: (other - own) w
+        }
+    }
+}
+
+template <int E>
+__device__ __forceinline__ void warp_fft_inv(double2 (&z)[E], const double2* tw, int P, int lane) {
+    const int half = P >> 1;
+#pragma unroll
+    for (int d = 1; d <= 16; d <<= 1) {
+        const bool upper = (lane & d) != 0;
+        const double2 w = cconj(twid(tw, (lane & (d - 1)) * (P / (2 * d)), half));
+#pragma unroll
+        for (int k1 = 0; k1 < E; ++k1) {
+            const double2 o = shfl_xor_d2(z[k1], d);
+            const double2 t = cmul(upper ? z[k1] : o, w);   // the upper element, turned
+            const double2 lo = upper ? o : z[k1];
+            z[k1] = upper ? csub(lo, t) : cadd(lo, t);
+        }
+    }
+#pragma unroll
+    for (int k1 = 1; k1 < E; ++k1) z[k1] = cmul(z[k1], cconj(twid(tw, lane * k1, half)));
+    if constexpr (E == 2) {
+        const double2 a = z[0], b = z[1];
+        z[0] = cadd(a, b);
+        z[1] = csub(a, b);
+    } else if constexpr (E == 4) {
+        const double2 a = cadd(z[0], z[2]), b = csub(z[0], z[2]), c = cadd(z[1], z[3]), d = csub(z[1], z[3]);
+        z[0] = cadd(a, c);
+        z[2] = csub(a, c);
+        z[1] = make_double2(b.x - d.y, b.y + d.x);  // b + i d
+        z[3] = make_double2(b.x + d.y, b.y - d.x);  // b - i d
+    }
+}
+
+// The value that element k1 of lane `lane` holds for mode P - k.
+template <int E>
+__device__ __forceinline__ double2 mode_partner(const double2 (&v)[E], int k1, int lane) {
+    if (k1 == 0) {
+        const int k2 = (int)(__brev((unsigned)lane) >> 27);
+        return shfl_d2(v[0], (int)(__brev((unsigned)((32 - k2) & 31)) >> 27));
+    }
+    return shfl_d2(v[E - k1], lane ^ 31);
+}
+
+// Spectrum Z of two real sequences -> their normal-mode coordinates (a, b):
+//   q_k = c0 Re X_k (k = 0, P/2), c Re X_k (k < P/2), c Im X_k (k > P/2).
+template <int E>
+__device__ __forceinline__ void warp_to_modes(double2 (&z)[E], int P, int lane) {
+    const double c = sqrt(2.0 / P), c0 = 1.0 / sqrt((double)P);
+    const int half = P >> 1;
+    double2 q[E];
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) {
+        const double2 zp = mode_partner<E>(z, k1, lane);
+        const int k = k1 + E * (int)(__brev((unsigned)lane) >> 27);
+        const double xar = 0.5 * (z[k1].x + zp.x), xai = 0.5 * (z[k1].y - zp.y);
+        const double xbr = 0.5 * (z[k1].y + zp.y), xbi = 0.5 * (zp.x - z[k1].x);
+        if (k == 0 || k == half) q[k1] = make_double2(c0 * xar, c0 * xbr);
+        else if (k < half) q[k1] = make_double2(c * xar, c * xbr);
+        else q[k1] = make_double2(c * xai, c * xbi);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) z[k1] = q[k1];
+}
+
+// Normal-mode coordinates (a, b) -> the spectrum whose conjugate transform
+// gives x_a + i x_b (the block kernel's nm_inverse_fft load).
+template <int E>
+__device__ __forceinline__ void warp_from_modes(double2 (&q)[E], int P, int lane) {
+    const double c = 0.5 * sqrt(2.0 / P), c0 = 1.0 / sqrt((double)P);
+    const int half = P >> 1;
+    double2 z[E];
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) {
+        const double2 qp = mode_partner<E>(q, k1, lane);
+        const int k = k1 + E * (int)(__brev((unsigned)lane) >> 27);
+        double zar, zai, zbr, zbi;
+        if (k == 0 || k == half) {
+            zar = c0 * q[k1].x;
+            zbr = c0 * q[k1].y;
+            zai = zbi = 0.0;
+        } else if (k < half) {
+            zar = c * q[k1].x;
+            zai = -c * qp.x;
+            zbr = c * q[k1].y;
+            zbi = -c * qp.y;
+        } else {
+            zar = c * qp.x;
+            zai = c * q[k1].x;
+            zbr = c * qp.y;
+            zbi = c * q[k1].y;
+        }
+        z[k1] = make_double2(zar - zbi, zai + zbr);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) q[k1] = z[k1];
+}
+
+template <int D, int E>
+__global__ void __launch_bounds__(256) k_nm_warp(Sys s, const double* __restrict__ rot, double* cmpart, unsigned* bar,
+                                                 int mode, StepRef sref, int fixcom, const double2* __restrict__ tw_g) {
+    constexpr int P = 32 * E;
+    __shared__ double2 tw[P / 2];
+    for (int t = threadIdx.x; t < P / 2; t += blockDim.x) tw[t] = tw_g[t];
+    __syncthreads();
+    const long long step = sref.get();
+    const int lane = threadIdx.x & 31;
+    const int half = (s.N + 1) / 2;
+    const int nwarps = D * half;
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const bool live = w < nwarps;  // idle warps still meet the block's barriers
+    const int a = live ? w / half : 0, i2 = live ? w % half : 0;
+    const int ia = 2 * i2, ib = 2 * i2 + 1;
+    const bool va = live && ia < s.N, vb = live && ib < s.N;
+    const bool head = mode & 2, tail = mode & 1;
+    double2 zp[E], zf[E], zx[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int b = 32 * e + lane;
+        zp[e] = zf[e] = zx[e] = make_double2(0.0, 0.0);
+        if (va) {
+            const size_t o = idx<D>(s, b, a, ia);
+            zp[e].x = s.p[o];
+            zx[e].x = s.x[o];
+            zf[e].x = nm_kick_force<D>(s, b, a, ia);
+        }
+        if (vb) {
+            const size_t o = idx<D>(s, b, a, ib);
+            zp[e].y = s.p[o];
+            zx[e].y = s.x[o];
+            zf[e].y = nm_kick_force<D>(s, b, a, ib);
+        }
+    }
+    warp_fft_fwd<E>(zp, tw, P, lane);
+    warp_fft_fwd<E>(zf, tw, P, lane);
+    if (head) warp_fft_fwd<E>(zx, tw, P, lane);
+    warp_to_modes<E>(zp, P, lane);
+    warp_to_modes<E>(zf, P, lane);
+    if (head) warp_to_modes<E>(zx, P, lane);
+    const double hdt = 0.5 * s.dt;
+    const int k2 = (int)(__brev((unsigned)lane) >> 27);
+    auto thermostat = [&](uint64_t t) {
+#pragma unroll
+        for (int k1 = 0; k1 < E; ++k1) {
+            const double2 z = langevin_pair<D>(s, t, k1 + E * k2, a, i2, half);
+            zp[k1].x = s.c1 * zp[k1].x + s.c2 * z.x;
+            zp[k1].y = s.c1 * zp[k1].y + s.c2 * z.y;
+        }
+    };
+    // centroid (mode 0: element 0 of lane 0) of every particle, one partial
+    // per warp; after the grid barrier each warp adds its axis' partials in
+    // order and shifts its own centroid mode by sqrt(P) cm
+    const double cm_scale = 1.0 / (double)s.N;
+    auto remove_com = [&](int buf) -> bool {
+        double* cp = cmpart + (size_t)buf * nwarps;
+        if (live && lane == 0) cp[w] = (va ? zp[0].x : 0.0) + (vb ? zp[0].y : 0.0);
+        if (!grid_barrier(bar, gridDim.x, s.err)) return false;
+        double acc = 0.0;
+        if (live)
+            for (int k = lane; k < half; k += 32) acc += ((volatile double*)cp)[a * half + k];
+        const double shift = warp_sum(acc) * cm_scale;
+        if (lane == 0) {
+            zp[0].x -= shift;
+            zp[0].y -= shift;
+        }
+        return true;
+    };
+    if (tail) {
+#pragma unroll
+        for (int k1 = 0; k1 < E; ++k1) {
+            zp[k1].x += hdt * zf[k1].x;
+            zp[k1].y += hdt * zf[k1].y;
+        }
+        thermostat(2ull * (unsigned long long)(step - 1) + 1);
+        // with the head in this launch one removal after its O-step stands
+        // for both (the removal commutes through the affine O-step)
+        if (fixcom && !head && !remove_com(0)) return;
+    }
+    if (head) {
+        thermostat(2ull * (unsigned long long)step);
+        if (fixcom && !remove_com(1)) return;
+#pragma unroll
+        for (int k1 = 0; k1 < E; ++k1) {
+            const int k = k1 + E * k2;
+            const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+            // kick, then the free ring rotation of (q, p) in mode k
+            auto turn = [&](double& q, double& pm, double g) {
+                const double q0 = q, pk = pm + hdt * g;
+                if (mw == 0.0) {
+                    q = q0 + s.dt / s.mass * pk;
+                    pm = pk;
+                } else {
+                    q = cs * q0 + sn / mw * pk;
+                    pm = -mw * sn * q0 + cs * pk;
+                }
+            };
+            turn(zx[k1].x, zp[k1].x, zf[k1].x);
+            turn(zx[k1].y, zp[k1].y, zf[k1].y);
+        }
+    }
+    warp_from_modes<E>(zp, P, lane);
+    warp_fft_inv<E>(zp, tw, P, lane);
+    if (head) {
+        warp_from_modes<E>(zx, P, lane);
+        warp_fft_inv<E>(zx, tw, P, lane);
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int b = 32 * e + lane;
+        if (va) {
+            const size_t o = idx<D>(s, b, a, ia);
+            s.p[o] = zp[e].x;
+            if (head) s.x[o] = zx[e].x;
+        }
+        if (vb) {
+            const size_t o = idx<D>(s, b, a, ib);
+            s.p[o] = zp[e].y;
+            if (head) s.x[o] = zx[e].y;
+        }
+    }
+}
+
+// Three warps per (particle pair, axis): warp 0 transforms p, warp 1 the
+// kick force, warp 2 x, each in registers as above, so the transforms run
+// side by side; the modes of F and x meet warp 0's in shared memory for the
+// per-mode operations, and warps 0 and 2 transform p and x back.  Used when
+// every block can be resident (the COM removal's grid barrier).
+template <int D, int E>
+__global__ void __launch_bounds__(96) k_nm_warp3(Sys s, const double* __restrict__ rot, double* cmpart, unsigned* bar,
+                                                 int mode, StepRef sref, int fixcom, const double2* __restrict__ tw_g) {
+    constexpr int P = 32 * E;
+    __shared__ double2 tw[P / 2];
+    __shared__ double2 sF[E][32], sX[E][32];
+    for (int t = threadIdx.x; t < P / 2; t += blockDim.x) tw[t] = tw_g[t];
+    __syncthreads();
+    const long long step = sref.get();
+    const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;  // 0: p, 1: F, 2: x
+    const int half = (s.N + 1) / 2;
+    const int u = blockIdx.x;  // (axis, particle pair)
+    const int a = u / half, i2 = u % half;
+    const int ia = 2 * i2, ib = 2 * i2 + 1;
+    const bool va = ia < s.N, vb = ib < s.N;
+    const bool head = mode & 2, tail = mode & 1;
+    const int k2 = (int)(__brev((unsigned)lane) >> 27);
+    double2 z[E];
+    if (role == 0 || role == 1 || head) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int b = 32 * e + lane;
+            z[e] = make_double2(0.0, 0.0);
+            if (va) {
+                const size_t o = idx<D>(s, b, a, ia);
+                z[e].x = role == 0 ? s.p[o] : role == 2 ? s.x[o] : nm_kick_force<D>(s, b, a, ia);
+            }
+            if (vb) {
+                const size_t o = idx<D>(s, b, a, ib);
+                z[e].y = role == 0 ? s.p[o] : role == 2 ? s.x[o] : nm_kick_force<D>(s, b, a, ib);
+            }
+        }
+        warp_fft_fwd<E>(z, tw, P, lane);
+        warp_to_modes<E>(z, P, lane);
+        if (role == 1) {
+#pragma unroll
+            for (int k1 = 0; k1 < E; ++k1) sF[k1][lane] = z[k1];
+        } else if (role == 2) {
+#pragma unroll
+            for (int k1 = 0; k1 < E; ++k1) sX[k1][lane] = z[k1];
+        }
+    }
+    __syncthreads();
+    const double hdt = 0.5 * s.dt;
+    auto thermostat = [&](uint64_t t) {
+#pragma unroll
+        for (int k1 = 0; k1 < E; ++k1) {
+            const double2 zn = langevin_pair<D>(s, t, k1 + E * k2, a, i2, half);
+            z[k1].x = s.c1 * z[k1].x + s.c2 * zn.x;
+            z[k1].y = s.c1 * z[k1].y + s.c2 * zn.y;
+        }
+    };
+    const int nunits = gridDim.x;
+    const double cm_scale = 1.0 / (double)s.N;
+    // every thread of the block takes part (the barrier's block syncs); the
+    // centroid mode is element 0 of warp 0's lane 0
+    auto remove_com = [&](int buf) -> bool {
+        double* cp = cmpart + (size_t)buf * nunits;
+        if (threadIdx.x == 0) cp[u] = (va ? z[0].x : 0.0) + (vb ? z[0].y : 0.0);
+        if (!grid_barrier(bar, gridDim.x, s.err)) return false;
+        if (role == 0) {
+            double acc = 0.0;
+            for (int k = lane; k < half; k += 32) acc += ((volatile double*)cp)[a * half + k];
+            const double shift = warp_sum(acc) * cm_scale;
+            if (lane == 0) {
+                z[0].x -= shift;
+                z[0].y -= shift;
+            }
+        }
+        return true;
+    };
+    if (tail) {
+        if (role == 0) {
+#pragma unroll
+            for (int k1 = 0; k1 < E; ++k1) {
+                const double2 g = sF[k1][lane];
+                z[k1].x += hdt * g.x;
+                z[k1].y += hdt * g.y;
+            }
+            thermostat(2ull * (unsigned long long)(step - 1) + 1);
+        }
+        if (fixcom && !head && !remove_com(0)) return;
+    }
+    if (head) {
+        if (role == 0) thermostat(2ull * (unsigned long long)step);
+        if (fixcom && !remove_com(1)) return;
+        if (role == 0) {
+#pragma unroll
+            for (int k1 = 0; k1 < E; ++k1) {
+                const int k = k1 + E * k2;
+                const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+                const double2 g = sF[k1][lane];
+                double2 q = sX[k1][lane];
+                auto turn = [&](double& qv, double& pm, double gv) {
+                    const double q0 = qv, pk = pm + hdt * gv;
+                    if (mw == 0.0) {
+                        qv = q0 + s.dt / s.mass * pk;
+                        pm = pk;
+                    } else {
+                        qv = cs * q0 + sn / mw * pk;
+                        pm = -mw * sn * q0 + cs * pk;
+                    }
+                };
+                turn(q.x, z[k1].x, g.x);
+                turn(q.y, z[k1].y, g.y);
+                sX[k1][lane] = q;
+            }
+        }
+        __syncthreads();
+        if (role == 2) {
+#pragma unroll
+            for (int k1 = 0; k1 < E; ++k1) z[k1] = sX[k1][lane];
+        }
+    }
+    if (role == 0 || (role == 2 && head)) {
+        warp_from_modes<E>(z, P, lane);
+        warp_fft_inv<E>(z, tw, P, lane);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int b = 32 * e + lane;
+            double* dst = role == 0 ? s.p : s.x;
+            if (va) dst[idx<D>(s, b, a, ia)] = z[e].x;
+            if (vb) dst[idx<D>(s, b, a, ib)] = z[e].y;
+        }
+    }
+}
+
+template <int D, int E>
+static bool nm_warp3_fits(const Sys& s) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nm_warp3<D, E>, 96, 0) != cudaSuccess) return false;
+    return (long long)D * ((s.N + 1) / 2) <= (long long)per * sms;
+}
+
+// Warps per block of the warp kernel: the fewest (spreading the pairs over
+// the most SMs) with which every block is resident at once; 0 if none fits.
+template <int D, int E>
+static int nm_warp_block(const Sys& s) {
+    if (nm_warp3_fits<D, E>(s)) return 3;  // three warps per pair and axis
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long nwarps = (long long)D * ((s.N + 1) / 2);
+    for (int wpb = 1; wpb <= 8; wpb <<= 1) {  // one warp per pair and axis
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nm_warp<D, E>, 32 * wpb, 0) != cudaSuccess) return 0;
+        if ((nwarps + wpb - 1) / wpb <= (long long)per * sms) return wpb;
+    }
+    return 0;
+}
+
+template <int D>
+static int nm_warp_block_d(const Sys& s) {
+    if (s.P == 32) return nm_warp_block<D, 1>(s);
+    if (s.P == 64) return nm_warp_block<D, 2>(s);
+    if (s.P == 128) return nm_warp_block<D, 4>(s);
+    return 0;
+}
+
+static int nm_warp_block_any(const Sys& s, int D) {
+    if (D == 1) return nm_warp_block_d<1>(s);
+    if (D == 2) return nm_warp_block_d<2>(s);
+    return nm_warp_block_d<3>(s);
+}
+
+template <int D, int E>
+static cudaError_t nm_warp_t(const Sys& s, const double* rot, double* cmpart, unsigned* bar, int mode, StepRef step,
+                             int fixcom, const double2* tw, int wpb, cudaStream_t st) {
+    const long long nwarps = (long long)D * ((s.N + 1) / 2);
+    if (wpb == 3) {
+        Sys sc = s;
+        void* args[] = {&sc, &rot, &cmpart, &bar, &mode, &step, &fixcom, &tw};
+        return cudaLaunchCooperativeKernel((void*)k_nm_warp3<D, E>, dim3((unsigned)nwarps), dim3(96), args, 0, st);
+    }
+    dim3 grid((unsigned)((nwarps + wpb - 1) / wpb));
+    Sys sc = s;
+    void* args[] = {&sc, &rot, &cmpart, &bar, &mode, &step, &fixcom, &tw};
+    return cudaLaunchCooperativeKernel((void*)k_nm_warp<D, E>, grid, dim3(32 * wpb), args, 0, st);
+}
+
+template <int D>
+static cudaError_t nm_warp_d(const Sys& s, const double* rot, double* cmpart, unsigned* bar, int mode, StepRef step,
+                             int fixcom, const double2* tw, int wpb, cudaStream_t st) {
+    if (s.P == 32) return nm_warp_t<D, 1>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
+    if (s.P == 64) return nm_warp_t<D, 2>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
+    return nm_warp_t<D, 4>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
+}
+
 // [6][P][kNmTile] arrays plus two FFT work buffers of 3 kNmPairs complex transforms
 size_t nm_fused_smem(const Sys& s) {
     return sizeof(double) * (6 * (size_t)s.P * kNmTile + 2 * 2 * 3 * (kNmTile / 2) * (size_t)s.P);
@@ -679,10 +1150,16 @@ static bool nm_fused_fits_t(const Sys& s) {
     return need <= (long long)per * sms;
 }
 
-bool nm_fused_fits(const Sys& s, int D) {
+bool nm_block_fits(const Sys& s, int D) {
     if (D == 1) return nm_fused_fits_t<1>(s);
     if (D == 2) return nm_fused_fits_t<2>(s);
     return nm_fused_fits_t<3>(s);
+}
+
+bool nm_fused_fits(const Sys& s, int D) { return nm_warp_block_any(s, D) > 0 || nm_block_fits(s, D); }
+
+size_t nm_fused_partials(const Sys& s, int D) {
+    return 2 * std::max((size_t)nm_blocks(s, D), (size_t)D * ((s.N + 1) / 2));
 }
 
 template <int D>
@@ -698,6 +1175,21 @@ static cudaError_t nm_fused_t(const Sys& s, const double* C, const double* T, co
 cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
                             unsigned* bar, int mode, StepRef step, int fixcom, const double2* tw, int logP,
                             cudaStream_t st) {
+    // the warp kernel when P = 32, 64 or 128 and the FFTs are selected (or
+    // the block kernel cannot be resident); the block kernel otherwise
+    static int wpb_cache[4] = {-1, -1, -1, -1};
+    static long long wpb_key[4] = {-1, -1, -1, -1};
+    const long long key = ((long long)s.N << 20) | s.P;
+    if (wpb_key[D] != key) {
+        wpb_cache[D] = nm_warp_block_any(s, D);
+        wpb_key[D] = key;
+    }
+    const int wpb = wpb_cache[D];
+    if (wpb > 0 && tw) {
+        if (D == 1) return nm_warp_d<1>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
+        if (D == 2) return nm_warp_d<2>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
+        return nm_warp_d<3>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
+    }
     if (D == 1) return nm_fused_t<1>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
     if (D == 2) return nm_fused_t<2>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
     return nm_fused_t<3>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);

@@ -119,6 +119,11 @@ void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, 
 // kick, rotation).  Cooperative launch; nm_fused_fits tells whether every
 // block can be resident.
 bool nm_fused_fits(const Sys& s, int D);
+// whether the block kernel (any P) can be resident; the warp kernel (P = 32,
+// 64, 128, with the FFT twiddles) is used whenever it can be
+bool nm_block_fits(const Sys& s, int D);
+// doubles of COM partial sums the fused step needs (cmpart)
+size_t nm_fused_partials(const Sys& s, int D);
 // `tw` (P/2 twiddles exp(-2 pi i t/P)) selects the FFT transforms (P a power
 // of two, logP = log2 P); NULL selects the P x P matrix products.
 cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,

@@ -102,9 +102,25 @@ TRAJ_CASES = {
     "nm_nmthermo_bosons_P16_2d": dict(ndim=2, natoms=24, nbeads=16, propagator="normal_modes", nmthermostat=True,
                                       inter="dipole", int_p=(2.4799673e-4, 0, 0), ext="harmonic",
                                       ext_p=(1.0 * 0.036749326e-3, 0, 0), box_ang=40.0),
+    # P = 32, 64, 128: the fused step runs in registers, one warp per particle pair
+    "nm_nmthermo_dist_P32_odd_N": dict(natoms=7, nbeads=32, bosonic=False, propagator="normal_modes",
+                                       nmthermostat=True, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    "nm_nmthermo_bosons_P64_aziz": dict(natoms=20, nbeads=64, propagator="normal_modes", nmthermostat=True,
+                                        T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=11.0, inter="aziz",
+                                        cutoff_ang=5.5, dt_fs=2.0),
+    "nm_nmthermo_dist_P128_2d_nofixcom": dict(ndim=2, natoms=9, nbeads=128, bosonic=False, fixcom=False,
+                                              propagator="normal_modes", nmthermostat=True, ext="harmonic",
+                                              ext_p=(1.0 * 0.036749326e-3, 0, 0)),
+    "nm_nmthermo_bosons_P32_1d": dict(ndim=1, natoms=6, nbeads=32, propagator="normal_modes", nmthermostat=True,
+                                      ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    # too many pairs for three warps each to be resident at once: one warp each
+    "nm_nmthermo_dist_P32_N2300": dict(natoms=2300, nbeads=32, bosonic=False, propagator="normal_modes",
+                                       nmthermostat=True, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0),
+                                       box_ang=60.0),
 }
 # options applied to the GPU side only
-TRAJ_OPTIONS = {"nm_nmthermo_bosons_aziz": [{}, {"fused_normal_modes": 0}, {"fft_normal_modes": 0}]}
+TRAJ_OPTIONS = {"nm_nmthermo_bosons_aziz": [{}, {"fused_normal_modes": 0}, {"fft_normal_modes": 0}],
+                "nm_nmthermo_bosons_P64_aziz": [{}, {"fft_normal_modes": 0}, {"fused_normal_modes": 0}]}
 
 
 def _run_pair(kw, steps, seed_state=3, options=None):
