@@ -520,33 +520,62 @@ static int check_err_word(pimdb_handle* h) {
     return PIMDB_OK;
 }
 
-// The state in, enqueued: copies into the staging buffer, then one kernel
-// (pack, zero the forces, fresh exchange estimate).
+// The device address of page-locked host memory (registered or allocated
+// with the CUDA runtime), or null for any other pointer.  Kernels read and
+// write such memory directly (over NVLink-C2C on Grace systems), which
+// replaces a copy engine transfer plus a staging pass.
+static void* pinned_view(const void* host) {
+    if (!host) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// The state in, enqueued: one kernel (pack, zero the forces), reading
+// page-locked host arrays directly or the staging buffer after a copy.
 static int enqueue_state_in(pimdb_handle* h, const double* x, const double* p, cudaMemcpyKind kind) {
     complete_pending(h);
     const Sys& s = h->s;
     const size_t n = (size_t)s.P * s.N * h->D;
-    if (x) CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, x, n * sizeof(double), kind, h->stream));
-    if (p) CUDA_TRY(h, cudaMemcpyAsync(h->d_stage + n, p, n * sizeof(double), kind, h->stream));
-    launch(h, PIMDB_K_CART_UPDATE, [&] {
-        launch_state_in(s, h->D, x ? h->d_stage : nullptr, p ? h->d_stage + n : nullptr, h->stream);
-    });
+    const double* sx = x;
+    const double* sp = p;
+    if (kind == cudaMemcpyHostToDevice) {
+        const double* vx = static_cast<const double*>(pinned_view(x));
+        const double* vp = static_cast<const double*>(pinned_view(p));
+        sx = x ? (vx ? vx : h->d_stage) : nullptr;
+        sp = p ? (vp ? vp : h->d_stage + n) : nullptr;
+        if (x && !vx) CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, x, n * sizeof(double), kind, h->stream));
+        if (p && !vp) CUDA_TRY(h, cudaMemcpyAsync(h->d_stage + n, p, n * sizeof(double), kind, h->stream));
+    }
+    launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_in(s, h->D, sx, sp, h->stream); });
     h->com_pending = false;
     CUDA_TRY(h, cudaGetLastError());
     return PIMDB_OK;
 }
 
-// The state out, enqueued: the deferred tail of the last step, one unpack
-// kernel, then a copy per requested array.
+// The state out, enqueued: the deferred tail of the last step, then one
+// unpack kernel writing page-locked host arrays directly, or the staging
+// buffer followed by a copy per array.
 static int enqueue_state_out(pimdb_handle* h, double* x, double* p, double* f, cudaMemcpyKind kind) {
     complete_pending(h);
     const Sys& s = h->s;
     const size_t n = (size_t)s.P * s.N * h->D;
-    const int mask = (x ? 1 : 0) | (p ? 2 : 0) | (f ? 4 : 0);
-    if (mask) launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_out(s, h->D, h->d_stage, mask, h->stream); });
     double* dst[3] = {x, p, f};
+    double* out[3] = {x, p, f};  // what the kernel writes
+    bool copy[3] = {false, false, false};
+    for (int k = 0; k < 3; ++k) {
+        if (!dst[k] || kind != cudaMemcpyDeviceToHost) continue;
+        double* v = static_cast<double*>(pinned_view(dst[k]));
+        copy[k] = v == nullptr;
+        out[k] = v ? v : h->d_stage + k * n;
+    }
+    if (x || p || f)
+        launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_out(s, h->D, out[0], out[1], out[2], h->stream); });
     for (int k = 0; k < 3; ++k)
-        if (dst[k]) CUDA_TRY(h, cudaMemcpyAsync(dst[k], h->d_stage + k * n, n * sizeof(double), kind, h->stream));
+        if (copy[k]) CUDA_TRY(h, cudaMemcpyAsync(dst[k], out[k], n * sizeof(double), kind, h->stream));
     CUDA_TRY(h, cudaGetLastError());
     return PIMDB_OK;
 }

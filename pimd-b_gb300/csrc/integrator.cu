@@ -42,10 +42,12 @@ __global__ void k_unpack(Sys s, const double* __restrict__ src, double* __restri
     }
 }
 
-// State in, one launch: x and p from host-order staging (either may be
-// absent), every force array zeroed (as after the reference's constructor,
-// src/simulation.cpp:16-101), and xflags[3] set so the exchange draws a
-// fresh FP32 estimate for the new coordinates.
+// State in, one launch: x and p in host order (either may be absent; device
+// staging or page-locked host memory, read directly) and every force array
+// zeroed (as after the reference's
+// constructor, src/simulation.cpp:16-101).  The exchange keeps reusing its
+// last potentials as the estimate: where new coordinates make that estimate
+// fail, its retry phase draws a fresh one.
 template <int D>
 __global__ void k_state_in(Sys s, const double* __restrict__ sx, const double* __restrict__ sp) {
     const size_t n = (size_t)s.P * s.N * D;
@@ -64,21 +66,21 @@ __global__ void k_state_in(Sys s, const double* __restrict__ sx, const double* _
         s.fphys[q] = 0.0;
         if (q < (size_t)2 * D * s.ld) s.fx[q] = 0.0;
     }
-    if (t0 == 0) s.xflags[3] = 1;
 }
 
-// State out, one launch: x, p and f (bits 1, 2, 4 of `mask`) into
-// host-order staging out[k * n + e].
+// State out, one launch: x, p and f (each output may be null) in host
+// order.  The outputs are device staging or page-locked host memory, which
+// the kernel writes directly.
 template <int D>
-__global__ void k_state_out(Sys s, double* __restrict__ out, int mask) {
+__global__ void k_state_out(Sys s, double* __restrict__ ox, double* __restrict__ op, double* __restrict__ of) {
     const size_t n = (size_t)s.P * s.N * D;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
         const int a = (int)(e % D);
         const size_t bi = e / D;
         const size_t o = idx<D>(s, (int)(bi / s.N), a, (int)(bi % s.N));
-        if (mask & 1) out[e] = s.x[o];
-        if (mask & 2) out[n + e] = s.p[o];
-        if (mask & 4) out[2 * n + e] = s.f[o];
+        if (ox) ox[e] = s.x[o];
+        if (op) op[e] = s.p[o];
+        if (of) of[e] = s.f[o];
     }
 }
 
@@ -1361,11 +1363,11 @@ void launch_state_in(const Sys& s, int D, const double* sx, const double* sp, cu
     else k_state_in<3><<<g, 256, 0, st>>>(s, sx, sp);
 }
 
-void launch_state_out(const Sys& s, int D, double* out, int mask, cudaStream_t st) {
+void launch_state_out(const Sys& s, int D, double* ox, double* op, double* of, cudaStream_t st) {
     const int g = pack_grid((size_t)s.P * s.N * D);
-    if (D == 1) k_state_out<1><<<g, 256, 0, st>>>(s, out, mask);
-    else if (D == 2) k_state_out<2><<<g, 256, 0, st>>>(s, out, mask);
-    else k_state_out<3><<<g, 256, 0, st>>>(s, out, mask);
+    if (D == 1) k_state_out<1><<<g, 256, 0, st>>>(s, ox, op, of);
+    else if (D == 2) k_state_out<2><<<g, 256, 0, st>>>(s, ox, op, of);
+    else k_state_out<3><<<g, 256, 0, st>>>(s, ox, op, of);
 }
 
 int cart_update_blocks(const Sys& s, int D) {

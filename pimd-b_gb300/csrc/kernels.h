@@ -100,11 +100,11 @@ int launch_nose_hoover(const Sys& s, int D, const NHPar& q, const double* C, con
 void launch_pack(const Sys& s, int D, const double* src, double* dst, cudaStream_t st);
 void launch_unpack(const Sys& s, int D, const double* src, double* dst, cudaStream_t st);
 // The state crossing the boundary in one launch each way: k_state_in packs
-// x and p (either may be null) from host-order staging and zeroes the force
-// arrays; k_state_out unpacks x, p, f (mask bits 1, 2, 4) into staging
-// [3][P*N*D].
+// x and p (either may be null) from host-order arrays and zeroes the force
+// arrays; k_state_out unpacks x, p, f (any may be null) into host-order
+// arrays.  The arrays are device staging or page-locked host memory.
 void launch_state_in(const Sys& s, int D, const double* sx, const double* sp, cudaStream_t st);
-void launch_state_out(const Sys& s, int D, double* out, int mask, cudaStream_t st);
+void launch_state_out(const Sys& s, int D, double* ox, double* op, double* of, cudaStream_t st);
 int cart_update_blocks(const Sys& s, int D);
 int nm_blocks(const Sys& s, int D);
 void launch_cart_update(const Sys& s, int D, int flags, const double* red_in, int nred_in, double* red_out,

@@ -442,3 +442,27 @@ def test_step_io_reports_a_nonfinite_exchange():
     with pk.System(cfg) as g:
         with pytest.raises(pk.ExchangeOverflowError):
             g.step_io(x, np.zeros_like(x), 1)
+
+
+def test_step_io_with_page_locked_buffers():
+    """Page-locked host arrays are read and written by the state kernels
+    directly: the same state, bitwise, as through copies of pageable arrays."""
+    torch = pytest.importorskip("torch")
+    s, cfg = case(**TRAJ_CASES["nm_nmthermo_bosons_P64_aziz"])
+    x = ring(s, seed=6, spread_ang=0.2)
+    p = momenta(s, 6)
+    hx, hp, hf = (torch.empty(x.shape, dtype=torch.float64, pin_memory=True) for _ in range(3))
+    hx.copy_(torch.from_numpy(x))
+    hp.copy_(torch.from_numpy(p))
+    with pk.System(cfg) as a, pk.System(cfg) as b:
+        for g in (a, b):
+            g.set_step(0)
+        xa, pa = x.copy(), p.copy()
+        for _ in range(3):
+            xa, pa, fa = a.step_io(xa, pa, 1)
+            b.step_io_ptr(hx.data_ptr(), hp.data_ptr(), 1, hx.data_ptr(), hp.data_ptr(), hf.data_ptr())
+            for u, v in ((xa, hx), (pa, hp), (fa, hf)):
+                assert np.array_equal(u, v.numpy())
+        b.set_state_ptr(hx.data_ptr(), hp.data_ptr(), device=False)
+        b.get_state_ptr(hx.data_ptr(), None, hf.data_ptr(), device=False)
+        assert np.array_equal(hx.numpy(), xa)
