@@ -418,12 +418,16 @@ def main():
     tot_s = max_over_ranks(sum(step_ms) / 1e3, dist)
     value = world * units * K / tot_s
 
-    # kernel launches in the timed region: the same K steps, counted
+    # kernel launches in the timed region: the same K steps, counted.  Each
+    # untimed block restarts from the initial state, so no run goes far past
+    # W + K steps (the 2D dipole system is not stable over thousands)
+    sysm.set_state(x0, p0)
     prof = sysm.profile(0)
     sysm.step_async(K)
     sysm.synchronize()
     launches = sysm.profile(-1)["launches"]
     # per-kernel device times (events around each launch on the library stream)
+    sysm.set_state(x0, p0)
     sysm.profile(1)
     sysm.step_async(K)
     sysm.synchronize()
@@ -435,6 +439,8 @@ def main():
     hx = torch.empty(shape, dtype=torch.float64, pin_memory=True)
     hp = torch.empty(shape, dtype=torch.float64, pin_memory=True)
     hf = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    sysm.set_state(x0, p0)
+    sysm.step(W)
     sysm.get_state_ptr(hx.data_ptr(), hp.data_ptr(), None, device=False)
     Ke = max(1, min(K // 2, 200))
     torch.cuda.synchronize()
