@@ -73,6 +73,11 @@ struct pimdb_handle {
     RanMarsState* d_rng = nullptr;
     double* d_noise = nullptr;
     int* h_err = nullptr;  // pinned copy of the error word
+    // the exchange's triangular solve across SMs (large N): y of both
+    // directions and the publication flags
+    double* d_ysol = nullptr;
+    double* d_cm = nullptr;  // the pending COM correction, reduced (3 doubles)
+    unsigned* d_gflags = nullptr;
     // CUDA graphs of pimdb_step_async: keyed by the step count and the
     // host-side step state at entry; the step index comes from d_step, which
     // every graph advances by its step count
@@ -319,7 +324,7 @@ static void free_handle(pimdb_handle* h) {
     double* bufs[] = {h->s.x,   h->s.p,   h->s.f,   h->s.fphys, h->s.fx,   h->s.E,        h->s.V,
                       h->s.Vb,  h->s.scal, h->s.Vh, h->s.Vbh,  h->s.yf,   h->s.yb,       h->s.Wf,
                       h->s.Wb,  h->s.Et, h->s.rowR, h->s.rowC, h->d_C,  h->d_T,    h->d_rot,      h->d_red[0],
-                      h->d_red[1], h->d_stage, h->d_part};
+                      h->d_red[1], h->d_stage, h->d_part, h->s.Vp};
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (h->d_err) cudaFree(h->d_err);
@@ -332,6 +337,9 @@ static void free_handle(pimdb_handle* h) {
     if (h->d_fact) cudaFree(h->d_fact);
     if (h->d_rng) cudaFree(h->d_rng);
     if (h->h_err) cudaFreeHost(h->h_err);
+    if (h->d_ysol) cudaFree(h->d_ysol);
+    if (h->d_cm) cudaFree(h->d_cm);
+    if (h->d_gflags) cudaFree(h->d_gflags);
     if (h->d_noise) cudaFree(h->d_noise);
     if (h->d_pnm) cudaFree(h->d_pnm);
     if (h->d_step) cudaFree(h->d_step);
@@ -396,6 +404,17 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     if (e == cudaSuccess) e = alloc(&s.Et, ntri);
     if (e == cudaSuccess) e = alloc(&s.rowR, (size_t)s.N);
     if (e == cudaSuccess) e = alloc(&s.rowC, (size_t)s.N);
+    if (e == cudaSuccess && s.bosonic) {
+        // no previous exchange result yet: NaN (0xff bytes) stops the first extrapolation
+        e = cudaMalloc((void**)&s.Vp, 2 * ((size_t)s.N + 1) * sizeof(double));
+        if (e == cudaSuccess) e = cudaMemset(s.Vp, 0xff, 2 * ((size_t)s.N + 1) * sizeof(double));
+    }
+    if (e == cudaSuccess) e = alloc(&h->d_cm, 3);
+    if (e == cudaSuccess && s.bosonic && exchange_grid_doubles(s) > 0) {
+        e = alloc(&h->d_ysol, exchange_grid_doubles(s));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_gflags, exchange_grid_flags(s) * sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMemset(h->d_gflags, 0, exchange_grid_flags(s) * sizeof(unsigned));
+    }
     // Newton's-third-law pair tiles need P * ceil(N/32) * D * ld partial sums;
     // beyond 512 MiB the all-pairs kernel (no partials) is used instead.
     const size_t npart = pair_partial_doubles(s, h->D);
@@ -430,7 +449,11 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    // the exchange chain's stream: highest priority, so its (latency-bound,
+    // few-block) kernels are dispatched between the waves of the pair forces
+    int prio_least = 0, prio_greatest = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_greatest);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
@@ -474,18 +497,20 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
         if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_bar, 2 * sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMemset(h->d_bar, 0, 2 * sizeof(unsigned));
         h->fused_nm = (e == cudaSuccess);
+    }
+    // FFT twiddles exp(-2 pi i t/P), t < P/2, for the normal-mode transforms
+    if (e == cudaSuccess && (c.propagator == PIMDB_PROP_NORMAL_MODES || c.nmthermostat) && s.P >= 2 &&
+        (s.P & (s.P - 1)) == 0) {
         const int P = s.P;
-        if (e == cudaSuccess && P >= 2 && (P & (P - 1)) == 0) {
-            std::vector<double> tw((size_t)P);
-            const double pi = 3.14159265358979323846;
-            for (int t = 0; t < P / 2; ++t) {
-                tw[2 * t] = std::cos(2 * pi * t / P);
-                tw[2 * t + 1] = -std::sin(2 * pi * t / P);
-            }
-            e = alloc(&h->d_tw, (size_t)P);
-            if (e == cudaSuccess) e = cudaMemcpy(h->d_tw, tw.data(), (size_t)P * sizeof(double), cudaMemcpyHostToDevice);
-            while ((1 << h->logP) < P) ++h->logP;
+        std::vector<double> tw((size_t)P);
+        const double pi = 3.14159265358979323846;
+        for (int t = 0; t < P / 2; ++t) {
+            tw[2 * t] = std::cos(2 * pi * t / P);
+            tw[2 * t + 1] = -std::sin(2 * pi * t / P);
         }
+        e = alloc(&h->d_tw, (size_t)P);
+        if (e == cudaSuccess) e = cudaMemcpy(h->d_tw, tw.data(), (size_t)P * sizeof(double), cudaMemcpyHostToDevice);
+        while ((1 << h->logP) < P) ++h->logP;
     }
     cudaGetLastError();
     s.err = h->d_err;
@@ -635,7 +660,8 @@ static void exchange_front(pimdb_handle* h, cudaStream_t st) {
     }
     launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, st); });
     const int ex = h->opt_exact_exchange;
-    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, st); }, ex ? 1 : 6);
+    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, st, h->d_ysol, h->d_gflags); },
+           ex ? 1 : (h->d_ysol ? 8 : 6));
 }
 static void exchange_forces(pimdb_handle* h, int accumulate, cudaStream_t st) {
     const Sys& s = h->s;
@@ -813,8 +839,8 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
             const int apply = h->com_pending ? 1 : 0;
             launch(h, PIMDB_K_NM_PROPAGATE, [&] {
                 launch_nm_propagate(h->s, h->D, h->d_C, h->d_T, h->d_rot, apply, h->d_red[rin], h->nred_last,
-                                    h->stream);
-            });
+                                    h->opt_fft ? (const double2*)h->d_tw : nullptr, h->d_cm, h->stream);
+            }, apply ? 2 : 1);
             h->com_pending = false;
             enqueue_forces(h);
             if (cart_langevin) {
@@ -1237,7 +1263,8 @@ extern "C" int pimdb_propagate(pimdb_handle* h) {
     complete_pending(h);
     if (h->cfg.propagator == PIMDB_PROP_NORMAL_MODES) {
         launch(h, PIMDB_K_NM_PROPAGATE, [&] {
-            launch_nm_propagate(h->s, h->D, h->d_C, h->d_T, h->d_rot, 0, h->d_red[0], 0, h->stream);
+            launch_nm_propagate(h->s, h->D, h->d_C, h->d_T, h->d_rot, 0, h->d_red[0], 0,
+                                h->opt_fft ? (const double2*)h->d_tw : nullptr, h->d_cm, h->stream);
         });
         enqueue_forces(h);
         cart(h, SF_KICK, 0, 1);

@@ -70,6 +70,8 @@ struct Sys {
     double* Et;     // E re-packed by backward node
     double* rowR;   // per-row factors exp(-beta (Vh[l+1] + Vb[l+1] - V[N])), N
     double* rowC;   // cut probabilities exp(-beta (V[l+1] + Vb[l+1] - V[N])), N
+    double* Vp;     // V and V_backwards of the previous evaluation, [2][N+1]
+                    // (null: the next estimate is the last result, not extrapolated)
     int* xflags;    // [0] forward used the exact fallback, [1] backward, [2] completion counter
     // Langevin normals drawn by the reference's RanMars streams (one per
     // bead, seeded seed + bead) for the current and the previous MD step:

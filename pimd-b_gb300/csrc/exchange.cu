@@ -74,12 +74,14 @@ __global__ void k_exch_weights(Sys s, int phase) {
 // the exact recursion when it reused the previous potentials (xflags[7]); a
 // failed solve then leaves xflags[6] set and the phase-1 kernels redo the
 // evaluation from a fresh estimate.
-__global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_exact, int phase) {
+__global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_exact, int phase,
+                                                             const double* __restrict__ pre) {
     extern __shared__ double ys[];  // y: N+1, acc: N+1, then 32 for reductions
     __shared__ int last_block;
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
     const int allow_exact = force_exact || phase == 1 || !((volatile int*)s.xflags)[7];
-    solve_direction(s, blockIdx.x, force_exact, ys, allow_exact);
+    solve_direction(s, blockIdx.x, force_exact, ys, allow_exact,
+                    pre ? pre + (size_t)blockIdx.x * (s.N + 1) : nullptr);
     // The block that finishes second runs solve_finish (threadFenceReduction
     // pattern; no waiting).
     __threadfence();
@@ -92,8 +94,107 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
         if (threadIdx.x == 0) s.xflags[2] = 0;  // retry pending: phase 1 finishes
         return;
     }
-    solve_finish(s);
+    solve_finish(s, !force_exact);
     if (threadIdx.x == 0) s.xflags[6] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 3 across SMs for large N.  The triangular solve y_n = sum_{u<n}
+// W[n-1][u] y_u costs N^2/2 FP64 multiply-adds per direction, which on the
+// one block of k_exch_solve is bound by a single SM's FP64 pipe.  Here 32-row
+// blocks go round-robin to `nct` CTAs per direction (all resident: cooperative
+// launch).  For every block j in order, its owner resolves the diagonal block
+// with warp shuffles (its rows already hold the contributions of blocks < j)
+// and publishes y_j behind a fence and a flag; every CTA then adds
+// W[rows][block j] y_j to the rows it owns (8 threads per row, shuffle sums:
+// a fixed order).  The critical path is one diagonal block plus one flag per
+// 32 levels.  Waits give up after a bounded number of polls (ERRB_TIMEOUT).
+// k_exch_solve then post-processes y as usual.
+__global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, int phase, double* ysol,
+                                                                      unsigned* gflags, int nct) {
+    if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    extern __shared__ double gsm[];
+    __shared__ int abort_solve;
+    const int dir = blockIdx.x / nct, c = blockIdx.x % nct;
+    const int nn = dir == 0 ? s.N + 1 : s.N;
+    const double* __restrict__ W = dir == 0 ? s.Wf : s.Wb;
+    double* y = ysol + (size_t)dir * (s.N + 1);
+    const int nbmax = (s.N + 1 + 31) / 32;
+    unsigned* flags = gflags + (size_t)dir * nbmax;
+    const int nb = (nn + 31) / 32;
+    const int nown = (nb - c + nct - 1) / nct;  // blocks c, c + nct, ...
+    double* acc = gsm;                           // [nown][32]
+    double* yj = gsm + (size_t)nown * 32;        // [32]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int e = tid; e < nown * 32; e += blockDim.x) acc[e] = 0.0;
+    if (tid == 0) abort_solve = 0;
+    __syncthreads();
+    for (int j = 0; j < nb; ++j) {
+        if (j % nct == c) {
+            if (warp == 0) {
+                const int n = 32 * j + lane;
+                double a = n == 0 ? 1.0 : (n < nn ? acc[(j / nct) * 32 + lane] : 0.0);
+                double w[32];
+#pragma unroll
+                for (int t = 0; t < 32; ++t) w[t] = (n < nn && n >= 1 && t < lane) ? W[tri(n - 1) + 32 * j + t] : 0.0;
+#pragma unroll
+                for (int t = 0; t < 32; ++t) {
+                    const double yt = __shfl_sync(0xffffffffu, a, t);
+                    if (lane > t) a = fma(w[t], yt, a);
+                }
+                if (n < nn) y[n] = a;
+                yj[lane] = n < nn ? a : 0.0;
+                __threadfence();
+                __syncwarp();
+                if (lane == 0) atomicExch(&flags[j], 1u);
+            }
+        } else if (tid == 0) {
+            unsigned it = 0;
+            while (((volatile unsigned*)flags)[j] == 0u) {
+                if (++it > (1u << 22)) {
+                    atomicOr(s.err, ERRB_TIMEOUT);
+                    abort_solve = 1;
+                    break;
+                }
+                __nanosleep(32);
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        if (abort_solve) break;
+        if (j % nct != c && tid < 32) {
+            const int n = 32 * j + tid;
+            yj[tid] = n < nn ? ((volatile double*)y)[n] : 0.0;
+        }
+        __syncthreads();
+        // rows this CTA owns below block j: W[rows][block j] y_j
+        const int i = tid >> 3, part = tid & 7;  // row of the block, quarter of the columns
+        for (int r = c; r < nb; r += nct) {
+            if (r <= j) continue;
+            const int n = 32 * r + i;
+            double sum = 0.0;
+            if (n < nn) {
+                const double* row = W + tri(n - 1) + 32 * j + 4 * part;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sum = fma(row[q], yj[4 * part + q], sum);
+            }
+            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+            sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+            sum += __shfl_xor_sync(0xffffffffu, sum, 4);
+            if (part == 0) acc[(r / nct) * 32 + i] += sum;
+        }
+        __syncthreads();
+    }
+    // the CTA that finishes last clears the flags for the next launch
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&gflags[2 * nbmax], 1u) == gridDim.x - 1) {
+            for (int e = 0; e < 2 * nbmax; ++e) gflags[e] = 0u;
+            gflags[2 * nbmax] = 0u;
+            __threadfence();
+        }
+    }
 }
 
 // Exterior spring forces: one warp per row (bead P) or column (bead 1).
@@ -118,24 +219,54 @@ void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
     else k_exch_energies<3><<<grid, warps * 32, 0, st>>>(s);
 }
 
-int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st) {
+size_t exchange_grid_doubles(const Sys& s) { return s.N >= kGridSolveMinN ? 2 * ((size_t)s.N + 1) : 0; }
+size_t exchange_grid_flags(const Sys& s) {
+    return s.N >= kGridSolveMinN ? 2 * (((size_t)s.N + 1 + 31) / 32) + 1 : 0;
+}
+
+// The cooperative solve if every CTA can be resident; false otherwise.
+static bool grid_solve(const Sys& s, int phase, double* ysol, unsigned* gflags, cudaStream_t st) {
+    const int nb = (s.N + 1 + 31) / 32;
+    const int nct = nb < kGridSolveCtas ? nb : kGridSolveCtas;
+    const size_t smem = sizeof(double) * (((size_t)(nb + nct - 1) / nct) * 32 + 32);
+    static int per = -1;
+    if (per < 0) {
+        int dev = 0, sms = 0, b = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_exch_solve_grid, kGridSolveThreads, 4096) != cudaSuccess)
+            b = 0;
+        per = b * sms;
+    }
+    if (2 * nct > per) return false;
+    Sys sc = s;
+    int ph = phase, n = nct;
+    void* args[] = {&sc, &ph, &ysol, &gflags, &n};
+    return cudaLaunchCooperativeKernel((void*)k_exch_solve_grid, dim3(2 * nct), dim3(kGridSolveThreads), args, smem,
+                                      st) == cudaSuccess;
+}
+
+int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double* ysol, unsigned* gflags) {
     const size_t esmem = sizeof(float) * 3 * (size_t)(s.N + 1);
     const size_t smem = sizeof(double) * (2 * (size_t)(s.N + 1) + 32);
     if (esmem + 1024 > 48 * 1024)
         cudaFuncSetAttribute(k_exch_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
     if (smem + 1024 > 48 * 1024) cudaFuncSetAttribute(k_exch_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (exact) {
-        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 1, 0);
+        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 1, 0, nullptr);
         return 1;
     }
     const dim3 wgrid((s.N + 255) / 256, s.N < 65535 ? s.N : 65535);
     const dim3 rgrid(1, s.N < 256 ? s.N : 256);  // the retry's weights: a small grid-stride launch
+    int n = 0;
     for (int phase = 0; phase < 2; ++phase) {
         k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s, phase);
         k_exch_weights<<<phase ? rgrid : wgrid, 256, 0, st>>>(s, phase);
-        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase);
+        const bool grid = ysol && gflags && grid_solve(s, phase, ysol, gflags, st);
+        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase, grid ? ysol : nullptr);
+        n += grid ? 4 : 3;
     }
-    return 6;
+    return n;
 }
 
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st) {

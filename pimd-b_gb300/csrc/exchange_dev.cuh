@@ -247,6 +247,9 @@ __device__ inline void exact_backward(const Sys& s, double* vs, double* red) {
 // |log y| above which the next evaluation computes a fresh FP32 estimate
 // instead of reusing the current potentials, and above which the present
 // evaluation switches to the exact level-by-level recursion.
+constexpr int kGridSolveMinN = 768;     // from here the solve runs across SMs
+constexpr int kGridSolveCtas = 64;      // CTAs per direction
+constexpr int kGridSolveThreads = 256;
 constexpr double kRefreshLogY = 30.0;
 constexpr double kExactLogY = 200.0;
 // Pass 3, one direction (0 forward, 1 backward) by the whole block: the y
@@ -255,7 +258,9 @@ constexpr double kExactLogY = 200.0;
 // estimate was the previous evaluation's potentials, not a fresh FP32
 // recursion), no exact recursion is run: xflags[6] asks the caller to
 // retry with a fresh estimate instead.
-__device__ inline void solve_direction(const Sys& s, int dir, int force_exact, double* ys, int allow_exact = 1) {
+// `pre`: y of this direction already solved (k_exch_solve_grid), or null.
+__device__ inline void solve_direction(const Sys& s, int dir, int force_exact, double* ys, int allow_exact = 1,
+                                       const double* pre = nullptr) {
     double* acc = ys + s.N + 1;
     double* red = ys + 2 * (s.N + 1);
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
@@ -263,7 +268,12 @@ __device__ inline void solve_direction(const Sys& s, int dir, int force_exact, d
     int bad = force_exact, stale = 0;
     if (dir == 0) {
         if (!force_exact) {
-            blocked_solve(s.Wf, N + 1, ys, acc);
+            if (pre) {
+                for (int m = tid; m <= N; m += bd) ys[m] = ((volatile const double*)pre)[m];
+                __syncthreads();
+            } else {
+                blocked_solve(s.Wf, N + 1, ys, acc);
+            }
             for (int m = tid; m <= N; m += bd) {
                 const double y = ys[m];
                 const double ly = log(y);
@@ -296,7 +306,12 @@ __device__ inline void solve_direction(const Sys& s, int dir, int force_exact, d
     } else {
         if (!force_exact) {
             // nodes r = 0..N-1 <-> levels l = N..1
-            blocked_solve(s.Wb, N, ys, acc);
+            if (pre) {
+                for (int r = tid; r < N; r += bd) ys[r] = ((volatile const double*)pre)[r];
+                __syncthreads();
+            } else {
+                blocked_solve(s.Wb, N, ys, acc);
+            }
             for (int l = tid + 1; l < N; l += bd) {
                 const double y = ys[N - l];
                 const double ly = log(y);
@@ -333,9 +348,11 @@ __device__ inline void solve_direction(const Sys& s, int dir, int force_exact, d
     }
 }
 // After both directions (one block): the per-row factors of the connection
-// probabilities, which need both V and V_backwards, and V, V_backwards kept
-// as the estimates of the next evaluation.
-__device__ inline void solve_finish(const Sys& s) {
+// probabilities, which need both V and V_backwards, and the estimates of the
+// next evaluation: V, V_backwards themselves or, with `extrapolate` and a
+// previous result in s.Vp (NaN until there is one), the linear extrapolation
+// 2 V(t) - V(t - dt), which smooth dynamics keep much closer.
+__device__ inline void solve_finish(const Sys& s, int extrapolate = 0) {
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
     const double beta = s.beta_ex;
     volatile double* V = s.V;
@@ -349,8 +366,18 @@ __device__ inline void solve_finish(const Sys& s) {
     __syncthreads();
     const int need = ((volatile int*)s.xflags)[4] | ((volatile int*)s.xflags)[5];
     for (int m = tid; m <= N; m += bd) {
-        s.Vh[m] = V[m];
-        s.Vbh[m] = m >= 1 ? Vb[m] : 0.0;
+        const double v = V[m], vb = m >= 1 ? Vb[m] : 0.0;
+        if (s.Vp && extrapolate && isfinite(s.Vp[m]) && isfinite(s.Vp[N + 1 + m])) {
+            s.Vh[m] = 2.0 * v - s.Vp[m];
+            s.Vbh[m] = 2.0 * vb - s.Vp[N + 1 + m];
+        } else {
+            s.Vh[m] = v;
+            s.Vbh[m] = vb;
+        }
+        if (s.Vp) {
+            s.Vp[m] = v;
+            s.Vp[N + 1 + m] = vb;
+        }
     }
     if (tid == 0) {
         s.xflags[2] = 0;

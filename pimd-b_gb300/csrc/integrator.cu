@@ -1077,6 +1077,79 @@ static bool nm_warp3_fits(const Sys& s) {
     return (long long)D * ((s.N + 1) / 2) <= (long long)per * sms;
 }
 
+// The normal-mode propagator's step (normal_modes_propagator.cpp:19-71:
+// [COM], half-kick, free ring rotation) with the transforms in registers,
+// for P = 32, 64, 128: two warps per (particle pair, axis), warp 0 on p and
+// warp 1 on x; they swap modes in shared memory for the rotation.  No grid
+// barrier: the pending COM correction comes reduced (`cmv`, or null).
+template <int D, int E>
+__global__ void __launch_bounds__(64) k_nm_prop_warp(Sys s, const double* __restrict__ rot,
+                                                     const double* __restrict__ cmv,
+                                                     const double2* __restrict__ tw_g) {
+    constexpr int P = 32 * E;
+    __shared__ double2 tw[P / 2];
+    __shared__ double2 sm2[2][E][32];  // [0] p modes, [1] x modes
+    for (int t = threadIdx.x; t < P / 2; t += blockDim.x) tw[t] = tw_g[t];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;  // 0: p, 1: x
+    const int half = (s.N + 1) / 2;
+    const int u = blockIdx.x;
+    const int a = u / half, i2 = u % half;
+    const int ia = 2 * i2, ib = 2 * i2 + 1;
+    const bool va = ia < s.N, vb = ib < s.N;
+    const double cm = cmv ? cmv[a] : 0.0, hdt = 0.5 * s.dt;
+    double2 z[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int b = 32 * e + lane;
+        z[e] = make_double2(0.0, 0.0);
+        if (va) {
+            const size_t o = idx<D>(s, b, a, ia);
+            z[e].x = role == 0 ? (s.p[o] - cm) + hdt * nm_kick_force<D>(s, b, a, ia) : s.x[o];
+        }
+        if (vb) {
+            const size_t o = idx<D>(s, b, a, ib);
+            z[e].y = role == 0 ? (s.p[o] - cm) + hdt * nm_kick_force<D>(s, b, a, ib) : s.x[o];
+        }
+    }
+    warp_fft_fwd<E>(z, tw, P, lane);
+    warp_to_modes<E>(z, P, lane);
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) sm2[role][k1][lane] = z[k1];
+    __syncthreads();
+    const int k2 = (int)(__brev((unsigned)lane) >> 27);
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) {
+        const int k = k1 + E * k2;
+        const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+        const double2 pm = sm2[0][k1][lane], q = sm2[1][k1][lane];
+        auto turn = [&](double q0, double p0) -> double {
+            if (mw == 0.0) return role == 0 ? p0 : q0 + s.dt / s.mass * p0;
+            return role == 0 ? -mw * sn * q0 + cs * p0 : cs * q0 + sn / mw * p0;
+        };
+        z[k1] = make_double2(turn(q.x, pm.x), turn(q.y, pm.y));
+    }
+    warp_from_modes<E>(z, P, lane);
+    warp_fft_inv<E>(z, tw, P, lane);
+    double* dst = role == 0 ? s.p : s.x;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int b = 32 * e + lane;
+        if (va) dst[idx<D>(s, b, a, ia)] = z[e].x;
+        if (vb) dst[idx<D>(s, b, a, ib)] = z[e].y;
+    }
+}
+
+// The pending COM correction reduced once: cm[a] from the partial sums.
+template <int D>
+__global__ void k_com_mean(Sys s, const double* __restrict__ red_in, int nred, double* __restrict__ cm) {
+    __shared__ double shred[32];
+    double c[3] = {0.0, 0.0, 0.0};
+    com_from_partials<D>(s, red_in, nred, c, shred);
+    if (threadIdx.x == 0)
+        for (int a = 0; a < D; ++a) cm[a] = c[a];
+}
+
 // Warps per block of the warp kernel: the fewest (spreading the pairs over
 // the most SMs) with which every block is resident at once; 0 if none fits.
 template <int D, int E>
@@ -1410,11 +1483,37 @@ static void nm_prop_launch(const Sys& s, const double* C, const double* T, const
     k_nm_propagate<D><<<grid, kNmThreads, smem, st>>>(s, C, T, rot, com_apply, red_in, nred_in);
 }
 
-void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, const double* rot, int com_apply,
-                         const double* red_in, int nred_in, cudaStream_t st) {
+template <int D, int E>
+static void nm_prop_warp_t(const Sys& s, const double* rot, int com_apply, const double* red_in, int nred_in,
+                           const double2* tw, double* cm, cudaStream_t st) {
+    if (com_apply) k_com_mean<D><<<1, 256, 0, st>>>(s, red_in, nred_in, cm);
+    const unsigned units = (unsigned)(D * ((s.N + 1) / 2));
+    k_nm_prop_warp<D, E><<<units, 64, 0, st>>>(s, rot, com_apply ? cm : nullptr, tw);
+}
+
+template <int D>
+static bool nm_prop_warp_d(const Sys& s, const double* rot, int com_apply, const double* red_in, int nred_in,
+                           const double2* tw, double* cm, cudaStream_t st) {
+    if (s.P == 32) nm_prop_warp_t<D, 1>(s, rot, com_apply, red_in, nred_in, tw, cm, st);
+    else if (s.P == 64) nm_prop_warp_t<D, 2>(s, rot, com_apply, red_in, nred_in, tw, cm, st);
+    else if (s.P == 128) nm_prop_warp_t<D, 4>(s, rot, com_apply, red_in, nred_in, tw, cm, st);
+    else return false;
+    return true;
+}
+
+int launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, const double* rot, int com_apply,
+                        const double* red_in, int nred_in, const double2* tw, double* cm, cudaStream_t st) {
+    if (tw && cm) {
+        bool done = false;
+        if (D == 1) done = nm_prop_warp_d<1>(s, rot, com_apply, red_in, nred_in, tw, cm, st);
+        else if (D == 2) done = nm_prop_warp_d<2>(s, rot, com_apply, red_in, nred_in, tw, cm, st);
+        else done = nm_prop_warp_d<3>(s, rot, com_apply, red_in, nred_in, tw, cm, st);
+        if (done) return com_apply ? 2 : 1;
+    }
     if (D == 1) nm_prop_launch<1>(s, C, T, rot, com_apply, red_in, nred_in, st);
     else if (D == 2) nm_prop_launch<2>(s, C, T, rot, com_apply, red_in, nred_in, st);
     else nm_prop_launch<3>(s, C, T, rot, com_apply, red_in, nred_in, st);
+    return 1;
 }
 
 }  // namespace pimdb

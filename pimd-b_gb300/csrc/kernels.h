@@ -52,7 +52,12 @@ void launch_exchange_energies(const Sys& s, int D, cudaStream_t st);
 // Returns the number of kernels launched (6: estimate, weights, solve and
 // their retry, which exits at once unless a reused estimate failed; or 1
 // with `exact`: the reference-order FP64 log-sum-exp recursion only).
-int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st);
+// For N >= 768 the solve runs across SMs when `ysol` (exchange_grid_doubles)
+// and `gflags` (exchange_grid_flags, zeroed once) are given.
+int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double* ysol = nullptr,
+                               unsigned* gflags = nullptr);
+size_t exchange_grid_doubles(const Sys& s);
+size_t exchange_grid_flags(const Sys& s);
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st);
 void launch_exchange_estimators(const Sys& s, cudaStream_t st);
 
@@ -111,8 +116,10 @@ void launch_cart_update(const Sys& s, int D, int flags, const double* red_in, in
                         StepRef step, int substep, int kick_nm, cudaStream_t st);
 void launch_nm_thermo(const Sys& s, int D, const double* C, const double* T, int flags, const double* red_in,
                       int nred_in, double* red_out, StepRef step, int substep, cudaStream_t st);
-void launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, const double* rot, int com_apply,
-                         const double* red_in, int nred_in, cudaStream_t st);
+// With `tw` (FFT twiddles) and `cm` (3 doubles of scratch), P = 32, 64, 128
+// run the register-transform kernel; returns the number of kernels launched.
+int launch_nm_propagate(const Sys& s, int D, const double* C, const double* T, const double* rot, int com_apply,
+                        const double* red_in, int nred_in, const double2* tw, double* cm, cudaStream_t st);
 
 // Fused normal-mode step (normal-mode propagator + normal-mode Langevin):
 // mode bit 0 = tail of step-1 (kick, O, COM), bit 1 = head of step (O, COM,

@@ -113,6 +113,13 @@ TRAJ_CASES = {
                                               ext_p=(1.0 * 0.036749326e-3, 0, 0)),
     "nm_nmthermo_bosons_P32_1d": dict(ndim=1, natoms=6, nbeads=32, propagator="normal_modes", nmthermostat=True,
                                       ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    # the normal-mode propagator without the normal-mode thermostat, P = 32, 64, 128
+    "nm_langevin_dist_P64": dict(natoms=9, nbeads=64, bosonic=False, propagator="normal_modes",
+                                 ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    "nm_none_bosons_P32_nofixcom": dict(natoms=6, nbeads=32, propagator="normal_modes", thermostat="none",
+                                        fixcom=False, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+    "nm_langevin_bosons_P128_2d": dict(ndim=2, natoms=5, nbeads=128, propagator="normal_modes",
+                                       ext="harmonic", ext_p=(1.0 * 0.036749326e-3, 0, 0)),
     # too many pairs for three warps each to be resident at once: one warp each
     "nm_nmthermo_dist_P32_N2300": dict(natoms=2300, nbeads=32, bosonic=False, propagator="normal_modes",
                                        nmthermostat=True, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0),
@@ -120,7 +127,8 @@ TRAJ_CASES = {
 }
 # options applied to the GPU side only
 TRAJ_OPTIONS = {"nm_nmthermo_bosons_aziz": [{}, {"fused_normal_modes": 0}, {"fft_normal_modes": 0}],
-                "nm_nmthermo_bosons_P64_aziz": [{}, {"fft_normal_modes": 0}, {"fused_normal_modes": 0}]}
+                "nm_nmthermo_bosons_P64_aziz": [{}, {"fft_normal_modes": 0}, {"fused_normal_modes": 0}],
+                "nm_langevin_dist_P64": [{}, {"fft_normal_modes": 0}]}
 
 
 def _run_pair(kw, steps, seed_state=3, options=None):
