@@ -77,6 +77,7 @@ struct pimdb_handle {
     // directions and the publication flags
     double* d_ysol = nullptr;
     double* d_cm = nullptr;  // the pending COM correction, reduced (3 doubles)
+    double* d_ework = nullptr;  // link prefix sums and wrapped end beads (large N)
     unsigned* d_gflags = nullptr;
     // CUDA graphs of pimdb_step_async: keyed by the step count and the
     // host-side step state at entry; the step index comes from d_step, which
@@ -339,6 +340,7 @@ static void free_handle(pimdb_handle* h) {
     if (h->h_err) cudaFreeHost(h->h_err);
     if (h->d_ysol) cudaFree(h->d_ysol);
     if (h->d_cm) cudaFree(h->d_cm);
+    if (h->d_ework) cudaFree(h->d_ework);
     if (h->d_gflags) cudaFree(h->d_gflags);
     if (h->d_noise) cudaFree(h->d_noise);
     if (h->d_pnm) cudaFree(h->d_pnm);
@@ -410,6 +412,8 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
         if (e == cudaSuccess) e = cudaMemset(s.Vp, 0xff, 2 * ((size_t)s.N + 1) * sizeof(double));
     }
     if (e == cudaSuccess) e = alloc(&h->d_cm, 3);
+    if (e == cudaSuccess && s.bosonic && exchange_energy_doubles(s, h->D) > 0)
+        e = alloc(&h->d_ework, exchange_energy_doubles(s, h->D));
     if (e == cudaSuccess && s.bosonic && exchange_grid_doubles(s) > 0) {
         e = alloc(&h->d_ysol, exchange_grid_doubles(s));
         if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_gflags, exchange_grid_flags(s) * sizeof(unsigned));
@@ -658,7 +662,8 @@ static void exchange_front(pimdb_handle* h, cudaStream_t st) {
         launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_factorial_sums(s, h->D, h->d_fact, st); }, 2);
         return;
     }
-    launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, st); });
+    launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, st, h->d_ework); },
+           h->d_ework ? 2 : 1);
     const int ex = h->opt_exact_exchange;
     launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_exchange_recursions(s, ex, st, h->d_ysol, h->d_gflags); },
            ex ? 1 : (h->d_ysol ? 8 : 6));
@@ -895,7 +900,10 @@ static bool graph_steps(pimdb_handle* h, int nsteps) {
         launch_step_advance(h->d_step, nsteps, h->stream);
         h->capturing = false;
         cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
-        if (e == cudaSuccess && h->async_err == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+        // kernel nodes keep the priority of the stream they were captured on
+        // (the exchange chain's stream is the higher one)
+        if (e == cudaSuccess && h->async_err == cudaSuccess)
+            e = cudaGraphInstantiateWithFlags(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
         if (graph) cudaGraphDestroy(graph);
         g.after = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
         g.kernels = h->launches - launches0 + 1;

@@ -46,6 +46,120 @@ __global__ void k_exch_energies(Sys s) {
     energy_row<D>(s, v, lane);
 }
 
+// Cycle energies for large N without a scan per row.  The row recursion
+// telescopes: E[v][u] = k/2 (L[v] - L[u] + |xP_v - x1_u|^2) with the prefix
+// sums L[w] = sum_{t<w} |x1_{t+1} - xP_t|^2 of the interior links, so every
+// entry is independent.  L is kept in double-double (hi, lo): the difference
+// of two long prefix sums then keeps the accuracy of the direct sum.
+// k_link_prefix (one block) builds L and the beads' positions wrapped into
+// the box; k_exch_energies_flat (one block per row) writes E and Et.
+__device__ __forceinline__ void dd_add(double ah, double al, double bh, double bl, double& h, double& l) {
+    const double s = ah + bh;
+    const double bb = s - ah;
+    double e = (ah - (s - bb)) + (bh - bb);
+    e += al + bl;
+    h = s + e;
+    l = e - (h - s);
+}
+
+template <int D>
+__global__ void __launch_bounds__(1024) k_link_prefix(Sys s, double* __restrict__ Lh, double* __restrict__ Ll,
+                                                       double* __restrict__ wrap) {
+    __shared__ double sh[32], sl[32];
+    const int N = s.N, tid = threadIdx.x, nt = blockDim.x;
+    const int first = 0, last = s.P - 1;
+    // positions of beads 1 and P wrapped into [-L/2, L/2): wrap[side][a][N]
+    for (int i = tid; i < N; i += nt)
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double x1 = s.x[idx<D>(s, first, a, i)], xP = s.x[idx<D>(s, last, a, i)];
+            if (s.pbc) {
+                x1 -= s.L * rint(x1 * s.invL);
+                xP -= s.L * rint(xP * s.invL);
+            }
+            wrap[(size_t)a * N + i] = x1;
+            wrap[(size_t)(D + a) * N + i] = xP;
+        }
+    // contiguous chunk per thread, double-double sums, then a scan of the chunks
+    const int chunk = (N + nt - 1) / nt;
+    const int w0 = tid * chunk, w1 = min(N, w0 + chunk);
+    double th = 0.0, tl = 0.0;
+    for (int w = w0; w < w1 && w + 1 <= N - 1; ++w) {
+        double d2 = sepsq<D>(s, last, w, first, w + 1);
+        dd_add(th, tl, d2, 0.0, th, tl);
+    }
+    // inclusive warp scan, then across warps
+    const int lane = tid & 31, warp = tid >> 5;
+    double ih = th, il = tl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double yh = __shfl_up_sync(0xffffffffu, ih, o), yl = __shfl_up_sync(0xffffffffu, il, o);
+        if (lane >= o) dd_add(yh, yl, ih, il, ih, il);
+    }
+    if (lane == 31) {
+        sh[warp] = ih;
+        sl[warp] = il;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        double wh = lane < nt / 32 ? sh[lane] : 0.0, wl = lane < nt / 32 ? sl[lane] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double yh = __shfl_up_sync(0xffffffffu, wh, o), yl = __shfl_up_sync(0xffffffffu, wl, o);
+            if (lane >= o) dd_add(yh, yl, wh, wl, wh, wl);
+        }
+        sh[lane] = wh;
+        sl[lane] = wl;
+    }
+    __syncthreads();
+    // exclusive prefix of this thread's chunk
+    double ph = 0.0, pl = 0.0;
+    if (warp > 0) {
+        ph = sh[warp - 1];
+        pl = sl[warp - 1];
+    }
+    const double xh = __shfl_up_sync(0xffffffffu, ih, 1), xl = __shfl_up_sync(0xffffffffu, il, 1);
+    if (lane > 0) dd_add(ph, pl, xh, xl, ph, pl);
+    for (int w = w0; w < w1; ++w) {
+        Lh[w] = ph;
+        Ll[w] = pl;
+        if (w + 1 <= N - 1) {
+            const double d2 = sepsq<D>(s, last, w, first, w + 1);
+            dd_add(ph, pl, d2, 0.0, ph, pl);
+        }
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_exch_energies_flat(Sys s, const double* __restrict__ Lh,
+                                                            const double* __restrict__ Ll,
+                                                            const double* __restrict__ wrap) {
+    const int N = s.N, v = blockIdx.x;
+    const double hk = 0.5 * s.kappa;
+    const long long half_bits = __double_as_longlong(0.5 * s.L);
+    double xv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xv[a] = wrap[(size_t)(D + a) * N + v];
+    const double lvh = Lh[v], lvl = Ll[v];
+    double* row = s.E + tri(v);
+    for (int u = threadIdx.x; u <= v; u += blockDim.x) {
+        double c = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double d = xv[a] - wrap[(size_t)a * N + u];
+            if (s.pbc) {
+                const long long bits = __double_as_longlong(d);
+                if ((bits & 0x7fffffffffffffffLL) > half_bits) d -= copysign(s.L, d);
+            }
+            c = fma(d, d, c);
+        }
+        const double e = hk * (((lvh - Lh[u]) + (lvl - Ll[u])) + c);
+        row[u] = e;
+        // backward node r = N - u depends on node r' = N - 1 - v
+        if (u >= 1) s.Et[tri(N - u - 1) + (N - 1 - v)] = e;
+    }
+}
+
 // Pass 1: block 0 forward, block 1 backward.  Phase 0 skips (early exit)
 // when the previous evaluation's exact potentials are still a good estimate
 // (xflags[3] == 0) and records in xflags[7] that they were reused; phase 1
@@ -66,8 +180,12 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_estimate(Sys s, int phase
 // (grid-stride over rows; phase 1 runs only on a retry).
 __global__ void k_exch_weights(Sys s, int phase) {
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    __shared__ double tbl[32];
+    if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
+    __syncthreads();
     for (int p = blockIdx.y; p < s.N; p += gridDim.y)
-        for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= p; u += gridDim.x * blockDim.x) exch_weight(s, p, u);
+        for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= p; u += gridDim.x * blockDim.x)
+            exch_weight(s, p, u, tbl);
 }
 
 // Pass 3: block 0 forward, block 1 backward.  Phase 0 may not fall back to
@@ -211,7 +329,27 @@ __global__ void k_exch_estimators(Sys s, int nbeads) {
     estimators_block(s, nbeads, sh);
 }
 
-void launch_exchange_energies(const Sys& s, int D, cudaStream_t st) {
+size_t exchange_energy_doubles(const Sys& s, int D) {
+    return s.N >= kFlatEnergiesMinN ? (size_t)(2 + 2 * D) * s.N : 0;
+}
+
+void launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work) {
+    if (work && s.N >= kFlatEnergiesMinN) {
+        double* Lh = work;
+        double* Ll = work + s.N;
+        double* wrap = work + 2 * (size_t)s.N;
+        if (D == 1) {
+            k_link_prefix<1><<<1, 1024, 0, st>>>(s, Lh, Ll, wrap);
+            k_exch_energies_flat<1><<<s.N, 256, 0, st>>>(s, Lh, Ll, wrap);
+        } else if (D == 2) {
+            k_link_prefix<2><<<1, 1024, 0, st>>>(s, Lh, Ll, wrap);
+            k_exch_energies_flat<2><<<s.N, 256, 0, st>>>(s, Lh, Ll, wrap);
+        } else {
+            k_link_prefix<3><<<1, 1024, 0, st>>>(s, Lh, Ll, wrap);
+            k_exch_energies_flat<3><<<s.N, 256, 0, st>>>(s, Lh, Ll, wrap);
+        }
+        return;
+    }
     const int warps = 2;
     dim3 grid((s.N + warps - 1) / warps);
     if (D == 1) k_exch_energies<1><<<grid, warps * 32, 0, st>>>(s);

@@ -7,6 +7,7 @@
 #include <math_constants.h>
 
 #include "common.cuh"
+#include "forces_dev.cuh"  // exp_tang
 
 namespace pimdb {
 __device__ __forceinline__ size_t tri(int v) { return (size_t)v * (size_t)(v + 1) / 2; }
@@ -199,14 +200,20 @@ __device__ inline void estimate_direction(const Sys& s, int dir, float* fsm) {
     }
 }
 // Pass 2: the FP64 weights of packed entry (row p, column u), both directions.
-__device__ __forceinline__ void exch_weight(const Sys& s, int p, int u) {
+// `tbl`: the exp_tang table in shared memory (null: CUDA's exp).  Arguments
+// of 709 and more give infinity either way (the solve then retries).
+__device__ __forceinline__ double weight_exp(double x, const double* tbl) {
+    if (!tbl) return exp(x);
+    return x < 709.0 ? exp_tang(x, tbl) : (double)INFINITY;
+}
+__device__ __forceinline__ void exch_weight(const Sys& s, int p, int u, const double* tbl = nullptr) {
     const double beta = s.beta_ex;
     const size_t e = tri(p) + u;
     const double E = s.E[e];
     const double inv = 1.0 / (p + 1);
-    s.Wf[e] = exp(-beta * (E + s.Vh[u] - s.Vh[p + 1])) * inv;
+    s.Wf[e] = weight_exp(-beta * (E + s.Vh[u] - s.Vh[p + 1]), tbl) * inv;
     // backward node r = N - u from node r' = N - 1 - p (u >= 1)
-    if (u >= 1) s.Wb[tri(s.N - u - 1) + (s.N - 1 - p)] = exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u])) * inv;
+    if (u >= 1) s.Wb[tri(s.N - u - 1) + (s.N - 1 - p)] = weight_exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u]), tbl) * inv;
 }
 // Exact level-by-level FP64 log-sum-exp in the reference's order (used only
 // when the estimate is unusable, or on request).  `vs` holds N+1 doubles,
@@ -248,6 +255,7 @@ __device__ inline void exact_backward(const Sys& s, double* vs, double* red) {
 // instead of reusing the current potentials, and above which the present
 // evaluation switches to the exact level-by-level recursion.
 constexpr int kGridSolveMinN = 768;     // from here the solve runs across SMs
+constexpr int kFlatEnergiesMinN = 512;  // from here the cycle energies come from link prefix sums
 constexpr int kGridSolveCtas = 64;      // CTAs per direction
 constexpr int kGridSolveThreads = 256;
 constexpr double kRefreshLogY = 30.0;

@@ -48,7 +48,10 @@ void launch_energy_terms(const Sys& s, int D, double* part, cudaStream_t st);
 void launch_local_energy(const Sys& s, int D, int n, const int* items, double* out, cudaStream_t st);
 
 // exchange.cu: Feldman-Hirshberg exchange on beads 1 and P.
-void launch_exchange_energies(const Sys& s, int D, cudaStream_t st);
+// For N >= 512 with `work` (exchange_energy_doubles) the energies come from
+// the links' prefix sums, one independent entry per thread.
+void launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work = nullptr);
+size_t exchange_energy_doubles(const Sys& s, int D);
 // Returns the number of kernels launched (6: estimate, weights, solve and
 // their retry, which exits at once unless a reused estimate failed; or 1
 // with `exact`: the reference-order FP64 log-sum-exp recursion only).
