@@ -247,18 +247,31 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
     for (int e = tid; e < nown * 32; e += blockDim.x) acc[e] = 0.0;
     if (tid == 0) abort_solve = 0;
     __syncthreads();
+    const int i = tid >> 3, part = tid & 7;  // update role: row of the block, quarter of the columns
+    // the next block's weights, loaded while its predecessor is awaited (only
+    // the CTA owning block j + 1 is on the critical path): the diagonal block
+    // (warp 0) and W[rows of j + 1][block j]
+    double wd[32], wn[4];
+    auto prefetch = [&](int b) {  // b: the block about to be resolved by this CTA
+        if (warp == 0) {
+            const int n = 32 * b + lane;
+#pragma unroll
+            for (int t = 0; t < 32; ++t) wd[t] = (n < nn && n >= 1 && t < lane) ? W[tri(n - 1) + 32 * b + t] : 0.0;
+        }
+        const int n = 32 * b + i;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) wn[q] = (b >= 1 && n < nn) ? W[tri(n - 1) + 32 * (b - 1) + 4 * part + q] : 0.0;
+    };
+    if (c == 0) prefetch(0);
     for (int j = 0; j < nb; ++j) {
         if (j % nct == c) {
             if (warp == 0) {
                 const int n = 32 * j + lane;
                 double a = n == 0 ? 1.0 : (n < nn ? acc[(j / nct) * 32 + lane] : 0.0);
-                double w[32];
-#pragma unroll
-                for (int t = 0; t < 32; ++t) w[t] = (n < nn && n >= 1 && t < lane) ? W[tri(n - 1) + 32 * j + t] : 0.0;
 #pragma unroll
                 for (int t = 0; t < 32; ++t) {
                     const double yt = __shfl_sync(0xffffffffu, a, t);
-                    if (lane > t) a = fma(w[t], yt, a);
+                    if (lane > t) a = fma(wd[t], yt, a);
                 }
                 if (n < nn) y[n] = a;
                 yj[lane] = n < nn ? a : 0.0;
@@ -266,17 +279,20 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
                 __syncwarp();
                 if (lane == 0) atomicExch(&flags[j], 1u);
             }
-        } else if (tid == 0) {
-            unsigned it = 0;
-            while (((volatile unsigned*)flags)[j] == 0u) {
-                if (++it > (1u << 22)) {
-                    atomicOr(s.err, ERRB_TIMEOUT);
-                    abort_solve = 1;
-                    break;
+        } else {
+            if ((j + 1) % nct == c && j + 1 < nb) prefetch(j + 1);
+            if (tid == 0) {
+                unsigned it = 0;
+                while (((volatile unsigned*)flags)[j] == 0u) {
+                    if (++it > (1u << 22)) {
+                        atomicOr(s.err, ERRB_TIMEOUT);
+                        abort_solve = 1;
+                        break;
+                    }
+                    if (it > 64) __nanosleep(32);
                 }
-                __nanosleep(32);
+                __threadfence();
             }
-            __threadfence();
         }
         __syncthreads();
         if (abort_solve) break;
@@ -285,16 +301,21 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
             yj[tid] = n < nn ? ((volatile double*)y)[n] : 0.0;
         }
         __syncthreads();
-        // rows this CTA owns below block j: W[rows][block j] y_j
-        const int i = tid >> 3, part = tid & 7;  // row of the block, quarter of the columns
+        // rows this CTA owns below block j: W[rows][block j] y_j, the next
+        // block first from the prefetched weights
         for (int r = c; r < nb; r += nct) {
             if (r <= j) continue;
             const int n = 32 * r + i;
             double sum = 0.0;
             if (n < nn) {
-                const double* row = W + tri(n - 1) + 32 * j + 4 * part;
+                if (r == j + 1) {
 #pragma unroll
-                for (int q = 0; q < 4; ++q) sum = fma(row[q], yj[4 * part + q], sum);
+                    for (int q = 0; q < 4; ++q) sum = fma(wn[q], yj[4 * part + q], sum);
+                } else {
+                    const double* row = W + tri(n - 1) + 32 * j + 4 * part;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) sum = fma(row[q], yj[4 * part + q], sum);
+                }
             }
             sum += __shfl_xor_sync(0xffffffffu, sum, 1);
             sum += __shfl_xor_sync(0xffffffffu, sum, 2);
