@@ -247,6 +247,7 @@ void sys_params_from_config(const pimdb_config& c, Sys& s) {
     s.invL = 1.0 / c.size;
     s.mass = c.mass;
     s.dt = c.dt;
+    s.dt_m = c.dt / c.mass;
     // simulation.cpp:37-52 (IPI convention, kB = hbar = 1)
     const double beta = 1.0 / (1.0 * c.temperature);
     const double thermo_beta = beta / c.nbeads;

@@ -111,7 +111,7 @@ __device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int s
                 if (com_in) p -= cm[a];
                 if (kick) p += 0.5 * s.dt * s.f[e];
                 if (o) p = s.c1 * p + s.c2 * (h == 0 ? z0 : z1);
-                if (drift) s.x[e] += s.dt * p / s.mass;
+                if (drift) s.x[e] = fma(p, s.dt_m, s.x[e]);
                 s.p[e] = p;
                 sum[a] += p;
             }
@@ -216,7 +216,7 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
 // The Feldman-Hirshberg exchange of one replica by the whole block; adds the
 // exterior springs to f on beads 1 and P (which hold the physical forces).
 template <int D>
-__device__ void batch_exchange(const Sys& s, unsigned char* work) {
+__device__ void batch_exchange(const Sys& s, unsigned char* work, const double* tbl) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int N = s.N;
     for (int v = warp; v < N; v += nw) energy_row<D>(s, v, lane);
@@ -231,7 +231,7 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work) {
             __syncthreads();
         }
         for (int p = warp; p < N; p += nw)
-            for (int u = lane; u <= p; u += 32) exch_weight(s, p, u);
+            for (int u = lane; u <= p; u += 32) exch_weight(s, p, u, tbl);
         __syncthreads();
         // a reused estimate that fails is replaced by a fresh one (second
         // attempt) rather than by the exact recursion
@@ -252,7 +252,8 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work) {
 }
 
 template <int D, typename R>
-__device__ void batch_replica(const Sys& s, int flags, long long step, int mode, double* red, unsigned char* work) {
+__device__ void batch_replica(const Sys& s, int flags, long long step, int mode, double* red, unsigned char* work,
+                              const double* tbl) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const bool langevin = flags & BF_LANGEVIN, fixcom = flags & BF_FIXCOM;
     const double inv_np = 1.0 / ((double)s.N * s.P);
@@ -278,7 +279,7 @@ __device__ void batch_replica(const Sys& s, int flags, long long step, int mode,
         for (int b = warp; b < s.P; b += nw) bead_forces_warp<D, R>(s, b, lane, stage);
         __syncthreads();
         if (s.bosonic) {
-            batch_exchange<D>(s, work);
+            batch_exchange<D>(s, work, tbl);
             __syncthreads();
         }
     }
@@ -310,6 +311,8 @@ __global__ void __launch_bounds__(kBatchMaxThreads)
     unsigned char* work = bsm + 3 * 32 * sizeof(double);
     __shared__ Sys ss;
     __shared__ int item, sflags;
+    __shared__ double tbl[32];  // exp_tang's table
+    if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
     const long long step = *(volatile long long*)step_ctr;
     for (;;) {
         if (threadIdx.x == 0) item = atomicAdd(&ctl[0], 1);
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads)
         }
         __syncthreads();
         if (k >= nrep) break;
-        batch_replica<D, R>(ss, sflags, step, mode, red, work);
+        batch_replica<D, R>(ss, sflags, step, mode, red, work, tbl);
         __syncthreads();
     }
     if (threadIdx.x == 0) {

@@ -37,6 +37,7 @@ struct Sys {
     int pbc;
     double L, invL; // box edge and its inverse
     double mass, dt;
+    double dt_m;    // dt / mass (the drift multiplies: FP64 division costs ~8 FP64 operations)
     double kappa;   // spring constant m omega_p^2
     double beta_ex; // exchange beta = beta/P
     double omega_p;

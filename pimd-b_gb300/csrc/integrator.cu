@@ -153,7 +153,7 @@ __global__ void k_cart_update(Sys s, int flags, const double* __restrict__ red_i
                 p += 0.5 * s.dt * fk;
             }
             if (flags & SF_LANGEVIN) p = s.c1 * p + s.c2 * (h == 0 ? z.x : z.y);
-            if (flags & SF_DRIFT) s.x[o] += s.dt * p / s.mass;
+            if (flags & SF_DRIFT) s.x[o] = fma(p, s.dt_m, s.x[o]);
             s.p[o] = p;
             part[a] += p;
         }
@@ -285,8 +285,8 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
         const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
         double qa, qb, pa, pb;
         if (mw == 0.0) {
-            qa = q0 + s.dt / s.mass * p0;
-            qb = q1 + s.dt / s.mass * p1;
+            qa = q0 + s.dt_m * p0;
+            qb = q1 + s.dt_m * p1;
             pa = p0;
             pb = p1;
         } else {
@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
                 const double q = sy[o];
                 const double pk = sq[o] + hdt * sg[o];
                 if (mw == 0.0) {
-                    sy[o] = q + s.dt / s.mass * pk;
+                    sy[o] = q + s.dt_m * pk;
                     sq[o] = pk;
                 } else {
                     sy[o] = cs * q + sn / mw * pk;
@@ -903,7 +903,7 @@ __global__ void __launch_bounds__(256) k_nm_warp(Sys s, const double* __restrict
             auto turn = [&](double& q, double& pm, double g) {
                 const double q0 = q, pk = pm + hdt * g;
                 if (mw == 0.0) {
-                    q = q0 + s.dt / s.mass * pk;
+                    q = q0 + s.dt_m * pk;
                     pm = pk;
                 } else {
                     q = cs * q0 + sn / mw * pk;
@@ -1037,7 +1037,7 @@ __global__ void __launch_bounds__(96) k_nm_warp3(Sys s, const double* __restrict
                 auto turn = [&](double& qv, double& pm, double gv) {
                     const double q0 = qv, pk = pm + hdt * gv;
                     if (mw == 0.0) {
-                        qv = q0 + s.dt / s.mass * pk;
+                        qv = q0 + s.dt_m * pk;
                         pm = pk;
                     } else {
                         qv = cs * q0 + sn / mw * pk;
@@ -1124,7 +1124,7 @@ __global__ void __launch_bounds__(64) k_nm_prop_warp(Sys s, const double* __rest
         const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
         const double2 pm = sm2[0][k1][lane], q = sm2[1][k1][lane];
         auto turn = [&](double q0, double p0) -> double {
-            if (mw == 0.0) return role == 0 ? p0 : q0 + s.dt / s.mass * p0;
+            if (mw == 0.0) return role == 0 ? p0 : q0 + s.dt_m * p0;
             return role == 0 ? -mw * sn * q0 + cs * p0 : cs * q0 + sn / mw * p0;
         };
         z[k1] = make_double2(turn(q.x, pm.x), turn(q.y, pm.y));
