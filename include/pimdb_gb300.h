@@ -288,7 +288,12 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
  *                    with at least 4 cutoff-wide cells per edge) on / off /
  *                    automatic (default: on from 512 particles);
  *   "cuda_graphs"    0: enqueue every step's kernels instead of replaying a
- *                    captured graph (default 1). */
+ *                    captured graph (default 1);
+ *   "pair_entry_cap" pair-tile kernel: gradients held in shared memory per
+ *                    warp (a multiple of 32 up to 1024; 0 = default).  Fewer
+ *                    let more warps share an SM; a tile with more pairs
+ *                    inside the cutoff is summed in chunks (same result up to
+ *                    the order of its j-side additions). */
 int pimdb_set_option(pimdb_handle* h, const char* name, int value);
 
 /* Bosonic exchange without any allocation (no counterpart in the reference).

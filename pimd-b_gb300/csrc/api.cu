@@ -1237,6 +1237,10 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
         h->opt_cells = value < 0 ? -1 : (value ? 1 : 0);
     } else if (n == "cuda_graphs") {
         h->opt_graph = value ? 1 : 0;
+    } else if (n == "pair_entry_cap") {
+        if (value < 0 || value > 1024 || value % 32)
+            return fail(h, PIMDB_ERR_ARG, "pair_entry_cap must be 0 or a multiple of 32 up to 1024");
+        h->s.pair_cap = value;
     } else return fail(h, PIMDB_ERR_ARG, "unknown option " + n);
     return PIMDB_OK;
 }

@@ -47,6 +47,7 @@ struct Sys {
     double ext_a, ext_b, ext_c; // harmonic: k | double well: 4 m s, loc^2, m s | cosine: -A k, k, phase
     int int_kind;
     double int_a;               // harmonic pair: k | dipole: strength
+    int pair_cap;               // pair-tile gradient capacity per warp (0: the default)
     uint64_t seed;
     uint32_t replica;
     // device arrays

@@ -282,19 +282,29 @@ __global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ 
 // dx - L floor(dx/L + 1/2).  The exponentials use exp_tang.  Same result as
 // k_pair_tiles up to rounding; the exact FP64 cutoff test is applied in step 2.
 constexpr int kCompactWarps = 2;
+// gradient capacity per warp unless Sys::pair_cap says otherwise
+constexpr int kCompactDefaultCap = 704;
 
+// Per-warp shared memory: the fixed part below, then the gradients of up to
+// `cap` entries (double[cap][D]) and their evaluation order
+// (unsigned short[cap]).  A tile with more entries inside the cutoff than
+// `cap` is evaluated and summed in chunks of `cap` entries.
 template <int D>
 struct CompactSmem {
     double xi[kTile][D], xj[kTile][D];  // wrapped into the box under PBC
     float xjf[kTile][D];                // FP32 copy of xj for the screen (hi part)
     float xjl[kTile][D];                // lo part, xj - xjf (mixed far path)
-    double g[kTile * kTile][D];
     unsigned char ilist[kTile][kTile];  // j's of lane i, bit 7 = short-range
     unsigned short jlist[kTile][kTile]; // (i << 8 | k) entries of lane j
     int icnt[kTile], jcnt[kTile], off[kTile];
     unsigned char fi[kTile * kTile], fj[kTile * kTile];  // fi bit 7 = short-range
-    unsigned short perm[kTile * kTile]; // evaluation order
 };
+constexpr int kCompactMaxCap = kTile * kTile;
+// bytes of one warp's shared memory for a gradient capacity of `cap` entries
+template <int D>
+__host__ __device__ constexpr size_t compact_warp_bytes(int cap) {
+    return (sizeof(CompactSmem<D>) + (size_t)cap * (D * sizeof(double) + sizeof(unsigned short)) + 15) / 16 * 16;
+}
 
 // d in (-L, L) -> its minimum image; `half_bits` = bit pattern of L/2.
 __device__ __forceinline__ double min_image_wrapped(double d, double L, long long half_bits) {
@@ -310,7 +320,8 @@ __device__ __forceinline__ double min_image_wrapped(double d, double L, long lon
 // cancel and FP32 would lose the difference.  Sums are FP64 either way.
 template <int D, bool kMixed>
 __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ part, int T, int b, int w,
-                                             CompactSmem<D>& sm, const double* tbl, int lane) {
+                                             CompactSmem<D>& sm, double (*g)[D], unsigned short* perm, int cap,
+                                             const double* tbl, int lane) {
     int it = (int)((2.0 * T + 1.0 - sqrt((2.0 * T + 1.0) * (2.0 * T + 1.0) - 8.0 * w)) * 0.5);
     while (it > 0 && it * T - it * (it - 1) / 2 > w) --it;
     while ((it + 1) * T - (it + 1) * it / 2 <= w) ++it;
@@ -382,22 +393,9 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         sm.fj[off + k] = (unsigned char)(e & 31);
     }
     __syncwarp();
-    // evaluation order: short-range entries, then the rest
-    const unsigned lt = (1u << lane) - 1u;
-    int pos = 0, nnear = 0;
-    for (int pass = 0; pass < 2; ++pass) {
-        for (int f0 = 0; f0 < total; f0 += 32) {
-            const int f = f0 + lane;
-            const bool take = f < total && ((sm.fi[f] >> 7) == (pass == 0 ? 1 : 0));
-            const unsigned bal = __ballot_sync(0xffffffffu, take);
-            if (take) sm.perm[pos + __popc(bal & lt)] = (unsigned short)f;
-            pos += __popc(bal);
-        }
-        if (pass == 0) nnear = pos;
-    }
-    __syncwarp();
     const long long half_bits = __double_as_longlong(0.5 * s.L);
     const double cut2 = cut * cut;
+    const long long cut2_bits = __double_as_longlong(cut2);
     auto separation = [&](int f, double* r) {
         const int il = sm.fi[f] & 31, jl = sm.fj[f];
         double r2 = 0.0;
@@ -410,9 +408,29 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         }
         return r2;
     };
+    double ai[D], aj[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) ai[a] = aj[a] = 0.0;
+    const unsigned lt = (1u << lane) - 1u;
+    const int jc = sm.jcnt[lane];
+    for (int c0 = 0; c0 < total; c0 += cap) {
+    const int cend = min(total, c0 + cap), cn = cend - c0;
+    // evaluation order within the chunk: short-range entries, then the rest
+    int pos = 0, nnear = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int f0 = c0; f0 < cend; f0 += 32) {
+            const int f = f0 + lane;
+            const bool take = f < cend && ((sm.fi[f] >> 7) == (pass == 0 ? 1 : 0));
+            const unsigned bal = __ballot_sync(0xffffffffu, take);
+            if (take) perm[pos + __popc(bal & lt)] = (unsigned short)f;
+            pos += __popc(bal);
+        }
+        if (pass == 0) nnear = pos;
+    }
+    __syncwarp();
     auto store = [&](int f, double sc, const double* r) {
 #pragma unroll
-        for (int a = 0; a < D; ++a) sm.g[f][a] = sc * r[a];  // grad V(r_i - r_j)
+        for (int a = 0; a < D; ++a) g[f - c0][a] = sc * r[a];  // grad V(r_i - r_j)
     };
     if (kMixed) {
         // FP64 for the short-range Aziz entries, FP32 for the rest
@@ -420,8 +438,8 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         const float paramf = (float)s.int_a;
         const float Lf = (float)s.L, halfLf = 0.5f * (float)s.L;
         const int nfp64 = s.int_kind == POT_AZIZ ? nnear : 0;
-        for (int k = lane; k < total; k += 32) {
-            const int f = sm.perm[k];
+        for (int k = lane; k < cn; k += 32) {
+            const int f = perm[k];
             if (k < nfp64) {
                 double r[D];
                 const double r2 = separation(f, r);
@@ -441,15 +459,15 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                 }
                 const float sc = r2 < cut2f32 ? pair_scale<float>(s.int_kind, r2, paramf) : 0.0f;
 #pragma unroll
-                for (int a = 0; a < D; ++a) sm.g[f][a] = (double)(sc * r[a]);
+                for (int a = 0; a < D; ++a) g[f - c0][a] = (double)(sc * r[a]);
             }
         }
         __syncwarp();
     } else {
     // short-range entries (and every entry of the other potentials)
-    const int ngen = s.int_kind == POT_AZIZ ? nnear : total;
+    const int ngen = s.int_kind == POT_AZIZ ? nnear : cn;
     for (int k = lane; k < ngen; k += 32) {
-        const int f = sm.perm[k];
+        const int f = perm[k];
         double r[D];
         const double r2 = separation(f, r);
         store(f, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
@@ -457,34 +475,35 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
     // Aziz beyond the damping radius: two independent entries per lane and
     // iteration on the branch-free path; an entry the FP32 screen placed
     // here although it lies inside D r_m takes the general path
-    for (int k = ngen + lane; k < total; k += 64) {
-        const int f0 = sm.perm[k];
-        const bool two = k + 32 < total;
-        const int f1 = two ? sm.perm[k + 32] : f0;
+    for (int k = ngen + lane; k < cn; k += 64) {
+        const int f0 = perm[k];
+        const bool two = k + 32 < cn;
+        const int f1 = two ? perm[k + 32] : f0;
         double r0[D], r1[D];
         const double q0 = separation(f0, r0), q1 = separation(f1, r1);
         double sc0 = aziz_far_scale(q0, tbl), sc1 = aziz_far_scale(q1, tbl);
         if (!aziz_is_far(q0)) sc0 = pair_scale_d<true>(s.int_kind, q0, s.int_a, tbl);
         if (!aziz_is_far(q1)) sc1 = pair_scale_d<true>(s.int_kind, q1, s.int_a, tbl);
-        store(f0, q0 < cut2 ? sc0 : 0.0, r0);
-        if (two) store(f1, q1 < cut2 ? sc1 : 0.0, r1);
+        // r2 >= 0: the cutoff test compares bit patterns (integer unit)
+        store(f0, __double_as_longlong(q0) < cut2_bits ? sc0 : 0.0, r0);
+        if (two) store(f1, __double_as_longlong(q1) < cut2_bits ? sc1 : 0.0, r1);
     }
     __syncwarp();
     }
     // 3. deterministic sums: i side over its own (contiguous) entries, j side
-    //    over its list in recording order
-    double ai[D], aj[D];
+    //    over its list in recording order (chunk by chunk)
+    for (int k = max(off, c0); k < min(off + icnt, cend); ++k)
 #pragma unroll
-    for (int a = 0; a < D; ++a) ai[a] = aj[a] = 0.0;
-    for (int k = 0; k < icnt; ++k)
-#pragma unroll
-        for (int a = 0; a < D; ++a) ai[a] -= sm.g[off + k][a];
-    const int jc = sm.jcnt[lane];
+        for (int a = 0; a < D; ++a) ai[a] -= g[k - c0][a];
     for (int k = 0; k < jc; ++k) {
         const int e = sm.jlist[lane][k];
         const int f = sm.off[e >> 8] + (e & 255);
+        if (cn == total || (f >= c0 && f < cend)) {
 #pragma unroll
-        for (int a = 0; a < D; ++a) aj[a] += sm.g[f][a];
+            for (int a = 0; a < D; ++a) aj[a] += g[f - c0][a];
+        }
+    }
+    __syncwarp();  // the next chunk overwrites g and perm
     }
     const size_t base_b = (size_t)b * T;
     if (diag) {
@@ -509,12 +528,15 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
 // launch (no waiting).
 template <int D, bool kMixed>
 __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s, double* __restrict__ part, int T,
-                                                                          int npairs, int* ctr) {
+                                                                          int npairs, int* ctr, int cap) {
     extern __shared__ __align__(16) unsigned char csm_raw[];
-    __shared__ double tbl[32];
-    if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
+    __shared__ double tbl[256];
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) tbl[j] = kExp2Table256[j];
     __syncthreads();
-    CompactSmem<D>& sm = reinterpret_cast<CompactSmem<D>*>(csm_raw)[threadIdx.x >> 5];
+    unsigned char* wbase = csm_raw + (threadIdx.x >> 5) * compact_warp_bytes<D>(cap);
+    CompactSmem<D>& sm = *reinterpret_cast<CompactSmem<D>*>(wbase);
+    auto g = reinterpret_cast<double (*)[D]>(wbase + sizeof(CompactSmem<D>));
+    auto perm = reinterpret_cast<unsigned short*>(wbase + sizeof(CompactSmem<D>) + (size_t)cap * D * sizeof(double));
     const int lane = threadIdx.x & 31;
     const int ntask = s.P * npairs;
     for (;;) {
@@ -523,7 +545,7 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= ntask) break;
         const int b = task / npairs;
-        compact_tile<D, kMixed>(s, part, T, b, task - b * npairs, sm, tbl, lane);
+        compact_tile<D, kMixed>(s, part, T, b, task - b * npairs, sm, g, perm, cap, tbl, lane);
         __syncwarp();
     }
     if (lane == 0) {
@@ -691,9 +713,9 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
                                                              const double* __restrict__ xw,
                                                              const float* __restrict__ xh,
                                                              const float* __restrict__ xl, double* __restrict__ fpair) {
-    __shared__ double tbl[32];
+    __shared__ double tbl[256];
     extern __shared__ int lists[];  // kCellList x kCellThreads
-    if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) tbl[j] = kExp2Table256[j];
     __syncthreads();
     int ncell = 1;
     for (int a = 0; a < D; ++a) ncell *= nc;
@@ -881,21 +903,24 @@ static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, 
     if (pairs) {
         const int np = T * (T + 1) / 2;
         if (s.cutoff > 0.0) {
-            const size_t smem = sizeof(CompactSmem<D>) * kCompactWarps;
-            static int resident[2] = {0, 0}, sms = 0;
+            const int cap = s.pair_cap > 0 ? std::min(s.pair_cap, kCompactMaxCap) : kCompactDefaultCap;
+            const size_t smem = compact_warp_bytes<D>(cap) * kCompactWarps;
+            static int resident[2] = {0, 0}, rcap[2] = {0, 0}, sms = 0;
             auto kern = mixed ? k_pair_tiles_compact<D, true> : k_pair_tiles_compact<D, false>;
-            if (!resident[mixed]) {
-                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (rcap[mixed] != cap) {
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(compact_warp_bytes<D>(kCompactMaxCap) * kCompactWarps));
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[mixed], kern, 32 * kCompactWarps, smem);
                 int dev = 0;
                 cudaGetDevice(&dev);
                 cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
                 if (resident[mixed] < 1) resident[mixed] = 1;
+                rcap[mixed] = cap;
             }
             const int ntask = s.P * np;
             const int blocks = std::min((ntask + kCompactWarps - 1) / kCompactWarps, resident[mixed] * sms);
             int* ctr = reinterpret_cast<int*>(part + (pair_partial_doubles(s, D) - 1));
-            kern<<<blocks, 32 * kCompactWarps, smem, st>>>(s, part, T, np, ctr);
+            kern<<<blocks, 32 * kCompactWarps, smem, st>>>(s, part, T, np, ctr, cap);
         } else {
             dim3 grid((np + 3) / 4, s.P);
             if (mixed) k_pair_tiles<D, float><<<grid, 128, 0, st>>>(s, part, T, np);
