@@ -266,44 +266,51 @@ __global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ 
 // A warp-instruction on the FP64 pipe costs the same whether or not its lanes
 // are active, so evaluating the Aziz gradient only in the lanes whose pair is
 // inside the cutoff wastes the pipe on the others.  Each warp therefore
-//   1. screens its tile's pairs with FP32 distances (an FP32 copy of the j
-//      positions, converted once) and records, per i lane, the j's inside
-//      the cutoff plus a small margin, and per j lane the (i, position) of
-//      those entries; entries inside the Aziz damping radius D r_m are marked;
-//   2. lays the entries out i-major, orders them short-range first (so that
-//      the rarely taken damping branch stays within a few 32-entry chunks
-//      instead of splitting most of them) and evaluates them 32 at a time in
-//      FP64, every lane busy, storing each gradient in shared memory;
-//   3. sums the gradients per i and per j in list order (deterministic: the
+//   1. screens its tile's pairs with FP32 distances: lane i meets the j lanes
+//      one rotation step at a time (j positions by shuffle) and sets bit j
+//      of its mask for a pair inside the cutoff plus a small margin (and of
+//      a second mask inside the Aziz damping radius D r_m); the steps are
+//      independent, so they overlap;
+//   2. lays the entries out i-major (ascending j within a lane: entry f of
+//      lane i at off_i + its rank in the mask), evaluates all of them 32 (two
+//      per lane) at a time in FP64 on the branch-free path of the potential
+//      (the Aziz form beyond the damping radius), every lane busy, storing
+//      each gradient in shared memory, then evaluates the few entries inside
+//      the damping radius again on the general path (compacted by ballot so
+//      that the branch occupies a single 32-entry pass);
+//   3. sums the gradients per i over its contiguous entries and per j over
+//      the column of the masks in ascending i (deterministic: the
 //      evaluation order does not enter any sum).
 // Under PBC the tile's positions are wrapped into the box once, so a
 // separation lies in (-L, L) and its minimum image is one conditional shift
 // (a compare of the bit patterns and one FP64 add) instead of
-// dx - L floor(dx/L + 1/2).  The exponentials use exp_tang.  Same result as
-// k_pair_tiles up to rounding; the exact FP64 cutoff test is applied in step 2.
+// dx - L floor(dx/L + 1/2).  The exponentials use exp_tang256.  Same result
+// as k_pair_tiles up to rounding; the exact FP64 cutoff test is applied in
+// step 2.
 constexpr int kCompactWarps = 2;
 // gradient capacity per warp unless Sys::pair_cap says otherwise
-constexpr int kCompactDefaultCap = 704;
+constexpr int kCompactDefaultCap = 640;
+// entries of the damping-radius list evaluated per pass
+constexpr int kCompactNear = 256;
 
 // Per-warp shared memory: the fixed part below, then the gradients of up to
-// `cap` entries (double[cap][D]) and their evaluation order
-// (unsigned short[cap]).  A tile with more entries inside the cutoff than
-// `cap` is evaluated and summed in chunks of `cap` entries.
+// `cap` entries (double[cap][D]).  A tile with more entries inside the
+// cutoff than `cap` is evaluated and summed in chunks of `cap` entries.
 template <int D>
 struct CompactSmem {
-    double xi[kTile][D], xj[kTile][D];  // wrapped into the box under PBC
-    float xjf[kTile][D];                // FP32 copy of xj for the screen (hi part)
-    float xjl[kTile][D];                // lo part, xj - xjf (mixed far path)
-    unsigned char ilist[kTile][kTile];  // j's of lane i, bit 7 = short-range
-    unsigned short jlist[kTile][kTile]; // (i << 8 | k) entries of lane j
-    int icnt[kTile], jcnt[kTile], off[kTile];
-    unsigned char fi[kTile * kTile], fj[kTile * kTile];  // fi bit 7 = short-range
+    double xi[kTile][D], xj[kTile][D];   // wrapped into the box under PBC
+    float xif[kTile][D], xjf[kTile][D];  // FP32 hi parts
+    float xil[kTile][D], xjl[kTile][D];  // lo parts, x - hi (mixed far path)
+    unsigned mask[kTile];                // lane i: bit j for each entry (i, j)
+    int off[kTile];                      // lane i's first entry
+    unsigned short fe[kTile * kTile];    // entry f: near << 15 | i << 5 | j
+    unsigned short nl[kCompactNear];     // damping-radius entries of one pass
 };
 constexpr int kCompactMaxCap = kTile * kTile;
 // bytes of one warp's shared memory for a gradient capacity of `cap` entries
 template <int D>
 __host__ __device__ constexpr size_t compact_warp_bytes(int cap) {
-    return (sizeof(CompactSmem<D>) + (size_t)cap * (D * sizeof(double) + sizeof(unsigned short)) + 15) / 16 * 16;
+    return (sizeof(CompactSmem<D>) + (size_t)cap * D * sizeof(double) + 15) / 16 * 16;
 }
 
 // d in (-L, L) -> its minimum image; `half_bits` = bit pattern of L/2.
@@ -320,14 +327,17 @@ __device__ __forceinline__ double min_image_wrapped(double d, double L, long lon
 // cancel and FP32 would lose the difference.  Sums are FP64 either way.
 template <int D, bool kMixed>
 __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ part, int T, int b, int w,
-                                             CompactSmem<D>& sm, double (*g)[D], unsigned short* perm, int cap,
-                                             const double* tbl, int lane) {
-    int it = (int)((2.0 * T + 1.0 - sqrt((2.0 * T + 1.0) * (2.0 * T + 1.0) - 8.0 * w)) * 0.5);
-    while (it > 0 && it * T - it * (it - 1) / 2 > w) --it;
-    while ((it + 1) * T - (it + 1) * it / 2 <= w) ++it;
-    const int jt = it + (w - (it * T - it * (it - 1) / 2));
+                                             CompactSmem<D>& sm, double (*g)[D], int cap, const double* tbl,
+                                             int lane) {
+    int it = 0, rem = w;  // row it holds the T - it tile pairs (it, it..T-1)
+    while (rem >= T - it) {
+        rem -= T - it;
+        ++it;
+    }
+    const int jt = it + rem;
     const bool diag = it == jt;
     const int i = it * kTile + lane, j = jt * kTile + lane;
+    float xif[D], xjf[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
         double xv = i < s.N ? s.x[idx<D>(s, b, a, i)] : 0.0;
@@ -338,46 +348,41 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         }
         sm.xi[lane][a] = xv;
         sm.xj[lane][a] = yv;
-        const float yh = (float)yv;
-        sm.xjf[lane][a] = yh;
-        if (kMixed) sm.xjl[lane][a] = (float)(yv - (double)yh);
+        xif[a] = (float)xv;
+        xjf[a] = (float)yv;
+        if (kMixed) {
+            sm.xif[lane][a] = xif[a];
+            sm.xjf[lane][a] = xjf[a];
+            sm.xil[lane][a] = (float)(xv - (double)xif[a]);
+            sm.xjl[lane][a] = (float)(yv - (double)xjf[a]);
+        }
     }
-    sm.icnt[lane] = 0;
-    sm.jcnt[lane] = 0;
-    __syncwarp();
-    // 1. FP32 screen, one rotation step at a time (lane i meets j = i + st)
+    // 1. FP32 screen
     const double cut = s.cutoff;
     const float cut2f = (float)(cut * cut) * 1.0001f;
-    const float near2f = s.int_kind == POT_AZIZ ? (float)(Aziz::D * Aziz::rm * Aziz::D * Aziz::rm) * 1.0001f : -1.0f;
+    const bool aziz = s.int_kind == POT_AZIZ;
+    const float near2f = aziz ? (float)(Aziz::D * Aziz::rm * Aziz::D * Aziz::rm) * 1.0001f : -1.0f;
     const float Lf = (float)s.L, halfLf = 0.5f * (float)s.L;
-    float xif[D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) xif[a] = (float)sm.xi[lane][a];
-    int icnt = 0;
+    const int nj = min(kTile, s.N - jt * kTile);  // valid j lanes
+    const bool ivalid = i < s.N;
+    unsigned mask = 0u, nmask = 0u;
     const int first = diag ? 1 : 0, lastS = diag ? 16 : 31;
+#pragma unroll 4
     for (int st = first; st <= lastS; ++st) {
         const int jl = (lane + st) & 31;
-        bool in = i < s.N && jt * kTile + jl < s.N && (!diag || st < 16 || lane < 16);
         float r2 = 0.0f;
-        if (in) {
 #pragma unroll
-            for (int a = 0; a < D; ++a) {
-                float d = xif[a] - sm.xjf[jl][a];
-                if (s.pbc && fabsf(d) > halfLf) d -= copysignf(Lf, d);
-                r2 += d * d;
-            }
-            in = r2 <= cut2f;
+        for (int a = 0; a < D; ++a) {
+            float d = xif[a] - __shfl_sync(0xffffffffu, xjf[a], jl);
+            if (s.pbc && fabsf(d) > halfLf) d -= copysignf(Lf, d);
+            r2 = fmaf(d, d, r2);
         }
-        if (in) {
-            const int jc = sm.jcnt[jl];  // lanes of one step hit distinct j's
-            sm.jlist[jl][jc] = (unsigned short)((lane << 8) | icnt);
-            sm.jcnt[jl] = jc + 1;
-            sm.ilist[lane][icnt++] = (unsigned char)(jl | (r2 < near2f ? 0x80 : 0));
-        }
-        __syncwarp();
+        const bool in = ivalid && jl < nj && (!diag || st < 16 || lane < 16) && r2 <= cut2f;
+        mask |= (unsigned)in << jl;
+        nmask |= (unsigned)(in && r2 < near2f) << jl;
     }
-    sm.icnt[lane] = icnt;
     // 2. i-major layout: offsets by a warp scan of the counts
+    const int icnt = __popc(mask);
     int off = icnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -386,18 +391,29 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
     }
     const int total = __shfl_sync(0xffffffffu, off, 31);
     off -= icnt;
+    sm.mask[lane] = mask;
     sm.off[lane] = off;
-    for (int k = 0; k < icnt; ++k) {
-        const int e = sm.ilist[lane][k];
-        sm.fi[off + k] = (unsigned char)(lane | (e & 0x80));
-        sm.fj[off + k] = (unsigned char)(e & 31);
+    {
+        unsigned mm = mask;
+        for (int f = off; mm; ++f) {
+            const int jj = __ffs(mm) - 1;
+            mm &= mm - 1u;
+            sm.fe[f] = (unsigned short)((((nmask >> jj) & 1u) << 15) | (lane << 5) | jj);
+        }
+    }
+    // the column of lane j: the i's whose masks hold bit j
+    unsigned col = 0u;
+#pragma unroll
+    for (int t = 0; t < 32; ++t) {
+        const unsigned bt = __ballot_sync(0xffffffffu, (mask >> t) & 1u);
+        if (lane == t) col = bt;
     }
     __syncwarp();
     const long long half_bits = __double_as_longlong(0.5 * s.L);
     const double cut2 = cut * cut;
     const long long cut2_bits = __double_as_longlong(cut2);
     auto separation = [&](int f, double* r) {
-        const int il = sm.fi[f] & 31, jl = sm.fj[f];
+        const int e = sm.fe[f], il = (e >> 5) & 31, jl = e & 31;
         double r2 = 0.0;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
@@ -412,98 +428,89 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
 #pragma unroll
     for (int a = 0; a < D; ++a) ai[a] = aj[a] = 0.0;
     const unsigned lt = (1u << lane) - 1u;
-    const int jc = sm.jcnt[lane];
     for (int c0 = 0; c0 < total; c0 += cap) {
-    const int cend = min(total, c0 + cap), cn = cend - c0;
-    // evaluation order within the chunk: short-range entries, then the rest
-    int pos = 0, nnear = 0;
-    for (int pass = 0; pass < 2; ++pass) {
-        for (int f0 = c0; f0 < cend; f0 += 32) {
-            const int f = f0 + lane;
-            const bool take = f < cend && ((sm.fi[f] >> 7) == (pass == 0 ? 1 : 0));
-            const unsigned bal = __ballot_sync(0xffffffffu, take);
-            if (take) perm[pos + __popc(bal & lt)] = (unsigned short)f;
-            pos += __popc(bal);
-        }
-        if (pass == 0) nnear = pos;
-    }
-    __syncwarp();
-    auto store = [&](int f, double sc, const double* r) {
+        const int cend = min(total, c0 + cap), cn = cend - c0;
+        auto store = [&](int f, double sc, const double* r) {
 #pragma unroll
-        for (int a = 0; a < D; ++a) g[f - c0][a] = sc * r[a];  // grad V(r_i - r_j)
-    };
-    if (kMixed) {
-        // FP64 for the short-range Aziz entries, FP32 for the rest
-        const float cut2f32 = (float)cut2;
-        const float paramf = (float)s.int_a;
-        const float Lf = (float)s.L, halfLf = 0.5f * (float)s.L;
-        const int nfp64 = s.int_kind == POT_AZIZ ? nnear : 0;
-        for (int k = lane; k < cn; k += 32) {
-            const int f = perm[k];
-            if (k < nfp64) {
-                double r[D];
-                const double r2 = separation(f, r);
-                store(f, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
-            } else {
-                const int il = sm.fi[f] & 31, jl = sm.fj[f];
+            for (int a = 0; a < D; ++a) g[f - c0][a] = sc * r[a];  // grad V(r_i - r_j)
+        };
+        // every entry of the chunk on the branch-free path
+        if (kMixed) {
+            const float cut2f32 = (float)cut2;
+            const float paramf = (float)s.int_a;
+            for (int k = lane; k < cn; k += 32) {
+                const int e = sm.fe[c0 + k], il = (e >> 5) & 31, jl = e & 31;
                 float r[D];
                 float r2 = 0.0f;
 #pragma unroll
                 for (int a = 0; a < D; ++a) {
-                    const double xi = sm.xi[il][a];
-                    const float ih = (float)xi, il_ = (float)(xi - (double)ih);
-                    float d = (ih - sm.xjf[jl][a]) + (il_ - sm.xjl[jl][a]);
+                    float d = (sm.xif[il][a] - sm.xjf[jl][a]) + (sm.xil[il][a] - sm.xjl[jl][a]);
                     if (s.pbc && fabsf(d) > halfLf) d -= copysignf(Lf, d);
                     r[a] = d;
                     r2 += d * d;
                 }
                 const float sc = r2 < cut2f32 ? pair_scale<float>(s.int_kind, r2, paramf) : 0.0f;
 #pragma unroll
-                for (int a = 0; a < D; ++a) g[f - c0][a] = (double)(sc * r[a]);
+                for (int a = 0; a < D; ++a) g[k][a] = (double)(sc * r[a]);
+            }
+        } else if (aziz) {
+            // two independent entries per lane and iteration; entries inside
+            // the damping radius are redone below
+            for (int k = lane; k < cn; k += 64) {
+                const bool two = k + 32 < cn;
+                const int f0 = c0 + k, f1 = two ? f0 + 32 : f0;
+                double r0[D], r1[D];
+                const double q0 = separation(f0, r0), q1 = separation(f1, r1);
+                const double sc0 = aziz_far_scale(q0, tbl), sc1 = aziz_far_scale(q1, tbl);
+                // r2 >= 0: the cutoff test compares bit patterns (integer unit)
+                store(f0, __double_as_longlong(q0) < cut2_bits ? sc0 : 0.0, r0);
+                if (two) store(f1, __double_as_longlong(q1) < cut2_bits ? sc1 : 0.0, r1);
+            }
+        } else {
+            for (int k = lane; k < cn; k += 32) {
+                double r[D];
+                const double r2 = separation(c0 + k, r);
+                store(c0 + k, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
             }
         }
         __syncwarp();
-    } else {
-    // short-range entries (and every entry of the other potentials)
-    const int ngen = s.int_kind == POT_AZIZ ? nnear : cn;
-    for (int k = lane; k < ngen; k += 32) {
-        const int f = perm[k];
-        double r[D];
-        const double r2 = separation(f, r);
-        store(f, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
-    }
-    // Aziz beyond the damping radius: two independent entries per lane and
-    // iteration on the branch-free path; an entry the FP32 screen placed
-    // here although it lies inside D r_m takes the general path
-    for (int k = ngen + lane; k < cn; k += 64) {
-        const int f0 = perm[k];
-        const bool two = k + 32 < cn;
-        const int f1 = two ? perm[k + 32] : f0;
-        double r0[D], r1[D];
-        const double q0 = separation(f0, r0), q1 = separation(f1, r1);
-        double sc0 = aziz_far_scale(q0, tbl), sc1 = aziz_far_scale(q1, tbl);
-        if (!aziz_is_far(q0)) sc0 = pair_scale_d<true>(s.int_kind, q0, s.int_a, tbl);
-        if (!aziz_is_far(q1)) sc1 = pair_scale_d<true>(s.int_kind, q1, s.int_a, tbl);
-        // r2 >= 0: the cutoff test compares bit patterns (integer unit)
-        store(f0, __double_as_longlong(q0) < cut2_bits ? sc0 : 0.0, r0);
-        if (two) store(f1, __double_as_longlong(q1) < cut2_bits ? sc1 : 0.0, r1);
-    }
-    __syncwarp();
-    }
-    // 3. deterministic sums: i side over its own (contiguous) entries, j side
-    //    over its list in recording order (chunk by chunk)
-    for (int k = max(off, c0); k < min(off + icnt, cend); ++k)
-#pragma unroll
-        for (int a = 0; a < D; ++a) ai[a] -= g[k - c0][a];
-    for (int k = 0; k < jc; ++k) {
-        const int e = sm.jlist[lane][k];
-        const int f = sm.off[e >> 8] + (e & 255);
-        if (cn == total || (f >= c0 && f < cend)) {
-#pragma unroll
-            for (int a = 0; a < D; ++a) aj[a] += g[f - c0][a];
+        // Aziz entries inside the damping radius on the general FP64 path,
+        // gathered by ballot into passes of up to kCompactNear entries
+        if (aziz) {
+            int cnt = 0;
+            for (int f0 = c0; f0 < cend; f0 += 32) {
+                const int f = f0 + lane;
+                const bool take = f < cend && (sm.fe[f] >> 15);
+                const unsigned bal = __ballot_sync(0xffffffffu, take);
+                if (take) sm.nl[cnt + __popc(bal & lt)] = (unsigned short)f;
+                cnt += __popc(bal);
+                if (cnt > kCompactNear - 32 || (f0 + 32 >= cend && cnt > 0)) {
+                    __syncwarp();
+                    for (int k = lane; k < cnt; k += 32) {
+                        const int fn = sm.nl[k];
+                        double r[D];
+                        const double r2 = separation(fn, r);
+                        store(fn, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
+                    }
+                    __syncwarp();
+                    cnt = 0;
+                }
+            }
         }
-    }
-    __syncwarp();  // the next chunk overwrites g and perm
+        // 3. deterministic sums: i side over its own (contiguous) entries, j
+        //    side down its column in ascending i (chunk by chunk)
+        for (int k = max(off, c0); k < min(off + icnt, cend); ++k)
+#pragma unroll
+            for (int a = 0; a < D; ++a) ai[a] -= g[k - c0][a];
+        for (unsigned cm = col; cm; cm &= cm - 1u) {
+            const int ii = __ffs(cm) - 1;
+            const int f = sm.off[ii] + __popc(sm.mask[ii] & lt);
+            if (cn == total || (f >= c0 && f < cend)) {
+#pragma unroll
+                for (int a = 0; a < D; ++a) aj[a] += g[f - c0][a];
+            }
+        }
+        __syncwarp();  // the next chunk overwrites g
     }
     const size_t base_b = (size_t)b * T;
     if (diag) {
@@ -536,7 +543,6 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
     unsigned char* wbase = csm_raw + (threadIdx.x >> 5) * compact_warp_bytes<D>(cap);
     CompactSmem<D>& sm = *reinterpret_cast<CompactSmem<D>*>(wbase);
     auto g = reinterpret_cast<double (*)[D]>(wbase + sizeof(CompactSmem<D>));
-    auto perm = reinterpret_cast<unsigned short*>(wbase + sizeof(CompactSmem<D>) + (size_t)cap * D * sizeof(double));
     const int lane = threadIdx.x & 31;
     const int ntask = s.P * npairs;
     for (;;) {
@@ -545,7 +551,7 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= ntask) break;
         const int b = task / npairs;
-        compact_tile<D, kMixed>(s, part, T, b, task - b * npairs, sm, g, perm, cap, tbl, lane);
+        compact_tile<D, kMixed>(s, part, T, b, task - b * npairs, sm, g, cap, tbl, lane);
         __syncwarp();
     }
     if (lane == 0) {
