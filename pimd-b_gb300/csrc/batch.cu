@@ -230,8 +230,10 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
             estimate_direction(s, 1, reinterpret_cast<float*>(work));
             __syncthreads();
         }
-        for (int p = warp; p < N; p += nw)
-            for (int u = lane; u <= p; u += 32) exch_weight(s, p, u, tbl);
+        for (int p = warp; p < N; p += nw) {
+            const double inv = 1.0 / (p + 1);
+            for (int u = lane; u <= p; u += 32) exch_weight(s, p, u, inv, tbl);
+        }
         __syncthreads();
         // a reused estimate that fails is replaced by a fresh one (second
         // attempt) rather than by the exact recursion

@@ -183,23 +183,37 @@ __global__ void k_exch_weights(Sys s, int phase) {
     __shared__ double tbl[32];
     if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
     __syncthreads();
-    for (int p = blockIdx.y; p < s.N; p += gridDim.y)
+    for (int p = blockIdx.y; p < s.N; p += gridDim.y) {
+        const double inv = 1.0 / (p + 1);  // once per row and thread (FP64 division: ~8 operations)
         for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= p; u += gridDim.x * blockDim.x)
-            exch_weight(s, p, u, tbl);
+            exch_weight(s, p, u, inv, tbl);
+    }
 }
 
 // Pass 3: block 0 forward, block 1 backward.  Phase 0 may not fall back to
 // the exact recursion when it reused the previous potentials (xflags[7]); a
 // failed solve then leaves xflags[6] set and the phase-1 kernels redo the
-// evaluation from a fresh estimate.
+// evaluation from a fresh estimate.  With `inline_retry` (smaller systems,
+// where the retry's three launches would cost more than its work) the block
+// whose solve failed redoes its direction itself: FP32 estimate, weights,
+// solve; no phase 1 is launched.  No static shared memory beyond a flag:
+// the block has to fit beside the pair kernel's resident blocks.
 __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_exact, int phase,
-                                                             const double* __restrict__ pre) {
+                                                             const double* __restrict__ pre, int inline_retry) {
     extern __shared__ double ys[];  // y: N+1, acc: N+1, then 32 for reductions
     __shared__ int last_block;
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
     const int allow_exact = force_exact || phase == 1 || !((volatile int*)s.xflags)[7];
-    solve_direction(s, blockIdx.x, force_exact, ys, allow_exact,
-                    pre ? pre + (size_t)blockIdx.x * (s.N + 1) : nullptr);
+    const int dir = blockIdx.x;
+    const int gave_up = solve_direction(s, dir, force_exact, ys, allow_exact,
+                                        pre ? pre + (size_t)dir * (s.N + 1) : nullptr, !inline_retry);
+    if (gave_up && inline_retry) {
+        estimate_direction(s, dir, reinterpret_cast<float*>(ys));  // 3 (N+1) floats fit in ys
+        __syncthreads();
+        weights_direction(s, dir, nullptr);  // CUDA's exp (a rare path)
+        __syncthreads();
+        solve_direction(s, dir, 0, ys, 1);
+    }
     // The block that finishes second runs solve_finish (threadFenceReduction
     // pattern; no waiting).
     __threadfence();
@@ -412,24 +426,27 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
         cudaFuncSetAttribute(k_exch_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
     if (smem + 1024 > 48 * 1024) cudaFuncSetAttribute(k_exch_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (exact) {
-        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 1, 0, nullptr);
+        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 1, 0, nullptr, 0);
         return 1;
     }
     const dim3 wgrid((s.N + 255) / 256, s.N < 65535 ? s.N : 65535);
     const dim3 rgrid(1, s.N < 256 ? s.N : 256);  // the retry's weights: a small grid-stride launch
+    // below the multi-SM solve's size a failed solve is retried inside
+    // k_exch_solve (phase 0 only)
+    const int inline_retry = s.N < kGridSolveMinN;
     int n = 0;
-    for (int phase = 0; phase < 2; ++phase) {
+    for (int phase = 0; phase < (inline_retry ? 1 : 2); ++phase) {
         k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s, phase);
         k_exch_weights<<<phase ? rgrid : wgrid, 256, 0, st>>>(s, phase);
         const bool grid = ysol && gflags && grid_solve(s, phase, ysol, gflags, st);
-        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase, grid ? ysol : nullptr);
+        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase, grid ? ysol : nullptr, inline_retry);
         n += grid ? 4 : 3;
     }
     return n;
 }
 
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st) {
-    const int warps = 8;
+    const int warps = 2;  // small blocks: the 2N rows spread over every SM
     dim3 grid((2 * s.N + warps - 1) / warps);
     if (D == 1) k_exch_forces<1><<<grid, warps * 32, 0, st>>>(s, accumulate);
     else if (D == 2) k_exch_forces<2><<<grid, warps * 32, 0, st>>>(s, accumulate);

@@ -199,21 +199,32 @@ __device__ inline void estimate_direction(const Sys& s, int dir, float* fsm) {
         for (int l = threadIdx.x; l <= N; l += blockDim.x) s.Vbh[l] = (l >= 1) ? (double)val[N - l] : 0.0;
     }
 }
-// Pass 2: the FP64 weights of packed entry (row p, column u), both directions.
-// `tbl`: the exp_tang table in shared memory (null: CUDA's exp).  Arguments
-// of 709 and more give infinity either way (the solve then retries).
+// Pass 2: the FP64 weights of packed entry (row p, column u), both directions
+// (dir 0 forward only, 1 backward only, -1 both); `inv` = 1/(p+1), once per
+// row.  `tbl`: the exp_tang table (32 entries: a weights block then still
+// fits beside the pair kernel's resident blocks) in shared memory (null:
+// CUDA's exp).  Arguments of 709 and more give infinity either way (the
+// solve then retries).
 __device__ __forceinline__ double weight_exp(double x, const double* tbl) {
     if (!tbl) return exp(x);
     return x < 709.0 ? exp_tang(x, tbl) : (double)INFINITY;
 }
-__device__ __forceinline__ void exch_weight(const Sys& s, int p, int u, const double* tbl = nullptr) {
+__device__ __forceinline__ void exch_weight(const Sys& s, int p, int u, double inv, const double* tbl = nullptr,
+                                            int dir = -1) {
     const double beta = s.beta_ex;
     const size_t e = tri(p) + u;
     const double E = s.E[e];
-    const double inv = 1.0 / (p + 1);
-    s.Wf[e] = weight_exp(-beta * (E + s.Vh[u] - s.Vh[p + 1]), tbl) * inv;
+    if (dir <= 0) s.Wf[e] = weight_exp(-beta * (E + s.Vh[u] - s.Vh[p + 1]), tbl) * inv;
     // backward node r = N - u from node r' = N - 1 - p (u >= 1)
-    if (u >= 1) s.Wb[tri(s.N - u - 1) + (s.N - 1 - p)] = weight_exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u]), tbl) * inv;
+    if (dir != 0 && u >= 1)
+        s.Wb[tri(s.N - u - 1) + (s.N - 1 - p)] = weight_exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u]), tbl) * inv;
+}
+// One direction's weights by the whole block (the in-block retry).
+__device__ inline void weights_direction(const Sys& s, int dir, const double* tbl) {
+    for (int p = 0; p < s.N; ++p) {
+        const double inv = 1.0 / (p + 1);
+        for (int u = threadIdx.x; u <= p; u += blockDim.x) exch_weight(s, p, u, inv, tbl, dir);
+    }
 }
 // Exact level-by-level FP64 log-sum-exp in the reference's order (used only
 // when the estimate is unusable, or on request).  `vs` holds N+1 doubles,
@@ -267,8 +278,10 @@ constexpr double kExactLogY = 200.0;
 // recursion), no exact recursion is run: xflags[6] asks the caller to
 // retry with a fresh estimate instead.
 // `pre`: y of this direction already solved (k_exch_solve_grid), or null.
-__device__ inline void solve_direction(const Sys& s, int dir, int force_exact, double* ys, int allow_exact = 1,
-                                       const double* pre = nullptr) {
+// Returns 1 when it gave up that way (block-uniform); with `flag_retry` 0
+// xflags[6] is left alone (the caller retries in the same block).
+__device__ inline int solve_direction(const Sys& s, int dir, int force_exact, double* ys, int allow_exact = 1,
+                                      const double* pre = nullptr, int flag_retry = 1) {
     double* acc = ys + s.N + 1;
     double* red = ys + 2 * (s.N + 1);
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
@@ -293,8 +306,8 @@ __device__ inline void solve_direction(const Sys& s, int dir, int force_exact, d
         }
         bad = __syncthreads_or(bad);
         if (bad && !allow_exact) {
-            if (tid == 0) s.xflags[6] = 1;
-            return;
+            if (tid == 0 && flag_retry) s.xflags[6] = 1;
+            return 1;
         }
         if (bad) {
             exact_forward(s, ys, red);
@@ -335,8 +348,8 @@ __device__ inline void solve_direction(const Sys& s, int dir, int force_exact, d
         }
         bad = __syncthreads_or(bad);
         if (bad && !allow_exact) {
-            if (tid == 0) s.xflags[6] = 1;
-            return;
+            if (tid == 0 && flag_retry) s.xflags[6] = 1;
+            return 1;
         }
         if (bad) {
             exact_backward(s, ys, red);
@@ -354,6 +367,7 @@ __device__ inline void solve_direction(const Sys& s, int dir, int force_exact, d
             if (nonfinite) atomicOr(s.err, ERRB_NONFINITE_VB);
         }
     }
+    return 0;
 }
 // After both directions (one block): the per-row factors of the connection
 // probabilities, which need both V and V_backwards, and the estimates of the
