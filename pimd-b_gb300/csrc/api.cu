@@ -706,6 +706,10 @@ static void enqueue_forces(pimdb_handle* h) {
     // with the tile or cell paths the exchange forces go to fx on the side
     // stream and the finishing kernel adds them: off the critical path
     const bool fx_in_finish = s.bosonic && (cells || tiles);
+    // With the pair tiles and the exchange on two streams, the tiles leave
+    // SMs to the exchange's one-block passes (estimate, solve), whose
+    // sequential chains would otherwise share the FP64 pipes with them.
+    h->s.reserve_sms = fork && tiles ? exchange_reserved_sms(s) : 0;
     if (s.bosonic) {
         exchange_front(h, xs);
         if (fx_in_finish) exchange_forces(h, 0, xs);

@@ -48,6 +48,8 @@ struct Sys {
     int int_kind;
     double int_a;               // harmonic pair: k | dipole: strength
     int pair_cap;               // pair-tile gradient capacity per warp (0: the default)
+    int reserve_sms;            // SMs (the highest ids) the pair tiles leave to the exchange's
+                                // one-block passes running beside them (0: none)
     uint64_t seed;
     uint32_t replica;
     // device arrays

@@ -32,6 +32,8 @@
 // non-finite input), the solve kernel recomputes the level-by-level FP64
 // log-sum-exp in the reference's own order instead.  The backward recursion
 // is handled the same way by the second block of each kernel.
+#include <algorithm>
+
 #include "exchange_dev.cuh"
 #include "kernels.h"
 
@@ -364,11 +366,32 @@ __global__ void k_exch_estimators(Sys s, int nbeads) {
     estimators_block(s, nbeads, sh);
 }
 
+// Every exchange kernel takes the largest shared-memory carveout.  An SM runs
+// all its resident blocks under one carveout, so a kernel that prefers a
+// smaller one (more L1) could start only on SMs without pair-tile blocks,
+// and the pair tiles' blocks could not start beside it: launched first in a
+// step graph, the exchange would hold back part of the pair kernel.
+static void exchange_carveouts() {
+    static bool done = false;
+    if (done) return;
+    done = true;
+    const void* k[] = {(const void*)k_exch_energies<1>, (const void*)k_exch_energies<2>,
+                       (const void*)k_exch_energies<3>, (const void*)k_link_prefix<1>,
+                       (const void*)k_link_prefix<2>, (const void*)k_link_prefix<3>,
+                       (const void*)k_exch_energies_flat<1>, (const void*)k_exch_energies_flat<2>,
+                       (const void*)k_exch_energies_flat<3>, (const void*)k_exch_estimate,
+                       (const void*)k_exch_weights, (const void*)k_exch_solve, (const void*)k_exch_solve_grid,
+                       (const void*)k_exch_forces<1>, (const void*)k_exch_forces<2>, (const void*)k_exch_forces<3>};
+    for (const void* f : k)
+        cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+}
+
 size_t exchange_energy_doubles(const Sys& s, int D) {
     return s.N >= kFlatEnergiesMinN ? (size_t)(2 + 2 * D) * s.N : 0;
 }
 
 void launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work) {
+    exchange_carveouts();
     if (work && s.N >= kFlatEnergiesMinN) {
         double* Lh = work;
         double* Ll = work + s.N;
@@ -419,9 +442,18 @@ static bool grid_solve(const Sys& s, int phase, double* ysol, unsigned* gflags, 
                                       st) == cudaSuccess;
 }
 
+// SMs the pair tiles leave free while this exchange runs beside them: its
+// one-block passes (below the multi-SM solve's size) then run alone on an SM.
+int exchange_reserved_sms(const Sys& s) { return s.N < kGridSolveMinN ? 2 : 0; }
+
 int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double* ysol, unsigned* gflags) {
-    const size_t esmem = sizeof(float) * 3 * (size_t)(s.N + 1);
-    const size_t smem = sizeof(double) * (2 * (size_t)(s.N + 1) + 32);
+    exchange_carveouts();
+    // With reserved SMs the one-block passes ask for 116 KB of shared memory,
+    // whatever they use: more than an SM holding pair-tile blocks has left
+    // and more than half an SM, so each lands alone on a reserved SM.
+    const size_t least = s.reserve_sms ? 116 * 1024 : 0;
+    const size_t esmem = std::max(sizeof(float) * 3 * (size_t)(s.N + 1), least);
+    const size_t smem = std::max(sizeof(double) * (2 * (size_t)(s.N + 1) + 32), least);
     if (esmem + 1024 > 48 * 1024)
         cudaFuncSetAttribute(k_exch_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
     if (smem + 1024 > 48 * 1024) cudaFuncSetAttribute(k_exch_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -446,6 +478,7 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
 }
 
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st) {
+    exchange_carveouts();
     const int warps = 2;  // small blocks: the 2N rows spread over every SM
     dim3 grid((2 * s.N + warps - 1) / warps);
     if (D == 1) k_exch_forces<1><<<grid, warps * 32, 0, st>>>(s, accumulate);

@@ -532,10 +532,14 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
 
 // Persistent warps take tile tasks (bead-major) from ctr[0] until none are
 // left; the warp that finishes last resets both counters for the next
-// launch (no waiting).
+// launch (no waiting).  Blocks that land on one of the last s.reserve_sms of
+// the nsm SMs take no task: those SMs stay free for the exchange's one-block
+// passes (FP32 estimate, FP64 triangular solve) that run beside this kernel,
+// whose sequential chains would otherwise share the FP64 pipe with the
+// pair warps.
 template <int D, bool kMixed>
 __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s, double* __restrict__ part, int T,
-                                                                          int npairs, int* ctr, int cap) {
+                                                                          int npairs, int* ctr, int cap, int nsm) {
     extern __shared__ __align__(16) unsigned char csm_raw[];
     __shared__ double tbl[256];
     for (int j = threadIdx.x; j < 256; j += blockDim.x) tbl[j] = kExp2Table256[j];
@@ -544,8 +548,11 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
     CompactSmem<D>& sm = *reinterpret_cast<CompactSmem<D>*>(wbase);
     auto g = reinterpret_cast<double (*)[D]>(wbase + sizeof(CompactSmem<D>));
     const int lane = threadIdx.x & 31;
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    const bool reserved = (int)smid >= nsm - s.reserve_sms;  // never touches ctr[0]
     const int ntask = s.P * npairs;
-    for (;;) {
+    while (!reserved) {
         int task = 0;
         if (lane == 0) task = atomicAdd(&ctr[0], 1);
         task = __shfl_sync(0xffffffffu, task, 0);
@@ -926,7 +933,9 @@ static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, 
             const int ntask = s.P * np;
             const int blocks = std::min((ntask + kCompactWarps - 1) / kCompactWarps, resident[mixed] * sms);
             int* ctr = reinterpret_cast<int*>(part + (pair_partial_doubles(s, D) - 1));
-            kern<<<blocks, 32 * kCompactWarps, smem, st>>>(s, part, T, np, ctr, cap);
+            Sys sr = s;
+            if (sms <= 16) sr.reserve_sms = 0;
+            kern<<<blocks, 32 * kCompactWarps, smem, st>>>(sr, part, T, np, ctr, cap, sms);
         } else {
             dim3 grid((np + 3) / 4, s.P);
             if (mixed) k_pair_tiles<D, float><<<grid, 128, 0, st>>>(s, part, T, np);

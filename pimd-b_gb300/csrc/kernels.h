@@ -60,6 +60,9 @@ size_t exchange_energy_doubles(const Sys& s, int D);
 int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double* ysol = nullptr,
                                unsigned* gflags = nullptr);
 size_t exchange_grid_doubles(const Sys& s);
+// SMs the pair tiles should leave free (Sys::reserve_sms) while the exchange
+// runs beside them on another stream.
+int exchange_reserved_sms(const Sys& s);
 size_t exchange_grid_flags(const Sys& s);
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st);
 void launch_exchange_estimators(const Sys& s, cudaStream_t st);
