@@ -31,7 +31,7 @@ EXPORTS = [
     "pimdb_step_io",
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
     "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
-    "pimdb_measure_fp64_peak", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
+    "pimdb_measure_fp64_peak", "pimdb_math_check", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
     "pimdb_propagate", "pimdb_compute_observables", "pimdb_potential_energy", "pimdb_local_energy", "pimdb_batch_create", "pimdb_batch_destroy", "pimdb_batch_size", "pimdb_batch_set_states",
     "pimdb_batch_get_states", "pimdb_batch_set_step", "pimdb_batch_get_step", "pimdb_batch_compute_forces",
     "pimdb_batch_step", "pimdb_batch_step_async", "pimdb_batch_synchronize", "pimdb_batch_exchange",
@@ -102,6 +102,7 @@ def lib():
             "pimdb_status_string": ([C.c_int], C.c_char_p),
             "pimdb_profile": ([vp, C.c_int, vp, vp, vp], C.c_int),
             "pimdb_measure_fp64_peak": ([vp], C.c_int),
+            "pimdb_math_check": ([vp, C.c_int, vp], C.c_int),
             "pimdb_set_option": ([vp, C.c_char_p, C.c_int], C.c_int),
             "pimdb_thermostat_step": ([vp, C.c_int], C.c_int),
             "pimdb_zero_momentum": ([vp], C.c_int),
@@ -167,6 +168,16 @@ def measure_fp64_peak() -> float:
     v = C.c_double()
     _check(lib().pimdb_measure_fp64_peak(C.byref(v)))
     return v.value
+
+
+def math_check(x):
+    """CUDA's exp and rsqrt beside the library's exp_tang, exp_tang256 and
+    rsqrt_newton: array (n, 5) of exp(x), exp_tang(x), exp_tang256(x),
+    rsqrt(r), rsqrt_newton(r) with r = |x| + 1e-3."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros((x.size, 5))
+    _check(lib().pimdb_math_check(_ptr(x), x.size, _ptr(out)))
+    return out
 
 
 def default_config() -> Config:

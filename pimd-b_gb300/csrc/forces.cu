@@ -947,6 +947,26 @@ static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, 
     k_bead_finish<D><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, part, T, write_phys, add_fx);
 }
 
+// pimdb_math_check: CUDA's exp and rsqrt beside exp_tang, exp_tang256 and
+// rsqrt_newton on the same inputs.
+__global__ void k_math_check(const double* __restrict__ x, int n, double* __restrict__ out) {
+    __shared__ double t32[32], t256[256];
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) t256[j] = kExp2Table256[j];
+    if (threadIdx.x < 32) t32[threadIdx.x] = kExp2Table[threadIdx.x];
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double v = x[i], r = fabs(v) + 1e-3;
+        out[5 * (size_t)i + 0] = exp(v);
+        out[5 * (size_t)i + 1] = exp_tang(v, t32);
+        out[5 * (size_t)i + 2] = exp_tang256(v, t256);
+        out[5 * (size_t)i + 3] = rsqrt(r);
+        out[5 * (size_t)i + 4] = rsqrt_newton(r);
+    }
+}
+void launch_math_check(const double* x, int n, double* out, cudaStream_t st) {
+    k_math_check<<<(n + 255) / 256, 256, 0, st>>>(x, n, out);
+}
+
 void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part,
                                   cudaEvent_t before_finish, int add_fx, cudaStream_t st) {
     if (D == 1) tiles_launch<1>(s, mixed, write_phys, part, before_finish, add_fx, st);
