@@ -219,7 +219,12 @@ template <int D>
 __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* tbl) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int N = s.N;
-    for (int v = warp; v < N; v += nw) energy_row<D>(s, v, lane);
+    // the interior links |x1_{u+1} - xP_u|^2 once per u (shared memory),
+    // instead of once per cycle-energy entry
+    double* link = reinterpret_cast<double*>(work);
+    for (int u = threadIdx.x; u < N - 1; u += blockDim.x) link[u] = sepsq<D>(s, s.P - 1, u, 0, u + 1);
+    __syncthreads();
+    for (int v = warp; v < N; v += nw) energy_row<D>(s, v, lane, link);
     __syncthreads();
     int fresh = ((volatile int*)s.xflags)[3];
     __syncthreads();

@@ -28,9 +28,10 @@ __device__ __forceinline__ double sepsq(const Sys& s, int ba, int ia, int bb, in
 // E[v][u] = E[v][u+1] + k/2 (|x1_{u+1} - xP_u|^2 - |xP_v - x1_{u+1}|^2 + |xP_v - x1_u|^2)
 // for u = v-1 .. 0, evaluated as a warp-wide suffix scan over u.  The middle
 // distance of entry u is the last distance of entry u+1, so each entry costs
-// two distance evaluations (passed between lanes by a shuffle).
+// two distance evaluations (passed between lanes by a shuffle), or one with
+// `link` (link[u] = |x1_{u+1} - xP_u|^2, computed once per u by the caller).
 template <int D>
-__device__ inline void energy_row(const Sys& s, int v, int lane) {
+__device__ inline void energy_row(const Sys& s, int v, int lane, const double* link = nullptr) {
     const int first = 0, last = s.P - 1;
     const double hk = 0.5 * s.kappa;
     double* row = s.E + tri(v);
@@ -56,7 +57,7 @@ __device__ inline void energy_row(const Sys& s, int v, int lane) {
         double cu1 = __shfl_up_sync(0xffffffffu, c, 1);
         if (lane == 0) cu1 = cnext;
         double term = 0.0;
-        if (u >= 0) term = hk * (sepsq<D>(s, last, u, first, u + 1) - cu1 + c);
+        if (u >= 0) term = hk * ((link ? link[u] : sepsq<D>(s, last, u, first, u + 1)) - cu1 + c);
         cnext = __shfl_sync(0xffffffffu, c, 31);
         // inclusive scan over lanes (lane 0 holds the largest u)
 #pragma unroll
