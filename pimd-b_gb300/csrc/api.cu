@@ -96,6 +96,18 @@ struct pimdb_handle {
         long long kernels = 0;
     };
     std::map<std::pair<int, StepState>, StepGraph> graphs;
+    // whole pimdb_step_io calls on page-locked buffers: (steps, state before,
+    // device views of x_in, p_in, x_out, p_out, f_out)
+    struct IoKey {
+        int nsteps;
+        StepState before;
+        const void* v[5];
+        bool operator<(const IoKey& o) const {
+            return std::tie(nsteps, before, v[0], v[1], v[2], v[3], v[4]) <
+                   std::tie(o.nsteps, o.before, o.v[0], o.v[1], o.v[2], o.v[3], o.v[4]);
+        }
+    };
+    std::map<IoKey, StepGraph> io_graphs;
     long long* d_step = nullptr;
     bool dstep_valid = false;
     bool capturing = false;
@@ -142,6 +154,9 @@ static void drop_graphs(pimdb_handle* h) {
     for (auto& kv : h->graphs)
         if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     h->graphs.clear();
+    for (auto& kv : h->io_graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    h->io_graphs.clear();
 }
 
 static void complete_pending(pimdb_handle* h);
@@ -564,6 +579,16 @@ static void* pinned_view(const void* host) {
     return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
+// The state kernels on device-accessible arrays (device memory, or the
+// device views of page-locked host arrays).
+static void state_in_launch(pimdb_handle* h, const double* sx, const double* sp) {
+    launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_in(h->s, h->D, sx, sp, h->stream); });
+    h->com_pending = false;
+}
+static void state_out_launch(pimdb_handle* h, double* ox, double* op, double* of) {
+    if (ox || op || of) launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_out(h->s, h->D, ox, op, of, h->stream); });
+}
+
 // The state in, enqueued: one kernel (pack, zero the forces), reading
 // page-locked host arrays directly or the staging buffer after a copy.
 static int enqueue_state_in(pimdb_handle* h, const double* x, const double* p, cudaMemcpyKind kind) {
@@ -580,8 +605,7 @@ static int enqueue_state_in(pimdb_handle* h, const double* x, const double* p, c
         if (x && !vx) CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, x, n * sizeof(double), kind, h->stream));
         if (p && !vp) CUDA_TRY(h, cudaMemcpyAsync(h->d_stage + n, p, n * sizeof(double), kind, h->stream));
     }
-    launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_in(s, h->D, sx, sp, h->stream); });
-    h->com_pending = false;
+    state_in_launch(h, sx, sp);
     CUDA_TRY(h, cudaGetLastError());
     return PIMDB_OK;
 }
@@ -602,8 +626,7 @@ static int enqueue_state_out(pimdb_handle* h, double* x, double* p, double* f, c
         copy[k] = v == nullptr;
         out[k] = v ? v : h->d_stage + k * n;
     }
-    if (x || p || f)
-        launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_out(s, h->D, out[0], out[1], out[2], h->stream); });
+    state_out_launch(h, out[0], out[1], out[2]);
     for (int k = 0; k < 3; ++k)
         if (copy[k]) CUDA_TRY(h, cudaMemcpyAsync(dst[k], out[k], n * sizeof(double), kind, h->stream));
     CUDA_TRY(h, cudaGetLastError());
@@ -972,9 +995,99 @@ extern "C" int pimdb_step(pimdb_handle* h, int nsteps) {
     return check_err_word(h);
 }
 
+// A whole pimdb_step_io call as one CUDA graph when every host array given
+// is page-locked (the state kernels then read and write them directly):
+// state in, the steps, the deferred tail, state out and the error word, with
+// no host work between them.  Returns -1 when it does not apply (the caller
+// enqueues the call), else the status of the launch.
+static int graph_io(pimdb_handle* h, const double* xi, const double* pi, int nsteps, double* xo, double* po,
+                    double* fo) {
+    if (!h->opt_graph || h->graph_broken || h->profile || !h->warm || nsteps < 1) return -1;
+    const void* host[5] = {xi, pi, xo, po, fo};
+    pimdb_handle::IoKey key{};
+    key.nsteps = nsteps;
+    key.before = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
+    for (int k = 0; k < 5; ++k) {
+        key.v[k] = host[k] ? pinned_view(host[k]) : nullptr;
+        if (host[k] && !key.v[k]) return -1;
+    }
+    auto it = h->io_graphs.find(key);
+    if (it == h->io_graphs.end()) {
+        if (h->io_graphs.size() >= 8) {  // callers passing new arrays every time
+            for (auto& kv : h->io_graphs)
+                if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+            h->io_graphs.clear();
+        }
+        pimdb_handle::StepGraph g;
+        const pimdb_handle::StepState before = key.before;
+        const long long step0 = h->step, launches0 = h->launches;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            h->graph_broken = true;
+            return -1;
+        }
+        h->capturing = true;
+        h->graph_base = step0;
+        if (xi || pi) {
+            complete_pending(h);
+            state_in_launch(h, static_cast<const double*>(key.v[0]), static_cast<const double*>(key.v[1]));
+        }
+        enqueue_steps(h, nsteps);
+        complete_pending(h);
+        state_out_launch(h, (double*)key.v[2], (double*)key.v[3], (double*)key.v[4]);
+        // last: every captured kernel reads the step index relative to the
+        // device counter as it was when the graph started
+        launch_step_advance(h->d_step, nsteps, h->stream);
+        cudaMemcpyAsync(h->h_err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+        h->capturing = false;
+        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        if (e == cudaSuccess && h->async_err == cudaSuccess)
+            e = cudaGraphInstantiateWithFlags(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+        if (graph) cudaGraphDestroy(graph);
+        g.after = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
+        g.kernels = h->launches - launches0 + 1;
+        // the capture only recorded the work: restore the host state
+        h->step = step0;
+        h->launches = launches0;
+        h->red_last = before.red_last;
+        h->nred_last = before.nred_last;
+        h->com_pending = before.com_pending;
+        h->nm_tail_pending = before.nm_tail_pending;
+        if (e != cudaSuccess || h->async_err != cudaSuccess) {
+            cudaGetLastError();
+            h->async_err = cudaSuccess;
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            h->graph_broken = true;
+            return -1;
+        }
+        it = h->io_graphs.emplace(key, g).first;
+    }
+    if (!h->dstep_valid) {
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        CUDA_TRY(h, cudaMemcpy(h->d_step, &h->step, sizeof(long long), cudaMemcpyHostToDevice));
+        h->dstep_valid = true;
+    }
+    CUDA_TRY(h, cudaGraphLaunch(it->second.exec, h->stream));
+    h->step += nsteps;
+    h->launches += it->second.kernels;
+    const pimdb_handle::StepState& a = it->second.after;
+    h->red_last = a.red_last;
+    h->nred_last = a.nred_last;
+    h->com_pending = a.com_pending;
+    h->nm_tail_pending = a.nm_tail_pending;
+    return PIMDB_OK;
+}
+
 extern "C" int pimdb_step_io(pimdb_handle* h, const double* x_in, const double* p_in, int nsteps, double* x_out,
                              double* p_out, double* f_out) {
     if (!h || nsteps < 0) return PIMDB_ERR_ARG;
+    const int gio = graph_io(h, x_in, p_in, nsteps, x_out, p_out, f_out);
+    if (gio > 0) return gio;
+    if (gio == 0) {
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        return *h->h_err ? check_err_word(h) : PIMDB_OK;
+    }
     int st = PIMDB_OK;
     if (x_in || p_in) st = enqueue_state_in(h, x_in, p_in, cudaMemcpyHostToDevice);
     if (st == PIMDB_OK && nsteps > 0) st = pimdb_step_async(h, nsteps);

@@ -452,6 +452,40 @@ def test_step_io_reports_a_nonfinite_exchange():
             g.step_io(x, np.zeros_like(x), 1)
 
 
+def test_step_io_graph_replay_equals_plain_launches():
+    """On page-locked arrays a whole step_io call (state in, steps, deferred
+    tail, state out, error word) is replayed as one CUDA graph, cached by
+    step count, step state and arrays: bitwise the state of plain launches,
+    with step counts and array sets changing between calls and ordinary
+    calls in between."""
+    torch = pytest.importorskip("torch")
+    s, cfg = case(**TRAJ_CASES["nm_nmthermo_bosons_P64_aziz"])
+    x = ring(s, seed=9, spread_ang=0.2)
+    p = momenta(s, 9)
+    bufs = [[torch.empty(x.shape, dtype=torch.float64, pin_memory=True) for _ in range(3)] for _ in range(2)]
+    with pk.System(cfg) as a, pk.System(cfg) as b:
+        a.set_option("cuda_graphs", 0)
+        for g in (a, b):
+            g.set_step(0)
+            g.set_state(x, p)
+            g.step(1)
+        xa, pa, _ = a.get_state()
+        for k, n in enumerate((1, 2, 1, 3, 1, 1)):
+            hx, hp, hf = bufs[k % 2]
+            hx.copy_(torch.from_numpy(xa))
+            hp.copy_(torch.from_numpy(pa))
+            xa, pa, fa = a.step_io(xa, pa, n)
+            b.step_io_ptr(hx.data_ptr(), hp.data_ptr(), n, hx.data_ptr(), hp.data_ptr(), hf.data_ptr())
+            for u, v in ((xa, hx), (pa, hp), (fa, hf)):
+                assert np.array_equal(u, v.numpy()), (k, n)
+            if k == 2:  # an ordinary call between graph replays
+                a.step(1)
+                b.step(1)
+                xa, pa, _ = a.get_state()
+                xb, pb, _ = b.get_state()
+                assert np.array_equal(xa, xb) and np.array_equal(pa, pb)
+
+
 def test_step_io_with_page_locked_buffers():
     """Page-locked host arrays are read and written by the state kernels
     directly: the same state, bitwise, as through copies of pageable arrays."""
