@@ -485,9 +485,16 @@ def main():
         fl, inside = pair_flops(w, x0)
         ach = fl / (dom_ms * 1e-3) / 1e12
         peak = fp64_peak if args.precision == "fp64" else None
+        # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one
+        # k_pair_tiles_compact launch on this workload, from an ncu capture
+        # (ncu --set full -k regex:k_pair_tiles_compact -s 2 -c 1 of
+        # --profile-only --steps 3 --warmup 3); the per-step state (2.4 MB)
+        # stays in L2 between launches
+        traffic = 459008 if (args.workload == "cfg2" and args.precision == "fp64") else None
         roof.update({"bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": ach,
                      "peak": peak, "unit": "TFLOP/s", "frac": (ach / peak) if peak else None,
-                     "traffic": None, "peak_source": "measured in-run (FP64 FMA probe)",
+                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu capture)" if traffic else None,
+                     "peak_source": "measured in-run (FP64 FMA probe)",
                      "algorithmic": f"{fl:.4g} FLOP per launch ({inside} unique pairs inside the cutoff)"})
     else:
         bytes_per = 6 * 8 * units * D
