@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ 
 // step 2.
 constexpr int kCompactWarps = 2;
 // gradient capacity per warp unless Sys::pair_cap says otherwise
-constexpr int kCompactDefaultCap = 640;
+constexpr int kCompactDefaultCap = 608;
 // entries of the damping-radius list evaluated per pass
 constexpr int kCompactNear = 256;
 
@@ -300,7 +300,10 @@ template <int D>
 struct CompactSmem {
     double xi[kTile][D], xj[kTile][D];   // wrapped into the box under PBC
     float xif[kTile][D], xjf[kTile][D];  // FP32 hi parts
-    float xil[kTile][D], xjl[kTile][D];  // lo parts, x - hi (mixed far path)
+    union {
+        double xjs[2][kTile][D];         // FP64 path under PBC: xj - L, xj + L
+        float lo[2][kTile][D];           // mixed path: x - hi of i, of j
+    } u;
     unsigned mask[kTile];                // lane i: bit j for each entry (i, j)
     int off[kTile];                      // lane i's first entry
     unsigned short fe[kTile * kTile];    // entry f: near << 15 | i << 5 | j
@@ -350,11 +353,14 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         sm.xj[lane][a] = yv;
         xif[a] = (float)xv;
         xjf[a] = (float)yv;
+        sm.xif[lane][a] = xif[a];
+        sm.xjf[lane][a] = xjf[a];
         if (kMixed) {
-            sm.xif[lane][a] = xif[a];
-            sm.xjf[lane][a] = xjf[a];
-            sm.xil[lane][a] = (float)(xv - (double)xif[a]);
-            sm.xjl[lane][a] = (float)(yv - (double)xjf[a]);
+            sm.u.lo[0][lane][a] = (float)(xv - (double)xif[a]);
+            sm.u.lo[1][lane][a] = (float)(yv - (double)xjf[a]);
+        } else if (s.pbc) {
+            sm.u.xjs[0][lane][a] = yv - s.L;
+            sm.u.xjs[1][lane][a] = yv + s.L;
         }
     }
     // 1. FP32 screen
@@ -367,19 +373,27 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
     const bool ivalid = i < s.N;
     unsigned mask = 0u, nmask = 0u;
     const int first = diag ? 1 : 0, lastS = diag ? 16 : 31;
+    // |dx| within this of L/2 in FP32: the FP32 image choice might differ
+    // from the FP64 one, so the entry takes the exact path (with the
+    // damping-radius entries).  Bound on the FP32 error: 2.5 2^-24 L.
+    const float amb = 1e-6f * Lf;
 #pragma unroll 4
     for (int st = first; st <= lastS; ++st) {
         const int jl = (lane + st) & 31;
         float r2 = 0.0f;
+        bool edge = false;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
             float d = xif[a] - __shfl_sync(0xffffffffu, xjf[a], jl);
-            if (s.pbc && fabsf(d) > halfLf) d -= copysignf(Lf, d);
+            if (s.pbc) {
+                edge |= fabsf(fabsf(d) - halfLf) <= amb;
+                if (fabsf(d) > halfLf) d -= copysignf(Lf, d);
+            }
             r2 = fmaf(d, d, r2);
         }
         const bool in = ivalid && jl < nj && (!diag || st < 16 || lane < 16) && r2 <= cut2f;
         mask |= (unsigned)in << jl;
-        nmask |= (unsigned)(in && r2 < near2f) << jl;
+        nmask |= (unsigned)(in && (r2 < near2f || (aziz && edge))) << jl;
     }
     // 2. i-major layout: offsets by a warp scan of the counts
     const int icnt = __popc(mask);
@@ -424,6 +438,25 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         }
         return r2;
     };
+    // The far path's separation: the image is the one the FP32 screen chose
+    // (xj - L, xj or xj + L, each rounded once), so one FP64 subtraction per
+    // axis; entries where that choice is not certain were marked above.
+    auto separation_far = [&](int f, double* r) {
+        const int e = sm.fe[f], il = (e >> 5) & 31, jl = e & 31;
+        double r2 = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double xjv = sm.xj[jl][a];
+            if (s.pbc) {
+                const float df = sm.xif[il][a] - sm.xjf[jl][a];
+                if (fabsf(df) > halfLf) xjv = sm.u.xjs[df > 0.0f ? 1 : 0][jl][a];
+            }
+            const double d = sm.xi[il][a] - xjv;
+            r[a] = d;
+            r2 += d * d;
+        }
+        return r2;
+    };
     double ai[D], aj[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) ai[a] = aj[a] = 0.0;
@@ -444,7 +477,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                 float r2 = 0.0f;
 #pragma unroll
                 for (int a = 0; a < D; ++a) {
-                    float d = (sm.xif[il][a] - sm.xjf[jl][a]) + (sm.xil[il][a] - sm.xjl[jl][a]);
+                    float d = (sm.xif[il][a] - sm.xjf[jl][a]) + (sm.u.lo[0][il][a] - sm.u.lo[1][jl][a]);
                     if (s.pbc && fabsf(d) > halfLf) d -= copysignf(Lf, d);
                     r[a] = d;
                     r2 += d * d;
@@ -460,7 +493,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                 const bool two = k + 32 < cn;
                 const int f0 = c0 + k, f1 = two ? f0 + 32 : f0;
                 double r0[D], r1[D];
-                const double q0 = separation(f0, r0), q1 = separation(f1, r1);
+                const double q0 = separation_far(f0, r0), q1 = separation_far(f1, r1);
                 const double sc0 = aziz_far_scale(q0, tbl), sc1 = aziz_far_scale(q1, tbl);
                 // r2 >= 0: the cutoff test compares bit patterns (integer unit)
                 store(f0, __double_as_longlong(q0) < cut2_bits ? sc0 : 0.0, r0);
