@@ -146,6 +146,7 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
     const double cut = s.cutoff;
     const R cut2 = (R)(cut * cut);
     const R param = (R)s.int_a;
+    const bool all_pairs = cut < 0.0;  // hoisted: a double compare is an FP64-pipe instruction
     const bool bosonic_bead = s.bosonic && (b == 0 || b == s.P - 1);
     const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
     for (int i = lane; i < N; i += 32) {
@@ -161,14 +162,20 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
                 hi[a] = sh[a * N + i];
                 lo[a] = (sizeof(R) == 8) ? (R)0 : sl[a * N + i];
             }
+            // FP32: the 32-pair partial sums are added up error-free in two
+            // floats (Knuth's two-sum), so the FP64 pipe is not touched
+            // until the particle's total
+            R ch[D], cl[D];
+#pragma unroll
+            for (int a = 0; a < D; ++a) ch[a] = cl[a] = (R)0;
             for (int j0 = 0; j0 < N; j0 += 32) {
                 const int jn = min(32, N - j0);
                 R t[D];
 #pragma unroll
                 for (int a = 0; a < D; ++a) t[a] = (R)0;
+#pragma unroll 4
                 for (int jj = 0; jj < jn; ++jj) {
                     const int j = j0 + jj;
-                    if (j == i) continue;
                     R r[D];
                     R r2 = (R)0;
 #pragma unroll
@@ -184,14 +191,28 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
                         r[a] = d;
                         r2 += d * d;
                     }
-                    if (cut < 0.0 || r2 < cut2) {
-                        const R sc = pair_scale<R>(s.int_kind, r2, param);
+                    // a select, not a branch: the self term (r = 0) may be
+                    // infinite for the dipole and must not enter
+                    const bool use = j != i && (all_pairs || r2 < cut2);
+                    const R sc = pair_scale<R>(s.int_kind, r2, param);
 #pragma unroll
-                        for (int a = 0; a < D; ++a) t[a] -= sc * r[a];
-                    }
+                    for (int a = 0; a < D; ++a) t[a] -= use ? sc * r[a] : (R)0;
                 }
 #pragma unroll
-                for (int a = 0; a < D; ++a) acc[a] += (double)t[a];
+                for (int a = 0; a < D; ++a) {
+                    if constexpr (sizeof(R) == 8) {
+                        acc[a] += t[a];
+                    } else {
+                        const R sum = ch[a] + t[a];
+                        const R bb = sum - ch[a];
+                        cl[a] += (ch[a] - (sum - bb)) + (t[a] - bb);
+                        ch[a] = sum;
+                    }
+                }
+            }
+            if constexpr (sizeof(R) == 4) {
+#pragma unroll
+                for (int a = 0; a < D; ++a) acc[a] += (double)ch[a] + (double)cl[a];
             }
         }
 #pragma unroll
@@ -254,8 +275,14 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
         __syncthreads();
     }
     solve_finish(s);
+    // beads 1 and P staged in the (now free) shared scratch for the forces
+    double* xs = reinterpret_cast<double*>(work);
+    for (int e = threadIdx.x; e < 2 * D * N; e += blockDim.x) {
+        const int side = e / (D * N), a = (e / N) % D, i = e % N;
+        xs[e] = s.x[idx<D>(s, side ? s.P - 1 : 0, a, i)];
+    }
     __syncthreads();
-    for (int w = warp; w < 2 * N; w += nw) exch_force_row<D>(s, w, lane, 1);
+    for (int w = warp; w < 2 * N; w += nw) exch_force_row<D>(s, w, lane, 1, xs);
 }
 
 template <int D, typename R>
@@ -442,8 +469,9 @@ static size_t batch_smem(int D, int maxN, int threads) {
     const size_t stage = nw * (size_t)D * maxN * sizeof(double);
     const size_t est = sizeof(float) * 3 * (size_t)(maxN + 1);
     const size_t solve = sizeof(double) * (2 * (size_t)(maxN + 1) + 32);
+    const size_t xforces = sizeof(double) * 2 * (size_t)D * maxN;  // beads 1 and P for the exchange forces
     const size_t estim = sizeof(double) * ((size_t)maxN + 1 + 32);
-    return 3 * 32 * sizeof(double) + std::max(std::max(stage, est), std::max(solve, estim));
+    return 3 * 32 * sizeof(double) + std::max(std::max(std::max(stage, est), std::max(solve, estim)), xforces);
 }
 
 template <typename F>

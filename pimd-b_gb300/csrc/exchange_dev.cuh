@@ -415,8 +415,10 @@ __device__ inline void solve_finish(const Sys& s, int extrapolate = 0) {
 // link P[l][l+1] = 1 - C_l; with the exact fallback they are evaluated
 // from their defining exponentials.  When `accumulate`, the spring force is
 // added to f (which holds the physical forces; simulation.cpp:363-373).
+// `xs` (optional): the positions of beads 1 and P staged in shared memory,
+// xs[(side * D + a) * N + i] with side 0 = bead 1, 1 = bead P.
 template <int D>
-__device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumulate) {
+__device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumulate, const double* xs = nullptr) {
     const int N = s.N;
     const double beta = s.beta_ex;
     const double VN = s.V[N];
@@ -446,7 +448,7 @@ __device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumul
             }
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                double d = s.x[idx<D>(s, first, a, n)] - xl[a];
+                double d = (xs ? xs[(size_t)a * N + n] : s.x[idx<D>(s, first, a, n)]) - xl[a];
                 if (s.pbc) d = min_image(d, s.L, s.invL);
                 sum[a] += pr * d;
             }
@@ -470,7 +472,7 @@ __device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumul
             }
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                double d = s.x[idx<D>(s, last, a, q)] - xl[a];
+                double d = (xs ? xs[((size_t)D + a) * N + q] : s.x[idx<D>(s, last, a, q)]) - xl[a];
                 if (s.pbc) d = min_image(d, s.L, s.invL);
                 sum[a] += pr * d;
             }
