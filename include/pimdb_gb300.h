@@ -170,7 +170,9 @@ int pimdb_synchronize(pimdb_handle* h);
  * both NULL keeps the device state), pimdb_step(nsteps) and pimdb_get_state
  * (x_out, p_out, f_out; any may be NULL) in one call with one
  * synchronisation.  The host arrays may be pinned or pageable and may
- * alias (x_in == x_out). */
+ * alias (x_in == x_out).  Page-locked arrays are read and written by the
+ * state kernels directly, and then the whole call (state in, steps, state
+ * out) is captured once per (nsteps, arrays) and replayed as one CUDA graph. */
 int pimdb_step_io(pimdb_handle* h, const double* x_in, const double* p_in, int nsteps, double* x_out, double* p_out,
                   double* f_out);
 
