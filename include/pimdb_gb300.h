@@ -373,9 +373,11 @@ int pimdb_batch_last_error(const pimdb_batch* b, char* buf, int len);
 int pimdb_measure_fp64_peak(double* tflops);
 
 /* Diagnostics of the hand-written FP64 functions against CUDA's own, on n
- * host values x (no counterpart in the reference).  out (5 n doubles, host):
+ * host values x (no counterpart in the reference).  out (8 n doubles, host):
  * per value, exp(x), exp_tang(x) (32-entry table) and exp_tang256(x)
- * (256-entry table), then rsqrt(r) and rsqrt_newton(r) for r = |x| + 1e-3. */
+ * (256-entry table), then rsqrt(r) and rsqrt_newton(r) for r = |x| + 1e-3,
+ * then the bit-pattern conversions: hi and lo of split_f32(x) and
+ * f32_to_f64((float)x). */
 int pimdb_math_check(const double* x, int n, double* out);
 
 /* Human-readable text of the last error on this handle (or a global one if

@@ -172,10 +172,11 @@ def measure_fp64_peak() -> float:
 
 def math_check(x):
     """CUDA's exp and rsqrt beside the library's exp_tang, exp_tang256 and
-    rsqrt_newton: array (n, 5) of exp(x), exp_tang(x), exp_tang256(x),
-    rsqrt(r), rsqrt_newton(r) with r = |x| + 1e-3."""
+    rsqrt_newton, and the bit-pattern conversions: array (n, 8) of exp(x),
+    exp_tang(x), exp_tang256(x), rsqrt(r), rsqrt_newton(r) with
+    r = |x| + 1e-3, hi and lo of split_f32(x), f32_to_f64(float(x))."""
     x = np.ascontiguousarray(x, dtype=np.float64)
-    out = np.zeros((x.size, 5))
+    out = np.zeros((x.size, 8))
     _check(lib().pimdb_math_check(_ptr(x), x.size, _ptr(out)))
     return out
 

@@ -1314,13 +1314,13 @@ extern "C" int pimdb_math_check(const double* x, int n, double* out) {
     if (!x || !out || n < 0) return PIMDB_ERR_ARG;
     if (n == 0) return PIMDB_OK;
     double* d = nullptr;
-    CUDA_TRY(nullptr, cudaMalloc(&d, sizeof(double) * 6 * (size_t)n));
+    CUDA_TRY(nullptr, cudaMalloc(&d, sizeof(double) * 9 * (size_t)n));
     cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         launch_math_check(d, n, d + n, nullptr);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpy(out, d + n, sizeof(double) * 5 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + n, sizeof(double) * 8 * (size_t)n, cudaMemcpyDeviceToHost);
     cudaFree(d);
     CUDA_TRY(nullptr, e);
     return PIMDB_OK;

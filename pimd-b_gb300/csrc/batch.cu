@@ -58,8 +58,8 @@ __device__ __forceinline__ void normal_pair(const Sys& s, long long step, int su
     const uint64_t t = 2ull * (unsigned long long)step + substep;
     // the one-system path's normals (drawn on the FP32 pipe in either precision)
     const float2 z = philox_normal_pair_f32(s.seed, s.replica, t, pair);
-    z0 = (double)z.x;
-    z1 = (double)z.y;
+    z0 = f32_to_f64(z.x);
+    z1 = f32_to_f64(z.y);
 }
 
 // Sums v[0..D) over the block; every thread receives the totals.  `sh`
@@ -136,17 +136,23 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
                 if constexpr (sizeof(R) == 8) {
                     sh[a * N + j] = x;
                 } else {
-                    const float h = (float)x;
+                    float h, l;
+                    split_f32(x, h, l);  // no FP64-pipe instruction
                     sh[a * N + j] = h;
-                    sl[a * N + j] = (float)(x - (double)h);
+                    sl[a * N + j] = l;
                 }
             }
         __syncwarp();
     }
     const double cut = s.cutoff;
-    const R cut2 = (R)(cut * cut);
-    const R param = (R)s.int_a;
-    const bool all_pairs = cut < 0.0;  // hoisted: a double compare is an FP64-pipe instruction
+    // The loop constants are made opaque (an empty asm that takes them as
+    // in/out operands): under register pressure the compiler otherwise
+    // recomputes them from the shared Sys inside the pair loop, a DMUL and a
+    // conversion per pair on the FP64 pipe.  All pairs: an infinite cutoff.
+    R cut2 = cut < 0.0 ? (R)INFINITY : (R)(cut * cut);
+    R param = (R)s.int_a;
+    if constexpr (sizeof(R) == 4) asm volatile("" : "+f"(cut2), "+f"(param));
+    else asm volatile("" : "+d"(cut2), "+d"(param));
     const bool bosonic_bead = s.bosonic && (b == 0 || b == s.P - 1);
     const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
     for (int i = lane; i < N; i += 32) {
@@ -193,7 +199,7 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
                     }
                     // a select, not a branch: the self term (r = 0) may be
                     // infinite for the dipole and must not enter
-                    const bool use = j != i && (all_pairs || r2 < cut2);
+                    const bool use = j != i && !(r2 >= cut2);  // a NaN separation still enters
                     const R sc = pair_scale<R>(s.int_kind, r2, param);
 #pragma unroll
                     for (int a = 0; a < D; ++a) t[a] -= use ? sc * r[a] : (R)0;
@@ -212,7 +218,7 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
             }
             if constexpr (sizeof(R) == 4) {
 #pragma unroll
-                for (int a = 0; a < D; ++a) acc[a] += (double)ch[a] + (double)cl[a];
+                for (int a = 0; a < D; ++a) acc[a] += f32_to_f64(ch[a]) + f32_to_f64(cl[a]);
             }
         }
 #pragma unroll

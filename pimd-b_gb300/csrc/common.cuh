@@ -227,9 +227,43 @@ __device__ __forceinline__ float2 philox_normal_pair_f32(uint64_t seed, uint32_t
     return make_float2(__fmul_rn(r, cs), __fmul_rn(r, sn));
 }
 
+// float -> double by bit patterns (exact), so that no FP64-pipe conversion
+// is issued (on GB300 a conversion takes the FP64 pipe at half its add
+// rate); zero, subnormal, infinite and NaN values take the conversion.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ef = (u >> 23) & 0xffu;
+    if (ef == 0u || ef == 0xffu) return (double)f;
+    return __hiloint2double((int)((u & 0x80000000u) | ((ef + 896u) << 20) | ((u & 0x7fffffu) >> 3)), (int)(u << 29));
+}
+// x = hi + lo by bit patterns: hi holds the sign, exponent and leading 24
+// significand bits of x (truncated), lo the remaining 29 bits, truncated to
+// a float's 24 (|lo| < 2^-23 |x|; hi + lo carries 47 or more bits of x).
+// Outside 2^-60 <= |x| < 2^100 (and for zero) the conversions are used.
+__device__ __forceinline__ void split_f32(double x, float& hi, float& lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ffu);
+    if (e < 1023 - 60 || e >= 1023 + 100) {
+        hi = (float)x;
+        lo = (float)(x - (double)hi);
+        return;
+    }
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const unsigned long long m = b & 0xfffffffffffffULL;  // 52 fraction bits
+    hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(m >> 29));
+    const unsigned m29 = (unsigned)(m & 0x1fffffffu);  // value m29 2^(e - 1075)
+    if (m29 == 0u) {
+        lo = 0.0f;
+        return;
+    }
+    const int top = 31 - __clz((int)m29);  // leading bit of m29, 0..28
+    const unsigned frac = top >= 23 ? (m29 >> (top - 23)) & 0x7fffffu : (m29 << (23 - top)) & 0x7fffffu;
+    lo = __uint_as_float(sign | ((unsigned)(e - 1075 + top + 127) << 23) | frac);
+}
+
 __device__ __forceinline__ double2 philox_normal_pair(uint64_t seed, uint32_t replica, uint64_t t, uint32_t pair) {
     const float2 z = philox_normal_pair_f32(seed, replica, t, pair);
-    return make_double2((double)z.x, (double)z.y);
+    return make_double2(f32_to_f64(z.x), f32_to_f64(z.y));
 }
 
 // The two Langevin normals of (bead-or-mode k, axis a, particles 2 i2 and

@@ -484,7 +484,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                 }
                 const float sc = r2 < cut2f32 ? pair_scale<float>(s.int_kind, r2, paramf) : 0.0f;
 #pragma unroll
-                for (int a = 0; a < D; ++a) g[k][a] = (double)(sc * r[a]);
+                for (int a = 0; a < D; ++a) g[k][a] = f32_to_f64(sc * r[a]);
             }
         } else if (aziz) {
             // two independent entries per lane and iteration; entries inside
@@ -989,11 +989,17 @@ __global__ void k_math_check(const double* __restrict__ x, int n, double* __rest
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double v = x[i], r = fabs(v) + 1e-3;
-        out[5 * (size_t)i + 0] = exp(v);
-        out[5 * (size_t)i + 1] = exp_tang(v, t32);
-        out[5 * (size_t)i + 2] = exp_tang256(v, t256);
-        out[5 * (size_t)i + 3] = rsqrt(r);
-        out[5 * (size_t)i + 4] = rsqrt_newton(r);
+        double* o = out + 8 * (size_t)i;
+        o[0] = exp(v);
+        o[1] = exp_tang(v, t32);
+        o[2] = exp_tang256(v, t256);
+        o[3] = rsqrt(r);
+        o[4] = rsqrt_newton(r);
+        float hi, lo;
+        split_f32(v, hi, lo);
+        o[5] = (double)hi;
+        o[6] = (double)lo;
+        o[7] = f32_to_f64((float)v);
     }
 }
 void launch_math_check(const double* x, int n, double* out, cudaStream_t st) {

@@ -27,7 +27,7 @@ void launch_bead_forces(const Sys& s, int D, int mixed, int write_phys, cudaStre
 // forces (fx) on beads 1 and P, after waiting for `before_finish` (may be
 // null) that marks them done.
 size_t pair_partial_doubles(const Sys& s, int D);
-// pimdb_math_check's kernel (device arrays; out holds 5 n doubles).
+// pimdb_math_check's kernel (device arrays; out holds 8 n doubles).
 void launch_math_check(const double* x, int n, double* out, cudaStream_t st);
 void launch_pair_tiles_and_finish(const Sys& s, int D, int mixed, int write_phys, double* part,
                                   cudaEvent_t before_finish, int add_fx, cudaStream_t st);
