@@ -95,6 +95,9 @@ __device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int s
                                              bool kick, bool o, bool drift, double* sum) {
     const int H = (s.N + 1) / 2;
     const int total = s.P * H;
+    // loop constants kept in registers (opaque: not recomputed per element)
+    double hdt = 0.5 * s.dt, c1 = s.c1, c2 = s.c2, dt_m = s.dt_m;
+    asm volatile("" : "+d"(hdt), "+d"(c1), "+d"(c2), "+d"(dt_m));
 #pragma unroll
     for (int a = 0; a < D; ++a) {
         sum[a] = 0.0;
@@ -109,9 +112,9 @@ __device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int s
                 const size_t e = idx<D>(s, b, a, i);
                 double p = s.p[e];
                 if (com_in) p -= cm[a];
-                if (kick) p += 0.5 * s.dt * s.f[e];
-                if (o) p = s.c1 * p + s.c2 * (h == 0 ? z0 : z1);
-                if (drift) s.x[e] = fma(p, s.dt_m, s.x[e]);
+                if (kick) p += hdt * s.f[e];
+                if (o) p = c1 * p + c2 * (h == 0 ? z0 : z1);
+                if (drift) s.x[e] = fma(p, dt_m, s.x[e]);
                 s.p[e] = p;
                 sum[a] += p;
             }
