@@ -490,7 +490,7 @@ def main():
         # (ncu --set full -k regex:k_pair_tiles_compact -s 2 -c 1 of
         # --profile-only --steps 3 --warmup 3); the per-step state (2.4 MB)
         # stays in L2 between launches
-        traffic = 459008 if (args.workload == "cfg2" and args.precision == "fp64") else None
+        traffic = 458496 if (args.workload == "cfg2" and args.precision == "fp64") else None
         roof.update({"bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": ach,
                      "peak": peak, "unit": "TFLOP/s", "frac": (ach / peak) if peak else None,
                      "traffic": traffic, "traffic_unit": "bytes per launch (ncu capture)" if traffic else None,
