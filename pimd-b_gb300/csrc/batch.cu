@@ -266,7 +266,7 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
             __syncthreads();
         }
         for (int p = warp; p < N; p += nw) {
-            const double inv = 1.0 / (p + 1);
+            const double inv = recip_row(p);
             for (int u = lane; u <= p; u += 32) exch_weight(s, p, u, inv, tbl);
         }
         __syncthreads();

@@ -186,7 +186,7 @@ __global__ void k_exch_weights(Sys s, int phase) {
     if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
     __syncthreads();
     for (int p = blockIdx.y; p < s.N; p += gridDim.y) {
-        const double inv = 1.0 / (p + 1);  // once per row and thread (FP64 division: ~8 operations)
+        const double inv = recip_row(p);
         for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= p; u += gridDim.x * blockDim.x)
             exch_weight(s, p, u, inv, tbl);
     }

@@ -206,6 +206,18 @@ __device__ inline void estimate_direction(const Sys& s, int dir, float* fsm) {
 // fits beside the pair kernel's resident blocks) in shared memory (null:
 // CUDA's exp).  Arguments of 709 and more give infinity either way (the
 // solve then retries).
+// 1/(p+1) for p < 4096, evaluated by the compiler (IEEE division, the
+// device's own result) into constant memory: the weights read it once per row
+// (a uniform index, one broadcast) instead of dividing.
+struct RecipTable {
+    double v[4096];
+    constexpr RecipTable() : v() {
+        for (int i = 0; i < 4096; ++i) v[i] = 1.0 / (i + 1);
+    }
+};
+static __constant__ RecipTable kRecip = RecipTable();
+__device__ __forceinline__ double recip_row(int p) { return p < 4096 ? kRecip.v[p] : 1.0 / (p + 1); }
+
 __device__ __forceinline__ double weight_exp(double x, const double* tbl) {
     if (!tbl) return exp(x);
     return x < 709.0 ? exp_tang(x, tbl) : (double)INFINITY;
@@ -223,7 +235,7 @@ __device__ __forceinline__ void exch_weight(const Sys& s, int p, int u, double i
 // One direction's weights by the whole block (the in-block retry).
 __device__ inline void weights_direction(const Sys& s, int dir, const double* tbl) {
     for (int p = 0; p < s.N; ++p) {
-        const double inv = 1.0 / (p + 1);
+        const double inv = recip_row(p);
         for (int u = threadIdx.x; u <= p; u += blockDim.x) exch_weight(s, p, u, inv, tbl, dir);
     }
 }
