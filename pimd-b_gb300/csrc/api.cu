@@ -31,7 +31,7 @@ struct pimdb_handle {
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     double* d_C = nullptr;    // cart -> NM rows [P][P]
     double* d_T = nullptr;    // NM -> cart rows [P][P]
-    double* d_rot = nullptr;  // [P][3]
+    double* d_rot = nullptr;  // [P][4]: cos, sin, m omega_k, sin / (m omega_k)
     double* d_red[2] = {nullptr, nullptr};
     double* d_stage = nullptr;
     double* d_part = nullptr;  // pair-tile partial sums (Newton's third law path)
@@ -303,7 +303,7 @@ static void nm_tables(int P, double omega_p, double mass, double dt, std::vector
     const double pi = 3.14159265358979323846;
     C.assign((size_t)P * P, 0.0);
     T.assign((size_t)P * P, 0.0);
-    rot.assign((size_t)P * 3, 0.0);
+    rot.assign((size_t)P * 4, 0.0);
     for (int k = 0; k < P; ++k) {
         double* row = &C[(size_t)k * P];
         const double fund = 2 * pi / P * k;
@@ -322,9 +322,13 @@ static void nm_tables(int P, double omega_p, double mass, double dt, std::vector
         }
         // normal_modes_propagator.cpp:13-16
         const double freq = 2 * omega_p * std::sin(k * pi / P);
-        rot[3 * k] = std::cos(freq * dt);
-        rot[3 * k + 1] = std::sin(freq * dt);
-        rot[3 * k + 2] = mass * freq;
+        rot[4 * k] = std::cos(freq * dt);
+        rot[4 * k + 1] = std::sin(freq * dt);
+        rot[4 * k + 2] = mass * freq;
+        // sin / (m omega_k) once here (IEEE division, as on the device)
+        // instead of an FP64 division per mode and step (0 for the centroid,
+        // which takes the free-particle branch)
+        rot[4 * k + 3] = freq != 0.0 ? rot[4 * k + 1] / rot[4 * k + 2] : 0.0;
     }
     for (int j = 0; j < P; ++j) {
         double* row = &T[(size_t)j * P];

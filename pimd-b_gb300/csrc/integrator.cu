@@ -240,8 +240,8 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_thermo(Sys s, const double* _
 // Normal-mode propagator step up to the force evaluation
 // (normal_modes_propagator.cpp:19-63): half-kick with the stored physical
 // forces, Cartesian -> normal modes, exact free ring-polymer rotation, back
-// to Cartesian.  rot[k] = {cos(w_k dt), sin(w_k dt), m w_k} (w_0 = 0 is the
-// free-particle drift).
+// to Cartesian.  rot[4 k ..] = {cos(w_k dt), sin(w_k dt), m w_k,
+// sin(w_k dt) / (m w_k)} (w_0 = 0 is the free-particle drift).
 template <int D>
 __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double* __restrict__ C,
                                                              const double* __restrict__ T,
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
             p0 += c * sp[b * kNmTile + 2 * pp];
             p1 += c * sp[b * kNmTile + 2 * pp + 1];
         }
-        const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+        const double cs = rot[4 * k], sn = rot[4 * k + 1], mw = rot[4 * k + 2], snw = rot[4 * k + 3];
         double qa, qb, pa, pb;
         if (mw == 0.0) {
             qa = q0 + s.dt_m * p0;
@@ -290,8 +290,8 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_propagate(Sys s, const double
             pa = p0;
             pb = p1;
         } else {
-            qa = cs * q0 + sn / mw * p0;
-            qb = cs * q1 + sn / mw * p1;
+            qa = cs * q0 + snw * p0;
+            qb = cs * q1 + snw * p1;
             pa = -mw * sn * q0 + cs * p0;
             pb = -mw * sn * q1 + cs * p1;
         }
@@ -595,7 +595,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
         thermostat(2ull * (unsigned long long)step);
         if (fixcom && !remove_com(1)) return;
         for (int k = g; k < P; k += kNmGroups) {
-            const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+            const double cs = rot[4 * k], sn = rot[4 * k + 1], mw = rot[4 * k + 2], snw = rot[4 * k + 3];
             for (int h2 = 0; h2 < 2; ++h2) {
                 const int o = k * kNmTile + 2 * pp + h2;
                 const double q = sy[o];
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(kNmThreads) k_nm_fused(Sys s, const double* __
                     sy[o] = q + s.dt_m * pk;
                     sq[o] = pk;
                 } else {
-                    sy[o] = cs * q + sn / mw * pk;
+                    sy[o] = cs * q + snw * pk;
                     sq[o] = -mw * sn * q + cs * pk;
                 }
             }
@@ -898,7 +898,7 @@ __global__ void __launch_bounds__(256) k_nm_warp(Sys s, const double* __restrict
 #pragma unroll
         for (int k1 = 0; k1 < E; ++k1) {
             const int k = k1 + E * k2;
-            const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+            const double cs = rot[4 * k], sn = rot[4 * k + 1], mw = rot[4 * k + 2], snw = rot[4 * k + 3];
             // kick, then the free ring rotation of (q, p) in mode k
             auto turn = [&](double& q, double& pm, double g) {
                 const double q0 = q, pk = pm + hdt * g;
@@ -906,7 +906,7 @@ __global__ void __launch_bounds__(256) k_nm_warp(Sys s, const double* __restrict
                     q = q0 + s.dt_m * pk;
                     pm = pk;
                 } else {
-                    q = cs * q0 + sn / mw * pk;
+                    q = cs * q0 + snw * pk;
                     pm = -mw * sn * q0 + cs * pk;
                 }
             };
@@ -1031,7 +1031,7 @@ __global__ void __launch_bounds__(96) k_nm_warp3(Sys s, const double* __restrict
 #pragma unroll
             for (int k1 = 0; k1 < E; ++k1) {
                 const int k = k1 + E * k2;
-                const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+                const double cs = rot[4 * k], sn = rot[4 * k + 1], mw = rot[4 * k + 2], snw = rot[4 * k + 3];
                 const double2 g = sF[k1][lane];
                 double2 q = sX[k1][lane];
                 auto turn = [&](double& qv, double& pm, double gv) {
@@ -1040,7 +1040,7 @@ __global__ void __launch_bounds__(96) k_nm_warp3(Sys s, const double* __restrict
                         qv = q0 + s.dt_m * pk;
                         pm = pk;
                     } else {
-                        qv = cs * q0 + sn / mw * pk;
+                        qv = cs * q0 + snw * pk;
                         pm = -mw * sn * q0 + cs * pk;
                     }
                 };
@@ -1121,11 +1121,11 @@ __global__ void __launch_bounds__(64) k_nm_prop_warp(Sys s, const double* __rest
 #pragma unroll
     for (int k1 = 0; k1 < E; ++k1) {
         const int k = k1 + E * k2;
-        const double cs = rot[3 * k], sn = rot[3 * k + 1], mw = rot[3 * k + 2];
+        const double cs = rot[4 * k], sn = rot[4 * k + 1], mw = rot[4 * k + 2], snw = rot[4 * k + 3];
         const double2 pm = sm2[0][k1][lane], q = sm2[1][k1][lane];
         auto turn = [&](double q0, double p0) -> double {
             if (mw == 0.0) return role == 0 ? p0 : q0 + s.dt_m * p0;
-            return role == 0 ? -mw * sn * q0 + cs * p0 : cs * q0 + sn / mw * p0;
+            return role == 0 ? -mw * sn * q0 + cs * p0 : cs * q0 + snw * p0;
         };
         z[k1] = make_double2(turn(q.x, pm.x), turn(q.y, pm.y));
     }
