@@ -452,6 +452,46 @@ def test_step_io_reports_a_nonfinite_exchange():
             g.step_io(x, np.zeros_like(x), 1)
 
 
+def test_pair_tiles_half_box_edge_images():
+    """Far-field pair separations take the image the FP32 screen chose; pairs
+    whose FP32 test lies within 1e-6 L of the half-box edge take the exact
+    FP64 minimum image.  Six pairs with the cutoff at L/2, each just inside
+    it and with its separation along one axis 1e-9 .. 1e-5 L short of L/2
+    (or past it, the other image), match the oracle (FP64 tolerance).  No
+    two particles are closer than 2.8 A, so every pair's force counts."""
+    L_ang = 22.7297
+    eps_list = [1e-9, 1e-7, 5e-7, 2e-6, 1e-5, 3e-6]
+    s, cfg = case(natoms=2 * len(eps_list), nbeads=2, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=L_ang,
+                  inter="aziz", cutoff_ang=0.5 * L_ang)
+    L = s.size
+    pts = []
+    for k, eps in enumerate(eps_list):
+        axis = k % 3
+        sign = 1.0 if (k // 3) % 2 == 0 else -1.0
+        o1, o2 = (axis + 1) % 3, (axis + 2) % 3
+        base = np.zeros(3)
+        base[o1] = (k % 3 - 1) * 0.18 * L
+        base[o2] = (k // 3 - 0.5) * 0.3 * L
+        a, b = base.copy(), base.copy()
+        a[axis] = -0.25 * L
+        b[axis] = 0.25 * L - sign * eps * L
+        b[o1] += 0.3 * np.sqrt(eps) * L  # r just inside L/2
+        pts += [a, b]
+    x = np.repeat(np.array(pts)[None], s.nbeads, axis=0)
+    x[1] += np.random.default_rng(17).normal(0.0, 1e-4, x[1].shape)
+    d = x[0][:, None] - x[0][None]
+    d -= L * np.round(d / L)
+    r = np.sqrt((d ** 2).sum(-1)) + 1e9 * np.eye(s.natoms)
+    assert r.min() > 2.8 * 1.8897261
+    want = O.update_forces(s, x)["f"]
+    with pk.System(cfg) as g:
+        g.set_option("cell_lists", 0)
+        g.set_state(x, np.zeros_like(x))
+        g.compute_forces()
+        got = g.get_state()[2]
+    assert rel_per_bead(got, want) < FP64_TOL
+
+
 def test_step_io_graph_replay_equals_plain_launches():
     """On page-locked arrays a whole step_io call (state in, steps, deferred
     tail, state out, error word) is replayed as one CUDA graph, cached by
