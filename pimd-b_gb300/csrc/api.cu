@@ -51,6 +51,10 @@ struct pimdb_handle {
     double* d_cmpart = nullptr;
     unsigned* d_bar = nullptr;
     double* d_tw = nullptr;   // FFT twiddles (P/2 complex) when P is a power of two
+    // the normal modes of p and x the last fused head left (three-warp
+    // kernel), valid while nothing else has changed x or p
+    double* d_modes = nullptr;
+    bool modes_valid = false;
     int logP = 0;
     int opt_fft = 1;
     cudaError_t async_err = cudaSuccess;
@@ -84,10 +88,10 @@ struct pimdb_handle {
     // every graph advances by its step count
     struct StepState {
         int red_last, nred_last;
-        bool com_pending, nm_tail_pending;
+        bool com_pending, nm_tail_pending, modes_valid;
         bool operator<(const StepState& o) const {
-            return std::tie(red_last, nred_last, com_pending, nm_tail_pending) <
-                   std::tie(o.red_last, o.nred_last, o.com_pending, o.nm_tail_pending);
+            return std::tie(red_last, nred_last, com_pending, nm_tail_pending, modes_valid) <
+                   std::tie(o.red_last, o.nred_last, o.com_pending, o.nm_tail_pending, o.modes_valid);
         }
     };
     struct StepGraph {
@@ -353,6 +357,7 @@ static void free_handle(pimdb_handle* h) {
     if (h->d_cmpart) cudaFree(h->d_cmpart);
     if (h->d_bar) cudaFree(h->d_bar);
     if (h->d_tw) cudaFree(h->d_tw);
+    if (h->d_modes) cudaFree(h->d_modes);
     if (h->d_cells) cudaFree(h->d_cells);
     if (h->d_nh) cudaFree(h->d_nh);
     if (h->d_fact) cudaFree(h->d_fact);
@@ -535,6 +540,7 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
         e = alloc(&h->d_tw, (size_t)P);
         if (e == cudaSuccess) e = cudaMemcpy(h->d_tw, tw.data(), (size_t)P * sizeof(double), cudaMemcpyHostToDevice);
         while ((1 << h->logP) < P) ++h->logP;
+        if (e == cudaSuccess && (P == 32 || P == 64 || P == 128)) e = alloc(&h->d_modes, 2 * nm_mode_doubles(s, h->D));
     }
     cudaGetLastError();
     s.err = h->d_err;
@@ -586,6 +592,7 @@ static void* pinned_view(const void* host) {
 // The state kernels on device-accessible arrays (device memory, or the
 // device views of page-locked host arrays).
 static void state_in_launch(pimdb_handle* h, const double* sx, const double* sp) {
+    h->modes_valid = false;
     launch(h, PIMDB_K_CART_UPDATE, [&] { launch_state_in(h->s, h->D, sx, sp, h->stream); });
     h->com_pending = false;
 }
@@ -776,6 +783,7 @@ extern "C" int pimdb_compute_forces(pimdb_handle* h) {
 // pending correction reads buffer red_last and writes new partials into the
 // other buffer.
 static void cart(pimdb_handle* h, int flags, int substep, int kick_nm) {
+    h->modes_valid = false;
     const int rin = h->red_last, rout = 1 - h->red_last;
     if (!h->com_pending) flags &= ~SF_COM_APPLY;
     launch(h, PIMDB_K_CART_UPDATE, [&] {
@@ -791,6 +799,7 @@ static void cart(pimdb_handle* h, int flags, int substep, int kick_nm) {
 }
 
 static void nm_thermo(pimdb_handle* h, int flags, int substep) {
+    h->modes_valid = false;
     const int rin = h->red_last, rout = 1 - h->red_last;
     if (!h->com_pending) flags &= ~SF_COM_APPLY;
     launch(h, PIMDB_K_NM_THERMO, [&] {
@@ -808,6 +817,7 @@ static void nm_thermo(pimdb_handle* h, int flags, int substep) {
 // Applies the O-step of the configured thermostat (thermostat.cpp:15-19)
 // followed, when fixcom, by the partial sums for the COM removal.
 static void nose_hoover(pimdb_handle* h) {
+    h->modes_valid = false;
     const bool nmc = h->cfg.nmthermostat != 0;
     launch(h, PIMDB_K_NM_THERMO, [&] {
         launch_nose_hoover(h->s, h->D, h->nh, nmc ? h->d_C : nullptr, nmc ? h->d_T : nullptr, h->d_pnm, h->stream);
@@ -864,16 +874,22 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
             // tail of the previous step (if pending) and head of this one
             const int mode = (h->nm_tail_pending ? 1 : 0) | 2;
             const long long st = h->step;
+            const size_t nmd = h->d_modes ? nm_mode_doubles(h->s, h->D) : 0;
+            const NmModes mm{(double2*)h->d_modes, (double2*)(h->d_modes + nmd),
+                             h->modes_valid && h->nm_tail_pending ? 1 : 0, false};
             launch(h, PIMDB_K_NM_PROPAGATE, [&] {
                 cudaError_t e = launch_nm_fused(h->s, h->D, h->d_C, h->d_T, h->d_rot, h->d_cmpart, h->d_bar, mode,
                                                 step_ref(h, st), c.fixcom,
-                                                h->opt_fft ? (const double2*)h->d_tw : nullptr, h->logP, h->stream);
+                                                h->opt_fft ? (const double2*)h->d_tw : nullptr, h->logP, h->stream,
+                                                h->d_modes ? &mm : nullptr);
                 if (e != cudaSuccess) h->async_err = e;
             });
+            h->modes_valid = h->d_modes != nullptr && mm.written;
             enqueue_forces(h);
             h->nm_tail_pending = true;
         } else {
             // [COM] + half-kick + free ring-polymer propagation
+            h->modes_valid = false;
             const int rin = h->red_last;
             const int apply = h->com_pending ? 1 : 0;
             launch(h, PIMDB_K_NM_PROPAGATE, [&] {
@@ -898,6 +914,7 @@ static void enqueue_steps(pimdb_handle* h, int nsteps) {
 // COM correction.  The next step absorbs both when it comes first, so a
 // run of pimdb_step calls pays for one fused launch per step.
 static void complete_pending(pimdb_handle* h) {
+    if (h->nm_tail_pending || h->com_pending) h->modes_valid = false;  // the tail changes p
     if (h->nm_tail_pending) {
         const long long st = h->step;
         launch(h, PIMDB_K_NM_PROPAGATE, [&] {
@@ -916,7 +933,8 @@ static void complete_pending(pimdb_handle* h) {
 // the caller then enqueues the steps directly.
 static bool graph_steps(pimdb_handle* h, int nsteps) {
     if (!h->opt_graph || h->graph_broken || h->profile || !h->warm || nsteps < 1) return false;
-    const pimdb_handle::StepState before{h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
+    const pimdb_handle::StepState before{h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending,
+                                         h->modes_valid};
     const auto key = std::make_pair(nsteps, before);
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
@@ -939,7 +957,7 @@ static bool graph_steps(pimdb_handle* h, int nsteps) {
         if (e == cudaSuccess && h->async_err == cudaSuccess)
             e = cudaGraphInstantiateWithFlags(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
         if (graph) cudaGraphDestroy(graph);
-        g.after = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
+        g.after = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending, h->modes_valid};
         g.kernels = h->launches - launches0 + 1;
         // the capture only recorded the work: restore the host state
         h->step = step0;
@@ -948,6 +966,7 @@ static bool graph_steps(pimdb_handle* h, int nsteps) {
         h->nred_last = before.nred_last;
         h->com_pending = before.com_pending;
         h->nm_tail_pending = before.nm_tail_pending;
+        h->modes_valid = before.modes_valid;
         if (e != cudaSuccess || h->async_err != cudaSuccess) {
             cudaGetLastError();
             h->async_err = cudaSuccess;
@@ -974,6 +993,7 @@ static bool graph_steps(pimdb_handle* h, int nsteps) {
     h->nred_last = a.nred_last;
     h->com_pending = a.com_pending;
     h->nm_tail_pending = a.nm_tail_pending;
+    h->modes_valid = a.modes_valid;
     return true;
 }
 
@@ -1010,7 +1030,7 @@ static int graph_io(pimdb_handle* h, const double* xi, const double* pi, int nst
     const void* host[5] = {xi, pi, xo, po, fo};
     pimdb_handle::IoKey key{};
     key.nsteps = nsteps;
-    key.before = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
+    key.before = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending, h->modes_valid};
     for (int k = 0; k < 5; ++k) {
         key.v[k] = host[k] ? pinned_view(host[k]) : nullptr;
         if (host[k] && !key.v[k]) return -1;
@@ -1049,7 +1069,7 @@ static int graph_io(pimdb_handle* h, const double* xi, const double* pi, int nst
         if (e == cudaSuccess && h->async_err == cudaSuccess)
             e = cudaGraphInstantiateWithFlags(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
         if (graph) cudaGraphDestroy(graph);
-        g.after = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending};
+        g.after = {h->red_last, h->nred_last, h->com_pending, h->nm_tail_pending, h->modes_valid};
         g.kernels = h->launches - launches0 + 1;
         // the capture only recorded the work: restore the host state
         h->step = step0;
@@ -1058,6 +1078,7 @@ static int graph_io(pimdb_handle* h, const double* xi, const double* pi, int nst
         h->nred_last = before.nred_last;
         h->com_pending = before.com_pending;
         h->nm_tail_pending = before.nm_tail_pending;
+        h->modes_valid = before.modes_valid;
         if (e != cudaSuccess || h->async_err != cudaSuccess) {
             cudaGetLastError();
             h->async_err = cudaSuccess;
@@ -1080,6 +1101,7 @@ static int graph_io(pimdb_handle* h, const double* xi, const double* pi, int nst
     h->nred_last = a.nred_last;
     h->com_pending = a.com_pending;
     h->nm_tail_pending = a.nm_tail_pending;
+    h->modes_valid = a.modes_valid;
     return PIMDB_OK;
 }
 
@@ -1414,6 +1436,7 @@ extern "C" int pimdb_propagate(pimdb_handle* h) {
     if (!h) return PIMDB_ERR_ARG;
     complete_pending(h);
     if (h->cfg.propagator == PIMDB_PROP_NORMAL_MODES) {
+        h->modes_valid = false;
         launch(h, PIMDB_K_NM_PROPAGATE, [&] {
             launch_nm_propagate(h->s, h->D, h->d_C, h->d_T, h->d_rot, 0, h->d_red[0], 0,
                                 h->opt_fft ? (const double2*)h->d_tw : nullptr, h->d_cm, h->stream);

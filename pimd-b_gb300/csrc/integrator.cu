@@ -943,7 +943,8 @@ __global__ void __launch_bounds__(256) k_nm_warp(Sys s, const double* __restrict
 // every block can be resident (the COM removal's grid barrier).
 template <int D, int E>
 __global__ void __launch_bounds__(96) k_nm_warp3(Sys s, const double* __restrict__ rot, double* cmpart, unsigned* bar,
-                                                 int mode, StepRef sref, int fixcom, const double2* __restrict__ tw_g) {
+                                                 int mode, StepRef sref, int fixcom, const double2* __restrict__ tw_g,
+                                                 double2* __restrict__ mp, double2* __restrict__ mx, int use_modes) {
     constexpr int P = 32 * E;
     __shared__ double2 tw[P / 2];
     __shared__ double2 sF[E][32], sX[E][32];
@@ -959,7 +960,20 @@ __global__ void __launch_bounds__(96) k_nm_warp3(Sys s, const double* __restrict
     const bool head = mode & 2, tail = mode & 1;
     const int k2 = (int)(__brev((unsigned)lane) >> 27);
     double2 z[E];
-    if (role == 0 || role == 1 || head) {
+    // The normal modes of p and x as the previous head left them (in this
+    // warp's register order), when nothing has changed x or p since: no
+    // forward transform for those two.
+    const size_t mbase = (size_t)blockIdx.x * E * 32 + lane;
+    const bool cached = use_modes && mp && (role == 0 || (role == 2 && head));
+    if (cached) {
+        const double2* src = role == 0 ? mp : mx;
+#pragma unroll
+        for (int k1 = 0; k1 < E; ++k1) z[k1] = src[mbase + (size_t)k1 * 32];
+        if (role == 2) {
+#pragma unroll
+            for (int k1 = 0; k1 < E; ++k1) sX[k1][lane] = z[k1];
+        }
+    } else if (role == 0 || role == 1 || head) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int b = 32 * e + lane;
@@ -1053,6 +1067,12 @@ __global__ void __launch_bounds__(96) k_nm_warp3(Sys s, const double* __restrict
         if (role == 2) {
 #pragma unroll
             for (int k1 = 0; k1 < E; ++k1) z[k1] = sX[k1][lane];
+        }
+        // the modes of this head, for the next launch
+        if (mp && (role == 0 || role == 2)) {
+            double2* dst = role == 0 ? mp : mx;
+#pragma unroll
+            for (int k1 = 0; k1 < E; ++k1) dst[mbase + (size_t)k1 * 32] = z[k1];
         }
     }
     if (role == 0 || (role == 2 && head)) {
@@ -1183,11 +1203,15 @@ static int nm_warp_block_any(const Sys& s, int D) {
 
 template <int D, int E>
 static cudaError_t nm_warp_t(const Sys& s, const double* rot, double* cmpart, unsigned* bar, int mode, StepRef step,
-                             int fixcom, const double2* tw, int wpb, cudaStream_t st) {
+                             int fixcom, const double2* tw, int wpb, cudaStream_t st, const NmModes* modes) {
     const long long nwarps = (long long)D * ((s.N + 1) / 2);
     if (wpb == 3) {
         Sys sc = s;
-        void* args[] = {&sc, &rot, &cmpart, &bar, &mode, &step, &fixcom, &tw};
+        double2* mp = modes ? modes->p : nullptr;
+        double2* mx = modes ? modes->x : nullptr;
+        int use = modes ? modes->use : 0;
+        if (modes) modes->written = (mode & 2) != 0;
+        void* args[] = {&sc, &rot, &cmpart, &bar, &mode, &step, &fixcom, &tw, &mp, &mx, &use};
         return cudaLaunchCooperativeKernel((void*)k_nm_warp3<D, E>, dim3((unsigned)nwarps), dim3(96), args, 0, st);
     }
     dim3 grid((unsigned)((nwarps + wpb - 1) / wpb));
@@ -1198,10 +1222,10 @@ static cudaError_t nm_warp_t(const Sys& s, const double* rot, double* cmpart, un
 
 template <int D>
 static cudaError_t nm_warp_d(const Sys& s, const double* rot, double* cmpart, unsigned* bar, int mode, StepRef step,
-                             int fixcom, const double2* tw, int wpb, cudaStream_t st) {
-    if (s.P == 32) return nm_warp_t<D, 1>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
-    if (s.P == 64) return nm_warp_t<D, 2>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
-    return nm_warp_t<D, 4>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
+                             int fixcom, const double2* tw, int wpb, cudaStream_t st, const NmModes* modes) {
+    if (s.P == 32) return nm_warp_t<D, 1>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st, modes);
+    if (s.P == 64) return nm_warp_t<D, 2>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st, modes);
+    return nm_warp_t<D, 4>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st, modes);
 }
 
 // [6][P][kNmTile] arrays plus two FFT work buffers of 3 kNmPairs complex transforms
@@ -1233,6 +1257,9 @@ bool nm_block_fits(const Sys& s, int D) {
 
 bool nm_fused_fits(const Sys& s, int D) { return nm_warp_block_any(s, D) > 0 || nm_block_fits(s, D); }
 
+// one block per (axis, particle pair), E x 32 complex values each (P = 32 E)
+size_t nm_mode_doubles(const Sys& s, int D) { return 2 * (size_t)D * ((s.N + 1) / 2) * (size_t)s.P; }
+
 size_t nm_fused_partials(const Sys& s, int D) {
     return 2 * std::max((size_t)nm_blocks(s, D), (size_t)D * ((s.N + 1) / 2));
 }
@@ -1249,9 +1276,10 @@ static cudaError_t nm_fused_t(const Sys& s, const double* C, const double* T, co
 
 cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
                             unsigned* bar, int mode, StepRef step, int fixcom, const double2* tw, int logP,
-                            cudaStream_t st) {
+                            cudaStream_t st, const NmModes* modes) {
     // the warp kernel when P = 32, 64 or 128 and the FFTs are selected (or
     // the block kernel cannot be resident); the block kernel otherwise
+    if (modes) modes->written = false;
     static int wpb_cache[4] = {-1, -1, -1, -1};
     static long long wpb_key[4] = {-1, -1, -1, -1};
     const long long key = ((long long)s.N << 20) | s.P;
@@ -1261,9 +1289,9 @@ cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* 
     }
     const int wpb = wpb_cache[D];
     if (wpb > 0 && tw) {
-        if (D == 1) return nm_warp_d<1>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
-        if (D == 2) return nm_warp_d<2>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
-        return nm_warp_d<3>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st);
+        if (D == 1) return nm_warp_d<1>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st, modes);
+        if (D == 2) return nm_warp_d<2>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st, modes);
+        return nm_warp_d<3>(s, rot, cmpart, bar, mode, step, fixcom, tw, wpb, st, modes);
     }
     if (D == 1) return nm_fused_t<1>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);
     if (D == 2) return nm_fused_t<2>(s, C, T, rot, cmpart, bar, mode, step, fixcom, tw, logP, st);

@@ -141,8 +141,21 @@ bool nm_block_fits(const Sys& s, int D);
 size_t nm_fused_partials(const Sys& s, int D);
 // `tw` (P/2 twiddles exp(-2 pi i t/P)) selects the FFT transforms (P a power
 // of two, logP = log2 P); NULL selects the P x P matrix products.
+// `modes` (may be null): buffers for the normal modes of p and x
+// (nm_mode_doubles doubles each).  With the three-warp register kernel a
+// launch with the head stores the modes its rotation produced (written is
+// set), and with `use` the next launch takes p's (and, with the head, x's)
+// from them instead of transforming the Cartesian arrays: valid only while
+// nothing else has changed x or p.
+struct NmModes {
+    double2* p;
+    double2* x;
+    int use;
+    mutable bool written;
+};
+size_t nm_mode_doubles(const Sys& s, int D);
 cudaError_t launch_nm_fused(const Sys& s, int D, const double* C, const double* T, const double* rot, double* cmpart,
                             unsigned* bar, int mode, StepRef step, int fixcom, const double2* tw, int logP,
-                            cudaStream_t st);
+                            cudaStream_t st, const NmModes* modes = nullptr);
 
 }  // namespace pimdb
