@@ -282,11 +282,15 @@ __global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ 
 //      the column of the masks in ascending i (deterministic: the
 //      evaluation order does not enter any sum).
 // Under PBC the tile's positions are wrapped into the box once, so a
-// separation lies in (-L, L) and its minimum image is one conditional shift
-// (a compare of the bit patterns and one FP64 add) instead of
-// dx - L floor(dx/L + 1/2).  The exponentials use exp_tang256.  Same result
-// as k_pair_tiles up to rounding; the exact FP64 cutoff test is applied in
-// step 2.
+// separation lies in (-L, L).  On the far path each axis is one FP64
+// subtraction from the image the FP32 screen chose (x_j - L, x_j or x_j + L,
+// kept in shared memory); an entry whose FP32 test lies within 1e-6 L of the
+// half-box edge, where the FP32 and FP64 choices could differ, joins the
+// damping-radius list, whose exact path takes the minimum image as one
+// conditional shift (a compare of the bit patterns and one FP64 add) instead
+// of dx - L floor(dx/L + 1/2).  The exponentials use exp_tang256.  Same
+// result as k_pair_tiles up to rounding; the exact FP64 cutoff test is
+// applied in step 2.
 constexpr int kCompactWarps = 2;
 // gradient capacity per warp unless Sys::pair_cap says otherwise
 constexpr int kCompactDefaultCap = 608;
