@@ -32,6 +32,10 @@
 // non-finite input), the solve kernel recomputes the level-by-level FP64
 // log-sum-exp in the reference's own order instead.  The backward recursion
 // is handled the same way by the second block of each kernel.
+// Usually the previous evaluations' potentials (extrapolated linearly) serve
+// as Vh and pass 1 is skipped; a solve that fails with them is retried from
+// a fresh estimate, inside k_exch_solve below the multi-SM solve's size and
+// by the phase-1 launches from there on.
 #include <algorithm>
 
 #include "exchange_dev.cuh"
