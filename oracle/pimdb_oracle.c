@@ -58,7 +58,7 @@ static inline double sepsq(const orc_system* s, const double* a, const double* b
 }
 
 /* ------------------------------------------------------------------------ */
-/* potentials (src/potentials/*.cpp)                                          */
+/* potentials (src/potentials, one file each)                                        */
 
 void orc_ext_grad(const orc_system* s, const double* x, int n, double* g) {
     const int D = s->ndim;

@@ -64,8 +64,8 @@ void orc_system_init(orc_system* s, double temperature, double raw_cutoff);
 
 /* ---- elementary pieces ---- */
 double orc_min_image(double dx, double L);                                   /* common.cpp:41-43 */
-void orc_ext_grad(const orc_system* s, const double* x, int n, double* g);  /* potentials/*.cpp gradV */
-double orc_ext_value(const orc_system* s, const double* x, int n);          /* potentials/*.cpp V */
+void orc_ext_grad(const orc_system* s, const double* x, int n, double* g);  /* src/potentials: gradV */
+double orc_ext_value(const orc_system* s, const double* x, int n);          /* src/potentials: V */
 void orc_pair_grad(const orc_system* s, const double* r, double* g);        /* one separation vector */
 double orc_pair_value(const orc_system* s, const double* r);
 
