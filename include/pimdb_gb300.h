@@ -299,9 +299,9 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
 int pimdb_set_option(pimdb_handle* h, const char* name, int value);
 
 /* Bosonic exchange without any allocation (no counterpart in the reference).
- * For callers that may not call cudaMalloc while they need the exchange: an
- * engine holding a CUDA stream capture open across its step, a program whose
- * device memory belongs to another allocator or a fixed budget, or a loop
+ * For callers that may not call cudaMalloc while they need the exchange: a
+ * program whose device memory belongs to another allocator or a fixed budget
+ * (an allocation behind its back fails or breaks its accounting), or a loop
  * that cannot afford cudaMalloc's implicit device synchronisation.
  * Inputs and outputs are device memory supplied by the caller:
  *   ring       x[bead][particle][axis] of all `nbeads` beads (only beads 1, 2,
@@ -317,8 +317,10 @@ int pimdb_set_option(pimdb_handle* h, const char* name, int value);
  * err).  The first call on a device looks up that array's device address, so
  * make it before any stream capture.  Calls share the array: calls that
  * overlap on the GPU (different streams or host threads) race.  The call runs
- * on `cuda_stream` (NULL = legacy default stream) and returns after it is
- * done, reporting a non-finite V_B as PIMDB_ERR_NONFINITE_VB. */
+ * on `cuda_stream` (NULL = legacy default stream), which must belong to the
+ * current device (PIMDB_ERR_ARG otherwise); it synchronises that stream and
+ * returns after the work is done, reporting a non-finite V_B as
+ * PIMDB_ERR_NONFINITE_VB. */
 int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms, int ndim, double spring_constant,
                            double beta_ex, int pbc, double box, double* scalars, double* f_first, double* f_last,
                            void* cuda_stream, char* err, int err_len);

@@ -26,7 +26,11 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-DEFAULT_REF = Path(os.environ.get("PIMDB_REFERENCE_DIR", "/root/reference"))
+# The reference checkout: $PIMDB_REFERENCE_DIR, else a directory named
+# "reference" beside this repository (where the build container keeps it).
+# The GPU host has neither, and nothing there needs it.
+DEFAULT_REF = Path(os.environ["PIMDB_REFERENCE_DIR"]) if os.environ.get("PIMDB_REFERENCE_DIR") else \
+    HERE.parent.parent / "reference"
 
 VARIANTS = {
     "d3": ["-DNDIM=3"],

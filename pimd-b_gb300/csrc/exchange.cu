@@ -37,6 +37,7 @@
 // a fresh estimate, inside k_exch_solve below the multi-SM solve's size and
 // by the phase-1 launches from there on.
 #include <algorithm>
+#include <atomic>
 
 #include "exchange_dev.cuh"
 #include "kernels.h"
@@ -375,10 +376,19 @@ __global__ void k_exch_estimators(Sys s, int nbeads) {
 // smaller one (more L1) could start only on SMs without pair-tile blocks,
 // and the pair tiles' blocks could not start beside it: launched first in a
 // step graph, the exchange would hold back part of the pair kernel.
+// Attributes belong to the current device: they are set once per device (a
+// bit per device id below 64, every call above), and two host threads that
+// set them at once only repeat the same cheap calls.
+static std::atomic<unsigned long long> g_carveout_devices{0};
+
 static void exchange_carveouts() {
-    static bool done = false;
-    if (done) return;
-    done = true;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+    if (bit && (g_carveout_devices.load(std::memory_order_acquire) & bit)) return;
     const void* k[] = {(const void*)k_exch_energies<1>, (const void*)k_exch_energies<2>,
                        (const void*)k_exch_energies<3>, (const void*)k_link_prefix<1>,
                        (const void*)k_link_prefix<2>, (const void*)k_link_prefix<3>,
@@ -388,6 +398,7 @@ static void exchange_carveouts() {
                        (const void*)k_exch_forces<1>, (const void*)k_exch_forces<2>, (const void*)k_exch_forces<3>};
     for (const void* f : k)
         cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (bit) g_carveout_devices.fetch_or(bit, std::memory_order_acq_rel);
 }
 
 size_t exchange_energy_doubles(const Sys& s, int D) {
@@ -429,14 +440,18 @@ static bool grid_solve(const Sys& s, int phase, double* ysol, unsigned* gflags, 
     const int nb = (s.N + 1 + 31) / 32;
     const int nct = nb < kGridSolveCtas ? nb : kGridSolveCtas;
     const size_t smem = sizeof(double) * (((size_t)(nb + nct - 1) / nct) * 32 + 32);
-    static int per = -1;
+    // resident CTAs of the whole GPU, per device (0 = not measured yet)
+    static std::atomic<int> per_dev[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int per = (dev >= 0 && dev < 64) ? per_dev[dev].load(std::memory_order_relaxed) - 1 : -1;
     if (per < 0) {
-        int dev = 0, sms = 0, b = 0;
-        cudaGetDevice(&dev);
+        int sms = 0, b = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_exch_solve_grid, kGridSolveThreads, 4096) != cudaSuccess)
             b = 0;
         per = b * sms;
+        if (dev >= 0 && dev < 64) per_dev[dev].store(per + 1, std::memory_order_relaxed);
     }
     if (2 * nct > per) return false;
     Sys sc = s;

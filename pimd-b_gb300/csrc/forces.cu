@@ -13,6 +13,7 @@
 // tile's float partial sum into a double accumulator).
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "forces_dev.cuh"
 #include "kernels.h"
@@ -955,20 +956,33 @@ static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, 
         if (s.cutoff > 0.0) {
             const int cap = s.pair_cap > 0 ? std::min(s.pair_cap, kCompactMaxCap) : kCompactDefaultCap;
             const size_t smem = compact_warp_bytes<D>(cap) * kCompactWarps;
-            static int resident[2] = {0, 0}, rcap[2] = {0, 0}, sms = 0;
+            // occupancy per device and precision, measured again when the
+            // entry cap changes (the attribute is set on the current device)
+            struct Occ {
+                int resident, cap, sms;
+            };
+            static Occ occ[64][2] = {};
+            static std::mutex occ_mu;
             auto kern = mixed ? k_pair_tiles_compact<D, true> : k_pair_tiles_compact<D, false>;
-            if (rcap[mixed] != cap) {
-                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(compact_warp_bytes<D>(kCompactMaxCap) * kCompactWarps));
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[mixed], kern, 32 * kCompactWarps, smem);
-                int dev = 0;
-                cudaGetDevice(&dev);
-                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                if (resident[mixed] < 1) resident[mixed] = 1;
-                rcap[mixed] = cap;
+            int dev = 0;
+            cudaGetDevice(&dev);
+            Occ o{};
+            {
+                std::lock_guard<std::mutex> lock(occ_mu);
+                Occ& slot = occ[(dev >= 0 && dev < 64) ? dev : 0][mixed];
+                if (slot.cap != cap || dev < 0 || dev >= 64) {
+                    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(compact_warp_bytes<D>(kCompactMaxCap) * kCompactWarps));
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&slot.resident, kern, 32 * kCompactWarps, smem);
+                    cudaDeviceGetAttribute(&slot.sms, cudaDevAttrMultiProcessorCount, dev);
+                    if (slot.resident < 1) slot.resident = 1;
+                    slot.cap = cap;
+                }
+                o = slot;
             }
+            const int sms = o.sms;
             const int ntask = s.P * np;
-            const int blocks = std::min((ntask + kCompactWarps - 1) / kCompactWarps, resident[mixed] * sms);
+            const int blocks = std::min((ntask + kCompactWarps - 1) / kCompactWarps, o.resident * sms);
             int* ctr = reinterpret_cast<int*>(part + (pair_partial_doubles(s, D) - 1));
             Sys sr = s;
             if (sms <= 16) sr.reserve_sms = 0;

@@ -1,20 +1,24 @@
 // Exchange evaluation that allocates nothing.
 //
 // Some callers cannot call cudaMalloc at the moment they need the bosonic
-// exchange: a molecular-dynamics engine that keeps a CUDA stream capture open
-// across its whole step (allocating inside a capture is an error), a host
-// program whose device memory is owned by another allocator or a fixed
-// budget, or a latency-critical loop that must not pay the implicit device
-// synchronisation of cudaMalloc/cudaFree.  pimdb_exchange_noalloc serves them:
-// the caller passes device inputs and outputs, and every intermediate array of
-// the exchange (cycle energies, weights, potentials, work flags) lives in one
-// file-scope __device__ array of fixed size, reserved on every GPU that loads
-// this library for as long as the process lives.
+// exchange: a host program whose device memory is owned by another allocator
+// or held to a fixed budget (a cudaMalloc behind its back would fail or break
+// its accounting), or a latency-critical loop that must not pay the implicit
+// device synchronisation of cudaMalloc/cudaFree.  pimdb_exchange_noalloc
+// serves them: the caller passes device inputs and outputs, and every
+// intermediate array of the exchange (cycle energies, weights, potentials,
+// work flags) lives in one file-scope __device__ array of fixed size,
+// reserved on every GPU that loads this library for as long as the process
+// lives.
 //
 // The fixed size limits the system to kNoAllocMaxN particles.  Every call
 // reuses the same array and leaves its contents behind, so each call first
 // clears the flags that must start at zero, and two calls that overlap on the
 // GPU (on different streams, or from different host threads) race on it.
+// The first call on a device looks up the array's device address
+// (cudaGetSymbolAddress, with that device current); make that first call
+// before any stream capture.  The call synchronises `cuda_stream` and reads
+// an error word back before it returns.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -106,6 +110,21 @@ extern "C" int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms
         cudaGetLastError();
         report("no usable CUDA device");
         return PIMDB_ERR_NO_DEVICE;
+    }
+    if (cuda_stream) {
+        // the scratch address below is the current device's: the stream must
+        // belong to that device
+        int sdev = -1;
+        if (cudaStreamGetDevice((cudaStream_t)cuda_stream, &sdev) != cudaSuccess) {
+            cudaGetLastError();
+            report("cuda_stream is not a valid CUDA stream");
+            return PIMDB_ERR_ARG;
+        }
+        if (sdev != dev) {
+            report("cuda_stream belongs to device " + std::to_string(sdev) + " but device " + std::to_string(dev) +
+                   " is current");
+            return PIMDB_ERR_ARG;
+        }
     }
     double* base = nullptr;
     {

@@ -64,4 +64,6 @@ def main(ref: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    sys.path.insert(0, str(Path(__file__).resolve().parents[2]))
+    from oracle.build_ref import DEFAULT_REF  # $PIMDB_REFERENCE_DIR or ../reference beside the repository
+    main(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REF)
