@@ -8,9 +8,13 @@ density 0.0218 A^-3 (L = 22.7297 A), no external potential, normal-mode
 propagator with the normal-mode Langevin thermostat, dt = 2 fs, FP64.
 
 One bench "step" is one MD step of the whole ring polymer.  Synthetic inputs:
-uniform random particle centres (random sequential addition keeping pairs
->= 2.2 A apart, seed 12345) shared by all beads plus a 0.05 A per-bead
-jitter; Maxwell-Boltzmann momenta at the ring-polymer temperature.
+particle centres on the reference's "grid" placement (uniformParticleGrid,
+src/simulation.cpp:133-193: a cubic grid of ceil(L / rho^(-1/3)) cells per
+edge filled in order), shared by all beads, plus a 0.05 A per-bead Gaussian
+jitter (seed 12345); Maxwell-Boltzmann momenta at the ring-polymer
+temperature.  (Random placement at liquid density leaves pairs on the Aziz
+wall, and the N = 4096 system heated up by orders of magnitude within tens of
+steps from it.)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload cfg2|cfg1|cfg3|cfg5] [--precision fp64|mixed]
@@ -60,21 +64,21 @@ WORKLOADS = {
                       "(L=22.7297 A), T=1.5 K, normal-mode propagator + normal-mode Langevin, dt=2 fs",
                  ndim=3, natoms=256, nbeads=64, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=22.7297,
                  inter="aziz", int_p=(0, 0, 0), cutoff_ang=11.36485, ext="free", ext_p=(0, 0, 0),
-                 propagator="normal_modes", nmthermostat=True, dt_fs=2.0, min_sep_ang=2.2, jitter_ang=0.05),
+                 propagator="normal_modes", nmthermostat=True, dt_fs=2.0, placement="grid", jitter_ang=0.05),
     "cfg1": dict(desc="N=16 bosons, P=32, 3D, harmonic trap 3 meV, free pair, VV + Langevin, dt=1 fs",
                  ndim=3, natoms=16, nbeads=32, T_K=1.0, mass_amu=1.0, pbc=False, box_ang=10.0, inter="free",
                  int_p=(0, 0, 0), cutoff_ang=-1.0, ext="harmonic", ext_p=(3.0 * MEV, 0, 0), propagator="cartesian",
-                 nmthermostat=False, dt_fs=1.0, min_sep_ang=0.0, jitter_ang=0.0),
+                 nmthermostat=False, dt_fs=1.0, placement="uniform", jitter_ang=0.0),
     "cfg3": dict(desc="N=1024 bosons, P=32, 2D, dipole D=1 meV A^3 (no cutoff), harmonic trap 1 meV, "
                       "VV + Langevin, dt=1 fs", ndim=2, natoms=1024, nbeads=32, T_K=2.0, mass_amu=1.0, pbc=False,
                  box_ang=60.0, inter="dipole", int_p=(2.4799673e-4, 0, 0), cutoff_ang=-1.0, ext="harmonic",
-                 ext_p=(1.0 * MEV, 0, 0), propagator="cartesian", nmthermostat=False, dt_fs=1.0, min_sep_ang=1.0,
-                 jitter_ang=0.3),
+                 ext_p=(1.0 * MEV, 0, 0), propagator="cartesian", nmthermostat=False, dt_fs=1.0,
+                 placement="separated", min_sep_ang=1.0, jitter_ang=0.3),
     "cfg5": dict(desc="N=4096 He-4 bosons, P=128, 3D PBC, Aziz cutoff 7 A + double well, rho=0.0218/A^3 "
                       "(L=57.2754 A), T=1 K, normal-mode propagator, dt=2 fs", ndim=3, natoms=4096, nbeads=128,
                  T_K=1.0, mass_amu=4.0026, pbc=True, box_ang=57.2754, inter="aziz", int_p=(0, 0, 0), cutoff_ang=7.0,
                  ext="double_well", ext_p=(1.32684e-7 * MEV, 3.0 * ANG, 0), propagator="normal_modes",
-                 nmthermostat=False, dt_fs=2.0, min_sep_ang=2.2, jitter_ang=0.05),
+                 nmthermostat=False, dt_fs=2.0, placement="grid", jitter_ang=0.05),
 }
 
 
@@ -196,22 +200,47 @@ def workload_config(w, precision):
         cutoff=w["cutoff_ang"] * ANG, seed=12345, replica=0)
 
 
+def grid_centres(N, D, L, pbc):
+    """The reference's "grid" initial positions (Simulation::
+    uniformParticleGrid, src/simulation.cpp:133-193): ceil(L / side - 1e-7)
+    cells per edge with side = (N / L^D)^(-1/D), particles at the cell
+    centres in row-major cell order, wrapped by the minimum image under PBC."""
+    side = (N / L ** D) ** (-1.0 / D)
+    n = max(int(math.ceil(L / side - 1.0e-7)), 1)
+    if n ** D < N:
+        raise ValueError("Number of grid boxes is less than the number of particles")
+    cell = L / n
+    idx = np.arange(N)
+    out = np.empty((N, D))
+    for a in range(D):
+        out[:, a] = ((idx // n ** (D - 1 - a)) % n + 0.5) * cell - 0.5 * L
+    if pbc:
+        out -= L * np.floor(out / L + 0.5)
+    return out
+
+
 def initial_state(w, seed=12345):
     rng = np.random.default_rng(seed)
     N, P, D = w["natoms"], w["nbeads"], w["ndim"]
     L = w["box_ang"] * ANG
-    dmin = w["min_sep_ang"] * ANG
-    pts = []
-    while len(pts) < N:
-        c = rng.uniform(-0.5 * L, 0.5 * L, D)
-        if dmin > 0 and pts:
-            d = np.asarray(pts) - c
-            if w["pbc"]:
-                d -= L * np.floor(d / L + 0.5)
-            if np.min(np.einsum("ij,ij->i", d, d)) < dmin * dmin:
-                continue
-        pts.append(c)
-    x = np.asarray(pts)[None] + rng.normal(0.0, w["jitter_ang"] * ANG, (P, N, D))
+    if w["placement"] == "grid":
+        centres = grid_centres(N, D, L, w["pbc"])
+    else:
+        # uniform in the box; "separated": random sequential addition keeping
+        # centres min_sep apart (minimum image under PBC)
+        dmin = w.get("min_sep_ang", 0.0) * ANG if w["placement"] == "separated" else 0.0
+        pts = []
+        while len(pts) < N:
+            c = rng.uniform(-0.5 * L, 0.5 * L, D)
+            if dmin > 0 and pts:
+                d = np.asarray(pts) - c
+                if w["pbc"]:
+                    d -= L * np.floor(d / L + 0.5)
+                if np.min(np.einsum("ij,ij->i", d, d)) < dmin * dmin:
+                    continue
+            pts.append(c)
+        centres = np.asarray(pts)
+    x = centres[None] + rng.normal(0.0, w["jitter_ang"] * ANG, (P, N, D))
     m = w["mass_amu"] * DALTON
     thermo_beta = 1.0 / (w["T_K"] * KELVIN) / P
     p = rng.normal(0.0, math.sqrt(m / thermo_beta), (P, N, D))

@@ -86,6 +86,8 @@ def lib():
         L.orc_update_forces.restype = C.c_int
         L.orc_md_step.argtypes = [S, C.POINTER(State), dp, C.c_int]
         L.orc_md_step.restype = C.c_int
+        L.orc_sample_run.argtypes = [S, C.POINTER(State), C.c_int, C.c_long, C.c_long, dp]
+        L.orc_sample_run.restype = C.c_int
         L.orc_philox_normals.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, C.c_int64, dp]
         L.orc_ranmars_new.argtypes = [C.c_int]
         L.orc_ranmars_new.restype = C.c_void_p
@@ -206,6 +208,16 @@ class Trajectory:
     def nh_energy(self) -> float:
         """Sum over beads of the Nose-Hoover chains' getAdditionToH."""
         return lib().orc_nh_energy(C.byref(self.s), _dp(self.nh))
+
+    def sample_run(self, seed: int, nsteps: int, every: int) -> np.ndarray:
+        """nsteps MD steps with RanMars noise (streams seed+bead); the
+        observables after every `every`-th step, rows of OBSERVABLES."""
+        rows = nsteps // every if every > 0 else 0
+        out = np.zeros((max(rows, 1), len(OBSERVABLES)))
+        st = lib().orc_sample_run(C.byref(self.s), C.byref(self._st), seed, nsteps, every, _dp(out))
+        if st != 0:
+            raise RuntimeError(f"orc_sample_run status {st}")
+        return out[:rows]
 
     def step(self, xi: np.ndarray, nthreads: int = 1) -> int:
         xi = np.ascontiguousarray(xi, dtype=np.float64)

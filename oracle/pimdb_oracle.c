@@ -1349,3 +1349,35 @@ double orc_ranmars_gaussian(orc_ranmars* r) {
 void orc_ranmars_gaussians(orc_ranmars* r, int64_t n, double* out) {
     for (int64_t i = 0; i < n; ++i) out[i] = orc_ranmars_gaussian(r);
 }
+
+/* Test harness with no counterpart in the reference: a thermostatted run for
+ * estimator statistics.  Langevin noise comes from one RanMars stream per
+ * bead seeded seed+bead, drawn in the reference's order (each O-step draws
+ * N*D normals per bead, langevin.cpp:18-25).  Every `every` steps (after
+ * step k, k = every-1, 2*every-1, ...) the 12 values of orc_observables are
+ * appended to out. */
+int orc_sample_run(const orc_system* s, orc_state* st, int seed, long nsteps, long every, double* out) {
+    const int P = s->nbeads;
+    const long bead = (long)s->natoms * s->ndim;
+    orc_ranmars** rs = (orc_ranmars**)calloc((size_t)P, sizeof(orc_ranmars*));
+    double* xi = (double*)malloc(sizeof(double) * 2 * (size_t)P * (size_t)bead);
+    int status = 0;
+    for (int b = 0; b < P; ++b) {
+        rs[b] = orc_ranmars_new(seed + b);
+        if (!rs[b]) status = 1;
+    }
+    long row = 0;
+    for (long k = 0; k < nsteps && status == 0; ++k) {
+        for (int o = 0; o < 2; ++o)
+            for (int b = 0; b < P; ++b) orc_ranmars_gaussians(rs[b], bead, xi + ((long)o * P + b) * bead);
+        status = orc_md_step(s, st, xi, 1);
+        if (status == 0 && every > 0 && (k + 1) % every == 0) {
+            status = orc_observables(s, st->x, st->p, out + 12 * row);
+            ++row;
+        }
+    }
+    for (int b = 0; b < P; ++b) orc_ranmars_free(rs[b]);
+    free(rs);
+    free(xi);
+    return status;
+}

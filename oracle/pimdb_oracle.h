@@ -141,6 +141,12 @@ double orc_nh_energy(const orc_system* s, const double* nh);
  * identical).  Returns the exchange status. */
 int orc_md_step(const orc_system* s, orc_state* st, const double* xi, int nthreads);
 
+/* Test harness (no counterpart in the reference): nsteps MD steps with
+ * Langevin noise from RanMars streams seeded seed+bead, storing the 12
+ * orc_observables values after every `every`-th step in out[row][12].
+ * Returns 0, 1 for an invalid seed, or the exchange status. */
+int orc_sample_run(const orc_system* s, orc_state* st, int seed, long nsteps, long every, double* out);
+
 /* Individual pieces of the step, exposed for unit tests. */
 void orc_zero_momentum(const orc_system* s, double* p);                       /* simulation.cpp:581-603 */
 void orc_langevin(const orc_system* s, double* p, const double* xi);          /* langevin.cpp:15-27 */
