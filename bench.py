@@ -18,15 +18,22 @@ steps from it.)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload cfg2|cfg1|cfg3|cfg5] [--precision fp64|mixed]
-                  [--batch-steps K4] [--no-batched]
+                  [--batch-steps K4] [--no-batched] [--no-others]
 
-The same JSON line carries a "batched" object: the batched-replica engine on
-the ensemble workload (512 independent replicas from default_rng(12345):
-N ~ U{8..128}, P ~ U{16,32,64}, T ~ U[0.5,4] K, 3D bosons of mass 1 Da in a
-3 meV harmonic trap with a 1 meV harmonic pair interaction (all pairs),
-cartesian velocity Verlet + Langevin, dt = 1 fs, replica seed 12345+r), in
-mixed precision, K4 steps replayed as one CUDA graph; its force error is
-measured against the engine's FP64 path on the same coordinates.
+The same JSON line carries:
+- "systems": the other benchmark systems on the plain single-system path
+  (N = 16 trap; N = 1024 2D dipole; N = 4096, P = 128 in FP64 and mixed),
+  each with its mixed-precision force error against the FP64 path;
+- "batched" / "batched_fp64": the batched-replica engine on the ensemble
+  workload (512 independent replicas from default_rng(12345): N ~ U{8..128},
+  P ~ U{16,32,64}, T ~ U[0.5,4] K, 3D bosons of mass 1 Da in a 3 meV
+  harmonic trap with a 1 meV harmonic pair interaction (all pairs),
+  cartesian velocity Verlet + Langevin, dt = 1 fs, replica seed 12345+r),
+  K4 steps replayed as one CUDA graph, in mixed precision and in FP64, each
+  with its roofline;
+- "plain_fp64_same_ensemble": the same 512 replicas run one by one through
+  the plain FP64 single-system path, the denominator of the batched
+  engine's speed-up on the same work.
 
 For N > 1 (torchrun) every rank runs its own replica (replicas only: the
 bead ring of one system is never split across GPUs); value = all ranks'
@@ -123,24 +130,50 @@ def batched_workload(precision, n=512, seed=12345):
         ps.append(rng.normal(0.0, math.sqrt(mass / thermo_beta), (P, N, 3)))
     return cfgs, xs, ps
 
-
-def run_batched(pk, torch, stream, K, W, rank, world, dist):
-    """Mixed-precision batched ensemble: device-timed graph replay, force
-    error against the FP64 path, and an end-to-end run through the C ABI."""
-    cfgs, xs, ps = batched_workload("mixed")
-    c64, _, _ = batched_workload("fp64")
+def batched_roofline(cfgs, t_step, precision, peaks):
+    """The ensemble step against its roofline, by the accounting of the
+    project: t_ideal = B / BW + F_pair / peak_pair + F_exch / peak_FP64 with
+    B = 6 d 8 bytes per bead-particle (x, p, f read and written), F_pair =
+    17 FLOPs per unique harmonic pair and bead (FMA = 2; FP32 pipe in mixed
+    precision), F_exch = 19 N^2 FP64 FLOPs per replica (its 1.5 N^2 + 0.5 N^2
+    exponentials are counted apart).  frac = t_ideal / t_measured."""
     units = sum(c.natoms * c.nbeads for c in cfgs)
-    with pk.Batch(c64, stream=stream.cuda_stream) as b64, pk.Batch(cfgs, stream=stream.cuda_stream) as b:
-        b64.set_states(xs, ps)
-        b64.compute_forces()
-        f64 = b64.get_states(flat=True)[2]
+    B = 6 * 3 * 8 * units
+    F_pair = sum(17 * c.nbeads * c.natoms * (c.natoms - 1) // 2 for c in cfgs)
+    F_exch = sum(19 * c.natoms ** 2 for c in cfgs)
+    exps = sum(2 * c.natoms ** 2 for c in cfgs)
+    bw = peaks["hbm_gbs"] * 1e9
+    p64 = peaks["fp64_tflops"] * 1e12
+    ppair = (peaks["fp32_tflops"] if precision == "mixed" else peaks["fp64_tflops"]) * 1e12
+    t_ideal = B / bw + F_pair / ppair + F_exch / p64
+    return {"bound": "fp64 pipe (exchange) + " + ("fp32" if precision == "mixed" else "fp64") + " pipe (pairs) + hbm",
+            "t_ideal_ms": 1e3 * t_ideal, "t_measured_ms": 1e3 * t_step, "frac": t_ideal / t_step,
+            "streaming_bytes_per_step": B, "pair_flops_per_step": F_pair, "exchange_flops_per_step": F_exch,
+            "exchange_exps_per_step": exps,
+            "peaks": {"hbm_gbs": peaks["hbm_gbs"], "fp64_tflops": peaks["fp64_tflops"],
+                      "fp32_tflops": peaks["fp32_tflops"]},
+            "peak_source": "HBM: MEASURED_PEAKS.json; FP64 and FP32: FMA probes measured in this run "
+                           "(MEASURED_PEAKS.json has neither)"}
+
+
+def run_batched(pk, torch, stream, K, W, rank, world, dist, precision, peaks, e2e=True, ref_forces=None):
+    """The batched ensemble: device-timed replay of one CUDA graph of K steps;
+    for mixed precision also the force error against the FP64 batch and an
+    end-to-end run through the C ABI."""
+    cfgs, xs, ps = batched_workload(precision)
+    units = sum(c.natoms * c.nbeads for c in cfgs)
+    out = {}
+    with pk.Batch(cfgs, stream=stream.cuda_stream) as b:
         b.set_states(xs, ps)
         b.compute_forces()
-        f32 = b.get_states(flat=True)[2]
-        errs = []
-        for r in range(len(cfgs)):
-            lo, hi = b.offsets[r], b.offsets[r + 1]
-            errs.append(float(np.linalg.norm(f32[lo:hi] - f64[lo:hi]) / np.linalg.norm(f64[lo:hi])))
+        f = b.get_states(flat=True)[2]
+        if ref_forces is not None:
+            errs = [float(np.linalg.norm(f[b.offsets[r]:b.offsets[r + 1]] - ref_forces[b.offsets[r]:b.offsets[r + 1]])
+                          / np.linalg.norm(ref_forces[b.offsets[r]:b.offsets[r + 1]])) for r in range(len(cfgs))]
+            out["force_error"] = {
+                "max_norm_rel": max(errs), "median_norm_rel": float(np.median(errs)),
+                "against": "the FP64 batch on the same coordinates; tests/test_baseline_sizes.py checks every "
+                           "replica of both against the FP64 oracle (FP64 within 1e-10 per bead, mixed within 1e-6)"}
         threads, ctas = b.autotune(steps=3)
         b.step_async(max(W, 3))
         b.synchronize()
@@ -158,36 +191,77 @@ def run_batched(pk, torch, stream, K, W, rank, world, dist):
         b.synchronize()
         t = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, dist)
         launches = b.launch()["launches"] - launches0
-        # end to end: pinned host state in, one step, state and forces out
-        n = int(b.offsets[-1])
-        hx = torch.empty(n, dtype=torch.float64, pin_memory=True)
-        hp = torch.empty(n, dtype=torch.float64, pin_memory=True)
-        hf = torch.empty(n, dtype=torch.float64, pin_memory=True)
-        hx.numpy()[:] = b.flatten(xs)
-        hp.numpy()[:] = b.flatten(ps)
-        Ke = 20
-        lib = pk.lib()
-        ptr = lambda a: pk.C.c_void_p(a.data_ptr())
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(Ke):
-            b._c(lib.pimdb_batch_set_states(b._b, ptr(hx), ptr(hp)))
-            b.step(1)
-            b._c(lib.pimdb_batch_get_states(b._b, ptr(hx), ptr(hp), ptr(hf)))
-        te = max_over_ranks(time.perf_counter() - t0, dist)
-    return {"value": world * units * K / t, "unit": "bead-steps/s", "ms_per_step": 1e3 * t / K, "steps": K,
-            "replicas": len(cfgs), "bead_particles": units, "precision": "mixed (FP32 pair forces, FP64 accumulation, "
-            "exchange and integrator)",
-            "force_error": {"max_norm_rel": max(errs), "median_norm_rel": float(np.median(errs)),
-                            "against": "the engine's FP64 path on the same coordinates (which matches the FP64 "
-                                       "oracle within 1e-10)"},
-            "launch": {"threads": threads, "ctas_per_sm": ctas, "graph": "one CUDA graph of K step launches",
-                       "autotuned": True},
-            "gpu_launches": launches, "l2": "not flushed inside the graph; working set 140+ MB > 129 MB L2",
-            "e2e": {"value": world * units * Ke / te, "unit": "bead-steps/s", "h2d_bytes_per_step": 2 * n * 8,
-                    "d2h_bytes_per_step": 3 * n * 8, "steps": Ke},
-            "workload": "512 replicas, N~U{8..128}, P~U{16,32,64}, T~U[0.5,4] K, 3D bosons, mass 1 Da, harmonic "
-                        "trap 3 meV + harmonic pair 1 meV (all pairs), no PBC, cartesian VV + Langevin, dt=1 fs"}
+        if e2e:
+            # end to end: pinned host state in, one step, state and forces out
+            n = int(b.offsets[-1])
+            hx = torch.empty(n, dtype=torch.float64, pin_memory=True)
+            hp = torch.empty(n, dtype=torch.float64, pin_memory=True)
+            hf = torch.empty(n, dtype=torch.float64, pin_memory=True)
+            hx.numpy()[:] = b.flatten(xs)
+            hp.numpy()[:] = b.flatten(ps)
+            Ke = 20
+            lib = pk.lib()
+            ptr = lambda a: pk.C.c_void_p(a.data_ptr())
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(Ke):
+                b._c(lib.pimdb_batch_set_states(b._b, ptr(hx), ptr(hp)))
+                b.step(1)
+                b._c(lib.pimdb_batch_get_states(b._b, ptr(hx), ptr(hp), ptr(hf)))
+            te = max_over_ranks(time.perf_counter() - t0, dist)
+            out["e2e"] = {"value": world * units * Ke / te, "unit": "bead-steps/s", "h2d_bytes_per_step": 2 * n * 8,
+                          "d2h_bytes_per_step": 3 * n * 8, "steps": Ke}
+    out.update({
+        "value": world * units * K / t, "unit": "bead-steps/s", "ms_per_step": 1e3 * t / K, "steps": K,
+        "replicas": len(cfgs), "bead_particles": units,
+        "precision": ("mixed (FP32 pair forces, FP64 accumulation, exchange and integrator)" if precision == "mixed"
+                      else "fp64"),
+        "launch": {"threads": threads, "ctas_per_sm": ctas, "graph": "one CUDA graph of K step launches",
+                   "autotuned": True},
+        "gpu_launches": launches, "l2": "not flushed inside the graph; working set 140+ MB > 129 MB L2",
+        "workload": "512 replicas, N~U{8..128}, P~U{16,32,64}, T~U[0.5,4] K, 3D bosons, mass 1 Da, harmonic "
+                    "trap 3 meV + harmonic pair 1 meV (all pairs), no PBC, cartesian VV + Langevin, dt=1 fs",
+        "roofline": batched_roofline(cfgs, t / K, precision, peaks)})
+    return out
+
+
+def batched_fp64_forces(pk, stream):
+    cfgs, xs, ps = batched_workload("fp64")
+    with pk.Batch(cfgs, stream=stream.cuda_stream) as b:
+        b.set_states(xs, ps)
+        b.compute_forces()
+        return b.get_states(flat=True)[2]
+
+
+def run_ensemble_single(pk, torch, stream, K, W):
+    """The plain FP64 single-system path on the ensemble workload: every
+    replica through its own handle (pimdb_step), one after another, each a
+    K-step graph replay timed with events after W warm-up steps.  value =
+    all replicas' bead-steps / the summed device time."""
+    cfgs, xs, ps = batched_workload("fp64")
+    tot, units = 0.0, 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    for r, c in enumerate(cfgs):
+        with pk.System(c, stream=stream.cuda_stream) as g:
+            g.set_state(xs[r], ps[r])
+            g.step_async(max(W, 1))
+            g.step_async(K)  # captures the K-step graph
+            g.synchronize()
+            g.profile(0)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            g.step_async(K)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            g.synchronize()
+            launches += g.profile(-1)["launches"]
+            tot += ev0.elapsed_time(ev1) / 1e3
+            units += c.natoms * c.nbeads * K
+    return {"value": units / tot, "unit": "bead-steps/s", "ms_per_step": 1e3 * tot / K, "steps": K,
+            "replicas": len(cfgs), "precision": "fp64", "gpu_launches": launches,
+            "how": "each replica alone through pimdb_step (a K-step CUDA graph per handle), replicas one after "
+                   "another; summed device time"}
 
 
 def workload_config(w, precision):
@@ -246,29 +320,42 @@ def initial_state(w, seed=12345):
     p = rng.normal(0.0, math.sqrt(m / thermo_beta), (P, N, D))
     return x, p
 
+# FLOPs of one pair's force (FMA = 2): Aziz 63, dipole 16 (2D) or 20 (3D),
+# harmonic 17, plus 9 for the minimum image under PBC; transcendentals
+# (square root, reciprocal, exponential, division) counted apart.  A pair
+# only tested against the cutoff costs 15 FLOPs with the minimum image, 6
+# without.
+PAIR_FLOPS = {"aziz": 63, "harmonic": 17, "free": 0}
+PAIR_TRANSC = {"aziz": 4, "dipole": 1, "harmonic": 0, "free": 0}
 
-def pair_flops(w, x):
-    """Algorithmic FLOPs of one evaluation of the pair kernel: every unique
-    pair costs the separation test (15 FLOPs with the minimum image); pairs
-    inside the cutoff add the gradient.  Aziz: 63 arithmetic + sqrt + 3
-    divisions (10 each) + 2 exp (20 each) = 133; dipole: 8 + sqrt + div = 28;
-    harmonic: 6."""
-    per_in = {"aziz": 133, "dipole": 28, "harmonic": 6, "free": 0}[w["inter"]]
+
+def pair_work(w, x):
+    """Algorithmic work of one pair-force evaluation (all beads) of
+    workload w at positions x: unique pairs, pairs inside the cutoff, FLOPs
+    with every unique pair priced at the full force (the project's
+    accounting), FLOPs with only the pairs inside the cutoff priced at the
+    force and the others at the test, and the transcendental count."""
     if w["inter"] == "free":
-        return 0.0, 0
+        return None
+    per = PAIR_FLOPS.get(w["inter"], 16 if w["ndim"] == 2 else 20) + (9 if w["pbc"] else 0)
+    tested = 15 if w["pbc"] else 6
     N, P = w["natoms"], w["nbeads"]
     L = w["box_ang"] * ANG
     cut = w["cutoff_ang"] * ANG
     inside = 0
+    iu = np.triu_indices(N, 1)
     for b in range(P):
-        d = x[b][:, None, :] - x[b][None, :, :]
+        d = x[b][iu[0]] - x[b][iu[1]]
         if w["pbc"]:
             d -= L * np.floor(d / L + 0.5)
-        r = np.sqrt(np.einsum("ijk,ijk->ij", d, d))
-        iu = np.triu_indices(N, 1)
-        inside += int(np.sum(r[iu] < cut)) if cut > 0 else len(iu[0])
+        r2 = np.einsum("ij,ij->i", d, d)
+        inside += int(np.sum(r2 < cut * cut)) if cut > 0 else len(r2)
     pairs = P * N * (N - 1) // 2
-    return float(pairs * 15 + inside * per_in), inside
+    return {"pairs": pairs, "inside": inside, "flops_all": float(pairs * per),
+            "flops_in_cutoff": float(pairs * tested + inside * (per - (9 if w["pbc"] else 0))),
+            "transcendentals_in_cutoff": inside * PAIR_TRANSC[w["inter"]], "per_pair": per}
+
+PAIR_NCU = {"dram_bytes": 458496, "fp64_pipe": {"active": 0.752, "elapsed": 0.654}}
 
 
 class ClockSampler:
@@ -330,7 +417,7 @@ def cpu_baseline(w, seconds=12.0, nthreads=None):
         if (el >= seconds and steps >= 2) or steps >= 100000:
             break
     value = w["natoms"] * w["nbeads"] * steps / el
-    return {"value": value, "unit": "bead-steps/s", "cores": nthreads, "kind": "port",
+    return {"value": value, "unit": "bead-steps/s", "cores": nthreads, "kind": "port", "cpu": host_cpu(),
             "sample": f"{steps} MD steps of the same workload ({el:.1f} s), FP64 oracle port with the "
                       f"per-bead force loops on {nthreads} POSIX threads"}
 
@@ -363,10 +450,122 @@ def run_reference(args, w, rank, world):
             "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": w["desc"], "precision": "fp64"},
             "cpu_baseline": {"value": value, "unit": "bead-steps/s", "cores": nthreads, "kind": "port",
+                             "cpu": host_cpu(),
                              "sample": f"{K} MD steps after {W} warm-up steps, FP64 oracle port of the reference "
                                        f"(the reference's own build needs its sources, absent on the GPU host)"},
             "e2e": {"value": value, "unit": "bead-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def time_single(pk, torch, stream, w, precision, K, W, dist, rank, world, sampler=None, profile=False):
+    """One system of workload w through the plain single-system path: W
+    warm-up steps, then K steps each bracketed by events on the library's
+    stream (L2 flushed before each one when the working set fits in twice
+    the L2).  Returns the timing, launch count and optionally per-kernel
+    device times, plus the handle and initial state for further use."""
+    cfg, (x0, p0) = rank_workload(w, precision, rank)
+    N, P, D = w["natoms"], w["nbeads"], w["ndim"]
+    sysm = pk.System(cfg, stream=stream.cuda_stream)
+    sysm.set_state(x0, p0)
+    # warm-up as single steps, like the timed loop: the step graphs are
+    # captured here, outside the timed region
+    for _ in range(W):
+        sysm.step_async(1)
+    sysm.synchronize()
+    ld = (N + 31) // 32 * 32
+    ws = 4 * P * D * ld * 8 + 4 * N * (N + 1) // 2 * 8
+    do_flush = ws <= 2 * 129e6
+    l2_note = ("flushed before every timed step (512 MiB write, outside the step's events)" if do_flush else
+               f"not flushed: working set {ws / 1e6:.0f} MB (state and exchange arrays) > 2 x 129 MB L2")
+    flush = torch.empty(512 * 1024 * 1024 // 4 if do_flush else 1, dtype=torch.float32, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(K):
+        if do_flush:
+            flush.zero_()
+        ev[k][0].record(stream)
+        sysm.step_async(1)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    sysm.synchronize()
+    clocks = sampler.stop() if sampler else None
+    del flush
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_s = max_over_ranks(sum(step_ms) / 1e3, dist)
+    # kernel launches in the timed region: the same K steps, counted.  Each
+    # untimed block restarts from the initial state, so no run goes far past
+    # W + K steps (the 2D dipole system is not stable over thousands)
+    sysm.set_state(x0, p0)
+    sysm.profile(0)
+    sysm.step_async(K)
+    sysm.synchronize()
+    launches = sysm.profile(-1)["launches"]
+    prof = None
+    if profile:
+        # per-kernel device times (events around each launch on the library stream)
+        sysm.set_state(x0, p0)
+        sysm.profile(1)
+        sysm.step_async(K)
+        sysm.synchronize()
+        prof = sysm.profile(-1)
+        sysm.profile(0)
+    res = {"value": world * N * P * K / tot_s, "unit": "bead-steps/s", "ms_per_step": 1e3 * tot_s / K, "steps": K,
+           "warmup": W, "gpu_launches": launches, "l2": l2_note, "precision": precision, "workload": w["desc"]}
+    return res, sysm, (x0, p0), prof, clocks
+
+
+def forces_of(pk, stream, w, precision, x):
+    cfg = workload_config(w, precision)
+    with pk.System(cfg, stream=stream.cuda_stream) as g:
+        g.set_state(x, np.zeros_like(x))
+        g.compute_forces()
+        return g.get_state()[2]
+
+
+def run_other_systems(pk, torch, stream, K, W, dist, rank, world):
+    """The other benchmark systems on the plain single-system path: the
+    N = 16 trap, the N = 1024 2D dipole system and the N = 4096 system in
+    FP64 and in mixed precision, each with its mixed-precision force error
+    against the FP64 path on its initial state."""
+    out = {}
+    for name, precs in (("cfg1", ("fp64",)), ("cfg3", ("fp64",)), ("cfg5", ("fp64", "mixed"))):
+        w = WORKLOADS[name]
+        x0 = initial_state(w)[0]
+        f64 = forces_of(pk, stream, w, "fp64", x0)
+        fmx = forces_of(pk, stream, w, "mixed", x0)
+        err = float(np.linalg.norm(fmx - f64) / np.linalg.norm(f64))
+        for prec in precs:
+            Ks = min(K, 100)
+            res, sysm, _, prof, _ = time_single(pk, torch, stream, w, prec, Ks, W, dist, rank, world, profile=True)
+            sysm.close()
+            ms, cnt = prof["ms"], prof["counts"]
+            res["per_class_ms_per_step"] = {k: v / Ks for k, v in ms.items() if v > 0}
+            res["force_error_mixed_vs_fp64"] = err
+            res["parity"] = ("FP64 forces, exchange and 5-step trajectories of this initial state match the oracle "
+                             "within 1e-10 / 1e-9 (tests/test_baseline_sizes.py); mixed within 1e-6")
+            out[f"{name}_{prec}"] = res
+    return out
+
+
+def host_cpu():
+    model = ""
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith("model name"):
+                model = ln.split(":", 1)[1].strip()
+                break
+        if not model:
+            r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+            for ln in r.stdout.splitlines():
+                if ln.startswith("Model name"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+    except Exception:
+        pass
+    import platform
+    return {"model": model or "unknown", "arch": platform.machine(), "logical_cpus": os.cpu_count()}
 
 
 def main():
@@ -382,6 +581,7 @@ def main():
     ap.add_argument("--profile-only", action="store_true", help="short run for an ncu capture")
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-others", action="store_true", help="skip the other benchmark systems")
     ap.add_argument("--profile-only-batched", action="store_true",
                     help="short run of the batched ensemble only (plain launches) for an ncu capture")
     args = ap.parse_args()
@@ -412,64 +612,24 @@ def main():
             b.set_states(xs, ps)
             b.step(max(args.warmup, 1) + max(args.steps, 1))
         return
-    cfg, (x0, p0) = rank_workload(w, args.precision, rank)
-    N, P, D = w["natoms"], w["nbeads"], w["ndim"]
-    units = N * P
-    sysm = pk.System(cfg, stream=stream.cuda_stream)
-    sysm.set_state(x0, p0)
     W = max(args.warmup, 3)
     K = max(args.steps, 1)
-    # warm-up as single steps, like the timed loop: the step graphs are
-    # captured here, outside the timed region
-    for _ in range(W):
-        sysm.step_async(1)
-    sysm.synchronize()
     if args.profile_only:
-        sysm.step_async(K)
-        sysm.synchronize()
+        cfg, (x0, p0) = rank_workload(w, args.precision, rank)
+        with pk.System(cfg, stream=stream.cuda_stream) as sysm:
+            sysm.set_state(x0, p0)
+            for _ in range(W):
+                sysm.step_async(1)
+            sysm.step_async(K)
+            sysm.synchronize()
         return
 
-    # L2 between timed steps: flushed (a 512 MiB write) unless the step's own
-    # working set is more than twice the 129 MB L2
-    ld = (N + 31) // 32 * 32
-    ws = 4 * P * D * ld * 8 + (4 * N * (N + 1) // 2 * 8 if w.get("bosonic", True) else 0)
-    do_flush = ws <= 2 * 129e6
-    l2_note = ("flushed before every timed step (512 MiB write, outside the step's events)" if do_flush else
-               f"not flushed: working set {ws / 1e6:.0f} MB (state and exchange arrays) > 2 x 129 MB L2")
-    flush = torch.empty(512 * 1024 * 1024 // 4 if do_flush else 1, dtype=torch.float32, device="cuda")
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    N, P, D = w["natoms"], w["nbeads"], w["ndim"]
+    units = N * P
     sampler = ClockSampler(local) if rank == 0 else None
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    for k in range(K):
-        if do_flush:
-            flush.zero_()
-        ev[k][0].record(stream)
-        sysm.step_async(1)
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
-    sysm.synchronize()
-    clocks = sampler.stop() if sampler else None
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    tot_s = max_over_ranks(sum(step_ms) / 1e3, dist)
-    value = world * units * K / tot_s
-
-    # kernel launches in the timed region: the same K steps, counted.  Each
-    # untimed block restarts from the initial state, so no run goes far past
-    # W + K steps (the 2D dipole system is not stable over thousands)
-    sysm.set_state(x0, p0)
-    prof = sysm.profile(0)
-    sysm.step_async(K)
-    sysm.synchronize()
-    launches = sysm.profile(-1)["launches"]
-    # per-kernel device times (events around each launch on the library stream)
-    sysm.set_state(x0, p0)
-    sysm.profile(1)
-    sysm.step_async(K)
-    sysm.synchronize()
-    prof = sysm.profile(-1)
-    sysm.profile(0)
+    head, sysm, (x0, p0), prof, clocks = time_single(pk, torch, stream, w, args.precision, K, W, dist, rank, world,
+                                                     sampler=sampler, profile=True)
+    value = head["value"]
 
     # end to end through the C ABI (pimdb_step_io) with pinned host buffers
     shape = (P, N, D)
@@ -489,9 +649,25 @@ def main():
     e2e = {"value": world * units * Ke / e2e_s, "unit": "bead-steps/s", "h2d_bytes_per_step": 2 * P * N * D * 8,
            "d2h_bytes_per_step": 3 * P * N * D * 8, "steps": Ke}
     sysm.close()
-    del flush
-    batched = None if args.no_batched else run_batched(pk, torch, stream, max(args.batch_steps, 1), W, rank, world,
-                                                      dist)
+
+    fp64_peak = pk.measure_fp64_peak()
+    fp32_peak = pk.measure_fp32_peak()
+    peaks = {"hbm_gbs": 6800.0, "hbm_source": "fallback"}
+    try:
+        mp = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        peaks = {"hbm_gbs": float(mp["hbm_gbs"]), "hbm_source": "MEASURED_PEAKS.json"}
+    except Exception:
+        pass
+    peaks.update(fp64_tflops=fp64_peak, fp32_tflops=fp32_peak)
+
+    others = None if args.no_others else run_other_systems(pk, torch, stream, K, W, dist, rank, world)
+    batched = batched64 = plain_ens = None
+    if not args.no_batched:
+        Kb = max(args.batch_steps, 1)
+        f64 = batched_fp64_forces(pk, stream)
+        batched = run_batched(pk, torch, stream, Kb, W, rank, world, dist, "mixed", peaks, ref_forces=f64)
+        batched64 = run_batched(pk, torch, stream, Kb, W, rank, world, dist, "fp64", peaks, e2e=False)
+        plain_ens = run_ensemble_single(pk, torch, stream, min(K, 20), W)
 
     if rank != 0:
         if dist:
@@ -502,47 +678,59 @@ def main():
     ms, cnt = prof["ms"], prof["counts"]
     dom = max(ms, key=lambda k: ms[k])
     dom_ms = ms[dom] / max(cnt[dom], 1)
-    fp64_peak = pk.measure_fp64_peak()
-    peaks = {}
-    try:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-    except Exception:
-        pass
     roof = {"kernel": dom, "kernel_share": ms[dom] / max(sum(ms.values()), 1e-30), "launch_ms": dom_ms,
             "per_class_ms_per_step": {k: v / K for k, v in ms.items() if v > 0}}
-    if dom == "bead_forces" and w["inter"] != "free":
-        fl, inside = pair_flops(w, x0)
-        ach = fl / (dom_ms * 1e-3) / 1e12
-        peak = fp64_peak if args.precision == "fp64" else None
+    work = pair_work(w, x0) if dom == "bead_forces" else None
+    if work:
+        t = dom_ms * 1e-3
+        peak = fp64_peak if args.precision == "fp64" else fp32_peak
         # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one
-        # k_pair_tiles_compact launch on this workload, from an ncu capture
-        # (ncu --set full -k regex:k_pair_tiles_compact -s 2 -c 1 of
-        # --profile-only --steps 3 --warmup 3); the per-step state (2.4 MB)
-        # stays in L2 between launches
-        traffic = 458496 if (args.workload == "cfg2" and args.precision == "fp64") else None
-        roof.update({"bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": ach,
-                     "peak": peak, "unit": "TFLOP/s", "frac": (ach / peak) if peak else None,
-                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu capture)" if traffic else None,
-                     "peak_source": "measured in-run (FP64 FMA probe)",
-                     "algorithmic": f"{fl:.4g} FLOP per launch ({inside} unique pairs inside the cutoff)"})
+        # k_pair_tiles_compact launch on this workload and its FP64 pipe
+        # utilisation, from the ncu capture in
+        # profiles/step_kernels_aziz_pbc_N256_P64_fp64.md
+        ncu = PAIR_NCU if (args.workload == "cfg2" and args.precision == "fp64") else None
+        roof.update({
+            "bound": "fp64" if args.precision == "fp64" else "fp32",
+            "achieved": work["flops_all"] / t / 1e12, "peak": peak, "unit": "TFLOP/s",
+            "frac": work["flops_all"] / t / 1e12 / peak,
+            "algorithmic": (f"{work['flops_all']:.4g} FLOP per launch: {work['pairs']} unique pairs x "
+                            f"{work['per_pair']} FLOP (force with minimum image, FMA = 2)"),
+            "achieved_in_cutoff": work["flops_in_cutoff"] / t / 1e12,
+            "frac_in_cutoff": work["flops_in_cutoff"] / t / 1e12 / peak,
+            "algorithmic_in_cutoff": (f"{work['flops_in_cutoff']:.4g} FLOP per launch: {work['inside']} pairs "
+                                      f"inside the cutoff at the force, the rest at the 15-FLOP test"),
+            "transcendentals_per_launch": work["transcendentals_in_cutoff"],
+            "fp64_pipe_ncu": ncu["fp64_pipe"] if ncu else None,
+            "traffic": ncu["dram_bytes"] if ncu else None,
+            "traffic_unit": "DRAM bytes per launch (ncu capture)" if ncu else None,
+            "peak_source": ("FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 entry)"
+                            if args.precision == "fp64" else "FP32 FMA probe measured in this run")})
     else:
         bytes_per = 6 * 8 * units * D
         ach = bytes_per / (dom_ms * 1e-3) / 1e9
-        peak = peaks.get("hbm_gbs", 6800.0)
-        roof.update({"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs"})
+        roof.update({"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["hbm_source"]})
     line = {"metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": 1e3 * tot_s / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32 pair forces / f64 exchange and integrator",
             "data": "synthetic",
             "config": {"workload": w["desc"], "natoms": N, "nbeads": P, "ndim": D, "precision": args.precision,
+                       "init": "grid placement (reference uniformParticleGrid) + 0.05 A jitter"
+                       if w["placement"] == "grid" else w["placement"],
                        "parallelism": f"replicas x{world}" if world > 1 else "single system",
-                       "l2": l2_note},
-            "e2e": e2e, "roofline": roof, "gpu_launches": launches, "clocks": clocks,
-            "fp64_peak_tflops": fp64_peak}
+                       "l2": head["l2"]},
+            "e2e": e2e, "roofline": roof, "gpu_launches": head["gpu_launches"], "clocks": clocks,
+            "peaks": peaks}
+    if others:
+        line["systems"] = others
     if batched:
-        batched["vs_plain_fp64"] = batched["value"] / value if args.precision == "fp64" else None
+        batched["vs_batched_fp64"] = batched["value"] / batched64["value"]
+        batched["vs_plain_fp64_same_ensemble"] = batched["value"] / plain_ens["value"]
+        batched64["vs_plain_fp64_same_ensemble"] = batched64["value"] / plain_ens["value"]
+        batched["vs_plain_fp64_benchmark_system"] = batched["value"] / value if args.precision == "fp64" else None
         line["batched"] = batched
+        line["batched_fp64"] = batched64
+        line["plain_fp64_same_ensemble"] = plain_ens
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, seconds=args.cpu_seconds)
     print(json.dumps(line), flush=True)

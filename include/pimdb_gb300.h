@@ -205,6 +205,32 @@ int pimdb_propagate(pimdb_handle* h);
  *   f_last     = exterior spring force on bead P (springForceLastBead)
  * Any output may be NULL.  Requires a bosonic configuration. */
 int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first, double* f_last);
+/* The same exchange as a forward function and its adjoint, for callers that
+ * compose V_B with something else (BosonicExchangeBase's split into
+ * prepare / effectivePotential / exteriorSpringForce / primEstimator,
+ * include/bosonic_exchange/bosonic_exchange_base.h:16-54; Feldman-Hirshberg
+ * exchange only, PIMDB_ERR_CONFIG with the factorial one).
+ *
+ * pimdb_exchange_forward: prepare() + effectivePotential() on the current
+ * coordinates (quadratic_bosonic_exchange.cpp:30-132): cycle energies, the
+ * V and V_backwards recursions, and V_B = V[N] into *VB (may be NULL).  The
+ * arrays stay on the device for the two calls below.
+ *
+ * pimdb_exchange_adjoint: the vector-Jacobian product of V_B with an
+ * incoming cotangent vb_bar = dL/dV_B: x1_bar = vb_bar * dV_B/dx_1 and
+ * xP_bar = vb_bar * dV_B/dx_P, [particle][axis] (either may be NULL).  With
+ * vb_bar = 1 these are minus the exchange part of springForceFirstBead /
+ * springForceLastBead (:159-215), without their interior neighbour spring.
+ *
+ * pimdb_exchange_dbeta: primEstimator() (:250-279), -d(beta_ex V_B)/d(beta_ex)
+ * / P at fixed cycle energies, the bosonic term of the primitive energy.
+ *
+ * The adjoint and dbeta read the last forward evaluation; they return
+ * PIMDB_ERR_ARG when the coordinates changed since (a state set, a step). */
+int pimdb_exchange_forward(pimdb_handle* h, double* VB);
+int pimdb_exchange_adjoint(pimdb_handle* h, double vb_bar, double* x1_bar, double* xP_bar);
+int pimdb_exchange_dbeta(pimdb_handle* h, double* dbeta);
+
 /* Intermediate arrays of the last pimdb_exchange / force evaluation:
  * E (N(N+1)/2, the reference's E_kn order, getEnk(m,k) = E[m(m+1)/2 - k]),
  * V (N+1), V_backwards (N+1).  Any may be NULL.  PIMDB_ERR_CONFIG with the
@@ -373,6 +399,8 @@ int pimdb_batch_last_error(const pimdb_batch* b, char* buf, int len);
 /* Measures the FP64 fused-multiply-add throughput of the current device in
  * TFLOP/s (the roofline denominator of the FP64 kernels). */
 int pimdb_measure_fp64_peak(double* tflops);
+/* The same for FP32 fused multiply-adds (the mixed paths' pair forces). */
+int pimdb_measure_fp32_peak(double* tflops);
 
 /* Diagnostics of the hand-written FP64 functions against CUDA's own, on n
  * host values x (no counterpart in the reference).  out (8 n doubles, host):

@@ -30,8 +30,9 @@ EXPORTS = [
     "pimdb_set_state_device", "pimdb_get_state", "pimdb_get_state_device", "pimdb_set_step", "pimdb_get_step",
     "pimdb_step_io",
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
-    "pimdb_exchange_arrays", "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
-    "pimdb_measure_fp64_peak", "pimdb_math_check", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
+    "pimdb_exchange_arrays", "pimdb_exchange_forward", "pimdb_exchange_adjoint", "pimdb_exchange_dbeta",
+    "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
+    "pimdb_measure_fp64_peak", "pimdb_measure_fp32_peak", "pimdb_math_check", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
     "pimdb_propagate", "pimdb_compute_observables", "pimdb_potential_energy", "pimdb_local_energy", "pimdb_batch_create", "pimdb_batch_destroy", "pimdb_batch_size", "pimdb_batch_set_states",
     "pimdb_batch_get_states", "pimdb_batch_set_step", "pimdb_batch_get_step", "pimdb_batch_compute_forces",
     "pimdb_batch_step", "pimdb_batch_step_async", "pimdb_batch_synchronize", "pimdb_batch_exchange",
@@ -98,10 +99,14 @@ def lib():
             "pimdb_synchronize": ([vp], C.c_int),
             "pimdb_exchange": ([vp, vp, vp, vp], C.c_int),
             "pimdb_exchange_arrays": ([vp, vp, vp, vp], C.c_int),
+            "pimdb_exchange_forward": ([vp, vp], C.c_int),
+            "pimdb_exchange_adjoint": ([vp, C.c_double, vp, vp], C.c_int),
+            "pimdb_exchange_dbeta": ([vp, vp], C.c_int),
             "pimdb_last_error": ([vp, C.c_char_p, C.c_int], C.c_int),
             "pimdb_status_string": ([C.c_int], C.c_char_p),
             "pimdb_profile": ([vp, C.c_int, vp, vp, vp], C.c_int),
             "pimdb_measure_fp64_peak": ([vp], C.c_int),
+            "pimdb_measure_fp32_peak": ([vp], C.c_int),
             "pimdb_math_check": ([vp, C.c_int, vp], C.c_int),
             "pimdb_set_option": ([vp, C.c_char_p, C.c_int], C.c_int),
             "pimdb_thermostat_step": ([vp, C.c_int], C.c_int),
@@ -161,6 +166,13 @@ def _check(st: int, h=None, batch=False):
     if st == ERR_NONFINITE_VB:
         raise ExchangeOverflowError(msg)
     raise PimdbError(msg)
+
+
+def measure_fp32_peak() -> float:
+    """FP32 FMA throughput of the current device, TFLOP/s."""
+    v = C.c_double()
+    _check(lib().pimdb_measure_fp32_peak(C.byref(v)))
+    return v.value
 
 
 def measure_fp64_peak() -> float:
@@ -362,6 +374,26 @@ class System:
         out = np.zeros(len(it))
         _check(lib().pimdb_local_energy(self._h, len(it), _ptr(it), _ptr(out)), self._h)
         return out
+
+    def exchange_forward(self) -> float:
+        """V_B of the current coordinates (the forward half of the exchange)."""
+        v = C.c_double()
+        _check(lib().pimdb_exchange_forward(self._h, C.byref(v)), self._h)
+        return v.value
+
+    def exchange_adjoint(self, vb_bar: float = 1.0):
+        """(vb_bar dV_B/dx_1, vb_bar dV_B/dx_P), each [particle][axis], from
+        the last exchange_forward."""
+        N, D = self.cfg.natoms, self.cfg.ndim
+        x1, xP = np.zeros((N, D)), np.zeros((N, D))
+        _check(lib().pimdb_exchange_adjoint(self._h, float(vb_bar), _ptr(x1), _ptr(xP)), self._h)
+        return x1, xP
+
+    def exchange_dbeta(self) -> float:
+        """primEstimator of the last exchange_forward."""
+        v = C.c_double()
+        _check(lib().pimdb_exchange_dbeta(self._h, C.byref(v)), self._h)
+        return v.value
 
     def exchange_arrays(self):
         N = self.cfg.natoms

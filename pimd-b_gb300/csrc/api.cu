@@ -37,6 +37,9 @@ struct pimdb_handle {
     double* d_part = nullptr;  // pair-tile partial sums (Newton's third law path)
     int* d_err = nullptr;
     long long step = 0;
+    // coordinate generation: advanced by every call that can change x; the
+    // split exchange's adjoint and dbeta need the forward of the current one
+    long long xgen = 0, fwd_gen = -1;
     int red_last = 0;         // buffer holding the pending COM partials
     int nred_last = 0;
     bool com_pending = false;
@@ -603,6 +606,7 @@ static void state_out_launch(pimdb_handle* h, double* ox, double* op, double* of
 // The state in, enqueued: one kernel (pack, zero the forces), reading
 // page-locked host arrays directly or the staging buffer after a copy.
 static int enqueue_state_in(pimdb_handle* h, const double* x, const double* p, cudaMemcpyKind kind) {
+    if (h && x) ++h->xgen;
     complete_pending(h);
     const Sys& s = h->s;
     const size_t n = (size_t)s.P * s.N * h->D;
@@ -999,6 +1003,7 @@ static bool graph_steps(pimdb_handle* h, int nsteps) {
 
 extern "C" int pimdb_step_async(pimdb_handle* h, int nsteps) {
     if (!h || nsteps < 0) return PIMDB_ERR_ARG;
+    if (nsteps > 0) ++h->xgen;
     if (!graph_steps(h, nsteps)) {
         enqueue_steps(h, nsteps);
         h->dstep_valid = false;
@@ -1027,6 +1032,7 @@ extern "C" int pimdb_step(pimdb_handle* h, int nsteps) {
 static int graph_io(pimdb_handle* h, const double* xi, const double* pi, int nsteps, double* xo, double* po,
                     double* fo) {
     if (!h->opt_graph || h->graph_broken || h->profile || !h->warm || nsteps < 1) return -1;
+    ++h->xgen;
     const void* host[5] = {xi, pi, xo, po, fo};
     pimdb_handle::IoKey key{};
     key.nsteps = nsteps;
@@ -1157,6 +1163,67 @@ extern "C" int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first,
                 for (int a = 0; a < D; ++a) out[(size_t)i * D + a] = fx[((size_t)side * D + a) * s.ld + i];
         }
     }
+    return PIMDB_OK;
+}
+
+static int fh_exchange_only(pimdb_handle* h, const char* what) {
+    if (!h->s.bosonic || h->factorial)
+        return fail(h, PIMDB_ERR_CONFIG,
+                    std::string(what) + " needs the Feldman-Hirshberg exchange (bosonic, nbeads > 1)");
+    return PIMDB_OK;
+}
+
+static int exchange_forward_current(pimdb_handle* h, const char* what) {
+    if (h->fwd_gen != h->xgen)
+        return fail(h, PIMDB_ERR_ARG,
+                    std::string(what) + " needs pimdb_exchange_forward on the current coordinates first");
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_exchange_forward(pimdb_handle* h, double* VB) {
+    if (!h) return PIMDB_ERR_ARG;
+    int st = fh_exchange_only(h, "pimdb_exchange_forward");
+    if (st != PIMDB_OK) return st;
+    complete_pending(h);
+    exchange_front(h, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    st = check_err_word(h);
+    if (st != PIMDB_OK) return st;
+    h->fwd_gen = h->xgen;
+    if (VB) CUDA_TRY(h, cudaMemcpy(VB, h->s.V + h->s.N, sizeof(double), cudaMemcpyDeviceToHost));
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_exchange_adjoint(pimdb_handle* h, double vb_bar, double* x1_bar, double* xP_bar) {
+    if (!h) return PIMDB_ERR_ARG;
+    int st = fh_exchange_only(h, "pimdb_exchange_adjoint");
+    if (st == PIMDB_OK) st = exchange_forward_current(h, "pimdb_exchange_adjoint");
+    if (st != PIMDB_OK) return st;
+    const Sys& s = h->s;
+    const int D = h->D;
+    launch(h, PIMDB_K_EXCH_FORCES, [&] { launch_exchange_adjoint(s, D, vb_bar, h->stream); });
+    CUDA_TRY(h, cudaGetLastError());
+    std::vector<double> fx((size_t)2 * D * s.ld);
+    CUDA_TRY(h, cudaMemcpyAsync(fx.data(), s.fx, fx.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    for (int side = 0; side < 2; ++side) {
+        double* out = side == 0 ? x1_bar : xP_bar;
+        if (!out) continue;
+        for (int i = 0; i < s.N; ++i)
+            for (int a = 0; a < D; ++a) out[(size_t)i * D + a] = fx[((size_t)side * D + a) * s.ld + i];
+    }
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_exchange_dbeta(pimdb_handle* h, double* dbeta) {
+    if (!h || !dbeta) return fail(h, PIMDB_ERR_ARG, "NULL argument");
+    int st = fh_exchange_only(h, "pimdb_exchange_dbeta");
+    if (st == PIMDB_OK) st = exchange_forward_current(h, "pimdb_exchange_dbeta");
+    if (st != PIMDB_OK) return st;
+    exchange_scalars(h, false, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaMemcpyAsync(dbeta, h->s.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return PIMDB_OK;
 }
 
@@ -1336,6 +1403,19 @@ __global__ void k_fp64_fma_probe(double* out, int iters, double a, double b) {
     if (s == 1.2345) out[0] = s;  // keeps the chains alive
 }
 
+// FP32 pipe throughput probe: the same shape with float chains (the mixed
+// paths' pair forces run on this pipe).
+__global__ void k_fp32_fma_probe(float* out, int iters, float a, float b) {
+    float r0 = threadIdx.x * 1e-6f, r1 = r0 + 1e-6f, r2 = r0 + 2e-6f, r3 = r0 + 3e-6f;
+    float r4 = r0 + 4e-6f, r5 = r0 + 5e-6f, r6 = r0 + 6e-6f, r7 = r0 + 7e-6f;
+    for (int i = 0; i < iters; ++i) {
+        r0 = fmaf(r0, a, b); r1 = fmaf(r1, a, b); r2 = fmaf(r2, a, b); r3 = fmaf(r3, a, b);
+        r4 = fmaf(r4, a, b); r5 = fmaf(r5, a, b); r6 = fmaf(r6, a, b); r7 = fmaf(r7, a, b);
+    }
+    const float s = r0 + r1 + r2 + r3 + r4 + r5 + r6 + r7;
+    if (s == 1.2345f) out[0] = s;
+}
+
 extern "C" int pimdb_math_check(const double* x, int n, double* out) {
     if (!x || !out || n < 0) return PIMDB_ERR_ARG;
     if (n == 0) return PIMDB_OK;
@@ -1367,6 +1447,34 @@ extern "C" int pimdb_measure_fp64_peak(double* tflops) {
     cudaEventRecord(e0);
     const int reps = 5;
     for (int r = 0; r < reps; ++r) k_fp64_fma_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    CUDA_TRY(nullptr, cudaGetLastError());
+    const double flops = 2.0 * 8.0 * iters * (double)threads * blocks * reps;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_measure_fp32_peak(double* tflops) {
+    if (!tflops) return PIMDB_ERR_ARG;
+    int dev = 0, sms = 0;
+    CUDA_TRY(nullptr, cudaGetDevice(&dev));
+    CUDA_TRY(nullptr, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    float* out = nullptr;
+    CUDA_TRY(nullptr, cudaMalloc((void**)&out, sizeof(float)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8, threads = 256, iters = 65536;
+    k_fp32_fma_probe<<<blocks, threads>>>(out, iters, 0.9999f, 1e-7f);
+    cudaEventRecord(e0);
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r) k_fp32_fma_probe<<<blocks, threads>>>(out, iters, 0.9999f, 1e-7f);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -1435,6 +1543,7 @@ extern "C" int pimdb_zero_momentum(pimdb_handle* h) {
 extern "C" int pimdb_propagate(pimdb_handle* h) {
     if (!h) return PIMDB_ERR_ARG;
     complete_pending(h);
+    ++h->xgen;
     if (h->cfg.propagator == PIMDB_PROP_NORMAL_MODES) {
         h->modes_valid = false;
         launch(h, PIMDB_K_NM_PROPAGATE, [&] {

@@ -359,11 +359,11 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
 
 // Exterior spring forces: one warp per row (bead P) or column (bead 1).
 template <int D>
-__global__ void k_exch_forces(Sys s, int accumulate) {
+__global__ void k_exch_forces(Sys s, int accumulate, int adjoint, double vb_bar) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (w >= 2 * s.N) return;
-    exch_force_row<D>(s, w, lane, accumulate);
+    exch_force_row<D>(s, w, lane, accumulate, nullptr, adjoint, vb_bar);
 }
 
 __global__ void k_exch_estimators(Sys s, int nbeads) {
@@ -496,13 +496,21 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
     return n;
 }
 
-void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st) {
+static void exchange_rows(const Sys& s, int D, int accumulate, int adjoint, double vb_bar, cudaStream_t st) {
     exchange_carveouts();
     const int warps = 2;  // small blocks: the 2N rows spread over every SM
     dim3 grid((2 * s.N + warps - 1) / warps);
-    if (D == 1) k_exch_forces<1><<<grid, warps * 32, 0, st>>>(s, accumulate);
-    else if (D == 2) k_exch_forces<2><<<grid, warps * 32, 0, st>>>(s, accumulate);
-    else k_exch_forces<3><<<grid, warps * 32, 0, st>>>(s, accumulate);
+    if (D == 1) k_exch_forces<1><<<grid, warps * 32, 0, st>>>(s, accumulate, adjoint, vb_bar);
+    else if (D == 2) k_exch_forces<2><<<grid, warps * 32, 0, st>>>(s, accumulate, adjoint, vb_bar);
+    else k_exch_forces<3><<<grid, warps * 32, 0, st>>>(s, accumulate, adjoint, vb_bar);
+}
+
+void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st) {
+    exchange_rows(s, D, accumulate, 0, 0.0, st);
+}
+
+void launch_exchange_adjoint(const Sys& s, int D, double vb_bar, cudaStream_t st) {
+    exchange_rows(s, D, 0, 1, vb_bar, st);
 }
 
 void launch_exchange_estimators(const Sys& s, cudaStream_t st) {

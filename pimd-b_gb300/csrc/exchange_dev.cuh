@@ -430,7 +430,11 @@ __device__ inline void solve_finish(const Sys& s, int extrapolate = 0) {
 // `xs` (optional): the positions of beads 1 and P staged in shared memory,
 // xs[(side * D + a) * N + i] with side 0 = bead 1, 1 = bead P.
 template <int D>
-__device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumulate, const double* xs = nullptr) {
+// With `adjoint` set, the row writes the cotangent of the exchange potential
+// instead of the force: fx = vb_bar * dV_B/dx = -vb_bar * kappa * sum, with
+// neither the interior neighbour spring nor the accumulation into f.
+__device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumulate, const double* xs = nullptr,
+                                      int adjoint = 0, double vb_bar = 0.0) {
     const int N = s.N;
     const double beta = s.beta_ex;
     const double VN = s.V[N];
@@ -492,7 +496,12 @@ __device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumul
     }
 #pragma unroll
     for (int a = 0; a < D; ++a) sum[a] = warp_sum(sum[a]);
-    if (lane == 0) {
+    if (lane == 0 && adjoint) {
+        const int side = (bead == first) ? 0 : 1;
+        const double c = -vb_bar * s.kappa;
+#pragma unroll
+        for (int a = 0; a < D; ++a) s.fx[((size_t)side * D + a) * s.ld + l] = c * sum[a];
+    } else if (lane == 0) {
         const int side = (bead == first) ? 0 : 1;
 #pragma unroll
         for (int a = 0; a < D; ++a) {

@@ -12,8 +12,13 @@ own initial states (bench.initial_state), against the oracle.
   stratified sample of replicas.
 
 Tolerances as in the other parity tests: 1e-10 relative per bead for FP64
-forces and exchange results, 1e-9 per bead for trajectories, 1e-6
-norm-relative force error for mixed precision.  Besides the initial states
+forces, V_B and the V / V_backwards arrays, 1e-9 per bead for trajectories,
+1e-6 norm-relative force error for mixed precision.  The exterior spring
+forces alone (the exchange part of beads 1 and P) are compared within 1e-10
+of their largest component or within what the measured difference of V and
+V_backwards implies through the formula's conditioning, whichever is
+larger: at N = 1024 and 4096 a few units of rounding in V move them by 1e-10
+to 1e-9 (exterior_force_conditioning).  Besides the initial states
 (particles near the reference's grid placement), each large system is also
 checked on a hot liquid: the state the GPU reaches after a run from random
 placement, where ring polymers have spread, many pairs sit inside the Aziz
@@ -56,14 +61,72 @@ def gpu_forces(cfg, x, options=None):
     return f, ex, arr
 
 
-def check_exchange(ex, arr, ref):
+def exterior_forces(s, x, E, V, Vb):
+    """The reference's exterior spring forces on beads 1 and P
+    (quadratic_bosonic_exchange.cpp:142-215) from given E, V, V_backwards,
+    vectorised."""
+    N, P, beta, k = s.natoms, s.nbeads, s.beta_ex, s.spring_constant
+    x1, xP = x[0], x[P - 1]
+    VN = V[N]
+
+    def mi(d):
+        return d - s.size * np.floor(d / s.size + 0.5) if s.pbc else d
+
+    tri = lambda m: m * (m + 1) // 2
+    f1, fP = mi(x[1 % P] - x1), mi(x[(P - 2 + P) % P] - xP)
+    for l in range(N):
+        q = np.arange(l, N)
+        pr = np.exp(-beta * (V[l] + E[tri(q) + l] + Vb[q + 1] - VN)) / (q + 1)
+        f1[l] += (pr[:, None] * mi(xP[q] - x1[l])).sum(0)
+        n = np.arange(0, l + 1)
+        pr = np.exp(-beta * (V[n] + E[tri(l) + n] + Vb[l + 1] - VN)) / (l + 1)
+        fP[l] += (pr[:, None] * mi(x1[n] - xP[l])).sum(0)
+        if l >= 1:  # the direct links l-1 -> l and l -> l+1
+            f1[l] += (1.0 - np.exp(-beta * (V[l] + Vb[l] - VN))) * mi(xP[l - 1] - x1[l])
+        if l + 1 < N:
+            fP[l] += (1.0 - np.exp(-beta * (V[l + 1] + Vb[l + 1] - VN))) * mi(x1[l + 1] - xP[l])
+    return k * f1, k * fP
+
+
+def exterior_force_conditioning(s, x, ref, dv, seed=0):
+    """How far the exterior spring forces move, relative to their largest
+    component, when the oracle's own V and V_backwards are perturbed at
+    random by `dv` (absolute): the agreement two FP64 evaluations of the
+    recursion that differ by that much can reach.  The direct-link
+    probabilities 1 - exp(-beta (V[l] + V_b[l] - V[N])) difference numbers
+    of size V_B, so their rounding is scaled by beta_ex V_B (about 3e4 at
+    N = 4096, T = 1 K)."""
+    rng = np.random.default_rng(seed)
+    f1, fP = exterior_forces(s, x, ref["E"], ref["V"], ref["Vb"])
+    g1, gP = exterior_forces(s, x, ref["E"], ref["V"] + dv * rng.standard_normal(ref["V"].shape),
+                             ref["Vb"] + dv * rng.standard_normal(ref["Vb"].shape))
+    assert np.abs(f1 - ref["f1"]).max() <= 1e-12 * np.abs(ref["f1"]).max()  # the restatement itself
+    return max(np.abs(g1 - f1).max() / np.abs(f1).max(), np.abs(gP - fP).max() / np.abs(fP).max())
+
+
+def check_exchange(ex, arr, ref, s=None, x=None):
+    """V_B, primEstimator and E, V, V_backwards within the FP64 tolerances;
+    the exterior spring forces within 1e-10 of their largest component, or,
+    where the recursion's conditioning allows less (s and x given), within
+    twice the spread measured by exterior_force_conditioning."""
     assert abs(ex["VB"] - ref["VB"]) <= FP64_TOL * abs(ref["VB"])
     assert abs(ex["prim"] - ref["prim"]) <= 1e-9 * abs(ref["prim"]) + 1e-300
-    for key in ("f1", "fP"):
-        assert np.abs(ex[key] - ref[key]).max() <= FP64_TOL * np.abs(ref[key]).max(), key
     np.testing.assert_allclose(arr["E"], ref["E"], rtol=1e-12, atol=1e-14 * np.abs(ref["E"]).max())
     np.testing.assert_allclose(arr["V"], ref["V"], rtol=FP64_TOL, atol=1e-14 * np.abs(ref["V"]).max())
     np.testing.assert_allclose(arr["Vb"][1:], ref["Vb"][1:], rtol=FP64_TOL, atol=1e-14 * np.abs(ref["Vb"]).max())
+    tol = FP64_TOL
+    if s is not None:
+        # the GPU's V and V_backwards against the oracle's (at least 4 units
+        # of rounding), carried to the forces through the formula's
+        # conditioning, with a factor 3 for the random sampling of it
+        n = s.natoms
+        dv = max(float(np.max(np.abs(arr["V"][1:] - ref["V"][1:]))), float(np.max(np.abs(arr["Vb"][1:n] -
+                                                                                          ref["Vb"][1:n]))),
+                 2.0 * np.finfo(float).eps * abs(ref["VB"]))
+        tol = max(tol, 3.0 * exterior_force_conditioning(s, x, ref, dv))
+    for key in ("f1", "fP"):
+        err = np.abs(ex[key] - ref[key]).max() / np.abs(ref[key]).max()
+        assert err <= tol, (key, err, tol)
 
 
 def hot_state(w, steps, placement="separated", min_sep_ang=2.2, seed=777):
@@ -160,7 +223,7 @@ def test_large_system_forces_and_exchange(state, request):
     ref = O.exchange(s, x)
     f, ex, arr = gpu_forces(bench.workload_config(W5, "fp64"), x)
     assert rel_per_bead(f, want["f"]) < FP64_TOL
-    check_exchange(ex, arr, ref)
+    check_exchange(ex, arr, ref, s, x)
     fm, exm, _ = gpu_forces(bench.workload_config(W5, "mixed"), x)
     err = [np.linalg.norm(fm[b] - want["f"][b]) / np.linalg.norm(want["f"][b]) for b in range(s.nbeads)]
     assert max(err) <= MIXED_TOL, max(err)
@@ -209,7 +272,7 @@ def test_other_benchmark_systems(name):
     ref = O.exchange(s, x)
     f, ex, arr = gpu_forces(bench.workload_config(w, "fp64"), x)
     assert rel_per_bead(f, want["f"]) < FP64_TOL
-    check_exchange(ex, arr, ref)
+    check_exchange(ex, arr, ref, s, x)
     fm, _, _ = gpu_forces(bench.workload_config(w, "mixed"), x)
     assert np.linalg.norm(fm - want["f"]) / np.linalg.norm(want["f"]) <= MIXED_TOL
     # 5 steps of the trajectory

@@ -21,8 +21,9 @@ the same recursion the Feldman-Hirshberg V_B evaluates configuration by
 configuration.  Then E = -(hbar omega / P) d ln Z_N / du, and the
 potential estimator averages to E/2 (d ln Z/d omega at fixed beta).
 
-The runs: N = 3, P = 16, beta hbar omega = 2, where exchange lowers E by 12%
-(5.255 against 5.899 hbar omega for distinguishable particles).  fixcom is
+The runs: N = 3, P = 8 or 16, beta hbar omega = 2, where exchange lowers E
+by 11-12% (P = 16: 5.255 against 5.899 hbar omega for distinguishable
+particles).  fixcom is
 off: removing the centre-of-mass momentum in a trap would freeze the centroid
 and bias the means.  Each mean is a 20-block average; a run must agree with
 the exact E within 4 standard errors, and that band must be narrow enough to
@@ -116,8 +117,8 @@ def test_oracle_langevin_means_match_exact_energy():
     check_means(obs[:, 0], obs[:, 1], 4, "oracle VV Langevin P=4")
 
 
-def _gpu_run(kw, nsteps=400000, every=20, seed=7):
-    s, cfg = trap_case(**kw)
+def _gpu_run(kw, nbeads, nsteps, every, seed=7):
+    s, cfg = trap_case(nbeads=nbeads, **kw)
     x, p = start(s, seed)
     kin, pot = [], []
     with pk.System(cfg) as g:
@@ -135,13 +136,15 @@ def _gpu_run(kw, nsteps=400000, every=20, seed=7):
 @pytest.mark.parametrize("kw", [dict(), dict(propagator="normal_modes", nmthermostat=True)],
                          ids=["vv_langevin", "nm_nm_langevin"])
 def test_gpu_thermostatted_means_match_exact_energy_and_oracle(kw):
-    s, kin, pot = _gpu_run(kw)
-    E, sE = check_means(kin, pot, 16, f"GPU {kw}")
+    # P = 8 halves the variance of the primitive kinetic estimator against
+    # P = 16; 800000 steps then give a standard error near 0.04 hbar omega
+    s, kin, pot = _gpu_run(kw, nbeads=8, nsteps=800000, every=40)
+    E, sE = check_means(kin, pot, 8, f"GPU {kw}")
     # and an independent oracle run of the same system (RanMars streams)
     x, p = start(s, 8)
     tr = O.Trajectory(s, x, p)
     tr.sample_run(303, 20000, 0)
-    obs = tr.sample_run(404, 400000, 20)
+    obs = tr.sample_run(404, 800000, 40)
     Eo, sEo = block_mean((obs[:, 0] + obs[:, 1]) / HW)
     assert abs(E - Eo) < NSIG * np.hypot(sE, sEo), (E, sE, Eo, sEo)
 
