@@ -25,6 +25,7 @@ CU_SOURCES = ["csrc/forces.cu", "csrc/exchange.cu", "csrc/factorial.cu", "csrc/i
 CPP_SOURCES = ["host/params.cpp"]
 CLI_SOURCES = ["host/pimdb_main.cpp"]
 HEADERS = ["csrc/common.cuh", "csrc/kernels.h", "csrc/config.h", "csrc/exchange_dev.cuh", "csrc/forces_dev.cuh",
+           "csrc/dfloat.cuh", "csrc/aziz_df.cuh",
            "host/units.hpp", "host/pimdb_host.hpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

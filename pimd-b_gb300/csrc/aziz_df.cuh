@@ -1,0 +1,45 @@
+// The Aziz HFDHE2 pair gradient outside its damping radius, evaluated in
+// double-float on the FP32 pipe (dfloat.cuh).  Parameters of the reference
+// (src/potentials/aziz.cpp:6-13); compiles for the host too, where the unit
+// test of this arithmetic checks it against an extended-precision form.
+#pragma once
+
+#include "dfloat.cuh"
+
+namespace pimdb {
+
+// Aziz HFDHE2 (reference aziz.cpp:6-13, aziz.h:25-34), bohr and hartree.
+struct Aziz {
+    static constexpr double rm = 5.60738, A = 0.5448504e6, eps = 3.42016E-5, alpha = 13.353384, D = 1.241314,
+                            C6 = 1.3732412, C8 = 0.4253785, C10 = 0.1781;
+};
+
+// ln(A alpha eps / r_m) of the Aziz parameters above (aziz.cpp:6-13).
+constexpr double kAzizLnK = 3.7927146577859623;
+
+// Gradient scale s(r) = (dV/dr) / r for r_s = r / r_m >= D (F = 1, dF = 0):
+//   s = r^-8 (c6 + c8 r^-2 + c10 r^-4) - exp(ln(A alpha eps / r_m) - alpha r / r_m) / r,
+// c_n = n C_n r_m^n eps, the same factoring as the FP64 far-field scale.
+// r2 = |r|^2 as a double-float.  Relative error a few 2^-48 (the attractive
+// and repulsive terms do not cancel beyond the damping radius).
+DF_HD dfl::df aziz_far_scale_df(dfl::df r2, const dfl::ExpTable& tbl) {
+    using namespace dfl;
+    constexpr double rm2 = Aziz::rm * Aziz::rm, rm6 = rm2 * rm2 * rm2, rm8 = rm6 * rm2, rm10 = rm8 * rm2;
+    constexpr double c6 = 6.0 * Aziz::C6 * Aziz::eps * rm6, c8 = 8.0 * Aziz::C8 * Aziz::eps * rm8,
+                     c10 = 10.0 * Aziz::C10 * Aziz::eps * rm10, ka = Aziz::alpha / Aziz::rm;
+    constexpr float c6h = (float)c6, c6l = (float)(c6 - (double)c6h);
+    constexpr float c8h = (float)c8, c8l = (float)(c8 - (double)c8h);
+    constexpr float c10h = (float)c10, c10l = (float)(c10 - (double)c10h);
+    constexpr float kah = (float)ka, kal = (float)(ka - (double)kah);
+    constexpr float lkh = (float)kAzizLnK, lkl = (float)(kAzizLnK - (double)lkh);
+    const df rinv = rsqrt(r2);
+    const df r = mul(r2, rinv);
+    const df arg = add(df{lkh, lkl}, neg(mul(df{kah, kal}, r)));
+    const df e = dfl::exp(arg, tbl);
+    const df ri2 = sqr(rinv);
+    const df ri4 = sqr(ri2);
+    const df pa = add_sloppy(mul(add_sloppy(mul(df{c10h, c10l}, ri2), df{c8h, c8l}), ri2), df{c6h, c6l});
+    return add(mul(sqr(ri4), pa), neg(mul(e, rinv)));
+}
+
+}  // namespace pimdb

@@ -293,8 +293,10 @@ __global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ 
 // result as k_pair_tiles up to rounding; the exact FP64 cutoff test is
 // applied in step 2.
 constexpr int kCompactWarps = 2;
-// gradient capacity per warp unless Sys::pair_cap says otherwise
-constexpr int kCompactDefaultCap = 608;
+// gradient capacity per warp unless Sys::pair_cap says otherwise (the
+// double-float path keeps two more small arrays per warp; 544 entries let
+// five blocks share an SM, as 608 did before them)
+constexpr int kCompactDefaultCap = 544;
 // entries of the damping-radius list evaluated per pass
 constexpr int kCompactNear = 256;
 
@@ -304,10 +306,14 @@ constexpr int kCompactNear = 256;
 template <int D>
 struct CompactSmem {
     double xi[kTile][D], xj[kTile][D];   // wrapped into the box under PBC
-    float xif[kTile][D], xjf[kTile][D];  // FP32 hi parts
+    float xif[kTile][D], xjf[kTile][D];  // FP32 hi parts (nearest floats)
+    float xil[kTile][D], xjl[kTile][D];  // double-float path: x - hi, the low words
     union {
         double xjs[2][kTile][D];         // FP64 path under PBC: xj - L, xj + L
         float lo[2][kTile][D];           // mixed path: x - hi of i, of j
+        struct {
+            float h[2][kTile][D], l[2][kTile][D];
+        } img;                           // double-float path under PBC: xj - L, xj + L
     } u;
     unsigned mask[kTile];                // lane i: bit j for each entry (i, j)
     int off[kTile];                      // lane i's first entry
@@ -333,10 +339,19 @@ __device__ __forceinline__ double min_image_wrapped(double d, double L, long lon
 // other potentials) are evaluated in FP32 from hi/lo separations; entries
 // inside it stay FP64, where the repulsive and attractive terms nearly
 // cancel and FP32 would lose the difference.  Sums are FP64 either way.
-template <int D, bool kMixed>
+//
+// kDf (FP64 path with the Aziz potential): the far entries are evaluated in
+// double-float on the FP32 pipe (aziz_far_scale_df, about 2^-44 relative),
+// their gradients kept as double-floats and every sum formed in
+// double-float; the entries inside the damping radius, within 1e-6 L of the
+// half-box edge or within 1e-5 of the cutoff (where the in/out decision must
+// be the FP64 one) take the exact FP64 path as before.
+template <int D, bool kMixed, bool kDf>
 __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ part, int T, int b, int w,
                                              CompactSmem<D>& sm, double (*g)[D], int cap, const double* tbl,
-                                             int lane) {
+                                             const dfl::ExpTable* etbl, int lane) {
+    using dfl::df;
+    auto gd = reinterpret_cast<float2 (*)[D]>(g);  // kDf: gradient entries as (hi, lo)
     int it = 0, rem = w;  // row it holds the T - it tile pairs (it, it..T-1)
     while (rem >= T - it) {
         rem -= T - it;
@@ -346,6 +361,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
     const bool diag = it == jt;
     const int i = it * kTile + lane, j = jt * kTile + lane;
     float xif[D], xjf[D];
+    const df Ldf{(float)s.L, (float)(s.L - f32_to_f64((float)s.L))};
 #pragma unroll
     for (int a = 0; a < D; ++a) {
         double xv = i < s.N ? s.x[idx<D>(s, b, a, i)] : 0.0;
@@ -363,6 +379,19 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         if (kMixed) {
             sm.u.lo[0][lane][a] = (float)(xv - (double)xif[a]);
             sm.u.lo[1][lane][a] = (float)(yv - (double)xjf[a]);
+        } else if (kDf) {
+            // x = hi + lo exactly in double, lo rounded to float: 48 bits
+            sm.xil[lane][a] = (float)(xv - f32_to_f64(xif[a]));
+            const float yl = (float)(yv - f32_to_f64(xjf[a]));
+            sm.xjl[lane][a] = yl;
+            if (s.pbc) {
+                const df m = dfl::add(df{xjf[a], yl}, dfl::neg(Ldf));
+                const df q = dfl::add(df{xjf[a], yl}, Ldf);
+                sm.u.img.h[0][lane][a] = m.hi;
+                sm.u.img.l[0][lane][a] = m.lo;
+                sm.u.img.h[1][lane][a] = q.hi;
+                sm.u.img.l[1][lane][a] = q.lo;
+            }
         } else if (s.pbc) {
             sm.u.xjs[0][lane][a] = yv - s.L;
             sm.u.xjs[1][lane][a] = yv + s.L;
@@ -382,6 +411,9 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
     // from the FP64 one, so the entry takes the exact path (with the
     // damping-radius entries).  Bound on the FP32 error: 2.5 2^-24 L.
     const float amb = 1e-6f * Lf;
+    // the double-float path applies no cutoff test: entries within 1e-5 of
+    // the cutoff (far above the FP32 error of r2) take the exact FP64 path
+    const float shell2f = (float)(cut * cut) * (1.0f - 1e-5f);
 #pragma unroll 4
     for (int st = first; st <= lastS; ++st) {
         const int jl = (lane + st) & 31;
@@ -398,7 +430,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         }
         const bool in = ivalid && jl < nj && (!diag || st < 16 || lane < 16) && r2 <= cut2f;
         mask |= (unsigned)in << jl;
-        nmask |= (unsigned)(in && (r2 < near2f || (aziz && edge))) << jl;
+        nmask |= (unsigned)(in && (r2 < near2f || (aziz && edge) || (kDf && r2 >= shell2f))) << jl;
     }
     // 2. i-major layout: offsets by a warp scan of the counts
     const int icnt = __popc(mask);
@@ -462,15 +494,49 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         }
         return r2;
     };
-    double ai[D], aj[D];
+    // The double-float far path's separation: the image the FP32 screen
+    // chose (xj - L, xj or xj + L as double-floats), one double-float
+    // subtraction per axis.
+    auto separation_df = [&](int f, df* r) {
+        const int e = sm.fe[f], il = (e >> 5) & 31, jl = e & 31;
+        df r2{0.0f, 0.0f};
 #pragma unroll
-    for (int a = 0; a < D; ++a) ai[a] = aj[a] = 0.0;
+        for (int a = 0; a < D; ++a) {
+            df xjv{sm.xjf[jl][a], sm.xjl[jl][a]};
+            if (s.pbc) {
+                const float dd = sm.xif[il][a] - sm.xjf[jl][a];
+                if (fabsf(dd) > halfLf) {
+                    const int side = dd > 0.0f ? 1 : 0;
+                    xjv = df{sm.u.img.h[side][jl][a], sm.u.img.l[side][jl][a]};
+                }
+            }
+            const df d = dfl::add_sloppy(df{sm.xif[il][a], sm.xil[il][a]}, dfl::neg(xjv));
+            r[a] = d;
+            r2 = a == 0 ? dfl::sqr(d) : dfl::add_sloppy(r2, dfl::sqr(d));
+        }
+        return r2;
+    };
+    double ai[D], aj[D];
+    df aid[D], ajd[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        ai[a] = aj[a] = 0.0;
+        aid[a] = ajd[a] = df{0.0f, 0.0f};
+    }
     const unsigned lt = (1u << lane) - 1u;
     for (int c0 = 0; c0 < total; c0 += cap) {
         const int cend = min(total, c0 + cap), cn = cend - c0;
         auto store = [&](int f, double sc, const double* r) {
 #pragma unroll
-            for (int a = 0; a < D; ++a) g[f - c0][a] = sc * r[a];  // grad V(r_i - r_j)
+            for (int a = 0; a < D; ++a) {
+                const double v = sc * r[a];  // grad V(r_i - r_j)
+                if (kDf) {
+                    const float h = (float)v;
+                    gd[f - c0][a] = make_float2(h, (float)(v - f32_to_f64(h)));
+                } else {
+                    g[f - c0][a] = v;
+                }
+            }
         };
         // every entry of the chunk on the branch-free path
         if (kMixed) {
@@ -490,6 +556,26 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                 const float sc = r2 < cut2f32 ? pair_scale<float>(s.int_kind, r2, paramf) : 0.0f;
 #pragma unroll
                 for (int a = 0; a < D; ++a) g[k][a] = f32_to_f64(sc * r[a]);
+            }
+        } else if (kDf) {
+            // every entry on the double-float far path, two independent ones
+            // per lane and iteration; the entries marked in the screen are
+            // redone below on the exact FP64 path
+            for (int k = lane; k < cn; k += 64) {
+                const bool two = k + 32 < cn;
+                const int f0 = c0 + k, f1 = two ? f0 + 32 : f0;
+                df r0[D], r1[D];
+                const df q0 = separation_df(f0, r0), q1 = separation_df(f1, r1);
+                const df sc0 = aziz_far_scale_df(q0, *etbl), sc1 = aziz_far_scale_df(q1, *etbl);
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    const df v0 = dfl::mul(sc0, r0[a]);
+                    gd[f0 - c0][a] = make_float2(v0.hi, v0.lo);
+                    if (two) {
+                        const df v1 = dfl::mul(sc1, r1[a]);
+                        gd[f1 - c0][a] = make_float2(v1.hi, v1.lo);
+                    }
+                }
             }
         } else if (aziz) {
             // two independent entries per lane and iteration; entries inside
@@ -539,16 +625,37 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         //    side down its column in ascending i (chunk by chunk)
         for (int k = max(off, c0); k < min(off + icnt, cend); ++k)
 #pragma unroll
-            for (int a = 0; a < D; ++a) ai[a] -= g[k - c0][a];
+            for (int a = 0; a < D; ++a) {
+                if (kDf) {
+                    const float2 v = gd[k - c0][a];
+                    aid[a] = dfl::add_sloppy(aid[a], df{-v.x, -v.y});
+                } else {
+                    ai[a] -= g[k - c0][a];
+                }
+            }
         for (unsigned cm = col; cm; cm &= cm - 1u) {
             const int ii = __ffs(cm) - 1;
             const int f = sm.off[ii] + __popc(sm.mask[ii] & lt);
             if (cn == total || (f >= c0 && f < cend)) {
 #pragma unroll
-                for (int a = 0; a < D; ++a) aj[a] += g[f - c0][a];
+                for (int a = 0; a < D; ++a) {
+                    if (kDf) {
+                        const float2 v = gd[f - c0][a];
+                        ajd[a] = dfl::add_sloppy(ajd[a], df{v.x, v.y});
+                    } else {
+                        aj[a] += g[f - c0][a];
+                    }
+                }
             }
         }
         __syncwarp();  // the next chunk overwrites g
+    }
+    if (kDf) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            ai[a] = f32_to_f64(aid[a].hi) + f32_to_f64(aid[a].lo);
+            aj[a] = f32_to_f64(ajd[a].hi) + f32_to_f64(ajd[a].lo);
+        }
     }
     const size_t base_b = (size_t)b * T;
     if (diag) {
@@ -575,12 +682,23 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
 // passes (FP32 estimate, FP64 triangular solve) that run beside this kernel,
 // whose sequential chains would otherwise share the FP64 pipe with the
 // pair warps.
-template <int D, bool kMixed>
+template <int D, bool kMixed, bool kDf>
 __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s, double* __restrict__ part, int T,
                                                                           int npairs, int* ctr, int cap, int nsm) {
     extern __shared__ __align__(16) unsigned char csm_raw[];
     __shared__ double tbl[256];
-    for (int j = threadIdx.x; j < 256; j += blockDim.x) tbl[j] = kExp2Table256[j];
+    __shared__ dfl::ExpTable etbl;
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) {
+        const double v = kExp2Table256[j];
+        tbl[j] = v;
+        if (kDf) {  // 2^(j/256) as a double-float (47 bits or more; bit patterns, no FP64 work)
+            float h, l;
+            split_f32(v, h, l);
+            const dfl::df n = dfl::fast_two_sum(h, l);
+            etbl.hi[j] = n.hi;
+            etbl.lo[j] = n.lo;
+        }
+    }
     __syncthreads();
     unsigned char* wbase = csm_raw + (threadIdx.x >> 5) * compact_warp_bytes<D>(cap);
     CompactSmem<D>& sm = *reinterpret_cast<CompactSmem<D>*>(wbase);
@@ -596,7 +714,7 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= ntask) break;
         const int b = task / npairs;
-        compact_tile<D, kMixed>(s, part, T, b, task - b * npairs, sm, g, cap, tbl, lane);
+        compact_tile<D, kMixed, kDf>(s, part, T, b, task - b * npairs, sm, g, cap, tbl, &etbl, lane);
         __syncwarp();
     }
     if (lane == 0) {
@@ -961,15 +1079,19 @@ static void tiles_launch(const Sys& s, int mixed, int write_phys, double* part, 
             struct Occ {
                 int resident, cap, sms;
             };
-            static Occ occ[64][2] = {};
+            static Occ occ[64][3] = {};
             static std::mutex occ_mu;
-            auto kern = mixed ? k_pair_tiles_compact<D, true> : k_pair_tiles_compact<D, false>;
+            // FP64 with the Aziz potential: the double-float far path
+            const bool dfp = !mixed && s.int_kind == POT_AZIZ;
+            auto kern = mixed ? k_pair_tiles_compact<D, true, false>
+                              : (dfp ? k_pair_tiles_compact<D, false, true> : k_pair_tiles_compact<D, false, false>);
+            const int variant = mixed ? 1 : (dfp ? 2 : 0);
             int dev = 0;
             cudaGetDevice(&dev);
             Occ o{};
             {
                 std::lock_guard<std::mutex> lock(occ_mu);
-                Occ& slot = occ[(dev >= 0 && dev < 64) ? dev : 0][mixed];
+                Occ& slot = occ[(dev >= 0 && dev < 64) ? dev : 0][variant];
                 if (slot.cap != cap || dev < 0 || dev >= 64) {
                     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(compact_warp_bytes<D>(kCompactMaxCap) * kCompactWarps));

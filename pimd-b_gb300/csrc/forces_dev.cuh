@@ -4,15 +4,10 @@
 // (src/potentials/{harmonic,aziz,dipole,double_well,cosine}.cpp).
 #pragma once
 
+#include "aziz_df.cuh"
 #include "common.cuh"
 
 namespace pimdb {
-
-// Aziz HFDHE2 (reference aziz.cpp:6-13, aziz.h:25-34).
-struct Aziz {
-    static constexpr double rm = 5.60738, A = 0.5448504e6, eps = 3.42016E-5, alpha = 13.353384, D = 1.241314,
-                            C6 = 1.3732412, C8 = 0.4253785, C10 = 0.1781;
-};
 
 // exp(x) by Tang's table-driven method (P. T. P. Tang, "Table-driven
 // implementation of the exponential function in IEEE floating-point
@@ -206,9 +201,6 @@ template <>
 __device__ __forceinline__ double pair_scale<double>(int kind, double r2, double param) {
     return pair_scale_d<false>(kind, r2, param, nullptr);
 }
-
-// ln(A alpha eps / r_m) of the Aziz parameters above (aziz.cpp:6-13).
-constexpr double kAzizLnK = 3.7927146577859623;
 
 // Aziz gradient scale outside the damping radius (r_s >= D, where F = 1 and
 // dF = 0): (eps/r_m) [-A alpha exp(-alpha r_s) + ix^7 (6 C6 + 8 C8 ix^2 +

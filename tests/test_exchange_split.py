@@ -64,7 +64,7 @@ def test_forward_adjoint_dbeta_match_oracle(name):
     assert np.abs(x1c + 2.5 * x1b).max() <= 1e-14 * scale
     assert np.abs(xPc + 2.5 * xPb).max() <= 1e-14 * scale
     # and the fused call is their composition
-    assert fused["VB"] == vb and fused["prim"] == prim
+    assert abs(fused["VB"] - vb) <= 1e-13 * abs(vb) and abs(fused["prim"] - prim) <= 1e-12 * abs(prim)
     assert np.abs(fused["f1"] - (-x1b + interior(s, x, 0, 1 % P))).max() <= 1e-13 * scale
 
 
