@@ -65,7 +65,7 @@ def test_forward_adjoint_dbeta_match_oracle(name):
     assert np.abs(xPc + 2.5 * xPb).max() <= 1e-14 * scale
     # and the fused call is their composition
     assert abs(fused["VB"] - vb) <= 1e-13 * abs(vb) and abs(fused["prim"] - prim) <= 1e-12 * abs(prim)
-    assert np.abs(fused["f1"] - (-x1b + interior(s, x, 0, 1 % P))).max() <= 1e-13 * scale
+    assert np.abs(fused["f1"] - (-x1b + interior(s, x, 0, 1 % P))).max() <= TOL * scale
 
 
 @pytest.mark.parametrize("name", ["trap_N24_P8", "aziz_pbc_N64_P6", "dipole_2d_N40_P4"])
