@@ -340,12 +340,13 @@ __device__ __forceinline__ double min_image_wrapped(double d, double L, long lon
 // inside it stay FP64, where the repulsive and attractive terms nearly
 // cancel and FP32 would lose the difference.  Sums are FP64 either way.
 //
-// kDf (FP64 path with the Aziz potential): the far entries are evaluated in
-// double-float on the FP32 pipe (aziz_far_scale_df, about 2^-44 relative),
-// their gradients kept as double-floats and every sum formed in
-// double-float; the entries inside the damping radius, within 1e-6 L of the
-// half-box edge or within 1e-5 of the cutoff (where the in/out decision must
-// be the FP64 one) take the exact FP64 path as before.
+// kDf (FP64 path with the Aziz potential): the entries are evaluated in
+// double-float on the FP32 pipe (aziz_far_scale_df beyond the damping radius,
+// aziz_near_scale_df inside it; about 2^-43 relative), their gradients kept
+// as double-floats and every sum formed in double-float; only the entries
+// within 1e-6 L of the half-box edge or within 1e-5 of the cutoff (where the
+// image or the in/out decision must be the FP64 one) take the exact FP64
+// path, as every marked entry does without kDf.
 template <int D, bool kMixed, bool kDf>
 __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ part, int T, int b, int w,
                                              CompactSmem<D>& sm, double (*g)[D], int cap, const double* tbl,
@@ -405,7 +406,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
     const float Lf = (float)s.L, halfLf = 0.5f * (float)s.L;
     const int nj = min(kTile, s.N - jt * kTile);  // valid j lanes
     const bool ivalid = i < s.N;
-    unsigned mask = 0u, nmask = 0u;
+    unsigned mask = 0u, nmask = 0u, xmask = 0u;
     const int first = diag ? 1 : 0, lastS = diag ? 16 : 31;
     // |dx| within this of L/2 in FP32: the FP32 image choice might differ
     // from the FP64 one, so the entry takes the exact path (with the
@@ -430,7 +431,9 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         }
         const bool in = ivalid && jl < nj && (!diag || st < 16 || lane < 16) && r2 <= cut2f;
         mask |= (unsigned)in << jl;
-        nmask |= (unsigned)(in && (r2 < near2f || (aziz && edge) || (kDf && r2 >= shell2f))) << jl;
+        const bool exact = aziz && (edge || (kDf && r2 >= shell2f));
+        nmask |= (unsigned)(in && (r2 < near2f || exact)) << jl;
+        xmask |= (unsigned)(in && exact) << jl;
     }
     // 2. i-major layout: offsets by a warp scan of the counts
     const int icnt = __popc(mask);
@@ -449,7 +452,9 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
         for (int f = off; mm; ++f) {
             const int jj = __ffs(mm) - 1;
             mm &= mm - 1u;
-            sm.fe[f] = (unsigned short)((((nmask >> jj) & 1u) << 15) | (lane << 5) | jj);
+            // bit 15: redo on the near path; bit 14: on the exact FP64 path
+            sm.fe[f] = (unsigned short)((((nmask >> jj) & 1u) << 15) | (((xmask >> jj) & 1u) << 14) | (lane << 5) |
+                                        jj);
         }
     }
     // the column of lane j: the i's whose masks hold bit j
@@ -558,22 +563,24 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                 for (int a = 0; a < D; ++a) g[k][a] = f32_to_f64(sc * r[a]);
             }
         } else if (kDf) {
-            // every entry on the double-float far path, two independent ones
-            // per lane and iteration; the entries marked in the screen are
-            // redone below on the exact FP64 path
-            for (int k = lane; k < cn; k += 64) {
-                const bool two = k + 32 < cn;
-                const int f0 = c0 + k, f1 = two ? f0 + 32 : f0;
-                df r0[D], r1[D];
-                const df q0 = separation_df(f0, r0), q1 = separation_df(f1, r1);
-                const df sc0 = aziz_far_scale_df(q0, *etbl), sc1 = aziz_far_scale_df(q1, *etbl);
+            // every entry on the double-float far path, four independent ones
+            // per lane and iteration (the chains of dependent FP32 operations
+            // interleave); the entries marked in the screen are redone below
+            constexpr int kIlp = 4;
+            for (int k = lane; k < cn; k += 32 * kIlp) {
+                df sc[kIlp], r[kIlp][D];
 #pragma unroll
-                for (int a = 0; a < D; ++a) {
-                    const df v0 = dfl::mul(sc0, r0[a]);
-                    gd[f0 - c0][a] = make_float2(v0.hi, v0.lo);
-                    if (two) {
-                        const df v1 = dfl::mul(sc1, r1[a]);
-                        gd[f1 - c0][a] = make_float2(v1.hi, v1.lo);
+                for (int q = 0; q < kIlp; ++q) {
+                    const int f = c0 + min(k + 32 * q, cn - 1);  // past the end: a repeat, not stored
+                    sc[q] = aziz_far_scale_df(separation_df(f, r[q]), *etbl);
+                }
+#pragma unroll
+                for (int q = 0; q < kIlp; ++q) {
+                    if (k + 32 * q >= cn) break;
+#pragma unroll
+                    for (int a = 0; a < D; ++a) {
+                        const df v = dfl::mul(sc[q], r[q][a]);
+                        gd[k + 32 * q][a] = make_float2(v.hi, v.lo);
                     }
                 }
             }
@@ -612,6 +619,21 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                     __syncwarp();
                     for (int k = lane; k < cnt; k += 32) {
                         const int fn = sm.nl[k];
+                        if (kDf && !(sm.fe[fn] & 0x4000u)) {
+                            // inside the damping radius, the image certain and
+                            // the pair clearly inside the cutoff: double-float
+                            df r[D];
+                            const df q = separation_df(fn, r);
+                            if (q.hi >= (float)kAzizNearMinR2) {
+                                const df sc = aziz_near_scale_df(q, *etbl);
+#pragma unroll
+                                for (int a = 0; a < D; ++a) {
+                                    const df v = dfl::mul(sc, r[a]);
+                                    gd[fn - c0][a] = make_float2(v.hi, v.lo);
+                                }
+                                continue;
+                            }
+                        }
                         double r[D];
                         const double r2 = separation(fn, r);
                         store(fn, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);

@@ -70,6 +70,24 @@ int main() {
                         R;
         e_aziz = std::max(e_aziz, rel(val(aziz_far_scale_df(r2, tbl)), want));
     }
+    // inside the damping radius, r_s in [0.01, D): error against the size of
+    // the terms (the force crosses zero at r_m)
+    ld e_near = 0;
+    for (int k = 0; k < 400000; ++k) {
+        const ld r = rm * (0.01L + ((ld)Aziz::D - 0.01L) * U(rng));
+        const df r2 = mk(r * r);
+        const ld R = sqrtl(val(r2));
+        const ld x = R / rm, ix = 1.0L / x, D = Aziz::D;
+        const ld F = expl(-(D * ix - 1.0L) * (D * ix - 1.0L));
+        const ld dF = 2.0L * D * ix * ix * (D * ix - 1.0L) * F;
+        const ld T1 = -(ld)Aziz::A * al * expl(-al * x);
+        const ld T2 = (6.0L * Aziz::C6 * powl(ix, 7) + 8.0L * Aziz::C8 * powl(ix, 9) + 10.0L * Aziz::C10 * powl(ix, 11)) * F;
+        const ld T3 = -(Aziz::C6 * powl(ix, 6) + Aziz::C8 * powl(ix, 8) + Aziz::C10 * powl(ix, 10)) * dF;
+        const ld want = (eps / rm) * (T1 + T2 + T3) / R;
+        const ld size = (eps / rm) * (fabsl(T1) + fabsl(T2) + fabsl(T3)) / R;
+        e_near = std::max(e_near, fabsl(val(aziz_near_scale_df(r2, tbl)) - want) / size);
+    }
+    std::printf("aziz_near %.3Le\n", e_near);
     std::printf("add %.3Le\nadd_sloppy_abs %.3Le\nmul %.3Le\nsqr %.3Le\nexp %.3Le\nrsqrt %.3Le\nrsqrt_seed8ulp %.3Le\n"
                 "aziz_far %.3Le\n",
                 e_add, e_sloppy_abs, e_mul, e_sqr, e_exp, e_rsqrt, e_rsqrt_seed, e_aziz);

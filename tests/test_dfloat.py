@@ -6,7 +6,8 @@ Bounds, with u = 2^-24: the sum and product primitives within the published
 error bounds (AccurateDWPlusDW 3u^2, DWTimesDW 5u^2), the exponential within
 a few u^2 over [-69, 80], 1/sqrt within a few u^2 (and within 1e-12 from a
 seed eight float ulps off), and the Aziz far-field gradient scale within
-1e-12 relative: the GPU's FP64 parity bar (1e-10 per bead) is two orders of
+1e-12 relative (inside the damping radius, where the force crosses zero
+at r_m, within 1e-12 of the size of its terms): the GPU's FP64 parity bar (1e-10 per bead) is two orders of
 magnitude above what a sum of such pair terms can lose.
 """
 import shutil
@@ -46,3 +47,8 @@ def test_exp_and_rsqrt(errors):
 
 def test_aziz_far_scale(errors):
     assert errors["aziz_far"] <= 1e-12
+
+
+def test_aziz_near_scale(errors):
+    # inside the damping radius, against the size of the cancelling terms
+    assert errors["aziz_near"] <= 1e-12
