@@ -355,7 +355,18 @@ def pair_work(w, x):
             "flops_in_cutoff": float(pairs * tested + inside * (per - (9 if w["pbc"] else 0))),
             "transcendentals_in_cutoff": inside * PAIR_TRANSC[w["inter"]], "per_pair": per}
 
-PAIR_NCU = {"dram_bytes": 458496, "fp64_pipe": {"active": 0.752, "elapsed": 0.654}}
+# FP32 operations of the double-float Aziz pair evaluation, counted from the
+# source (pimd-b_gb300/csrc/forces.cu compact_tile, aziz_df.cuh, dfloat.cuh):
+# separation 76, gradient scale 248 (1/sqrt 21, |r| 9, exponent argument
+# 29, exp 81, powers, polynomial and the two terms 108), gradient 27, the
+# i- and j-side sums 66; the FP32 screen costs about 12 per tested pair.
+DF_OPS_PER_PAIR = 417
+SCREEN_OPS_PER_PAIR = 12
+# One k_pair_tiles_compact launch on the benchmark system (ncu --set full,
+# profiles/pair_tiles_compact_aziz_pbc_N256_P64_fp64.md): DRAM bytes read +
+# written, and pipe utilisation over active cycles.
+PAIR_NCU = {"dram_bytes": 466688, "fma_pipe_active": 0.229, "fp64_pipe_active": 0.287, "warps_active": 0.123,
+            "issue_per_sm_cycle": 1.49}
 
 
 class ClockSampler:
@@ -681,14 +692,40 @@ def main():
     roof = {"kernel": dom, "kernel_share": ms[dom] / max(sum(ms.values()), 1e-30), "launch_ms": dom_ms,
             "per_class_ms_per_step": {k: v / K for k, v in ms.items() if v > 0}}
     work = pair_work(w, x0) if dom == "bead_forces" else None
-    if work:
+    dfpath = work is not None and args.precision == "fp64" and w["inter"] == "aziz" and w["cutoff_ang"] > 0
+    if work and dfpath:
+        # The FP64 Aziz pair tiles evaluate in double-float on the FP32 pipe:
+        # their roofline is the FP32 issue rate.  Algorithmic FP32 operations
+        # per launch: DF_OPS_PER_PAIR per pair inside the cutoff (separation,
+        # gradient scale, gradient and the two sums in double-float) plus
+        # SCREEN_OPS_PER_PAIR per tested pair (the FP32 screen); the FP32
+        # peak in operations is the FMA probe's FLOP rate / 2.
+        t = dom_ms * 1e-3
+        ops = work["inside"] * DF_OPS_PER_PAIR + work["pairs"] * SCREEN_OPS_PER_PAIR
+        peak_ops = fp32_peak / 2.0
+        ncu = PAIR_NCU if args.workload == "cfg2" else None
+        roof.update({
+            "bound": "fp32 pipe (double-float arithmetic)",
+            "achieved": ops / t / 1e12, "peak": peak_ops, "unit": "T FP32 operations/s",
+            "frac": ops / t / 1e12 / peak_ops,
+            "algorithmic": (f"{ops:.4g} FP32 operations per launch: {work['inside']} pairs inside the cutoff x "
+                            f"{DF_OPS_PER_PAIR} (double-float separation, Aziz gradient scale, gradient, i and j "
+                            f"sums) + {work['pairs']} tested pairs x {SCREEN_OPS_PER_PAIR} (FP32 screen)"),
+            "fp64_equivalent": {
+                "achieved_tflops": work["flops_all"] / t / 1e12, "fp64_peak_tflops": fp64_peak,
+                "vs_fp64_peak": work["flops_all"] / t / 1e12 / fp64_peak,
+                "accounting": (f"{work['flops_all']:.4g} FLOP per launch: {work['pairs']} unique pairs x "
+                               f"{work['per_pair']} FLOP (force with minimum image, FMA = 2); above 1: the "
+                               f"arithmetic no longer runs on the FP64 pipe"),
+                "in_cutoff_tflops": work["flops_in_cutoff"] / t / 1e12},
+            "transcendentals_per_launch": work["transcendentals_in_cutoff"],
+            "ncu": ncu,
+            "traffic": ncu["dram_bytes"] if ncu else None,
+            "traffic_unit": "DRAM bytes per launch (ncu capture)" if ncu else None,
+            "peak_source": "FP32 FMA probe measured in this run (MEASURED_PEAKS.json has no FP32 entry)"})
+    elif work:
         t = dom_ms * 1e-3
         peak = fp64_peak if args.precision == "fp64" else fp32_peak
-        # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one
-        # k_pair_tiles_compact launch on this workload and its FP64 pipe
-        # utilisation, from the ncu capture in
-        # profiles/step_kernels_aziz_pbc_N256_P64_fp64.md
-        ncu = PAIR_NCU if (args.workload == "cfg2" and args.precision == "fp64") else None
         roof.update({
             "bound": "fp64" if args.precision == "fp64" else "fp32",
             "achieved": work["flops_all"] / t / 1e12, "peak": peak, "unit": "TFLOP/s",
@@ -697,12 +734,7 @@ def main():
                             f"{work['per_pair']} FLOP (force with minimum image, FMA = 2)"),
             "achieved_in_cutoff": work["flops_in_cutoff"] / t / 1e12,
             "frac_in_cutoff": work["flops_in_cutoff"] / t / 1e12 / peak,
-            "algorithmic_in_cutoff": (f"{work['flops_in_cutoff']:.4g} FLOP per launch: {work['inside']} pairs "
-                                      f"inside the cutoff at the force, the rest at the 15-FLOP test"),
-            "transcendentals_per_launch": work["transcendentals_in_cutoff"],
-            "fp64_pipe_ncu": ncu["fp64_pipe"] if ncu else None,
-            "traffic": ncu["dram_bytes"] if ncu else None,
-            "traffic_unit": "DRAM bytes per launch (ncu capture)" if ncu else None,
+            "transcendentals_per_launch": work["transcendentals_in_cutoff"], "traffic": None,
             "peak_source": ("FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 entry)"
                             if args.precision == "fp64" else "FP32 FMA probe measured in this run")})
     else:

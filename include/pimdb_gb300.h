@@ -317,6 +317,10 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
  *                    automatic (default: on from 512 particles);
  *   "cuda_graphs"    0: enqueue every step's kernels instead of replaying a
  *                    captured graph (default 1);
+ *   "flat_energies"  1 / 0 / -1: cycle energies from prefix sums of the
+ *                    interior links (one independent entry per thread) /
+ *                    from a scan per row / automatic (default: prefix sums
+ *                    from 512 particles);
  *   "pair_entry_cap" pair-tile kernel: gradients held in shared memory per
  *                    warp (a multiple of 32 up to 1024; 0 = default).  Fewer
  *                    let more warps share an SM; a tile with more pairs

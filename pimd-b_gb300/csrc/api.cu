@@ -261,6 +261,7 @@ std::string validate_config(const pimdb_config& c) {
 
 void sys_params_from_config(const pimdb_config& c, Sys& s) {
     s.N = c.natoms;
+    s.eflat = exchange_flat_default(c.natoms);
     s.P = c.nbeads;
     s.ld = (c.natoms + 31) / 32 * 32;
     s.bosonic = (c.bosonic && c.nbeads > 1) ? 1 : 0;  // simulation.cpp:690
@@ -1506,6 +1507,8 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
         h->opt_cells = value < 0 ? -1 : (value ? 1 : 0);
     } else if (n == "cuda_graphs") {
         h->opt_graph = value ? 1 : 0;
+    } else if (n == "flat_energies") {
+        h->s.eflat = value < 0 ? exchange_flat_default(h->s.N) : (value ? 1 : 0);
     } else if (n == "pair_entry_cap") {
         if (value < 0 || value > 1024 || value % 32)
             return fail(h, PIMDB_ERR_ARG, "pair_entry_cap must be 0 or a multiple of 32 up to 1024");

@@ -52,7 +52,24 @@ DF_HD dfl::df aziz_far_scale_df(dfl::df r2, const dfl::ExpTable& tbl) {
 // short-range branch) is left to the FP64 path.
 constexpr double kAzizNearMinR2 = (0.01 * Aziz::rm) * (0.01 * Aziz::rm);
 
-DF_HD dfl::df aziz_near_scale_df(dfl::df r2, const dfl::ExpTable& tbl) {
+// r_s >= D on a double-float r2 (the reference compares r_s = r / r_m with
+// D; at the boundary F = 1 and dF = 0 on both sides, so a decision that
+// differs from the FP64 one within the double-float rounding of r2 changes
+// the result by far less than that rounding).
+DF_HD bool aziz_is_far_df(dfl::df r2) {
+    constexpr double far2 = (Aziz::D * Aziz::rm) * (Aziz::D * Aziz::rm);
+    constexpr float fh = (float)far2, fl = (float)(far2 - (double)fh);
+    return r2.hi > fh || (r2.hi == fh && r2.lo >= fl);
+}
+
+#if defined(__CUDA_ARCH__)
+// out of line on the device: a pass over the few entries inside the damping
+// radius per tile calls it, and the pair kernel's hot loop stays smaller
+__device__ __noinline__
+#else
+inline
+#endif
+dfl::df aziz_near_scale_df(dfl::df r2, const dfl::ExpTable& tbl) {
     using namespace dfl;
     constexpr double irm = 1.0 / Aziz::rm, aal = Aziz::A * Aziz::alpha, erm = Aziz::eps / Aziz::rm,
                      c6a = 6.0 * Aziz::C6, c8a = 8.0 * Aziz::C8, c10a = 10.0 * Aziz::C10, d2 = 2.0 * Aziz::D;

@@ -50,6 +50,7 @@ struct Sys {
     int pair_cap;               // pair-tile gradient capacity per warp (0: the default)
     int reserve_sms;            // SMs (the highest ids) the pair tiles leave to the exchange's
                                 // one-block passes running beside them (0: none)
+    int eflat;                  // cycle energies from link prefix sums (given a work array)
     uint64_t seed;
     uint32_t replica;
     // device arrays

@@ -293,10 +293,11 @@ __global__ void __launch_bounds__(128) k_pair_tiles(Sys s, double* __restrict__ 
 // result as k_pair_tiles up to rounding; the exact FP64 cutoff test is
 // applied in step 2.
 constexpr int kCompactWarps = 2;
-// gradient capacity per warp unless Sys::pair_cap says otherwise (the
-// double-float path keeps two more small arrays per warp; 544 entries let
-// five blocks share an SM, as 608 did before them)
-constexpr int kCompactDefaultCap = 544;
+// gradient capacity per warp unless Sys::pair_cap says otherwise: 384
+// entries let six blocks share an SM; a tile with more entries is summed in
+// two chunks (measured on the benchmark system: 82 us at 384 against 86 at
+// 544 and 85 at 640)
+constexpr int kCompactDefaultCap = 384;
 // entries of the damping-radius list evaluated per pass
 constexpr int kCompactNear = 256;
 
@@ -563,10 +564,11 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                 for (int a = 0; a < D; ++a) g[k][a] = f32_to_f64(sc * r[a]);
             }
         } else if (kDf) {
-            // every entry on the double-float far path, four independent ones
-            // per lane and iteration (the chains of dependent FP32 operations
-            // interleave); the entries marked in the screen are redone below
-            constexpr int kIlp = 4;
+            // every entry on the double-float far path, two independent ones
+            // per lane and iteration (their chains of dependent FP32
+            // operations interleave; four measured slower, with twice the
+            // code); the entries marked in the screen are redone below
+            constexpr int kIlp = 2;
             for (int k = lane; k < cn; k += 32 * kIlp) {
                 df sc[kIlp], r[kIlp][D];
 #pragma unroll
@@ -625,7 +627,10 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                             df r[D];
                             const df q = separation_df(fn, r);
                             if (q.hi >= (float)kAzizNearMinR2) {
-                                const df sc = aziz_near_scale_df(q, *etbl);
+                                // the screen's margin lets entries just beyond the
+                                // damping radius in, where F = 1 and dF = 0
+                                const df sc = aziz_is_far_df(q) ? aziz_far_scale_df(q, *etbl)
+                                                                : aziz_near_scale_df(q, *etbl);
 #pragma unroll
                                 for (int a = 0; a < D; ++a) {
                                     const df v = dfl::mul(sc, r[a]);

@@ -67,6 +67,9 @@ size_t exchange_grid_doubles(const Sys& s);
 int exchange_reserved_sms(const Sys& s);
 size_t exchange_grid_flags(const Sys& s);
 void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream_t st);
+// Whether the cycle energies of a system of N particles come from link prefix
+// sums by default (Sys::eflat; the option "flat_energies" overrides it).
+int exchange_flat_default(int N);
 // The cotangent of V_B on beads 1 and P into fx: vb_bar * dV_B/dx (the
 // exterior spring forces' exchange part times -vb_bar).
 void launch_exchange_adjoint(const Sys& s, int D, double vb_bar, cudaStream_t st);
