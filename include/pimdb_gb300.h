@@ -228,6 +228,13 @@ int pimdb_exchange(pimdb_handle* h, double* scalars, double* f_first, double* f_
  * The adjoint and dbeta read the last forward evaluation; they return
  * PIMDB_ERR_ARG when the coordinates changed since (a state set, a step). */
 int pimdb_exchange_forward(pimdb_handle* h, double* VB);
+/* Diagnostic (no counterpart in the reference): how many exchange
+ * evaluations since creation found the reused estimate of V (the previous
+ * evaluations' potentials, extrapolated) unusable and were redone from a
+ * fresh FP32 estimate, per direction for the in-block retry below 768
+ * particles and per evaluation above.  Smooth dynamics keep it near 0; each
+ * retry costs a slower evaluation, not accuracy. */
+int pimdb_exchange_retries(pimdb_handle* h, long long* count);
 int pimdb_exchange_adjoint(pimdb_handle* h, double vb_bar, double* x1_bar, double* xP_bar);
 int pimdb_exchange_dbeta(pimdb_handle* h, double* dbeta);
 

@@ -470,9 +470,11 @@ extern "C" int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_ha
     }
     // xflags: [0],[1] exact fallback used (forward, backward); [2] completion
     // counter; [3] next evaluation needs a fresh FP32 estimate; [4],[5] the
-    // forward / backward solve asked for one.
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s.xflags, 8 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(s.xflags, 0, 8 * sizeof(int));
+    // forward / backward solve asked for one; [6] retry pending; [7] the
+    // estimate was reused; [kExchRetryCount] evaluations redone from a fresh
+    // estimate after the reused one failed.
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s.xflags, 16 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(s.xflags, 0, 16 * sizeof(int));
     const int one = 1;
     if (e == cudaSuccess) e = cudaMemcpy(s.xflags + 3, &one, sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = alloc(&h->d_red[0], (size_t)3 * nred);
@@ -1178,6 +1180,17 @@ static int exchange_forward_current(pimdb_handle* h, const char* what) {
     if (h->fwd_gen != h->xgen)
         return fail(h, PIMDB_ERR_ARG,
                     std::string(what) + " needs pimdb_exchange_forward on the current coordinates first");
+    return PIMDB_OK;
+}
+
+extern "C" int pimdb_exchange_retries(pimdb_handle* h, long long* count) {
+    if (!h || !count) return PIMDB_ERR_ARG;
+    *count = 0;
+    if (!h->s.bosonic || h->factorial) return PIMDB_OK;
+    int v = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&v, h->s.xflags + kExchRetryCount, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    *count = v;
     return PIMDB_OK;
 }
 

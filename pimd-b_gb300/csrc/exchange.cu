@@ -212,11 +212,13 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
     extern __shared__ double ys[];  // y: N+1, acc: N+1, then 32 for reductions
     __shared__ int last_block;
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    if (phase == 1 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.xflags[kExchRetryCount], 1);
     const int allow_exact = force_exact || phase == 1 || !((volatile int*)s.xflags)[7];
     const int dir = blockIdx.x;
     const int gave_up = solve_direction(s, dir, force_exact, ys, allow_exact,
                                         pre ? pre + (size_t)dir * (s.N + 1) : nullptr, !inline_retry);
     if (gave_up && inline_retry) {
+        if (threadIdx.x == 0) atomicAdd(&s.xflags[kExchRetryCount], 1);
         estimate_direction(s, dir, reinterpret_cast<float*>(ys));  // 3 (N+1) floats fit in ys
         __syncthreads();
         weights_direction(s, dir, nullptr);  // CUDA's exp (a rare path)
@@ -387,10 +389,13 @@ __global__ void __launch_bounds__(kClusterSolveThreads) k_exch_solve_cluster(Sys
     double* y = ysol + (size_t)dir * (s.N + 1);
     const int nb = (nn + 31) / 32;
     const int nown = (nb - c + C - 1) / C;  // blocks c, c + C, ...
+    const int nmax = (nb + C - 1) / C;      // the most any CTA owns: the same layout in every CTA
     extern __shared__ double csm[];
-    double* acc = csm;                      // [nown][32]
-    double* yown = csm + (size_t)nown * 32;  // [nown][32]: y of the owned blocks, read by the other CTAs
-    double* yj = yown + (size_t)nown * 32;   // [32]
+    // yown first, at the same offset in every CTA: the other CTAs map this
+    // CTA's address of it onto their own (map_shared_rank)
+    double* yown = csm;                      // [nmax][32]: y of the owned blocks
+    double* acc = csm + (size_t)nmax * 32;   // [nmax][32]
+    double* yj = acc + (size_t)nmax * 32;    // [32]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int e = tid; e < nown * 32; e += blockDim.x) acc[e] = 0.0;
     __syncthreads();

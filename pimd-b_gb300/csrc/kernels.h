@@ -70,6 +70,9 @@ void launch_exchange_forces_mode(const Sys& s, int D, int accumulate, cudaStream
 // Whether the cycle energies of a system of N particles come from link prefix
 // sums by default (Sys::eflat; the option "flat_energies" overrides it).
 int exchange_flat_default(int N);
+// Index in Sys::xflags (16 ints) of the count of exchange evaluations redone
+// from a fresh estimate after the reused one failed.
+constexpr int kExchRetryCount = 10;
 // The cotangent of V_B on beads 1 and P into fx: vb_bar * dV_B/dx (the
 // exterior spring forces' exchange part times -vb_bar).
 void launch_exchange_adjoint(const Sys& s, int D, double vb_bar, cudaStream_t st);

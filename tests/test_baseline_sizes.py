@@ -198,6 +198,9 @@ def test_benchmark_system_trajectory(options):
             for got, want, label in ((gx, tr.x, "x"), (gp, tr.p, "p"), (gf, tr.f, "f")):
                 assert rel_per_bead(got, want) < TRAJ_TOL, (st, label)
         hx, hp, hf = h.get_state()
+        # smooth dynamics: the fast path (reused estimate, cluster solve)
+        # served every evaluation, none was redone from a fresh estimate
+        assert g.exchange_retries() == 0 and h.exchange_retries() == 0
     for got, want, label in ((hx, tr.x, "x"), (hp, tr.p, "p"), (hf, tr.f, "f")):
         assert rel_per_bead(got, want) < TRAJ_TOL, label
 
@@ -255,6 +258,7 @@ def test_large_system_trajectory():
                            nthreads=NTH) == 0
             g.step(1)
         gx, gp, gf = g.get_state()
+        assert g.exchange_retries() == 0
     for got, want, label in ((gx, tr.x, "x"), (gp, tr.p, "p"), (gf, tr.f, "f")):
         assert rel_per_bead(got, want) < TRAJ_TOL, label
 
@@ -286,6 +290,7 @@ def test_other_benchmark_systems(name):
                            nthreads=NTH) == 0
         g.step(5)
         gx, gp, _ = g.get_state()
+        assert g.exchange_retries() == 0
     assert rel_per_bead(gx, tr.x) < TRAJ_TOL and rel_per_bead(gp, tr.p) < TRAJ_TOL
 
 

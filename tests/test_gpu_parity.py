@@ -266,6 +266,8 @@ def test_exchange_retry_after_large_jump():
             gx, gp, gf = g.get_state()
             for got, want, label in ((gx, tr.x, "x"), (gp, tr.p, "p"), (gf, tr.f, "f")):
                 assert rel_per_bead(got, want) < 1e-9, (st, label, rel_per_bead(got, want))
+        # the violent steps did take the retry
+        assert g.exchange_retries() > 0
 
 
 CELL_CASES = {
