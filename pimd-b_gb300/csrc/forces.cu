@@ -799,9 +799,11 @@ __global__ void k_bead_finish(Sys s, const double* __restrict__ part, int T, int
 // cell in ascending index: the order of every later sum is fixed), with
 // FP64 and FP32 hi/lo copies.  k_pair_cells (one thread per particle in
 // sorted order) screens the candidates in FP32 into a per-thread list, then
-// the warp evaluates the lists in lockstep (FP64, or FP32 in the mixed
-// path) and sums the pair gradient on its own particle only; the result is
-// one partial-sum slot for k_bead_finish.
+// the warp evaluates the lists in lockstep (FP64 Aziz pairs in double-float
+// on the FP32 pipe, other FP64 potentials in FP64, FP32 in the mixed path)
+// and sums the pair gradient on its own particle only; the result is one
+// partial-sum slot for k_bead_finish.  The hi/lo copies are the wrapped
+// position's nearest float and the float of the remainder: a double-float.
 constexpr int kCellBinThreads = 1024;
 constexpr int kCellThreads = 128;
 constexpr int kCellList = 64;
@@ -910,8 +912,24 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
                                                              const float* __restrict__ xh,
                                                              const float* __restrict__ xl, double* __restrict__ fpair) {
     __shared__ double tbl[256];
+    __shared__ dfl::ExpTable etbl;
     extern __shared__ int lists[];  // kCellList x kCellThreads
-    for (int j = threadIdx.x; j < 256; j += blockDim.x) tbl[j] = kExp2Table256[j];
+    // FP64 with the Aziz potential: the pairs in double-float on the FP32
+    // pipe (as the pair tiles), the few at the cutoff or closer than 0.01 r_m
+    // on the exact FP64 path
+    constexpr bool kFp64 = sizeof(R) == 8;
+    const bool dfp = kFp64 && s.int_kind == POT_AZIZ;
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) {
+        const double v = kExp2Table256[j];
+        tbl[j] = v;
+        if (kFp64) {
+            float h, l;
+            split_f32(v, h, l);
+            const dfl::df n = dfl::fast_two_sum(h, l);
+            etbl.hi[j] = n.hi;
+            etbl.lo[j] = n.lo;
+        }
+    }
     __syncthreads();
     int ncell = 1;
     for (int a = 0; a < D; ++a) ncell *= nc;
@@ -941,10 +959,35 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
         cc[a] = min(max((int)floor((xi[a] + 0.5 * s.L) * (nc / s.L)), 0), nc - 1);
     }
     double acc[D];
+    dfl::df accd[D];
 #pragma unroll
-    for (int a = 0; a < D; ++a) acc[a] = 0.0;
+    for (int a = 0; a < D; ++a) {
+        acc[a] = 0.0;
+        accd[a] = dfl::df{0.0f, 0.0f};
+    }
+    const dfl::df Ldf{(float)s.L, (float)(s.L - f32_to_f64((float)s.L))};
+    const float shell2f = (float)cut2 * (1.0f - 1e-5f);
+    // the double-float gradient of candidate q; false: take the FP64 path
+    auto eval_df = [&](int q) {
+        dfl::df d[D], r2{0.0f, 0.0f};
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            dfl::df v = dfl::add_sloppy(dfl::df{hi[a], lo[a]},
+                                        dfl::df{-Xh[(size_t)a * N + q], -Xl[(size_t)a * N + q]});
+            if (fabsf(v.hi) > halfLf) v = dfl::add(v, v.hi > 0.0f ? dfl::neg(Ldf) : Ldf);
+            d[a] = v;
+            r2 = a == 0 ? dfl::sqr(v) : dfl::add_sloppy(r2, dfl::sqr(v));
+        }
+        // at the cutoff the in/out decision must be the FP64 one
+        if (r2.hi >= shell2f || r2.hi < (float)kAzizNearMinR2) return false;
+        const dfl::df sc = aziz_is_far_df(r2) ? aziz_far_scale_df(r2, etbl) : aziz_near_scale_df(r2, etbl);
+#pragma unroll
+        for (int a = 0; a < D; ++a) accd[a] = dfl::add_sloppy(accd[a], dfl::neg(dfl::mul(sc, d[a])));
+        return true;
+    };
     // gradient of one candidate q (sorted index), subtracted from acc
     auto eval = [&](int q) {
+        if (dfp && eval_df(q)) return;
         R r[D];
         R r2 = (R)0;
 #pragma unroll
@@ -1026,7 +1069,8 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
     if (active) {
         const int i = clist[(size_t)b * N + k];
 #pragma unroll
-        for (int a = 0; a < D; ++a) fpair[idx<D>(s, b, a, i)] = acc[a];
+        for (int a = 0; a < D; ++a)
+            fpair[idx<D>(s, b, a, i)] = dfp ? acc[a] + (f32_to_f64(accd[a].hi) + f32_to_f64(accd[a].lo)) : acc[a];
     }
 }
 
