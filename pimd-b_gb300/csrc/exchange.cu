@@ -246,13 +246,16 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
 // W[n-1][u] y_u costs N^2/2 FP64 multiply-adds per direction, which on the
 // one block of k_exch_solve is bound by a single SM's FP64 pipe.  Here 32-row
 // blocks go round-robin to `nct` CTAs per direction (all resident: cooperative
-// launch).  For every block j in order, its owner resolves the diagonal block
-// with warp shuffles (its rows already hold the contributions of blocks < j)
-// and publishes y_j behind a fence and a flag; every CTA then adds
-// W[rows][block j] y_j to the rows it owns (8 threads per row, shuffle sums:
-// a fixed order).  The critical path is one diagonal block plus one flag per
-// 32 levels.  Waits give up after a bounded number of polls (ERRB_TIMEOUT).
-// k_exch_solve then post-processes y as usual.
+// launch).  Block j's owner resolves its diagonal block with warp shuffles
+// (its rows then hold the contributions of blocks < j) and publishes y_j
+// behind a fence and a flag.  Once y_j is out, the owner of block j + 1 adds
+// W[rows of j + 1][block j] y_j to those rows first, from weights loaded
+// while it waited, resolves block j + 1 and publishes it; only then does it
+// fold y_j into its other rows, as every other CTA does meanwhile (8 threads
+// per row, shuffle sums: a fixed order).  The critical path per block is a
+// flag, one 32x32 fold and one diagonal block.  Waits give up after a
+// bounded number of polls (ERRB_TIMEOUT).  k_exch_solve then post-processes
+// y as usual.
 __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, int phase, double* ysol,
                                                                       unsigned* gflags, int nct) {
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
@@ -272,12 +275,11 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
     for (int e = tid; e < nown * 32; e += blockDim.x) acc[e] = 0.0;
     if (tid == 0) abort_solve = 0;
     __syncthreads();
-    const int i = tid >> 3, part = tid & 7;  // update role: row of the block, quarter of the columns
-    // the next block's weights, loaded while its predecessor is awaited (only
-    // the CTA owning block j + 1 is on the critical path): the diagonal block
-    // (warp 0) and W[rows of j + 1][block j]
+    const int i = tid >> 3, part = tid & 7;  // fold role: row of the block, quarter of the columns
+    // weights of the block this CTA resolves next, loaded ahead: its
+    // diagonal block (warp 0) and W[rows of b][block b - 1]
     double wd[32], wn[4];
-    auto prefetch = [&](int b) {  // b: the block about to be resolved by this CTA
+    auto prefetch = [&](int b) {
         if (warp == 0) {
             const int n = 32 * b + lane;
 #pragma unroll
@@ -287,66 +289,75 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
 #pragma unroll
         for (int q = 0; q < 4; ++q) wn[q] = (b >= 1 && n < nn) ? W[tri(n - 1) + 32 * (b - 1) + 4 * part + q] : 0.0;
     };
-    if (c == 0) prefetch(0);
-    for (int j = 0; j < nb; ++j) {
-        if (j % nct == c) {
-            if (warp == 0) {
-                const int n = 32 * j + lane;
-                double a = n == 0 ? 1.0 : (n < nn ? acc[(j / nct) * 32 + lane] : 0.0);
+    auto diag_publish = [&](int b) {  // warp 0 of the owner of block b
+        const int n = 32 * b + lane;
+        double a = n == 0 ? 1.0 : (n < nn ? acc[(b / nct) * 32 + lane] : 0.0);
 #pragma unroll
-                for (int t = 0; t < 32; ++t) {
-                    const double yt = __shfl_sync(0xffffffffu, a, t);
-                    if (lane > t) a = fma(wd[t], yt, a);
-                }
-                if (n < nn) y[n] = a;
-                yj[lane] = n < nn ? a : 0.0;
-                __threadfence();
-                __syncwarp();
-                if (lane == 0) atomicExch(&flags[j], 1u);
+        for (int t = 0; t < 32; ++t) {
+            const double yt = __shfl_sync(0xffffffffu, a, t);
+            if (lane > t) a = fma(wd[t], yt, a);
+        }
+        if (n < nn) y[n] = a;
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) atomicExch(&flags[b], 1u);
+    };
+    auto fold = [&](int r, int j, bool pre) {  // owned block r += W[rows of r][block j] y_j
+        const int n = 32 * r + i;
+        double sum = 0.0;
+        if (n < nn) {
+            if (pre) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sum = fma(wn[q], yj[4 * part + q], sum);
+            } else {
+                const double* row = W + tri(n - 1) + 32 * j + 4 * part;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sum = fma(row[q], yj[4 * part + q], sum);
             }
-        } else {
-            if ((j + 1) % nct == c && j + 1 < nb) prefetch(j + 1);
-            if (tid == 0) {
-                unsigned it = 0;
-                while (((volatile unsigned*)flags)[j] == 0u) {
-                    if (++it > (1u << 22)) {
-                        atomicOr(s.err, ERRB_TIMEOUT);
-                        abort_solve = 1;
-                        break;
-                    }
-                    if (it > 64) __nanosleep(32);
+        }
+        sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 4);
+        if (part == 0 && n < nn) acc[(r / nct) * 32 + i] += sum;
+    };
+    if (c == 0) {
+        prefetch(0);
+        if (warp == 0) diag_publish(0);
+    }
+    if (nb > 1 && 1 % nct == c) prefetch(1);
+    for (int j = 0; j + 1 < nb; ++j) {
+        if (j % nct != c && tid == 0) {  // the owner of block j has y_j already
+            unsigned it = 0;
+            while (((volatile unsigned*)flags)[j] == 0u) {
+                if (++it > (1u << 22)) {
+                    atomicOr(s.err, ERRB_TIMEOUT);
+                    abort_solve = 1;
+                    break;
                 }
-                __threadfence();
+                if (it > 64) __nanosleep(32);
             }
+            __threadfence();
         }
         __syncthreads();
         if (abort_solve) break;
-        if (j % nct != c && tid < 32) {
+        if (tid < 32) {
             const int n = 32 * j + tid;
             yj[tid] = n < nn ? ((volatile double*)y)[n] : 0.0;
         }
         __syncthreads();
-        // rows this CTA owns below block j: W[rows][block j] y_j, the next
-        // block first from the prefetched weights
-        for (int r = c; r < nb; r += nct) {
-            if (r <= j) continue;
-            const int n = 32 * r + i;
-            double sum = 0.0;
-            if (n < nn) {
-                if (r == j + 1) {
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) sum = fma(wn[q], yj[4 * part + q], sum);
-                } else {
-                    const double* row = W + tri(n - 1) + 32 * j + 4 * part;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) sum = fma(row[q], yj[4 * part + q], sum);
-                }
-            }
-            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-            sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-            sum += __shfl_xor_sync(0xffffffffu, sum, 4);
-            if (part == 0) acc[(r / nct) * 32 + i] += sum;
+        const int jn = j + 1;
+        const bool mine = jn % nct == c;
+        if (mine) {  // the critical path: the next diagonal block's rows, then that block
+            fold(jn, j, true);
+            __syncthreads();
+            if (warp == 0) diag_publish(jn);
         }
+        for (int r = jn + (c - jn % nct + nct) % nct; r < nb; r += nct) {
+            if (r == jn) continue;
+            fold(r, j, false);
+        }
+        // weights for the next block this CTA resolves, while others work
+        if (jn + 1 < nb && (jn + 1) % nct == c) prefetch(jn + 1);
         __syncthreads();
     }
     // the CTA that finishes last clears the flags for the next launch
