@@ -458,6 +458,8 @@ __device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumul
         for (int n = lane; n <= nmax; n += 32) {
             double pr;
             if (n <= l) {
+                // a zero weight (a cycle too costly to contribute) adds exactly 0
+                if (!exact && s.Wf[r + n] == 0.0) continue;
                 pr = exact ? exp(-beta * (s.V[n] + s.E[r + n] + vbl - VN)) / (l + 1) : s.Wf[r + n] * s.yf[n] * Rl;
             } else {
                 pr = 1.0 - s.rowC[l];
@@ -481,6 +483,7 @@ __device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumul
         for (int q = max(0, l - 1) + lane; q < N; q += 32) {
             double pr;
             if (q >= l) {
+                if (!exact && s.Wf[tri(q) + l] == 0.0) continue;
                 pr = exact ? exp(-beta * (vl + s.E[tri(q) + l] + s.Vb[q + 1] - VN)) / (q + 1)
                            : s.Wf[tri(q) + l] * yl * s.rowR[q];
             } else {

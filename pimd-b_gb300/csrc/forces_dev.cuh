@@ -35,6 +35,9 @@ __device__ __forceinline__ double exp_tang(double x, const double* tbl) {
     const double shifter = 6755399441055744.0;  // 1.5 * 2^52
     const double t = fma(x, 46.16624130844683, shifter);  // 32 / ln2
     const int n = __double2loint(t);
+    // the result would be returned as 0 below: skip the polynomial (most of
+    // a large system's exchange weights land here)
+    if (n < -32318) return 0.0;
     const double nd = t - shifter;
     double r = fma(nd, -0.021660849392446835, x);  // L1
     r = fma(nd, -5.145609244655338e-14, r);        // L2
@@ -46,7 +49,7 @@ __device__ __forceinline__ double exp_tang(double x, const double* tbl) {
     const double tj = tbl[n & 31];
     const double y = fma(tj, p, tj);
     const int hi = __double2hiint(y) + ((n >> 5) << 20);
-    return n < -32318 ? 0.0 : __hiloint2double(hi, __double2loint(y));
+    return __hiloint2double(hi, __double2loint(y));
 }
 
 // The same method with a 256-entry table (kExp2Table256: 2^(j/256), j =
