@@ -44,7 +44,6 @@ DF_HD float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 DF_HD float bits_to_float(int b) { return __int_as_float(b); }
 DF_HD int float_to_bits(float f) { return __float_as_int(f); }
 DF_HD float rsqrt_approx(float x) { return rsqrtf(x); }
-DF_HD float rint_f(float x) { return rintf(x); }
 #else
 DF_HD float add_rn(float a, float b) { return a + b; }
 DF_HD float sub_rn(float a, float b) { return a - b; }
@@ -61,7 +60,6 @@ DF_HD int float_to_bits(float f) {
     return b;
 }
 DF_HD float rsqrt_approx(float x) { return 1.0f / sqrtf(x); }
-DF_HD float rint_f(float x) { return rintf(x); }
 #endif
 
 DF_HD df two_sum(float a, float b) {
@@ -169,9 +167,19 @@ constexpr float kLn2_256_2 = 0x1.0bfbe8p-23f;  // the next 24 bits
 constexpr float kLn2_256_3 = 0x1.cf79acp-48f;  // the remainder (sum within 5e-23 of ln2/256)
 constexpr float kInvLn2_256 = 369.32992553710938f;  // 256 / ln2 rounded to float
 
+constexpr float kRoundShift = 12582912.0f;  // 1.5 * 2^23: adding it rounds |v| < 2^22 to an integer
+
 DF_HD df exp(df x, const ExpTable& tbl) {
-    const float nf = rint_f(mul_rn(x.hi, kInvLn2_256));
-    const int n = (int)nf;
+    // outside [-88, 88] the result is below the normal range (0) or
+    // overflows; NaN passes through
+    if (x.hi < -88.0f) return {0.0f, 0.0f};
+    if (!(x.hi <= 88.0f)) return {x.hi * 3.0e38f, 0.0f};  // +inf, or NaN
+    // n = round(x.hi 256/ln2) by the shifter: the sum's low mantissa bits
+    // hold n, and no rounding or float-to-integer instruction is issued
+    // (those run on the FP64/conversion pipe on this GPU)
+    const float tsh = fma_rn(x.hi, kInvLn2_256, kRoundShift);
+    const int n = float_to_bits(tsh) - float_to_bits(kRoundShift);
+    const float nf = sub_rn(tsh, kRoundShift);
     // t = x - n ln2/256, in double-float
     const float r1 = fma_rn(-nf, kLn2_256_1, x.hi);      // exact: n L1 has <= 24 bits, r1 ~ x.hi - n L1 (Sterbenz)
     const df p2 = two_prod(nf, kLn2_256_2);              // n L2 exactly
