@@ -364,9 +364,10 @@ DF_OPS_PER_PAIR = 417
 SCREEN_OPS_PER_PAIR = 12
 # One k_pair_tiles_compact launch on the benchmark system (ncu --set full,
 # profiles/pair_tiles_compact_aziz_pbc_N256_P64_fp64.md): DRAM bytes read +
-# written, and pipe utilisation over active cycles.
-PAIR_NCU = {"dram_bytes": 466688, "fma_pipe_active": 0.229, "fp64_pipe_active": 0.287, "warps_active": 0.123,
-            "issue_per_sm_cycle": 1.49}
+# written, pipe utilisation over active cycles, warps active and
+# warp-instructions issued per SM cycle (of 4).
+PAIR_NCU = {"dram_bytes": 470784, "fma_pipe_active": 0.286, "alu_pipe_active": 0.175, "warps_active": 0.147,
+            "issue_per_sm_cycle": 1.77, "duration_us_cold": 75.6}
 
 
 class ClockSampler:
