@@ -187,16 +187,21 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_estimate(Sys s, int phase
 
 // Pass 2: every FP64 exponential at once, one thread per packed entry
 // (grid-stride over rows; phase 1 runs only on a retry).
+// Also records the band of the weights (kExchBand: the largest p + 1 - u of
+// a nonzero weight) for the banded solve; one atomic per warp.
 __global__ void k_exch_weights(Sys s, int phase) {
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
     __shared__ double tbl[32];
     if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
     __syncthreads();
+    int band = 0;
     for (int p = blockIdx.y; p < s.N; p += gridDim.y) {
         const double inv = recip_row(p);
         for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= p; u += gridDim.x * blockDim.x)
-            exch_weight(s, p, u, inv, tbl);
+            if (exch_weight(s, p, u, inv, tbl)) band = max(band, p + 1 - u);
     }
+    band = __reduce_max_sync(0xffffffffu, band);
+    if ((threadIdx.x & 31) == 0 && band > 0) atomicMax(&s.xflags[kExchBand], band);
 }
 
 // Pass 3: block 0 forward, block 1 backward.  Phase 0 may not fall back to
@@ -238,7 +243,10 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
         return;
     }
     solve_finish(s, !force_exact);
-    if (threadIdx.x == 0) s.xflags[6] = 0;
+    if (threadIdx.x == 0) {
+        s.xflags[6] = 0;
+        s.xflags[kExchBand] = 0;  // the next evaluation's weights measure it anew
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -257,8 +265,9 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
 // bounded number of polls (ERRB_TIMEOUT).  k_exch_solve then post-processes
 // y as usual.
 __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, int phase, double* ysol,
-                                                                      unsigned* gflags, int nct) {
+                                                                      unsigned* gflags, int nct, int banded) {
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    if (banded && ((volatile int*)s.xflags)[kExchBand] <= kBandMax) return;  // k_exch_solve_band solved it
     extern __shared__ double gsm[];
     __shared__ int abort_solve;
     const int dir = blockIdx.x / nct, c = blockIdx.x % nct;
@@ -373,6 +382,88 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
 }
 
 // ---------------------------------------------------------------------------
+// Pass 3 when the weights are banded.  A weight is exactly zero when its
+// cycle costs beta_ex E > 700 (the exponential's result is returned as 0):
+// at liquid-helium densities and temperatures every cycle of more than a
+// dozen or so particles, so node n depends only on nodes n - band .. n - 1
+// with a band far below N.  k_exch_weights records the band of the current
+// evaluation; when it is at most kBandMax (two 32-row blocks) this kernel
+// solves each direction on one CTA: block b's rows take the two previous
+// blocks' y from shared memory (all threads, 8 columns each), then warp 0
+// resolves the diagonal block by shuffles, while warps 1-7 stage the next
+// block's weights into the other half of a double buffer.  No flags and no
+// inter-CTA waits; y lands in ysol as from the dense solves, which step
+// aside (their `banded` argument) and stay the general path.
+__global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int phase, double* ysol) {
+    if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    if (((volatile int*)s.xflags)[kExchBand] > kBandMax) return;  // the dense solve runs instead
+    extern __shared__ double bsm[];
+    __shared__ double accb[32];
+    const int dir = blockIdx.x;
+    const int nn = dir == 0 ? s.N + 1 : s.N;
+    const double* __restrict__ W = dir == 0 ? s.Wf : s.Wb;
+    double* y = ysol + (size_t)dir * (s.N + 1);
+    const int nnpad = (nn + 1) & ~1;
+    double* ys = bsm;                    // [nn]
+    double* wdiag = bsm + nnpad;         // [2][32][32]: block b's diagonal block, row-major
+    double* wfold = wdiag + 2 * 1024;    // [2][32][64]: block b's rows, columns 32b - 64 .. 32b - 1
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nb = (nn + 31) / 32;
+    auto stage = [&](int b, int t0, int nt) {  // threads t0.. stage block b's weights
+        double* d = wdiag + (b & 1) * 1024;
+        double* f = wfold + (b & 1) * 2048;
+        for (int e = tid - t0; e < 1024; e += nt) {
+            const int r = e >> 5, c = e & 31, m = 32 * b + r;
+            d[e] = (m < nn && m >= 1 && c < r) ? W[tri(m - 1) + 32 * b + c] : 0.0;
+        }
+        for (int e = tid - t0; e < 2048; e += nt) {
+            const int r = e >> 6, q = e & 63, m = 32 * b + r, c = 32 * b - 64 + q;
+            f[e] = (m < nn && m >= 1 && c >= 0) ? W[tri(m - 1) + c] : 0.0;
+        }
+    };
+    stage(0, 0, blockDim.x);
+    __syncthreads();
+    const int i = tid >> 3, part = tid & 7;  // fold role: row of the block, 8 of its 64 columns
+    for (int b = 0; b < nb; ++b) {
+        const double* f = wfold + (b & 1) * 2048;
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int col = 8 * part + q, c = 32 * b - 64 + col;
+            if (c >= 0) sum = fma(f[i * 64 + col], ys[c], sum);
+        }
+        sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 4);
+        if (part == 0) accb[i] = sum;
+        __syncthreads();
+        if (warp == 0) {
+            const double* d = wdiag + (b & 1) * 1024;
+            const int m = 32 * b + lane;
+            double a = m == 0 ? 1.0 : (m < nn ? accb[lane] : 0.0);
+#pragma unroll
+            for (int t = 0; t < 32; ++t) {
+                const double yt = __shfl_sync(0xffffffffu, a, t);
+                if (lane > t) a = fma(d[lane * 32 + t], yt, a);
+            }
+            if (m < nn) {
+                ys[m] = a;
+                y[m] = a;
+            }
+        } else if (b + 1 < nb) {
+            stage(b + 1, 32, blockDim.x - 32);
+        }
+        __syncthreads();
+    }
+}
+
+bool banded_solve_fits(const Sys& s) { return s.N + 1 <= kBandMaxN; }
+
+size_t banded_solve_smem(const Sys& s) {
+    return sizeof(double) * ((((size_t)s.N + 2) & ~(size_t)1) + 2 * 1024 + 2 * 2048);
+}
+
+// ---------------------------------------------------------------------------
 // Pass 3 on a thread-block cluster, below the multi-SM solve's size.  On one
 // block the solve's N^2/2 FP64 multiply-adds are bound by a single SM's FP64
 // pipe (2 lanes per clock).  Here each direction runs on a cluster of C CTAs
@@ -389,10 +480,12 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
 constexpr int kClusterSolveMax = 8;
 constexpr int kClusterSolveThreads = 256;
 
-__global__ void __launch_bounds__(kClusterSolveThreads) k_exch_solve_cluster(Sys s, int phase, double* ysol) {
+__global__ void __launch_bounds__(kClusterSolveThreads) k_exch_solve_cluster(Sys s, int phase, double* ysol,
+                                                                            int banded) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;  // uniform over the cluster
+    if (banded && ((volatile int*)s.xflags)[kExchBand] <= kBandMax) return;  // k_exch_solve_band solved it
     const int C = (int)cl.num_blocks(), c = (int)cl.block_rank();
     const int dir = blockIdx.x / C;
     const int nn = dir == 0 ? s.N + 1 : s.N;
@@ -461,7 +554,7 @@ __global__ void __launch_bounds__(kClusterSolveThreads) k_exch_solve_cluster(Sys
     cl.sync();  // no CTA leaves while another may still read its y
 }
 
-static bool cluster_solve(const Sys& s, int phase, double* ysol, cudaStream_t st) {
+static bool cluster_solve(const Sys& s, int phase, double* ysol, int banded, cudaStream_t st) {
     const int nb = (s.N + 1 + 31) / 32;
     const int C = nb < kClusterSolveMax ? nb : kClusterSolveMax;
     const int nown = (nb + C - 1) / C;
@@ -477,7 +570,7 @@ static bool cluster_solve(const Sys& s, int phase, double* ysol, cudaStream_t st
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_exch_solve_cluster, s, phase, ysol) == cudaSuccess;
+    return cudaLaunchKernelEx(&cfg, k_exch_solve_cluster, s, phase, ysol, banded) == cudaSuccess;
 }
 
 // Exterior spring forces: one warp per row (bead P) or column (bead 1).
@@ -562,7 +655,7 @@ size_t exchange_grid_flags(const Sys& s) {
 }
 
 // The cooperative solve if every CTA can be resident; false otherwise.
-static bool grid_solve(const Sys& s, int phase, double* ysol, unsigned* gflags, cudaStream_t st) {
+static bool grid_solve(const Sys& s, int phase, double* ysol, unsigned* gflags, int banded, cudaStream_t st) {
     const int nb = (s.N + 1 + 31) / 32;
     const int nct = nb < kGridSolveCtas ? nb : kGridSolveCtas;
     const size_t smem = sizeof(double) * (((size_t)(nb + nct - 1) / nct) * 32 + 32);
@@ -581,8 +674,8 @@ static bool grid_solve(const Sys& s, int phase, double* ysol, unsigned* gflags, 
     }
     if (2 * nct > per) return false;
     Sys sc = s;
-    int ph = phase, n = nct;
-    void* args[] = {&sc, &ph, &ysol, &gflags, &n};
+    int ph = phase, n = nct, bd = banded;
+    void* args[] = {&sc, &ph, &ysol, &gflags, &n, &bd};
     return cudaLaunchCooperativeKernel((void*)k_exch_solve_grid, dim3(2 * nct), dim3(kGridSolveThreads), args, smem,
                                       st) == cudaSuccess;
 }
@@ -615,11 +708,22 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
     for (int phase = 0; phase < (inline_retry ? 1 : 2); ++phase) {
         k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s, phase);
         k_exch_weights<<<phase ? rgrid : wgrid, 256, 0, st>>>(s, phase);
-        // the solve on a cluster below the multi-SM solve's size, across SMs from it
-        const bool grid = ysol && (inline_retry ? cluster_solve(s, phase, ysol, st)
-                                                : gflags && grid_solve(s, phase, ysol, gflags, st));
-        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase, grid ? ysol : nullptr, inline_retry);
-        n += grid ? 4 : 3;
+        // banded weights: one CTA per direction; otherwise the solve on a
+        // cluster below the multi-SM solve's size, across SMs from it
+        int banded = 0;
+        if (ysol && banded_solve_fits(s)) {
+            const size_t bs = std::max(banded_solve_smem(s), least);
+            if (bs + 1024 > 48 * 1024)
+                cudaFuncSetAttribute(k_exch_solve_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bs);
+            k_exch_solve_band<<<2, kBandThreads, bs, st>>>(s, phase, ysol);
+            banded = 1;
+            ++n;
+        }
+        const bool dense = ysol && (inline_retry ? cluster_solve(s, phase, ysol, banded, st)
+                                                 : gflags && grid_solve(s, phase, ysol, gflags, banded, st));
+        const bool pre = banded || dense;
+        k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase, pre ? ysol : nullptr, inline_retry);
+        n += dense ? 4 : 3;
     }
     return n;
 }

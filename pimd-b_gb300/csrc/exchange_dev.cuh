@@ -222,15 +222,27 @@ __device__ __forceinline__ double weight_exp(double x, const double* tbl) {
     if (!tbl) return exp(x);
     return x < 709.0 ? exp_tang(x, tbl) : (double)INFINITY;
 }
-__device__ __forceinline__ void exch_weight(const Sys& s, int p, int u, double inv, const double* tbl = nullptr,
+// Returns whether either weight it wrote is nonzero (the solve's band: node
+// p + 1 depends on node u, backward node N - u on node N - 1 - p, both at
+// distance p + 1 - u).
+__device__ __forceinline__ bool exch_weight(const Sys& s, int p, int u, double inv, const double* tbl = nullptr,
                                             int dir = -1) {
     const double beta = s.beta_ex;
     const size_t e = tri(p) + u;
     const double E = s.E[e];
-    if (dir <= 0) s.Wf[e] = weight_exp(-beta * (E + s.Vh[u] - s.Vh[p + 1]), tbl) * inv;
+    bool nz = false;
+    if (dir <= 0) {
+        const double w = weight_exp(-beta * (E + s.Vh[u] - s.Vh[p + 1]), tbl) * inv;
+        s.Wf[e] = w;
+        nz = w != 0.0;
+    }
     // backward node r = N - u from node r' = N - 1 - p (u >= 1)
-    if (dir != 0 && u >= 1)
-        s.Wb[tri(s.N - u - 1) + (s.N - 1 - p)] = weight_exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u]), tbl) * inv;
+    if (dir != 0 && u >= 1) {
+        const double w = weight_exp(-beta * (E + s.Vbh[p + 1] - s.Vbh[u]), tbl) * inv;
+        s.Wb[tri(s.N - u - 1) + (s.N - 1 - p)] = w;
+        nz = nz || w != 0.0;
+    }
+    return nz;
 }
 // One direction's weights by the whole block (the in-block retry).
 __device__ inline void weights_direction(const Sys& s, int dir, const double* tbl) {

@@ -621,6 +621,27 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                     __syncwarp();
                     for (int k = lane; k < cnt; k += 32) {
                         const int fn = sm.nl[k];
+                        if (kMixed && !(sm.fe[fn] & 0x4000u)) {
+                            // mixed precision inside the damping radius:
+                            // double-float from the hi/lo positions, FP64 sums
+                            const int e = sm.fe[fn], il = (e >> 5) & 31, jl = e & 31;
+                            df r[D], q{0.0f, 0.0f};
+#pragma unroll
+                            for (int a = 0; a < D; ++a) {
+                                df d = dfl::add_sloppy(df{sm.xif[il][a], sm.u.lo[0][il][a]},
+                                                       df{-sm.xjf[jl][a], -sm.u.lo[1][jl][a]});
+                                if (s.pbc && fabsf(d.hi) > halfLf) d = dfl::add(d, d.hi > 0.0f ? dfl::neg(Ldf) : Ldf);
+                                r[a] = d;
+                                q = a == 0 ? dfl::sqr(d) : dfl::add_sloppy(q, dfl::sqr(d));
+                            }
+                            if (q.hi >= (float)kAzizNearMinR2 && q.hi < shell2f) {
+                                const df sc = aziz_is_far_df(q) ? aziz_far_scale_df(q, *etbl)
+                                                                : aziz_near_scale_df(q, *etbl);
+#pragma unroll
+                                for (int a = 0; a < D; ++a) g[fn - c0][a] = dfl::to_double(dfl::mul(sc, r[a]));
+                                continue;
+                            }
+                        }
                         if (kDf && !(sm.fe[fn] & 0x4000u)) {
                             // inside the damping radius, the image certain and
                             // the pair clearly inside the cutoff: double-float
@@ -718,7 +739,7 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
     for (int j = threadIdx.x; j < 256; j += blockDim.x) {
         const double v = kExp2Table256[j];
         tbl[j] = v;
-        if (kDf) {  // 2^(j/256) as a double-float (47 bits or more; bit patterns, no FP64 work)
+        if (kDf || kMixed) {  // 2^(j/256) as a double-float (47 bits or more; bit patterns, no FP64 work)
             float h, l;
             split_f32(v, h, l);
             const dfl::df n = dfl::fast_two_sum(h, l);
@@ -919,10 +940,13 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
     // on the exact FP64 path
     constexpr bool kFp64 = sizeof(R) == 8;
     const bool dfp = kFp64 && s.int_kind == POT_AZIZ;
+    // mixed precision: the Aziz pairs inside the damping radius in
+    // double-float too (FP32 would lose the cancelling terms' difference)
+    const bool dfnear = s.int_kind == POT_AZIZ;
     for (int j = threadIdx.x; j < 256; j += blockDim.x) {
         const double v = kExp2Table256[j];
         tbl[j] = v;
-        if (kFp64) {
+        if (dfnear) {
             float h, l;
             split_f32(v, h, l);
             const dfl::df n = dfl::fast_two_sum(h, l);
@@ -1010,7 +1034,9 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
         } else {
             if (s.int_kind == POT_AZIZ && r2 < near2f) {
                 // inside the damping radius the repulsive and attractive
-                // terms nearly cancel: FP64 from the FP64 positions
+                // terms nearly cancel: double-float, or FP64 from the FP64
+                // positions at the cutoff shell
+                if (eval_df(q)) return;
                 double rd[D];
                 double q2 = 0.0;
 #pragma unroll
@@ -1070,7 +1096,7 @@ __global__ void __launch_bounds__(kCellThreads) k_pair_cells(Sys s, int nc, cons
         const int i = clist[(size_t)b * N + k];
 #pragma unroll
         for (int a = 0; a < D; ++a)
-            fpair[idx<D>(s, b, a, i)] = dfp ? acc[a] + (f32_to_f64(accd[a].hi) + f32_to_f64(accd[a].lo)) : acc[a];
+            fpair[idx<D>(s, b, a, i)] = dfnear ? acc[a] + (f32_to_f64(accd[a].hi) + f32_to_f64(accd[a].lo)) : acc[a];
     }
 }
 

@@ -73,6 +73,14 @@ int exchange_flat_default(int N);
 // Index in Sys::xflags (16 ints) of the count of exchange evaluations redone
 // from a fresh estimate after the reused one failed.
 constexpr int kExchRetryCount = 10;
+// Index in Sys::xflags of the solve's band: the largest node distance p + 1
+// - u of a nonzero weight of the current evaluation (0 between evaluations).
+constexpr int kExchBand = 11;
+// The banded solve: weights within kBandMax levels of the diagonal, one CTA
+// of kBandThreads per direction, y of up to kBandMaxN nodes in shared memory.
+constexpr int kBandMax = 64;
+constexpr int kBandThreads = 256;
+constexpr int kBandMaxN = 8192;
 // The cotangent of V_B on beads 1 and P into fx: vb_bar * dV_B/dx (the
 // exterior spring forces' exchange part times -vb_bar).
 void launch_exchange_adjoint(const Sys& s, int D, double vb_bar, cudaStream_t st);
