@@ -90,61 +90,172 @@ __device__ __forceinline__ void block_sum_axes(double* v, double* sh) {
 //   o:       p = c1 p + c2 xi (substep)
 //   drift:   x += dt p / m
 // Returns the per-axis sums of the new p in `sum` (this thread's share).
+// The pair (2 i2, 2 i2 + 1) is one aligned 16-byte word of each array (the
+// leading dimension is a multiple of 32 and every array starts on 256
+// bytes; for odd N the second element of the last pair is padding, loaded
+// and stored back unchanged).  Each thread loads kPassUnroll pairs of every
+// array it touches before it computes any of them: the passes stream state
+// that left L2 a step ago, and one pair's loads in flight per thread leave
+// them latency-bound.  The elements are taken in the same per-thread order
+// as one pair at a time (the same sums, bit for bit).
+constexpr int kPassUnroll = 4;
 template <int D, typename R>
 __device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int substep, const double* cm, bool com_in,
                                              bool kick, bool o, bool drift, double* sum) {
-    const int H = (s.N + 1) / 2;
-    const int total = s.P * H;
+    const int N = s.N, H = (N + 1) / 2;
+    const int total = s.P * H, stride = blockDim.x;
     // loop constants kept in registers (opaque: not recomputed per element)
     double hdt = 0.5 * s.dt, c1 = s.c1, c2 = s.c2, dt_m = s.dt_m;
     asm volatile("" : "+d"(hdt), "+d"(c1), "+d"(c2), "+d"(dt_m));
-#pragma unroll
+#pragma unroll 1
     for (int a = 0; a < D; ++a) {
-        sum[a] = 0.0;
-        for (int q = threadIdx.x; q < total; q += blockDim.x) {
-            const int b = q / H, i2 = q - b * H;
-            double z0 = 0.0, z1 = 0.0;
-            if (o) normal_pair<R>(s, step, substep, (uint32_t)((b * D + a) * H + i2), z0, z1);
+        double sa = 0.0;
+        const double cma = com_in ? cm[a] : 0.0;
+        for (int q0 = threadIdx.x; q0 < total; q0 += kPassUnroll * stride) {
+            double2 pv[kPassUnroll], fv[kPassUnroll], xv[kPassUnroll];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int i = 2 * i2 + h;
-                if (i >= s.N) break;
-                const size_t e = idx<D>(s, b, a, i);
-                double p = s.p[e];
-                if (com_in) p -= cm[a];
-                if (kick) p += hdt * s.f[e];
-                if (o) p = c1 * p + c2 * (h == 0 ? z0 : z1);
-                if (drift) s.x[e] = fma(p, dt_m, s.x[e]);
-                s.p[e] = p;
-                sum[a] += p;
+            for (int k = 0; k < kPassUnroll; ++k) {
+                const int q = min(q0 + k * stride, total - 1);  // past the end: a repeat, not stored
+                const int b = q / H, i2 = q - b * H;
+                const size_t e = idx<D>(s, b, a, 2 * i2);
+                pv[k] = *reinterpret_cast<const double2*>(s.p + e);
+                if (kick) fv[k] = *reinterpret_cast<const double2*>(s.f + e);
+                if (drift) xv[k] = *reinterpret_cast<const double2*>(s.x + e);
             }
+#pragma unroll
+            for (int k = 0; k < kPassUnroll; ++k) {
+                const int q = q0 + k * stride;
+                if (q < total) {
+                    const int b = q / H, i2 = q - b * H;
+                    const size_t e = idx<D>(s, b, a, 2 * i2);
+                    const bool two = 2 * i2 + 1 < N;
+                    double z0 = 0.0, z1 = 0.0;
+                    if (o) normal_pair<R>(s, step, substep, (uint32_t)((b * D + a) * H + i2), z0, z1);
+                    double p0 = pv[k].x, p1 = pv[k].y;
+                    if (com_in) {
+                        p0 -= cma;
+                        p1 -= cma;
+                    }
+                    if (kick) {
+                        p0 += hdt * fv[k].x;
+                        p1 += hdt * fv[k].y;
+                    }
+                    if (o) {
+                        p0 = c1 * p0 + c2 * z0;
+                        p1 = c1 * p1 + c2 * z1;
+                    }
+                    if (!two) p1 = pv[k].y;  // padding: unchanged
+                    if (drift)
+                        *reinterpret_cast<double2*>(s.x + e) =
+                            make_double2(fma(p0, dt_m, xv[k].x), two ? fma(p1, dt_m, xv[k].y) : xv[k].y);
+                    *reinterpret_cast<double2*>(s.p + e) = make_double2(p0, p1);
+                    sa += p0;
+                    if (two) sa += p1;
+                }
+            }
+        }
+        sum[a] = sa;
+    }
+}
+
+// Bytes of one particle's staged position: FP64, x y | z (one 16-byte and
+// one 8-byte shared load per pair in 3D); mixed, hx hy hz lx | ly lz.
+template <int D>
+__host__ __device__ constexpr int stage_bytes() { return D == 3 ? 32 : 8 * D; }
+
+template <int D, typename R>
+__device__ __forceinline__ void stage_put(unsigned char* st, int j, const double* x) {
+    unsigned char* q = st + (size_t)j * stage_bytes<D>();
+    if constexpr (sizeof(R) == 8) {
+        if constexpr (D == 3) {
+            *reinterpret_cast<double2*>(q) = make_double2(x[0], x[1]);
+            *reinterpret_cast<double*>(q + 16) = x[2];
+        } else if constexpr (D == 2) {
+            *reinterpret_cast<double2*>(q) = make_double2(x[0], x[1]);
+        } else {
+            *reinterpret_cast<double*>(q) = x[0];
+        }
+    } else {
+        float h[D], l[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) split_f32(x[a], h[a], l[a]);  // no FP64-pipe instruction
+        if constexpr (D == 3) {
+            *reinterpret_cast<float4*>(q) = make_float4(h[0], h[1], h[2], l[0]);
+            *reinterpret_cast<float2*>(q + 16) = make_float2(l[1], l[2]);
+        } else if constexpr (D == 2) {
+            *reinterpret_cast<float4*>(q) = make_float4(h[0], h[1], l[0], l[1]);
+        } else {
+            *reinterpret_cast<float2*>(q) = make_float2(h[0], l[0]);
+        }
+    }
+}
+
+template <int D, typename R>
+__device__ __forceinline__ void stage_get(const unsigned char* st, int j, R* h, R* l) {
+    const unsigned char* q = st + (size_t)j * stage_bytes<D>();
+    if constexpr (sizeof(R) == 8) {
+        if constexpr (D == 3) {
+            const double2 v = *reinterpret_cast<const double2*>(q);
+            h[0] = v.x;
+            h[1] = v.y;
+            h[2] = *reinterpret_cast<const double*>(q + 16);
+        } else if constexpr (D == 2) {
+            const double2 v = *reinterpret_cast<const double2*>(q);
+            h[0] = v.x;
+            h[1] = v.y;
+        } else {
+            h[0] = *reinterpret_cast<const double*>(q);
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) l[a] = 0.0;
+    } else {
+        if constexpr (D == 3) {
+            const float4 v = *reinterpret_cast<const float4*>(q);
+            const float2 w = *reinterpret_cast<const float2*>(q + 16);
+            h[0] = v.x;
+            h[1] = v.y;
+            h[2] = v.z;
+            l[0] = v.w;
+            l[1] = w.x;
+            l[2] = w.y;
+        } else if constexpr (D == 2) {
+            const float4 v = *reinterpret_cast<const float4*>(q);
+            h[0] = v.x;
+            h[1] = v.y;
+            l[0] = v.z;
+            l[1] = v.w;
+        } else {
+            const float2 v = *reinterpret_cast<const float2*>(q);
+            h[0] = v.x;
+            l[0] = v.y;
         }
     }
 }
 
 // Physical forces of bead b plus its interior springs, by one warp.  The
-// bead's positions are staged in `stage` (D N doubles for R = double; hi
-// and lo floats, D N each, for R = float).  Bosonic end beads keep the
-// physical part only: the exchange adds their springs.
+// bead's positions are staged in `stage` (N slots of stage_bytes<D>()).
+// Bosonic end beads keep the physical part only: the exchange adds their
+// springs.  Global loads are issued in groups (kStageUnroll particles per
+// lane when staging; a particle's own and both neighbour positions at once)
+// so that a warp waits once per group rather than once per load.
+constexpr int kStageUnroll = 4;
 template <int D, typename R>
-__device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
+__device__ void bead_forces_warp(const Sys& s, int b, int lane, unsigned char* stage) {
     const int N = s.N;
     const bool pairs = s.int_kind != POT_FREE && s.cutoff != 0.0;
-    R* sh = stage;
-    R* sl = stage + D * N;
     if (pairs) {
-        for (int a = 0; a < D; ++a)
-            for (int j = lane; j < N; j += 32) {
-                const double x = s.x[idx<D>(s, b, a, j)];
-                if constexpr (sizeof(R) == 8) {
-                    sh[a * N + j] = x;
-                } else {
-                    float h, l;
-                    split_f32(x, h, l);  // no FP64-pipe instruction
-                    sh[a * N + j] = h;
-                    sl[a * N + j] = l;
-                }
+        for (int j0 = lane; j0 < N; j0 += 32 * kStageUnroll) {
+            double xs[kStageUnroll][D];
+#pragma unroll
+            for (int k = 0; k < kStageUnroll; ++k) {
+                const int j = min(j0 + 32 * k, N - 1);  // past the end: a repeat, not stored
+#pragma unroll
+                for (int a = 0; a < D; ++a) xs[k][a] = s.x[idx<D>(s, b, a, j)];
             }
+#pragma unroll
+            for (int k = 0; k < kStageUnroll; ++k)
+                if (j0 + 32 * k < N) stage_put<D, R>(stage, j0 + 32 * k, xs[k]);
+        }
         __syncwarp();
     }
     const double cut = s.cutoff;
@@ -159,18 +270,36 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
     const bool bosonic_bead = s.bosonic && (b == 0 || b == s.P - 1);
     const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
     for (int i = lane; i < N; i += 32) {
-        double xi[D];
+        double xi[D], xp[D], xn[D];
 #pragma unroll
-        for (int a = 0; a < D; ++a) xi[a] = s.x[idx<D>(s, b, a, i)];
+        for (int a = 0; a < D; ++a) {
+            xi[a] = s.x[idx<D>(s, b, a, i)];
+            if (!bosonic_bead) {
+                xp[a] = s.x[idx<D>(s, bp, a, i)];
+                xn[a] = s.x[idx<D>(s, bn, a, i)];
+            }
+        }
+        // the interior springs' separations (simulation.cpp:405-419), added
+        // after the physical forces as before
+        double sp[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            sp[a] = 0.0;
+            if (!bosonic_bead) {
+                double dp = xp[a] - xi[a];
+                double dn = xn[a] - xi[a];
+                if (s.pbc) {
+                    dp = min_image(dp, s.L, s.invL);
+                    dn = min_image(dn, s.L, s.invL);
+                }
+                sp[a] = dp + dn;
+            }
+        }
         double acc[D];
         ext_force<D>(s, xi, acc);
         if (pairs) {
             R hi[D], lo[D];
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-                hi[a] = sh[a * N + i];
-                lo[a] = (sizeof(R) == 8) ? (R)0 : sl[a * N + i];
-            }
+            stage_get<D, R>(stage, i, hi, lo);
             // FP32: the 32-pair partial sums are added up error-free in two
             // floats (Knuth's two-sum), so the FP64 pipe is not touched
             // until the particle's total
@@ -185,16 +314,18 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
 #pragma unroll 4
                 for (int jj = 0; jj < jn; ++jj) {
                     const int j = j0 + jj;
+                    R hj[D], lj[D];
+                    stage_get<D, R>(stage, j, hj, lj);
                     R r[D];
                     R r2 = (R)0;
 #pragma unroll
                     for (int a = 0; a < D; ++a) {
                         R d;
                         if constexpr (sizeof(R) == 8) {
-                            d = hi[a] - sh[a * N + j];
+                            d = hi[a] - hj[a];
                             if (s.pbc) d = min_image(d, s.L, s.invL);
                         } else {
-                            d = (hi[a] - sh[a * N + j]) + (lo[a] - sl[a * N + j]);
+                            d = (hi[a] - hj[a]) + (lo[a] - lj[a]);
                             if (s.pbc) d = min_image_f(d, (float)s.L, (float)s.invL);
                         }
                         r[a] = d;
@@ -227,26 +358,190 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, R* stage) {
 #pragma unroll
         for (int a = 0; a < D; ++a) {
             const size_t o = idx<D>(s, b, a, i);
-            if (bosonic_bead) {
-                s.f[o] = acc[a];
-            } else {
-                double dp = s.x[idx<D>(s, bp, a, i)] - xi[a];
-                double dn = s.x[idx<D>(s, bn, a, i)] - xi[a];
-                if (s.pbc) {
-                    dp = min_image(dp, s.L, s.invL);
-                    dn = min_image(dn, s.L, s.invL);
-                }
-                s.f[o] = s.kappa * (dp + dn) + acc[a];  // simulation.cpp:405-419, :363-373
-            }
+            s.f[o] = bosonic_bead ? acc[a] : s.kappa * sp[a] + acc[a];  // simulation.cpp:363-373
         }
     }
     __syncwarp();
 }
 
+// ------------------------------------------------ mixed-precision exchange
+// This GPU's FP64 pipe finishes about one warp-wide FP64 instruction per 16
+// SM cycles, against 4 FP32 ones per cycle, so the mixed path moves the two
+// largest FP64 parts of the exchange to the FP32 pipe: the weights in
+// double-float (about 2^-44 relative) and the exterior spring forces in FP32
+// with compensated sums (about 2e-7 relative per term).  The potentials, the
+// triangular solve and the energies stay FP64, as on the FP64 path.
+
+// A double as a normalised double-float, by bit patterns (no FP64 or
+// conversion-pipe instruction).
+__device__ __forceinline__ dfl::df split_df(double x) {
+    float h, l;
+    split_f32(x, h, l);
+    return dfl::fast_two_sum(h, l);
+}
+// A double rounded to float (to within 2^-24 ulp of round-to-nearest).
+__device__ __forceinline__ float round_f32(double x) {
+    float h, l;
+    split_f32(x, h, l);
+    return h + l;
+}
+// The double of a double-float: the one FP64 instruction of the conversion.
+__device__ __forceinline__ double df_to_f64(dfl::df v) { return f32_to_f64(v.hi) + f32_to_f64(v.lo); }
+// Whether a double is +-0 (integer compare, not a DSETP).
+__device__ __forceinline__ bool f64_is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+
+// The weights of every packed entry (row p, column u), both directions, as
+// exch_weight computes them, in double-float: w = exp(-beta (E + Vh_u -
+// Vh_{p+1})) / (p + 1) forward, exp(-beta (E + Vbh_{p+1} - Vbh_u)) / (p + 1)
+// backward.  Arguments above 88 give infinity (the solve then retries with a
+// fresh estimate or the exact recursion), below -88 zero (a weight under
+// 1e-38 of the ones that normalise the row).  `vsm` holds 4 (N + 1) floats.
+__device__ void batch_weights_df(const Sys& s, const dfl::ExpTable& etbl, float* vsm) {
+    using dfl::df;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int N = s.N;
+    float* vh = vsm;               // Vh hi, lo
+    float* vbh = vsm + 2 * (N + 1);  // Vbh hi, lo
+    for (int m = threadIdx.x; m <= N; m += blockDim.x) {
+        split_f32(s.Vh[m], vh[m], vh[N + 1 + m]);
+        split_f32(s.Vbh[m], vbh[m], vbh[N + 1 + m]);
+    }
+    __syncthreads();
+    const df nbeta = dfl::neg(split_df(s.beta_ex));
+    for (int p = warp; p < N; p += nw) {
+        const df inv = split_df(recip_row(p));
+        const df vp = dfl::fast_two_sum(vh[p + 1], vh[N + 2 + p]);
+        const df vbp = dfl::fast_two_sum(vbh[p + 1], vbh[N + 2 + p]);
+        const size_t r = tri(p);
+        for (int u = lane; u <= p; u += 32) {
+            const df E = split_df(s.E[r + u]);
+            const df vu = dfl::fast_two_sum(vh[u], vh[N + 1 + u]);
+            const df tf = dfl::add(dfl::add(E, vu), dfl::neg(vp));
+            s.Wf[r + u] = df_to_f64(dfl::mul(dfl::exp(dfl::mul(nbeta, tf), etbl), inv));
+            if (u >= 1) {
+                const df vbu = dfl::fast_two_sum(vbh[u], vbh[N + 1 + u]);
+                const df tb = dfl::add(dfl::add(E, vbp), dfl::neg(vbu));
+                s.Wb[tri(N - u - 1) + (N - 1 - p)] = df_to_f64(dfl::mul(dfl::exp(dfl::mul(nbeta, tb), etbl), inv));
+            }
+        }
+    }
+}
+
+// Shared floats batch_exchange_forces_f32 stages.
+__host__ __device__ constexpr size_t xforces_f32_floats(int D, int N) { return 4 * (size_t)D * N + 3 * (size_t)N; }
+
+// The exterior spring forces of exch_force_row (accumulated into f) in FP32:
+// probabilities Wf y R and 1 - C rounded to float, separations from hi/lo
+// floats, each lane's terms and the warp's lanes summed with two-sum error
+// terms.  Lanes 0..D-1 add the interior neighbour spring and write axis
+// a = lane: one FP64 add per row joins the result to f.
+template <int D>
+__device__ void batch_exchange_forces_f32(const Sys& s, float* sm) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int N = s.N, P = s.P;
+    float* xh = sm;  // (side D + a) N + i; side 0 bead 1, 1 bead P
+    float* xl = xh + 2 * D * N;
+    float* yv = xl + 2 * D * N;  // y_l
+    float* rr = yv + N;          // R_l
+    float* cc = rr + N;          // 1 - C_l
+    for (int e = threadIdx.x; e < 2 * D * N; e += blockDim.x) {
+        const int side = e / (D * N), a = (e / N) % D, i = e % N;
+        split_f32(s.x[idx<D>(s, side ? P - 1 : 0, a, i)], xh[e], xl[e]);
+    }
+    for (int l = threadIdx.x; l < N; l += blockDim.x) {
+        yv[l] = round_f32(s.yf[l]);
+        rr[l] = round_f32(s.rowR[l]);
+        cc[l] = round_f32(1.0 - s.rowC[l]);
+    }
+    __syncthreads();
+    const float Lf = round_f32(s.L), invLf = round_f32(s.invL), kf = round_f32(s.kappa);
+    for (int w = warp; w < 2 * N; w += nw) {
+        const bool lastb = w < N;  // bead P, particle l (row l); else bead 1 (column l)
+        const int l = lastb ? w : w - N, side = lastb ? 1 : 0, other = 1 - side;
+        float ph[D], pl[D], sh[D], sl[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            ph[a] = xh[(side * D + a) * N + l];
+            pl[a] = xl[(side * D + a) * N + l];
+            sh[a] = sl[a] = 0.0f;
+        }
+        auto add_term = [&](float pr, int n) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                float d = (xh[(other * D + a) * N + n] - ph[a]) + (xl[(other * D + a) * N + n] - pl[a]);
+                if (s.pbc) d = min_image_f(d, Lf, invLf);
+                const float t = pr * d;
+                const float sum = sh[a] + t, bb = sum - sh[a];
+                sl[a] += (sh[a] - (sum - bb)) + (t - bb);
+                sh[a] = sum;
+            }
+        };
+        if (lastb) {  // n <= l + 1: close-cycle entries, then the direct link
+            const size_t r = tri(l);
+            const float Rl = rr[l];
+            const int nmax = min(l + 1, N - 1);
+            for (int n = lane; n <= nmax; n += 32) {
+                if (n <= l) {
+                    const double wd = s.Wf[r + n];
+                    if (f64_is_zero(wd)) continue;  // a cycle too costly to contribute adds exactly 0
+                    add_term(round_f32(wd) * yv[n] * Rl, n);
+                } else {
+                    add_term(cc[l], n);
+                }
+            }
+        } else {  // q >= l - 1: the direct link, then close-cycle entries
+            const float yl = yv[l];
+            for (int q = max(0, l - 1) + lane; q < N; q += 32) {
+                if (q >= l) {
+                    const double wd = s.Wf[tri(q) + l];
+                    if (f64_is_zero(wd)) continue;
+                    add_term(round_f32(wd) * yl * rr[q], q);
+                } else {
+                    add_term(cc[q], q);
+                }
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, sh[a], o), ol = __shfl_xor_sync(0xffffffffu, sl[a], o);
+                const float sum = sh[a] + oh, bb = sum - sh[a];
+                sl[a] = (sl[a] + ol) + ((sh[a] - (sum - bb)) + (oh - bb));
+                sh[a] = sum;
+            }
+        }
+        if (lane < D) {
+            const int a = lane;
+            float hs = sh[0], ls = sl[0], hb = ph[0], lb = pl[0];
+#pragma unroll
+            for (int k = 1; k < D; ++k)
+                if (a == k) {
+                    hs = sh[k];
+                    ls = sl[k];
+                    hb = ph[k];
+                    lb = pl[k];
+                }
+            const int bead = lastb ? P - 1 : 0, nb = lastb ? (P - 2 + P) % P : 1 % P;
+            float nh, nl;
+            split_f32(s.x[idx<D>(s, nb, a, l)], nh, nl);
+            float d = (nh - hb) + (nl - lb);
+            if (s.pbc) d = min_image_f(d, Lf, invLf);
+            const float fs = kf * ((hs + d) + ls);
+            const size_t o = idx<D>(s, bead, a, l);
+            const double fsd = f32_to_f64(fs);
+            s.fx[((size_t)side * D + a) * s.ld + l] = fsd;
+            s.f[o] = fsd + s.f[o];
+        }
+    }
+}
+
 // The Feldman-Hirshberg exchange of one replica by the whole block; adds the
 // exterior springs to f on beads 1 and P (which hold the physical forces).
-template <int D>
-__device__ void batch_exchange(const Sys& s, unsigned char* work, const double* tbl) {
+// R = float: weights and exterior forces on the FP32 pipe (above).
+template <int D, typename R>
+__device__ void batch_exchange(const Sys& s, unsigned char* work, const double* tbl, const dfl::ExpTable* etbl) {
+    constexpr bool kMixed = sizeof(R) == 4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int N = s.N;
     // the interior links |x1_{u+1} - xP_u|^2 once per u (shared memory),
@@ -265,9 +560,13 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
             estimate_direction(s, 1, reinterpret_cast<float*>(work));
             __syncthreads();
         }
-        for (int p = warp; p < N; p += nw) {
-            const double inv = recip_row(p);
-            for (int u = lane; u <= p; u += 32) exch_weight(s, p, u, inv, tbl);
+        if (kMixed) {
+            batch_weights_df(s, *etbl, reinterpret_cast<float*>(work));
+        } else {
+            for (int p = warp; p < N; p += nw) {
+                const double inv = recip_row(p);
+                for (int u = lane; u <= p; u += 32) exch_weight(s, p, u, inv, tbl);
+            }
         }
         __syncthreads();
         // a reused estimate that fails is replaced by a fresh one (second
@@ -284,6 +583,12 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
         __syncthreads();
     }
     solve_finish(s);
+    // the exact fallback's probabilities come from their exponentials: FP64 rows
+    if (kMixed && !((volatile int*)s.xflags)[0]) {
+        __syncthreads();
+        batch_exchange_forces_f32<D>(s, reinterpret_cast<float*>(work));
+        return;
+    }
     // beads 1 and P staged in the (now free) shared scratch for the forces
     double* xs = reinterpret_cast<double*>(work);
     for (int e = threadIdx.x; e < 2 * D * N; e += blockDim.x) {
@@ -296,7 +601,7 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
 
 template <int D, typename R>
 __device__ void batch_replica(const Sys& s, int flags, long long step, int mode, double* red, unsigned char* work,
-                              const double* tbl) {
+                              const double* tbl, const dfl::ExpTable* etbl) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const bool langevin = flags & BF_LANGEVIN, fixcom = flags & BF_FIXCOM;
     const double inv_np = 1.0 / ((double)s.N * s.P);
@@ -318,11 +623,11 @@ __device__ void batch_replica(const Sys& s, int flags, long long step, int mode,
         __syncthreads();
     }
     if (mode & BM_FORCES) {
-        R* stage = reinterpret_cast<R*>(work) + (size_t)warp * ((sizeof(R) == 8 ? 1 : 2) * D * s.N);
+        unsigned char* stage = work + (size_t)warp * stage_bytes<D>() * s.N;
         for (int b = warp; b < s.P; b += nw) bead_forces_warp<D, R>(s, b, lane, stage);
         __syncthreads();
         if (s.bosonic) {
-            batch_exchange<D>(s, work, tbl);
+            batch_exchange<D, R>(s, work, tbl, etbl);
             __syncthreads();
         }
     }
@@ -355,7 +660,14 @@ __global__ void __launch_bounds__(kBatchMaxThreads)
     __shared__ Sys ss;
     __shared__ int item, sflags;
     __shared__ double tbl[32];  // exp_tang's table
+    __shared__ dfl::ExpTable etbl;  // mixed: 2^(j/256) as double-floats (bit patterns)
     if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
+    if (sizeof(R) == 4)
+        for (int j = threadIdx.x; j < 256; j += blockDim.x) {
+            const dfl::df v = split_df(kExp2Table256[j]);
+            etbl.hi[j] = v.hi;
+            etbl.lo[j] = v.lo;
+        }
     const long long step = *(volatile long long*)step_ctr;
     for (;;) {
         if (threadIdx.x == 0) item = atomicAdd(&ctl[0], 1);
@@ -367,7 +679,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads)
         }
         __syncthreads();
         if (k >= nrep) break;
-        batch_replica<D, R>(ss, sflags, step, mode, red, work, tbl);
+        batch_replica<D, R>(ss, sflags, step, mode, red, work, tbl, &etbl);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -475,12 +787,14 @@ static int bfail(pimdb_batch* b, int code, const std::string& msg) {
 
 static size_t batch_smem(int D, int maxN, int threads) {
     const size_t nw = threads / 32;
-    const size_t stage = nw * (size_t)D * maxN * sizeof(double);
+    const size_t stage = nw * (size_t)maxN * (D == 3 ? stage_bytes<3>() : D == 2 ? stage_bytes<2>() : stage_bytes<1>());
     const size_t est = sizeof(float) * 3 * (size_t)(maxN + 1);
     const size_t solve = sizeof(double) * (2 * (size_t)(maxN + 1) + 32);
     const size_t xforces = sizeof(double) * 2 * (size_t)D * maxN;  // beads 1 and P for the exchange forces
+    const size_t xforces32 = sizeof(float) * std::max(xforces_f32_floats(D, maxN), 4 * (size_t)(maxN + 1));
     const size_t estim = sizeof(double) * ((size_t)maxN + 1 + 32);
-    return 3 * 32 * sizeof(double) + std::max(std::max(std::max(stage, est), std::max(solve, estim)), xforces);
+    return 3 * 32 * sizeof(double) +
+           std::max(std::max(std::max(stage, est), std::max(solve, estim)), std::max(xforces, xforces32));
 }
 
 template <typename F>
