@@ -235,6 +235,12 @@ int pimdb_exchange_forward(pimdb_handle* h, double* VB);
  * particles and per evaluation above.  Smooth dynamics keep it near 0; each
  * retry costs a slower evaluation, not accuracy. */
 int pimdb_exchange_retries(pimdb_handle* h, long long* count);
+/* Diagnostic (no counterpart in the reference): how many exchange
+ * evaluations since creation began with a fresh FP32 estimate of V (the
+ * first one, and those after a solve found the reused potentials more than
+ * 30 kT off), counted below 768 particles by the estimate kernel of the
+ * first pass only (not the in-block retries pimdb_exchange_retries counts). */
+int pimdb_exchange_fresh_estimates(pimdb_handle* h, long long* count);
 int pimdb_exchange_adjoint(pimdb_handle* h, double vb_bar, double* x1_bar, double* xP_bar);
 int pimdb_exchange_dbeta(pimdb_handle* h, double* dbeta);
 
@@ -332,7 +338,13 @@ int pimdb_profile(pimdb_handle* h, int enable, double* ms, long long* counts, lo
  *                    warp (a multiple of 32 up to 1024; 0 = default).  Fewer
  *                    let more warps share an SM; a tile with more pairs
  *                    inside the cutoff is summed in chunks (same result up to
- *                    the order of its j-side additions). */
+ *                    the order of its j-side additions);
+ *   "reserved_sms"   pair-tile kernel beside the bosonic exchange: how many
+ *                    SMs (the highest ids) its blocks leave to the
+ *                    exchange's one-block passes (-1 = automatic: 2 below 768
+ *                    particles, else 0).  Blocks placed there take no tile;
+ *                    the warp that finishes last takes any tile still left,
+ *                    so any value gives the same forces. */
 int pimdb_set_option(pimdb_handle* h, const char* name, int value);
 
 /* Bosonic exchange without any allocation (no counterpart in the reference).

@@ -32,6 +32,7 @@ EXPORTS = [
     "pimdb_compute_forces", "pimdb_step", "pimdb_step_async", "pimdb_synchronize", "pimdb_exchange",
     "pimdb_exchange_arrays", "pimdb_exchange_forward", "pimdb_exchange_adjoint", "pimdb_exchange_dbeta",
     "pimdb_exchange_retries",
+    "pimdb_exchange_fresh_estimates",
     "pimdb_last_error", "pimdb_status_string", "pimdb_profile",
     "pimdb_measure_fp64_peak", "pimdb_measure_fp32_peak", "pimdb_math_check", "pimdb_set_option", "pimdb_thermostat_step", "pimdb_zero_momentum",
     "pimdb_propagate", "pimdb_compute_observables", "pimdb_potential_energy", "pimdb_local_energy", "pimdb_batch_create", "pimdb_batch_destroy", "pimdb_batch_size", "pimdb_batch_set_states",
@@ -104,6 +105,7 @@ def lib():
             "pimdb_exchange_adjoint": ([vp, C.c_double, vp, vp], C.c_int),
             "pimdb_exchange_dbeta": ([vp, vp], C.c_int),
             "pimdb_exchange_retries": ([vp, C.POINTER(C.c_longlong)], C.c_int),
+            "pimdb_exchange_fresh_estimates": ([vp, C.POINTER(C.c_longlong)], C.c_int),
             "pimdb_last_error": ([vp, C.c_char_p, C.c_int], C.c_int),
             "pimdb_status_string": ([C.c_int], C.c_char_p),
             "pimdb_profile": ([vp, C.c_int, vp, vp, vp], C.c_int),
@@ -401,6 +403,12 @@ class System:
         """Exchange evaluations redone from a fresh estimate since creation."""
         v = C.c_longlong()
         _check(lib().pimdb_exchange_retries(self._h, C.byref(v)), self._h)
+        return v.value
+
+    def exchange_fresh_estimates(self) -> int:
+        """Exchange evaluations that began with a fresh FP32 estimate."""
+        v = C.c_longlong()
+        _check(lib().pimdb_exchange_fresh_estimates(self._h, C.byref(v)), self._h)
         return v.value
 
     def exchange_arrays(self):

@@ -62,6 +62,7 @@ struct pimdb_handle {
     int opt_fft = 1;
     cudaError_t async_err = cudaSuccess;
     int opt_newton3 = 1;
+    int opt_reserved_sms = -1;  // SMs the pair tiles leave to the exchange (-1: by exchange size)
     // cell lists (periodic box with a short cutoff): cells per edge, work
     // buffer, and the option (-1 automatic: on when nc >= 4 and N >= 512)
     int cell_nc = 0;
@@ -277,6 +278,7 @@ void sys_params_from_config(const pimdb_config& c, Sys& s) {
     s.omega_p = c.nbeads / (beta * 1.0);
     s.kappa = c.mass * s.omega_p * s.omega_p;
     s.beta_ex = beta / c.nbeads;  // bosonic_exchange_base.cpp:16-18
+    s.inv_beta_ex = 1.0 / s.beta_ex;
     // langevin.cpp:11-12, params.cpp:17-20
     const double gamma = c.gamma < 0 ? 1 / (100.0 * c.dt) : c.gamma;
     s.c1 = std::exp(-0.5 * gamma * c.dt);
@@ -750,7 +752,8 @@ static void enqueue_forces(pimdb_handle* h) {
     // With the pair tiles and the exchange on two streams, the tiles leave
     // SMs to the exchange's one-block passes (estimate, solve), whose
     // sequential chains would otherwise share the FP64 pipes with them.
-    h->s.reserve_sms = fork && tiles ? exchange_reserved_sms(s) : 0;
+    h->s.reserve_sms =
+        fork && tiles ? (h->opt_reserved_sms >= 0 ? h->opt_reserved_sms : exchange_reserved_sms(s)) : 0;
     if (s.bosonic) {
         exchange_front(h, xs);
         if (fx_in_finish) exchange_forces(h, 0, xs);
@@ -1194,6 +1197,17 @@ extern "C" int pimdb_exchange_retries(pimdb_handle* h, long long* count) {
     return PIMDB_OK;
 }
 
+extern "C" int pimdb_exchange_fresh_estimates(pimdb_handle* h, long long* count) {
+    if (!h || !count) return PIMDB_ERR_ARG;
+    *count = 0;
+    if (!h->s.bosonic || h->factorial) return PIMDB_OK;
+    int v = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&v, h->s.xflags + kExchFreshCount, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    *count = v;
+    return PIMDB_OK;
+}
+
 extern "C" int pimdb_exchange_forward(pimdb_handle* h, double* VB) {
     if (!h) return PIMDB_ERR_ARG;
     int st = fh_exchange_only(h, "pimdb_exchange_forward");
@@ -1522,6 +1536,8 @@ extern "C" int pimdb_set_option(pimdb_handle* h, const char* name, int value) {
         h->opt_graph = value ? 1 : 0;
     } else if (n == "flat_energies") {
         h->s.eflat = value < 0 ? exchange_flat_default(h->s.N) : (value ? 1 : 0);
+    } else if (n == "reserved_sms") {
+        h->opt_reserved_sms = value < 0 ? -1 : value;
     } else if (n == "pair_entry_cap") {
         if (value < 0 || value > 1024 || value % 32)
             return fail(h, PIMDB_ERR_ARG, "pair_entry_cap must be 0 or a multiple of 32 up to 1024");

@@ -571,9 +571,9 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
         __syncthreads();
         // a reused estimate that fails is replaced by a fresh one (second
         // attempt) rather than by the exact recursion
-        solve_direction(s, 0, 0, reinterpret_cast<double*>(work), fresh);
+        solve_direction(s, 0, 0, reinterpret_cast<double*>(work), fresh, nullptr, 1, etbl);
         __syncthreads();
-        solve_direction(s, 1, 0, reinterpret_cast<double*>(work), fresh);
+        solve_direction(s, 1, 0, reinterpret_cast<double*>(work), fresh, nullptr, 1, etbl);
         __syncthreads();
         const int retry = ((volatile int*)s.xflags)[6];
         __syncthreads();
@@ -582,7 +582,7 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
         fresh = 1;
         __syncthreads();
     }
-    solve_finish(s);
+    solve_finish(s, 0, etbl);
     // the exact fallback's probabilities come from their exponentials: FP64 rows
     if (kMixed && !((volatile int*)s.xflags)[0]) {
         __syncthreads();
@@ -660,14 +660,9 @@ __global__ void __launch_bounds__(kBatchMaxThreads)
     __shared__ Sys ss;
     __shared__ int item, sflags;
     __shared__ double tbl[32];  // exp_tang's table
-    __shared__ dfl::ExpTable etbl;  // mixed: 2^(j/256) as double-floats (bit patterns)
+    __shared__ dfl::ExpTable etbl;  // 2^(j/256) as double-floats (bit patterns)
     if (threadIdx.x < 32) tbl[threadIdx.x] = kExp2Table[threadIdx.x];
-    if (sizeof(R) == 4)
-        for (int j = threadIdx.x; j < 256; j += blockDim.x) {
-            const dfl::df v = split_df(kExp2Table256[j]);
-            etbl.hi[j] = v.hi;
-            etbl.lo[j] = v.lo;
-        }
+    fill_exp_table_df(etbl);
     const long long step = *(volatile long long*)step_ctr;
     for (;;) {
         if (threadIdx.x == 0) item = atomicAdd(&ctl[0], 1);

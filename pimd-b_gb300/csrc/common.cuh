@@ -40,6 +40,7 @@ struct Sys {
     double dt_m;    // dt / mass (the drift multiplies: FP64 division costs ~8 FP64 operations)
     double kappa;   // spring constant m omega_p^2
     double beta_ex; // exchange beta = beta/P
+    double inv_beta_ex;  // 1 / beta_ex
     double omega_p;
     double c1, c2;  // Langevin friction and noise coefficients
     double cutoff;  // effective pair cutoff: 0 none, < 0 all pairs

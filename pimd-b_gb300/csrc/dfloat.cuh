@@ -44,6 +44,7 @@ DF_HD float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 DF_HD float bits_to_float(int b) { return __int_as_float(b); }
 DF_HD int float_to_bits(float f) { return __float_as_int(f); }
 DF_HD float rsqrt_approx(float x) { return rsqrtf(x); }
+DF_HD float log_approx(float x) { return logf(x); }
 #else
 DF_HD float add_rn(float a, float b) { return a + b; }
 DF_HD float sub_rn(float a, float b) { return a - b; }
@@ -60,6 +61,7 @@ DF_HD int float_to_bits(float f) {
     return b;
 }
 DF_HD float rsqrt_approx(float x) { return 1.0f / sqrtf(x); }
+DF_HD float log_approx(float x) { return logf(x); }
 #endif
 
 DF_HD df two_sum(float a, float b) {
@@ -201,6 +203,17 @@ DF_HD df exp(df x, const ExpTable& tbl) {
     if (m < -126) return {0.0f, 0.0f};
     const float sc = bits_to_float((m + 127) << 23);  // 2^m, a normal float for m in [-126, 127]
     return {mul_rn(y.hi, sc), mul_rn(y.lo, sc)};
+}
+
+// log(y) for a double-float y with y.hi in [1e-30, 1e30]: x0 = logf(y.hi)
+// on the FP32 pipe (a few float ulps), r = y exp(-x0) - 1 (|r| < 2^-16),
+// log y = x0 + r - r^2/2 + r^3/3 (the next term is below 2^-64).  About
+// 2^-46 absolute plus 2^-46 relative.
+DF_HD df log(df y, const ExpTable& tbl) {
+    const float x0 = log_approx(y.hi);
+    const df r = add_f(mul(y, exp(df{-x0, 0.0f}, tbl)), -1.0f);
+    const df lp = add_f(r, mul_rn(mul_rn(r.hi, r.hi), fma_rn(r.hi, 1.0f / 3.0f, -0.5f)));
+    return add(df{x0, 0.0f}, lp);
 }
 
 }  // namespace dfl

@@ -176,7 +176,10 @@ __global__ void __launch_bounds__(256) k_exch_energies_flat(Sys s, const double*
 __global__ void __launch_bounds__(kWaveThreads) k_exch_estimate(Sys s, int phase) {
     if (phase == 0) {
         const int fresh = ((volatile int*)s.xflags)[3];
-        if (blockIdx.x == 0 && threadIdx.x == 0) s.xflags[7] = !fresh;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            s.xflags[7] = !fresh;
+            if (fresh) atomicAdd(&s.xflags[kExchFreshCount], 1);
+        }
         if (!fresh) return;
     } else if (((volatile int*)s.xflags)[6] == 0) {
         return;
@@ -216,19 +219,22 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
                                                              const double* __restrict__ pre, int inline_retry) {
     extern __shared__ double ys[];  // y: N+1, acc: N+1, then 32 for reductions
     __shared__ int last_block;
+    __shared__ dfl::ExpTable etbl;  // log y and the row exponentials in double-float
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    fill_exp_table_df(etbl);
+    __syncthreads();
     if (phase == 1 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.xflags[kExchRetryCount], 1);
     const int allow_exact = force_exact || phase == 1 || !((volatile int*)s.xflags)[7];
     const int dir = blockIdx.x;
     const int gave_up = solve_direction(s, dir, force_exact, ys, allow_exact,
-                                        pre ? pre + (size_t)dir * (s.N + 1) : nullptr, !inline_retry);
+                                        pre ? pre + (size_t)dir * (s.N + 1) : nullptr, !inline_retry, &etbl);
     if (gave_up && inline_retry) {
         if (threadIdx.x == 0) atomicAdd(&s.xflags[kExchRetryCount], 1);
         estimate_direction(s, dir, reinterpret_cast<float*>(ys));  // 3 (N+1) floats fit in ys
         __syncthreads();
         weights_direction(s, dir, nullptr);  // CUDA's exp (a rare path)
         __syncthreads();
-        solve_direction(s, dir, 0, ys, 1);
+        solve_direction(s, dir, 0, ys, 1, nullptr, 1, &etbl);
     }
     // The block that finishes second runs solve_finish (threadFenceReduction
     // pattern; no waiting).
@@ -242,7 +248,7 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
         if (threadIdx.x == 0) s.xflags[2] = 0;  // retry pending: phase 1 finishes
         return;
     }
-    solve_finish(s, !force_exact);
+    solve_finish(s, !force_exact, &etbl);
     if (threadIdx.x == 0) {
         s.xflags[6] = 0;
         s.xflags[kExchBand] = 0;  // the next evaluation's weights measure it anew

@@ -305,12 +305,14 @@ constexpr double kExactLogY = 200.0;
 // `pre`: y of this direction already solved (k_exch_solve_grid), or null.
 // Returns 1 when it gave up that way (block-uniform); with `flag_retry` 0
 // xflags[6] is left alone (the caller retries in the same block).
+// `et` (2^(j/256) as double-floats in shared memory): log y in double-float
+// on the FP32 pipe (log_df); null: CUDA's FP64 log.
 __device__ inline int solve_direction(const Sys& s, int dir, int force_exact, double* ys, int allow_exact = 1,
-                                      const double* pre = nullptr, int flag_retry = 1) {
+                                      const double* pre = nullptr, int flag_retry = 1,
+                                      const dfl::ExpTable* et = nullptr) {
     double* acc = ys + s.N + 1;
     double* red = ys + 2 * (s.N + 1);
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
-    const double beta = s.beta_ex;
     int bad = force_exact, stale = 0;
     if (dir == 0) {
         if (!force_exact) {
@@ -322,11 +324,11 @@ __device__ inline int solve_direction(const Sys& s, int dir, int force_exact, do
             }
             for (int m = tid; m <= N; m += bd) {
                 const double y = ys[m];
-                const double ly = log(y);
+                const double ly = et ? log_df(y, *et) : log(y);
                 if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
                 if (!(fabs(ly) < kRefreshLogY)) stale = 1;
                 s.yf[m] = y;
-                s.V[m] = s.Vh[m] - ly / beta;
+                s.V[m] = s.Vh[m] - ly * s.inv_beta_ex;
             }
         }
         bad = __syncthreads_or(bad);
@@ -360,11 +362,11 @@ __device__ inline int solve_direction(const Sys& s, int dir, int force_exact, do
             }
             for (int l = tid + 1; l < N; l += bd) {
                 const double y = ys[N - l];
-                const double ly = log(y);
+                const double ly = et ? log_df(y, *et) : log(y);
                 if (!(y > 0.0) || !(fabs(ly) < kExactLogY)) bad = 1;
                 if (!(fabs(ly) < kRefreshLogY)) stale = 1;
                 s.yb[l] = y;
-                s.Vb[l] = s.Vbh[l] - ly / beta;
+                s.Vb[l] = s.Vbh[l] - ly * s.inv_beta_ex;
             }
         }
         if (tid == 0) {
@@ -398,8 +400,9 @@ __device__ inline int solve_direction(const Sys& s, int dir, int force_exact, do
 // probabilities, which need both V and V_backwards, and the estimates of the
 // next evaluation: V, V_backwards themselves or, with `extrapolate` and a
 // previous result in s.Vp (NaN until there is one), the linear extrapolation
-// 2 V(t) - V(t - dt), which smooth dynamics keep much closer.
-__device__ inline void solve_finish(const Sys& s, int extrapolate = 0) {
+// 2 V(t) - V(t - dt), which smooth dynamics keep much closer.  With `et` the
+// row exponentials in double-float (exp_df).
+__device__ inline void solve_finish(const Sys& s, int extrapolate = 0, const dfl::ExpTable* et = nullptr) {
     const int N = s.N, tid = threadIdx.x, bd = blockDim.x;
     const double beta = s.beta_ex;
     volatile double* V = s.V;
@@ -407,8 +410,9 @@ __device__ inline void solve_finish(const Sys& s, int extrapolate = 0) {
     const double VN = V[N];
     for (int l = tid; l < N; l += bd) {
         const double vbl = Vb[l + 1];
-        s.rowR[l] = exp(-beta * (s.Vh[l + 1] + vbl - VN));
-        s.rowC[l] = exp(-beta * (V[l + 1] + vbl - VN));
+        const double aR = -beta * (s.Vh[l + 1] + vbl - VN), aC = -beta * (V[l + 1] + vbl - VN);
+        s.rowR[l] = et ? exp_df(aR, *et) : exp(aR);
+        s.rowC[l] = et ? exp_df(aC, *et) : exp(aC);
     }
     __syncthreads();
     const int need = ((volatile int*)s.xflags)[4] | ((volatile int*)s.xflags)[5];

@@ -729,7 +729,9 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
 // the nsm SMs take no task: those SMs stay free for the exchange's one-block
 // passes (FP32 estimate, FP64 triangular solve) that run beside this kernel,
 // whose sequential chains would otherwise share the FP64 pipe with the
-// pair warps.
+// pair warps.  The scheduler may place every block of a small grid there on
+// a busy GPU, so the warp that finishes last first takes whatever tasks are
+// left: the forces never depend on where blocks run.
 template <int D, bool kMixed, bool kDf>
 __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s, double* __restrict__ part, int T,
                                                                           int npairs, int* ctr, int cap, int nsm) {
@@ -754,20 +756,32 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
     const int lane = threadIdx.x & 31;
     unsigned smid;
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-    const bool reserved = (int)smid >= nsm - s.reserve_sms;  // never touches ctr[0]
+    const bool reserved = (int)smid >= nsm - s.reserve_sms;
     const int ntask = s.P * npairs;
-    while (!reserved) {
-        int task = 0;
-        if (lane == 0) task = atomicAdd(&ctr[0], 1);
-        task = __shfl_sync(0xffffffffu, task, 0);
-        if (task >= ntask) break;
-        const int b = task / npairs;
-        compact_tile<D, kMixed, kDf>(s, part, T, b, task - b * npairs, sm, g, cap, tbl, &etbl, lane);
-        __syncwarp();
-    }
+    auto take_tasks = [&]() {
+        for (;;) {
+            int task = 0;
+            if (lane == 0) task = atomicAdd(&ctr[0], 1);
+            task = __shfl_sync(0xffffffffu, task, 0);
+            if (task >= ntask) break;
+            const int b = task / npairs;
+            compact_tile<D, kMixed, kDf>(s, part, T, b, task - b * npairs, sm, g, cap, tbl, &etbl, lane);
+            __syncwarp();
+        }
+    };
+    if (!reserved) take_tasks();
+    int last = 0;
     if (lane == 0) {
         __threadfence();
-        if (atomicAdd(&ctr[1], 1) == (int)(gridDim.x * kCompactWarps) - 1) {
+        last = atomicAdd(&ctr[1], 1) == (int)(gridDim.x * kCompactWarps) - 1;
+    }
+    if (__shfl_sync(0xffffffffu, last, 0)) {
+        // every other warp has finished; where the scheduler placed every
+        // block on a reserved SM (a small grid on a busy GPU) the tasks are
+        // still untaken, and this warp evaluates them
+        __threadfence();
+        take_tasks();
+        if (lane == 0) {
             ctr[0] = 0;
             ctr[1] = 0;
             __threadfence();

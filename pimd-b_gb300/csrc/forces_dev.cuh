@@ -140,6 +140,39 @@ __device__ __forceinline__ double exp_tang256(double x, const double* tbl) {
     return n < -258560 ? 0.0 : __hiloint2double(hi, __double2loint(y));
 }
 
+// A block fills `t` with 2^(j/256) as double-floats (bit patterns of the
+// FP64 table; no FP64 instruction).  The caller synchronises.
+__device__ __forceinline__ void fill_exp_table_df(dfl::ExpTable& t) {
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) {
+        float h, l;
+        split_f32(kExp2Table256[j], h, l);
+        const dfl::df n = dfl::fast_two_sum(h, l);
+        t.hi[j] = n.hi;
+        t.lo[j] = n.lo;
+    }
+}
+
+// exp(a) of a double through the double-float exponential (about 2^-46
+// relative, plus a's own rounding to 48 bits times |a|); outside [-87, 87]
+// CUDA's FP64 exp.  One FP64 instruction (the final add) in range.
+__device__ __forceinline__ double exp_df(double a, const dfl::ExpTable& et) {
+    float h, l;
+    split_f32(a, h, l);
+    if (!(fabsf(h) <= 87.0f)) return exp(a);
+    const dfl::df v = dfl::exp(dfl::fast_two_sum(h, l), et);
+    return f32_to_f64(v.hi) + f32_to_f64(v.lo);
+}
+
+// log(y) of a double y > 0 through the double-float logarithm (dfl::log);
+// outside [1e-30, 1e30] CUDA's FP64 log.  One FP64 instruction in range.
+__device__ __forceinline__ double log_df(double y, const dfl::ExpTable& et) {
+    float h, l;
+    split_f32(y, h, l);
+    if (!(h > 1e-30f && h < 1e30f)) return log(y);
+    const dfl::df v = dfl::log(dfl::fast_two_sum(h, l), et);
+    return f32_to_f64(v.hi) + f32_to_f64(v.lo);
+}
+
 // 1/sqrt(r2) for a positive normal double whose float image is normal:
 // Newton-Raphson with the second-order term, y = y0 (1 + e/2 + 3 e^2/8),
 // e = 1 - r2 y0^2, from the FP32 approximation y0 = rsqrtf(r2).  r2 reaches

@@ -76,6 +76,9 @@ constexpr int kExchRetryCount = 10;
 // Index in Sys::xflags of the solve's band: the largest node distance p + 1
 // - u of a nonzero weight of the current evaluation (0 between evaluations).
 constexpr int kExchBand = 11;
+// Index in Sys::xflags of the count of evaluations whose first pass computed
+// a fresh FP32 estimate (the previous potentials were not reusable).
+constexpr int kExchFreshCount = 12;
 // The banded solve: weights within kBandMax levels of the diagonal, one CTA
 // of kBandThreads per direction, y of up to kBandMaxN nodes in shared memory.
 constexpr int kBandMax = 64;

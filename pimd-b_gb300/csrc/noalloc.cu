@@ -152,6 +152,7 @@ extern "C" int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms
     s.invL = 1.0 / s.L;
     s.kappa = spring_constant;
     s.beta_ex = beta_ex;
+    s.inv_beta_ex = 1.0 / beta_ex;
     s.x = base + kOffX;
     s.fx = base + kOffFx;
     s.E = base + kOffE;

@@ -88,6 +88,16 @@ int main() {
         e_near = std::max(e_near, fabsl(val(aziz_near_scale_df(r2, tbl)) - want) / size);
     }
     std::printf("aziz_near %.3Le\n", e_near);
+    // log over [1e-20, 1e20] (log-uniform) and just around 1: error against
+    // max(|log y|, 1)
+    ld e_log = 0;
+    for (int k = 0; k < 400000; ++k) {
+        const ld y = (k & 1) ? powl(10.0L, -20.0L + 40.0L * U(rng)) : 1.0L + (U(rng) - 0.5) * 1e-3L;
+        const df dy = mk(y);
+        const ld Y = val(dy);
+        e_log = std::max(e_log, fabsl(val(dfl::log(dy, tbl)) - logl(Y)) / std::max(fabsl(logl(Y)), 1.0L));
+    }
+    std::printf("log %.3Le\n", e_log);
     std::printf("add %.3Le\nadd_sloppy_abs %.3Le\nmul %.3Le\nsqr %.3Le\nexp %.3Le\nrsqrt %.3Le\nrsqrt_seed8ulp %.3Le\n"
                 "aziz_far %.3Le\n",
                 e_add, e_sloppy_abs, e_mul, e_sqr, e_exp, e_rsqrt, e_rsqrt_seed, e_aziz);

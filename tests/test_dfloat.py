@@ -4,7 +4,8 @@ checked against long double (tests/dfloat_check.cpp).
 
 Bounds, with u = 2^-24: the sum and product primitives within the published
 error bounds (AccurateDWPlusDW 3u^2, DWTimesDW 5u^2), the exponential within
-a few u^2 over [-69, 80], 1/sqrt within a few u^2 (and within 1e-12 from a
+a few u^2 over [-69, 80], the logarithm within a few u^2 of max(|log y|, 1)
+over [1e-20, 1e20], 1/sqrt within a few u^2 (and within 1e-12 from a
 seed eight float ulps off), and the Aziz far-field gradient scale within
 1e-12 relative (inside the damping radius, where the force crosses zero
 at r_m, within 1e-12 of the size of its terms): the GPU's FP64 parity bar (1e-10 per bead) is two orders of
@@ -41,6 +42,8 @@ def test_sum_and_product_bounds(errors):
 
 def test_exp_and_rsqrt(errors):
     assert errors["exp"] <= 8 * U2
+    # log (the exchange solve's log y): within a few u^2 of max(|log y|, 1)
+    assert errors["log"] <= 8 * U2
     assert errors["rsqrt"] <= 8 * U2
     assert errors["rsqrt_seed8ulp"] <= 1e-12
 

@@ -454,6 +454,32 @@ def test_step_io_reports_a_nonfinite_exchange():
             g.step_io(x, np.zeros_like(x), 1)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("reserved", [0, 4096])
+def test_pair_tiles_forces_do_not_depend_on_reserved_sms(reserved, precision):
+    """Beside the bosonic exchange the pair-tile blocks that land on the
+    reserved SMs take no tile; the warp that finishes last takes the tiles
+    left.  With every SM reserved (4096: all blocks idle until that warp) and
+    with none, the forces match the oracle and the automatic setting."""
+    s, cfg = case(natoms=70, nbeads=4, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=14.0, inter="aziz",
+                  cutoff_ang=7.0, precision=precision)
+    x = ring_separated(s, seed=41, dmin_ang=2.2)
+    want = O.update_forces(s, x)["f"]
+    out = {}
+    for opt in (-1, reserved):
+        with pk.System(cfg) as g:
+            g.set_option("cell_lists", 0)
+            g.set_option("reserved_sms", opt)
+            g.set_state(x, np.zeros_like(x))
+            g.compute_forces()
+            out[opt] = g.get_state()[2]
+    if precision == "fp64":
+        assert rel_per_bead(out[reserved], want) < FP64_TOL
+    else:
+        assert np.linalg.norm(out[reserved] - want) <= 1e-6 * np.linalg.norm(want)
+    assert rel_per_bead(out[reserved], out[-1]) < 1e-12
+
+
 def test_pair_tiles_half_box_edge_images():
     """Far-field pair separations take the image the FP32 screen chose; pairs
     whose FP32 test lies within 1e-6 L of the half-box edge take the exact
