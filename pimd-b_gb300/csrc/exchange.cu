@@ -415,16 +415,32 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
     double* wfold = wdiag + 2 * 1024;    // [2][32][64]: block b's rows, columns 32b - 64 .. 32b - 1
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb = (nn + 31) / 32;
-    auto stage = [&](int b, int t0, int nt) {  // threads t0.. stage block b's weights
+    // Threads t0.. stage block b's weights: row r of the block needs columns
+    // 32b - 64 .. 32b + r - 1 of its packed row (contiguous), taken as one
+    // row-major index e = 96 r + q (q < 64: fold, else diagonal) so that a
+    // warp's loads are coalesced.  Every load of a thread is issued before
+    // any store: one L2 round trip per block rather than one per element.
+    constexpr int kStagePer = (32 * 96 + (kBandThreads - 32) - 1) / (kBandThreads - 32);
+    auto stage = [&](int b, int t0, int nt) {
         double* d = wdiag + (b & 1) * 1024;
         double* f = wfold + (b & 1) * 2048;
-        for (int e = tid - t0; e < 1024; e += nt) {
-            const int r = e >> 5, c = e & 31, m = 32 * b + r;
-            d[e] = (m < nn && m >= 1 && c < r) ? W[tri(m - 1) + 32 * b + c] : 0.0;
+        double v[kStagePer];
+#pragma unroll
+        for (int k = 0; k < kStagePer; ++k) {
+            const int e = tid - t0 + k * nt;
+            const int r = e / 96, q = e - 96 * r, m = 32 * b + r;
+            const int c = q < 64 ? 32 * b - 64 + q : 32 * b + (q - 64);
+            const bool in = e < 32 * 96 && m < nn && m >= 1 && (q < 64 ? c >= 0 : q - 64 < r);
+            v[k] = in ? W[tri(m - 1) + c] : 0.0;
         }
-        for (int e = tid - t0; e < 2048; e += nt) {
-            const int r = e >> 6, q = e & 63, m = 32 * b + r, c = 32 * b - 64 + q;
-            f[e] = (m < nn && m >= 1 && c >= 0) ? W[tri(m - 1) + c] : 0.0;
+#pragma unroll
+        for (int k = 0; k < kStagePer; ++k) {
+            const int e = tid - t0 + k * nt;
+            if (e < 32 * 96) {
+                const int r = e / 96, q = e - 96 * r;
+                if (q < 64) f[r * 64 + q] = v[k];
+                else d[r * 32 + (q - 64)] = v[k];
+            }
         }
     };
     stage(0, 0, blockDim.x);
