@@ -221,6 +221,16 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
     __shared__ int last_block;
     __shared__ dfl::ExpTable etbl;  // log y and the row exponentials in double-float
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
+    if (phase == 0) {
+        // k_exch_solve_band post-processed both directions and finished: it
+        // set the flag to 2, and each of the two blocks takes one off
+        if (threadIdx.x == 0) {
+            last_block = ((volatile int*)s.xflags)[kExchBandDone] > 0;
+            if (last_block) atomicSub(&s.xflags[kExchBandDone], 1);
+        }
+        __syncthreads();
+        if (last_block) return;
+    }
     fill_exp_table_df(etbl);
     __syncthreads();
     if (phase == 1 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.xflags[kExchRetryCount], 1);
@@ -405,6 +415,8 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
     if (((volatile int*)s.xflags)[kExchBand] > kBandMax) return;  // the dense solve runs instead
     extern __shared__ double bsm[];
     __shared__ double accb[32];
+    __shared__ dfl::ExpTable etbl;
+    __shared__ int last_band;
     const int dir = blockIdx.x;
     const int nn = dir == 0 ? s.N + 1 : s.N;
     const double* __restrict__ W = dir == 0 ? s.Wf : s.Wb;
@@ -477,6 +489,33 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
         }
         __syncthreads();
     }
+    // The post-processing of k_exch_solve for this direction, from y in
+    // shared memory (no exact fallback here: a direction that would need one
+    // or a fresh estimate leaves the whole evaluation to k_exch_solve).  The
+    // CTA that finishes second runs solve_finish when both directions
+    // succeeded and marks the evaluation done.
+    if (phase != 0) return;
+    fill_exp_table_df(etbl);
+    __syncthreads();
+    const int gave_up = solve_direction(s, dir, 0, ys, 0, ys, 0, &etbl);
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        // count 2 per direction that succeeded, 1 per direction that gave up
+        const int prev = atomicAdd(&s.xflags[kExchBandCount], gave_up ? 1 : 2);
+        last_band = prev > 0 ? (prev + (gave_up ? 1 : 2)) : 0;
+    }
+    __syncthreads();
+    if (last_band == 0) return;
+    __threadfence();
+    if (last_band == 4) {
+        solve_finish(s, 1, &etbl);
+        if (tid == 0) {
+            s.xflags[kExchBand] = 0;  // the next evaluation's weights measure it anew
+            s.xflags[kExchBandDone] = 2;  // one for each block of k_exch_solve
+        }
+    }
+    if (tid == 0) s.xflags[kExchBandCount] = 0;
 }
 
 bool banded_solve_fits(const Sys& s) { return s.N + 1 <= kBandMaxN; }

@@ -79,6 +79,11 @@ constexpr int kExchBand = 11;
 // Index in Sys::xflags of the count of evaluations whose first pass computed
 // a fresh FP32 estimate (the previous potentials were not reusable).
 constexpr int kExchFreshCount = 12;
+// Indices in Sys::xflags of the banded solve's finishing handshake: its CTAs
+// that post-processed their direction (count), and whether the evaluation is
+// complete (2: each of k_exch_solve's two blocks takes one off and exits).
+constexpr int kExchBandCount = 13;
+constexpr int kExchBandDone = 14;
 // The banded solve: weights within kBandMax levels of the diagonal, one CTA
 // of kBandThreads per direction, y of up to kBandMaxN nodes in shared memory.
 constexpr int kBandMax = 64;
