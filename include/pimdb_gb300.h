@@ -380,13 +380,18 @@ int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms, int ndim,
  * each with its own pimdb_config (natoms, nbeads, temperature, potentials,
  * seed, replica), advanced together: one launch per MD step, and a run of
  * steps is replayed as one CUDA graph.  Each step is the body of
- * Simulation::run (src/simulation.cpp:246-259) with the cartesian
- * propagator (VelocityVerletPropagator::step,
- * src/propagators/velocity_verlet.cpp:7-22) and the cartesian Langevin
- * thermostat or none, for every replica.  Every replica must share ndim and
- * precision; natoms <= 2048; at most 65535 replicas.  With PIMDB_MIXED the
- * pair forces are FP32 with FP64 accumulation; exchange and integrator stay
- * FP64.  The Langevin normals are the one-system path's in both precisions.
+ * Simulation::run (src/simulation.cpp:246-259) with, per replica, the
+ * cartesian propagator (VelocityVerletPropagator::step,
+ * src/propagators/velocity_verlet.cpp:7-22) or the normal-mode one
+ * (NormalModesPropagator::step, src/propagators/normal_modes_propagator.cpp:
+ * 19-71; nbeads <= 256), and the Langevin thermostat in the cartesian or the
+ * normal-mode frame, or none (Nose-Hoover chains: one system at a time).
+ * Every replica must share ndim and precision; natoms <= 2048; at most 65535
+ * replicas.  With PIMDB_MIXED the pair forces are FP32 with FP64
+ * accumulation, the exchange weights double-float and its exterior spring
+ * forces FP32 with compensated sums; potentials, triangular solve, cycle
+ * energies and integrator stay FP64.  The Langevin normals are the
+ * one-system path's in both precisions.
  * Host arrays of the batch are the replicas' [bead][particle][axis] arrays
  * concatenated in replica order (pimdb_batch_size gives the total length).
  */

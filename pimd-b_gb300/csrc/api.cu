@@ -308,8 +308,8 @@ void sys_params_from_config(const pimdb_config& c, Sys& s) {
 }
 
 // Reference normal-mode rows (src/normal_modes.cpp:48-79), bit for bit.
-static void nm_tables(int P, double omega_p, double mass, double dt, std::vector<double>& C, std::vector<double>& T,
-                      std::vector<double>& rot) {
+void pimdb::nm_tables(int P, double omega_p, double mass, double dt, std::vector<double>& C,
+                      std::vector<double>& T, std::vector<double>& rot) {
     const double pi = 3.14159265358979323846;
     C.assign((size_t)P * P, 0.0);
     T.assign((size_t)P * P, 0.0);

@@ -41,16 +41,30 @@
 
 namespace pimdb {
 
-enum BatchFlags : int { BF_LANGEVIN = 1, BF_FIXCOM = 2 };
+enum BatchFlags : int { BF_LANGEVIN = 1, BF_FIXCOM = 2, BF_NM = 4, BF_NMTHERMO = 8 };
 enum BatchMode : int { BM_HEAD = 1, BM_FORCES = 2, BM_TAIL = 4, BM_ADVANCE = 8, BM_ESTIMATORS = 16 };
+
+// Normal-mode tables of one replica (BF_NM or BF_NMTHERMO), transposed so
+// that a warp's lanes (one mode or one bead each) read P consecutive
+// doubles: Ct[b P + k] = C[k][b], Tt[k P + j] = T[j][k]; rot[4 k ..] as the
+// one-system path's.
+struct NmTabs {
+    const double* Ct;
+    const double* Tt;
+    const double* rot;
+};
 
 struct BatchRep {
     Sys s;
     int flags;  // BatchFlags
     int pad;
+    NmTabs nm;
 };
 
 constexpr int kBatchMaxThreads = 512;
+// Beads of a replica with normal modes: each warp holds 8 P doubles of one
+// particle pair's lines in shared memory.
+constexpr int kBatchMaxNmBeads = 256;
 
 template <typename R>
 __device__ __forceinline__ void normal_pair(const Sys& s, long long step, int substep, uint32_t pair, double& z0,
@@ -82,11 +96,35 @@ __device__ __forceinline__ void block_sum_axes(double* v, double* sh) {
     __syncthreads();
 }
 
+// The normal-mode propagator's kick force of elements (b, a, i0) and
+// (b, a, i0 + 1), as the one-system path forms it (nm_kick_force): the
+// physical force, and on the bosonic end beads the exchange's spring force
+// fx less the distinguishable ring spring the free propagation carries.
+// All stored forces are zero until the first force evaluation after a state
+// is set, as in the reference.
+template <int D>
+__device__ __forceinline__ double2 nm_kick_pair(const Sys& s, int b, int a, int i0) {
+    const size_t o = idx<D>(s, b, a, i0);
+    double2 fk = *reinterpret_cast<const double2*>(s.fphys + o);
+    if (s.bosonic && (b == 0 || b == s.P - 1)) {
+        const int bp = (b - 1 + s.P) % s.P, bn = (b + 1) % s.P;
+        const double2 x = *reinterpret_cast<const double2*>(s.x + o);
+        const double2 xp = *reinterpret_cast<const double2*>(s.x + idx<D>(s, bp, a, i0));
+        const double2 xn = *reinterpret_cast<const double2*>(s.x + idx<D>(s, bn, a, i0));
+        const double2 fx = *reinterpret_cast<const double2*>(s.fx + ((size_t)(b == 0 ? 0 : 1) * D + a) * s.ld + i0);
+        const double in0 = -s.kappa * (2 * x.x - xp.x - xn.x), in1 = -s.kappa * (2 * x.y - xp.y - xn.y);
+        fk.x = fk.x + fx.x - in0;
+        fk.y = fk.y + fx.y - in1;
+    }
+    return fk;
+}
+
 // One pass over the momenta of a replica, element pairs (i, i+1) per thread
 // so that one Philox call serves both normals (pair index as in the
 // one-system kernels: (b D + a) ceil(N/2) + i/2).
 //   com_in:  subtract cm (a COM correction computed before this pass)
-//   kick:    p += dt/2 f
+//   kick:    p += dt/2 f (nmkick: the normal-mode propagator's kick force,
+//            nm_kick_pair)
 //   o:       p = c1 p + c2 xi (substep)
 //   drift:   x += dt p / m
 // Returns the per-axis sums of the new p in `sum` (this thread's share).
@@ -101,7 +139,7 @@ __device__ __forceinline__ void block_sum_axes(double* v, double* sh) {
 constexpr int kPassUnroll = 4;
 template <int D, typename R>
 __device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int substep, const double* cm, bool com_in,
-                                             bool kick, bool o, bool drift, double* sum) {
+                                             bool kick, bool o, bool drift, double* sum, bool nmkick = false) {
     const int N = s.N, H = (N + 1) / 2;
     const int total = s.P * H, stride = blockDim.x;
     // loop constants kept in registers (opaque: not recomputed per element)
@@ -119,8 +157,9 @@ __device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int s
                 const int b = q / H, i2 = q - b * H;
                 const size_t e = idx<D>(s, b, a, 2 * i2);
                 pv[k] = *reinterpret_cast<const double2*>(s.p + e);
-                if (kick) fv[k] = *reinterpret_cast<const double2*>(s.f + e);
+                if (kick && !nmkick) fv[k] = *reinterpret_cast<const double2*>(s.f + e);
                 if (drift) xv[k] = *reinterpret_cast<const double2*>(s.x + e);
+                if (kick && nmkick) fv[k] = nm_kick_pair<D>(s, b, a, 2 * i2);
             }
 #pragma unroll
             for (int k = 0; k < kPassUnroll; ++k) {
@@ -359,6 +398,7 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, unsigned char* s
         for (int a = 0; a < D; ++a) {
             const size_t o = idx<D>(s, b, a, i);
             s.f[o] = bosonic_bead ? acc[a] : s.kappa * sp[a] + acc[a];  // simulation.cpp:363-373
+            if (s.fphys) s.fphys[o] = acc[a];  // the normal-mode propagator's kick force
         }
     }
     __syncwarp();
@@ -599,18 +639,164 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
     for (int w = warp; w < 2 * N; w += nw) exch_force_row<D>(s, w, lane, 1, xs);
 }
 
+// ------------------------------------------------------------ normal modes
+// The normal-mode propagator (normal_modes_propagator.cpp:19-71) and the
+// Langevin O-step in the normal-mode frame, with the one-system path's
+// P x P transforms (k_nm_propagate, k_nm_thermo): every mode and every bead
+// is a sum over beads (modes) in ascending order.  One warp per (axis,
+// particle pair), both particles in shared memory (`wsm`: 8 P doubles per
+// warp); lanes take modes (beads) k, k + 32, ...
+
+// [COM], half-kick with the normal-mode kick force, Cartesian -> modes, the
+// exact free ring-polymer rotation, modes -> Cartesian; x and p written.
+template <int D>
+__device__ __noinline__ void nm_propagate_block(const Sys& s, const NmTabs& nm, const double* cm, bool com_in, double* wsm) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int P = s.P, N = s.N, H = (N + 1) / 2;
+    double* w = wsm + (size_t)warp * 8 * P;  // x0 x1 p0 p1 | q0 q1 u0 u1
+    const double hdt = 0.5 * s.dt;
+    for (int line = warp; line < D * H; line += nw) {
+        const int a = line / H, i0 = 2 * (line - a * H);
+        const bool two = i0 + 1 < N;
+        const double ca = com_in ? cm[a] : 0.0;
+        for (int b = lane; b < P; b += 32) {
+            const size_t o = idx<D>(s, b, a, i0);
+            const double2 fk = nm_kick_pair<D>(s, b, a, i0);
+            const double2 x = *reinterpret_cast<const double2*>(s.x + o);
+            const double2 pv = *reinterpret_cast<const double2*>(s.p + o);
+            double p0 = pv.x - ca, p1 = pv.y - ca;
+            p0 += hdt * fk.x;
+            p1 += hdt * fk.y;
+            // the second particle of an odd N's last pair is padding: zeros,
+            // as outside the one-system kernels' range
+            w[b] = x.x;
+            w[P + b] = two ? x.y : 0.0;
+            w[2 * P + b] = p0;
+            w[3 * P + b] = two ? p1 : 0.0;
+        }
+        __syncwarp();
+        for (int k = lane; k < P; k += 32) {
+            double q0 = 0.0, q1 = 0.0, p0 = 0.0, p1 = 0.0;
+            for (int b = 0; b < P; ++b) {
+                const double c = nm.Ct[(size_t)b * P + k];
+                q0 += c * w[b];
+                q1 += c * w[P + b];
+                p0 += c * w[2 * P + b];
+                p1 += c * w[3 * P + b];
+            }
+            const double cs = nm.rot[4 * k], sn = nm.rot[4 * k + 1], mw = nm.rot[4 * k + 2], snw = nm.rot[4 * k + 3];
+            double qa, qb, pa, pb;
+            if (mw == 0.0) {
+                qa = q0 + s.dt_m * p0;
+                qb = q1 + s.dt_m * p1;
+                pa = p0;
+                pb = p1;
+            } else {
+                qa = cs * q0 + snw * p0;
+                qb = cs * q1 + snw * p1;
+                pa = -mw * sn * q0 + cs * p0;
+                pb = -mw * sn * q1 + cs * p1;
+            }
+            w[4 * P + k] = qa;
+            w[5 * P + k] = qb;
+            w[6 * P + k] = pa;
+            w[7 * P + k] = pb;
+        }
+        __syncwarp();
+        for (int j = lane; j < P; j += 32) {
+            double x0 = 0.0, x1 = 0.0, v0 = 0.0, v1 = 0.0;
+            for (int k = 0; k < P; ++k) {
+                const double c = nm.Tt[(size_t)k * P + j];
+                x0 += c * w[4 * P + k];
+                x1 += c * w[5 * P + k];
+                v0 += c * w[6 * P + k];
+                v1 += c * w[7 * P + k];
+            }
+            const size_t o = idx<D>(s, j, a, i0);
+            s.x[o] = x0;
+            s.p[o] = v0;
+            if (two) {
+                s.x[o + 1] = x1;
+                s.p[o + 1] = v1;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// [COM], then the Langevin O-step on the normal modes of p (the normals of
+// mode k drawn as the Cartesian ones of bead k: pair index (k D + a)
+// ceil(N/2) + i/2); p written, and its per-axis sums (this thread's share)
+// in `sum`.
 template <int D, typename R>
-__device__ void batch_replica(const Sys& s, int flags, long long step, int mode, double* red, unsigned char* work,
-                              const double* tbl, const dfl::ExpTable* etbl) {
+__device__ __noinline__ void nm_thermo_block(const Sys& s, const NmTabs& nm, long long step, int substep, const double* cm,
+                                bool com_in, double* sum, double* wsm) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int P = s.P, N = s.N, H = (N + 1) / 2;
+    double* w = wsm + (size_t)warp * 8 * P;  // p0 p1 | u0 u1
+    for (int a = 0; a < D; ++a) sum[a] = 0.0;
+    for (int line = warp; line < D * H; line += nw) {
+        const int a = line / H, i2 = line - a * H, i0 = 2 * i2;
+        const bool two = i0 + 1 < N;
+        const double ca = com_in ? cm[a] : 0.0;
+        for (int b = lane; b < P; b += 32) {
+            w[b] = s.p[idx<D>(s, b, a, i0)] - ca;
+            w[P + b] = two ? s.p[idx<D>(s, b, a, i0 + 1)] - ca : 0.0;
+        }
+        __syncwarp();
+        for (int k = lane; k < P; k += 32) {
+            double q0 = 0.0, q1 = 0.0;
+            for (int b = 0; b < P; ++b) {
+                const double c = nm.Ct[(size_t)b * P + k];
+                q0 += c * w[b];
+                q1 += c * w[P + b];
+            }
+            double z0, z1;
+            normal_pair<R>(s, step, substep, (uint32_t)((k * D + a) * H + i2), z0, z1);
+            w[2 * P + k] = s.c1 * q0 + s.c2 * z0;
+            w[3 * P + k] = s.c1 * q1 + s.c2 * z1;
+        }
+        __syncwarp();
+        double part = 0.0;
+        for (int j = lane; j < P; j += 32) {
+            double v0 = 0.0, v1 = 0.0;
+            for (int k = 0; k < P; ++k) {
+                const double c = nm.Tt[(size_t)k * P + j];
+                v0 += c * w[2 * P + k];
+                v1 += c * w[3 * P + k];
+            }
+            const size_t o = idx<D>(s, j, a, i0);
+            s.p[o] = v0;
+            part += v0;
+            if (two) {
+                s.p[o + 1] = v1;
+                part += v1;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c)
+            if (c == a) sum[c] += part;
+        __syncwarp();
+    }
+}
+
+template <int D, typename R>
+__device__ void batch_replica(const Sys& s, int flags, const NmTabs& nm, long long step, int mode, double* red,
+                              unsigned char* work, const double* tbl, const dfl::ExpTable* etbl) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const bool langevin = flags & BF_LANGEVIN, fixcom = flags & BF_FIXCOM;
+    const bool nmprop = flags & BF_NM, nmthermo = langevin && (flags & BF_NMTHERMO);
+    const bool cart_langevin = langevin && !nmthermo;
+    double* wsm = reinterpret_cast<double*>(work);  // normal-mode lines (free outside the force phase)
     const double inv_np = 1.0 / ((double)s.N * s.P);
     double cm[D], sum[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) cm[a] = 0.0;
     if (mode & BM_HEAD) {
-        if (langevin || fixcom) {
-            momenta_pass<D, R>(s, step, 0, cm, false, false, langevin, false, sum);
+        // O-step (substep 0) and the sums for the COM removal
+        if (nmthermo || cart_langevin || fixcom) {
+            if (nmthermo) nm_thermo_block<D, R>(s, nm, step, 0, cm, false, sum, wsm);
+            else momenta_pass<D, R>(s, step, 0, cm, false, false, cart_langevin, false, sum);
             if (fixcom) {
                 block_sum_axes<D>(sum, red);
 #pragma unroll
@@ -619,7 +805,10 @@ __device__ void batch_replica(const Sys& s, int flags, long long step, int mode,
                 __syncthreads();
             }
         }
-        momenta_pass<D, R>(s, step, 0, cm, fixcom, true, false, true, sum);
+        // [COM], B, A (velocity_verlet.cpp:9-12) or the normal-mode
+        // propagation up to the forces (normal_modes_propagator.cpp:19-63)
+        if (nmprop) nm_propagate_block<D>(s, nm, cm, fixcom, wsm);
+        else momenta_pass<D, R>(s, step, 0, cm, fixcom, true, false, true, sum);
         __syncthreads();
     }
     if (mode & BM_FORCES) {
@@ -632,7 +821,18 @@ __device__ void batch_replica(const Sys& s, int flags, long long step, int mode,
         }
     }
     if (mode & BM_TAIL) {
-        momenta_pass<D, R>(s, step, 1, cm, false, true, langevin, false, sum);
+        // B (the normal-mode kick force under the normal-mode propagator),
+        // O-step (substep 1), COM removal
+        if (nmthermo) {
+            if (nmprop) momenta_pass<D, R>(s, step, 1, cm, false, true, false, false, sum, true);
+            else momenta_pass<D, R>(s, step, 1, cm, false, true, false, false, sum, false);
+            __syncthreads();
+            nm_thermo_block<D, R>(s, nm, step, 1, cm, false, sum, wsm);
+        } else if (nmprop) {
+            momenta_pass<D, R>(s, step, 1, cm, false, true, cart_langevin, false, sum, true);
+        } else {
+            momenta_pass<D, R>(s, step, 1, cm, false, true, cart_langevin, false, sum, false);
+        }
         if (fixcom) {
             block_sum_axes<D>(sum, red);
 #pragma unroll
@@ -658,6 +858,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads)
     double* red = reinterpret_cast<double*>(bsm);
     unsigned char* work = bsm + 3 * 32 * sizeof(double);
     __shared__ Sys ss;
+    __shared__ NmTabs snm;
     __shared__ int item, sflags;
     __shared__ double tbl[32];  // exp_tang's table
     __shared__ dfl::ExpTable etbl;  // 2^(j/256) as double-floats (bit patterns)
@@ -671,10 +872,11 @@ __global__ void __launch_bounds__(kBatchMaxThreads)
         if (k < nrep && threadIdx.x == 0) {
             ss = reps[order[k]].s;
             sflags = reps[order[k]].flags;
+            snm = reps[order[k]].nm;
         }
         __syncthreads();
         if (k >= nrep) break;
-        batch_replica<D, R>(ss, sflags, step, mode, red, work, tbl, &etbl);
+        batch_replica<D, R>(ss, sflags, snm, step, mode, red, work, tbl, &etbl);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -726,6 +928,8 @@ __global__ void k_batch_reset(const BatchRep* __restrict__ reps, int D) {
     const Sys& s = reps[blockIdx.x].s;
     const size_t n = (size_t)s.P * D * s.ld;
     for (size_t e = threadIdx.x; e < n; e += blockDim.x) s.f[e] = 0.0;
+    if (s.fphys)
+        for (size_t e = threadIdx.x; e < n; e += blockDim.x) s.fphys[e] = 0.0;
     for (size_t e = threadIdx.x; e < (size_t)2 * D * s.ld; e += blockDim.x) s.fx[e] = 0.0;
     if (threadIdx.x < 8) s.xflags[threadIdx.x] = threadIdx.x == 3 ? 1 : 0;
     if (threadIdx.x == 0) *s.err = 0;
@@ -756,7 +960,7 @@ struct pimdb_batch {
     double* d_stage = nullptr;  // host-layout staging (htotal doubles)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    int threads = 256, ctas_per_sm = 2, grid = 1, maxN = 1, sms = 1;
+    int threads = 256, ctas_per_sm = 2, grid = 1, maxN = 1, sms = 1, maxPnm = 0;
     size_t smem = 0;
     bool use_graph = true;
     cudaGraphExec_t graph = nullptr;
@@ -780,7 +984,7 @@ static int bfail(pimdb_batch* b, int code, const std::string& msg) {
         if (e_ != cudaSuccess) return bfail(b, PIMDB_ERR_CUDA, cudaGetErrorString(e_));   \
     } while (0)
 
-static size_t batch_smem(int D, int maxN, int threads) {
+static size_t batch_smem(int D, int maxN, int threads, int maxPnm) {
     const size_t nw = threads / 32;
     const size_t stage = nw * (size_t)maxN * (D == 3 ? stage_bytes<3>() : D == 2 ? stage_bytes<2>() : stage_bytes<1>());
     const size_t est = sizeof(float) * 3 * (size_t)(maxN + 1);
@@ -788,8 +992,10 @@ static size_t batch_smem(int D, int maxN, int threads) {
     const size_t xforces = sizeof(double) * 2 * (size_t)D * maxN;  // beads 1 and P for the exchange forces
     const size_t xforces32 = sizeof(float) * std::max(xforces_f32_floats(D, maxN), 4 * (size_t)(maxN + 1));
     const size_t estim = sizeof(double) * ((size_t)maxN + 1 + 32);
+    const size_t nmlines = sizeof(double) * nw * 8 * (size_t)maxPnm;  // normal-mode lines, 8 P per warp
     return 3 * 32 * sizeof(double) +
-           std::max(std::max(std::max(stage, est), std::max(solve, estim)), std::max(xforces, xforces32));
+           std::max(std::max(std::max(stage, est), std::max(solve, estim)),
+                    std::max(std::max(xforces, xforces32), nmlines));
 }
 
 template <typename F>
@@ -808,7 +1014,7 @@ static void with_kernel(int D, int mixed, F&& f) {
 static int configure_launch(pimdb_batch* b, int threads, int ctas_per_sm) {
     if (threads < 32 || threads > kBatchMaxThreads || threads % 32) return bfail(b, PIMDB_ERR_ARG, "threads must be a multiple of 32 in [32, 512]");
     if (ctas_per_sm < 1) return bfail(b, PIMDB_ERR_ARG, "ctas_per_sm must be >= 1");
-    const size_t smem = batch_smem(b->D, b->maxN, threads);
+    const size_t smem = batch_smem(b->D, b->maxN, threads, b->maxPnm);
     int resident = 0;
     cudaError_t e = cudaSuccess;
     with_kernel(b->D, b->mixed, [&](auto k) {
@@ -859,10 +1065,14 @@ extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void*
         if (c.ndim != D) return bfail(nullptr, PIMDB_ERR_CONFIG, "every replica of a batch must have the same ndim");
         if (c.precision != precision)
             return bfail(nullptr, PIMDB_ERR_CONFIG, "every replica of a batch must have the same precision");
-        if (c.propagator != PIMDB_PROP_CARTESIAN || c.nmthermostat || c.thermostat >= PIMDB_THERMO_NOSE_HOOVER)
+        if (c.thermostat >= PIMDB_THERMO_NOSE_HOOVER)
             return bfail(nullptr, PIMDB_ERR_CONFIG,
                          "replica " + std::to_string(r) +
-                             ": the batched engine runs the cartesian propagator with the cartesian Langevin thermostat");
+                             ": the batched engine runs the Langevin thermostat (cartesian or normal-mode) or none");
+        if ((c.propagator == PIMDB_PROP_NORMAL_MODES || c.nmthermostat) && c.nbeads > kBatchMaxNmBeads)
+            return bfail(nullptr, PIMDB_ERR_CONFIG,
+                         "replica " + std::to_string(r) + ": the batched engine's normal modes take at most " +
+                             std::to_string(kBatchMaxNmBeads) + " beads");
         if (c.natoms > 2048) return bfail(nullptr, PIMDB_ERR_CONFIG, "the batched engine supports at most 2048 particles per replica");
         if (c.rng != PIMDB_RNG_PHILOX)
             return bfail(nullptr, PIMDB_ERR_CONFIG,
@@ -894,15 +1104,24 @@ extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void*
         b->maxN = std::max(b->maxN, s.N);
         const size_t nstate = (size_t)s.P * D * s.ld;
         const size_t ntri = s.bosonic ? (size_t)s.N * (s.N + 1) / 2 : 1;
+        const bool nm = cfgs[r].propagator == PIMDB_PROP_NORMAL_MODES || cfgs[r].nmthermostat;
         const size_t sizes[] = {nstate, nstate, nstate, (size_t)2 * D * s.ld, ntri, ntri, ntri, ntri,
                                 (size_t)s.N + 1, (size_t)s.N + 1, (size_t)s.N + 1, (size_t)s.N + 1,
-                                (size_t)s.N + 1, (size_t)s.N + 1, (size_t)s.N, (size_t)s.N};
+                                (size_t)s.N + 1, (size_t)s.N + 1, (size_t)s.N, (size_t)s.N,
+                                // normal-mode tables Ct, Tt, rot and the physical forces
+                                // (empty without normal modes)
+                                nm ? (size_t)s.P * s.P : 0, nm ? (size_t)s.P * s.P : 0, nm ? (size_t)4 * s.P : 0,
+                                nm ? nstate : 0};
         for (size_t n : sizes) {
             offs[r].push_back(off);
             off += up(n);
         }
+        if (nm) b->maxPnm = std::max(b->maxPnm, s.P);
         b->reps[r].s = s;
-        b->reps[r].flags = (cfgs[r].thermostat == PIMDB_THERMO_LANGEVIN ? BF_LANGEVIN : 0) | (cfgs[r].fixcom ? BF_FIXCOM : 0);
+        b->reps[r].flags = (cfgs[r].thermostat == PIMDB_THERMO_LANGEVIN ? BF_LANGEVIN : 0) |
+                           (cfgs[r].fixcom ? BF_FIXCOM : 0) |
+                           (cfgs[r].propagator == PIMDB_PROP_NORMAL_MODES ? BF_NM : 0) |
+                           (cfgs[r].nmthermostat ? BF_NMTHERMO : 0);
         b->hoff[r] = hoff;
         hoff += (size_t)s.P * s.N * D;
     }
@@ -939,7 +1158,7 @@ extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void*
         s.x = P + o[0];
         s.p = P + o[1];
         s.f = P + o[2];
-        s.fphys = nullptr;
+        s.fphys = (b->reps[r].flags & BF_NM) ? P + o[19] : nullptr;  // the normal-mode kick force
         s.fx = P + o[3];
         s.E = P + o[4];
         s.Et = P + o[5];
@@ -958,6 +1177,22 @@ extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void*
         s.err = b->d_err + r;
         s.xflags = b->d_iflags + 8 * (size_t)r;
         iflags[8 * (size_t)r + 3] = 1;
+        b->reps[r].nm = NmTabs{nullptr, nullptr, nullptr};
+        if (b->reps[r].flags & (BF_NM | BF_NMTHERMO)) {
+            // the one-system path's tables, transposed for the warps' reads
+            std::vector<double> C, T, rot;
+            nm_tables(s.P, s.omega_p, s.mass, s.dt, C, T, rot);
+            std::vector<double> Ct(C.size()), Tt(T.size());
+            for (int k = 0; k < s.P; ++k)
+                for (int j = 0; j < s.P; ++j) {
+                    Ct[(size_t)j * s.P + k] = C[(size_t)k * s.P + j];
+                    Tt[(size_t)k * s.P + j] = T[(size_t)j * s.P + k];
+                }
+            b->reps[r].nm = NmTabs{P + o[16], P + o[17], P + o[18]};
+            if (e == cudaSuccess) e = cudaMemcpy(P + o[16], Ct.data(), Ct.size() * sizeof(double), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(P + o[17], Tt.data(), Tt.size() * sizeof(double), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(P + o[18], rot.data(), rot.size() * sizeof(double), cudaMemcpyHostToDevice);
+        }
     }
     // largest replicas first: pair work P N^2, exchange N^2 FP64 exponentials
     b->order.resize(nreplicas);
@@ -965,7 +1200,9 @@ extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void*
     auto cost = [&](int r) {
         const Sys& s = b->reps[r].s;
         const double n = s.N, p = s.P;
-        return p * n * (n + 32.0) + (s.bosonic ? 64.0 * n * n : 0.0);
+        const int fl = b->reps[r].flags;
+        const double nm = ((fl & BF_NM) ? 4.0 : 0.0) + ((fl & BF_NMTHERMO) && (fl & BF_LANGEVIN) ? 4.0 : 0.0);
+        return p * n * (n + 32.0) + (s.bosonic ? 64.0 * n * n : 0.0) + nm * 64.0 * n * p * p;
     };
     std::stable_sort(b->order.begin(), b->order.end(), [&](int a, int c) { return cost(a) > cost(c); });
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_reps, sizeof(BatchRep) * nreplicas);

@@ -3,9 +3,18 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace pimdb {
+
+// The reference's normal-mode rows C (row k: mode k over beads), their
+// inverse T (row j: bead j over modes) and per mode {cos(w_k dt),
+// sin(w_k dt), m w_k, sin(w_k dt) / (m w_k)} (normal_modes.cpp:48-79,
+// normal_modes_propagator.cpp:13-16); host code.
+void nm_tables(int P, double omega_p, double mass, double dt, std::vector<double>& C, std::vector<double>& T,
+               std::vector<double>& rot);
 
 // Flags of the momentum-update kernels.  Within one launch the operations
 // run in this order: COM correction from the pending partial sums, B

@@ -61,10 +61,25 @@ def test_batch_rejects_mixed_dimensions():
         pk.Batch([c3, c2])
 
 
-def test_batch_rejects_normal_mode_propagator():
-    _, c = case(natoms=4, nbeads=4, bosonic=False, propagator="normal_modes")
-    with pytest.raises(pk.ConfigError, match="cartesian propagator"):
+def test_batch_rejects_nose_hoover():
+    _, c = case(natoms=4, nbeads=4, bosonic=False, thermostat="nose_hoover")
+    with pytest.raises(pk.ConfigError, match="Langevin thermostat"):
         pk.Batch([c])
+
+
+def test_batch_accepts_normal_modes_and_rejects_too_many_beads():
+    # normal modes pass the configuration checks (without a GPU the batch
+    # then fails for want of a device, not of the configuration)
+    _, c = case(natoms=4, nbeads=8, propagator="normal_modes", nmthermostat=True)
+    try:
+        pk.Batch([c]).close()
+    except pk.ConfigError:
+        pytest.fail("a normal-mode replica was rejected")
+    except pk.PimdbError:
+        pass
+    _, big = case(natoms=2, nbeads=512, propagator="normal_modes")
+    with pytest.raises(pk.ConfigError, match="256 beads"):
+        pk.Batch([big])
 
 
 def test_batch_rejects_mixed_precisions():
@@ -138,6 +153,80 @@ def test_batch_replica_equals_one_system_path():
             x, p, f = g.get_state()
         for u, v in ((bx[r], x), (bp[r], p), (bf[r], f)):
             assert rel_per_bead(u, v) < 1e-12, r
+
+
+REPLICAS_NM = [
+    # the normal-mode propagator with each thermostat, and the normal-mode
+    # thermostat under velocity Verlet; bosons and distinguishable, PBC, 2D
+    dict(natoms=16, nbeads=32, propagator="normal_modes", nmthermostat=True, ext="harmonic", ext_p=(3.0 * MEV, 0, 0)),
+    dict(natoms=20, nbeads=8, propagator="normal_modes", T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=11.0,
+         inter="aziz", cutoff_ang=5.5, dt_fs=2.0),
+    dict(natoms=13, nbeads=6, bosonic=False, propagator="normal_modes", nmthermostat=True, fixcom=False,
+         ext="harmonic", ext_p=(3.0 * MEV, 0, 0)),
+    dict(natoms=7, nbeads=5, bosonic=False, propagator="normal_modes", thermostat="none",
+         ext="harmonic", ext_p=(3.0 * MEV, 0, 0), inter="harmonic", int_p=(1.0 * MEV, 0, 0)),
+    dict(natoms=8, nbeads=8, nmthermostat=True, ext="harmonic", ext_p=(3.0 * MEV, 0, 0)),
+    dict(ndim=2, natoms=11, nbeads=64, propagator="normal_modes", nmthermostat=True, ext="harmonic",
+         ext_p=(1.0 * MEV, 0, 0)),
+    dict(natoms=5, nbeads=1, propagator="normal_modes", ext="harmonic", ext_p=(3.0 * MEV, 0, 0)),
+]
+
+
+@pytest.mark.gpu
+def test_batch_normal_modes_match_oracle():
+    """Normal-mode replicas (normal_modes_propagator.cpp:19-71, the Langevin
+    O-step in the normal-mode frame) against the oracle run on each alone:
+    8 steps within 1e-9 relative per bead, as the Cartesian replicas."""
+    for group in (REPLICAS_NM[:5], REPLICAS_NM[5:6], REPLICAS_NM[6:]):  # one batch per ndim (and P = 1 apart)
+        systems, cfgs, xs, ps = build(group)
+        trs = [O.Trajectory(s, xs[r], ps[r]) for r, s in enumerate(systems)]
+        with pk.Batch(cfgs) as b:
+            b.set_states(xs, ps)
+            b.set_step(0)
+            for st in range(8):
+                for r, (s, c) in enumerate(zip(systems, cfgs)):
+                    xi = O.philox_noise_device(c.seed, c.replica, st, s.nbeads, s.natoms, s.ndim)
+                    assert trs[r].step(xi) == 0
+                b.step(1)
+                gx, gp, gf = b.get_states()
+                for r, tr in enumerate(trs):
+                    for got, want, label in ((gx[r], tr.x, "x"), (gp[r], tr.p, "p"), (gf[r], tr.f, "f")):
+                        assert rel_per_bead(got, want) < 1e-9, (st, r, label, rel_per_bead(got, want))
+
+
+@pytest.mark.gpu
+def test_batch_normal_modes_equal_one_system_matrix_path():
+    """The batch's transforms sum in the order of the one-system path's
+    matrix kernels (fused_normal_modes 0): 6 steps within 1e-12."""
+    systems, cfgs, xs, ps = build(REPLICAS_NM[:4])
+    with pk.Batch(cfgs) as b:
+        b.set_states(xs, ps)
+        b.set_step(0)
+        b.step(6)
+        bx, bp, bf = b.get_states()
+    for r, c in enumerate(cfgs):
+        with pk.System(c) as g:
+            g.set_option("fused_normal_modes", 0)
+            g.set_state(xs[r], ps[r])
+            g.set_step(0)
+            g.step(6)
+            x, p, f = g.get_state()
+        for u, v in ((bx[r], x), (bp[r], p), (bf[r], f)):
+            assert rel_per_bead(u, v) < 1e-12, r
+
+
+@pytest.mark.gpu
+def test_batch_normal_modes_mixed_tracks_fp64():
+    _, c64, xs, ps = build(REPLICAS_NM[:5])
+    _, c32, _, _ = build(REPLICAS_NM[:5], precision="mixed")
+    out = []
+    for cfgs in (c64, c32):
+        with pk.Batch(cfgs) as b:
+            b.set_states(xs, ps)
+            b.step(5)
+            out.append(b.get_states()[0])
+    for r in range(len(c64)):
+        assert norm_rel(out[1][r], out[0][r]) < 1e-6, r
 
 
 @pytest.mark.gpu
