@@ -197,11 +197,31 @@ __device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int s
     }
 }
 
+// A double as a normalised double-float, by bit patterns (no FP64 or
+// conversion-pipe instruction).
+__device__ __forceinline__ dfl::df split_df(double x) {
+    float h, l;
+    split_f32(x, h, l);
+    return dfl::fast_two_sum(h, l);
+}
+// A double rounded to float (to within 2^-24 ulp of round-to-nearest).
+__device__ __forceinline__ float round_f32(double x) {
+    float h, l;
+    split_f32(x, h, l);
+    return h + l;
+}
+// The double of a double-float: the one FP64 instruction of the conversion.
+__device__ __forceinline__ double df_to_f64(dfl::df v) { return f32_to_f64(v.hi) + f32_to_f64(v.lo); }
+// Whether a double is +-0 (integer compare, not a DSETP).
+__device__ __forceinline__ bool f64_is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+
 // Bytes of one particle's staged position: FP64, x y | z (one 16-byte and
 // one 8-byte shared load per pair in 3D); mixed, hx hy hz lx | ly lz.
 template <int D>
 __host__ __device__ constexpr int stage_bytes() { return D == 3 ? 32 : 8 * D; }
 
+// R = float: the hi/lo layout, hi + lo a normalised double-float of x
+// (the mixed path's FP32 separations, the FP64 path's double-float pairs).
 template <int D, typename R>
 __device__ __forceinline__ void stage_put(unsigned char* st, int j, const double* x) {
     unsigned char* q = st + (size_t)j * stage_bytes<D>();
@@ -217,7 +237,11 @@ __device__ __forceinline__ void stage_put(unsigned char* st, int j, const double
     } else {
         float h[D], l[D];
 #pragma unroll
-        for (int a = 0; a < D; ++a) split_f32(x[a], h[a], l[a]);  // no FP64-pipe instruction
+        for (int a = 0; a < D; ++a) {
+            const dfl::df v = split_df(x[a]);  // no FP64-pipe instruction
+            h[a] = v.hi;
+            l[a] = v.lo;
+        }
         if constexpr (D == 3) {
             *reinterpret_cast<float4*>(q) = make_float4(h[0], h[1], h[2], l[0]);
             *reinterpret_cast<float2*>(q + 16) = make_float2(l[1], l[2]);
@@ -271,6 +295,88 @@ __device__ __forceinline__ void stage_get(const unsigned char* st, int j, R* h, 
     }
 }
 
+// The pair gradient sum of particle i of bead b (FP64 path, harmonic or
+// dipole pair potential) in double-float on the FP32 pipe: separations as
+// double-float differences of the staged hi/lo positions (about 2^-47
+// relative), the gradient scale (k, or -3 D |r|^-5 from the double-float
+// 1/sqrt) and the sum over j in double-float (AccurateDWPlusDW).  A pair
+// within 1e-6 L of the half-box edge (the image must be the FP64 one) or
+// within 1e-5 of the cutoff (the in/out decision must be the FP64 one) is
+// evaluated in FP64 from the FP64 positions, as the FP64 loop does.  The
+// all-pairs harmonic force needs no distance: r^2 is not formed.
+template <int D>
+__device__ __noinline__ void bead_pairs_df(const Sys& s, int b, int i, const double* xi, const unsigned char* stage,
+                                           double* g) {
+    using dfl::df;
+    const int N = s.N;
+    const bool harm = s.int_kind == POT_HARMONIC;
+    const double cut = s.cutoff;
+    const bool need_r2 = !(harm && cut < 0.0);
+    const float cut2f = cut < 0.0 ? INFINITY : round_f32(cut * cut);
+    const float shell = 1e-5f * cut2f;
+    const float Lf = round_f32(s.L), halfL = 0.5f * Lf, amb = 1e-6f * Lf;
+    const df Ldf = split_df(s.L);
+    const df K = split_df(harm ? s.int_a : -3.0 * s.int_a);  // harmonic k; dipole -3 D
+    float hi[D], lo[D];
+    stage_get<D, float>(stage, i, hi, lo);
+    df acc[D];
+    double accx[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        acc[a] = df{0.0f, 0.0f};
+        accx[a] = 0.0;
+    }
+    for (int j = 0; j < N; ++j) {
+        float hj[D], lj[D];
+        stage_get<D, float>(stage, j, hj, lj);
+        df d[D];
+        bool exact = false;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            d[a] = dfl::add(df{hi[a], lo[a]}, df{-hj[a], -lj[a]});
+            if (s.pbc) {
+                exact |= fabsf(fabsf(d[a].hi) - halfL) <= amb;
+                if (fabsf(d[a].hi) > halfL) d[a] = dfl::add(d[a], d[a].hi > 0.0f ? dfl::neg(Ldf) : Ldf);
+            }
+        }
+        bool use = j != i;
+        df sc = K;
+        if (need_r2) {
+            df r2 = dfl::sqr(d[0]);
+#pragma unroll
+            for (int a = 1; a < D; ++a) r2 = dfl::add_sloppy(r2, dfl::sqr(d[a]));  // non-negative terms
+            if (fabsf(r2.hi - cut2f) <= shell) exact = true;
+            use = use && r2.hi < cut2f;
+            if (!harm) {  // dipole: -3 D |r|^-5
+                const df ri = dfl::rsqrt(r2);
+                const df ri2 = dfl::sqr(ri);
+                sc = dfl::mul(K, dfl::mul(dfl::sqr(ri2), ri));
+            }
+        }
+        if (exact && j != i) {
+            // FP64, as the FP64 pair loop
+            double r[D], q2 = 0.0;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                double dd = xi[a] - s.x[idx<D>(s, b, a, j)];
+                if (s.pbc) dd = min_image(dd, s.L, s.invL);
+                r[a] = dd;
+                q2 += dd * dd;
+            }
+            if (!(q2 >= (cut < 0.0 ? INFINITY : cut * cut))) {
+                const double scd = pair_scale<double>(s.int_kind, q2, s.int_a);
+#pragma unroll
+                for (int a = 0; a < D; ++a) accx[a] -= scd * r[a];
+            }
+        } else if (use) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) acc[a] = dfl::add(acc[a], dfl::neg(dfl::mul(sc, d[a])));
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) g[a] = df_to_f64(acc[a]) + accx[a];
+}
+
 // Physical forces of bead b plus its interior springs, by one warp.  The
 // bead's positions are staged in `stage` (N slots of stage_bytes<D>()).
 // Bosonic end beads keep the physical part only: the exchange adds their
@@ -282,6 +388,9 @@ template <int D, typename R>
 __device__ void bead_forces_warp(const Sys& s, int b, int lane, unsigned char* stage) {
     const int N = s.N;
     const bool pairs = s.int_kind != POT_FREE && s.cutoff != 0.0;
+    // FP64 with the harmonic or dipole pair potential: pairs in double-float
+    // (bead_pairs_df), from the hi/lo layout
+    const bool dfp = sizeof(R) == 8 && (s.int_kind == POT_HARMONIC || s.int_kind == POT_DIPOLE);
     if (pairs) {
         for (int j0 = lane; j0 < N; j0 += 32 * kStageUnroll) {
             double xs[kStageUnroll][D];
@@ -293,7 +402,10 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, unsigned char* s
             }
 #pragma unroll
             for (int k = 0; k < kStageUnroll; ++k)
-                if (j0 + 32 * k < N) stage_put<D, R>(stage, j0 + 32 * k, xs[k]);
+                if (j0 + 32 * k < N) {
+                    if (dfp) stage_put<D, float>(stage, j0 + 32 * k, xs[k]);
+                    else stage_put<D, R>(stage, j0 + 32 * k, xs[k]);
+                }
         }
         __syncwarp();
     }
@@ -336,7 +448,12 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, unsigned char* s
         }
         double acc[D];
         ext_force<D>(s, xi, acc);
-        if (pairs) {
+        if (pairs && dfp) {
+            double g[D];
+            bead_pairs_df<D>(s, b, i, xi, stage, g);
+#pragma unroll
+            for (int a = 0; a < D; ++a) acc[a] += g[a];
+        } else if (pairs) {
             R hi[D], lo[D];
             stage_get<D, R>(stage, i, hi, lo);
             // FP32: the 32-pair partial sums are added up error-free in two
@@ -411,24 +528,6 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, unsigned char* s
 // double-float (about 2^-44 relative) and the exterior spring forces in FP32
 // with compensated sums (about 2e-7 relative per term).  The potentials, the
 // triangular solve and the energies stay FP64, as on the FP64 path.
-
-// A double as a normalised double-float, by bit patterns (no FP64 or
-// conversion-pipe instruction).
-__device__ __forceinline__ dfl::df split_df(double x) {
-    float h, l;
-    split_f32(x, h, l);
-    return dfl::fast_two_sum(h, l);
-}
-// A double rounded to float (to within 2^-24 ulp of round-to-nearest).
-__device__ __forceinline__ float round_f32(double x) {
-    float h, l;
-    split_f32(x, h, l);
-    return h + l;
-}
-// The double of a double-float: the one FP64 instruction of the conversion.
-__device__ __forceinline__ double df_to_f64(dfl::df v) { return f32_to_f64(v.hi) + f32_to_f64(v.lo); }
-// Whether a double is +-0 (integer compare, not a DSETP).
-__device__ __forceinline__ bool f64_is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
 // The weights of every packed entry (row p, column u), both directions, as
 // exch_weight computes them, in double-float: w = exp(-beta (E + Vh_u -
