@@ -230,6 +230,42 @@ def test_batch_normal_modes_mixed_tracks_fp64():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("inter,int_p", [("harmonic", (1.0 * MEV, 0, 0)), ("dipole", (2.4799673e-4, 0, 0))])
+def test_batch_fp64_double_float_pairs_at_edge_and_cutoff(inter, int_p):
+    """The FP64 batch evaluates harmonic and dipole pairs in double-float; a
+    pair within 1e-6 L of the half-box edge or within 1e-5 of the cutoff takes
+    the FP64 image and in/out decision.  Six pairs with the cutoff at L/2,
+    each with its separation along one axis 1e-9 .. 1e-5 L short of L/2 (or
+    past it) and just inside the cutoff, match the oracle within 1e-10."""
+    L_ang = 12.0
+    eps_list = [1e-9, 1e-7, 5e-7, 2e-6, 1e-5, 3e-6]
+    s, cfg = case(natoms=2 * len(eps_list), nbeads=2, T_K=2.0, pbc=True, box_ang=L_ang, inter=inter, int_p=int_p,
+                  cutoff_ang=0.5 * L_ang)
+    L = s.size
+    pts = []
+    for k, eps in enumerate(eps_list):
+        axis = k % 3
+        sign = 1.0 if (k // 3) % 2 == 0 else -1.0
+        o1, o2 = (axis + 1) % 3, (axis + 2) % 3
+        base = np.zeros(3)
+        base[o1] = (k % 3 - 1) * 0.18 * L
+        base[o2] = (k // 3 - 0.5) * 0.3 * L
+        a, c = base.copy(), base.copy()
+        a[axis] = -0.25 * L
+        c[axis] = 0.25 * L - sign * eps * L
+        c[o1] += 0.3 * np.sqrt(eps) * L
+        pts += [a, c]
+    x = np.repeat(np.array(pts)[None], s.nbeads, axis=0)
+    x[1] += np.random.default_rng(19).normal(0.0, 1e-4, x[1].shape)
+    want = O.update_forces(s, x)["f"]
+    with pk.Batch([cfg]) as b:
+        b.set_states([x], [np.zeros_like(x)])
+        b.compute_forces()
+        got = b.get_states()[2][0]
+    assert rel_per_bead(got, want) < 1e-10
+
+
+@pytest.mark.gpu
 def test_batch_graph_replay_equals_plain_launches():
     _, cfgs, xs, ps = build(REPLICAS_3D)
     out = []
