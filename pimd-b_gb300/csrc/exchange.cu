@@ -55,6 +55,75 @@ __global__ void k_exch_energies(Sys s) {
     energy_row<D>(s, v, lane);
 }
 
+// Cycle energies below the flat form's size, one block per row: the row's
+// 32-entry chunks (u = v - 1 - 32 k - lane) are independent but for the
+// running carry, so every warp scans its chunks at once; thread 0 then
+// forms each chunk's carry from E[v][v] and the chunk totals in the order
+// energy_row adds them, and the warps add it.  The terms, the scans and the
+// carries are energy_row's, operation for operation: the same bits.  The
+// critical path of a row is one chunk instead of all of them.
+constexpr int kEnergyRowThreads = 256;
+template <int D>
+__global__ void __launch_bounds__(kEnergyRowThreads) k_exch_energies_rows(Sys s) {
+    extern __shared__ double rsm[];  // scans [N], then the chunks' totals and carries
+    const int v = blockIdx.x, N = s.N;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int first = 0, last = s.P - 1;
+    const double hk = 0.5 * s.kappa;
+    const int nch = (v + 31) / 32;  // chunks of u = v-1 .. 0
+    double* scan = rsm;
+    double* tot = rsm + N;
+    double* carry = tot + nch;
+    double xv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xv[a] = s.x[idx<D>(s, last, a, v)];
+    auto dist_to_v = [&](int u) {  // |xP_v - x1_u|^2
+        double d2 = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            double d = xv[a] - s.x[idx<D>(s, first, a, u)];
+            if (s.pbc) d = min_image(d, s.L, s.invL);
+            d2 += d * d;
+        }
+        return d2;
+    };
+    for (int k = warp; k < nch; k += nw) {
+        const int base = v - 1 - 32 * k, u = base - lane;
+        const double c = u >= 0 ? dist_to_v(u) : 0.0;
+        double cu1 = __shfl_up_sync(0xffffffffu, c, 1);
+        if (lane == 0) cu1 = dist_to_v(base + 1);  // the previous chunk's last distance
+        double term = 0.0;
+        if (u >= 0) term = hk * (sepsq<D>(s, last, u, first, u + 1) - cu1 + c);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, term, o);
+            if (lane >= o) term += y;
+        }
+        if (u >= 0) scan[32 * k + lane] = term;
+        const double tk = __shfl_sync(0xffffffffu, term, 31);
+        if (lane == 0) tot[k] = tk;
+    }
+    __syncthreads();
+    double* row = s.E + tri(v);
+    if (threadIdx.x == 0) {
+        double cr = hk * dist_to_v(v);
+        row[v] = cr;
+        if (v >= 1) s.Et[tri(N - v - 1) + (N - 1 - v)] = cr;
+        for (int k = 0; k < nch; ++k) {
+            carry[k] = cr;
+            cr += tot[k];
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < v; e += blockDim.x) {
+        const int k = e >> 5, u = v - 1 - e;
+        const double val = carry[k] + scan[e];
+        row[u] = val;
+        // backward node r = N - u depends on node r' = N - 1 - v
+        if (u >= 1) s.Et[tri(N - u - 1) + (N - 1 - v)] = val;
+    }
+}
+
 // Cycle energies for large N without a scan per row.  The row recursion
 // telescopes: E[v][u] = k/2 (L[v] - L[u] + |xP_v - x1_u|^2) with the prefix
 // sums L[w] = sum_{t<w} |x1_{t+1} - xP_t|^2 of the interior links, so every
@@ -667,7 +736,8 @@ static void exchange_carveouts() {
     const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
     if (bit && (g_carveout_devices.load(std::memory_order_acquire) & bit)) return;
     const void* k[] = {(const void*)k_exch_energies<1>, (const void*)k_exch_energies<2>,
-                       (const void*)k_exch_energies<3>, (const void*)k_link_prefix<1>,
+                       (const void*)k_exch_energies<3>, (const void*)k_exch_energies_rows<1>,
+                       (const void*)k_exch_energies_rows<2>, (const void*)k_exch_energies_rows<3>, (const void*)k_link_prefix<1>,
                        (const void*)k_link_prefix<2>, (const void*)k_link_prefix<3>,
                        (const void*)k_exch_energies_flat<1>, (const void*)k_exch_energies_flat<2>,
                        (const void*)k_exch_energies_flat<3>, (const void*)k_exch_estimate,
@@ -699,6 +769,14 @@ void launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work
             k_link_prefix<3><<<1, 1024, 0, st>>>(s, Lh, Ll, wrap);
             k_exch_energies_flat<3><<<s.N, 256, 0, st>>>(s, Lh, Ll, wrap);
         }
+        return;
+    }
+    // one block per row; scans [N] and two chunk arrays in shared memory
+    const size_t rs = sizeof(double) * ((size_t)s.N + 2 * (((size_t)s.N + 31) / 32) + 2);
+    if (rs <= 48 * 1024) {
+        if (D == 1) k_exch_energies_rows<1><<<s.N, kEnergyRowThreads, rs, st>>>(s);
+        else if (D == 2) k_exch_energies_rows<2><<<s.N, kEnergyRowThreads, rs, st>>>(s);
+        else k_exch_energies_rows<3><<<s.N, kEnergyRowThreads, rs, st>>>(s);
         return;
     }
     const int warps = 2;
