@@ -331,6 +331,7 @@ __global__ void __launch_bounds__(kWaveThreads) k_exch_solve(Sys s, int force_ex
     if (threadIdx.x == 0) {
         s.xflags[6] = 0;
         s.xflags[kExchBand] = 0;  // the next evaluation's weights measure it anew
+        s.xflags[kExchBandLast] = 0;  // not the banded solve's evaluation: full rows
     }
 }
 
@@ -580,6 +581,7 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
     if (last_band == 4) {
         solve_finish(s, 1, &etbl);
         if (tid == 0) {
+            s.xflags[kExchBandLast] = s.xflags[kExchBand];
             s.xflags[kExchBand] = 0;  // the next evaluation's weights measure it anew
             s.xflags[kExchBandDone] = 2;  // one for each block of k_exch_solve
         }
@@ -709,7 +711,7 @@ __global__ void k_exch_forces(Sys s, int accumulate, int adjoint, double vb_bar)
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (w >= 2 * s.N) return;
-    exch_force_row<D>(s, w, lane, accumulate, nullptr, adjoint, vb_bar);
+    exch_force_row<D>(s, w, lane, accumulate, nullptr, adjoint, vb_bar, ((volatile int*)s.xflags)[kExchBandLast]);
 }
 
 __global__ void k_exch_estimators(Sys s, int nbeads) {

@@ -449,8 +449,12 @@ template <int D>
 // With `adjoint` set, the row writes the cotangent of the exchange potential
 // instead of the force: fx = vb_bar * dV_B/dx = -vb_bar * kappa * sum, with
 // neither the interior neighbour spring nor the accumulation into f.
+// `band` > 0: every weight beyond that distance from the diagonal is exactly
+// zero (the banded solve's measurement); the rows skip the 32-entry chunks
+// that hold only such entries, each lane keeping its own entries (the same
+// sums, bit for bit).
 __device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumulate, const double* xs = nullptr,
-                                      int adjoint = 0, double vb_bar = 0.0) {
+                                      int adjoint = 0, double vb_bar = 0.0, int band = 0) {
     const int N = s.N;
     const double beta = s.beta_ex;
     const double VN = s.V[N];
@@ -471,7 +475,8 @@ __device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumul
         double xl[D];
 #pragma unroll
         for (int a = 0; a < D; ++a) xl[a] = s.x[idx<D>(s, last, a, l)];
-        for (int n = lane; n <= nmax; n += 32) {
+        const int n0 = (band > 0 && !exact) ? max(0, l + 1 - band) / 32 * 32 : 0;
+        for (int n = n0 + lane; n <= nmax; n += 32) {
             double pr;
             if (n <= l) {
                 // a zero weight (a cycle too costly to contribute) adds exactly 0
@@ -496,7 +501,8 @@ __device__ inline void exch_force_row(const Sys& s, int w, int lane, int accumul
         double xl[D];
 #pragma unroll
         for (int a = 0; a < D; ++a) xl[a] = s.x[idx<D>(s, first, a, l)];
-        for (int q = max(0, l - 1) + lane; q < N; q += 32) {
+        const int qend = (band > 0 && !exact) ? min(N, l + band) : N;  // q + 1 - l <= band
+        for (int q = max(0, l - 1) + lane; q < qend; q += 32) {
             double pr;
             if (q >= l) {
                 if (!exact && s.Wf[tri(q) + l] == 0.0) continue;

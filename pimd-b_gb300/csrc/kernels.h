@@ -93,6 +93,10 @@ constexpr int kExchFreshCount = 12;
 // complete (2: each of k_exch_solve's two blocks takes one off and exits).
 constexpr int kExchBandCount = 13;
 constexpr int kExchBandDone = 14;
+// Index in Sys::xflags of the band of the evaluation the banded solve
+// completed (0 when another path solved it): the exterior-force rows skip
+// the entries beyond it, all exact zeros.
+constexpr int kExchBandLast = 15;
 // The banded solve: weights within kBandMax levels of the diagonal, one CTA
 // of kBandThreads per direction, y of up to kBandMaxN nodes in shared memory.
 constexpr int kBandMax = 64;
