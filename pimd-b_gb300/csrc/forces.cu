@@ -335,6 +335,14 @@ __device__ __forceinline__ double min_image_wrapped(double d, double L, long lon
     return d - sh;
 }
 
+// The FP64 gradient scale of the rare entries the tiles evaluate exactly
+// (half-box edge, cutoff shell, the reference's short-range branch), out of
+// line: the general Aziz form is long, and inlined into the tile loop it
+// enlarges the code every warp runs through (instruction-cache misses).
+__device__ __noinline__ double pair_scale_exact(int kind, double r2, double param, const double* tbl) {
+    return pair_scale_d<true>(kind, r2, param, tbl);
+}
+
 // One tile task: bead b, tile pair w (it <= jt) of the bead's T(T+1)/2.
 // kMixed: entries beyond the Aziz damping radius (and every entry of the
 // other potentials) are evaluated in FP32 from hi/lo separations; entries
@@ -662,7 +670,7 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
                         }
                         double r[D];
                         const double r2 = separation(fn, r);
-                        store(fn, r2 < cut2 ? pair_scale_d<true>(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
+                        store(fn, r2 < cut2 ? pair_scale_exact(s.int_kind, r2, s.int_a, tbl) : 0.0, r);
                     }
                     __syncwarp();
                     cnt = 0;
