@@ -731,7 +731,33 @@ __device__ __forceinline__ void compact_tile(const Sys& s, double* __restrict__ 
     }
 }
 
-// Persistent warps take tile tasks (bead-major) from ctr[0] until none are
+// Task order: every bead's off-diagonal tile pairs (it < jt) first, then
+// the diagonal ones, which hold half the pairs.  With more tasks than
+// resident warps the second round then takes the short tasks (the benchmark
+// system: 1792 off-diagonal tiles for 1800 warps, then 512 diagonal ones).
+// w is the tile pair's index in compact_tile's row-major order over
+// it <= jt; results do not depend on the order (each tile has its slots).
+__device__ __forceinline__ void tile_of_task(int task, int P, int T, int& b, int& w) {
+    const int noff = T * (T - 1) / 2;
+    int it, jt;
+    if (task < P * noff) {
+        b = task / noff;
+        int r = task - b * noff;
+        it = 0;
+        while (r >= T - 1 - it) {  // row it holds jt = it + 1 .. T - 1
+            r -= T - 1 - it;
+            ++it;
+        }
+        jt = it + 1 + r;
+    } else {
+        const int d = task - P * noff;
+        b = d / T;
+        it = jt = d - b * T;
+    }
+    w = it * T - it * (it - 1) / 2 + (jt - it);
+}
+
+// Persistent warps take tile tasks from ctr[0] until none are
 // left; the warp that finishes last resets both counters for the next
 // launch (no waiting).  Blocks that land on one of the last s.reserve_sms of
 // the nsm SMs take no task: those SMs stay free for the exchange's one-block
@@ -772,8 +798,9 @@ __global__ void __launch_bounds__(32 * kCompactWarps) k_pair_tiles_compact(Sys s
             if (lane == 0) task = atomicAdd(&ctr[0], 1);
             task = __shfl_sync(0xffffffffu, task, 0);
             if (task >= ntask) break;
-            const int b = task / npairs;
-            compact_tile<D, kMixed, kDf>(s, part, T, b, task - b * npairs, sm, g, cap, tbl, &etbl, lane);
+            int b, w;
+            tile_of_task(task, s.P, T, b, w);
+            compact_tile<D, kMixed, kDf>(s, part, T, b, w, sm, g, cap, tbl, &etbl, lane);
             __syncwarp();
         }
     };
