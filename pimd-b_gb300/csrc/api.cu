@@ -706,12 +706,13 @@ static void exchange_front(pimdb_handle* h, cudaStream_t st) {
         launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { launch_factorial_sums(s, h->D, h->d_fact, st); }, 2);
         return;
     }
-    launch(h, PIMDB_K_EXCH_ENERGIES, [&] { launch_exchange_energies(s, h->D, st, h->d_ework); },
+    int est = 0;
+    launch(h, PIMDB_K_EXCH_ENERGIES, [&] { est = launch_exchange_energies(s, h->D, st, h->d_ework); },
            h->d_ework ? 2 : 1);
     const int ex = h->opt_exact_exchange;
     int nk = 0;
-    launch(h, PIMDB_K_EXCH_RECURSIONS, [&] { nk = launch_exchange_recursions(s, ex, st, h->d_ysol, h->d_gflags); },
-           0);
+    launch(h, PIMDB_K_EXCH_RECURSIONS,
+           [&] { nk = launch_exchange_recursions(s, ex, st, h->d_ysol, h->d_gflags, est); }, 0);
     h->launches += nk;
 }
 static void exchange_forces(pimdb_handle* h, int accumulate, cudaStream_t st) {

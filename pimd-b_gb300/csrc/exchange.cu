@@ -61,10 +61,15 @@ __global__ void k_exch_energies(Sys s) {
 // forms each chunk's carry from E[v][v] and the chunk totals in the order
 // energy_row adds them, and the warps add it.  The terms, the scans and the
 // carries are energy_row's, operation for operation: the same bits.  The
-// critical path of a row is one chunk instead of all of them.
+// critical path of a row is one chunk instead of all of them.  The block
+// that finishes last runs a due FP32 estimate (k_exch_estimate's phase-0
+// work, both directions in turn), so that the chain has no launch that
+// usually does nothing.  Four blocks per SM bound the registers (the rare
+// estimate's arrays would otherwise set them for every row).
 constexpr int kEnergyRowThreads = 256;
+static_assert(kEnergyRowThreads == kWaveThreads, "the estimate runs with the energy kernel's block");
 template <int D>
-__global__ void __launch_bounds__(kEnergyRowThreads) k_exch_energies_rows(Sys s) {
+__global__ void __launch_bounds__(kEnergyRowThreads, 4) k_exch_energies_rows(Sys s) {
     extern __shared__ double rsm[];  // scans [N], then the chunks' totals and carries
     const int v = blockIdx.x, N = s.N;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -122,6 +127,33 @@ __global__ void __launch_bounds__(kEnergyRowThreads) k_exch_energies_rows(Sys s)
         // backward node r = N - u depends on node r' = N - 1 - v
         if (u >= 1) s.Et[tri(N - u - 1) + (N - 1 - v)] = val;
     }
+    __shared__ int is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = atomicAdd(&s.xflags[kExchRowsCount], 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    const int fresh = ((volatile int*)s.xflags)[3];
+    if (threadIdx.x == 0) {
+        s.xflags[kExchRowsCount] = 0;
+        s.xflags[7] = !fresh;
+        if (fresh) atomicAdd(&s.xflags[kExchFreshCount], 1);
+    }
+    if (!fresh) return;
+    estimate_direction(s, 0, reinterpret_cast<float*>(rsm));
+    __syncthreads();
+    estimate_direction(s, 1, reinterpret_cast<float*>(rsm));
+}
+
+// Whether the cycle energies of s come from k_exch_energies_rows (which then
+// also runs the phase-0 estimate).
+static size_t energies_rows_smem(const Sys& s) {
+    return std::max(sizeof(double) * ((size_t)s.N + 2 * (((size_t)s.N + 31) / 32) + 2),
+                    sizeof(float) * 3 * ((size_t)s.N + 1));
+}
+static bool energies_by_rows(const Sys& s, const double* work) {
+    return !(work && s.eflat) && energies_rows_smem(s) <= 48 * 1024;
 }
 
 // Cycle energies for large N without a scan per row.  The row recursion
@@ -480,9 +512,51 @@ __global__ void __launch_bounds__(kGridSolveThreads) k_exch_solve_grid(Sys s, in
 // block's weights into the other half of a double buffer.  No flags and no
 // inter-CTA waits; y lands in ysol as from the dense solves, which step
 // aside (their `banded` argument) and stay the general path.
-__global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int phase, double* ysol) {
+// `standalone` (below the multi-SM solve's size): this kernel is the whole
+// pass 3.  A band above kBandMax is solved densely on the same CTA
+// (blocked_solve), a reused estimate that fails is redone from a fresh one
+// in the block (k_exch_solve's in-block retry), and the CTA that finishes
+// second runs solve_finish; no other solve kernel is launched.
+__device__ __noinline__ void band_standalone_tail(const Sys& s, int dir, double* ys, const dfl::ExpTable& etbl,
+                                                  int band, bool dense, int* last_band) {
+    const int tid = threadIdx.x;
+    const int allow_exact = !((volatile int*)s.xflags)[7];  // the estimate was fresh
+    int retried = 0;
+    if (solve_direction(s, dir, 0, ys, allow_exact, ys, 0, &etbl)) {
+        if (tid == 0) atomicAdd(&s.xflags[kExchRetryCount], 1);
+        estimate_direction(s, dir, reinterpret_cast<float*>(ys));  // 3 (N+1) floats fit in ys
+        __syncthreads();
+        weights_direction(s, dir, nullptr);  // CUDA's exp (a rare path)
+        __syncthreads();
+        solve_direction(s, dir, 0, ys, 1, nullptr, 1, &etbl);
+        retried = 1;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        // 1 per direction, 16 per direction that was redone
+        const int mine = retried ? 16 : 1;
+        const int prev = atomicAdd(&s.xflags[kExchBandCount], mine);
+        *last_band = prev == 0 ? 0 : 1 + (((prev + mine) >> 4) ? 2 : 0);
+    }
+    __syncthreads();
+    if (*last_band == 0) return;
+    __threadfence();
+    solve_finish(s, 1, &etbl);
+    if (tid == 0) {
+        s.xflags[6] = 0;
+        // full exterior-force rows after a dense solve or a redone direction
+        s.xflags[kExchBandLast] = (dense || *last_band == 3) ? 0 : band;
+        s.xflags[kExchBand] = 0;  // the next evaluation's weights measure it anew
+        s.xflags[kExchBandCount] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int phase, double* ysol, int standalone) {
     if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;
-    if (((volatile int*)s.xflags)[kExchBand] > kBandMax) return;  // the dense solve runs instead
+    const int band = ((volatile int*)s.xflags)[kExchBand];
+    const bool dense = band > kBandMax;
+    if (dense && !standalone) return;  // the dense solve runs instead
     extern __shared__ double bsm[];
     __shared__ double accb[32];
     __shared__ dfl::ExpTable etbl;
@@ -525,10 +599,15 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
             }
         }
     };
-    stage(0, 0, blockDim.x);
+    if (dense) {
+        blocked_solve(W, nn, ys, wdiag);  // accumulators in the (unused) staging buffers
+        for (int m = tid; m < nn; m += blockDim.x) y[m] = ys[m];
+        __syncthreads();
+    }
+    if (!dense) stage(0, 0, blockDim.x);
     __syncthreads();
     const int i = tid >> 3, part = tid & 7;  // fold role: row of the block, 8 of its 64 columns
-    for (int b = 0; b < nb; ++b) {
+    for (int b = 0; b < (dense ? 0 : nb); ++b) {
         const double* f = wfold + (b & 1) * 2048;
         double sum = 0.0;
 #pragma unroll
@@ -567,6 +646,10 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
     if (phase != 0) return;
     fill_exp_table_df(etbl);
     __syncthreads();
+    if (standalone) {
+        band_standalone_tail(s, dir, ys, etbl, band, dense, &last_band);
+        return;
+    }
     const int gave_up = solve_direction(s, dir, 0, ys, 0, ys, 0, &etbl);
     __threadfence();
     __syncthreads();
@@ -755,7 +838,7 @@ int exchange_flat_default(int N) { return N >= kFlatEnergiesMinN ? 1 : 0; }
 // The work array of the prefix-sum energies (any N: Sys::eflat chooses).
 size_t exchange_energy_doubles(const Sys& s, int D) { return (size_t)(2 + 2 * D) * s.N; }
 
-void launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work) {
+int launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work) {
     exchange_carveouts();
     if (work && s.eflat) {
         double* Lh = work;
@@ -771,21 +854,23 @@ void launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work
             k_link_prefix<3><<<1, 1024, 0, st>>>(s, Lh, Ll, wrap);
             k_exch_energies_flat<3><<<s.N, 256, 0, st>>>(s, Lh, Ll, wrap);
         }
-        return;
+        return 0;
     }
     // one block per row; scans [N] and two chunk arrays in shared memory
-    const size_t rs = sizeof(double) * ((size_t)s.N + 2 * (((size_t)s.N + 31) / 32) + 2);
-    if (rs <= 48 * 1024) {
+    // (or the estimate's 3 (N + 1) floats)
+    const size_t rs = energies_rows_smem(s);
+    if (energies_by_rows(s, work)) {
         if (D == 1) k_exch_energies_rows<1><<<s.N, kEnergyRowThreads, rs, st>>>(s);
         else if (D == 2) k_exch_energies_rows<2><<<s.N, kEnergyRowThreads, rs, st>>>(s);
         else k_exch_energies_rows<3><<<s.N, kEnergyRowThreads, rs, st>>>(s);
-        return;
+        return 1;
     }
     const int warps = 2;
     dim3 grid((s.N + warps - 1) / warps);
     if (D == 1) k_exch_energies<1><<<grid, warps * 32, 0, st>>>(s);
     else if (D == 2) k_exch_energies<2><<<grid, warps * 32, 0, st>>>(s);
     else k_exch_energies<3><<<grid, warps * 32, 0, st>>>(s);
+    return 0;
 }
 
 // y of both directions for the cluster solve (below kGridSolveMinN) or the
@@ -825,7 +910,8 @@ static bool grid_solve(const Sys& s, int phase, double* ysol, unsigned* gflags, 
 // one-block passes (below the multi-SM solve's size) then run alone on an SM.
 int exchange_reserved_sms(const Sys& s) { return s.N < kGridSolveMinN ? 2 : 0; }
 
-int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double* ysol, unsigned* gflags) {
+int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double* ysol, unsigned* gflags,
+                               int estimate_done) {
     exchange_carveouts();
     // With reserved SMs the one-block passes ask for 116 KB of shared memory,
     // whatever they use: more than an SM holding pair-tile blocks has left
@@ -845,10 +931,16 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
     // below the multi-SM solve's size a failed solve is retried inside
     // k_exch_solve (phase 0 only)
     const int inline_retry = s.N < kGridSolveMinN;
+    // below the multi-SM solve's size the banded kernel is the whole pass 3
+    const int standalone = inline_retry && ysol && banded_solve_fits(s);
     int n = 0;
     for (int phase = 0; phase < (inline_retry ? 1 : 2); ++phase) {
-        k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s, phase);
+        if (!(phase == 0 && estimate_done)) {  // else the energy kernel ran it
+            k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s, phase);
+            ++n;
+        }
         k_exch_weights<<<phase ? rgrid : wgrid, 256, 0, st>>>(s, phase);
+        ++n;
         // banded weights: one CTA per direction; otherwise the solve on a
         // cluster below the multi-SM solve's size, across SMs from it
         int banded = 0;
@@ -856,15 +948,16 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
             const size_t bs = std::max(banded_solve_smem(s), least);
             if (bs + 1024 > 48 * 1024)
                 cudaFuncSetAttribute(k_exch_solve_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bs);
-            k_exch_solve_band<<<2, kBandThreads, bs, st>>>(s, phase, ysol);
+            k_exch_solve_band<<<2, kBandThreads, bs, st>>>(s, phase, ysol, standalone);
             banded = 1;
             ++n;
         }
+        if (standalone) continue;
         const bool dense = ysol && (inline_retry ? cluster_solve(s, phase, ysol, banded, st)
                                                  : gflags && grid_solve(s, phase, ysol, gflags, banded, st));
         const bool pre = banded || dense;
         k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase, pre ? ysol : nullptr, inline_retry);
-        n += dense ? 4 : 3;
+        n += dense ? 2 : 1;
     }
     return n;
 }

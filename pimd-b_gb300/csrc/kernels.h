@@ -61,15 +61,18 @@ void launch_local_energy(const Sys& s, int D, int n, const int* items, double* o
 // exchange.cu: Feldman-Hirshberg exchange on beads 1 and P.
 // For N >= 512 with `work` (exchange_energy_doubles) the energies come from
 // the links' prefix sums, one independent entry per thread.
-void launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work = nullptr);
+// Returns 1 when the per-row energy kernel ran, which also runs a due FP32
+// estimate (pass `estimate_done` = 1 to launch_exchange_recursions).
+int launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work = nullptr);
 size_t exchange_energy_doubles(const Sys& s, int D);
-// Returns the number of kernels launched (6: estimate, weights, solve and
-// their retry, which exits at once unless a reused estimate failed; or 1
-// with `exact`: the reference-order FP64 log-sum-exp recursion only).
-// For N >= 768 the solve runs across SMs when `ysol` (exchange_grid_doubles)
-// and `gflags` (exchange_grid_flags, zeroed once) are given.
+// Returns the number of kernels launched: the estimate (unless the energy
+// kernel ran it), the weights and the solve kernels (with their retry phase
+// from 768 particles), or 1 with `exact` (the reference-order FP64
+// log-sum-exp recursion only).  With `ysol` (exchange_grid_doubles) below 768
+// particles the banded kernel is the whole solve; from 768 the solve runs
+// across SMs when `gflags` (exchange_grid_flags, zeroed once) is given.
 int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double* ysol = nullptr,
-                               unsigned* gflags = nullptr);
+                               unsigned* gflags = nullptr, int estimate_done = 0);
 size_t exchange_grid_doubles(const Sys& s);
 // SMs the pair tiles should leave free (Sys::reserve_sms) while the exchange
 // runs beside them on another stream.
@@ -97,6 +100,9 @@ constexpr int kExchBandDone = 14;
 // completed (0 when another path solved it): the exterior-force rows skip
 // the entries beyond it, all exact zeros.
 constexpr int kExchBandLast = 15;
+// Index in Sys::xflags of the count of finished blocks of the per-row energy
+// kernel (its last block runs a due FP32 estimate).
+constexpr int kExchRowsCount = 9;
 // The banded solve: weights within kBandMax levels of the diagonal, one CTA
 // of kBandThreads per direction, y of up to kBandMaxN nodes in shared memory.
 constexpr int kBandMax = 64;

@@ -56,6 +56,7 @@ static __device__ __align__(256) double g_exchange_scratch[kScratchDoubles];
 // reads) and clears the work flags.
 __global__ void k_noalloc_prepare(Sys s, const double* __restrict__ ring, int P, int D) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e == 9) s.xflags[kExchRowsCount] = 0;  // the energy kernel's block count
     if (e < 8) {
         s.xflags[e] = (e == 3) ? 1 : 0;  // [3]: compute a fresh estimate
         if (e == 0) {
@@ -172,8 +173,8 @@ extern "C" int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms
     s.err = s.xflags + 8;
     const int n4 = 4 * natoms * ndim;
     k_noalloc_prepare<<<(n4 + 255) / 256, 256, 0, st>>>(s, ring, nbeads, ndim);
-    launch_exchange_energies(s, ndim, st);
-    launch_exchange_recursions(s, 0, st);
+    const int est = launch_exchange_energies(s, ndim, st);
+    launch_exchange_recursions(s, 0, st, nullptr, nullptr, est);
     launch_exchange_forces_mode(s, ndim, 0, st);
     Sys se = s;
     se.P = nbeads;  // primEstimator divides by the true number of beads
