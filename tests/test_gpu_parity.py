@@ -37,6 +37,9 @@ FORCE_CASES = {
     "dist_P1": (dict(natoms=9, nbeads=1, inter="harmonic", int_p=(1.0 * 0.036749326e-3, 0, 0)), dict()),
     "bosons_aziz_pbc_N300_P4": (dict(natoms=300, nbeads=4, T_K=1.5, mass_amu=4.0026, pbc=True, box_ang=24.0,
                                      inter="aziz", cutoff_ang=12.0), dict(spread_ang=0.2)),
+    # every cycle contributes (all weights nonzero): the banded kernel's dense solve
+    "bosons_trap_N100_P4_dense_weights": (dict(natoms=100, nbeads=4, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0)),
+                                          dict(spread_ang=0.05)),
     "bosons_trap_N1100_P3_far_from_equilibrium": (dict(natoms=1100, nbeads=3, ext="harmonic",
                                                        ext_p=(3.0 * 0.036749326e-3, 0, 0), box_ang=40.0),
                                                   dict(spread_ang=3.0)),
