@@ -197,24 +197,6 @@ __device__ __forceinline__ void momenta_pass(const Sys& s, long long step, int s
     }
 }
 
-// A double as a normalised double-float, by bit patterns (no FP64 or
-// conversion-pipe instruction).
-__device__ __forceinline__ dfl::df split_df(double x) {
-    float h, l;
-    split_f32(x, h, l);
-    return dfl::fast_two_sum(h, l);
-}
-// A double rounded to float (to within 2^-24 ulp of round-to-nearest).
-__device__ __forceinline__ float round_f32(double x) {
-    float h, l;
-    split_f32(x, h, l);
-    return h + l;
-}
-// The double of a double-float: the one FP64 instruction of the conversion.
-__device__ __forceinline__ double df_to_f64(dfl::df v) { return f32_to_f64(v.hi) + f32_to_f64(v.lo); }
-// Whether a double is +-0 (integer compare, not a DSETP).
-__device__ __forceinline__ bool f64_is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
-
 // Bytes of one particle's staged position: FP64, x y | z (one 16-byte and
 // one 8-byte shared load per pair in 3D); mixed, hx hy hz lx | ly lz.
 template <int D>
@@ -529,43 +511,6 @@ __device__ void bead_forces_warp(const Sys& s, int b, int lane, unsigned char* s
 // with compensated sums (about 2e-7 relative per term).  The potentials, the
 // triangular solve and the energies stay FP64, as on the FP64 path.
 
-// The weights of every packed entry (row p, column u), both directions, as
-// exch_weight computes them, in double-float: w = exp(-beta (E + Vh_u -
-// Vh_{p+1})) / (p + 1) forward, exp(-beta (E + Vbh_{p+1} - Vbh_u)) / (p + 1)
-// backward.  Arguments above 88 give infinity (the solve then retries with a
-// fresh estimate or the exact recursion), below -88 zero (a weight under
-// 1e-38 of the ones that normalise the row).  `vsm` holds 4 (N + 1) floats.
-__device__ void batch_weights_df(const Sys& s, const dfl::ExpTable& etbl, float* vsm) {
-    using dfl::df;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int N = s.N;
-    float* vh = vsm;               // Vh hi, lo
-    float* vbh = vsm + 2 * (N + 1);  // Vbh hi, lo
-    for (int m = threadIdx.x; m <= N; m += blockDim.x) {
-        split_f32(s.Vh[m], vh[m], vh[N + 1 + m]);
-        split_f32(s.Vbh[m], vbh[m], vbh[N + 1 + m]);
-    }
-    __syncthreads();
-    const df nbeta = dfl::neg(split_df(s.beta_ex));
-    for (int p = warp; p < N; p += nw) {
-        const df inv = split_df(recip_row(p));
-        const df vp = dfl::fast_two_sum(vh[p + 1], vh[N + 2 + p]);
-        const df vbp = dfl::fast_two_sum(vbh[p + 1], vbh[N + 2 + p]);
-        const size_t r = tri(p);
-        for (int u = lane; u <= p; u += 32) {
-            const df E = split_df(s.E[r + u]);
-            const df vu = dfl::fast_two_sum(vh[u], vh[N + 1 + u]);
-            const df tf = dfl::add(dfl::add(E, vu), dfl::neg(vp));
-            s.Wf[r + u] = df_to_f64(dfl::mul(dfl::exp(dfl::mul(nbeta, tf), etbl), inv));
-            if (u >= 1) {
-                const df vbu = dfl::fast_two_sum(vbh[u], vbh[N + 1 + u]);
-                const df tb = dfl::add(dfl::add(E, vbp), dfl::neg(vbu));
-                s.Wb[tri(N - u - 1) + (N - 1 - p)] = df_to_f64(dfl::mul(dfl::exp(dfl::mul(nbeta, tb), etbl), inv));
-            }
-        }
-    }
-}
-
 // Shared floats batch_exchange_forces_f32 stages.
 __host__ __device__ constexpr size_t xforces_f32_floats(int D, int N) { return 4 * (size_t)D * N + 3 * (size_t)N; }
 
@@ -700,7 +645,7 @@ __device__ void batch_exchange(const Sys& s, unsigned char* work, const double* 
             __syncthreads();
         }
         if (kMixed) {
-            batch_weights_df(s, *etbl, reinterpret_cast<float*>(work));
+            weights_df_block(s, *etbl, reinterpret_cast<float*>(work));
         } else {
             for (int p = warp; p < N; p += nw) {
                 const double inv = recip_row(p);

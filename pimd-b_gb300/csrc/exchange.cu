@@ -61,17 +61,25 @@ __global__ void k_exch_energies(Sys s) {
 // forms each chunk's carry from E[v][v] and the chunk totals in the order
 // energy_row adds them, and the warps add it.  The terms, the scans and the
 // carries are energy_row's, operation for operation: the same bits.  The
-// critical path of a row is one chunk instead of all of them.  The block
-// that finishes last runs a due FP32 estimate (k_exch_estimate's phase-0
-// work, both directions in turn), so that the chain has no launch that
-// usually does nothing.  Four blocks per SM bound the registers (the rare
-// estimate's arrays would otherwise set them for every row).
+// critical path of a row is one chunk instead of all of them.
+// The weights follow in the same launch (k_exch_weights' phase-0 work, with
+// its band measurement).  With the previous potentials as the estimate, each
+// block forms its own row's weights (exch_weight, FP64) from the energies it
+// just wrote.  When a fresh estimate is due, the block that finishes last
+// runs it (both directions in turn) and then forms every weight in
+// double-float on the FP32 pipe (weights_df_block; on one SM the FP64
+// exponentials would take a quarter of a millisecond).  Four blocks per SM
+// bound the registers (the rare estimate's arrays would otherwise set them
+// for every row).
 constexpr int kEnergyRowThreads = 256;
 static_assert(kEnergyRowThreads == kWaveThreads, "the estimate runs with the energy kernel's block");
 template <int D>
 __global__ void __launch_bounds__(kEnergyRowThreads, 4) k_exch_energies_rows(Sys s) {
     extern __shared__ double rsm[];  // scans [N], then the chunks' totals and carries
+    __shared__ double wtbl[32];      // exp_tang's table
     const int v = blockIdx.x, N = s.N;
+    if (threadIdx.x < 32) wtbl[threadIdx.x] = kExp2Table[threadIdx.x];
+    const int fresh = ((volatile int*)s.xflags)[3];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int first = 0, last = s.P - 1;
     const double hk = 0.5 * s.kappa;
@@ -127,6 +135,15 @@ __global__ void __launch_bounds__(kEnergyRowThreads, 4) k_exch_energies_rows(Sys
         // backward node r = N - u depends on node r' = N - 1 - v
         if (u >= 1) s.Et[tri(N - u - 1) + (N - 1 - v)] = val;
     }
+    if (!fresh) {
+        __syncthreads();  // this row's energies, written by the block
+        const double inv = recip_row(v);
+        int band = 0;
+        for (int u = threadIdx.x; u <= v; u += blockDim.x)
+            if (exch_weight(s, v, u, inv, wtbl)) band = max(band, v + 1 - u);
+        band = __reduce_max_sync(0xffffffffu, band);
+        if ((threadIdx.x & 31) == 0 && band > 0) atomicMax(&s.xflags[kExchBand], band);
+    }
     __shared__ int is_last;
     __threadfence();
     __syncthreads();
@@ -134,7 +151,6 @@ __global__ void __launch_bounds__(kEnergyRowThreads, 4) k_exch_energies_rows(Sys
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    const int fresh = ((volatile int*)s.xflags)[3];
     if (threadIdx.x == 0) {
         s.xflags[kExchRowsCount] = 0;
         s.xflags[7] = !fresh;
@@ -144,13 +160,20 @@ __global__ void __launch_bounds__(kEnergyRowThreads, 4) k_exch_energies_rows(Sys
     estimate_direction(s, 0, reinterpret_cast<float*>(rsm));
     __syncthreads();
     estimate_direction(s, 1, reinterpret_cast<float*>(rsm));
+    __syncthreads();
+    __shared__ dfl::ExpTable etbl;
+    fill_exp_table_df(etbl);
+    __syncthreads();
+    int band = weights_df_block(s, etbl, reinterpret_cast<float*>(rsm));
+    band = __reduce_max_sync(0xffffffffu, band);
+    if ((threadIdx.x & 31) == 0 && band > 0) atomicMax(&s.xflags[kExchBand], band);
 }
 
 // Whether the cycle energies of s come from k_exch_energies_rows (which then
-// also runs the phase-0 estimate).
+// also runs the phase-0 estimate and weights).
 static size_t energies_rows_smem(const Sys& s) {
     return std::max(sizeof(double) * ((size_t)s.N + 2 * (((size_t)s.N + 31) / 32) + 2),
-                    sizeof(float) * 3 * ((size_t)s.N + 1));
+                    sizeof(float) * 4 * ((size_t)s.N + 1));
 }
 static bool energies_by_rows(const Sys& s, const double* work) {
     return !(work && s.eflat) && energies_rows_smem(s) <= 48 * 1024;
@@ -939,8 +962,10 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
             k_exch_estimate<<<2, kWaveThreads, esmem, st>>>(s, phase);
             ++n;
         }
-        k_exch_weights<<<phase ? rgrid : wgrid, 256, 0, st>>>(s, phase);
-        ++n;
+        if (!(phase == 0 && estimate_done)) {  // else the energy kernel formed them
+            k_exch_weights<<<phase ? rgrid : wgrid, 256, 0, st>>>(s, phase);
+            ++n;
+        }
         // banded weights: one CTA per direction; otherwise the solve on a
         // cluster below the multi-SM solve's size, across SMs from it
         int banded = 0;

@@ -251,6 +251,52 @@ __device__ inline void weights_direction(const Sys& s, int dir, const double* tb
         for (int u = threadIdx.x; u <= p; u += blockDim.x) exch_weight(s, p, u, inv, tbl, dir);
     }
 }
+// The weights of every packed entry (row p, column u), both directions, as
+// exch_weight computes them, in double-float on the FP32 pipe, by one block
+// (the batched engine's mixed path; the one block that ran a fresh
+// estimate): w = exp(-beta (E + Vh_u - Vh_{p+1})) / (p + 1) forward,
+// exp(-beta (E + Vbh_{p+1} - Vbh_u)) / (p + 1) backward.  Arguments above 88 give infinity (the solve then retries with a
+// fresh estimate or the exact recursion), below -88 zero (a weight under
+// 1e-38 of the ones that normalise the row).  `vsm` holds 4 (N + 1) floats.
+// Returns this thread's band: the largest p + 1 - u of a nonzero weight.
+__device__ inline int weights_df_block(const Sys& s, const dfl::ExpTable& etbl, float* vsm) {
+    using dfl::df;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int N = s.N;
+    float* vh = vsm;               // Vh hi, lo
+    float* vbh = vsm + 2 * (N + 1);  // Vbh hi, lo
+    for (int m = threadIdx.x; m <= N; m += blockDim.x) {
+        split_f32(s.Vh[m], vh[m], vh[N + 1 + m]);
+        split_f32(s.Vbh[m], vbh[m], vbh[N + 1 + m]);
+    }
+    __syncthreads();
+    const df nbeta = dfl::neg(split_df(s.beta_ex));
+    int band = 0;
+    for (int p = warp; p < N; p += nw) {
+        const df inv = split_df(recip_row(p));
+        const df vp = dfl::fast_two_sum(vh[p + 1], vh[N + 2 + p]);
+        const df vbp = dfl::fast_two_sum(vbh[p + 1], vbh[N + 2 + p]);
+        const size_t r = tri(p);
+        for (int u = lane; u <= p; u += 32) {
+            const df E = split_df(s.E[r + u]);
+            const df vu = dfl::fast_two_sum(vh[u], vh[N + 1 + u]);
+            const df tf = dfl::add(dfl::add(E, vu), dfl::neg(vp));
+            const double wf = df_to_f64(dfl::mul(dfl::exp(dfl::mul(nbeta, tf), etbl), inv));
+            s.Wf[r + u] = wf;
+            bool nz = !f64_is_zero(wf);
+            if (u >= 1) {
+                const df vbu = dfl::fast_two_sum(vbh[u], vbh[N + 1 + u]);
+                const df tb = dfl::add(dfl::add(E, vbp), dfl::neg(vbu));
+                const double wb = df_to_f64(dfl::mul(dfl::exp(dfl::mul(nbeta, tb), etbl), inv));
+                s.Wb[tri(N - u - 1) + (N - 1 - p)] = wb;
+                nz = nz || !f64_is_zero(wb);
+            }
+            if (nz) band = max(band, p + 1 - u);
+        }
+    }
+    return band;
+}
+
 // Exact level-by-level FP64 log-sum-exp in the reference's order (used only
 // when the estimate is unusable, or on request).  `vs` holds N+1 doubles,
 // `red` 32.

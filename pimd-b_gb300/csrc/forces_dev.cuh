@@ -140,6 +140,24 @@ __device__ __forceinline__ double exp_tang256(double x, const double* tbl) {
     return n < -258560 ? 0.0 : __hiloint2double(hi, __double2loint(y));
 }
 
+// A double as a normalised double-float, by bit patterns (no FP64 or
+// conversion-pipe instruction).
+__device__ __forceinline__ dfl::df split_df(double x) {
+    float h, l;
+    split_f32(x, h, l);
+    return dfl::fast_two_sum(h, l);
+}
+// A double rounded to float (to within 2^-24 ulp of round-to-nearest).
+__device__ __forceinline__ float round_f32(double x) {
+    float h, l;
+    split_f32(x, h, l);
+    return h + l;
+}
+// The double of a double-float: the one FP64 instruction of the conversion.
+__device__ __forceinline__ double df_to_f64(dfl::df v) { return f32_to_f64(v.hi) + f32_to_f64(v.lo); }
+// Whether a double is +-0 (integer compare, not a DSETP).
+__device__ __forceinline__ bool f64_is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+
 // A block fills `t` with 2^(j/256) as double-floats (bit patterns of the
 // FP64 table; no FP64 instruction).  The caller synchronises.
 __device__ __forceinline__ void fill_exp_table_df(dfl::ExpTable& t) {

@@ -62,11 +62,12 @@ void launch_local_energy(const Sys& s, int D, int n, const int* items, double* o
 // For N >= 512 with `work` (exchange_energy_doubles) the energies come from
 // the links' prefix sums, one independent entry per thread.
 // Returns 1 when the per-row energy kernel ran, which also runs a due FP32
-// estimate (pass `estimate_done` = 1 to launch_exchange_recursions).
+// estimate and forms the weights (pass `estimate_done` = 1 to
+// launch_exchange_recursions).
 int launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work = nullptr);
 size_t exchange_energy_doubles(const Sys& s, int D);
-// Returns the number of kernels launched: the estimate (unless the energy
-// kernel ran it), the weights and the solve kernels (with their retry phase
+// Returns the number of kernels launched: the estimate and the weights
+// (unless the energy kernel formed them) and the solve kernels (with their retry phase
 // from 768 particles), or 1 with `exact` (the reference-order FP64
 // log-sum-exp recursion only).  With `ysol` (exchange_grid_doubles) below 768
 // particles the banded kernel is the whole solve; from 768 the solve runs
