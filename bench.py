@@ -389,8 +389,8 @@ SCREEN_OPS_PER_PAIR = 12
 # profiles/pair_tiles_compact_aziz_pbc_N256_P64_fp64.md): DRAM bytes read +
 # written, pipe utilisation over active cycles, warps active and
 # warp-instructions issued per SM cycle (of 4).
-PAIR_NCU = {"dram_bytes": 470784, "fma_pipe_active": 0.286, "alu_pipe_active": 0.175, "warps_active": 0.147,
-            "issue_per_sm_cycle": 1.77, "duration_us_cold": 75.6}
+PAIR_NCU = {"dram_bytes": 475648, "fma_pipe_active": 0.320, "alu_pipe_active": 0.196, "warps_active": 0.164,
+            "issue_per_sm_cycle": 1.98, "duration_us_cold": 62.5}
 
 
 class ClockSampler:
