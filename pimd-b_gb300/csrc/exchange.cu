@@ -36,8 +36,6 @@
 // as Vh and pass 1 is skipped; a solve that fails with them is retried from
 // a fresh estimate, inside k_exch_solve below the multi-SM solve's size and
 // by the phase-1 launches from there on.
-#include <cooperative_groups.h>
-
 #include <algorithm>
 #include <atomic>
 
@@ -701,115 +699,6 @@ size_t banded_solve_smem(const Sys& s) {
     return sizeof(double) * ((((size_t)s.N + 2) & ~(size_t)1) + 2 * 1024 + 2 * 2048);
 }
 
-// ---------------------------------------------------------------------------
-// Pass 3 on a thread-block cluster, below the multi-SM solve's size.  On one
-// block the solve's N^2/2 FP64 multiply-adds are bound by a single SM's FP64
-// pipe (2 lanes per clock).  Here each direction runs on a cluster of C CTAs
-// (C <= 8, one per SM, beside the pair kernel's blocks: a CTA needs a few KB
-// of shared memory).  The 32-row blocks go round-robin to the CTAs.  For
-// every block j in order, its owner resolves the diagonal block with warp
-// shuffles (its rows hold the contributions of blocks < j) and publishes y_j
-// in its own shared memory; after a cluster barrier every CTA reads y_j
-// through distributed shared memory and adds W[rows][block j] y_j to the
-// rows it owns, the owner of block j + 1 those rows first (they are the
-// next diagonal block's input).  The barrier is the hardware cluster
-// barrier: no flags, no polling.  Same arithmetic and summation order per
-// row as k_exch_solve_grid; k_exch_solve then post-processes y (pre).
-constexpr int kClusterSolveMax = 8;
-constexpr int kClusterSolveThreads = 256;
-
-__global__ void __launch_bounds__(kClusterSolveThreads) k_exch_solve_cluster(Sys s, int phase, double* ysol,
-                                                                            int banded) {
-    namespace cg = cooperative_groups;
-    cg::cluster_group cl = cg::this_cluster();
-    if (phase == 1 && ((volatile int*)s.xflags)[6] == 0) return;  // uniform over the cluster
-    if (banded && ((volatile int*)s.xflags)[kExchBand] <= kBandMax) return;  // k_exch_solve_band solved it
-    const int C = (int)cl.num_blocks(), c = (int)cl.block_rank();
-    const int dir = blockIdx.x / C;
-    const int nn = dir == 0 ? s.N + 1 : s.N;
-    const double* __restrict__ W = dir == 0 ? s.Wf : s.Wb;
-    double* y = ysol + (size_t)dir * (s.N + 1);
-    const int nb = (nn + 31) / 32;
-    const int nown = (nb - c + C - 1) / C;  // blocks c, c + C, ...
-    const int nmax = (nb + C - 1) / C;      // the most any CTA owns: the same layout in every CTA
-    extern __shared__ double csm[];
-    // yown first, at the same offset in every CTA: the other CTAs map this
-    // CTA's address of it onto their own (map_shared_rank)
-    double* yown = csm;                      // [nmax][32]: y of the owned blocks
-    double* acc = csm + (size_t)nmax * 32;   // [nmax][32]
-    double* yj = acc + (size_t)nmax * 32;    // [32]
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int e = tid; e < nown * 32; e += blockDim.x) acc[e] = 0.0;
-    __syncthreads();
-    auto diag = [&](int b) {  // warp 0 of the owner of block b
-        const int n = 32 * b + lane;
-        double a = n == 0 ? 1.0 : (n < nn ? acc[(b / C) * 32 + lane] : 0.0);
-        double w[32];
-#pragma unroll
-        for (int t = 0; t < 32; ++t) w[t] = (n < nn && n >= 1 && t < lane) ? W[tri(n - 1) + 32 * b + t] : 0.0;
-#pragma unroll
-        for (int t = 0; t < 32; ++t) {
-            const double yt = __shfl_sync(0xffffffffu, a, t);
-            if (lane > t) a = fma(w[t], yt, a);
-        }
-        yown[(b / C) * 32 + lane] = n < nn ? a : 0.0;
-        if (n < nn) y[n] = a;
-    };
-    const int i = tid >> 3, part = tid & 7;  // fold role: row of the block, quarter of the columns
-    auto fold = [&](int r, int j) {          // owned block r += W[rows of r][block j] y_j
-        const int n = 32 * r + i;
-        double sum = 0.0;
-        if (n < nn) {
-            const double* row = W + tri(n - 1) + 32 * j + 4 * part;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) sum = fma(row[q], yj[4 * part + q], sum);
-        }
-        sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-        sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-        sum += __shfl_xor_sync(0xffffffffu, sum, 4);
-        if (part == 0 && n < nn) acc[(r / C) * 32 + i] += sum;
-    };
-    if (c == 0 && warp == 0) diag(0);
-    for (int j = 0; j + 1 < nb; ++j) {
-        cl.sync();  // y_j is published (release / acquire over the cluster)
-        if (tid < 32) {
-            const double* src = cl.map_shared_rank(yown, j % C);
-            yj[tid] = src[(j / C) * 32 + tid];
-        }
-        __syncthreads();
-        const int jn = j + 1;
-        if (jn % C == c) {
-            fold(jn, j);
-            __syncthreads();
-            if (warp == 0) diag(jn);
-        }
-        for (int r = jn + (c - jn % C + C) % C; r < nb; r += C) {  // the owned blocks from jn on
-            if (r == jn) continue;                                 // folded above by its owner
-            fold(r, j);
-        }
-        __syncthreads();
-    }
-    cl.sync();  // no CTA leaves while another may still read its y
-}
-
-static bool cluster_solve(const Sys& s, int phase, double* ysol, int banded, cudaStream_t st) {
-    const int nb = (s.N + 1 + 31) / 32;
-    const int C = nb < kClusterSolveMax ? nb : kClusterSolveMax;
-    const int nown = (nb + C - 1) / C;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(2 * C);
-    cfg.blockDim = dim3(kClusterSolveThreads);
-    cfg.dynamicSmemBytes = sizeof(double) * (2 * (size_t)nown * 32 + 32);
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = C;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_exch_solve_cluster, s, phase, ysol, banded) == cudaSuccess;
-}
 
 // Exterior spring forces: one warp per row (bead P) or column (bead 1).
 template <int D>
@@ -896,8 +785,8 @@ int launch_exchange_energies(const Sys& s, int D, cudaStream_t st, double* work)
     return 0;
 }
 
-// y of both directions for the cluster solve (below kGridSolveMinN) or the
-// multi-SM solve; publication flags for the latter.
+// y of both directions for the banded solve and the multi-SM solve;
+// publication flags for the latter.
 size_t exchange_grid_doubles(const Sys& s) { return 2 * ((size_t)s.N + 1); }
 size_t exchange_grid_flags(const Sys& s) {
     return s.N >= kGridSolveMinN ? 2 * (((size_t)s.N + 1 + 31) / 32) + 1 : 1;
@@ -966,8 +855,8 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
             k_exch_weights<<<phase ? rgrid : wgrid, 256, 0, st>>>(s, phase);
             ++n;
         }
-        // banded weights: one CTA per direction; otherwise the solve on a
-        // cluster below the multi-SM solve's size, across SMs from it
+        // the banded kernel (one CTA per direction): below the multi-SM
+        // solve's size the whole pass 3, from it the banded case only
         int banded = 0;
         if (ysol && banded_solve_fits(s)) {
             const size_t bs = std::max(banded_solve_smem(s), least);
@@ -978,8 +867,9 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
             ++n;
         }
         if (standalone) continue;
-        const bool dense = ysol && (inline_retry ? cluster_solve(s, phase, ysol, banded, st)
-                                                 : gflags && grid_solve(s, phase, ysol, gflags, banded, st));
+        // from kGridSolveMinN the dense solve runs across SMs; below it (no
+        // ysol) k_exch_solve solves on its own block
+        const bool dense = ysol && !inline_retry && gflags && grid_solve(s, phase, ysol, gflags, banded, st);
         const bool pre = banded || dense;
         k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 0, phase, pre ? ysol : nullptr, inline_retry);
         n += dense ? 2 : 1;

@@ -198,7 +198,7 @@ def test_benchmark_system_trajectory(options):
             for got, want, label in ((gx, tr.x, "x"), (gp, tr.p, "p"), (gf, tr.f, "f")):
                 assert rel_per_bead(got, want) < TRAJ_TOL, (st, label)
         hx, hp, hf = h.get_state()
-        # smooth dynamics: the fast path (reused estimate, cluster solve)
+        # smooth dynamics: the fast path (reused estimate, banded solve)
         # served every evaluation, none was redone from a fresh estimate
         assert g.exchange_retries() == 0 and h.exchange_retries() == 0
     for got, want, label in ((hx, tr.x, "x"), (hp, tr.p, "p"), (hf, tr.f, "f")):
