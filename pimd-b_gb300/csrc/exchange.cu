@@ -628,6 +628,7 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
     if (!dense) stage(0, 0, blockDim.x);
     __syncthreads();
     const int i = tid >> 3, part = tid & 7;  // fold role: row of the block, 8 of its 64 columns
+    const int dband = dense ? 32 : band;  // the diagonal chain's reach
     for (int b = 0; b < (dense ? 0 : nb); ++b) {
         const double* f = wfold + (b & 1) * 2048;
         double sum = 0.0;
@@ -645,10 +646,12 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
             const double* d = wdiag + (b & 1) * 1024;
             const int m = 32 * b + lane;
             double a = m == 0 ? 1.0 : (m < nn ? accb[lane] : 0.0);
+            // lanes more than `band` below t hold exact zero weights for t:
+            // only the band's lanes issue the multiply-add
 #pragma unroll
             for (int t = 0; t < 32; ++t) {
                 const double yt = __shfl_sync(0xffffffffu, a, t);
-                if (lane > t) a = fma(d[lane * 32 + t], yt, a);
+                if (lane > t && lane - t <= dband) a = fma(d[lane * 32 + t], yt, a);
             }
             if (m < nn) {
                 ys[m] = a;
