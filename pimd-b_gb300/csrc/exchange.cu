@@ -632,10 +632,12 @@ __global__ void __launch_bounds__(kBandThreads) k_exch_solve_band(Sys s, int pha
     for (int b = 0; b < (dense ? 0 : nb); ++b) {
         const double* f = wfold + (b & 1) * 2048;
         double sum = 0.0;
+        // columns more than `band` before the block's first row hold exact
+        // zero weights: no multiply-add for them
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int col = 8 * part + q, c = 32 * b - 64 + col;
-            if (c >= 0) sum = fma(f[i * 64 + col], ys[c], sum);
+            if (c >= 0 && col >= 64 - band) sum = fma(f[i * 64 + col], ys[c], sum);
         }
         sum += __shfl_xor_sync(0xffffffffu, sum, 1);
         sum += __shfl_xor_sync(0xffffffffu, sum, 2);
