@@ -13,18 +13,23 @@
 //           (the block-level pieces shared with the one-system kernels)
 //   tail    B half-kick, O-step (substep 1), COM removal
 // in the order of src/simulation.cpp:246-259 with the cartesian propagator
-// (src/propagators/velocity_verlet.cpp:7-38) and the Langevin thermostat
-// (src/thermostats/langevin.cpp:10-27).  Nothing waits on another CTA: the
-// only cross-CTA state is the work counter, reset by the CTA that finishes
-// last, which also advances the device-side step counter, so a sequence of
-// step launches can be captured once in a CUDA graph and replayed.
+// (src/propagators/velocity_verlet.cpp:7-38) or the normal-mode one
+// (src/propagators/normal_modes_propagator.cpp:19-71) and the Langevin
+// thermostat (src/thermostats/langevin.cpp:10-27) in either frame.  Nothing
+// waits on another CTA: the only cross-CTA state is the work counter, reset
+// by the CTA that finishes last, which also advances the device-side step
+// counter, so a sequence of step launches can be captured once in a CUDA
+// graph and replayed.
 //
 // Precision: `R` is the pair-force arithmetic.  R = double is the FP64 path
-// (same noise, formulas and exchange as the one-system path).  R = float
-// computes pair separations from hi/lo float pairs and pair gradients in
-// FP32, sums each 32-particle tile in FP32 and accumulates tiles in FP64,
-// and draws the Langevin normals with FP32 Box-Muller from the same Philox
-// bits; the exchange recursions and the integrator stay FP64.
+// (same noise, formulas and exchange as the one-system path; harmonic and
+// dipole pairs in double-float, bead_pairs_df).  R = float computes pair
+// separations from hi/lo float pairs and pair gradients in FP32, sums each
+// 32-particle tile in FP32 and accumulates tiles in FP64, forms the
+// exchange weights in double-float and the exterior spring forces in FP32
+// with compensated sums; the potentials, the triangular solve, the cycle
+// energies and the integrator stay FP64.  Both draw the Langevin normals
+// with FP32 Box-Muller from the same Philox bits.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
