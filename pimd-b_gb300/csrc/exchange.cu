@@ -1,9 +1,10 @@
 // Feldman-Hirshberg bosonic exchange on the first and last beads.
 //
 // Reference: BosonicExchange (src/bosonic_exchange/quadratic_bosonic_exchange.cpp)
-//   evaluateCycleEnergies :34-61            -> k_exch_energies
+//   evaluateCycleEnergies :34-61            -> k_exch_energies_rows (below 512
+//                                              particles), k_exch_energies_flat
 //   evaluateVBn :73-99, evaluateVBackwards :101-128
-//                                           -> k_exch_estimate + k_exch_weights + k_exch_solve
+//                                           -> estimate + weights + solve (below)
 //   evaluateConnectionProbabilities :142-157,
 //   springForceLastBead / springForceFirstBead :159-215
 //                                           -> k_exch_forces (probabilities formed on the fly)
@@ -34,8 +35,14 @@
 // is handled the same way by the second block of each kernel.
 // Usually the previous evaluations' potentials (extrapolated linearly) serve
 // as Vh and pass 1 is skipped; a solve that fails with them is retried from
-// a fresh estimate, inside k_exch_solve below the multi-SM solve's size and
+// a fresh estimate, in the solving block below the multi-SM solve's size and
 // by the phase-1 launches from there on.
+// Launches per evaluation below 512 particles: k_exch_energies_rows (the
+// energies, a due estimate in its last block, the weights), then
+// k_exch_solve_band (pass 3 whole: banded or dense solve, post-processing,
+// retry, finish), then k_exch_forces.  From 512 particles the passes run as
+// the separate kernels named above, the solve across SMs from 768
+// (k_exch_solve_grid) unless the weights are banded.
 #include <algorithm>
 #include <atomic>
 
