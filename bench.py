@@ -137,6 +137,33 @@ def batched_workload(precision, n=512, seed=12345):
 # ordered pair (each unique pair twice).
 DF_OPS_PER_BATCH_PAIR = 141
 
+# The exchange's FP64 accounting per evaluation: about 19 N^2 FLOPs and
+# 1.5 N^2 exponentials (cycle energies, both recursions, the exterior
+# forces).  The recursions are sequential in their levels (N + 1 forward, N
+# backward, the two directions side by side, one SM each), so the chain is
+# reported as time per level, a latency bound, beside its FP64 rate.
+EXCH_FLOP_PER_N2 = 19.0
+EXCH_EXP_PER_N2 = 1.5
+
+
+def exchange_latency(per_class_ms, N, fp64_peak_tflops):
+    """The exchange chain of one step from the event-timed kernel classes
+    (ms per step): its classes, ns per recursion level and its FP64 rate
+    against the FP64 peak.  None when the step ran no exchange."""
+    keys = sorted(k for k in per_class_ms if k.startswith("exch_"))
+    if not keys or N < 1:
+        return None
+    chain = sum(per_class_ms[k] for k in keys)
+    rec = per_class_ms.get("exch_recursions", 0.0)
+    flops = EXCH_FLOP_PER_N2 * N * N
+    rate = flops / (chain * 1e-3) / 1e12
+    return {"chain_ms_per_step": chain, "classes": {k: per_class_ms[k] for k in keys},
+            "levels_per_direction": N + 1, "ns_per_level": rec * 1e6 / (N + 1),
+            "fp64_flop_per_step": flops, "exp_per_step": EXCH_EXP_PER_N2 * N * N,
+            "fp64_tflops": rate, "vs_fp64_peak": rate / fp64_peak_tflops,
+            "bound": "latency: the recursions are sequential in their levels",
+            "note": "each class event-timed on its own; in a step the chain overlaps the pair kernel"}
+
 
 def batched_roofline(cfgs, t_step, precision, peaks):
     """The ensemble step against its roofline, by the accounting of the
@@ -777,6 +804,9 @@ def main():
                        "l2": head["l2"]},
             "e2e": e2e, "roofline": roof, "gpu_launches": head["gpu_launches"], "clocks": clocks,
             "peaks": peaks}
+    xl = exchange_latency(roof["per_class_ms_per_step"], N, fp64_peak)
+    if xl:
+        line["exchange"] = xl
     if others:
         line["systems"] = others
     if batched:

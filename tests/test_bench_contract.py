@@ -41,3 +41,22 @@ def test_reference_arm_other_ranks_do_no_work():
     r = _run({"RANK": "1", "WORLD_SIZE": "2"})
     assert r.returncode == 0, r.stderr[-2000:]
     assert not [l for l in r.stdout.splitlines() if l.strip().startswith("{")]
+
+
+def test_exchange_latency_accounting():
+    """The exchange chain's report: ns per recursion level from the
+    recursions class, and its FP64 rate from 19 N^2 FLOPs over the chain's
+    classes; nothing for a step without exchange."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    per_class = {"bead_forces": 0.070, "exch_energies": 0.019, "exch_recursions": 0.0432, "exch_forces": 0.0104,
+                 "nm_propagate": 0.028}
+    x = bench.exchange_latency(per_class, 256, 1.25)
+    assert x["levels_per_direction"] == 257
+    assert abs(x["ns_per_level"] - 0.0432e6 / 257) < 1e-9
+    assert abs(x["chain_ms_per_step"] - (0.019 + 0.0432 + 0.0104)) < 1e-12
+    assert set(x["classes"]) == {"exch_energies", "exch_recursions", "exch_forces"}
+    assert abs(x["fp64_tflops"] - 19.0 * 256 ** 2 / (x["chain_ms_per_step"] * 1e-3) / 1e12) < 1e-12
+    assert abs(x["vs_fp64_peak"] - x["fp64_tflops"] / 1.25) < 1e-12
+    assert x["exp_per_step"] == 1.5 * 256 ** 2
+    assert bench.exchange_latency({"bead_forces": 0.07, "cart_update": 0.03}, 256, 1.25) is None
