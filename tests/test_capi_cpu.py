@@ -109,3 +109,38 @@ def test_create_validates_before_touching_the_gpu():
     c = pk.make_config(natoms=0)
     with pytest.raises(pk.ConfigError):
         pk.System(c)
+
+
+def test_integration_snippets_compile_against_the_header(tmp_path):
+    """Every C++ snippet of INTEGRATION.md that uses only the C ABI compiles
+    against include/pimdb_gb300.h (g++ -fsyntax-only), so the documented calls
+    keep the header's names, argument counts and types.  The caller's own
+    variables are declared by the stub below; `= ...;` placeholders become
+    value-initialisation.  The BosonicExchange snippet needs the reference's
+    own headers and is left out."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not found")
+    text = (ROOT / "INTEGRATION.md").read_text()
+    blocks = re.findall(r"```cpp\n(.*?)```", text, re.S)
+    abi = [b for b in blocks if "pimdb_" in b and "BosonicExchangeBase" not in b]
+    assert len(abi) >= 4
+    stub = """#include <stdexcept>
+#include <vector>
+#include "pimdb_gb300.h"
+static double x_all_beads[1], p_all_beads[1], x[1], p[1], f[1], g_first[1], g_last[1];
+static double x_all[1], p_all[1], f_all[1];
+static const long steps = 1, sfreq = 1;
+static const int NDIM = 3;
+static double dLoss_dVB(double v) { return v; }
+static pimdb_handle* h = nullptr;
+"""
+    fixed = [re.sub(r"= \.\.\.;", "{};", blk) for blk in abi]
+    body = "".join(f"void snippet_{k}() {{\n{blk}}}\n" for k, blk in enumerate(fixed))
+    src = tmp_path / "snippets.cpp"
+    src.write_text(stub + body)
+    r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wno-unused", "-I", str(ROOT / "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
