@@ -144,3 +144,27 @@ static pimdb_handle* h = nullptr;
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wno-unused", "-I", str(ROOT / "include"), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_integration_bosonic_exchange_snippet_compiles_against_the_reference(tmp_path):
+    """The guide's GpuBosonicExchange overrides the reference's own
+    BosonicExchangeBase (include/bosonic_exchange/bosonic_exchange_base.h):
+    compiled with g++ -fsyntax-only against the reference's headers (and
+    the oracle's MPI declarations), every `override` must match.  Skipped
+    where the reference checkout is absent."""
+    import shutil
+    import subprocess
+    from oracle import build_ref
+    ref = build_ref.DEFAULT_REF
+    gxx = shutil.which("g++")
+    if gxx is None or not (ref / "include" / "bosonic_exchange" / "bosonic_exchange_base.h").exists():
+        pytest.skip("reference checkout or g++ not available")
+    text = (ROOT / "INTEGRATION.md").read_text()
+    blk = [b for b in re.findall(r"```cpp\n(.*?)```", text, re.S) if "BosonicExchangeBase" in b]
+    assert len(blk) == 1
+    src = tmp_path / "gpu_bosonic_exchange.cpp"
+    src.write_text("#include <algorithm>\n#include <stdexcept>\n#include <vector>\n" + blk[0])
+    r = subprocess.run([gxx, "-std=c++20", "-fsyntax-only", "-I", str(ref / "include"), "-I",
+                        str(ROOT / "oracle" / "ref"), "-I", str(ROOT / "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
