@@ -180,8 +180,12 @@ static size_t energies_rows_smem(const Sys& s) {
     return std::max(sizeof(double) * ((size_t)s.N + 2 * (((size_t)s.N + 31) / 32) + 2),
                     sizeof(float) * 4 * ((size_t)s.N + 1));
 }
+// The kernel's static shared memory (exp_tang's table, the double-float
+// exponential table, the last-block flag) counts against the 48 KB that a
+// launch gets without opting in to more.
+constexpr size_t kRowsStaticSmem = 32 * sizeof(double) + sizeof(dfl::ExpTable) + 64;
 static bool energies_by_rows(const Sys& s, const double* work) {
-    return !(work && s.eflat) && energies_rows_smem(s) <= 48 * 1024;
+    return !(work && s.eflat) && energies_rows_smem(s) + kRowsStaticSmem <= 48 * 1024;
 }
 
 // Cycle energies for large N without a scan per row.  The row recursion
@@ -759,6 +763,16 @@ static void exchange_carveouts() {
 
 int exchange_flat_default(int N) { return N >= kFlatEnergiesMinN ? 1 : 0; }
 
+// A launch gets 48 KB of shared memory without opting in, static and
+// dynamic together.  The kernels here hold up to about 2.3 KB of static
+// shared memory (their exponential tables), so a dynamic size within
+// kSmemOptInMargin of 48 KB opts in as well; opting in when the default
+// would have done is harmless.
+constexpr size_t kSmemOptInMargin = 8 * 1024;
+static void opt_in_smem(const void* k, size_t dyn) {
+    if (dyn + kSmemOptInMargin > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+}
+
 // The work array of the prefix-sum energies (any N: Sys::eflat chooses).
 size_t exchange_energy_doubles(const Sys& s, int D) { return (size_t)(2 + 2 * D) * s.N; }
 
@@ -843,9 +857,8 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
     const size_t least = s.reserve_sms ? 116 * 1024 : 0;
     const size_t esmem = std::max(sizeof(float) * 3 * (size_t)(s.N + 1), least);
     const size_t smem = std::max(sizeof(double) * (2 * (size_t)(s.N + 1) + 32), least);
-    if (esmem + 1024 > 48 * 1024)
-        cudaFuncSetAttribute(k_exch_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem);
-    if (smem + 1024 > 48 * 1024) cudaFuncSetAttribute(k_exch_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    opt_in_smem((const void*)k_exch_estimate, esmem);
+    opt_in_smem((const void*)k_exch_solve, smem);
     if (exact) {
         k_exch_solve<<<2, kWaveThreads, smem, st>>>(s, 1, 0, nullptr, 0);
         return 1;
@@ -872,8 +885,7 @@ int launch_exchange_recursions(const Sys& s, int exact, cudaStream_t st, double*
         int banded = 0;
         if (ysol && banded_solve_fits(s)) {
             const size_t bs = std::max(banded_solve_smem(s), least);
-            if (bs + 1024 > 48 * 1024)
-                cudaFuncSetAttribute(k_exch_solve_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bs);
+            opt_in_smem((const void*)k_exch_solve_band, bs);
             k_exch_solve_band<<<2, kBandThreads, bs, st>>>(s, phase, ysol, standalone);
             banded = 1;
             ++n;
@@ -910,7 +922,7 @@ void launch_exchange_estimators(const Sys& s, cudaStream_t st) {
     const size_t smem = sizeof(double) * (size_t)(s.N + 1 + 32);
     int t = ((s.N + 31) / 32) * 32;
     t = t > 512 ? 512 : (t < 32 ? 32 : t);
-    if (smem + 1024 > 48 * 1024) cudaFuncSetAttribute(k_exch_estimators, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    opt_in_smem((const void*)k_exch_estimators, smem);
     k_exch_estimators<<<1, t, smem, st>>>(s, s.P);
 }
 

@@ -31,7 +31,7 @@ import pytest
 
 import bench
 from oracle import oracle as O
-from tests.gpu_cases import pk, rel_per_bead
+from tests.gpu_cases import case, pk, rel_per_bead, ring
 
 pytestmark = pytest.mark.gpu
 
@@ -352,3 +352,23 @@ def test_ensemble_trajectories_of_a_stratified_sample():
         for st in range(10):
             assert tr.step(O.philox_noise_device(c64[r].seed, c64[r].replica, st, s.nbeads, s.natoms, 3)) == 0
         assert rel_per_bead(bx[k], tr.x) < TRAJ_TOL and rel_per_bead(bp[k], tr.p) < TRAJ_TOL, r
+
+
+@pytest.mark.parametrize("flat", [0, 1])
+def test_exchange_energy_forms_at_2950_particles(flat):
+    """Both cycle-energy forms at N = 2950: the link prefix sums (flat 1)
+    and, with the flat form off, the warp-per-row kernel.  At this size the
+    per-row kernel's scans would fit 48 KB of shared memory on their own but
+    not beside its static tables, and the one-block solve's dynamic shared
+    memory is within its static tables of 48 KB: both launches must count
+    the static part.  Results as the full-size checks, with the exterior
+    forces against the recursion's measured conditioning."""
+    s, cfg = case(natoms=2950, nbeads=2, ext="harmonic", ext_p=(3.0 * 0.036749326e-3, 0, 0), box_ang=60.0)
+    x = ring(s, seed=29, spread_ang=3.0)
+    ref = O.exchange(s, x)
+    with pk.System(cfg) as g:
+        g.set_option("flat_energies", flat)
+        g.set_state(x, np.zeros_like(x))
+        ex = g.exchange()
+        arr = g.exchange_arrays()
+    check_exchange(ex, arr, ref, s, x)
