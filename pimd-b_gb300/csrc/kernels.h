@@ -109,6 +109,13 @@ constexpr int kExchRowsCount = 9;
 constexpr int kBandMax = 64;
 constexpr int kBandThreads = 256;
 constexpr int kBandMaxN = 8192;
+// The largest bosonic system: the one-block solve holds 2 (N + 1) + 32
+// doubles of dynamic shared memory beside about 2 KB of static tables, and
+// a block gets at most 227 KB (sm_103a), which allows N = 14382; 14000
+// leaves room for the static part to grow.
+constexpr int kExchangeMaxN = 14000;
+static_assert(sizeof(double) * (2 * (kExchangeMaxN + 1) + 32) + 4096 <= 227 * 1024,
+              "the one-block solve's shared memory at the largest bosonic system");
 // The cotangent of V_B on beads 1 and P into fx: vb_bar * dV_B/dx (the
 // exterior spring forces' exchange part times -vb_bar).
 void launch_exchange_adjoint(const Sys& s, int D, double vb_bar, cudaStream_t st);

@@ -111,6 +111,24 @@ def test_create_validates_before_touching_the_gpu():
         pk.System(c)
 
 
+def test_bosonic_system_size_limit():
+    """A bosonic ring polymer is limited to 14000 particles, where the
+    one-block solve's shared memory (2 (N + 1) + 32 doubles beside its
+    static tables) still fits a block; larger ones are rejected as a
+    configuration error before any GPU work, distinguishable ones are not
+    limited by it."""
+    c = pk.make_config(natoms=14001, nbeads=4, bosonic=1)
+    with pytest.raises(pk.ConfigError, match="at most 14000 particles"):
+        pk.System(c)
+    c = pk.make_config(natoms=14001, nbeads=1, bosonic=1)   # one bead: no exchange
+    try:
+        pk.System(c).close()
+    except pk.ConfigError:
+        pytest.fail("a one-bead system has no exchange to limit it")
+    except pk.PimdbError:
+        pass  # no GPU here
+
+
 def test_integration_snippets_compile_against_the_header(tmp_path):
     """Every C++ snippet of INTEGRATION.md that uses only the C ABI compiles
     against include/pimdb_gb300.h (g++ -fsyntax-only), so the documented calls
