@@ -390,7 +390,9 @@ int pimdb_exchange_noalloc(const double* ring, int nbeads, int natoms, int ndim,
  * 19-71; nbeads <= 256), and the Langevin thermostat in the cartesian or the
  * normal-mode frame, or none (Nose-Hoover chains: one system at a time).
  * Every replica must share ndim and precision; natoms <= 2048; at most 65535
- * replicas.  With PIMDB_MIXED the pair forces are FP32 with FP64
+ * replicas.  Blocks are 256 threads unless every warp's staged copy of the
+ * largest replica needs smaller ones (above about 900 particles); a block
+ * shape that cannot hold it returns PIMDB_ERR_CONFIG.  With PIMDB_MIXED the pair forces are FP32 with FP64
  * accumulation, the exchange weights double-float and its exterior spring
  * forces FP32 with compensated sums; potentials, triangular solve, cycle
  * energies and integrator stay FP64.  The Langevin normals are the

@@ -1064,13 +1064,31 @@ static int configure_launch(pimdb_batch* b, int threads, int ctas_per_sm) {
     if (threads < 32 || threads > kBatchMaxThreads || threads % 32) return bfail(b, PIMDB_ERR_ARG, "threads must be a multiple of 32 in [32, 512]");
     if (ctas_per_sm < 1) return bfail(b, PIMDB_ERR_ARG, "ctas_per_sm must be >= 1");
     const size_t smem = batch_smem(b->D, b->maxN, threads, b->maxPnm);
+    // every warp stages the largest replica's positions: with many warps a
+    // large replica needs more shared memory than a block can have
+    int dev = 0, optin = 0;
+    size_t stat = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    with_kernel(b->D, b->mixed, [&](auto k) {
+        cudaFuncAttributes fa{};
+        if (cudaFuncGetAttributes(&fa, k) == cudaSuccess) stat = fa.sharedSizeBytes;
+    });
+    cudaGetLastError();
+    if (optin > 0 && smem + stat > (size_t)optin)
+        return bfail(b, PIMDB_ERR_CONFIG, "the batched kernel needs " + std::to_string(smem + stat) +
+                                              " bytes of shared memory for " + std::to_string(b->maxN) +
+                                              " particles at " + std::to_string(threads) + " threads per block");
     int resident = 0;
     cudaError_t e = cudaSuccess;
     with_kernel(b->D, b->mixed, [&](auto k) {
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k, threads, smem);
     });
-    if (e != cudaSuccess) return bfail(b, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return bfail(b, PIMDB_ERR_CUDA, cudaGetErrorString(e));
+    }
     if (resident < 1) return bfail(b, PIMDB_ERR_CONFIG, "batched kernel does not fit on an SM with this block size");
     b->threads = threads;
     b->ctas_per_sm = std::min(ctas_per_sm, resident);
@@ -1268,7 +1286,9 @@ extern "C" int pimdb_batch_create(const pimdb_config* cfgs, int nreplicas, void*
         free_batch(b);
         return bfail(nullptr, PIMDB_ERR_CUDA, cudaGetErrorString(e));
     }
-    const int st = configure_launch(b, 256, 2);
+    // 256 threads unless the largest replica's staging needs smaller blocks
+    int st = PIMDB_ERR_CONFIG;
+    for (int t = 256; t >= 32 && st == PIMDB_ERR_CONFIG; t /= 2) st = configure_launch(b, t, 2);
     if (st != PIMDB_OK) {
         const std::string msg = b->err;
         free_batch(b);

@@ -104,6 +104,28 @@ def test_batch_forces_match_oracle(replicas):
 
 
 @pytest.mark.gpu
+def test_batch_large_replica_takes_smaller_blocks():
+    """A 1000-particle replica beside a small one: every warp stages the
+    largest replica's positions, which at 256 threads would need more
+    shared memory than a block can have, so the batch is created with
+    smaller blocks; its forces match the oracle (1e-10), and a block shape
+    that cannot hold the replica is refused as a configuration error."""
+    replicas = [dict(natoms=1000, nbeads=4, ext="harmonic", ext_p=(3.0 * MEV, 0, 0), box_ang=40.0),
+                dict(natoms=12, nbeads=8, ext="harmonic", ext_p=(3.0 * MEV, 0, 0))]
+    systems, cfgs, xs, ps = build(replicas)
+    with pk.Batch(cfgs) as b:
+        assert b.launch()["threads"] < 256
+        with pytest.raises(pk.ConfigError):
+            b.set_option("threads", 256)
+        b.set_states(xs, ps)
+        b.compute_forces()
+        _, _, fs = b.get_states()
+    for r, s in enumerate(systems):
+        want = O.update_forces(s, xs[r])["f"]
+        assert rel_per_bead(fs[r], want) < 1e-10, r
+
+
+@pytest.mark.gpu
 def test_batch_exchange_scalars_match_oracle():
     systems, cfgs, xs, ps = build(REPLICAS_3D)
     with pk.Batch(cfgs) as b:
