@@ -125,9 +125,10 @@ int pimdb_config_from_ini(const char* path, int ndim, pimdb_config* cfg, char* e
 /* Simulation::Simulation (src/simulation.cpp:16-101) minus initial
  * conditions: allocates the device state of all beads.  `cuda_stream` is a
  * cudaStream_t to run on, or NULL for a stream owned by the handle.  A
- * configuration the reference would reject, or a bosonic ring polymer of
- * more than 14000 particles (the largest whose exchange solve fits one
- * block's shared memory), returns PIMDB_ERR_CONFIG before any GPU work. */
+ * configuration the reference would reject, a bosonic ring polymer of more
+ * than 14000 particles (the largest whose exchange solve fits one block's
+ * shared memory) or normal modes with more than 1536 beads (likewise for
+ * the matrix-transform step) returns PIMDB_ERR_CONFIG before any GPU work. */
 int pimdb_create(const pimdb_config* cfg, void* cuda_stream, pimdb_handle** out);
 int pimdb_destroy(pimdb_handle* h);
 

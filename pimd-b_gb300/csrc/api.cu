@@ -248,6 +248,8 @@ std::string validate_config(const pimdb_config& c) {
         return "The specified interaction potential is not supported!";
     if (c.precision != PIMDB_FP64 && c.precision != PIMDB_MIXED) return "unknown precision";
     if ((long long)c.natoms * c.nbeads * c.ndim > (1ll << 31)) return "system too large";
+    if ((c.propagator == PIMDB_PROP_NORMAL_MODES || c.nmthermostat) && c.nbeads > kNmMaxBeads)
+        return "normal modes support at most " + std::to_string(kNmMaxBeads) + " beads";
     if (c.bosonic && c.nbeads > 1 && c.natoms > kExchangeMaxN)
         return "bosonic exchange supports at most " + std::to_string(kExchangeMaxN) + " particles";
     if (c.exchange != PIMDB_EXCHANGE_FELDMAN_HIRSHBERG && c.exchange != PIMDB_EXCHANGE_FACTORIAL)

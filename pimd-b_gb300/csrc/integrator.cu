@@ -162,6 +162,8 @@ __global__ void k_cart_update(Sys s, int flags, const double* __restrict__ red_i
 }
 
 constexpr int kNmTile = 4;                           // particles per block
+static_assert(sizeof(double) * 4 * (size_t)kNmMaxBeads * kNmTile + 4096 <= 227 * 1024,
+              "k_nm_propagate's shared memory at the most beads");
 constexpr int kNmPairs = kNmTile / 2;                // particle pairs per block
 constexpr int kNmGroups = 64;                        // mode groups
 constexpr int kNmThreads = kNmPairs * kNmGroups;

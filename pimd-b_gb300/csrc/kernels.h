@@ -116,6 +116,11 @@ constexpr int kBandMaxN = 8192;
 constexpr int kExchangeMaxN = 14000;
 static_assert(sizeof(double) * (2 * (kExchangeMaxN + 1) + 32) + 4096 <= 227 * 1024,
               "the one-block solve's shared memory at the largest bosonic system");
+// The most beads with the normal-mode propagator or thermostat: the
+// matrix-transform step (k_nm_propagate, the path for bead counts the
+// register and fused kernels do not take) holds 4 P x 4 particles' doubles
+// of shared memory, and a block gets at most 227 KB (sm_103a).
+constexpr int kNmMaxBeads = 1536;
 // The cotangent of V_B on beads 1 and P into fx: vb_bar * dV_B/dx (the
 // exterior spring forces' exchange part times -vb_bar).
 void launch_exchange_adjoint(const Sys& s, int D, double vb_bar, cudaStream_t st);

@@ -129,6 +129,16 @@ def test_bosonic_system_size_limit():
         pass  # no GPU here
 
 
+def test_normal_mode_bead_limit():
+    """The normal-mode propagator and thermostat take at most 1536 beads,
+    where the matrix-transform step's shared memory still fits a block;
+    more are a configuration error before any GPU work."""
+    for kw in (dict(propagator="normal_modes"), dict(nmthermostat=1)):
+        c = pk.make_config(natoms=2, nbeads=1537, bosonic=0, **kw)
+        with pytest.raises(pk.ConfigError, match="at most 1536 beads"):
+            pk.System(c)
+
+
 def test_integration_snippets_compile_against_the_header(tmp_path):
     """Every C++ snippet of INTEGRATION.md that uses only the C ABI compiles
     against include/pimdb_gb300.h (g++ -fsyntax-only), so the documented calls
